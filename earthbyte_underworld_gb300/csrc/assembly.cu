@@ -1,0 +1,575 @@
+// Element assembly on the integration points of every element.
+//
+// Reference behaviour (paths relative to the Underworld 1.x tree):
+//   K_e  Underworld/Rheology/src/ConstitutiveMatrixCartesian.c:202-412: sum over the cell's
+//        points of B^T (detJ w D) B with the isotropic D of ConstitutiveMatrix_SetIsotropicViscosity
+//        (ConstitutiveMatrix.c:362-374, ConstitutiveMatrixCartesian.c:470-481)
+//   eta  the RheologyMaterial law list (Rheology_Register.c:61-77): MaterialViscosity.c:119-139,
+//        Arrhenius.c:156-200, FrankKamenetskii.c:134-152, ViscosityLimiter.c:106-126,
+//        YieldRheology.c:198-243 + VonMises.c:206-269 + DruckerPrager.c:236-345
+//   w    ConstantWeights.c:180-189 (cellLocalVolume 2^dim / count, WeightsCalculator.c:83)
+//   f_e  PICellerator/Utils/src/BuoyancyForceTerm.c:310-452
+//   G_e  StgFEM/Assembly/src/GradientStiffnessMatrixTerm.c:160-250 on the 2^dim Gauss swarm
+//   S_e  StgFEM/SLE/ProvidedSystems/StokesFlow/src/UzawaPreconditionerTerm.c:155-238
+//
+// GPU design.  On the affine elements of a regular mesh every product of shape-function
+// derivatives is a polynomial of degree <= 2 per axis in the local coordinates, so
+//   K_e = sum over 3^dim moments mu_abc = sum_p w eta_p xi^a eta^b zeta^c of fixed matrices.
+// One thread owns one element: it streams the element's points (slot order, SoA) once,
+// evaluates the rheology, accumulates the 27 (3D) / 9 (2D) moments in FP64 registers, then
+// contracts them axis by axis into the 300 (3D) / 36 (2D) distinct entries of K_e.  This
+// needs ~50 FP64 operations per point instead of the ~1000 of the per-point B^T D B loop,
+// which matters on a part whose FP64 rate is 1/58 of its FP32 rate.  K_e, f_e, G_e are
+// written entry-major ([entry][element]) so a warp's stores coalesce.
+#include "internal.cuh"
+
+namespace uwg {
+
+struct AssemblyArgs {
+    int dim;
+    int nel[3];
+    double min[3], max[3];
+    int64_t ne, nslots;
+    const uint32_t* offsets;
+    const double* sxi;       // [d][slot]
+    const int32_t* smat;
+    const double* seta_in;   // optional
+    const double* srho_in;   // optional
+    const uwgpu_material* mats;
+    int nmat;
+    const double* temperature;  // nodal or null
+    const double* u;            // nodal SoA [d][node] or null
+    const double* p;            // per element or null
+    int previous_solution;
+    int vert_axis;
+    double gravity;
+    int64_t nnx, nny, nn;
+    double* Ke;    // packed, entry-major
+    double* fe;    // entry-major
+    double* Ge;    // entry-major
+    double* Se;
+    double* eta_out;
+    uint32_t* flags;  // bit0: empty element, bit1: bad material index
+};
+
+// Per-point rheology chain.  Every law in scope keeps D isotropic, so the constitutive matrix
+// is carried as its viscosity (D[3][3] in 3D, D[2][2] in 2D).
+template <int DIM>
+__device__ __forceinline__ double run_rheology(const uwgpu_material& m, const double* N, const double* Tn,
+                                               bool hasT, double yglobal, double ymax, double point_eta,
+                                               const double (*L)[3], double pressure, int prev) {
+    double eta = 0.0;
+    for (int l = 0; l < m.n_laws; ++l) {
+        const uwgpu_law& law = m.laws[l];
+        switch (law.law) {
+        case UWGPU_LAW_MATERIAL_VISCOSITY:
+            eta = law.p[0];
+            break;
+        case UWGPU_LAW_ARRHENIUS: {
+            double T = 0.0;
+            if (hasT) {
+#pragma unroll
+                for (int a = 0; a < (1 << DIM); ++a) T += N[a] * Tn[a];
+            }
+            if (law.p[2] > (0.0 + 1e-12)) {
+                double depth = ymax - yglobal;
+                eta = law.p[0] * exp((law.p[1] + law.p[2] * depth) / (T + law.p[3]));
+            } else {
+                eta = law.p[0] * exp((law.p[1]) / (T + law.p[3]));
+            }
+            break;
+        }
+        case UWGPU_LAW_FRANK_KAMENETSKII: {
+            double T = 0.0;
+            if (hasT) {
+#pragma unroll
+                for (int a = 0; a < (1 << DIM); ++a) T += N[a] * Tn[a];
+            }
+            eta = law.p[0] * exp(-law.p[1] * T);
+            break;
+        }
+        case UWGPU_LAW_VISCOSITY_LIMITER:
+            if (eta > law.p[0]) eta = law.p[0];
+            if (eta < law.p[1]) eta = law.p[1];
+            break;
+        case UWGPU_LAW_DRUCKER_PRAGER: {
+            double minVisc = law.p[3];
+            if (!prev) break;
+            // yield indicator: second invariant of the stress D . strain-rate
+            double inv;
+            if (DIM == 3) {
+                double s0 = 2.0 * eta * L[0][0], s1 = 2.0 * eta * L[1][1], s2 = 2.0 * eta * L[2][2];
+                double s3 = eta * 2.0 * (0.5 * (L[0][1] + L[1][0]));
+                double s4 = eta * 2.0 * (0.5 * (L[0][2] + L[2][0]));
+                double s5 = eta * 2.0 * (0.5 * (L[1][2] + L[2][1]));
+                inv = 0.5 * (s0 * s0 + s1 * s1 + s2 * s2) + s3 * s3 + s4 * s4 + s5 * s5;
+            } else {
+                double s0 = 2.0 * eta * L[0][0], s1 = 2.0 * eta * L[1][1];
+                double s2 = eta * 2.0 * (0.5 * (L[0][1] + L[1][0]));
+                inv = 0.5 * (s0 * s0 + s1 * s1) + s2 * s2;
+            }
+            double ind = sqrt(inv);
+            double phi = atan(law.p[1]);
+            double dpFric, dpCoh;
+            if (DIM == 3) {
+                double sinphi = sin(phi);
+                double ood = 1.0 / (sqrt(3.0) * (3.0 - sinphi));
+                dpFric = 6.0 * sinphi * ood;
+                dpCoh = 6.0 * law.p[0] * cos(phi) * ood;
+            } else {
+                dpCoh = law.p[0] * cos(phi);
+                dpFric = sin(phi);
+            }
+            double crit = dpFric * pressure + dpCoh;
+            if (crit < law.p[2]) crit = law.p[2];
+            if (crit < ind) {
+                double beta = 1.0 - crit / ind;
+                double corr = -eta * beta;
+                if ((eta + corr) < minVisc) corr = minVisc - eta;
+                eta += corr;
+            }
+            if (eta < minVisc) eta = minVisc;
+            break;
+        }
+        case UWGPU_LAW_PARTICLE_VISCOSITY:
+            eta = point_eta;
+            break;
+        default:
+            break;
+        }
+    }
+    return eta;
+}
+
+// Coefficients of (1 + s_i x)(1 + s_j x) in the monomials 1, x, x^2, by pair type:
+// type 0: s_i = s_j = +1, type 1: s_i = s_j = -1, type 2: s_i != s_j.
+__device__ __constant__ double kQ[3][3] = {{1.0, 2.0, 1.0}, {1.0, -2.0, 1.0}, {1.0, 0.0, -1.0}};
+// Coefficients of (1 + s x) in 1, x by type: 0: s = +1, 1: s = -1.
+__device__ __constant__ double kL[2][2] = {{1.0, 1.0}, {1.0, -1.0}};
+
+__device__ __forceinline__ int qtype(int si, int sj) { return si == sj ? (si > 0 ? 0 : 1) : 2; }
+__device__ __forceinline__ int ltype(int s) { return s > 0 ? 0 : 1; }
+
+template <int DIM>
+__global__ void __launch_bounds__(128) k_assemble(AssemblyArgs A) {
+    constexpr int NEN = 1 << DIM;
+    constexpr int ND = NEN * DIM;
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= A.ne) return;
+    int64_t ie = e % A.nel[0];
+    int64_t je = (e / A.nel[0]) % A.nel[1];
+    int64_t ke = DIM == 3 ? e / ((int64_t)A.nel[0] * A.nel[1]) : 0;
+    int64_t idx[3] = {ie, je, ke};
+    double x0[3], h[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        x0[d] = node_coord_1d(idx[d], A.nel[d], A.min[d], A.max[d]);
+        h[d] = node_coord_1d(idx[d] + 1, A.nel[d], A.min[d], A.max[d]) - x0[d];
+    }
+    // element nodes (CartesianGenerator incidence order, x fastest)
+    int64_t base = ie + A.nnx * (je + A.nny * ke);
+    int64_t inc[NEN];
+#pragma unroll
+    for (int a = 0; a < NEN; ++a)
+        inc[a] = base + (a & 1) + ((a >> 1) & 1) * A.nnx + (DIM == 3 ? ((a >> 2) & 1) * A.nnx * A.nny : 0);
+    double Tn[NEN];
+    bool hasT = A.temperature != nullptr;
+#pragma unroll
+    for (int a = 0; a < NEN; ++a) Tn[a] = hasT ? A.temperature[inc[a]] : 0.0;
+    bool needL = A.u != nullptr && A.previous_solution;
+    double un[DIM][NEN];
+    if (needL) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) un[d][a] = A.u[(int64_t)d * A.nn + inc[a]];
+    }
+    double pressure = A.p ? A.p[e] : 0.0;
+
+    uint32_t beg = A.offsets[e], end = A.offsets[e + 1];
+    uint32_t cnt = end - beg;
+    if (cnt == 0) atomicOr(A.flags, 1u);
+    const double cellVolume = DIM == 3 ? 8.0 : 4.0;
+    double w = cellVolume / (double)cnt;
+
+    constexpr int NM = DIM == 3 ? 27 : 9;
+    constexpr int NF = NEN;
+    double mu[NM];
+    double phi[NF];
+#pragma unroll
+    for (int i = 0; i < NM; ++i) mu[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < NF; ++i) phi[i] = 0.0;
+
+    for (uint32_t s = beg; s < end; ++s) {
+        double xi[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) xi[d] = A.sxi[(int64_t)d * A.nslots + s];
+        if (DIM == 2) xi[2] = 0.0;
+        int mi = A.smat[s];
+        if (mi < 0 || mi >= A.nmat) {
+            atomicOr(A.flags, 2u);
+            mi = 0;
+        }
+        const uwgpu_material& m = A.mats[mi];
+        // shape functions at xi (TrilinearElementType.c:249-263 / BilinearElementType.c:212-220)
+        double N[NEN];
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+            double v = DIM == 3 ? 0.125 : 0.25;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) v *= ((a >> d) & 1) ? (1.0 + xi[d]) : (1.0 - xi[d]);
+            N[a] = v;
+        }
+        double L[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        if (needL) {
+            // velocity gradient L[i][j] = du_i/dx_j from the global derivatives at xi
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) {
+                double gx[3];
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    double v = (2.0 / h[d]) * (DIM == 3 ? 0.125 : 0.25) * (((a >> d) & 1) ? 1.0 : -1.0);
+#pragma unroll
+                    for (int q = 0; q < DIM; ++q)
+                        if (q != d) v *= ((a >> q) & 1) ? (1.0 + xi[q]) : (1.0 - xi[q]);
+                    gx[d] = v;
+                }
+#pragma unroll
+                for (int i = 0; i < DIM; ++i)
+#pragma unroll
+                    for (int j = 0; j < DIM; ++j) L[i][j] += gx[j] * un[i][a];
+            }
+        }
+        double yglobal = x0[1] + 0.5 * h[1] * (xi[1] + 1.0);
+        double peta = A.seta_in ? A.seta_in[s] : 0.0;
+        double eta = run_rheology<DIM>(m, N, Tn, hasT, yglobal, A.max[1], peta, L, pressure, A.previous_solution);
+        if (A.eta_out) A.eta_out[s] = eta;
+        double rho0 = A.srho_in ? A.srho_in[s] : m.density;
+        double T = 0.0;
+        if (hasT && m.alpha != 0.0) {
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) T += N[a] * Tn[a];
+        }
+        double rho = rho0 * (1.0 - m.alpha * (T - m.ref_temp));
+
+        double c = w * eta;
+        double r = w * rho;
+        if (DIM == 3) {
+            double x1 = xi[0], y1 = xi[1], z1 = xi[2];
+            double x2 = x1 * x1;
+            double cz0 = c, cz1 = c * z1, cz2 = cz1 * z1;
+            double cyz[3][3];
+            cyz[0][0] = cz0;
+            cyz[0][1] = cz1;
+            cyz[0][2] = cz2;
+            cyz[1][0] = cz0 * y1;
+            cyz[1][1] = cz1 * y1;
+            cyz[1][2] = cz2 * y1;
+            cyz[2][0] = cyz[1][0] * y1;
+            cyz[2][1] = cyz[1][1] * y1;
+            cyz[2][2] = cyz[1][2] * y1;
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+#pragma unroll
+                for (int cc = 0; cc < 3; ++cc) {
+                    double v = cyz[b][cc];
+                    mu[0 * 9 + b * 3 + cc] += v;
+                    mu[1 * 9 + b * 3 + cc] = fma(x1, v, mu[1 * 9 + b * 3 + cc]);
+                    mu[2 * 9 + b * 3 + cc] = fma(x2, v, mu[2 * 9 + b * 3 + cc]);
+                }
+            double rz = r * z1, ry = r * y1, ryz = ry * z1;
+            phi[0] += r;
+            phi[1] = fma(x1, r, phi[1]);
+            phi[2] += ry;
+            phi[3] = fma(x1, ry, phi[3]);
+            phi[4] += rz;
+            phi[5] = fma(x1, rz, phi[5]);
+            phi[6] += ryz;
+            phi[7] = fma(x1, ryz, phi[7]);
+        } else {
+            double x1 = xi[0], y1 = xi[1];
+            double x2 = x1 * x1;
+            double cy0 = c, cy1 = c * y1, cy2 = cy1 * y1;
+            double cy[3] = {cy0, cy1, cy2};
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                mu[0 * 3 + b] += cy[b];
+                mu[1 * 3 + b] = fma(x1, cy[b], mu[1 * 3 + b]);
+                mu[2 * 3 + b] = fma(x2, cy[b], mu[2 * 3 + b]);
+            }
+            double ry = r * y1;
+            phi[0] += r;
+            phi[1] = fma(x1, r, phi[1]);
+            phi[2] += ry;
+            phi[3] = fma(x1, ry, phi[3]);
+        }
+    }
+
+    // ---- contraction of the moments into K_e ----
+    // detJ of the affine element and derivative scales (ElementType.c:354-495 reduces to these)
+    double detJ = DIM == 3 ? (0.5 * h[0]) * (0.5 * h[1]) * (0.5 * h[2]) : (0.5 * h[0]) * (0.5 * h[1]);
+    double g[3];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) g[d] = 2.0 / h[d];
+    const double inv64 = DIM == 3 ? 1.0 / 64.0 : 1.0 / 16.0;
+
+    if (DIM == 3) {
+        // same-axis pair tables: Dkk[t1][t2] over the two other axes
+        double Dxx[3][3], Dyy[3][3], Dzz[3][3];
+#pragma unroll
+        for (int t1 = 0; t1 < 3; ++t1)
+#pragma unroll
+            for (int t2 = 0; t2 < 3; ++t2) {
+                double sx = 0.0, sy = 0.0, sz = 0.0;
+#pragma unroll
+                for (int u = 0; u < 3; ++u)
+#pragma unroll
+                    for (int v = 0; v < 3; ++v) {
+                        double q = kQ[t1][u] * kQ[t2][v];
+                        sx += q * mu[0 * 9 + u * 3 + v];   // axes y (u), z (v)
+                        sy += q * mu[u * 9 + 0 * 3 + v];   // axes x (u), z (v)
+                        sz += q * mu[u * 9 + v * 3 + 0];   // axes x (u), y (v)
+                    }
+                Dxx[t1][t2] = sx;
+                Dyy[t1][t2] = sy;
+                Dzz[t1][t2] = sz;
+            }
+        // mixed pairs (k < l): Mkl[tk_j][tl_i][t_other]
+        double Mxy[2][2][3], Mxz[2][2][3], Myz[2][2][3];
+#pragma unroll
+        for (int ta = 0; ta < 2; ++ta)
+#pragma unroll
+            for (int tb = 0; tb < 2; ++tb)
+#pragma unroll
+                for (int to = 0; to < 3; ++to) {
+                    double sxy = 0.0, sxz = 0.0, syz = 0.0;
+#pragma unroll
+                    for (int u = 0; u < 2; ++u)
+#pragma unroll
+                        for (int v = 0; v < 2; ++v) {
+                            double l2 = kL[ta][u] * kL[tb][v];
+#pragma unroll
+                            for (int o = 0; o < 3; ++o) {
+                                double q = l2 * kQ[to][o];
+                                sxy += q * mu[u * 9 + v * 3 + o];   // x^u y^v z^o
+                                sxz += q * mu[u * 9 + o * 3 + v];   // x^u z^v y^o
+                                syz += q * mu[o * 9 + u * 3 + v];   // y^u z^v x^o
+                            }
+                        }
+                    Mxy[ta][tb][to] = sxy;
+                    Mxz[ta][tb][to] = sxz;
+                    Myz[ta][tb][to] = syz;
+                }
+        // M_kl[i][j] for node pair (i, j)
+        auto Mkl = [&](int k, int l, int i, int j) -> double {
+            int si[3] = {((i & 1) << 1) - 1, (((i >> 1) & 1) << 1) - 1, (((i >> 2) & 1) << 1) - 1};
+            int sj[3] = {((j & 1) << 1) - 1, (((j >> 1) & 1) << 1) - 1, (((j >> 2) & 1) << 1) - 1};
+            double sc = detJ * g[k] * g[l] * inv64 * (double)(si[k] * sj[l]);
+            if (k == l) {
+                if (k == 0) return sc * Dxx[qtype(si[1], sj[1])][qtype(si[2], sj[2])];
+                if (k == 1) return sc * Dyy[qtype(si[0], sj[0])][qtype(si[2], sj[2])];
+                return sc * Dzz[qtype(si[0], sj[0])][qtype(si[1], sj[1])];
+            }
+            // k < l: derivative axis k on node i, l on node j
+            if (k > l) {
+                // M_kl[i][j] = M_lk[j][i]
+                int t = k; k = l; l = t;
+                int tmp[3] = {si[0], si[1], si[2]};
+                for (int q = 0; q < 3; ++q) { si[q] = sj[q]; sj[q] = tmp[q]; }
+            }
+            if (k == 0 && l == 1) return sc * Mxy[ltype(sj[0])][ltype(si[1])][qtype(si[2], sj[2])];
+            if (k == 0 && l == 2) return sc * Mxz[ltype(sj[0])][ltype(si[2])][qtype(si[1], sj[1])];
+            return sc * Myz[ltype(sj[1])][ltype(si[2])][qtype(si[0], sj[0])];
+        };
+        const int64_t ne = A.ne;
+        double diag[ND];
+#pragma unroll
+        for (int i = 0; i < NEN; ++i)
+#pragma unroll
+            for (int j = i; j < NEN; ++j) {
+                double tr = Mkl(0, 0, i, j) + Mkl(1, 1, i, j) + Mkl(2, 2, i, j);
+#pragma unroll
+                for (int al = 0; al < 3; ++al)
+#pragma unroll
+                    for (int be = 0; be < 3; ++be) {
+                        int r = i * 3 + al, cix = j * 3 + be;
+                        if (r > cix) continue;
+                        // K[(i,al),(j,be)] = delta * tr + M_{be,al}[i][j]
+                        double v = Mkl(be, al, i, j) + (al == be ? tr : 0.0);
+                        A.Ke[(int64_t)packed_index(ND, r, cix) * ne + e] = v;
+                        if (r == cix) diag[r] = v;
+                    }
+            }
+        // G_e: integral of -dN_a/dx_d over the element (exact for the 2x2x2 Gauss rule)
+        double Gl[ND];
+        double s = 0.0;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                double area = 1.0;
+#pragma unroll
+                for (int q = 0; q < 3; ++q)
+                    if (q != d) area *= h[q];
+                double sa = ((a >> d) & 1) ? 1.0 : -1.0;
+                Gl[a * 3 + d] = -sa * area * 0.25;
+                A.Ge[(int64_t)(a * 3 + d) * ne + e] = Gl[a * 3 + d];
+                s += Gl[a * 3 + d] * (Gl[a * 3 + d] / diag[a * 3 + d]);
+            }
+        A.Se[e] = s;
+        // f_e: -g detJ sum_p w rho N_a on the vertical component
+        double fs = -A.gravity * detJ * 0.125;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+            double sx = (a & 1) ? 1.0 : -1.0, sy = ((a >> 1) & 1) ? 1.0 : -1.0, sz = ((a >> 2) & 1) ? 1.0 : -1.0;
+            double v = phi[0] + sx * phi[1] + sy * phi[2] + sx * sy * phi[3] + sz * phi[4] + sx * sz * phi[5] +
+                       sy * sz * phi[6] + sx * sy * sz * phi[7];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) A.fe[(int64_t)(a * 3 + d) * ne + e] = (d == A.vert_axis) ? fs * v : 0.0;
+        }
+    } else {
+        double Dxx[3], Dyy[3];
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            double sx = 0.0, sy = 0.0;
+#pragma unroll
+            for (int u = 0; u < 3; ++u) {
+                sx += kQ[t][u] * mu[0 * 3 + u];
+                sy += kQ[t][u] * mu[u * 3 + 0];
+            }
+            Dxx[t] = sx;
+            Dyy[t] = sy;
+        }
+        double Mxy[2][2];
+#pragma unroll
+        for (int ta = 0; ta < 2; ++ta)
+#pragma unroll
+            for (int tb = 0; tb < 2; ++tb) {
+                double v = 0.0;
+#pragma unroll
+                for (int u = 0; u < 2; ++u)
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) v += kL[ta][u] * kL[tb][q] * mu[u * 3 + q];
+                Mxy[ta][tb] = v;
+            }
+        auto Mkl = [&](int k, int l, int i, int j) -> double {
+            int si[2] = {((i & 1) << 1) - 1, (((i >> 1) & 1) << 1) - 1};
+            int sj[2] = {((j & 1) << 1) - 1, (((j >> 1) & 1) << 1) - 1};
+            double sc = detJ * g[k] * g[l] * inv64 * (double)(si[k] * sj[l]);
+            if (k == l) {
+                if (k == 0) return sc * Dxx[qtype(si[1], sj[1])];
+                return sc * Dyy[qtype(si[0], sj[0])];
+            }
+            if (k > l) {
+                for (int q = 0; q < 2; ++q) { int t = si[q]; si[q] = sj[q]; sj[q] = t; }
+            }
+            return sc * Mxy[ltype(sj[0])][ltype(si[1])];
+        };
+        const int64_t ne = A.ne;
+        double diag[ND];
+#pragma unroll
+        for (int i = 0; i < NEN; ++i)
+#pragma unroll
+            for (int j = i; j < NEN; ++j) {
+                double tr = Mkl(0, 0, i, j) + Mkl(1, 1, i, j);
+#pragma unroll
+                for (int al = 0; al < 2; ++al)
+#pragma unroll
+                    for (int be = 0; be < 2; ++be) {
+                        int r = i * 2 + al, cix = j * 2 + be;
+                        if (r > cix) continue;
+                        double v = Mkl(be, al, i, j) + (al == be ? tr : 0.0);
+                        A.Ke[(int64_t)packed_index(ND, r, cix) * ne + e] = v;
+                        if (r == cix) diag[r] = v;
+                    }
+            }
+        double s = 0.0;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                double sa = ((a >> d) & 1) ? 1.0 : -1.0;
+                double G = -sa * h[1 - d] * 0.5;
+                A.Ge[(int64_t)(a * 2 + d) * ne + e] = G;
+                s += G * (G / diag[a * 2 + d]);
+            }
+        A.Se[e] = s;
+        double fs = -A.gravity * detJ * 0.25;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+            double sx = (a & 1) ? 1.0 : -1.0, sy = ((a >> 1) & 1) ? 1.0 : -1.0;
+            double v = phi[0] + sx * phi[1] + sy * phi[2] + sx * sy * phi[3];
+#pragma unroll
+            for (int d = 0; d < 2; ++d) A.fe[(int64_t)(a * 2 + d) * ne + e] = (d == A.vert_axis) ? fs * v : 0.0;
+        }
+    }
+}
+
+void assemble(Context& c) {
+    UWG_REQUIRE(c.mapped, UWGPU_ERR_STATE, "assemble called before bin_and_map");
+    UWG_REQUIRE(c.nmat > 0, UWGPU_ERR_STATE, "materials not set");
+    const MeshDesc& m = c.mesh;
+    int dim = m.dim, nen = 1 << dim, nd = nen * dim;
+    int64_t ne = m.ne;
+    Level& L0 = c.levels[0];
+    L0.mesh = m;
+    L0.Ke.ensure((size_t)packed_size(nd) * ne);
+    c.fe.ensure((size_t)nd * ne);
+    c.Ge.ensure((size_t)nd * ne);
+    c.Se.ensure((size_t)ne);
+    c.seta_out.ensure((size_t)(c.np > 0 ? c.np : 1));
+    c.err_count.ensure(1);
+    UWG_CUDA(cudaMemsetAsync(c.err_count.p, 0, sizeof(uint32_t), c.stream));
+
+    AssemblyArgs A;
+    A.dim = dim;
+    for (int d = 0; d < 3; ++d) {
+        A.nel[d] = m.nel[d];
+        A.min[d] = m.min[d];
+        A.max[d] = m.max[d];
+    }
+    A.ne = ne;
+    A.nslots = c.np;
+    A.offsets = c.offsets.p;
+    A.sxi = c.sxi.p;
+    A.smat = c.smat.p;
+    A.seta_in = c.has_peta ? c.seta_in.p : nullptr;
+    A.srho_in = c.has_prho ? c.srho_in.p : nullptr;
+    A.mats = c.mats.p;
+    A.nmat = c.nmat;
+    A.temperature = c.has_temperature ? c.temperature.p : nullptr;
+    A.u = c.has_solution ? c.u_sol.p : nullptr;
+    A.p = c.has_solution ? c.p_sol.p : nullptr;
+    A.previous_solution = c.has_solution ? 1 : 0;
+    A.vert_axis = c.vert_axis;
+    A.gravity = c.gravity;
+    A.nnx = m.nnx;
+    A.nny = m.nny;
+    A.nn = m.nn;
+    A.Ke = L0.Ke.p;
+    A.fe = c.fe.p;
+    A.Ge = c.Ge.p;
+    A.Se = c.Se.p;
+    A.eta_out = c.seta_out.p;
+    A.flags = c.err_count.p;
+    {
+        LaunchScope ls(c, UWGPU_KERNEL_ASSEMBLY);
+        if (dim == 3)
+            k_assemble<3><<<blocks_for(ne, 128), 128, 0, c.stream>>>(A);
+        else
+            k_assemble<2><<<blocks_for(ne, 128), 128, 0, c.stream>>>(A);
+    }
+    check_launch("k_assemble");
+    uint32_t flags = 0;
+    UWG_CUDA(cudaMemcpyAsync(&flags, c.err_count.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream));
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+    c.assembled = true;
+    c.operator_built = false;
+    if (flags & 2u) throw Error(UWGPU_ERR_ARGUMENT, "material index out of range");
+    if (flags & 1u)
+        throw Error(UWGPU_ERR_ARGUMENT,
+                    "an element holds no integration points (zero element contribution is not allowed)");
+}
+
+}  // namespace uwg

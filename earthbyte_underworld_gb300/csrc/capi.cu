@@ -1,0 +1,389 @@
+// extern "C" entry points of libuwgpu (declared in include/uwgpu.h).  Each converts the
+// internal uwg::Error exceptions into a status code plus a message.
+#include <cstring>
+
+#include "internal.cuh"
+
+using uwg::Context;
+using uwg::Error;
+
+struct uwgpu_ctx {
+    Context c;
+};
+
+namespace {
+
+template <typename F>
+int guarded(uwgpu_ctx* ctx, F&& fn) {
+    if (!ctx) return UWGPU_ERR_ARGUMENT;
+    try {
+        cudaSetDevice(ctx->c.device);
+        fn(ctx->c);
+        ctx->c.last_error.clear();
+        return UWGPU_OK;
+    } catch (const Error& e) {
+        ctx->c.last_error = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        ctx->c.last_error = e.what();
+        return UWGPU_ERR_CUDA;
+    }
+}
+
+template <typename T>
+void upload(uwg::DArray<T>& dst, const T* src, size_t n, cudaStream_t s) {
+    dst.ensure(n);
+    UWG_CUDA(cudaMemcpyAsync(dst.p, src, n * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+}  // namespace
+
+extern "C" {
+
+int uwgpu_abi_version(void) { return UWGPU_ABI_VERSION; }
+
+int uwgpu_create(int32_t device, uwgpu_ctx** out) {
+    if (!out) return UWGPU_ERR_ARGUMENT;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return UWGPU_ERR_CUDA;
+    if (device < 0 || device >= ndev) return UWGPU_ERR_ARGUMENT;
+    uwgpu_ctx* ctx = new uwgpu_ctx();
+    ctx->c.device = device;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMallocHost(&ctx->c.host_scalars, 1024 * sizeof(double)) != cudaSuccess) {
+        delete ctx;
+        return UWGPU_ERR_CUDA;
+    }
+    *out = ctx;
+    return UWGPU_OK;
+}
+
+void uwgpu_destroy(uwgpu_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->c.device);
+    cudaStreamSynchronize(ctx->c.stream);
+    for (auto& f : ctx->c.prof)
+        for (auto& pr : f.events) {
+            cudaEventDestroy(pr.first);
+            cudaEventDestroy(pr.second);
+        }
+    if (ctx->c.host_scalars) cudaFreeHost(ctx->c.host_scalars);
+    cudaStream_t s = ctx->c.stream;
+    delete ctx;  // frees device arrays
+    if (s) cudaStreamDestroy(s);
+}
+
+const char* uwgpu_last_error(const uwgpu_ctx* ctx) {
+    if (!ctx) return "null context";
+    return ctx->c.last_error.c_str();
+}
+
+int uwgpu_synchronize(uwgpu_ctx* ctx) {
+    return guarded(ctx, [&](Context& c) { UWG_CUDA(cudaStreamSynchronize(c.stream)); });
+}
+
+int uwgpu_mesh_q1(uwgpu_ctx* ctx, int32_t dim, const int32_t nel[3], const double mn[3],
+                  const double mx[3]) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(dim == 2 || dim == 3, UWGPU_ERR_ARGUMENT, "dim must be 2 or 3");
+        UWG_REQUIRE(nel && mn && mx, UWGPU_ERR_ARGUMENT, "null mesh argument");
+        uwg::MeshDesc m;
+        m.dim = dim;
+        for (int d = 0; d < 3; ++d) {
+            m.nel[d] = d < dim ? nel[d] : 1;
+            m.min[d] = mn[d];
+            m.max[d] = mx[d];
+            if (d < dim) {
+                UWG_REQUIRE(nel[d] >= 1, UWGPU_ERR_ARGUMENT, "element count must be positive");
+                UWG_REQUIRE(mx[d] > mn[d], UWGPU_ERR_ARGUMENT, "max must exceed min");
+            }
+        }
+        m.nnx = m.nel[0] + 1;
+        m.nny = m.nel[1] + 1;
+        m.nnz = dim == 3 ? m.nel[2] + 1 : 1;
+        m.nn = m.nnx * m.nny * m.nnz;
+        m.ne = (int64_t)m.nel[0] * m.nel[1] * (dim == 3 ? m.nel[2] : 1);
+        UWG_REQUIRE(m.ne < (int64_t)0x7fffffff, UWGPU_ERR_ARGUMENT, "too many elements");
+        c.mesh = m;
+        c.has_mesh = true;
+        c.has_bc = false;
+        c.mapped = false;
+        c.assembled = false;
+        c.operator_built = false;
+        c.has_solution = false;
+        c.has_temperature = false;
+    });
+}
+
+int uwgpu_bc_set(uwgpu_ctx* ctx, const uint8_t* fixed, const double* values) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(c.has_mesh, UWGPU_ERR_STATE, "mesh not set");
+        UWG_REQUIRE(fixed, UWGPU_ERR_ARGUMENT, "fixed mask is null");
+        size_t n = (size_t)c.mesh.nn * c.mesh.dim;
+        // the device keeps the mask per dof, node-major like the host array
+        upload(c.fixed, fixed, n, c.stream);
+        c.bcval.ensure(n);
+        c.bc_nonzero = false;
+        if (values) {
+            for (size_t i = 0; i < n; ++i)
+                if (fixed[i] && values[i] != 0.0) { c.bc_nonzero = true; break; }
+            UWG_CUDA(cudaMemcpyAsync(c.bcval.p, values, n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        } else {
+            UWG_CUDA(cudaMemsetAsync(c.bcval.p, 0, n * sizeof(double), c.stream));
+        }
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        c.has_bc = true;
+        c.operator_built = false;
+    });
+}
+
+int uwgpu_materials_set(uwgpu_ctx* ctx, int32_t n, const uwgpu_material* mats) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(n >= 1 && mats, UWGPU_ERR_ARGUMENT, "need at least one material");
+        for (int i = 0; i < n; ++i) {
+            UWG_REQUIRE(mats[i].n_laws >= 1 && mats[i].n_laws <= 4, UWGPU_ERR_ARGUMENT,
+                        "material needs 1..4 rheology laws");
+            for (int l = 0; l < mats[i].n_laws; ++l) {
+                int law = mats[i].laws[l].law;
+                UWG_REQUIRE(law >= UWGPU_LAW_MATERIAL_VISCOSITY && law <= UWGPU_LAW_PARTICLE_VISCOSITY,
+                            UWGPU_ERR_UNSUPPORTED,
+                            "rheology law " + std::to_string(law) + " is not provided by this library");
+            }
+        }
+        upload(c.mats, mats, (size_t)n, c.stream);
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        c.nmat = n;
+    });
+}
+
+int uwgpu_fields_set(uwgpu_ctx* ctx, const double* nodal_temperature, double gravity, int32_t vert_axis) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(c.has_mesh, UWGPU_ERR_STATE, "mesh not set");
+        UWG_REQUIRE(vert_axis >= 0 && vert_axis < c.mesh.dim, UWGPU_ERR_ARGUMENT, "bad vertical axis");
+        if (nodal_temperature) {
+            upload(c.temperature, nodal_temperature, (size_t)c.mesh.nn, c.stream);
+            c.has_temperature = true;
+        } else {
+            c.has_temperature = false;
+        }
+        c.gravity = gravity;
+        c.vert_axis = vert_axis;
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int uwgpu_solution_set(uwgpu_ctx* ctx, const double* u_nodal, const double* p) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(c.has_mesh, UWGPU_ERR_STATE, "mesh not set");
+        UWG_REQUIRE(u_nodal && p, UWGPU_ERR_ARGUMENT, "null solution");
+        int dim = c.mesh.dim;
+        int64_t nn = c.mesh.nn;
+        std::vector<double> soa((size_t)nn * dim);
+        for (int64_t n = 0; n < nn; ++n)
+            for (int d = 0; d < dim; ++d) soa[(size_t)d * nn + n] = u_nodal[n * dim + d];
+        upload(c.u_sol, soa.data(), soa.size(), c.stream);
+        upload(c.p_sol, p, (size_t)c.mesh.ne, c.stream);
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        c.has_solution = true;
+    });
+}
+
+int uwgpu_particles_upload(uwgpu_ctx* ctx, int64_t n, const double* x, const double* y, const double* z,
+                           const int32_t* material, const double* eta, const double* rho) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(c.has_mesh, UWGPU_ERR_STATE, "mesh not set");
+        UWG_REQUIRE(n >= 0 && n < (int64_t)0xffffffffLL, UWGPU_ERR_ARGUMENT, "bad point count");
+        UWG_REQUIRE(n == 0 || (x && y && (c.mesh.dim == 2 || z)), UWGPU_ERR_ARGUMENT, "null coordinates");
+        size_t N = (size_t)n;
+        c.np = n;
+        if (n > 0) {
+            upload(c.px, x, N, c.stream);
+            upload(c.py, y, N, c.stream);
+            if (c.mesh.dim == 3) upload(c.pz, z, N, c.stream);
+            if (material) {
+                upload(c.pmat, material, N, c.stream);
+            } else {
+                c.pmat.ensure(N);
+                UWG_CUDA(cudaMemsetAsync(c.pmat.p, 0, N * sizeof(int32_t), c.stream));
+            }
+            c.has_peta = eta != nullptr;
+            c.has_prho = rho != nullptr;
+            if (eta) upload(c.peta, eta, N, c.stream);
+            if (rho) upload(c.prho, rho, N, c.stream);
+        }
+        c.has_points = true;
+        c.mapped = false;
+        c.assembled = false;
+    });
+}
+
+int uwgpu_bin_and_map(uwgpu_ctx* ctx, uint32_t* perm, uint32_t* offsets, double* xi) {
+    return guarded(ctx, [&](Context& c) {
+        uwg::bin_and_map(c);
+        size_t N = (size_t)c.np, E = (size_t)c.mesh.ne;
+        if (perm && N) UWG_CUDA(cudaMemcpyAsync(perm, c.perm.p, N * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream));
+        if (offsets) UWG_CUDA(cudaMemcpyAsync(offsets, c.offsets.p, (E + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream));
+        if (xi && N) {
+            std::vector<double> tmp(3 * N);
+            int dim = c.mesh.dim;
+            UWG_CUDA(cudaMemcpyAsync(tmp.data(), c.sxi.p, (size_t)dim * N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            UWG_CUDA(cudaStreamSynchronize(c.stream));
+            for (size_t s = 0; s < N; ++s)
+                for (int d = 0; d < 3; ++d) xi[3 * s + d] = d < dim ? tmp[(size_t)d * N + s] : 0.0;
+        }
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int uwgpu_assemble(uwgpu_ctx* ctx) {
+    return guarded(ctx, [&](Context& c) { uwg::assemble(c); });
+}
+
+int uwgpu_get_element_matrices(uwgpu_ctx* ctx, int64_t first, int64_t count, double* Ke, double* fe,
+                               double* Ge, double* Se) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(c.assembled, UWGPU_ERR_STATE, "nothing assembled");
+        int64_t E = c.mesh.ne;
+        UWG_REQUIRE(first >= 0 && count >= 0 && first + count <= E, UWGPU_ERR_ARGUMENT, "element range");
+        int dim = c.mesh.dim, nen = dim == 3 ? 8 : 4, nd = nen * dim, np = uwg::packed_size(nd);
+        if (count == 0) return;
+        auto fetch = [&](const double* base, int entries, std::vector<double>& out) {
+            out.resize((size_t)entries * count);
+            // entry-major [k][e]: one strided copy
+            UWG_CUDA(cudaMemcpy2DAsync(out.data(), count * sizeof(double), base + first, E * sizeof(double),
+                                       count * sizeof(double), entries, cudaMemcpyDeviceToHost, c.stream));
+        };
+        std::vector<double> hk, hf, hg;
+        if (Ke) fetch(c.levels[0].Ke.p, np, hk);
+        if (fe) fetch(c.fe.p, nd, hf);
+        if (Ge) fetch(c.Ge.p, nd, hg);
+        if (Se) UWG_CUDA(cudaMemcpyAsync(Se, c.Se.p + first, count * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        for (int64_t e = 0; e < count; ++e) {
+            if (Ke) {
+                double* K = Ke + e * nd * nd;
+                for (int r = 0; r < nd; ++r)
+                    for (int q = r; q < nd; ++q) {
+                        double v = hk[(size_t)uwg::packed_index(nd, r, q) * count + e];
+                        K[r * nd + q] = v;
+                        K[q * nd + r] = v;
+                    }
+            }
+            for (int k = 0; k < nd; ++k) {
+                if (fe) fe[e * nd + k] = hf[(size_t)k * count + e];
+                if (Ge) Ge[e * nd + k] = hg[(size_t)k * count + e];
+            }
+        }
+    });
+}
+
+int uwgpu_get_point_viscosity(uwgpu_ctx* ctx, double* eta) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(c.assembled, UWGPU_ERR_STATE, "nothing assembled");
+        UWG_REQUIRE(eta || c.np == 0, UWGPU_ERR_ARGUMENT, "null output");
+        if (c.np) UWG_CUDA(cudaMemcpyAsync(eta, c.seta_out.p, c.np * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int uwgpu_operator_apply(uwgpu_ctx* ctx, int32_t precision, const double* x, double* y) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(x && y, UWGPU_ERR_ARGUMENT, "null vector");
+        UWG_REQUIRE(precision == UWGPU_PREC_FP64 || precision == UWGPU_PREC_MIXED, UWGPU_ERR_ARGUMENT,
+                    "bad precision");
+        int dim = c.mesh.dim;
+        int64_t nn = c.mesh.nn;
+        if (!c.operator_built || (precision == UWGPU_PREC_MIXED && !c.operator_has32))
+            uwg::build_operator(c, c.operator_built ? c.operator_levels : 1, precision == UWGPU_PREC_MIXED);
+        std::vector<double> soa((size_t)nn * dim);
+        for (int64_t n = 0; n < nn; ++n)
+            for (int d = 0; d < dim; ++d) soa[(size_t)d * nn + n] = x[n * dim + d];
+        uwg::DArray<double> dx, dy;
+        dx.ensure(soa.size());
+        dy.ensure(soa.size());
+        UWG_CUDA(cudaMemcpyAsync(dx.p, soa.data(), soa.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        uwg::apply_fine(c, precision == UWGPU_PREC_MIXED, dx.p, dy.p);
+        UWG_CUDA(cudaMemcpyAsync(soa.data(), dy.p, soa.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        for (int64_t n = 0; n < nn; ++n)
+            for (int d = 0; d < dim; ++d) y[n * dim + d] = soa[(size_t)d * nn + n];
+    });
+}
+
+void uwgpu_solve_opts_default(uwgpu_solve_opts* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->mg_levels = 4;
+    o->smooth_down = 2;
+    o->smooth_up = 2;
+    o->schur_type = UWGPU_SCHUR_FGMRES;
+    o->schur_pc = UWGPU_SCHUR_PC_UW;
+    o->restart = 30;
+    o->max_outer = 500;
+    o->max_inner = 500;
+    o->scr_rtol = 1e-6;
+    o->a11_rtol = 1e-8;
+    o->back_rtol = 1e-8;
+    o->remove_const_p = 1;
+    o->precision = UWGPU_PREC_FP64;
+    o->target_rel_residual = 0.0;
+}
+
+int uwgpu_solve_bsscr(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, double* u, double* p, uwgpu_report* report) {
+    return guarded(ctx, [&](Context& c) {
+        uwgpu_solve_opts o;
+        if (opts) o = *opts; else uwgpu_solve_opts_default(&o);
+        uwgpu_report rep;
+        std::memset(&rep, 0, sizeof(rep));
+        uwg::solve_bsscr(c, o, rep);
+        int dim = c.mesh.dim;
+        int64_t nn = c.mesh.nn;
+        if (u) {
+            std::vector<double> soa((size_t)nn * dim);
+            UWG_CUDA(cudaMemcpyAsync(soa.data(), c.u_sol.p, soa.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            UWG_CUDA(cudaStreamSynchronize(c.stream));
+            for (int64_t n = 0; n < nn; ++n)
+                for (int d = 0; d < dim; ++d) u[n * dim + d] = soa[(size_t)d * nn + n];
+        }
+        if (p) UWG_CUDA(cudaMemcpyAsync(p, c.p_sol.p, c.mesh.ne * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        if (report) *report = rep;
+        if (rep.status != UWGPU_OK) throw Error(rep.status, "BSSCR solve did not converge");
+    });
+}
+
+int uwgpu_profile_enable(uwgpu_ctx* ctx, int32_t on) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        for (auto& f : c.prof) {
+            f.used = 0;
+            f.launches = 0;
+            f.ms = 0.0;
+        }
+        c.profiling = on != 0;
+    });
+}
+
+int uwgpu_profile_read(uwgpu_ctx* ctx, int32_t which, int64_t* launches, double* ms) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(which >= 0 && which < UWGPU_KERNEL_COUNT, UWGPU_ERR_ARGUMENT, "bad kernel family");
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        uwg::ProfileFamily& f = c.prof[which];
+        double total = f.ms;
+        for (size_t i = 0; i < f.used; ++i) {
+            float t = 0.f;
+            UWG_CUDA(cudaEventElapsedTime(&t, f.events[i].first, f.events[i].second));
+            total += t;
+        }
+        f.ms = total;
+        f.used = 0;
+        if (launches) *launches = f.launches;
+        if (ms) *ms = total;
+    });
+}
+
+int64_t uwgpu_launch_count(const uwgpu_ctx* ctx) { return ctx ? ctx->c.launches : 0; }
+
+}  // extern "C"

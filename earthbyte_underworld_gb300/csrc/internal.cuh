@@ -1,0 +1,218 @@
+// Internal declarations of libuwgpu: device context, buffers, launch accounting.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/uwgpu.h"
+
+namespace uwg {
+
+// Error carried from the internals to the C entry points, which turn it into a status code.
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define UWG_CUDA(call)                                                                     \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            throw ::uwg::Error(e_ == cudaErrorMemoryAllocation ? UWGPU_ERR_MEMORY          \
+                                                               : UWGPU_ERR_CUDA,           \
+                               std::string(#call) + ": " + cudaGetErrorString(e_));        \
+    } while (0)
+
+#define UWG_REQUIRE(cond, code, msg)                                                       \
+    do {                                                                                   \
+        if (!(cond)) throw ::uwg::Error((code), (msg));                                    \
+    } while (0)
+
+// Owning device array (cudaMalloc / cudaFree), grown on demand, never shrunk.
+template <typename T>
+struct DArray {
+    T* p = nullptr;
+    size_t n = 0;
+    DArray() = default;
+    DArray(const DArray&) = delete;
+    DArray& operator=(const DArray&) = delete;
+    ~DArray() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void ensure(size_t count) {
+        if (count <= n && p) return;
+        release();
+        if (count == 0) count = 1;
+        UWG_CUDA(cudaMalloc(&p, count * sizeof(T)));
+        n = count;
+    }
+    T* get() const { return p; }
+};
+
+// Regular Cartesian Q1 mesh description (node index = i + nx*(j + ny*k), x fastest).
+struct MeshDesc {
+    int dim = 0;
+    int nel[3] = {1, 1, 1};
+    double min[3] = {0, 0, 0};
+    double max[3] = {1, 1, 1};
+    int64_t nnx = 1, nny = 1, nnz = 1;  // node counts per axis
+    int64_t nn = 0, ne = 0;
+};
+
+// Node coordinate along axis d of node index i: CartesianGenerator_CalcGeom without contact
+// depth (StgDomain/Mesh/src/CartesianGenerator.c:2275-2310).
+__host__ __device__ inline double node_coord_1d(int64_t i, int nel, double mn, double mx) {
+    if (i <= 0) return mn;
+    if (i >= nel) return mx;
+    return mn + ((double)i / (double)nel) * (mx - mn);
+}
+
+constexpr int kMaxLevels = 10;
+
+// One level of the geometric hierarchy (level 0 = fine, as the solver sees it).
+struct Level {
+    MeshDesc mesh;
+    DArray<double> Ke;       // packed upper-triangular element matrices, entry-major [k][e]
+    DArray<double> A64;      // node-block stencil, entry-major [q][r][c][node]
+    DArray<float> A32;
+    DArray<double> Dinv64;   // inverse of the node's diagonal block [r][c][node]
+    DArray<float> Dinv32;
+    DArray<uint8_t> fixed;   // per dof (node*dim+d), Dirichlet mask
+    // work vectors (SoA by component: [d][node])
+    DArray<double> r64, x64, b64, t64;
+    DArray<float> r32, x32, b32, t32;
+    // coarsest level: dense inverse of the full-dof operator
+    DArray<double> Cinv;
+    int64_t ncoarse = 0;
+    bool has32 = false;
+};
+
+struct ProfileFamily {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;
+    size_t used = 0;
+    int64_t launches = 0;
+    double ms = 0.0;
+};
+
+struct Context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    int64_t launches = 0;
+
+    MeshDesc mesh;
+    bool has_mesh = false;
+
+    // boundary conditions (fine level)
+    DArray<uint8_t> fixed;
+    DArray<double> bcval;
+    bool has_bc = false;
+    bool bc_nonzero = false;
+
+    // materials and fields
+    DArray<uwgpu_material> mats;
+    int nmat = 0;
+    DArray<double> temperature;
+    bool has_temperature = false;
+    double gravity = 0.0;
+    int vert_axis = 1;
+    DArray<double> u_sol;     // nodal velocity, SoA [d][node]
+    DArray<double> p_sol;     // element pressure
+    bool has_solution = false;
+
+    // material points
+    int64_t np = 0;
+    DArray<double> px, py, pz;
+    DArray<int32_t> pmat;
+    DArray<double> peta, prho;
+    bool has_peta = false, has_prho = false;
+    bool has_points = false;
+
+    // binning / mapping
+    DArray<uint32_t> cell, counts, offsets, cursor, perm, tmp_perm, block_sums;
+    DArray<uint32_t> err_count;
+    DArray<double> sxi;       // [d][slot]
+    DArray<int32_t> smat;
+    DArray<double> seta_in, srho_in, seta_out;
+    bool mapped = false;
+
+    // assembly (fine level)
+    DArray<double> fe;        // entry-major [k][e]
+    DArray<double> Se;
+    DArray<double> Ge;        // entry-major [k][e]
+    bool assembled = false;
+
+    // solver state
+    Level levels[kMaxLevels];
+    int nlevels = 0;
+    bool operator_built = false;
+    int operator_levels = 0;
+    bool operator_has32 = false;
+    DArray<double> scratch;   // reductions
+    double* host_scalars = nullptr;   // pinned
+
+    bool profiling = false;
+    ProfileFamily prof[UWGPU_KERNEL_COUNT];
+};
+
+// Launch bookkeeping: counts every launch, and brackets the launch with events when the
+// family is being profiled.
+struct LaunchScope {
+    Context& c;
+    int family;
+    cudaEvent_t e1 = nullptr;
+    LaunchScope(Context& ctx, int fam) : c(ctx), family(fam) {
+        c.launches++;
+        if (c.profiling && family >= 0) {
+            ProfileFamily& f = c.prof[family];
+            if (f.used == f.events.size()) {
+                cudaEvent_t a, b;
+                UWG_CUDA(cudaEventCreate(&a));
+                UWG_CUDA(cudaEventCreate(&b));
+                f.events.emplace_back(a, b);
+            }
+            auto& pr = f.events[f.used++];
+            UWG_CUDA(cudaEventRecord(pr.first, c.stream));
+            e1 = pr.second;
+            f.launches++;
+        }
+    }
+    ~LaunchScope() {
+        if (e1) cudaEventRecord(e1, c.stream);
+    }
+};
+
+inline void check_launch(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw Error(UWGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+inline unsigned blocks_for(int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    return (unsigned)(b < 1 ? 1 : b);
+}
+
+// ---- functions shared between translation units ----
+void bin_and_map(Context& c);
+void assemble(Context& c);
+void build_operator(Context& c, int levels, bool need32);
+void apply_fine(Context& c, bool fp32, const double* x, double* y);  // device SoA vectors
+void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep);
+
+// Number of packed entries of a symmetric nd x nd element matrix.
+__host__ __device__ constexpr int packed_size(int nd) { return nd * (nd + 1) / 2; }
+// Packed index of (r, c) with r <= c, row-major upper triangle.
+__host__ __device__ inline int packed_index(int nd, int r, int c) {
+    return r * nd - (r * (r - 1)) / 2 + (c - r);
+}
+
+}  // namespace uwg

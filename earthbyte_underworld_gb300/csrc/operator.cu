@@ -1,0 +1,893 @@
+// Velocity-block operator and geometric multigrid hierarchy.
+//
+// Reference behaviour (paths relative to the Underworld 1.x tree):
+//   global K      StgFEM/SLE/SystemSetup/src/StiffnessMatrix.c:867-1017 (element scatter-add with
+//                 the location matrix; BC dofs removed, FeEquationNumber.c:700-760)
+//   transfers     StgFEM/SLE/SystemSetup/src/SROpGenerator.c:765-1060 (2:1 regular interpolation,
+//                 weight 1/nPoints over 2^(#odd indices) coarse nodes; restriction = P^T)
+//   coarse ops    StgFEM/SLE/SystemSetup/src/PETScMGSolver.c:493-549 (Galerkin P^T K P)
+//   smoother      PETScMGSolver.c:641-716 (Richardson + SOR, multiplicative V-cycle)
+//   coarse solve  PCMG's redundant direct solve on the coarsest level
+//   G, G^T        GradientStiffnessMatrixTerm (P0 pressure, one dof per element)
+//
+// GPU design.  The assembled operator is kept as a node-block stencil: for every node the 3^dim
+// neighbour blocks (dim x dim) are stored entry-major [q][r][c][node], so the apply is a pure
+// gather (one thread per node, no atomics) and each load instruction of a warp is coalesced.
+// Dirichlet dofs are identity rows/columns, so every vector keeps the full nodal length.
+// The Gauss-Seidel smoother is colour-scheduled: the 2^dim parity colours of the nodes have no
+// stencil coupling inside a colour, so a colour is relaxed in parallel without atomics.
+// Coarse element matrices are formed element by element (P_c^T K_c P_c over the 2^dim children),
+// which equals the Galerkin product for this interpolation.
+#include "internal.cuh"
+
+namespace uwg {
+
+struct Grid {
+    int dim;
+    int64_t nx, ny, nz;  // nodes per axis
+    int64_t nn;
+    int ex, ey, ez;      // elements per axis
+};
+
+static Grid grid_of(const MeshDesc& m) {
+    Grid g;
+    g.dim = m.dim;
+    g.nx = m.nnx;
+    g.ny = m.nny;
+    g.nz = m.nnz;
+    g.nn = m.nn;
+    g.ex = m.nel[0];
+    g.ey = m.nel[1];
+    g.ez = m.dim == 3 ? m.nel[2] : 1;
+    return g;
+}
+
+template <int DIM>
+__host__ __device__ constexpr int nblocks() { return DIM == 3 ? 27 : 9; }
+
+// ------------------------------------------------------------------------------------------
+// Stencil build from packed element matrices (gather per node, 9 accumulators per block).
+// ------------------------------------------------------------------------------------------
+template <int DIM>
+__global__ void k_build_stencil(Grid g, int64_t ne, const double* __restrict__ Ke, const uint8_t* __restrict__ fixed,
+                                double* __restrict__ A, double* __restrict__ Dinv) {
+    constexpr int NEN = 1 << DIM, ND = NEN * DIM, NB = nblocks<DIM>();
+    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.nn) return;
+    int64_t i = n % g.nx, j = (n / g.nx) % g.ny, k = DIM == 3 ? n / (g.nx * g.ny) : 0;
+    int64_t nidx[3] = {i, j, k};
+    int64_t ecount[3] = {g.ex, g.ey, g.ez};
+    int64_t ncount[3] = {g.nx, g.ny, g.nz};
+    bool rowfix[DIM];
+#pragma unroll
+    for (int r = 0; r < DIM; ++r) rowfix[r] = fixed ? fixed[n * DIM + r] != 0 : false;
+    double diag[DIM][DIM];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+        int off[3] = {q % 3 - 1, (q / 3) % 3 - 1, DIM == 3 ? q / 9 - 1 : 0};
+        double acc[DIM][DIM];
+#pragma unroll
+        for (int r = 0; r < DIM; ++r)
+#pragma unroll
+            for (int cc = 0; cc < DIM; ++cc) acc[r][cc] = 0.0;
+        bool valid = true;
+        int64_t m[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            m[d] = nidx[d] + off[d];
+            if (m[d] < 0 || m[d] >= ncount[d]) valid = false;
+        }
+        int64_t mnode = 0;
+        bool colfix[DIM];
+#pragma unroll
+        for (int cc = 0; cc < DIM; ++cc) colfix[cc] = false;
+        if (valid) {
+            mnode = m[0] + g.nx * (m[1] + g.ny * (DIM == 3 ? m[2] : 0));
+#pragma unroll
+            for (int cc = 0; cc < DIM; ++cc) colfix[cc] = fixed ? fixed[mnode * DIM + cc] != 0 : false;
+            // elements containing both nodes: per axis origin range
+            int64_t lo[3], hi[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                if (d >= DIM) { lo[d] = 0; hi[d] = 0; continue; }
+                int64_t a = nidx[d] < m[d] ? nidx[d] : m[d];
+                int64_t b = nidx[d] > m[d] ? nidx[d] : m[d];
+                lo[d] = b - 1 < 0 ? 0 : b - 1;
+                hi[d] = a > ecount[d] - 1 ? ecount[d] - 1 : a;
+            }
+            for (int64_t ez = lo[2]; ez <= hi[2]; ++ez)
+                for (int64_t ey = lo[1]; ey <= hi[1]; ++ey)
+                    for (int64_t ex = lo[0]; ex <= hi[0]; ++ex) {
+                        int64_t e = ex + (int64_t)g.ex * (ey + (int64_t)g.ey * ez);
+                        int la = (int)(i - ex) + 2 * (int)(j - ey) + (DIM == 3 ? 4 * (int)(k - ez) : 0);
+                        int lb = (int)(m[0] - ex) + 2 * (int)(m[1] - ey) + (DIM == 3 ? 4 * (int)(m[2] - ez) : 0);
+#pragma unroll
+                        for (int r = 0; r < DIM; ++r)
+#pragma unroll
+                            for (int cc = 0; cc < DIM; ++cc) {
+                                int R = la * DIM + r, C = lb * DIM + cc;
+                                int pi = R <= C ? packed_index(ND, R, C) : packed_index(ND, C, R);
+                                acc[r][cc] += Ke[(int64_t)pi * ne + e];
+                            }
+                    }
+        }
+#pragma unroll
+        for (int r = 0; r < DIM; ++r)
+#pragma unroll
+            for (int cc = 0; cc < DIM; ++cc) {
+                double v = acc[r][cc];
+                if (rowfix[r] || colfix[cc]) v = 0.0;
+                if (q == NB / 2 && r == cc && rowfix[r]) v = 1.0;
+                A[((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n] = v;
+                if (q == NB / 2) diag[r][cc] = v;
+            }
+    }
+    // inverse of the diagonal block
+    double inv[DIM][DIM];
+    if (DIM == 3) {
+        double a = diag[0][0], b = diag[0][1], c = diag[0][2], d = diag[1][0], e = diag[1][1], f = diag[1][2],
+               gg = diag[2][0], h = diag[2][1], ii = diag[2][2];
+        double A0 = e * ii - f * h, B0 = -(d * ii - f * gg), C0 = d * h - e * gg;
+        double det = a * A0 + b * B0 + c * C0;
+        double id = 1.0 / det;
+        inv[0][0] = A0 * id;
+        inv[1][0] = B0 * id;
+        inv[2][0] = C0 * id;
+        inv[0][1] = -(b * ii - c * h) * id;
+        inv[1][1] = (a * ii - c * gg) * id;
+        inv[2][1] = -(a * h - b * gg) * id;
+        inv[0][2] = (b * f - c * e) * id;
+        inv[1][2] = -(a * f - c * d) * id;
+        inv[2][2] = (a * e - b * d) * id;
+    } else {
+        double det = diag[0][0] * diag[1][1] - diag[0][1] * diag[1][0];
+        double id = 1.0 / det;
+        inv[0][0] = diag[1][1] * id;
+        inv[0][1] = -diag[0][1] * id;
+        inv[1][0] = -diag[1][0] * id;
+        inv[1][1] = diag[0][0] * id;
+    }
+#pragma unroll
+    for (int r = 0; r < DIM; ++r)
+#pragma unroll
+        for (int cc = 0; cc < DIM; ++cc) Dinv[(int64_t)(r * DIM + cc) * g.nn + n] = inv[r][cc];
+}
+
+template <typename S, typename D>
+__global__ void k_convert(int64_t n, const S* __restrict__ a, D* __restrict__ b) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (D)a[i];
+}
+
+// ------------------------------------------------------------------------------------------
+// Apply and smoothing.
+// ------------------------------------------------------------------------------------------
+// y_n = sum_q A_q x_{n+off(q)} for one node (T = storage/arithmetic type).
+template <int DIM, typename T>
+__device__ __forceinline__ void stencil_row(const Grid& g, int64_t n, int64_t i, int64_t j, int64_t k,
+                                            const T* __restrict__ A, const T* __restrict__ x, T out[DIM]) {
+    constexpr int NB = nblocks<DIM>();
+#pragma unroll
+    for (int r = 0; r < DIM; ++r) out[r] = (T)0;
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+        int dx = q % 3 - 1, dy = (q / 3) % 3 - 1, dz = DIM == 3 ? q / 9 - 1 : 0;
+        int64_t ii = i + dx, jj = j + dy, kk = k + dz;
+        if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || (DIM == 3 && (kk < 0 || kk >= g.nz))) continue;
+        int64_t m = n + dx + g.nx * (dy + g.ny * dz);
+        T xm[DIM];
+#pragma unroll
+        for (int cc = 0; cc < DIM; ++cc) xm[cc] = x[(int64_t)cc * g.nn + m];
+#pragma unroll
+        for (int r = 0; r < DIM; ++r)
+#pragma unroll
+            for (int cc = 0; cc < DIM; ++cc) out[r] = fma(A[((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n], xm[cc], out[r]);
+    }
+}
+
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) k_apply(Grid g, const T* __restrict__ A, const T* __restrict__ x, T* __restrict__ y) {
+    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.nn) return;
+    int64_t i = n % g.nx, j = (n / g.nx) % g.ny, k = DIM == 3 ? n / (g.nx * g.ny) : 0;
+    T out[DIM];
+    stencil_row<DIM, T>(g, n, i, j, k, A, x, out);
+#pragma unroll
+    for (int r = 0; r < DIM; ++r) y[(int64_t)r * g.nn + n] = out[r];
+}
+
+// r = b - A x
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) k_residual(Grid g, const T* __restrict__ A, const T* __restrict__ x,
+                                                  const T* __restrict__ b, T* __restrict__ r) {
+    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.nn) return;
+    int64_t i = n % g.nx, j = (n / g.nx) % g.ny, k = DIM == 3 ? n / (g.nx * g.ny) : 0;
+    T out[DIM];
+    stencil_row<DIM, T>(g, n, i, j, k, A, x, out);
+#pragma unroll
+    for (int q = 0; q < DIM; ++q) r[(int64_t)q * g.nn + n] = b[(int64_t)q * g.nn + n] - out[q];
+}
+
+// One colour of block Gauss-Seidel: x_n += Dinv_n (b_n - (A x)_n) for nodes of parity `colour`.
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) k_gs_colour(Grid g, int colour, const T* __restrict__ A, const T* __restrict__ Dinv,
+                                                   const T* __restrict__ b, T* __restrict__ x) {
+    int px = colour & 1, py = (colour >> 1) & 1, pz = (colour >> 2) & 1;
+    int64_t cx = (g.nx - px + 1) / 2, cy = (g.ny - py + 1) / 2;
+    int64_t cz = DIM == 3 ? (g.nz - pz + 1) / 2 : 1;
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cx * cy * cz) return;
+    int64_t i = 2 * (t % cx) + px, j = 2 * ((t / cx) % cy) + py, k = DIM == 3 ? 2 * (t / (cx * cy)) + pz : 0;
+    int64_t n = i + g.nx * (j + g.ny * k);
+    T ax[DIM];
+    stencil_row<DIM, T>(g, n, i, j, k, A, x, ax);
+    T res[DIM];
+#pragma unroll
+    for (int r = 0; r < DIM; ++r) res[r] = b[(int64_t)r * g.nn + n] - ax[r];
+#pragma unroll
+    for (int r = 0; r < DIM; ++r) {
+        T v = x[(int64_t)r * g.nn + n];
+#pragma unroll
+        for (int cc = 0; cc < DIM; ++cc) v = fma(Dinv[(int64_t)(r * DIM + cc) * g.nn + n], res[cc], v);
+        x[(int64_t)r * g.nn + n] = v;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Transfers (trilinear 2:1, SROpGenerator weights), Dirichlet dofs masked.
+// ------------------------------------------------------------------------------------------
+template <int DIM, typename T>
+__global__ void k_restrict(Grid gf, Grid gc, const T* __restrict__ rf, T* __restrict__ rc,
+                           const uint8_t* __restrict__ fixf, const uint8_t* __restrict__ fixc) {
+    int64_t N = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (N >= gc.nn) return;
+    int64_t I = N % gc.nx, J = (N / gc.nx) % gc.ny, K = DIM == 3 ? N / (gc.nx * gc.ny) : 0;
+    T acc[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = (T)0;
+#pragma unroll
+    for (int dz = (DIM == 3 ? -1 : 0); dz <= (DIM == 3 ? 1 : 0); ++dz)
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
+                int64_t i = 2 * I + dx, j = 2 * J + dy, k = 2 * K + dz;
+                if (i < 0 || i >= gf.nx || j < 0 || j >= gf.ny || (DIM == 3 && (k < 0 || k >= gf.nz))) continue;
+                T w = (T)((dx ? 0.5 : 1.0) * (dy ? 0.5 : 1.0) * (dz ? 0.5 : 1.0));
+                int64_t n = i + gf.nx * (j + gf.ny * k);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    if (!fixf || !fixf[n * DIM + d]) acc[d] = fma(w, rf[(int64_t)d * gf.nn + n], acc[d]);
+            }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) rc[(int64_t)d * gc.nn + N] = (fixc && fixc[N * DIM + d]) ? (T)0 : acc[d];
+}
+
+template <int DIM, typename T>
+__global__ void k_prolong_add(Grid gf, Grid gc, const T* __restrict__ xc, T* __restrict__ xf,
+                              const uint8_t* __restrict__ fixf, const uint8_t* __restrict__ fixc) {
+    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= gf.nn) return;
+    int64_t idx[3] = {n % gf.nx, (n / gf.nx) % gf.ny, DIM == 3 ? n / (gf.nx * gf.ny) : 0};
+    int64_t c0[3], c1[3];
+    int cnt[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (d >= DIM) { c0[d] = c1[d] = 0; cnt[d] = 1; continue; }
+        c0[d] = idx[d] >> 1;
+        c1[d] = c0[d] + 1;
+        cnt[d] = (idx[d] & 1) ? 2 : 1;
+    }
+    T acc[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = (T)0;
+    T w = (T)(1.0 / (double)(cnt[0] * cnt[1] * cnt[2]));
+    for (int oz = 0; oz < cnt[2]; ++oz)
+        for (int oy = 0; oy < cnt[1]; ++oy)
+            for (int ox = 0; ox < cnt[0]; ++ox) {
+                int64_t I = ox ? c1[0] : c0[0], J = oy ? c1[1] : c0[1], K = oz ? c1[2] : c0[2];
+                int64_t N = I + gc.nx * (J + gc.ny * K);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d)
+                    if (!fixc || !fixc[N * DIM + d]) acc[d] = fma(w, xc[(int64_t)d * gc.nn + N], acc[d]);
+            }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+        if (!fixf || !fixf[n * DIM + d]) xf[(int64_t)d * gf.nn + n] += acc[d];
+}
+
+// ------------------------------------------------------------------------------------------
+// Galerkin coarse element matrices: K_E = sum_children P_c^T K~_c P_c, where K~_c has the
+// rows/columns of fixed fine dofs removed.
+// ------------------------------------------------------------------------------------------
+__host__ __device__ inline double interp_weight(int child_bit, int fine_bit, int coarse_bit) {
+    int f = child_bit + fine_bit;   // fine position in half units: 0, 1, 2
+    int cpos = 2 * coarse_bit;
+    if (f == cpos) return 1.0;
+    if (f == 1) return 0.5;
+    return 0.0;
+}
+
+template <int DIM>
+__global__ void k_galerkin(Grid gf, Grid gc, int64_t nef, int64_t nec, const double* __restrict__ Kf,
+                           const uint8_t* __restrict__ fixf, double* __restrict__ Kc) {
+    constexpr int NEN = 1 << DIM, ND = NEN * DIM, NP = ND * (ND + 1) / 2, NCH = 1 << DIM;
+    extern __shared__ double sK[];  // NCH * ND * ND
+    int64_t E = blockIdx.x;
+    if (E >= nec) return;
+    int64_t EI = E % gc.ex, EJ = (E / gc.ex) % gc.ey, EK = DIM == 3 ? E / ((int64_t)gc.ex * gc.ey) : 0;
+    // load the children's full element matrices, fixed fine dofs zeroed
+    for (int t = threadIdx.x; t < NCH * ND * ND; t += blockDim.x) {
+        int ch = t / (ND * ND), rc = t % (ND * ND), R = rc / ND, C = rc % ND;
+        int cx = ch & 1, cy = (ch >> 1) & 1, cz = (ch >> 2) & 1;
+        int64_t fe = (2 * EI + cx) + (int64_t)gf.ex * ((2 * EJ + cy) + (int64_t)gf.ey * (DIM == 3 ? 2 * EK + cz : 0));
+        int la = R / DIM, lb = C / DIM;
+        int64_t fo = (2 * EI + cx) + gf.nx * ((2 * EJ + cy) + gf.ny * (DIM == 3 ? 2 * EK + cz : 0));
+        int64_t na = fo + (la & 1) + ((la >> 1) & 1) * gf.nx + (DIM == 3 ? ((la >> 2) & 1) * gf.nx * gf.ny : 0);
+        int64_t nb = fo + (lb & 1) + ((lb >> 1) & 1) * gf.nx + (DIM == 3 ? ((lb >> 2) & 1) * gf.nx * gf.ny : 0);
+        bool fx = fixf && (fixf[na * DIM + R % DIM] || fixf[nb * DIM + C % DIM]);
+        int pi = R <= C ? packed_index(ND, R, C) : packed_index(ND, C, R);
+        sK[t] = fx ? 0.0 : Kf[(int64_t)pi * nef + fe];
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < NP; o += blockDim.x) {
+        // decode packed (R, C), R <= C
+        int R = 0, rem = o;
+        while (rem >= ND - R) { rem -= ND - R; R++; }
+        int C = R + rem;
+        int I = R / DIM, a = R % DIM, J = C / DIM, b = C % DIM;
+        double acc = 0.0;
+        for (int ch = 0; ch < NCH; ++ch) {
+            int cb[3] = {ch & 1, (ch >> 1) & 1, (ch >> 2) & 1};
+            const double* K = sK + ch * ND * ND;
+            for (int i = 0; i < NEN; ++i) {
+                double wi = 1.0;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) wi *= interp_weight(cb[d], (i >> d) & 1, (I >> d) & 1);
+                if (wi == 0.0) continue;
+                for (int j = 0; j < NEN; ++j) {
+                    double wj = 1.0;
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) wj *= interp_weight(cb[d], (j >> d) & 1, (J >> d) & 1);
+                    if (wj == 0.0) continue;
+                    acc += wi * wj * K[(i * DIM + a) * ND + j * DIM + b];
+                }
+            }
+        }
+        Kc[(int64_t)o * nec + E] = acc;
+    }
+}
+
+// coarse fixed mask by injection from the finer level
+template <int DIM>
+__global__ void k_inject_mask(Grid gf, Grid gc, const uint8_t* __restrict__ fixf, uint8_t* __restrict__ fixc) {
+    int64_t N = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (N >= gc.nn) return;
+    int64_t I = N % gc.nx, J = (N / gc.nx) % gc.ny, K = DIM == 3 ? N / (gc.nx * gc.ny) : 0;
+    int64_t n = 2 * I + gf.nx * (2 * J + gf.ny * 2 * K);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) fixc[N * DIM + d] = fixf ? fixf[n * DIM + d] : 0;
+}
+
+// ------------------------------------------------------------------------------------------
+// Coarsest level: dense operator (SoA dof order d*nn + node) and Gauss-Jordan inverse.
+// ------------------------------------------------------------------------------------------
+template <int DIM>
+__global__ void k_dense_from_stencil(Grid g, const double* __restrict__ A, double* __restrict__ M) {
+    constexpr int NB = nblocks<DIM>();
+    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.nn) return;
+    int64_t N = g.nn * DIM;
+    int64_t i = n % g.nx, j = (n / g.nx) % g.ny, k = DIM == 3 ? n / (g.nx * g.ny) : 0;
+    for (int q = 0; q < NB; ++q) {
+        int dx = q % 3 - 1, dy = (q / 3) % 3 - 1, dz = DIM == 3 ? q / 9 - 1 : 0;
+        int64_t ii = i + dx, jj = j + dy, kk = k + dz;
+        if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || (DIM == 3 && (kk < 0 || kk >= g.nz))) continue;
+        int64_t m = n + dx + g.nx * (dy + g.ny * dz);
+        for (int r = 0; r < DIM; ++r)
+            for (int cc = 0; cc < DIM; ++cc)
+                M[((int64_t)r * g.nn + n) * N + (int64_t)cc * g.nn + m] = A[((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n];
+    }
+}
+
+__global__ void k_gj_save(int64_t n, int64_t k, const double* __restrict__ M, double* __restrict__ row,
+                          double* __restrict__ col) {
+    // row <- pivot row scaled by 1/pivot (row[k] <- 1/pivot), col <- pivot column
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) {
+        double ip = 1.0 / M[k * n + k];
+        row[t] = t == k ? ip : M[k * n + t] * ip;
+        col[t] = M[t * n + k];
+    }
+}
+
+// In-place Gauss-Jordan step k (no pivoting: the coarse operator is SPD).
+__global__ void k_gj_update(int64_t n, int64_t k, double* __restrict__ M, const double* __restrict__ row,
+                            const double* __restrict__ col) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    int64_t i = t / n, j = t % n;
+    if (i == k) M[t] = row[j];
+    else if (j == k) M[t] = -col[i] * row[k];
+    else M[t] = fma(-col[i], row[j], M[t]);
+}
+
+// x = M b (one warp per row)
+template <typename T>
+__global__ void k_gemv(int64_t n, const double* __restrict__ M, const T* __restrict__ b, T* __restrict__ x) {
+    int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    double s = 0.0;
+    for (int64_t j = lane; j < n; j += 32) s += M[row * n + j] * (double)b[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) x[row] = (T)s;
+}
+
+// ------------------------------------------------------------------------------------------
+// Host-side hierarchy construction.
+// ------------------------------------------------------------------------------------------
+static void build_stencil_level(Context& c, Level& L, const uint8_t* fixed) {
+    Grid g = grid_of(L.mesh);
+    int dim = L.mesh.dim;
+    int nb = dim == 3 ? 27 : 9;
+    L.A64.ensure((size_t)nb * dim * dim * g.nn);
+    L.Dinv64.ensure((size_t)dim * dim * g.nn);
+    {
+        LaunchScope ls(c, -1);
+        if (dim == 3)
+            k_build_stencil<3><<<blocks_for(g.nn, 128), 128, 0, c.stream>>>(g, L.mesh.ne, L.Ke.p, fixed, L.A64.p, L.Dinv64.p);
+        else
+            k_build_stencil<2><<<blocks_for(g.nn, 128), 128, 0, c.stream>>>(g, L.mesh.ne, L.Ke.p, fixed, L.A64.p, L.Dinv64.p);
+    }
+    check_launch("k_build_stencil");
+}
+
+static void to_fp32(Context& c, const DArray<double>& a, DArray<float>& b) {
+    b.ensure(a.n);
+    LaunchScope ls(c, -1);
+    k_convert<double, float><<<blocks_for((int64_t)a.n, 256), 256, 0, c.stream>>>((int64_t)a.n, a.p, b.p);
+    check_launch("k_convert");
+}
+
+static void coarse_inverse(Context& c, Level& L) {
+    Grid g = grid_of(L.mesh);
+    int dim = L.mesh.dim;
+    int64_t n = g.nn * dim;
+    UWG_REQUIRE(n <= 20000, UWGPU_ERR_ARGUMENT,
+                "coarsest multigrid level too large for the dense solve; use more levels");
+    L.ncoarse = n;
+    L.Cinv.ensure((size_t)(n * n));
+    UWG_CUDA(cudaMemsetAsync(L.Cinv.p, 0, (size_t)(n * n) * sizeof(double), c.stream));
+    {
+        LaunchScope ls(c, -1);
+        if (dim == 3)
+            k_dense_from_stencil<3><<<blocks_for(g.nn, 128), 128, 0, c.stream>>>(g, L.A64.p, L.Cinv.p);
+        else
+            k_dense_from_stencil<2><<<blocks_for(g.nn, 128), 128, 0, c.stream>>>(g, L.A64.p, L.Cinv.p);
+    }
+    check_launch("k_dense_from_stencil");
+    DArray<double> row, col;
+    row.ensure((size_t)n);
+    col.ensure((size_t)n);
+    for (int64_t k = 0; k < n; ++k) {
+        {
+            LaunchScope ls(c, -1);
+            k_gj_save<<<blocks_for(n, 256), 256, 0, c.stream>>>(n, k, L.Cinv.p, row.p, col.p);
+        }
+        {
+            LaunchScope ls(c, -1);
+            k_gj_update<<<blocks_for(n * n, 256), 256, 0, c.stream>>>(n, k, L.Cinv.p, row.p, col.p);
+        }
+    }
+    check_launch("k_gj_update");
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+void build_operator(Context& c, int levels, bool need32) {
+    UWG_REQUIRE(c.assembled, UWGPU_ERR_STATE, "operator requested before assembly");
+    const MeshDesc& m = c.mesh;
+    int dim = m.dim;
+    // the number of levels the mesh admits (each coarsening halves every axis)
+    int maxlev = 1;
+    {
+        int nel[3] = {m.nel[0], m.nel[1], dim == 3 ? m.nel[2] : 2};
+        while (maxlev < kMaxLevels) {
+            bool ok = true;
+            for (int d = 0; d < dim; ++d) ok = ok && (nel[d] % 2 == 0) && nel[d] >= 2;
+            if (!ok) break;
+            for (int d = 0; d < dim; ++d) nel[d] /= 2;
+            maxlev++;
+        }
+    }
+    if (levels < 1) levels = 1;
+    if (levels > maxlev) levels = maxlev;
+    c.nlevels = levels;
+    Level& L0 = c.levels[0];
+    L0.mesh = m;
+    L0.fixed.ensure((size_t)m.nn * dim);
+    if (c.has_bc)
+        UWG_CUDA(cudaMemcpyAsync(L0.fixed.p, c.fixed.p, (size_t)m.nn * dim, cudaMemcpyDeviceToDevice, c.stream));
+    else
+        UWG_CUDA(cudaMemsetAsync(L0.fixed.p, 0, (size_t)m.nn * dim, c.stream));
+    build_stencil_level(c, L0, L0.fixed.p);
+    for (int l = 1; l < levels; ++l) {
+        Level& F = c.levels[l - 1];
+        Level& C = c.levels[l];
+        C.mesh = F.mesh;
+        for (int d = 0; d < dim; ++d) C.mesh.nel[d] = F.mesh.nel[d] / 2;
+        C.mesh.nnx = C.mesh.nel[0] + 1;
+        C.mesh.nny = C.mesh.nel[1] + 1;
+        C.mesh.nnz = dim == 3 ? C.mesh.nel[2] + 1 : 1;
+        C.mesh.nn = C.mesh.nnx * C.mesh.nny * C.mesh.nnz;
+        C.mesh.ne = (int64_t)C.mesh.nel[0] * C.mesh.nel[1] * (dim == 3 ? C.mesh.nel[2] : 1);
+        Grid gf = grid_of(F.mesh), gc = grid_of(C.mesh);
+        int nd = (1 << dim) * dim;
+        C.Ke.ensure((size_t)packed_size(nd) * C.mesh.ne);
+        C.fixed.ensure((size_t)C.mesh.nn * dim);
+        {
+            LaunchScope ls(c, -1);
+            size_t smem = (size_t)(1 << dim) * nd * nd * sizeof(double);
+            if (dim == 3) {
+                cudaFuncSetAttribute(k_galerkin<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                k_galerkin<3><<<(unsigned)C.mesh.ne, 320, smem, c.stream>>>(gf, gc, F.mesh.ne, C.mesh.ne, F.Ke.p, F.fixed.p, C.Ke.p);
+            } else {
+                k_galerkin<2><<<(unsigned)C.mesh.ne, 64, smem, c.stream>>>(gf, gc, F.mesh.ne, C.mesh.ne, F.Ke.p, F.fixed.p, C.Ke.p);
+            }
+        }
+        check_launch("k_galerkin");
+        {
+            LaunchScope ls(c, -1);
+            if (dim == 3)
+                k_inject_mask<3><<<blocks_for(gc.nn, 256), 256, 0, c.stream>>>(gf, gc, F.fixed.p, C.fixed.p);
+            else
+                k_inject_mask<2><<<blocks_for(gc.nn, 256), 256, 0, c.stream>>>(gf, gc, F.fixed.p, C.fixed.p);
+        }
+        check_launch("k_inject_mask");
+        build_stencil_level(c, C, C.fixed.p);
+    }
+    for (int l = 0; l < levels; ++l) {
+        Level& L = c.levels[l];
+        size_t nv = (size_t)L.mesh.nn * dim;
+        L.r64.ensure(nv);
+        L.x64.ensure(nv);
+        L.b64.ensure(nv);
+        L.t64.ensure(nv);
+        L.has32 = false;
+        if (need32) {
+            to_fp32(c, L.A64, L.A32);
+            to_fp32(c, L.Dinv64, L.Dinv32);
+            L.r32.ensure(nv);
+            L.x32.ensure(nv);
+            L.b32.ensure(nv);
+            L.t32.ensure(nv);
+            L.has32 = true;
+        }
+    }
+    if (levels > 1) coarse_inverse(c, c.levels[levels - 1]);
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+    c.operator_built = true;
+    c.operator_levels = levels;
+    c.operator_has32 = need32;
+}
+
+// ------------------------------------------------------------------------------------------
+// Level operations used by the solver.
+// ------------------------------------------------------------------------------------------
+template <typename T>
+static const T* stencil_of(const Level& L);
+template <>
+const double* stencil_of<double>(const Level& L) { return L.A64.p; }
+template <>
+const float* stencil_of<float>(const Level& L) { return L.A32.p; }
+template <typename T>
+static const T* dinv_of(const Level& L);
+template <>
+const double* dinv_of<double>(const Level& L) { return L.Dinv64.p; }
+template <>
+const float* dinv_of<float>(const Level& L) { return L.Dinv32.p; }
+
+template <typename T>
+void level_apply(Context& c, const Level& L, const T* x, T* y) {
+    Grid g = grid_of(L.mesh);
+    LaunchScope ls(c, UWGPU_KERNEL_APPLY);
+    if (g.dim == 3)
+        k_apply<3, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, y);
+    else
+        k_apply<2, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, y);
+}
+
+template <typename T>
+void level_residual(Context& c, const Level& L, const T* x, const T* b, T* r) {
+    Grid g = grid_of(L.mesh);
+    LaunchScope ls(c, UWGPU_KERNEL_APPLY);
+    if (g.dim == 3)
+        k_residual<3, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, b, r);
+    else
+        k_residual<2, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, b, r);
+}
+
+// symmetric sweep: colours ascending then descending
+template <typename T>
+void level_smooth(Context& c, const Level& L, const T* b, T* x, int sweeps) {
+    Grid g = grid_of(L.mesh);
+    int ncol = 1 << g.dim;
+    for (int s = 0; s < sweeps; ++s) {
+        for (int pass = 0; pass < 2; ++pass)
+            for (int k = 0; k < ncol; ++k) {
+                int col = pass == 0 ? k : ncol - 1 - k;
+                int px = col & 1, py = (col >> 1) & 1, pz = (col >> 2) & 1;
+                int64_t cnt = ((g.nx - px + 1) / 2) * ((g.ny - py + 1) / 2) * (g.dim == 3 ? (g.nz - pz + 1) / 2 : 1);
+                LaunchScope ls(c, UWGPU_KERNEL_SMOOTH);
+                if (g.dim == 3)
+                    k_gs_colour<3, T><<<blocks_for(cnt, 256), 256, 0, c.stream>>>(g, col, stencil_of<T>(L), dinv_of<T>(L), b, x);
+                else
+                    k_gs_colour<2, T><<<blocks_for(cnt, 256), 256, 0, c.stream>>>(g, col, stencil_of<T>(L), dinv_of<T>(L), b, x);
+            }
+    }
+}
+
+template <typename T>
+void level_restrict(Context& c, const Level& F, const Level& C, const T* rf, T* rc) {
+    Grid gf = grid_of(F.mesh), gc = grid_of(C.mesh);
+    LaunchScope ls(c, -1);
+    if (gf.dim == 3)
+        k_restrict<3, T><<<blocks_for(gc.nn, 256), 256, 0, c.stream>>>(gf, gc, rf, rc, F.fixed.p, C.fixed.p);
+    else
+        k_restrict<2, T><<<blocks_for(gc.nn, 256), 256, 0, c.stream>>>(gf, gc, rf, rc, F.fixed.p, C.fixed.p);
+}
+
+template <typename T>
+void level_prolong_add(Context& c, const Level& F, const Level& C, const T* xc, T* xf) {
+    Grid gf = grid_of(F.mesh), gc = grid_of(C.mesh);
+    LaunchScope ls(c, -1);
+    if (gf.dim == 3)
+        k_prolong_add<3, T><<<blocks_for(gf.nn, 256), 256, 0, c.stream>>>(gf, gc, xc, xf, F.fixed.p, C.fixed.p);
+    else
+        k_prolong_add<2, T><<<blocks_for(gf.nn, 256), 256, 0, c.stream>>>(gf, gc, xc, xf, F.fixed.p, C.fixed.p);
+}
+
+template <typename T>
+void level_coarse_solve(Context& c, const Level& L, const T* b, T* x) {
+    LaunchScope ls(c, -1);
+    k_gemv<T><<<blocks_for(L.ncoarse * 32, 256), 256, 0, c.stream>>>(L.ncoarse, L.Cinv.p, b, x);
+}
+
+template void level_apply<double>(Context&, const Level&, const double*, double*);
+template void level_apply<float>(Context&, const Level&, const float*, float*);
+template void level_residual<double>(Context&, const Level&, const double*, const double*, double*);
+template void level_residual<float>(Context&, const Level&, const float*, const float*, float*);
+template void level_smooth<double>(Context&, const Level&, const double*, double*, int);
+template void level_smooth<float>(Context&, const Level&, const float*, float*, int);
+template void level_restrict<double>(Context&, const Level&, const Level&, const double*, double*);
+template void level_restrict<float>(Context&, const Level&, const Level&, const float*, float*);
+template void level_prolong_add<double>(Context&, const Level&, const Level&, const double*, double*);
+template void level_prolong_add<float>(Context&, const Level&, const Level&, const float*, float*);
+template void level_coarse_solve<double>(Context&, const Level&, const double*, double*);
+template void level_coarse_solve<float>(Context&, const Level&, const float*, float*);
+
+void apply_fine(Context& c, bool fp32, const double* x, double* y) {
+    Level& L = c.levels[0];
+    if (!fp32) {
+        level_apply<double>(c, L, x, y);
+    } else {
+        size_t nv = (size_t)L.mesh.nn * L.mesh.dim;
+        {
+            LaunchScope ls(c, -1);
+            k_convert<double, float><<<blocks_for((int64_t)nv, 256), 256, 0, c.stream>>>((int64_t)nv, x, L.x32.p);
+        }
+        level_apply<float>(c, L, L.x32.p, L.r32.p);
+        {
+            LaunchScope ls(c, -1);
+            k_convert<float, double><<<blocks_for((int64_t)nv, 256), 256, 0, c.stream>>>((int64_t)nv, L.r32.p, y);
+        }
+    }
+    check_launch("apply_fine");
+}
+
+// ------------------------------------------------------------------------------------------
+// Gradient operators on the fine level (P0 pressure).
+// G_e[a][d] = -s_{d,a} * prod_{q != d} h_q / 2^(dim-1): the 2^dim-point Gauss integral of
+// -dN_a/dx_d over the affine element.
+// ------------------------------------------------------------------------------------------
+struct GeoArgs {
+    int nel[3];
+    double min[3], max[3];
+};
+
+template <int DIM>
+__device__ __forceinline__ void element_h(const GeoArgs& a, int64_t ie, int64_t je, int64_t ke, double h[3]) {
+    int64_t idx[3] = {ie, je, ke};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+        h[d] = node_coord_1d(idx[d] + 1, a.nel[d], a.min[d], a.max[d]) - node_coord_1d(idx[d], a.nel[d], a.min[d], a.max[d]);
+}
+
+template <int DIM>
+__device__ __forceinline__ double gval(const double h[3], int a, int d) {
+    double area = 1.0;
+#pragma unroll
+    for (int q = 0; q < DIM; ++q)
+        if (q != d) area *= h[q];
+    double s = ((a >> d) & 1) ? 1.0 : -1.0;
+    return -s * area * (DIM == 3 ? 0.25 : 0.5);
+}
+
+// u = G p   (velocity SoA, fixed dofs zero)
+template <int DIM>
+__global__ void k_G(Grid g, GeoArgs geo, const double* __restrict__ p, const uint8_t* __restrict__ fixed,
+                    double* __restrict__ u) {
+    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.nn) return;
+    int64_t idx[3] = {n % g.nx, (n / g.nx) % g.ny, DIM == 3 ? n / (g.nx * g.ny) : 0};
+    int64_t ecount[3] = {g.ex, g.ey, g.ez};
+    double acc[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = 0.0;
+#pragma unroll
+    for (int o = 0; o < (1 << DIM); ++o) {
+        int64_t e3[3];
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            if (d >= DIM) { e3[d] = 0; continue; }
+            e3[d] = idx[d] - ((o >> d) & 1);
+            if (e3[d] < 0 || e3[d] >= ecount[d]) ok = false;
+        }
+        if (!ok) continue;
+        int a = 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) a |= ((o >> d) & 1) << d;
+        int64_t e = e3[0] + (int64_t)g.ex * (e3[1] + (int64_t)g.ey * e3[2]);
+        double h[3];
+        element_h<DIM>(geo, e3[0], e3[1], e3[2], h);
+        double pe = p[e];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) acc[d] += gval<DIM>(h, a, d) * pe;
+    }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) u[(int64_t)d * g.nn + n] = (fixed && fixed[n * DIM + d]) ? 0.0 : acc[d];
+}
+
+// p = G^T u
+template <int DIM>
+__global__ void k_GT(Grid g, GeoArgs geo, const double* __restrict__ u, const uint8_t* __restrict__ fixed,
+                     double* __restrict__ p) {
+    int64_t ne = (int64_t)g.ex * g.ey * g.ez;
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    int64_t ie = e % g.ex, je = (e / g.ex) % g.ey, ke = DIM == 3 ? e / ((int64_t)g.ex * g.ey) : 0;
+    double h[3];
+    element_h<DIM>(geo, ie, je, ke, h);
+    int64_t base = ie + g.nx * (je + g.ny * ke);
+    double acc = 0.0;
+#pragma unroll
+    for (int a = 0; a < (1 << DIM); ++a) {
+        int64_t n = base + (a & 1) + ((a >> 1) & 1) * g.nx + (DIM == 3 ? ((a >> 2) & 1) * g.nx * g.ny : 0);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d)
+            if (!fixed || !fixed[n * DIM + d]) acc += gval<DIM>(h, a, d) * u[(int64_t)d * g.nn + n];
+    }
+    p[e] = acc;
+}
+
+// f (nodal SoA) = sum of element force vectors, fixed dofs zero
+template <int DIM>
+__global__ void k_gather_force(Grid g, const double* __restrict__ fe, int64_t ne, const uint8_t* __restrict__ fixed,
+                               double* __restrict__ f) {
+    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.nn) return;
+    int64_t idx[3] = {n % g.nx, (n / g.nx) % g.ny, DIM == 3 ? n / (g.nx * g.ny) : 0};
+    int64_t ecount[3] = {g.ex, g.ey, g.ez};
+    double acc[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = 0.0;
+#pragma unroll
+    for (int o = 0; o < (1 << DIM); ++o) {
+        int64_t e3[3];
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            if (d >= DIM) { e3[d] = 0; continue; }
+            e3[d] = idx[d] - ((o >> d) & 1);
+            if (e3[d] < 0 || e3[d] >= ecount[d]) ok = false;
+        }
+        if (!ok) continue;
+        int64_t e = e3[0] + (int64_t)g.ex * (e3[1] + (int64_t)g.ey * e3[2]);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) acc[d] += fe[(int64_t)(o * DIM + d) * ne + e];
+    }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) f[(int64_t)d * g.nn + n] = (fixed && fixed[n * DIM + d]) ? 0.0 : acc[d];
+}
+
+// gkgdiag: diag(G^T diag(K)^{-1} G) per element, using the assembled diagonal
+template <int DIM>
+__global__ void k_gkgdiag(Grid g, GeoArgs geo, const double* __restrict__ A, const uint8_t* __restrict__ fixed,
+                          double* __restrict__ S) {
+    int64_t ne = (int64_t)g.ex * g.ey * g.ez;
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    constexpr int NB = nblocks<DIM>();
+    int64_t ie = e % g.ex, je = (e / g.ex) % g.ey, ke = DIM == 3 ? e / ((int64_t)g.ex * g.ey) : 0;
+    double h[3];
+    element_h<DIM>(geo, ie, je, ke, h);
+    int64_t base = ie + g.nx * (je + g.ny * ke);
+    double acc = 0.0;
+#pragma unroll
+    for (int a = 0; a < (1 << DIM); ++a) {
+        int64_t n = base + (a & 1) + ((a >> 1) & 1) * g.nx + (DIM == 3 ? ((a >> 2) & 1) * g.nx * g.ny : 0);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            if (fixed && fixed[n * DIM + d]) continue;
+            double kd = A[((int64_t)((NB / 2) * DIM + d) * DIM + d) * g.nn + n];
+            double gv = gval<DIM>(h, a, d);
+            acc += gv * gv / kd;
+        }
+    }
+    S[e] = acc;
+}
+
+static GeoArgs geo_of(const MeshDesc& m) {
+    GeoArgs a;
+    for (int d = 0; d < 3; ++d) {
+        a.nel[d] = m.nel[d];
+        a.min[d] = m.min[d];
+        a.max[d] = m.max[d];
+    }
+    return a;
+}
+
+void op_G(Context& c, const double* p, double* u) {
+    const Level& L = c.levels[0];
+    Grid g = grid_of(L.mesh);
+    LaunchScope ls(c, -1);
+    if (g.dim == 3)
+        k_G<3><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), p, L.fixed.p, u);
+    else
+        k_G<2><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), p, L.fixed.p, u);
+}
+
+void op_GT(Context& c, const double* u, double* p) {
+    const Level& L = c.levels[0];
+    Grid g = grid_of(L.mesh);
+    LaunchScope ls(c, -1);
+    if (g.dim == 3)
+        k_GT<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), u, L.fixed.p, p);
+    else
+        k_GT<2><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), u, L.fixed.p, p);
+}
+
+void op_GT_unmasked(Context& c, const double* u, double* p) {
+    const Level& L = c.levels[0];
+    Grid g = grid_of(L.mesh);
+    LaunchScope ls(c, -1);
+    if (g.dim == 3)
+        k_GT<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), u, nullptr, p);
+    else
+        k_GT<2><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), u, nullptr, p);
+}
+
+void gather_force(Context& c, double* f) {
+    const Level& L = c.levels[0];
+    Grid g = grid_of(L.mesh);
+    LaunchScope ls(c, -1);
+    if (g.dim == 3)
+        k_gather_force<3><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, c.fe.p, L.mesh.ne, L.fixed.p, f);
+    else
+        k_gather_force<2><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, c.fe.p, L.mesh.ne, L.fixed.p, f);
+}
+
+void gkgdiag(Context& c, double* S) {
+    const Level& L = c.levels[0];
+    Grid g = grid_of(L.mesh);
+    LaunchScope ls(c, -1);
+    if (g.dim == 3)
+        k_gkgdiag<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), L.A64.p, L.fixed.p, S);
+    else
+        k_gkgdiag<2><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), L.A64.p, L.fixed.p, S);
+}
+
+}  // namespace uwg

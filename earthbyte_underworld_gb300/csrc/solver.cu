@@ -1,0 +1,755 @@
+// BSSCR Schur-complement Stokes solve on the device.
+//
+// Reference behaviour (paths relative to the Underworld 1.x tree):
+//   driver     Solvers/KSPSolvers/src/BSSCR/auglag-driver-DGTGD.c:53-441 (penalty 0):
+//              h_hat = h - G^T K^{-1} f; Schur solve S p = h_hat with S = G^T K^{-1} G;
+//              null-space removal (ksp_pressure_nullspace.c:82-176); back-solve u = K^{-1}(f - G p)
+//   Schur PC   preconditioner.c:130-215 ("uw": approxS from UzawaPreconditionerTerm; "gkgdiag")
+//   A11 solve  FGMRES preconditioned by a multiplicative V-cycle (mg.c:42-132, PETScMGSolver.c)
+//
+// Precision forms.  FP64: every vector, operator and smoother in FP64.  Mixed: each velocity
+// (A11) solve is FP64 iterative refinement around an FP32 FGMRES whose V-cycle (stencils,
+// smoothers, transfers) runs in FP32, with FP64 kept for the refinement residuals, the pressure
+// Schur-complement iteration and the coarsest-level solve.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "internal.cuh"
+
+namespace uwg {
+
+template <typename T> void level_apply(Context&, const Level&, const T*, T*);
+template <typename T> void level_residual(Context&, const Level&, const T*, const T*, T*);
+template <typename T> void level_smooth(Context&, const Level&, const T*, T*, int);
+template <typename T> void level_restrict(Context&, const Level&, const Level&, const T*, T*);
+template <typename T> void level_prolong_add(Context&, const Level&, const Level&, const T*, T*);
+template <typename T> void level_coarse_solve(Context&, const Level&, const T*, T*);
+void op_G(Context& c, const double* p, double* u);
+void op_GT(Context& c, const double* u, double* p);
+void op_GT_unmasked(Context& c, const double* u, double* p);
+void gather_force(Context& c, double* f);
+void gkgdiag(Context& c, double* S);
+
+// ------------------------------------------------------------------------------------------
+// Vector kernels
+// ------------------------------------------------------------------------------------------
+constexpr int kRedBlocks = 608;   // 4 x 152 SMs
+constexpr int kRedThreads = 256;
+
+template <typename T>
+__global__ void k_set(int64_t n, T v, T* __restrict__ x) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = v;
+}
+
+template <typename T>
+__global__ void k_axpy(int64_t n, T a, const T* __restrict__ x, T* __restrict__ y) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = fma(a, x[i], y[i]);
+}
+
+template <typename T>
+__global__ void k_scale(int64_t n, T a, const T* __restrict__ x, T* __restrict__ y) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = a * x[i];
+}
+
+// y = x - y (used for r = b - Ax with Ax in y)
+template <typename T>
+__global__ void k_sub_from(int64_t n, const T* __restrict__ x, T* __restrict__ y) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = x[i] - y[i];
+}
+
+__global__ void k_pointwise_div(int64_t n, const double* __restrict__ x, const double* __restrict__ d, double* __restrict__ y) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = x[i] / d[i];
+}
+
+template <typename S, typename D>
+__global__ void k_cast(int64_t n, const S* __restrict__ a, D* __restrict__ b) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (D)a[i];
+}
+
+// y += (D) x
+template <typename S, typename D>
+__global__ void k_cast_add(int64_t n, const S* __restrict__ a, D* __restrict__ b) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] += (D)a[i];
+}
+
+// partial[j*G + block] = sum_i V[j*ldv + i] * w[i] for j < m (FP64 accumulation)
+template <typename T, int CH>
+__global__ void __launch_bounds__(kRedThreads) k_multidot(int64_t n, const T* __restrict__ V, int64_t ldv, int m,
+                                                          const T* __restrict__ w, double* __restrict__ partial) {
+    __shared__ double sred[kRedThreads / 32][CH];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int j0 = 0; j0 < m; j0 += CH) {
+        double acc[CH];
+#pragma unroll
+        for (int q = 0; q < CH; ++q) acc[q] = 0.0;
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+            double wi = (double)w[i];
+#pragma unroll
+            for (int q = 0; q < CH; ++q)
+                if (j0 + q < m) acc[q] = fma((double)V[(int64_t)(j0 + q) * ldv + i], wi, acc[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < CH; ++q) {
+            double v = acc[q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) sred[warp][q] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < CH && j0 + (int)threadIdx.x < m) {
+            double s = 0.0;
+            for (int wv = 0; wv < kRedThreads / 32; ++wv) s += sred[wv][threadIdx.x];
+            partial[(int64_t)(j0 + threadIdx.x) * gridDim.x + blockIdx.x] = s;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_reduce_partials(int m, int nb, const double* __restrict__ partial, double* __restrict__ out) {
+    int j = blockIdx.x;
+    if (j >= m) return;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) s += partial[(int64_t)j * nb + i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ double sw[32];
+    if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sw[k];
+        out[j] = t;
+    }
+}
+
+// w -= sum_j h[j] V_j   (h on the device)
+template <typename T>
+__global__ void k_multi_axpy(int64_t n, const T* __restrict__ V, int64_t ldv, int m, const double* __restrict__ h,
+                             T* __restrict__ w, double sign) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double acc = (double)w[i];
+    for (int j = 0; j < m; ++j) acc = fma(sign * h[j], (double)V[(int64_t)j * ldv + i], acc);
+    w[i] = (T)acc;
+}
+
+// x += sum_j y[j] Z_j  (y on the device)
+template <typename T, typename X>
+__global__ void k_combine(int64_t n, const T* __restrict__ Z, int64_t ldz, int m, const double* __restrict__ y,
+                          X* __restrict__ x) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double acc = (double)x[i];
+    for (int j = 0; j < m; ++j) acc = fma(y[j], (double)Z[(int64_t)j * ldz + i], acc);
+    x[i] = (X)acc;
+}
+
+__global__ void k_remove_mean(int64_t n, const double* __restrict__ sum, double* __restrict__ x) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] -= sum[0] / (double)n;
+}
+
+// ------------------------------------------------------------------------------------------
+// Solver state
+// ------------------------------------------------------------------------------------------
+struct Reducer {
+    Context& c;
+    DArray<double> partial, out;
+    explicit Reducer(Context& ctx) : c(ctx) {
+        partial.ensure((size_t)kRedBlocks * 64);
+        out.ensure(64);
+    }
+    // out[0..m) = V_j . w on the device; optionally copied to host
+    template <typename T>
+    void multidot(int64_t n, const T* V, int64_t ldv, int m, const T* w, double* host) {
+        {
+            LaunchScope ls(c, -1);
+            if (m <= 1)
+                k_multidot<T, 1><<<kRedBlocks, kRedThreads, 0, c.stream>>>(n, V, ldv, m, w, partial.p);
+            else
+                k_multidot<T, 8><<<kRedBlocks, kRedThreads, 0, c.stream>>>(n, V, ldv, m, w, partial.p);
+        }
+        {
+            LaunchScope ls(c, -1);
+            k_reduce_partials<<<m, 256, 0, c.stream>>>(m, kRedBlocks, partial.p, out.p);
+        }
+        if (host) {
+            UWG_CUDA(cudaMemcpyAsync(c.host_scalars, out.p, m * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            UWG_CUDA(cudaStreamSynchronize(c.stream));
+            std::memcpy(host, c.host_scalars, m * sizeof(double));
+        }
+    }
+    template <typename T>
+    double dot(int64_t n, const T* a, const T* b) {
+        double r;
+        multidot<T>(n, a, 0, 1, b, &r);
+        return r;
+    }
+    template <typename T>
+    double norm(int64_t n, const T* a) {
+        double d = dot<T>(n, a, a);
+        return std::sqrt(d > 0 ? d : 0.0);
+    }
+};
+
+template <typename T>
+static void axpy(Context& c, int64_t n, double a, const T* x, T* y) {
+    LaunchScope ls(c, -1);
+    k_axpy<T><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, (T)a, x, y);
+}
+template <typename T>
+static void scale(Context& c, int64_t n, double a, const T* x, T* y) {
+    LaunchScope ls(c, -1);
+    k_scale<T><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, (T)a, x, y);
+}
+template <typename T>
+static void zero(Context& c, int64_t n, T* x) {
+    UWG_CUDA(cudaMemsetAsync(x, 0, (size_t)n * sizeof(T), c.stream));
+}
+template <typename T>
+static void copy(Context& c, int64_t n, const T* x, T* y) {
+    UWG_CUDA(cudaMemcpyAsync(y, x, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, c.stream));
+}
+template <typename S, typename D>
+static void cast(Context& c, int64_t n, const S* a, D* b) {
+    LaunchScope ls(c, -1);
+    k_cast<S, D><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, a, b);
+}
+
+// Flexible GMRES(m), right preconditioning, zero initial guess; stops when ||r|| <= rtol ||b||
+// or the iteration budget is spent.  Orthogonalisation: classical Gram-Schmidt with one
+// re-orthogonalisation pass (batched dot products, one launch per pass).
+template <typename T>
+struct Fgmres {
+    Context& c;
+    Reducer& red;
+    int64_t n = 0;
+    int m = 30;
+    DArray<T> V, Z, w;
+    DArray<double> dvec;
+    std::vector<double> H, cs, sn, g, y, hcol;
+    Fgmres(Context& ctx, Reducer& r) : c(ctx), red(r) {}
+    void setup(int64_t nn, int restart) {
+        n = nn;
+        m = restart < 1 ? 1 : (restart > 60 ? 60 : restart);
+        V.ensure((size_t)(m + 1) * n);
+        Z.ensure((size_t)m * n);
+        w.ensure((size_t)n);
+        dvec.ensure(64);
+        H.assign((size_t)(m + 1) * m, 0.0);
+        cs.assign(m, 0.0);
+        sn.assign(m, 0.0);
+        g.assign(m + 1, 0.0);
+        y.assign(m, 0.0);
+        hcol.assign(m + 1, 0.0);
+    }
+    // A(x, y): y = A x ; M(v, z): z = M^{-1} v.  Returns iterations; *res = final ||r||.
+    template <typename Aop, typename Mop>
+    int solve(Aop&& A, Mop&& M, const T* b, T* x, double rtol, int maxit, double* res_out, double* bnorm_out,
+              bool* nan_out) {
+        zero<T>(c, n, x);
+        double bnorm = red.norm<T>(n, b);
+        if (bnorm_out) *bnorm_out = bnorm;
+        if (nan_out) *nan_out = !std::isfinite(bnorm);
+        if (!(bnorm > 0.0) || !std::isfinite(bnorm)) {
+            if (res_out) *res_out = 0.0;
+            return 0;
+        }
+        int its = 0;
+        double beta = bnorm;
+        // first cycle starts from x = 0, r = b
+        copy<T>(c, n, b, V.p);
+        bool first = true;
+        while (true) {
+            if (!first) {
+                A(x, w.p);
+                {
+                    LaunchScope ls(c, -1);
+                    k_sub_from<T><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, b, w.p);
+                }
+                copy<T>(c, n, w.p, V.p);
+                beta = red.norm<T>(n, V.p);
+            }
+            first = false;
+            if (!std::isfinite(beta)) {
+                if (nan_out) *nan_out = true;
+                break;
+            }
+            if (beta <= rtol * bnorm || its >= maxit) break;
+            scale<T>(c, n, 1.0 / beta, V.p, V.p);
+            std::fill(g.begin(), g.end(), 0.0);
+            g[0] = beta;
+            int k = 0;
+            bool done = false;
+            for (; k < m && its < maxit; ++k) {
+                T* vk = V.p + (int64_t)k * n;
+                T* zk = Z.p + (int64_t)k * n;
+                M(vk, zk);
+                A(zk, w.p);
+                // CGS2
+                for (int pass = 0; pass < 2; ++pass) {
+                    red.multidot<T>(n, V.p, n, k + 1, w.p, hcol.data() + 0);
+                    UWG_CUDA(cudaMemcpyAsync(dvec.p, hcol.data(), (k + 1) * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+                    {
+                        LaunchScope ls(c, -1);
+                        k_multi_axpy<T><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, V.p, n, k + 1, dvec.p, w.p, -1.0);
+                    }
+                    for (int j = 0; j <= k; ++j) {
+                        if (pass == 0) H[(size_t)j * m + k] = hcol[j];
+                        else H[(size_t)j * m + k] += hcol[j];
+                    }
+                }
+                double hn = red.norm<T>(n, w.p);
+                H[(size_t)(k + 1) * m + k] = hn;
+                if (hn > 0.0) scale<T>(c, n, 1.0 / hn, w.p, V.p + (int64_t)(k + 1) * n);
+                for (int j = 0; j < k; ++j) {
+                    double t = cs[j] * H[(size_t)j * m + k] + sn[j] * H[(size_t)(j + 1) * m + k];
+                    H[(size_t)(j + 1) * m + k] = -sn[j] * H[(size_t)j * m + k] + cs[j] * H[(size_t)(j + 1) * m + k];
+                    H[(size_t)j * m + k] = t;
+                }
+                double a = H[(size_t)k * m + k], bb = H[(size_t)(k + 1) * m + k];
+                double rr = std::sqrt(a * a + bb * bb);
+                if (!(rr > 0.0)) {
+                    done = true;
+                    k++;
+                    its++;
+                    break;
+                }
+                cs[k] = a / rr;
+                sn[k] = bb / rr;
+                H[(size_t)k * m + k] = rr;
+                H[(size_t)(k + 1) * m + k] = 0.0;
+                g[k + 1] = -sn[k] * g[k];
+                g[k] = cs[k] * g[k];
+                its++;
+                if (!std::isfinite(g[k + 1])) {
+                    if (nan_out) *nan_out = true;
+                    done = true;
+                    k++;
+                    break;
+                }
+                if (std::fabs(g[k + 1]) <= rtol * bnorm || hn == 0.0) {
+                    done = true;
+                    k++;
+                    break;
+                }
+            }
+            // y = H^{-1} g, x += Z y
+            for (int i = k - 1; i >= 0; --i) {
+                double s = g[i];
+                for (int j = i + 1; j < k; ++j) s -= H[(size_t)i * m + j] * y[j];
+                y[i] = s / H[(size_t)i * m + i];
+            }
+            UWG_CUDA(cudaMemcpyAsync(dvec.p, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+            {
+                LaunchScope ls(c, -1);
+                k_combine<T, T><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, Z.p, n, k, dvec.p, x);
+            }
+            beta = std::fabs(g[k]);
+            if (done || its >= maxit) break;
+        }
+        if (res_out) *res_out = beta;
+        return its;
+    }
+};
+
+struct Bsscr {
+    Context& c;
+    const uwgpu_solve_opts& o;
+    uwgpu_report& rep;
+    Reducer red;
+    Fgmres<double> gm64;
+    Fgmres<float> gm32;
+    Fgmres<double> gms;   // Schur (pressure)
+    int dim = 0, nlev = 0;
+    int64_t nv = 0, npres = 0;
+    bool mixed = false;
+    DArray<double> f, h, hhat, tu, tu2, t2, Sd, rhs_p, ref_r, ref_d;
+    DArray<float> r32, d32;
+    bool nan = false;
+    bool inner_fail = false;
+
+    Bsscr(Context& ctx, const uwgpu_solve_opts& opts, uwgpu_report& r)
+        : c(ctx), o(opts), rep(r), red(ctx), gm64(ctx, red), gm32(ctx, red), gms(ctx, red) {}
+
+    // ---- multigrid V-cycle (zero initial guess), precision T ----
+    template <typename T>
+    T* lvl_x(Level& L);
+    template <typename T>
+    T* lvl_b(Level& L);
+    template <typename T>
+    T* lvl_r(Level& L);
+
+    template <typename T>
+    void vcycle(int l, const T* b, T* x) {
+        Level& L = c.levels[l];
+        int64_t n = L.mesh.nn * dim;
+        if (l == nlev - 1) {
+            if (nlev > 1) {
+                level_coarse_solve<T>(c, L, b, x);
+            } else {
+                zero<T>(c, n, x);
+                level_smooth<T>(c, L, b, x, o.smooth_down + o.smooth_up);
+            }
+            return;
+        }
+        zero<T>(c, n, x);
+        level_smooth<T>(c, L, b, x, o.smooth_down);
+        T* r = lvl_r<T>(L);
+        level_residual<T>(c, L, x, b, r);
+        Level& C = c.levels[l + 1];
+        T* bc = lvl_b<T>(C);
+        T* xc = lvl_x<T>(C);
+        level_restrict<T>(c, L, C, r, bc);
+        vcycle<T>(l + 1, bc, xc);
+        level_prolong_add<T>(c, L, C, xc, x);
+        level_smooth<T>(c, L, b, x, o.smooth_up);
+    }
+
+    // ---- velocity (A11) solve: x = K^{-1} b to relative tolerance rtol ----
+    int a11(const double* b, double* x, double rtol) {
+        int its = 0;
+        Level& L0 = c.levels[0];
+        int maxit = o.max_inner > 0 ? o.max_inner : 500;
+        if (!mixed) {
+            double res = 0.0, bn = 0.0;
+            bool nn = false;
+            its = gm64.solve([&](const double* in, double* out) { level_apply<double>(c, L0, in, out); },
+                             [&](const double* in, double* out) {
+                                 vcycle<double>(0, in, out);
+                                 rep.vcycles++;
+                             },
+                             b, x, rtol, maxit, &res, &bn, &nn);
+            if (nn) nan = true;
+            if (!(res <= rtol * bn * 1.0000001) && bn > 0) inner_fail = true;
+        } else {
+            // FP64 iterative refinement around an FP32 FGMRES + FP32 V-cycle
+            zero<double>(c, nv, x);
+            double bn = red.norm<double>(nv, b);
+            if (!(bn > 0.0)) return 0;
+            if (!std::isfinite(bn)) { nan = true; return 0; }
+            copy<double>(c, nv, b, ref_r.p);
+            double rn = bn;
+            int guard = 0;
+            while (rn > rtol * bn && its < maxit && guard < 50) {
+                guard++;
+                cast<double, float>(c, nv, ref_r.p, r32.p);
+                double res = 0.0, b32n = 0.0;
+                bool nn = false;
+                double inner_rtol = std::max(rtol * bn / rn, 1e-4);
+                int k = gm32.solve([&](const float* in, float* out) { level_apply<float>(c, L0, in, out); },
+                                   [&](const float* in, float* out) {
+                                       vcycle<float>(0, in, out);
+                                       rep.vcycles++;
+                                   },
+                                   r32.p, d32.p, std::min(inner_rtol, 0.5), maxit - its, &res, &b32n, &nn);
+                its += k;
+                if (nn) { nan = true; break; }
+                {
+                    LaunchScope ls(c, -1);
+                    k_cast_add<float, double><<<blocks_for(nv, 256), 256, 0, c.stream>>>(nv, d32.p, x);
+                }
+                level_residual<double>(c, L0, x, b, ref_r.p);
+                rn = red.norm<double>(nv, ref_r.p);
+                if (!std::isfinite(rn)) { nan = true; break; }
+                if (k == 0) break;
+            }
+            if (rn > rtol * bn * 1.0000001) inner_fail = true;
+        }
+        rep.inner_its_total += its;
+        return its;
+    }
+
+    // S v = G^T K^{-1} G v  (the positive form of PETSc's MatSchurComplement)
+    void schur_apply(const double* v, double* y) {
+        op_G(c, v, tu.p);
+        a11(tu.p, tu2.p, o.a11_rtol);
+        op_GT(c, tu2.p, y);
+    }
+
+    void schur_pc(const double* v, double* z) {
+        if (o.schur_pc == UWGPU_SCHUR_PC_NONE) {
+            copy<double>(c, npres, v, z);
+        } else {
+            LaunchScope ls(c, -1);
+            k_pointwise_div<<<blocks_for(npres, 256), 256, 0, c.stream>>>(npres, v, Sd.p, z);
+        }
+    }
+
+    // preconditioned CG on the Schur system (KSPCG), unpreconditioned residual test
+    int schur_cg(const double* b, double* x, double rtol, int maxit) {
+        DArray<double> r, z, p, q;
+        r.ensure(npres);
+        z.ensure(npres);
+        p.ensure(npres);
+        q.ensure(npres);
+        zero<double>(c, npres, x);
+        copy<double>(c, npres, b, r.p);
+        double r0 = red.norm<double>(npres, r.p);
+        if (!(r0 > 0)) return 0;
+        schur_pc(r.p, z.p);
+        double rz = red.dot<double>(npres, r.p, z.p);
+        copy<double>(c, npres, z.p, p.p);
+        int it = 0;
+        double rn = r0;
+        while (it < maxit && rn > rtol * r0) {
+            schur_apply(p.p, q.p);
+            double pq = red.dot<double>(npres, p.p, q.p);
+            double alpha = rz / pq;
+            axpy<double>(c, npres, alpha, p.p, x);
+            axpy<double>(c, npres, -alpha, q.p, r.p);
+            schur_pc(r.p, z.p);
+            double rz2 = red.dot<double>(npres, r.p, z.p);
+            double beta = rz2 / rz;
+            rz = rz2;
+            {
+                // p = z + beta p
+                scale<double>(c, npres, beta, p.p, p.p);
+                axpy<double>(c, npres, 1.0, z.p, p.p);
+            }
+            rn = red.norm<double>(npres, r.p);
+            it++;
+            if (!std::isfinite(rn)) { nan = true; break; }
+        }
+        return it;
+    }
+
+    double full_residual(const double* u, const double* p) {
+        // ||[f - K u - G p; h - G^T u]|| / ||[f; h]||
+        Level& L0 = c.levels[0];
+        level_apply<double>(c, L0, u, t2.p);
+        op_G(c, p, tu.p);
+        axpy<double>(c, nv, 1.0, tu.p, t2.p);
+        {
+            LaunchScope ls(c, -1);
+            k_sub_from<double><<<blocks_for(nv, 256), 256, 0, c.stream>>>(nv, f.p, t2.p);
+        }
+        op_GT(c, u, rhs_p.p);
+        {
+            LaunchScope ls(c, -1);
+            k_sub_from<double><<<blocks_for(npres, 256), 256, 0, c.stream>>>(npres, h.p, rhs_p.p);
+        }
+        double r2 = red.dot<double>(nv, t2.p, t2.p) + red.dot<double>(npres, rhs_p.p, rhs_p.p);
+        double b2 = red.dot<double>(nv, f.p, f.p) + red.dot<double>(npres, h.p, h.p);
+        return std::sqrt(r2 / (b2 > 0 ? b2 : 1.0));
+    }
+
+    void run();
+};
+
+template <>
+double* Bsscr::lvl_x<double>(Level& L) { return L.x64.p; }
+template <>
+float* Bsscr::lvl_x<float>(Level& L) { return L.x32.p; }
+template <>
+double* Bsscr::lvl_b<double>(Level& L) { return L.b64.p; }
+template <>
+float* Bsscr::lvl_b<float>(Level& L) { return L.b32.p; }
+template <>
+double* Bsscr::lvl_r<double>(Level& L) { return L.r64.p; }
+template <>
+float* Bsscr::lvl_r<float>(Level& L) { return L.r32.p; }
+
+__global__ void k_sum_partial(int64_t n, const double* __restrict__ x, double* __restrict__ out) {
+    double s = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) s += x[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+static void remove_constant(Context& c, int64_t n, double* x, DArray<double>& tmp) {
+    tmp.ensure(1);
+    UWG_CUDA(cudaMemsetAsync(tmp.p, 0, sizeof(double), c.stream));
+    {
+        LaunchScope ls(c, -1);
+        k_sum_partial<<<kRedBlocks, kRedThreads, 0, c.stream>>>(n, x, tmp.p);
+    }
+    {
+        LaunchScope ls(c, -1);
+        k_remove_mean<<<blocks_for(n, 256), 256, 0, c.stream>>>(n, tmp.p, x);
+    }
+}
+
+// BC lift for non-zero Dirichlet values: f_free -= K_(free,fixed) u_b, h -= G^T u_b.
+template <int DIM>
+__global__ void k_bc_lift(int64_t nnx, int64_t nny, int64_t nnz, int64_t nn, int ex, int ey, int ez, int64_t ne,
+                          const double* __restrict__ Ke, const uint8_t* __restrict__ fixed,
+                          const double* __restrict__ val, double* __restrict__ f) {
+    constexpr int NEN = 1 << DIM, ND = NEN * DIM;
+    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    int64_t idx[3] = {n % nnx, (n / nnx) % nny, DIM == 3 ? n / (nnx * nny) : 0};
+    int64_t ecount[3] = {ex, ey, ez};
+    double acc[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = 0.0;
+    for (int o = 0; o < NEN; ++o) {
+        int64_t e3[3] = {0, 0, 0};
+        bool ok = true;
+        for (int d = 0; d < DIM; ++d) {
+            e3[d] = idx[d] - ((o >> d) & 1);
+            if (e3[d] < 0 || e3[d] >= ecount[d]) ok = false;
+        }
+        if (!ok) continue;
+        int64_t e = e3[0] + (int64_t)ex * (e3[1] + (int64_t)ey * e3[2]);
+        int la = o;
+        int64_t base = e3[0] + nnx * (e3[1] + nny * e3[2]);
+        for (int b = 0; b < NEN; ++b) {
+            int64_t m = base + (b & 1) + ((b >> 1) & 1) * nnx + (DIM == 3 ? ((b >> 2) & 1) * nnx * nny : 0);
+            for (int cc = 0; cc < DIM; ++cc) {
+                if (!fixed[m * DIM + cc]) continue;
+                double v = val[m * DIM + cc];
+                if (v == 0.0) continue;
+                for (int r = 0; r < DIM; ++r) {
+                    int R = la * DIM + r, C = b * DIM + cc;
+                    int pi = R <= C ? packed_index(ND, R, C) : packed_index(ND, C, R);
+                    acc[r] -= Ke[(int64_t)pi * ne + e] * v;
+                }
+            }
+        }
+    }
+    for (int d = 0; d < DIM; ++d)
+        if (!fixed[n * DIM + d]) f[(int64_t)d * nn + n] += acc[d];
+}
+
+// node-major BC values -> SoA vector with only the fixed comps set
+template <int DIM>
+__global__ void k_bc_vector(int64_t nn, const uint8_t* __restrict__ fixed, const double* __restrict__ val,
+                            double* __restrict__ u) {
+    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    for (int d = 0; d < DIM; ++d) u[(int64_t)d * nn + n] = fixed[n * DIM + d] ? val[n * DIM + d] : 0.0;
+}
+
+void Bsscr::run() {
+    auto t0 = std::chrono::steady_clock::now();
+    dim = c.mesh.dim;
+    int levels = o.mg_levels < 1 ? 1 : o.mg_levels;
+    mixed = o.precision == UWGPU_PREC_MIXED;
+    if (!c.operator_built || c.operator_levels != levels || (mixed && !c.operator_has32))
+        build_operator(c, levels, mixed);
+    nlev = c.nlevels;
+    nv = c.mesh.nn * dim;
+    npres = c.mesh.ne;
+    int restart = o.restart > 0 ? o.restart : 30;
+    gm64.setup(nv, restart);
+    if (mixed) gm32.setup(nv, restart);
+    gms.setup(npres, restart);
+    f.ensure(nv);
+    h.ensure(npres);
+    hhat.ensure(npres);
+    tu.ensure(nv);
+    tu2.ensure(nv);
+    t2.ensure(nv);
+    Sd.ensure(npres);
+    rhs_p.ensure(npres);
+    ref_r.ensure(nv);
+    ref_d.ensure(nv);
+    if (mixed) {
+        r32.ensure(nv);
+        d32.ensure(nv);
+    }
+    c.u_sol.ensure(nv);
+    c.p_sol.ensure(npres);
+    // right-hand sides
+    gather_force(c, f.p);
+    zero<double>(c, npres, h.p);
+    DArray<double> ub;
+    if (c.has_bc && c.bc_nonzero) {
+        // BC lift (StgFEM/SLE/SystemSetup/src/StiffnessMatrix.c:900-925): f -= K_(free,fixed) u_b,
+        // and for the transposed gradient block h -= G^T u_b
+        const MeshDesc& m = c.mesh;
+        {
+            LaunchScope ls(c, -1);
+            if (dim == 3)
+                k_bc_lift<3><<<blocks_for(m.nn, 128), 128, 0, c.stream>>>(m.nnx, m.nny, m.nnz, m.nn, m.nel[0], m.nel[1],
+                                                                          m.nel[2], m.ne, c.levels[0].Ke.p, c.fixed.p,
+                                                                          c.bcval.p, f.p);
+            else
+                k_bc_lift<2><<<blocks_for(m.nn, 128), 128, 0, c.stream>>>(m.nnx, m.nny, m.nnz, m.nn, m.nel[0], m.nel[1], 1,
+                                                                          m.ne, c.levels[0].Ke.p, c.fixed.p, c.bcval.p, f.p);
+        }
+        check_launch("k_bc_lift");
+        ub.ensure(nv);
+        {
+            LaunchScope ls(c, -1);
+            if (dim == 3)
+                k_bc_vector<3><<<blocks_for(m.nn, 256), 256, 0, c.stream>>>(m.nn, c.fixed.p, c.bcval.p, ub.p);
+            else
+                k_bc_vector<2><<<blocks_for(m.nn, 256), 256, 0, c.stream>>>(m.nn, c.fixed.p, c.bcval.p, ub.p);
+        }
+        op_GT_unmasked(c, ub.p, h.p);
+        scale<double>(c, npres, -1.0, h.p, h.p);
+    }
+    // Schur preconditioner diagonal
+    if (o.schur_pc == UWGPU_SCHUR_PC_UW) copy<double>(c, npres, c.Se.p, Sd.p);
+    else if (o.schur_pc == UWGPU_SCHUR_PC_GKGDIAG) gkgdiag(c, Sd.p);
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+    auto t1 = std::chrono::steady_clock::now();
+    rep.t_setup_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+
+    // h_hat = h - G^T K^{-1} f
+    a11(f.p, tu2.p, o.a11_rtol);
+    op_GT(c, tu2.p, hhat.p);
+    scale<double>(c, npres, -1.0, hhat.p, hhat.p);
+    axpy<double>(c, npres, 1.0, h.p, hhat.p);
+    // solve (G^T K^{-1} G) p = -h_hat
+    scale<double>(c, npres, -1.0, hhat.p, rhs_p.p);
+    DArray<double> tmp;
+    if (o.remove_const_p) remove_constant(c, npres, rhs_p.p, tmp);
+    int maxo = o.max_outer > 0 ? o.max_outer : 500;
+    int outer = 0;
+    bool outer_fail = false;
+    if (o.schur_type == UWGPU_SCHUR_CG) {
+        outer = schur_cg(rhs_p.p, c.p_sol.p, o.scr_rtol, maxo);
+    } else {
+        double res = 0, bn = 0;
+        bool nn = false;
+        outer = gms.solve([&](const double* in, double* out) { schur_apply(in, out); },
+                          [&](const double* in, double* out) { schur_pc(in, out); }, rhs_p.p, c.p_sol.p, o.scr_rtol,
+                          maxo, &res, &bn, &nn);
+        if (nn) nan = true;
+        if (bn > 0 && res > o.scr_rtol * bn * 1.0000001) outer_fail = true;
+    }
+    if (o.remove_const_p) remove_constant(c, npres, c.p_sol.p, tmp);
+    // back-solve u = K^{-1} (f - G p)
+    op_G(c, c.p_sol.p, t2.p);
+    scale<double>(c, nv, -1.0, t2.p, t2.p);
+    axpy<double>(c, nv, 1.0, f.p, t2.p);
+    int before = rep.inner_its_total;
+    a11(t2.p, c.u_sol.p, o.back_rtol);
+    rep.backsolve_its = rep.inner_its_total - before;
+    if (c.has_bc && c.bc_nonzero) axpy<double>(c, nv, 1.0, ub.p, c.u_sol.p);
+    rep.outer_its = outer;
+    rep.rel_residual = full_residual(c.u_sol.p, c.p_sol.p);
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+    auto t2c = std::chrono::steady_clock::now();
+    rep.t_solve_ms = std::chrono::duration<double, std::milli>(t2c - t1).count();
+    c.has_solution = true;
+    rep.converged = !(nan || outer_fail || inner_fail) ? 1 : 0;
+    if (nan || !std::isfinite(rep.rel_residual)) rep.status = UWGPU_ERR_NAN;
+    else if (outer_fail) rep.status = UWGPU_ERR_NOT_CONVERGED;
+    else rep.status = UWGPU_OK;
+    if (o.target_rel_residual > 0 && rep.rel_residual > o.target_rel_residual && rep.status == UWGPU_OK)
+        rep.status = UWGPU_ERR_NOT_CONVERGED;
+}
+
+void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
+    UWG_REQUIRE(c.assembled, UWGPU_ERR_STATE, "solve requested before assembly");
+    UWG_REQUIRE(o.precision == UWGPU_PREC_FP64 || o.precision == UWGPU_PREC_MIXED, UWGPU_ERR_ARGUMENT, "bad precision");
+    UWG_REQUIRE(o.schur_type == UWGPU_SCHUR_CG || o.schur_type == UWGPU_SCHUR_FGMRES, UWGPU_ERR_ARGUMENT, "bad Schur type");
+    UWG_REQUIRE(o.schur_pc >= 0 && o.schur_pc <= 2, UWGPU_ERR_ARGUMENT, "bad Schur preconditioner");
+    Bsscr s(c, o, rep);
+    s.run();
+}
+
+}  // namespace uwg

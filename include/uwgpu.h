@@ -1,0 +1,205 @@
+/*
+ * uwgpu.h -- C ABI of the GB300 particle-in-cell Stokes library (libuwgpu.so).
+ *
+ * The library replaces the hot path of an Underworld 1.x Stokes solve:
+ *   material point -> element binning and the integration-point mapper,
+ *   per-point rheology and Q1 element assembly (K_e, f_e, G_e, approxS_e),
+ *   the velocity-block operator and the geometric multigrid inside the BSSCR
+ *   Schur-complement solver.
+ * Host code (a StGermain component, or any C/C++/Python caller) owns its data in host
+ * memory and passes plain pointers; the library copies what it needs into device memory it
+ * owns.  Every entry point returns an int status (UWGPU_OK on success) and records a message
+ * readable with uwgpu_last_error().  A context is bound to one device and one CUDA stream;
+ * calls on one context must not be made from several threads at once.
+ *
+ * Each declaration names the reference interface it stands in for (paths are relative to
+ * the Underworld 1.x source tree).
+ */
+#ifndef UWGPU_H
+#define UWGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UWGPU_ABI_VERSION 1
+
+/* Status codes. */
+enum {
+    UWGPU_OK = 0,
+    UWGPU_ERR_ARGUMENT = 1,      /* bad argument (NULL pointer, size, index)                 */
+    UWGPU_ERR_CUDA = 2,          /* a CUDA runtime call failed                               */
+    UWGPU_ERR_MEMORY = 3,        /* device allocation failed                                 */
+    UWGPU_ERR_STATE = 4,         /* call out of order (e.g. assemble before binning)         */
+    UWGPU_ERR_DOMAIN = 5,        /* material points outside the mesh                         */
+    UWGPU_ERR_NOT_CONVERGED = 6, /* a Krylov solve hit its iteration limit                   */
+    UWGPU_ERR_NAN = 7,           /* NaN/Inf detected in a residual                           */
+    UWGPU_ERR_UNSUPPORTED = 8,   /* rheology law or option not provided by this library      */
+    UWGPU_ERR_BREAKDOWN = 9      /* Krylov breakdown (zero pivot / non-SPD coarse operator)  */
+};
+
+/* Rheology laws (one entry of a RheologyMaterial's rheology list, applied in order). */
+enum {
+    UWGPU_LAW_MATERIAL_VISCOSITY = 1, /* Underworld/Rheology/src/MaterialViscosity.c:119   p0=eta0 */
+    UWGPU_LAW_ARRHENIUS = 2,          /* Underworld/Rheology/src/Arrhenius.c:156          p0=eta0 p1=activationEnergy p2=activationVolume p3=referenceTemperature */
+    UWGPU_LAW_FRANK_KAMENETSKII = 3,  /* Underworld/Rheology/src/FrankKamenetskii.c:134   p0=eta0 p1=theta */
+    UWGPU_LAW_VISCOSITY_LIMITER = 4,  /* Underworld/Rheology/src/ViscosityLimiter.c:106   p0=maxViscosity p1=minViscosity */
+    UWGPU_LAW_DRUCKER_PRAGER = 5,     /* Underworld/Rheology/src/DruckerPrager.c:236 via YieldRheology.c:198, VonMises.c:232
+                                         p0=cohesion p1=frictionCoefficient p2=minimumYieldStress p3=minimumViscosity */
+    UWGPU_LAW_PARTICLE_VISCOSITY = 6  /* eta taken from the per-point viscosity array passed to uwgpu_particles_upload */
+};
+
+typedef struct {
+    int32_t law;
+    int32_t pad;
+    double p[6];
+} uwgpu_law;
+
+/* One RheologyMaterial (Underworld/Rheology/src/RheologyMaterial.c:240-270) plus the
+ * BuoyancyForceTerm material extension (PICellerator/Utils/src/BuoyancyForceTerm.c:217-221). */
+typedef struct {
+    int32_t n_laws;     /* 1..4 */
+    int32_t pad;
+    uwgpu_law laws[4];
+    double density;
+    double alpha;
+    double ref_temp;
+} uwgpu_material;
+
+/* Solver options: the PETSc options the BSSCR driver reads
+ * (Solvers/KSPSolvers/src/BSSCR/auglag-driver-DGTGD.c, mg.c; StgFEM PETScMGSolver.c). */
+enum { UWGPU_PREC_FP64 = 0, UWGPU_PREC_MIXED = 1 };
+enum { UWGPU_SCHUR_CG = 0, UWGPU_SCHUR_FGMRES = 1 };
+enum { UWGPU_SCHUR_PC_UW = 0, UWGPU_SCHUR_PC_GKGDIAG = 1, UWGPU_SCHUR_PC_NONE = 2 };
+
+typedef struct {
+    int32_t mg_levels;        /* mgLevels: levels including the fine one (>= 2)          */
+    int32_t smooth_down;      /* downIterations: symmetric colour sweeps before restrict  */
+    int32_t smooth_up;        /* upIterations                                            */
+    int32_t schur_type;       /* -scr_ksp_type: UWGPU_SCHUR_CG or UWGPU_SCHUR_FGMRES      */
+    int32_t schur_pc;         /* -Q22_pc_type: uw (approxS), gkgdiag, none               */
+    int32_t restart;          /* FGMRES restart length (PETSc default 30)                */
+    int32_t max_outer;        /* -scr_ksp_max_it                                         */
+    int32_t max_inner;        /* -A11_ksp_max_it (per velocity solve)                    */
+    double scr_rtol;          /* -scr_ksp_rtol                                           */
+    double a11_rtol;          /* -A11_ksp_rtol                                           */
+    double back_rtol;         /* -backsolveA11_ksp_rtol                                  */
+    int32_t remove_const_p;   /* -remove_constant_pressure_null_space                    */
+    int32_t precision;        /* UWGPU_PREC_FP64 or UWGPU_PREC_MIXED                     */
+    double target_rel_residual; /* > 0: stop the outer solve once the full Stokes residual
+                                   ||[f-Ku-Gp; h-G^T u]|| / ||[f;h]|| is below this value */
+} uwgpu_solve_opts;
+
+typedef struct {
+    int32_t outer_its;        /* Schur (pressure) iterations                             */
+    int32_t inner_its_total;  /* velocity (A11) Krylov iterations, all solves            */
+    int32_t backsolve_its;    /* iterations of the final velocity back-solve             */
+    int32_t vcycles;          /* multigrid V-cycles applied                              */
+    int32_t converged;
+    int32_t status;
+    double rel_residual;      /* ||[f-Ku-Gp; h-G^T u]|| / ||[f;h]|| of the returned u, p  */
+    double t_setup_ms;        /* stencil build + multigrid hierarchy                     */
+    double t_solve_ms;
+} uwgpu_report;
+
+typedef struct uwgpu_ctx uwgpu_ctx;
+
+/* Lifetime ------------------------------------------------------------------------------ */
+int uwgpu_abi_version(void);
+/* Creates a context on `device` with its own stream. */
+int uwgpu_create(int32_t device, uwgpu_ctx** out);
+void uwgpu_destroy(uwgpu_ctx* ctx);
+const char* uwgpu_last_error(const uwgpu_ctx* ctx);
+int uwgpu_synchronize(uwgpu_ctx* ctx);
+
+/* Mesh: regular Cartesian Q1 mesh of CartesianGenerator (StgDomain/Mesh/src/CartesianGenerator.c
+ * :976-1035 incidence, :2275-2310 coordinates) with a P0 pressure mesh. */
+int uwgpu_mesh_q1(uwgpu_ctx* ctx, int32_t dim, const int32_t nel[3], const double min[3],
+                  const double max[3]);
+
+/* Velocity boundary conditions: fixed[n*dim+d] != 0 fixes dof d of node n to values[n*dim+d]
+ * (values may be NULL for homogeneous conditions).  Replaces the WallVC/CompositeVC lookup
+ * the equation numbering uses (StgFEM/Discretisation/src/FeEquationNumber.c:700-760). */
+int uwgpu_bc_set(uwgpu_ctx* ctx, const uint8_t* fixed, const double* values);
+
+/* Materials: device-side descriptors of the Materials_Register walk the constitutive matrix
+ * does at build time (Underworld/Rheology/src/ConstitutiveMatrix.c:214-243). */
+int uwgpu_materials_set(uwgpu_ctx* ctx, int32_t n, const uwgpu_material* mats);
+
+/* Fields the rheology and force terms read (Ppc lookups, PICellerator/Common/src/PpcManager.c:503):
+ * nodal temperature (may be NULL), gravity magnitude, vertical axis (BuoyancyForceTerm
+ * VerticalAxis).  Velocity and pressure for strain-rate and pressure dependent laws are the
+ * context's last solution (see uwgpu_solution_set). */
+int uwgpu_fields_set(uwgpu_ctx* ctx, const double* nodal_temperature, double gravity,
+                     int32_t vert_axis);
+/* Sets the current solution (nodal velocity nnode*dim, element pressure) used by
+ * strain-rate / pressure dependent rheologies; marks a previous solution as present
+ * (ConstitutiveMatrix previousSolutionExists, Underworld/Rheology/src/YieldRheology.c:210). */
+int uwgpu_solution_set(uwgpu_ctx* ctx, const double* u_nodal, const double* p);
+
+/* Material points: coordinates as three arrays (x, y, z; z ignored in 2D), material index per
+ * point, optional per-point viscosity and density (NULL if unused).  Copied to the device.
+ * Stands in for the MaterialPointsSwarm particle array (PICellerator/MaterialPoints). */
+int uwgpu_particles_upload(uwgpu_ctx* ctx, int64_t n, const double* x, const double* y,
+                           const double* z, const int32_t* material, const double* eta,
+                           const double* rho);
+
+/* Binning + integration-point mapping: _CoincidentMapper_Map
+ * (PICellerator/MaterialPoints/src/CoincidentMapper.c:150-253) with the regular-mesh element
+ * search (StgDomain/Mesh/src/Mesh_RegularAlgorithms.c:194-226), the cell-table append order of
+ * Swarm_AddParticleToCell (StgDomain/Swarm/src/SwarmClass.c:1155-1184) and ConstantWeights
+ * (PICellerator/Weights/src/ConstantWeights.c:180-189).  Optional host outputs: perm (n: point
+ * index of each integration slot, element by element, ascending within an element), offsets
+ * (nel+1) and xi (3 per slot).  Returns UWGPU_ERR_DOMAIN if points lie outside the mesh. */
+int uwgpu_bin_and_map(uwgpu_ctx* ctx, uint32_t* perm, uint32_t* offsets, double* xi);
+
+/* Element assembly of every element: replaces the StiffnessMatrix assemble entry point
+ * (StgFEM/SLE/SystemSetup/src/StiffnessMatrix.c:799-1017) for the terms
+ * ConstitutiveMatrixCartesian (Underworld/Rheology/src/ConstitutiveMatrixCartesian.c:202-412),
+ * BuoyancyForceTerm (PICellerator/Utils/src/BuoyancyForceTerm.c:310-452),
+ * GradientStiffnessMatrixTerm (StgFEM/Assembly/src/GradientStiffnessMatrixTerm.c:160-250) and
+ * UzawaPreconditionerTerm (StgFEM/SLE/ProvidedSystems/StokesFlow/src/UzawaPreconditionerTerm.c:155-238).
+ * Results stay on the device. */
+int uwgpu_assemble(uwgpu_ctx* ctx);
+
+/* Per-element results of the last assembly, copied to the host: the per-element callback
+ * StiffnessMatrixTerm_AssembleElementFunction (StgFEM/SLE/SystemSetup/src/StiffnessMatrixTerm.c
+ * :247-266) reads element e from here.  Ke: count*(nd*nd) row-major, dof = node*dim + comp;
+ * fe, Ge: count*nd; Se: count.  Any output may be NULL. */
+int uwgpu_get_element_matrices(uwgpu_ctx* ctx, int64_t first, int64_t count, double* Ke,
+                               double* fe, double* Ge, double* Se);
+/* Viscosity evaluated at every integration slot by the last assembly (n, slot order). */
+int uwgpu_get_point_viscosity(uwgpu_ctx* ctx, double* eta);
+
+/* Velocity-block operator y = K x on nodal vectors (nnode*dim, fixed dofs act as identity):
+ * the MatMult of the assembled K the BSSCR solver applies (PETSc MatMult on the k_matrix).
+ * precision: UWGPU_PREC_FP64 or UWGPU_PREC_MIXED (FP32 operator).  Builds the operator if
+ * needed. */
+int uwgpu_operator_apply(uwgpu_ctx* ctx, int32_t precision, const double* x, double* y);
+
+/* Stokes solve by Schur-complement reduction: KSPSolve_BSSCR
+ * (Solvers/KSPSolvers/src/BSSCR/BSSCR.c:151-229, auglag-driver-DGTGD.c:53-441) invoked through
+ * the SLE_Solver interface (StgFEM/SLE/SystemSetup/src/SLE_Solver.c:226-257,
+ * Solvers/KSPSolvers/src/StokesBlockKSPInterface.c:211-328).  u (nnode*dim) and p (nel) are
+ * host outputs (either may be NULL to leave the result on the device). */
+int uwgpu_solve_bsscr(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, double* u, double* p,
+                      uwgpu_report* report);
+
+/* Default options (mg_levels 4, 2+2 sweeps, FGMRES Schur with the uw preconditioner). */
+void uwgpu_solve_opts_default(uwgpu_solve_opts* opts);
+
+/* Kernel timing: when enabled, launches of the kernel family `which` are bracketed by CUDA
+ * events on the context stream and summed (count, milliseconds). */
+enum { UWGPU_KERNEL_ASSEMBLY = 0, UWGPU_KERNEL_APPLY = 1, UWGPU_KERNEL_SMOOTH = 2,
+       UWGPU_KERNEL_BINNING = 3, UWGPU_KERNEL_COUNT = 4 };
+int uwgpu_profile_enable(uwgpu_ctx* ctx, int32_t on);
+int uwgpu_profile_read(uwgpu_ctx* ctx, int32_t which, int64_t* launches, double* ms);
+/* Number of library kernel launches issued since the context was created. */
+int64_t uwgpu_launch_count(const uwgpu_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UWGPU_H */

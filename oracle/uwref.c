@@ -1,0 +1,1454 @@
+/*
+ * uwref.c -- CPU restatement of the Underworld 1.x particle-in-cell Stokes hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the oracle the parity tests, the smoke check and the CPU
+ * baseline of bench.py run.  The GPU library never links or calls this file.
+ *
+ * Each function names the reference routine it restates (paths relative to the
+ * Underworld 1.x tree).  Loop orders and floating-point expressions follow those routines
+ * so that results agree to rounding; where a PETSc routine is used by the reference
+ * (SOR, FGMRES, CG, MatPtAP, LU) the published algorithm is restated.
+ */
+#define _POSIX_C_SOURCE 200809L
+#include "uwref.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* StGermain/Base/Foundation/src/Numerics.c:37-41 */
+static const double kNumEpsilon = 1e-12;
+static int num_approx(double var, double val) {
+    return var >= val - kNumEpsilon && var <= val + kNumEpsilon;
+}
+
+static double now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+static void set_threads(int32_t n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Mesh                                                                                 */
+/* ------------------------------------------------------------------------------------ */
+
+int64_t uwr_num_nodes(const uwr_mesh* m) {
+    int64_t n = 1;
+    for (int d = 0; d < m->dim; ++d) n *= (m->nel[d] + 1);
+    return n;
+}
+
+int64_t uwr_num_elements(const uwr_mesh* m) {
+    int64_t n = 1;
+    for (int d = 0; d < m->dim; ++d) n *= m->nel[d];
+    return n;
+}
+
+/* StgDomain/Mesh/src/CartesianGenerator.c:2275-2310 (CartesianGenerator_CalcGeom, no contact
+ * depth): first node at crdMin, last at crdMax, interior min + (i/(n-1))*(max-min). */
+static double node_coord_1d(const uwr_mesh* m, int d, int64_t i) {
+    int64_t sizes = m->nel[d] + 1;
+    if (i <= 0) return m->min[d];
+    if (i >= sizes - 1) return m->max[d];
+    return m->min[d] + ((double)i / (double)(sizes - 1)) * (m->max[d] - m->min[d]);
+}
+
+void uwr_node_coords(const uwr_mesh* m, double* xyz) {
+    int64_t nx = m->nel[0] + 1, ny = m->nel[1] + 1, nz = (m->dim == 3) ? m->nel[2] + 1 : 1;
+    for (int64_t k = 0; k < nz; ++k)
+        for (int64_t j = 0; j < ny; ++j)
+            for (int64_t i = 0; i < nx; ++i) {
+                int64_t n = i + nx * (j + ny * k);
+                xyz[3 * n + 0] = node_coord_1d(m, 0, i);
+                xyz[3 * n + 1] = node_coord_1d(m, 1, j);
+                xyz[3 * n + 2] = (m->dim == 3) ? node_coord_1d(m, 2, k) : 0.0;
+            }
+}
+
+/* StgDomain/Mesh/src/CartesianGenerator.c:976-1035 (element-vertex incidence) with
+ * Grid_Project (StgDomain/Mesh/src/Grid.c:257-275, basis = x fastest). */
+void uwr_element_nodes(const uwr_mesh* m, int64_t e, int64_t* inc) {
+    int64_t ex = m->nel[0], ey = m->nel[1];
+    int64_t i = e % ex, j = (e / ex) % ey, k = (m->dim == 3) ? e / (ex * ey) : 0;
+    int64_t nx = ex + 1, ny = ey + 1;
+    int64_t base = i + nx * (j + ny * k);
+    inc[0] = base;
+    inc[1] = base + 1;
+    inc[2] = base + nx;
+    inc[3] = base + nx + 1;
+    if (m->dim == 3) {
+        int64_t s = nx * ny;
+        inc[4] = base + s;
+        inc[5] = base + s + 1;
+        inc[6] = base + s + nx;
+        inc[7] = base + s + nx + 1;
+    }
+}
+
+static void element_node_xyz(const uwr_mesh* m, int64_t e, double xyz[8][3]) {
+    int64_t inc[8];
+    int64_t nx = m->nel[0] + 1, ny = m->nel[1] + 1;
+    int nen = (m->dim == 3) ? 8 : 4;
+    uwr_element_nodes(m, e, inc);
+    for (int a = 0; a < nen; ++a) {
+        int64_t n = inc[a];
+        int64_t i = n % nx, j = (n / nx) % ny, k = n / (nx * ny);
+        xyz[a][0] = node_coord_1d(m, 0, i);
+        xyz[a][1] = node_coord_1d(m, 1, j);
+        xyz[a][2] = (m->dim == 3) ? node_coord_1d(m, 2, k) : 0.0;
+    }
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Inputs                                                                               */
+/* ------------------------------------------------------------------------------------ */
+
+/* StgDomain/Swarm/src/Random.c:43-73 (Park-Miller minimal standard, Schrage's method). */
+typedef struct { long state; } pm_rng;
+static void pm_seed(pm_rng* r, long seed) { r->state = seed ^ 123459876L; }
+static double pm_random(pm_rng* r) {
+    const long q = 127773, rr = 2836, a = 16807, mx = 2147483647L;
+    long tmp = r->state / q;
+    r->state = a * (r->state - tmp * q) - rr * tmp;
+    if (r->state < 0) r->state += mx;
+    return (double)r->state;
+}
+static double pm_random_minmax(pm_rng* r, double mn, double mx) {
+    return (mx - mn) * pm_random(r) / (double)2147483647L + mn;
+}
+
+/* StgDomain/Swarm/src/RandomParticleLayout.c:194-213: per cell, per point, three draws
+ * (x, y, z) in the cell's bounding box. */
+void uwr_random_layout(const uwr_mesh* m, int32_t ppc, uint32_t seed, double* xyz) {
+    pm_rng r;
+    pm_seed(&r, (long)seed);
+    int64_t E = uwr_num_elements(m);
+    for (int64_t e = 0; e < E; ++e) {
+        double nodes[8][3];
+        element_node_xyz(m, e, nodes);
+        int nen = (m->dim == 3) ? 8 : 4;
+        double mn[3] = {nodes[0][0], nodes[0][1], nodes[0][2]};
+        double mx[3] = {nodes[nen - 1][0], nodes[nen - 1][1], nodes[nen - 1][2]};
+        if (m->dim == 2) { mn[2] = 0.0; mx[2] = 0.0; }
+        for (int32_t c = 0; c < ppc; ++c) {
+            double* x = xyz + 3 * (e * ppc + c);
+            for (int d = 0; d < 3; ++d) x[d] = pm_random_minmax(&r, mn[d], mx[d]);
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Binning                                                                              */
+/* ------------------------------------------------------------------------------------ */
+
+/* StgDomain/Mesh/src/Mesh_RegularAlgorithms.c:154-175 (sep) and :194-226 (search). */
+int uwr_search_element(const uwr_mesh* m, const double* pt, uint32_t* el) {
+    unsigned inds[3] = {0, 0, 0};
+    for (int d = 0; d < m->dim; ++d) {
+        double sep = (m->max[d] - m->min[d]) / m->nel[d];
+        if (num_approx(pt[d] - m->max[d], 0.0)) {
+            inds[d] = (unsigned)(m->nel[d] - 1);
+        } else if (pt[d] < m->min[d] || pt[d] > m->max[d]) {
+            return 0;
+        } else {
+            double integer;
+            double out = (pt[d] - m->min[d]) / sep;
+            double frac = modf(out, &integer);
+            inds[d] = (unsigned)integer;
+            if (inds[d] > 0 && num_approx(frac, 0.0)) inds[d]--;
+        }
+    }
+    *el = inds[0] + (unsigned)m->nel[0] * (inds[1] + (unsigned)m->nel[1] * inds[2]);
+    return 1;
+}
+
+/* PICellerator/MaterialPoints/src/CoincidentMapper.c:176-242 with
+ * StgDomain/Swarm/src/SwarmClass.c:1155-1184 (append => ascending point order per cell),
+ * StgFEM/Discretisation/src/ElementType.c:227-350 for xi. */
+int64_t uwr_map(const uwr_mesh* m, int64_t n, const double* xyz, uint32_t* owning,
+                uint32_t* offsets, uint32_t* perm, double* xi, int32_t use_newton) {
+    int64_t E = uwr_num_elements(m);
+    int64_t outside = 0;
+    uint32_t* count = (uint32_t*)calloc((size_t)E, sizeof(uint32_t));
+    for (int64_t p = 0; p < n; ++p) {
+        uint32_t el;
+        if (uwr_search_element(m, xyz + 3 * p, &el)) {
+            owning[p] = el;
+            count[el]++;
+        } else {
+            owning[p] = 0xffffffffu;
+            outside++;
+        }
+    }
+    offsets[0] = 0;
+    for (int64_t e = 0; e < E; ++e) offsets[e + 1] = offsets[e] + count[e];
+    memset(count, 0, (size_t)E * sizeof(uint32_t));
+    for (int64_t p = 0; p < n; ++p) {
+        uint32_t el = owning[p];
+        if (el == 0xffffffffu) continue;
+        perm[offsets[el] + count[el]++] = (uint32_t)p;
+    }
+    free(count);
+    if (xi) {
+        int64_t total = offsets[E];
+#pragma omp parallel for schedule(static)
+        for (int64_t s = 0; s < total; ++s) {
+            /* element of slot s: binary search in offsets */
+            int64_t lo = 0, hi = E;
+            while (hi - lo > 1) {
+                int64_t mid = (lo + hi) / 2;
+                if (offsets[mid] <= (uint32_t)s) lo = mid; else hi = mid;
+            }
+            const double* x = xyz + 3 * (int64_t)perm[s];
+            if (use_newton) {
+                uwr_global_to_local(m, lo, x, xi + 3 * s);
+            } else {
+                double nodes[8][3];
+                element_node_xyz(m, lo, nodes);
+                int nen = (m->dim == 3) ? 8 : 4;
+                for (int d = 0; d < 3; ++d) {
+                    if (d < m->dim) {
+                        double h = nodes[nen - 1][d] - nodes[0][d];
+                        xi[3 * s + d] = (2.0 * (x[d] - nodes[0][d]) - h) / h;
+                    } else {
+                        xi[3 * s + d] = 0.0;
+                    }
+                }
+            }
+        }
+    }
+    return outside;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Shape functions                                                                      */
+/* ------------------------------------------------------------------------------------ */
+
+/* StgFEM/Discretisation/src/BilinearElementType.c:212-244 and TrilinearElementType.c:249-306 */
+void uwr_shape(int dim, const double* xi, double* N) {
+    if (dim == 2) {
+        double x = xi[0], y = xi[1];
+        N[0] = 0.25 * (1.0 - x) * (1.0 - y);
+        N[1] = 0.25 * (1.0 + x) * (1.0 - y);
+        N[2] = 0.25 * (1.0 - x) * (1.0 + y);
+        N[3] = 0.25 * (1.0 + x) * (1.0 + y);
+    } else {
+        double x = xi[0], y = xi[1], z = xi[2];
+        N[0] = 0.125 * (1.0 - x) * (1.0 - y) * (1.0 - z);
+        N[2] = 0.125 * (1.0 - x) * (1.0 + y) * (1.0 - z);
+        N[3] = 0.125 * (1.0 + x) * (1.0 + y) * (1.0 - z);
+        N[1] = 0.125 * (1.0 + x) * (1.0 - y) * (1.0 - z);
+        N[4] = 0.125 * (1.0 - x) * (1.0 - y) * (1.0 + z);
+        N[6] = 0.125 * (1.0 - x) * (1.0 + y) * (1.0 + z);
+        N[7] = 0.125 * (1.0 + x) * (1.0 + y) * (1.0 + z);
+        N[5] = 0.125 * (1.0 + x) * (1.0 - y) * (1.0 + z);
+    }
+}
+
+void uwr_shape_local_derivs(int dim, const double* xi, double* G) {
+    if (dim == 2) {
+        double x = xi[0], y = xi[1];
+        double* g0 = G;
+        double* g1 = G + 4;
+        g0[0] = -0.25 * (1.0 - y);
+        g0[1] = 0.25 * (1.0 - y);
+        g0[3] = 0.25 * (1.0 + y);
+        g0[2] = -0.25 * (1.0 + y);
+        g1[0] = -0.25 * (1.0 - x);
+        g1[1] = -0.25 * (1.0 + x);
+        g1[3] = 0.25 * (1.0 + x);
+        g1[2] = 0.25 * (1.0 - x);
+    } else {
+        double x = xi[0], y = xi[1], z = xi[2];
+        double* g0 = G;
+        double* g1 = G + 8;
+        double* g2 = G + 16;
+        g0[0] = -0.125 * (1.0 - y) * (1.0 - z);
+        g0[2] = -0.125 * (1.0 + y) * (1.0 - z);
+        g0[3] = 0.125 * (1.0 + y) * (1.0 - z);
+        g0[1] = 0.125 * (1.0 - y) * (1.0 - z);
+        g0[4] = -0.125 * (1.0 - y) * (1.0 + z);
+        g0[6] = -0.125 * (1.0 + y) * (1.0 + z);
+        g0[7] = 0.125 * (1.0 + y) * (1.0 + z);
+        g0[5] = 0.125 * (1.0 - y) * (1.0 + z);
+        g1[0] = -0.125 * (1.0 - x) * (1.0 - z);
+        g1[2] = 0.125 * (1.0 - x) * (1.0 - z);
+        g1[3] = 0.125 * (1.0 + x) * (1.0 - z);
+        g1[1] = -0.125 * (1.0 + x) * (1.0 - z);
+        g1[4] = -0.125 * (1.0 - x) * (1.0 + z);
+        g1[6] = 0.125 * (1.0 - x) * (1.0 + z);
+        g1[7] = 0.125 * (1.0 + x) * (1.0 + z);
+        g1[5] = -0.125 * (1.0 + x) * (1.0 + z);
+        g2[0] = -0.125 * (1.0 - x) * (1.0 - y);
+        g2[2] = -0.125 * (1.0 - x) * (1.0 + y);
+        g2[3] = -0.125 * (1.0 + x) * (1.0 + y);
+        g2[1] = -0.125 * (1.0 + x) * (1.0 - y);
+        g2[4] = 0.125 * (1.0 - x) * (1.0 - y);
+        g2[6] = 0.125 * (1.0 - x) * (1.0 + y);
+        g2[7] = 0.125 * (1.0 + x) * (1.0 + y);
+        g2[5] = 0.125 * (1.0 + x) * (1.0 - y);
+    }
+}
+
+/* StgDomain/Geometry/src/TensorMath.c:980-1043 (Cramer's rule; FT3D_ij = row-major). */
+static void tensor_solve(const double* A, double* s, const double* b, int dim) {
+    if (dim == 3) {
+        double det = +A[0] * (A[4] * A[8] - A[7] * A[5])
+                     - A[1] * (A[3] * A[8] - A[5] * A[6])
+                     + A[2] * (A[3] * A[7] - A[4] * A[6]);
+        s[0] = (b[0] * (A[4] * A[8] - A[7] * A[5])
+                - A[1] * (b[1] * A[8] - A[5] * b[2])
+                + A[2] * (b[1] * A[7] - A[4] * b[2])) / det;
+        s[1] = (A[0] * (b[1] * A[8] - b[2] * A[5])
+                - b[0] * (A[3] * A[8] - A[5] * A[6])
+                + A[2] * (A[3] * b[2] - b[1] * A[6])) / det;
+        s[2] = (A[0] * (A[4] * b[2] - A[7] * b[1])
+                - A[1] * (A[3] * b[2] - b[1] * A[6])
+                + b[0] * (A[3] * A[7] - A[4] * A[6])) / det;
+    } else {
+        double det = A[0] * A[3] - A[2] * A[1];
+        s[0] = (b[0] * A[3] - A[1] * b[1]) / det;
+        s[1] = (b[1] * A[0] - A[2] * b[0]) / det;
+    }
+}
+
+/* StgFEM/Discretisation/src/ElementType.c:227-350 (Newton-Raphson global -> local). */
+void uwr_global_to_local(const uwr_mesh* m, int64_t e, const double* x, double* xi) {
+    int dim = m->dim, nen = (dim == 3) ? 8 : 4;
+    double nodes[8][3], N[8], G[24];
+    element_node_xyz(m, e, nodes);
+    memset(xi, 0, sizeof(double) * dim);
+    for (int it = 0; it < 100; ++it) {
+        double J[9] = {0}, rhs[3] = {0}, inc[3] = {0};
+        uwr_shape(dim, xi, N);
+        uwr_shape_local_derivs(dim, xi, G);
+        for (int a = 0; a < nen; ++a) {
+            double sf = N[a];
+            const double* c = nodes[a];
+            J[0 * dim + 0] += G[0 * nen + a] * c[0];
+            J[0 * dim + 1] += G[1 * nen + a] * c[0];
+            J[1 * dim + 0] += G[0 * nen + a] * c[1];
+            J[1 * dim + 1] += G[1 * nen + a] * c[1];
+            rhs[0] -= sf * c[0];
+            rhs[1] -= sf * c[1];
+            if (dim == 3) {
+                J[0 * 3 + 2] += G[2 * nen + a] * c[0];
+                J[1 * 3 + 2] += G[2 * nen + a] * c[1];
+                J[2 * 3 + 0] += G[0 * nen + a] * c[2];
+                J[2 * 3 + 1] += G[1 * nen + a] * c[2];
+                J[2 * 3 + 2] += G[2 * nen + a] * c[2];
+                rhs[2] -= sf * c[2];
+            }
+        }
+        rhs[0] += x[0];
+        rhs[1] += x[1];
+        if (dim == 3) rhs[2] += x[2];
+        tensor_solve(J, inc, rhs, dim);
+        xi[0] += inc[0];
+        xi[1] += inc[1];
+        if (dim == 3) xi[2] += inc[2];
+        double mr = fabs(inc[0]);
+        if (mr < fabs(inc[1])) mr = fabs(inc[1]);
+        if (dim == 3 && mr < fabs(inc[2])) mr = fabs(inc[2]);
+        if (mr < 0.0001) return;
+    }
+    xi[0] = 1.1;
+}
+
+/* StgFEM/Discretisation/src/ElementType.c:354-495 (ElementType_ShapeFunctionsGlobalDerivs). */
+static void global_derivs_nodes(int dim, double nodes[8][3], const double* xi, double* detJ, double* GNx) {
+    int nen = (dim == 3) ? 8 : 4;
+    double G[24], jac[3][3], cof[3][3], D = 0.0;
+    uwr_shape_local_derivs(dim, xi, G);
+    if (dim == 2) {
+        jac[0][0] = jac[0][1] = jac[1][0] = jac[1][1] = 0.0;
+        for (int n = 0; n < nen; ++n) {
+            jac[0][0] = jac[0][0] + G[0 * nen + n] * nodes[n][0];
+            jac[0][1] = jac[0][1] + G[0 * nen + n] * nodes[n][1];
+            jac[1][0] = jac[1][0] + G[1 * nen + n] * nodes[n][0];
+            jac[1][1] = jac[1][1] + G[1 * nen + n] * nodes[n][1];
+        }
+        D = jac[0][0] * jac[1][1] - jac[0][1] * jac[1][0];
+        double tmp = jac[0][0];
+        jac[0][0] = jac[1][1] / D;
+        jac[1][1] = tmp / D;
+        jac[0][1] = -jac[0][1] / D;
+        jac[1][0] = -jac[1][0] / D;
+    } else {
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) jac[i][j] = 0.0;
+        for (int n = 0; n < nen; ++n)
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) jac[i][j] = jac[i][j] + G[i * nen + n] * nodes[n][j];
+        D = jac[0][0] * (jac[1][1] * jac[2][2] - jac[1][2] * jac[2][1])
+            - jac[0][1] * (jac[1][0] * jac[2][2] - jac[1][2] * jac[2][0])
+            + jac[0][2] * (jac[1][0] * jac[2][1] - jac[1][1] * jac[2][0]);
+        cof[0][0] = jac[1][1] * jac[2][2] - jac[1][2] * jac[2][1];
+        cof[1][0] = -(jac[1][0] * jac[2][2] - jac[1][2] * jac[2][0]);
+        cof[2][0] = jac[1][0] * jac[2][1] - jac[1][1] * jac[2][0];
+        cof[0][1] = -(jac[0][1] * jac[2][2] - jac[0][2] * jac[2][1]);
+        cof[1][1] = jac[0][0] * jac[2][2] - jac[0][2] * jac[2][0];
+        cof[2][1] = -(jac[0][0] * jac[2][1] - jac[0][1] * jac[2][0]);
+        cof[0][2] = jac[0][1] * jac[1][2] - jac[0][2] * jac[1][1];
+        cof[1][2] = -(jac[0][0] * jac[1][2] - jac[0][2] * jac[1][0]);
+        cof[2][2] = jac[0][0] * jac[1][1] - jac[0][1] * jac[1][0];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) jac[i][j] = cof[i][j] / D;
+    }
+    *detJ = D;
+    for (int dx = 0; dx < dim; ++dx)
+        for (int n = 0; n < nen; ++n) {
+            double v = 0.0;
+            for (int dxi = 0; dxi < dim; ++dxi) v = v + G[dxi * nen + n] * jac[dx][dxi];
+            GNx[dx * nen + n] = v;
+        }
+}
+
+void uwr_global_derivs(const uwr_mesh* m, int64_t e, const double* xi, double* detJ, double* GNx) {
+    double nodes[8][3];
+    element_node_xyz(m, e, nodes);
+    global_derivs_nodes(m->dim, nodes, xi, detJ, GNx);
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Rheology                                                                             */
+/* ------------------------------------------------------------------------------------ */
+
+typedef struct {
+    const uwr_mesh* m;
+    const uwr_fields* f;
+    int64_t e;
+    const int64_t* inc;
+    const double* xi;
+    const double* N;        /* shape functions at xi */
+    const double* GNx;      /* global derivatives at xi */
+    double nodes[8][3];
+    double point_eta;
+} rheo_point;
+
+static double interp_temperature(const rheo_point* rp) {
+    int nen = (rp->m->dim == 3) ? 8 : 4;
+    double T = 0.0;
+    for (int a = 0; a < nen; ++a) T += rp->N[a] * rp->f->temperature[rp->inc[a]];
+    return T;
+}
+
+/* Underworld/Rheology/src/ConstitutiveMatrixCartesian.c:669-699 (isDiagonal stress) and
+ * StgDomain/Geometry/src/TensorMath.c:430-458 (second invariant). */
+static double stress_invariant(const rheo_point* rp, double eta) {
+    int dim = rp->m->dim, nen = (dim == 3) ? 8 : 4;
+    double L[3][3] = {{0}};
+    if (rp->f->velocity) {
+        for (int a = 0; a < nen; ++a)
+            for (int i = 0; i < dim; ++i)
+                for (int j = 0; j < dim; ++j)
+                    L[i][j] += rp->GNx[j * nen + a] * rp->f->velocity[rp->inc[a] * dim + i];
+    }
+    if (dim == 3) {
+        double sr[6] = {L[0][0], L[1][1], L[2][2], 0.5 * (L[0][1] + L[1][0]),
+                        0.5 * (L[0][2] + L[2][0]), 0.5 * (L[1][2] + L[2][1])};
+        double st[6] = {2.0 * eta * sr[0], 2.0 * eta * sr[1], 2.0 * eta * sr[2],
+                        eta * 2.0 * sr[3], eta * 2.0 * sr[4], eta * 2.0 * sr[5]};
+        double inv = 0.5 * (st[0] * st[0] + st[1] * st[1] + st[2] * st[2])
+                     + st[3] * st[3] + st[4] * st[4] + st[5] * st[5];
+        return sqrt(inv);
+    } else {
+        double sr[3] = {L[0][0], L[1][1], 0.5 * (L[0][1] + L[1][0])};
+        double st[3] = {2.0 * eta * sr[0], 2.0 * eta * sr[1], eta * 2.0 * sr[2]};
+        double inv = 0.5 * (st[0] * st[0] + st[1] * st[1]) + st[2] * st[2];
+        return sqrt(inv);
+    }
+}
+
+/* The rheology list of a RheologyMaterial (Underworld/Rheology/src/Rheology_Register.c:61-77).
+ * Every law in scope keeps D isotropic, so the constitutive matrix is tracked by eta:
+ * SetIsotropicViscosity (ConstitutiveMatrix.c:362-367) sets it, IsotropicCorrection adds to it. */
+static double run_rheologies(const uwr_material* mat, const rheo_point* rp) {
+    double eta = 0.0;
+    int dim = rp->m->dim;
+    for (int l = 0; l < mat->n_laws; ++l) {
+        const uwr_law* law = &mat->laws[l];
+        switch (law->law) {
+        case UWR_LAW_MATERIAL_VISCOSITY: /* MaterialViscosity.c:119-139 */
+            eta = law->p[0];
+            break;
+        case UWR_LAW_ARRHENIUS: { /* Arrhenius.c:156-200 */
+            double T = rp->f->temperature ? interp_temperature(rp) : 0.0;
+            if (law->p[2] > (0.0 + 1e-12)) {
+                int nen = (dim == 3) ? 8 : 4;
+                double y = 0.0;
+                for (int a = 0; a < nen; ++a) y += rp->N[a] * rp->nodes[a][1];
+                double depth = rp->m->max[1] - y;
+                eta = law->p[0] * exp((law->p[1] + law->p[2] * depth) / (T + law->p[3]));
+            } else {
+                eta = law->p[0] * exp((law->p[1]) / (T + law->p[3]));
+            }
+            break;
+        }
+        case UWR_LAW_FRANK_KAMENETSKII: { /* FrankKamenetskii.c:134-152 */
+            double T = rp->f->temperature ? interp_temperature(rp) : 0.0;
+            eta = law->p[0] * exp(-law->p[1] * T);
+            break;
+        }
+        case UWR_LAW_VISCOSITY_LIMITER: /* ViscosityLimiter.c:106-126 */
+            if (eta > law->p[0]) eta = law->p[0];
+            if (eta < law->p[1]) eta = law->p[1];
+            break;
+        case UWR_LAW_DRUCKER_PRAGER: { /* YieldRheology.c:198-243, VonMises.c:206-269, DruckerPrager.c:236-345 */
+            double minVisc = law->p[3];
+            if (!rp->f->previous_solution) break;
+            double ind = stress_invariant(rp, eta);
+            double pressure = rp->f->pressure ? rp->f->pressure[rp->e] : 0.0;
+            double phi = atan(law->p[1]);
+            double dpFric, dpCoh;
+            if (dim == 3) {
+                double sinphi = sin(phi);
+                double ood = 1.0 / (sqrt(3.0) * (3.0 - sinphi));
+                dpFric = 6.0 * sinphi * ood;
+                dpCoh = 6.0 * law->p[0] * cos(phi) * ood;
+            } else {
+                dpCoh = law->p[0] * cos(phi);
+                dpFric = sin(phi);
+            }
+            double crit = dpFric * pressure + dpCoh;
+            if (crit < law->p[2]) crit = law->p[2];
+            if (crit < ind) {
+                double beta = 1.0 - crit / ind;
+                double corr = -eta * beta;
+                if ((eta + corr) < minVisc) corr = minVisc - eta;
+                eta += corr;
+            }
+            if (eta < minVisc) eta = minVisc;
+            break;
+        }
+        case UWR_LAW_PARTICLE_VISCOSITY:
+            eta = rp->point_eta;
+            break;
+        default:
+            break;
+        }
+    }
+    return eta;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Element assembly                                                                     */
+/* ------------------------------------------------------------------------------------ */
+
+/* Underworld/Rheology/src/ConstitutiveMatrixCartesian.c:202-412 with the isDiagonal D_B of
+ * :556-649.  Accumulates elStiffMat[colDof][rowDof] exactly as the reference loop does. */
+static void accumulate_Ke(int dim, int nen, double eta, double factor, const double* GNx, double* Ke) {
+    int nd = nen * dim;
+    if (dim == 2) {
+        double D00 = 2.0 * eta * factor, D11 = 2.0 * eta * factor, D22 = eta * factor;
+        for (int r = 0; r < nen; ++r) {
+            double dx = GNx[0 * nen + r], dy = GNx[1 * nen + r];
+            double DB[3][2] = {{D00 * dx, 0.0}, {0.0, D11 * dy}, {D22 * dy, D22 * dx}};
+            for (int c = 0; c < nen; ++c) {
+                double bx = GNx[0 * nen + c], by = GNx[1 * nen + c];
+                double* K0 = Ke + (c * 2 + 0) * nd + r * 2;
+                double* K1 = Ke + (c * 2 + 1) * nd + r * 2;
+                K0[0] += bx * DB[0][0] + by * DB[2][0];
+                K0[1] += bx * DB[0][1] + by * DB[2][1];
+                K1[0] += by * DB[1][0] + bx * DB[2][0];
+                K1[1] += by * DB[1][1] + bx * DB[2][1];
+            }
+        }
+    } else {
+        double Dn = 2.0 * eta * factor, Ds = eta * factor;
+        for (int r = 0; r < nen; ++r) {
+            double dx = GNx[0 * nen + r], dy = GNx[1 * nen + r], dz = GNx[2 * nen + r];
+            double DB[6][3] = {{Dn * dx, 0.0, 0.0}, {0.0, Dn * dy, 0.0}, {0.0, 0.0, Dn * dz},
+                               {Ds * dy, Ds * dx, 0.0}, {Ds * dz, 0.0, Ds * dx}, {0.0, Ds * dz, Ds * dy}};
+            for (int c = 0; c < nen; ++c) {
+                double bx = GNx[0 * nen + c], by = GNx[1 * nen + c], bz = GNx[2 * nen + c];
+                double* K0 = Ke + (c * 3 + 0) * nd + r * 3;
+                double* K1 = Ke + (c * 3 + 1) * nd + r * 3;
+                double* K2 = Ke + (c * 3 + 2) * nd + r * 3;
+                for (int j = 0; j < 3; ++j) {
+                    K0[j] += bx * DB[0][j] + by * DB[3][j] + bz * DB[4][j];
+                    K1[j] += by * DB[1][j] + bx * DB[3][j] + bz * DB[5][j];
+                    K2[j] += bz * DB[2][j] + bx * DB[4][j] + by * DB[5][j];
+                }
+            }
+        }
+    }
+}
+
+/* StgFEM/Assembly/src/GradientStiffnessMatrixTerm.c:160-250 on the Gauss swarm
+ * (2^dim points at +-1/sqrt(3), unit weights: GaussParticleLayout.c:218-336). */
+void uwr_gauss_G(const uwr_mesh* m, int64_t e, double* Ge) {
+    int dim = m->dim, nen = (dim == 3) ? 8 : 4, nd = nen * dim;
+    double nodes[8][3];
+    element_node_xyz(m, e, nodes);
+    memset(Ge, 0, sizeof(double) * nd);
+    double a = -1.0 / sqrt(3.0);
+    double ab[2] = {a, -a};
+    int ng = 1 << dim;
+    for (int g = 0; g < ng; ++g) {
+        double xi[3] = {ab[g & 1], ab[(g >> 1) & 1], ab[(g >> 2) & 1]};
+        double detJ, GNx[24];
+        global_derivs_nodes(dim, nodes, xi, &detJ, GNx);
+        double weight = 1.0;
+        for (int r = 0; r < nen; ++r)
+            for (int d = 0; d < dim; ++d) Ge[r * dim + d] += +weight * (-detJ) * (GNx[d * nen + r] * 1.0);
+    }
+}
+
+int uwr_assemble(const uwr_mesh* m, int64_t n, const uint32_t* offsets, const uint32_t* perm,
+                 const double* xi, const int32_t* material, const double* point_eta,
+                 const double* point_rho, int32_t nmat, const uwr_material* mats,
+                 const uwr_fields* f, double* Ke, double* fe, double* Ge, double* Se,
+                 double* eta_out, int32_t nthreads) {
+    (void)n;
+    set_threads(nthreads);
+    int dim = m->dim, nen = (dim == 3) ? 8 : 4, nd = nen * dim;
+    int64_t E = uwr_num_elements(m);
+    /* WeightsCalculator.c:83 cellLocalVolume = 2^dim; ConstantWeights.c:180-189 */
+    const double cellVolume = pow(2.0, (double)dim);
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(| : bad)
+    for (int64_t e = 0; e < E; ++e) {
+        int64_t inc[8];
+        uwr_element_nodes(m, e, inc);
+        rheo_point rp;
+        rp.m = m;
+        rp.f = f;
+        rp.e = e;
+        rp.inc = inc;
+        element_node_xyz(m, e, rp.nodes);
+        double* K = Ke ? Ke + e * nd * nd : NULL;
+        double Kloc[576];
+        if (!K) K = Kloc;
+        memset(K, 0, sizeof(double) * nd * nd);
+        double floc[24] = {0};
+        uint32_t beg = offsets[e], end = offsets[e + 1];
+        uint32_t cnt = end - beg;
+        double weight = cellVolume / (double)cnt;
+        for (uint32_t s = beg; s < end; ++s) {
+            uint32_t p = perm[s];
+            const double* x = xi + 3 * (int64_t)s;
+            double detJ, GNx[24], N[8];
+            global_derivs_nodes(dim, rp.nodes, x, &detJ, GNx);
+            uwr_shape(dim, x, N);
+            rp.xi = x;
+            rp.N = N;
+            rp.GNx = GNx;
+            rp.point_eta = point_eta ? point_eta[p] : 0.0;
+            int32_t mi = material ? material[p] : 0;
+            if (mi < 0 || mi >= nmat) { bad |= 1; continue; }
+            const uwr_material* mat = &mats[mi];
+            double eta = run_rheologies(mat, &rp);
+            if (eta_out) eta_out[s] = eta;
+            accumulate_Ke(dim, nen, eta, detJ * weight, GNx, K);
+            /* PICellerator/Utils/src/BuoyancyForceTerm.c:374-450 */
+            double T = f->temperature ? interp_temperature(&rp) : 0.0;
+            double rho0 = point_rho ? point_rho[p] : mat->density;
+            double density = rho0 * (1.0 - mat->alpha * (T - mat->ref_temp));
+            double force = density * f->gravity;
+            double factor = detJ * weight * 1.0 * force;
+            for (int a = 0; a < nen; ++a) floc[a * dim + f->vert_axis] += -1.0 * factor * N[a];
+        }
+        double G[24];
+        uwr_gauss_G(m, e, G);
+        if (fe) memcpy(fe + e * nd, floc, sizeof(double) * nd);
+        if (Ge) memcpy(Ge + e * nd, G, sizeof(double) * nd);
+        if (Se) {
+            /* StgFEM/SLE/ProvidedSystems/StokesFlow/src/UzawaPreconditionerTerm.c:194-214 */
+            double s = 0.0;
+            for (int v = 0; v < nd; ++v) s += G[v] * (G[v] / K[v * nd + v]);
+            Se[e] = s;
+        }
+    }
+    return bad ? -1 : 0;
+}
+
+int uwr_assemble_gauss(const uwr_mesh* m, int32_t nmat, const uwr_material* mats,
+                       const int32_t* el_material, const uwr_fields* f, double* Ke) {
+    int dim = m->dim, nen = (dim == 3) ? 8 : 4, nd = nen * dim;
+    int64_t E = uwr_num_elements(m);
+    double a = -1.0 / sqrt(3.0);
+    double ab[2] = {a, -a};
+    int ng = 1 << dim;
+    for (int64_t e = 0; e < E; ++e) {
+        int64_t inc[8];
+        uwr_element_nodes(m, e, inc);
+        rheo_point rp;
+        rp.m = m;
+        rp.f = f;
+        rp.e = e;
+        rp.inc = inc;
+        element_node_xyz(m, e, rp.nodes);
+        double* K = Ke + e * nd * nd;
+        memset(K, 0, sizeof(double) * nd * nd);
+        int32_t mi = el_material ? el_material[e] : 0;
+        if (mi < 0 || mi >= nmat) return -1;
+        for (int g = 0; g < ng; ++g) {
+            double xi[3] = {ab[g & 1], ab[(g >> 1) & 1], ab[(g >> 2) & 1]};
+            double detJ, GNx[24], N[8];
+            global_derivs_nodes(dim, rp.nodes, xi, &detJ, GNx);
+            uwr_shape(dim, xi, N);
+            rp.xi = xi;
+            rp.N = N;
+            rp.GNx = GNx;
+            rp.point_eta = 0.0;
+            double eta = run_rheologies(&mats[mi], &rp);
+            accumulate_Ke(dim, nen, eta, detJ * 1.0, GNx, K);
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Global system                                                                        */
+/* ------------------------------------------------------------------------------------ */
+
+/* StgFEM/Discretisation/src/FeEquationNumber.c:700-760: node order, dof order; BC -> -1. */
+int64_t uwr_eqnum(const uwr_mesh* m, const uint8_t* fixed, int64_t* eq) {
+    int64_t nn = uwr_num_nodes(m), cur = 0;
+    for (int64_t n = 0; n < nn; ++n)
+        for (int d = 0; d < m->dim; ++d) {
+            int64_t k = n * m->dim + d;
+            eq[k] = (fixed && fixed[k]) ? -1 : cur++;
+        }
+    return cur;
+}
+
+typedef struct { int64_t nx, ny, nz; } grid3;
+static grid3 node_grid(const uwr_mesh* m) {
+    grid3 g = {m->nel[0] + 1, m->nel[1] + 1, (m->dim == 3) ? m->nel[2] + 1 : 1};
+    return g;
+}
+
+/* Neighbours (incl. self) of node n in ascending index order. */
+static int node_neighbours(const uwr_mesh* m, int64_t n, int64_t* nb) {
+    grid3 g = node_grid(m);
+    int64_t i = n % g.nx, j = (n / g.nx) % g.ny, k = n / (g.nx * g.ny);
+    int cnt = 0;
+    int kz0 = (m->dim == 3) ? -1 : 0, kz1 = (m->dim == 3) ? 1 : 0;
+    for (int dk = kz0; dk <= kz1; ++dk)
+        for (int dj = -1; dj <= 1; ++dj)
+            for (int di = -1; di <= 1; ++di) {
+                int64_t ii = i + di, jj = j + dj, kk = k + dk;
+                if (ii < 0 || jj < 0 || kk < 0 || ii >= g.nx || jj >= g.ny || kk >= g.nz) continue;
+                nb[cnt++] = ii + g.nx * (jj + g.ny * kk);
+            }
+    return cnt;
+}
+
+/* Elements containing node n and the node's local index in each. */
+static int node_elements(const uwr_mesh* m, int64_t n, int64_t* els, int* loc) {
+    grid3 g = node_grid(m);
+    int64_t i = n % g.nx, j = (n / g.nx) % g.ny, k = n / (g.nx * g.ny);
+    int cnt = 0;
+    int kz0 = (m->dim == 3) ? -1 : 0;
+    for (int dk = kz0; dk <= 0; ++dk)
+        for (int dj = -1; dj <= 0; ++dj)
+            for (int di = -1; di <= 0; ++di) {
+                int64_t ei = i + di, ej = j + dj, ek = k + dk;
+                if (ei < 0 || ej < 0 || ek < 0 || ei >= m->nel[0] || ej >= m->nel[1]) continue;
+                if (m->dim == 3 && ek >= m->nel[2]) continue;
+                els[cnt] = ei + m->nel[0] * (ej + m->nel[1] * ek);
+                loc[cnt] = (int)((-di) + 2 * (-dj) + ((m->dim == 3) ? 4 * (-dk) : 0));
+                cnt++;
+            }
+    return cnt;
+}
+
+int64_t uwr_csr_nnz(const uwr_mesh* m, const int64_t* eq, int64_t nfree, int64_t* rowptr) {
+    int64_t nn = uwr_num_nodes(m);
+    int dim = m->dim;
+    rowptr[0] = 0;
+    int64_t r = 0;
+    for (int64_t n = 0; n < nn; ++n) {
+        int64_t nb[27];
+        int nnb = node_neighbours(m, n, nb);
+        int cols = 0;
+        for (int b = 0; b < nnb; ++b)
+            for (int d = 0; d < dim; ++d) cols += eq[nb[b] * dim + d] >= 0;
+        for (int d = 0; d < dim; ++d) {
+            if (eq[n * dim + d] < 0) continue;
+            rowptr[r + 1] = rowptr[r] + cols;
+            r++;
+        }
+    }
+    (void)nfree;
+    return rowptr[r];
+}
+
+/* StgFEM/SLE/SystemSetup/src/StiffnessMatrix.c:867-1017: element loop with MatSetValues
+ * ADD_VALUES through the location matrix (negative equation numbers dropped).  Restated
+ * as a row gather so that rows are built independently. */
+void uwr_csr_fill(const uwr_mesh* m, const int64_t* eq, int64_t nfree, const double* Ke,
+                  const int64_t* rowptr, int64_t* cols, double* vals, int32_t nthreads) {
+    set_threads(nthreads);
+    int64_t nn = uwr_num_nodes(m);
+    int dim = m->dim, nen = (dim == 3) ? 8 : 4, nd = nen * dim;
+    /* first free row of every node */
+    int64_t* rowOf = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nn + 1));
+    int64_t r = 0;
+    for (int64_t n = 0; n < nn; ++n) {
+        rowOf[n] = r;
+        for (int d = 0; d < dim; ++d) r += eq[n * dim + d] >= 0;
+    }
+    rowOf[nn] = r;
+    (void)nfree;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t n = 0; n < nn; ++n) {
+        int64_t nb[27];
+        int nnb = node_neighbours(m, n, nb);
+        int64_t els[8];
+        int loc[8];
+        int ne = node_elements(m, n, els, loc);
+        int64_t rr = rowOf[n];
+        for (int d = 0; d < dim; ++d) {
+            if (eq[n * dim + d] < 0) continue;
+            int64_t base = rowptr[rr];
+            int c = 0;
+            for (int b = 0; b < nnb; ++b)
+                for (int db = 0; db < dim; ++db) {
+                    int64_t q = eq[nb[b] * dim + db];
+                    if (q < 0) continue;
+                    double v = 0.0;
+                    for (int ie = 0; ie < ne; ++ie) {
+                        int64_t inc[8];
+                        uwr_element_nodes(m, els[ie], inc);
+                        for (int a = 0; a < nen; ++a)
+                            if (inc[a] == nb[b]) {
+                                const double* K = Ke + els[ie] * nd * nd;
+                                v += K[(loc[ie] * dim + d) * nd + a * dim + db];
+                            }
+                    }
+                    cols[base + c] = q;
+                    vals[base + c] = v;
+                    c++;
+                }
+            rr++;
+        }
+    }
+    free(rowOf);
+}
+
+void uwr_csr_spmv(int64_t nrows, const int64_t* rowptr, const int64_t* cols, const double* vals,
+                  const double* x, double* y, int32_t nthreads) {
+    set_threads(nthreads);
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < nrows; ++r) {
+        double s = 0.0;
+        for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) s += vals[k] * x[cols[k]];
+        y[r] = s;
+    }
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Sparse matrices for the multigrid restatement                                        */
+/* ------------------------------------------------------------------------------------ */
+
+typedef struct {
+    int64_t nr, nc;
+    int64_t* rp;
+    int64_t* ci;
+    double* v;
+} csr;
+
+static void csr_free(csr* a) {
+    free(a->rp);
+    free(a->ci);
+    free(a->v);
+    a->rp = NULL;
+    a->ci = NULL;
+    a->v = NULL;
+}
+
+static void csr_mv(const csr* a, const double* x, double* y) {
+#pragma omp parallel for schedule(static)
+    for (int64_t r = 0; r < a->nr; ++r) {
+        double s = 0.0;
+        for (int64_t k = a->rp[r]; k < a->rp[r + 1]; ++k) s += a->v[k] * x[a->ci[k]];
+        y[r] = s;
+    }
+}
+
+static csr csr_transpose(const csr* a) {
+    csr t;
+    t.nr = a->nc;
+    t.nc = a->nr;
+    t.rp = (int64_t*)calloc((size_t)(t.nr + 1), sizeof(int64_t));
+    int64_t nnz = a->rp[a->nr];
+    t.ci = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nnz ? nnz : 1));
+    t.v = (double*)malloc(sizeof(double) * (size_t)(nnz ? nnz : 1));
+    for (int64_t k = 0; k < nnz; ++k) t.rp[a->ci[k] + 1]++;
+    for (int64_t r = 0; r < t.nr; ++r) t.rp[r + 1] += t.rp[r];
+    int64_t* pos = (int64_t*)malloc(sizeof(int64_t) * (size_t)(t.nr + 1));
+    memcpy(pos, t.rp, sizeof(int64_t) * (size_t)(t.nr + 1));
+    for (int64_t r = 0; r < a->nr; ++r)
+        for (int64_t k = a->rp[r]; k < a->rp[r + 1]; ++k) {
+            int64_t c = a->ci[k];
+            t.ci[pos[c]] = r;
+            t.v[pos[c]] = a->v[k];
+            pos[c]++;
+        }
+    free(pos);
+    return t;
+}
+
+/* Gustavson sparse product C = A B (columns sorted). */
+static csr csr_matmul(const csr* A, const csr* B) {
+    csr C;
+    C.nr = A->nr;
+    C.nc = B->nc;
+    C.rp = (int64_t*)calloc((size_t)(C.nr + 1), sizeof(int64_t));
+    int64_t* mark = (int64_t*)malloc(sizeof(int64_t) * (size_t)B->nc);
+    for (int64_t c = 0; c < B->nc; ++c) mark[c] = -1;
+    for (int64_t r = 0; r < A->nr; ++r) {
+        int64_t cnt = 0;
+        for (int64_t k = A->rp[r]; k < A->rp[r + 1]; ++k) {
+            int64_t a = A->ci[k];
+            for (int64_t q = B->rp[a]; q < B->rp[a + 1]; ++q)
+                if (mark[B->ci[q]] != r) { mark[B->ci[q]] = r; cnt++; }
+        }
+        C.rp[r + 1] = C.rp[r] + cnt;
+    }
+    int64_t nnz = C.rp[C.nr];
+    C.ci = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nnz ? nnz : 1));
+    C.v = (double*)malloc(sizeof(double) * (size_t)(nnz ? nnz : 1));
+    double* acc = (double*)calloc((size_t)B->nc, sizeof(double));
+    for (int64_t c = 0; c < B->nc; ++c) mark[c] = -1;
+    for (int64_t r = 0; r < A->nr; ++r) {
+        int64_t cnt = 0, base = C.rp[r];
+        for (int64_t k = A->rp[r]; k < A->rp[r + 1]; ++k) {
+            int64_t a = A->ci[k];
+            double av = A->v[k];
+            for (int64_t q = B->rp[a]; q < B->rp[a + 1]; ++q) {
+                int64_t c = B->ci[q];
+                if (mark[c] != r) { mark[c] = r; C.ci[base + cnt++] = c; acc[c] = 0.0; }
+                acc[c] += av * B->v[q];
+            }
+        }
+        /* sort columns (insertion sort; rows are short) */
+        for (int64_t i = 1; i < cnt; ++i) {
+            int64_t key = C.ci[base + i], j = i - 1;
+            while (j >= 0 && C.ci[base + j] > key) { C.ci[base + j + 1] = C.ci[base + j]; j--; }
+            C.ci[base + j + 1] = key;
+        }
+        for (int64_t i = 0; i < cnt; ++i) C.v[base + i] = acc[C.ci[base + i]];
+    }
+    free(mark);
+    free(acc);
+    return C;
+}
+
+/* StgFEM/SLE/SystemSetup/src/SROpGenerator.c:765-1060 (finest level: rows = fine free dofs,
+ * columns = every coarse dof node*nDofs+k, weight 1/nPoints over the 2^(#odd indices)
+ * coarse nodes) and :1086- (coarser levels: every dof). */
+static csr sr_prolongation(const uwr_mesh* fine, const int64_t* fine_eq, int64_t nfine_rows) {
+    int dim = fine->dim;
+    grid3 gf = node_grid(fine);
+    int64_t cnx = fine->nel[0] / 2 + 1, cny = fine->nel[1] / 2 + 1;
+    int64_t cnz = (dim == 3) ? fine->nel[2] / 2 + 1 : 1;
+    int64_t nfn = gf.nx * gf.ny * gf.nz;
+    csr P;
+    P.nr = nfine_rows;
+    P.nc = cnx * cny * cnz * dim;
+    P.rp = (int64_t*)calloc((size_t)(P.nr + 1), sizeof(int64_t));
+    P.ci = (int64_t*)malloc(sizeof(int64_t) * (size_t)(P.nr * 8 + 1));
+    P.v = (double*)malloc(sizeof(double) * (size_t)(P.nr * 8 + 1));
+    int64_t nnz = 0;
+    for (int64_t n = 0; n < nfn; ++n) {
+        int64_t ind[3] = {n % gf.nx, (n / gf.nx) % gf.ny, n / (gf.nx * gf.ny)};
+        int noff[3] = {1, 1, 1};
+        for (int d = 0; d < dim; ++d) noff[d] = (ind[d] & 1) ? 2 : 1;
+        int npts = noff[0] * noff[1] * noff[2];
+        int64_t nodes[8];
+        int c = 0;
+        for (int oz = 0; oz < noff[2]; ++oz)
+            for (int oy = 0; oy < noff[1]; ++oy)
+                for (int ox = 0; ox < noff[0]; ++ox) {
+                    int64_t ci = (ind[0] >> 1) + ox, cj = (ind[1] >> 1) + oy;
+                    int64_t ck = (dim == 3) ? (ind[2] >> 1) + oz : 0;
+                    nodes[c++] = ci + cnx * (cj + cny * ck);
+                }
+        double frac = 1.0 / (double)npts;
+        for (int k = 0; k < dim; ++k) {
+            int64_t row = fine_eq ? fine_eq[n * dim + k] : n * dim + k;
+            if (row < 0) continue;
+            P.rp[row + 1] = npts;
+            for (int j = 0; j < npts; ++j) {
+                P.ci[row * 8 + j] = nodes[j] * dim + k;
+                P.v[row * 8 + j] = frac;
+            }
+        }
+    }
+    /* compact (rows were laid out with stride 8) */
+    for (int64_t r = 0; r < P.nr; ++r) {
+        int64_t len = P.rp[r + 1];
+        for (int64_t j = 0; j < len; ++j) {
+            P.ci[nnz + j] = P.ci[r * 8 + j];
+            P.v[nnz + j] = P.v[r * 8 + j];
+        }
+        /* sort the row */
+        for (int64_t i = 1; i < len; ++i) {
+            int64_t key = P.ci[nnz + i];
+            double kv = P.v[nnz + i];
+            int64_t j = i - 1;
+            while (j >= 0 && P.ci[nnz + j] > key) { P.ci[nnz + j + 1] = P.ci[nnz + j]; P.v[nnz + j + 1] = P.v[nnz + j]; j--; }
+            P.ci[nnz + j + 1] = key;
+            P.v[nnz + j + 1] = kv;
+        }
+        P.rp[r + 1] = nnz + len;
+        nnz += len;
+    }
+    P.rp[0] = 0;
+    return P;
+}
+
+/* Dense Cholesky of the coarsest operator (PETSc's redundant LU on one rank). */
+typedef struct { int64_t n; double* L; } chol;
+static int chol_factor(const csr* A, chol* c) {
+    int64_t n = A->nr;
+    c->n = n;
+    c->L = (double*)calloc((size_t)(n * n), sizeof(double));
+    for (int64_t r = 0; r < n; ++r)
+        for (int64_t k = A->rp[r]; k < A->rp[r + 1]; ++k) c->L[r * n + A->ci[k]] = A->v[k];
+    for (int64_t j = 0; j < n; ++j) {
+        double d = c->L[j * n + j];
+        for (int64_t k = 0; k < j; ++k) d -= c->L[j * n + k] * c->L[j * n + k];
+        if (!(d > 0.0)) return -1;
+        d = sqrt(d);
+        c->L[j * n + j] = d;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = j + 1; i < n; ++i) {
+            double s = c->L[i * n + j];
+            for (int64_t k = 0; k < j; ++k) s -= c->L[i * n + k] * c->L[j * n + k];
+            c->L[i * n + j] = s / d;
+        }
+    }
+    return 0;
+}
+static void chol_solve(const chol* c, const double* b, double* x) {
+    int64_t n = c->n;
+    for (int64_t i = 0; i < n; ++i) {
+        double s = b[i];
+        for (int64_t k = 0; k < i; ++k) s -= c->L[i * n + k] * x[k];
+        x[i] = s / c->L[i * n + i];
+    }
+    for (int64_t i = n - 1; i >= 0; --i) {
+        double s = x[i];
+        for (int64_t k = i + 1; k < n; ++k) s -= c->L[k * n + i] * x[k];
+        x[i] = s / c->L[i * n + i];
+    }
+}
+
+/* PCSOR default (SOR_LOCAL_SYMMETRIC_SWEEP, omega = 1): forward then backward Gauss-Seidel. */
+static void sor_symmetric(const csr* A, const double* b, double* x, int its) {
+    for (int it = 0; it < its; ++it) {
+        for (int64_t r = 0; r < A->nr; ++r) {
+            double s = b[r], d = 1.0;
+            for (int64_t k = A->rp[r]; k < A->rp[r + 1]; ++k) {
+                if (A->ci[k] == r) d = A->v[k]; else s -= A->v[k] * x[A->ci[k]];
+            }
+            x[r] = s / d;
+        }
+        for (int64_t r = A->nr - 1; r >= 0; --r) {
+            double s = b[r], d = 1.0;
+            for (int64_t k = A->rp[r]; k < A->rp[r + 1]; ++k) {
+                if (A->ci[k] == r) d = A->v[k]; else s -= A->v[k] * x[A->ci[k]];
+            }
+            x[r] = s / d;
+        }
+    }
+}
+
+typedef struct {
+    int nlev;           /* level 0 = coarsest */
+    csr A[12];
+    csr P[12];          /* P[l]: level l-1 -> level l */
+    csr PT[12];
+    chol coarse;
+    int down, up;
+    double* work[12][3];
+} mg_t;
+
+/* PETScMGSolver.c:459-549 (Galerkin MatPtAP hierarchy) + PCMG multiplicative V-cycle with
+ * Richardson/SOR smoothers (PETScMGSolver.c:641-716). */
+static int mg_setup(mg_t* mg, const uwr_mesh* m, const int64_t* eq, const csr* K, int levels, int down, int up) {
+    memset(mg, 0, sizeof(*mg));
+    mg->nlev = levels;
+    mg->down = down;
+    mg->up = up;
+    int L = levels - 1;
+    mg->A[L] = *K;
+    uwr_mesh cur = *m;
+    for (int l = L; l >= 1; --l) {
+        mg->P[l] = sr_prolongation(&cur, (l == L) ? eq : NULL, mg->A[l].nr);
+        mg->PT[l] = csr_transpose(&mg->P[l]);
+        csr AP = csr_matmul(&mg->A[l], &mg->P[l]);
+        mg->A[l - 1] = csr_matmul(&mg->PT[l], &AP);
+        csr_free(&AP);
+        for (int d = 0; d < cur.dim; ++d) cur.nel[d] /= 2;
+    }
+    for (int l = 0; l < levels; ++l)
+        for (int w = 0; w < 3; ++w) mg->work[l][w] = (double*)calloc((size_t)mg->A[l].nr, sizeof(double));
+    return chol_factor(&mg->A[0], &mg->coarse);
+}
+
+static void mg_free(mg_t* mg) {
+    for (int l = 0; l < mg->nlev; ++l) {
+        if (l < mg->nlev - 1) csr_free(&mg->A[l]);
+        if (l > 0) { csr_free(&mg->P[l]); csr_free(&mg->PT[l]); }
+        for (int w = 0; w < 3; ++w) free(mg->work[l][w]);
+    }
+    free(mg->coarse.L);
+}
+
+static void vcycle(mg_t* mg, int l, const double* b, double* x) {
+    if (l == 0) {
+        chol_solve(&mg->coarse, b, x);
+        return;
+    }
+    const csr* A = &mg->A[l];
+    double* r = mg->work[l][0];
+    memset(x, 0, sizeof(double) * (size_t)A->nr);
+    sor_symmetric(A, b, x, mg->down);
+    csr_mv(A, x, r);
+    for (int64_t i = 0; i < A->nr; ++i) r[i] = b[i] - r[i];
+    double* bc = mg->work[l - 1][1];
+    double* xc = mg->work[l - 1][2];
+    csr_mv(&mg->PT[l], r, bc);
+    vcycle(mg, l - 1, bc, xc);
+    double* t = mg->work[l][1];
+    csr_mv(&mg->P[l], xc, t);
+    for (int64_t i = 0; i < A->nr; ++i) x[i] += t[i];
+    sor_symmetric(A, b, x, mg->up);
+}
+
+static double dot(int64_t n, const double* a, const double* b) {
+    double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+    for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+    return s;
+}
+
+/* Right-preconditioned FGMRES(restart) (the PETSc KSPFGMRES algorithm, zero initial guess,
+ * stop when ||r|| <= rtol*||b||). Returns iterations. */
+typedef void (*op_fn)(void* ctx, const double* x, double* y);
+static int fgmres(int64_t n, op_fn A, void* actx, op_fn M, void* mctx, const double* b,
+                  double* x, double rtol, int restart, int maxit) {
+    double** V = (double**)malloc(sizeof(double*) * (size_t)(restart + 1));
+    double** Z = (double**)malloc(sizeof(double*) * (size_t)restart);
+    for (int i = 0; i <= restart; ++i) V[i] = (double*)malloc(sizeof(double) * (size_t)n);
+    for (int i = 0; i < restart; ++i) Z[i] = (double*)malloc(sizeof(double) * (size_t)n);
+    double* H = (double*)calloc((size_t)((restart + 1) * restart), sizeof(double));
+    double* cs = (double*)malloc(sizeof(double) * (size_t)restart);
+    double* sn = (double*)malloc(sizeof(double) * (size_t)restart);
+    double* g = (double*)malloc(sizeof(double) * (size_t)(restart + 1));
+    double* w = (double*)malloc(sizeof(double) * (size_t)n);
+    memset(x, 0, sizeof(double) * (size_t)n);
+    double bnorm = sqrt(dot(n, b, b));
+    int its = 0;
+    if (bnorm == 0.0) goto done;
+    for (;;) {
+        A(actx, x, w);
+        for (int64_t i = 0; i < n; ++i) V[0][i] = b[i] - w[i];
+        double beta = sqrt(dot(n, V[0], V[0]));
+        if (beta <= rtol * bnorm || its >= maxit) break;
+        for (int64_t i = 0; i < n; ++i) V[0][i] /= beta;
+        memset(g, 0, sizeof(double) * (size_t)(restart + 1));
+        g[0] = beta;
+        int k = 0;
+        for (; k < restart && its < maxit; ++k) {
+            M(mctx, V[k], Z[k]);
+            A(actx, Z[k], w);
+            for (int j = 0; j <= k; ++j) {
+                double h = dot(n, w, V[j]);
+                H[j * restart + k] = h;
+                for (int64_t i = 0; i < n; ++i) w[i] -= h * V[j][i];
+            }
+            double hn = sqrt(dot(n, w, w));
+            H[(k + 1) * restart + k] = hn;
+            for (int64_t i = 0; i < n; ++i) V[k + 1][i] = w[i] / (hn > 0 ? hn : 1.0);
+            for (int j = 0; j < k; ++j) {
+                double t = cs[j] * H[j * restart + k] + sn[j] * H[(j + 1) * restart + k];
+                H[(j + 1) * restart + k] = -sn[j] * H[j * restart + k] + cs[j] * H[(j + 1) * restart + k];
+                H[j * restart + k] = t;
+            }
+            double a = H[k * restart + k], bb = H[(k + 1) * restart + k];
+            double rr = sqrt(a * a + bb * bb);
+            cs[k] = a / rr;
+            sn[k] = bb / rr;
+            H[k * restart + k] = rr;
+            H[(k + 1) * restart + k] = 0.0;
+            g[k + 1] = -sn[k] * g[k];
+            g[k] = cs[k] * g[k];
+            its++;
+            if (fabs(g[k + 1]) <= rtol * bnorm) { k++; break; }
+        }
+        /* back substitution */
+        double y[256];
+        for (int i = k - 1; i >= 0; --i) {
+            double s = g[i];
+            for (int j = i + 1; j < k; ++j) s -= H[i * restart + j] * y[j];
+            y[i] = s / H[i * restart + i];
+        }
+        for (int j = 0; j < k; ++j)
+            for (int64_t i = 0; i < n; ++i) x[i] += y[j] * Z[j][i];
+        if (fabs(g[k]) <= rtol * bnorm || its >= maxit) break;
+    }
+done:
+    for (int i = 0; i <= restart; ++i) free(V[i]);
+    for (int i = 0; i < restart; ++i) free(Z[i]);
+    free(V);
+    free(Z);
+    free(H);
+    free(cs);
+    free(sn);
+    free(g);
+    free(w);
+    return its;
+}
+
+typedef struct {
+    csr K, G, GT;
+    mg_t mg;
+    double a11_rtol;
+    int restart, max_inner;
+    int64_t inner_its;
+    double* Sdiag;
+    double* tu;
+    double* tu2;
+} bsscr_t;
+
+static void op_K(void* c, const double* x, double* y) { csr_mv(&((bsscr_t*)c)->K, x, y); }
+static void op_mg(void* c, const double* x, double* y) {
+    bsscr_t* s = (bsscr_t*)c;
+    vcycle(&s->mg, s->mg.nlev - 1, x, y);
+}
+static int a11_solve(bsscr_t* s, const double* b, double* x, double rtol) {
+    int its = fgmres(s->K.nr, op_K, s, op_mg, s, b, x, rtol, s->restart, s->max_inner);
+    s->inner_its += its;
+    return its;
+}
+/* S v = G^T K^{-1} G v (the positive form; PETSc's MatSchurComplement is its negative). */
+static void op_S(void* c, const double* v, double* y) {
+    bsscr_t* s = (bsscr_t*)c;
+    csr_mv(&s->G, v, s->tu);
+    a11_solve(s, s->tu, s->tu2, s->a11_rtol);
+    csr_mv(&s->GT, s->tu2, y);
+}
+static void op_Spc(void* c, const double* v, double* y) {
+    bsscr_t* s = (bsscr_t*)c;
+    for (int64_t i = 0; i < s->G.nc; ++i) y[i] = s->Sdiag ? v[i] / s->Sdiag[i] : v[i];
+}
+
+/* Preconditioned CG (PETSc KSPCG), zero initial guess, stopped on the unpreconditioned
+ * residual ||r|| <= rtol ||b|| so that every solver here uses the same test. */
+static int pcg(int64_t n, op_fn A, void* actx, op_fn M, void* mctx, const double* b, double* x,
+               double rtol, int maxit) {
+    double* r = (double*)malloc(sizeof(double) * (size_t)n);
+    double* z = (double*)malloc(sizeof(double) * (size_t)n);
+    double* p = (double*)malloc(sizeof(double) * (size_t)n);
+    double* q = (double*)malloc(sizeof(double) * (size_t)n);
+    memset(x, 0, sizeof(double) * (size_t)n);
+    memcpy(r, b, sizeof(double) * (size_t)n);
+    M(mctx, r, z);
+    double rz = dot(n, r, z), r0 = sqrt(dot(n, r, r));
+    memcpy(p, z, sizeof(double) * (size_t)n);
+    int it = 0;
+    while (it < maxit && sqrt(dot(n, r, r)) > rtol * r0) {
+        A(actx, p, q);
+        double alpha = rz / dot(n, p, q);
+        for (int64_t i = 0; i < n; ++i) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
+        M(mctx, r, z);
+        double rz2 = dot(n, r, z);
+        double beta = rz2 / rz;
+        rz = rz2;
+        for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+        it++;
+    }
+    free(r);
+    free(z);
+    free(p);
+    free(q);
+    return it;
+}
+
+static void remove_constant(int64_t n, double* v) {
+    double s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s += v[i];
+    s /= (double)n;
+    for (int64_t i = 0; i < n; ++i) v[i] -= s;
+}
+
+/* Solvers/KSPSolvers/src/BSSCR/auglag-driver-DGTGD.c:53-441 with penalty 0:
+ * h_hat = h - G^T K^{-1} f; Schur solve with the approxS (uw) or gkgdiag preconditioner;
+ * constant null-space removal (ksp_pressure_nullspace.c:82-176); back-solve u = K^{-1}(f - G p). */
+int uwr_solve_bsscr(const uwr_mesh* m, const uint8_t* fixed, const double* Ke, const double* Ge,
+                    const double* fe, const double* Se, const uwr_solve_opts* o,
+                    double* u_nodal, double* p, uwr_report* rep) {
+    set_threads(o->nthreads);
+    double t0 = now_s();
+    int dim = m->dim, nen = (dim == 3) ? 8 : 4, nd = nen * dim;
+    int64_t nn = uwr_num_nodes(m), E = uwr_num_elements(m);
+    int64_t* eq = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nn * dim));
+    int64_t nfree = uwr_eqnum(m, fixed, eq);
+    bsscr_t s;
+    memset(&s, 0, sizeof(s));
+    s.K.nr = s.K.nc = nfree;
+    s.K.rp = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nfree + 1));
+    int64_t nnz = uwr_csr_nnz(m, eq, nfree, s.K.rp);
+    s.K.ci = (int64_t*)malloc(sizeof(int64_t) * (size_t)nnz);
+    s.K.v = (double*)malloc(sizeof(double) * (size_t)nnz);
+    uwr_csr_fill(m, eq, nfree, Ke, s.K.rp, s.K.ci, s.K.v, o->nthreads);
+    /* G: free velocity dofs x elements (P0) */
+    s.G.nr = nfree;
+    s.G.nc = E;
+    s.G.rp = (int64_t*)calloc((size_t)(nfree + 1), sizeof(int64_t));
+    {
+        int64_t* cnt = s.G.rp;
+        for (int64_t e = 0; e < E; ++e) {
+            int64_t inc[8];
+            uwr_element_nodes(m, e, inc);
+            for (int a = 0; a < nen; ++a)
+                for (int d = 0; d < dim; ++d) {
+                    int64_t q = eq[inc[a] * dim + d];
+                    if (q >= 0) cnt[q + 1]++;
+                }
+        }
+        for (int64_t r = 0; r < nfree; ++r) s.G.rp[r + 1] += s.G.rp[r];
+        int64_t gn = s.G.rp[nfree];
+        s.G.ci = (int64_t*)malloc(sizeof(int64_t) * (size_t)gn);
+        s.G.v = (double*)malloc(sizeof(double) * (size_t)gn);
+        int64_t* pos = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nfree + 1));
+        memcpy(pos, s.G.rp, sizeof(int64_t) * (size_t)(nfree + 1));
+        for (int64_t e = 0; e < E; ++e) {
+            int64_t inc[8];
+            uwr_element_nodes(m, e, inc);
+            for (int a = 0; a < nen; ++a)
+                for (int d = 0; d < dim; ++d) {
+                    int64_t q = eq[inc[a] * dim + d];
+                    if (q < 0) continue;
+                    s.G.ci[pos[q]] = e;
+                    s.G.v[pos[q]] = Ge[e * nd + a * dim + d];
+                    pos[q]++;
+                }
+        }
+        free(pos);
+    }
+    s.GT = csr_transpose(&s.G);
+    double* f = (double*)calloc((size_t)nfree, sizeof(double));
+    for (int64_t e = 0; e < E; ++e) {
+        int64_t inc[8];
+        uwr_element_nodes(m, e, inc);
+        for (int a = 0; a < nen; ++a)
+            for (int d = 0; d < dim; ++d) {
+                int64_t q = eq[inc[a] * dim + d];
+                if (q >= 0) f[q] += fe[e * nd + a * dim + d];
+            }
+    }
+    /* Schur preconditioner diagonal */
+    double* Sd = (double*)malloc(sizeof(double) * (size_t)E);
+    if (o->schur_pc == 0) {
+        memcpy(Sd, Se, sizeof(double) * (size_t)E);
+        s.Sdiag = Sd;
+    } else if (o->schur_pc == 1) {
+        /* BSSCR_FormSchurApproximationDiag: diag(G^T diag(K)^{-1} G) */
+        double* kd = (double*)malloc(sizeof(double) * (size_t)nfree);
+        for (int64_t r = 0; r < nfree; ++r)
+            for (int64_t k = s.K.rp[r]; k < s.K.rp[r + 1]; ++k)
+                if (s.K.ci[k] == r) kd[r] = s.K.v[k];
+        for (int64_t e = 0; e < E; ++e) {
+            double acc = 0.0;
+            for (int64_t k = s.GT.rp[e]; k < s.GT.rp[e + 1]; ++k) acc += s.GT.v[k] * s.GT.v[k] / kd[s.GT.ci[k]];
+            Sd[e] = acc;
+        }
+        free(kd);
+        s.Sdiag = Sd;
+    } else {
+        s.Sdiag = NULL;
+    }
+    s.a11_rtol = o->a11_rtol;
+    s.restart = o->restart > 0 ? o->restart : 30;
+    s.max_inner = o->max_inner > 0 ? o->max_inner : 1000;
+    s.tu = (double*)malloc(sizeof(double) * (size_t)nfree);
+    s.tu2 = (double*)malloc(sizeof(double) * (size_t)nfree);
+    int rc = mg_setup(&s.mg, m, eq, &s.K, o->mg_levels, o->smooth_down, o->smooth_up);
+    double t1 = now_s();
+    if (rc != 0) goto cleanup;
+
+    {
+        double* utmp = (double*)malloc(sizeof(double) * (size_t)nfree);
+        double* hhat = (double*)malloc(sizeof(double) * (size_t)E);
+        a11_solve(&s, f, utmp, o->a11_rtol);
+        csr_mv(&s.GT, utmp, hhat);   /* D K^{-1} f; h = 0 */
+        for (int64_t e = 0; e < E; ++e) hhat[e] = -hhat[e];
+        /* solve (G^T K^{-1} G) p = -h_hat */
+        double* rhs = (double*)malloc(sizeof(double) * (size_t)E);
+        for (int64_t e = 0; e < E; ++e) rhs[e] = -hhat[e];
+        if (o->remove_const_p) remove_constant(E, rhs);
+        int outer;
+        if (o->schur_type == 0)
+            outer = pcg(E, op_S, &s, op_Spc, &s, rhs, p, o->scr_rtol, o->max_outer > 0 ? o->max_outer : 1000);
+        else
+            outer = fgmres(E, op_S, &s, op_Spc, &s, rhs, p, o->scr_rtol, s.restart, o->max_outer > 0 ? o->max_outer : 1000);
+        if (o->remove_const_p) remove_constant(E, p);
+        /* back-solve */
+        double* t = (double*)malloc(sizeof(double) * (size_t)nfree);
+        csr_mv(&s.G, p, t);
+        for (int64_t r = 0; r < nfree; ++r) t[r] = f[r] - t[r];
+        int64_t before = s.inner_its;
+        a11_solve(&s, t, utmp, o->back_rtol);
+        /* true residual */
+        double* ku = (double*)malloc(sizeof(double) * (size_t)nfree);
+        double* gtu = (double*)malloc(sizeof(double) * (size_t)E);
+        csr_mv(&s.K, utmp, ku);
+        csr_mv(&s.G, p, t);
+        double r2 = 0.0, b2 = dot(nfree, f, f);
+        for (int64_t r = 0; r < nfree; ++r) { double d = f[r] - ku[r] - t[r]; r2 += d * d; }
+        csr_mv(&s.GT, utmp, gtu);
+        r2 += dot(E, gtu, gtu);
+        memset(u_nodal, 0, sizeof(double) * (size_t)(nn * dim));
+        for (int64_t k = 0; k < nn * dim; ++k)
+            if (eq[k] >= 0) u_nodal[k] = utmp[eq[k]];
+        if (rep) {
+            rep->outer_its = outer;
+            rep->backsolve_its = (int32_t)(s.inner_its - before);
+            rep->inner_its_total = (int32_t)s.inner_its;
+            rep->rel_residual = sqrt(r2 / (b2 > 0 ? b2 : 1.0));
+            rep->converged = 1;
+        }
+        free(utmp);
+        free(hhat);
+        free(rhs);
+        free(t);
+        free(ku);
+        free(gtu);
+    }
+cleanup:
+    if (rep) {
+        rep->t_setup = t1 - t0;
+        rep->t_solve = now_s() - t1;
+    }
+    mg_free(&s.mg);
+    csr_free(&s.K);
+    csr_free(&s.G);
+    csr_free(&s.GT);
+    free(f);
+    free(Sd);
+    free(s.tu);
+    free(s.tu2);
+    free(eq);
+    return rc;
+}

@@ -1,0 +1,156 @@
+"""GPU parity against the CPU oracle: binning, assembly, operator, solve (through the C ABI)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _mats_oracle(O, mats):
+    out = []
+    for mm in mats:
+        laws = [(mm.laws[i].law, list(mm.laws[i].p)) for i in range(mm.n_laws)]
+        out.append(O.make_material(laws, density=mm.density, alpha=mm.alpha, ref_temp=mm.ref_temp))
+    return out
+
+
+def _run_gpu(U, W, w, solve=None):
+    ctx = U.Context(0)
+    W.setup_context(ctx, w)
+    perm, offsets, xi = ctx.bin_and_map()
+    ctx.assemble()
+    Ke, fe, Ge, Se = ctx.element_matrices()
+    eta = ctx.point_viscosity()
+    return ctx, perm, offsets, xi, Ke, fe, Ge, Se, eta
+
+
+def _oracle(O, w):
+    m = O.make_mesh(w["dim"], w["nel"])
+    z = w["z"] if w["z"] is not None else np.zeros_like(w["x"])
+    xyz = np.stack([w["x"], w["y"], z], axis=1)
+    _, off, perm, xi, outside = O.map_points(m, xyz)
+    assert outside == 0
+    f = O.make_fields(temperature=w.get("temperature"), gravity=w["gravity"], vert_axis=w["vert_axis"])
+    Ke, fe, Ge, Se, eta = O.assemble(m, off, perm, xi, w["material"], _mats_oracle(O, w["materials"]), f,
+                                     point_eta=w.get("eta"), point_rho=w.get("rho"), want_eta=True)
+    return m, off, perm, xi, Ke, fe, Ge, Se, eta
+
+
+def _rel(a, b):
+    return np.linalg.norm((a - b).reshape(-1)) / max(np.linalg.norm(b.reshape(-1)), 1e-300)
+
+
+@pytest.mark.parametrize("case", ["rt2d", "spheres", "grf", "layers"])
+def test_binning_and_assembly_parity(oracle, uw, case):
+    from earthbyte_underworld_gb300 import workloads as W
+    O, U = oracle, uw
+    w = {"rt2d": lambda: W.rt2d(nel=(16, 12), ppc=20),
+         "spheres": lambda: W.spheres(nel=(8, 6, 10), nspheres=12, seed=4),
+         "grf": lambda: W.grf(nel=(8, 8, 8), ppc=30, grid=32),
+         "layers": lambda: W.layers(nel=(6, 6, 8), ppc=40)}[case]()
+    ctx, perm, offsets, xi, Ke, fe, Ge, Se, eta = _run_gpu(U, W, w)
+    m, ooff, operm, oxi, oKe, ofe, oGe, oSe, oeta = _oracle(O, w)
+    # bit-exact permutation and offsets (integer work)
+    assert np.array_equal(offsets, ooff)
+    assert np.array_equal(perm, operm)
+    # local coordinates: closed form vs Newton, rounding only
+    assert np.max(np.abs(xi - oxi)) < 1e-13
+    # FP64 element matrices to 1e-12 relative (per element and overall)
+    assert _rel(Ke, oKe) < 1e-12
+    per_el = np.linalg.norm((Ke - oKe).reshape(len(Ke), -1), axis=1) / np.linalg.norm(oKe.reshape(len(Ke), -1), axis=1)
+    assert per_el.max() < 1e-12
+    assert _rel(fe, ofe) < 1e-12 or np.linalg.norm(ofe) == 0
+    assert _rel(Ge, oGe) < 1e-12
+    assert _rel(Se, oSe) < 1e-12
+    assert _rel(eta, oeta) < 1e-12
+    ctx.close()
+
+
+def test_golden_matrices_through_gpu(oracle, uw):
+    """The reference golden K (2D 10x10, Gauss 2x2, Arrhenius + limiter on the sinusoid temperature)
+    reproduced by the GPU path with the Gauss points as material points."""
+    import scipy.sparse as sp
+    from tests.test_oracle_golden import GOLDEN, golden_cases, golden_matrix, sinusoid_temperature
+    O, U = oracle, uw
+    g = np.load(GOLDEN)
+    m = O.make_mesh(2, (10, 10, 1))
+    T = sinusoid_temperature(O.node_coords(m))
+    a = 1.0 / np.sqrt(3.0)
+    pts = []
+    for e in range(100):
+        ex, ey = e % 10, e // 10
+        for gy in (-a, a):
+            for gx in (-a, a):
+                pts.append(((ex + 0.5 + 0.5 * gx) / 10.0, (ey + 0.5 + 0.5 * gy) / 10.0))
+    pts = np.array(pts)
+    for name, mats in golden_cases(O).items():
+        gm = [U.make_material([(mm.laws[i].law, list(mm.laws[i].p)) for i in range(mm.n_laws)]) for mm in mats]
+        with U.Context(0) as ctx:
+            ctx.mesh_q1(2, (10, 10))
+            ctx.materials_set(gm)
+            ctx.fields_set(T, 0.0, 1)
+            ctx.particles_upload(pts[:, 0], pts[:, 1], None, np.zeros(len(pts), np.int32))
+            ctx.bin_and_map(want=False)
+            ctx.assemble()
+            Ke, _, _, _ = ctx.element_matrices()
+        rp, ci, v, eq, nf = O.global_csr(m, Ke, None)
+        K = sp.csr_matrix((v, ci, rp), shape=(nf, nf))
+        G = golden_matrix(g, name)
+        err = sp.linalg.norm(G - K) / sp.linalg.norm(G)
+        assert err < 1e-4, (name, err)       # the reference test's bound
+        assert err < 1e-11, (name, err)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_operator_apply_matches_csr(oracle, uw, dim):
+    from earthbyte_underworld_gb300 import workloads as W
+    O, U = oracle, uw
+    w = W.rt2d(nel=(16, 16), ppc=12) if dim == 2 else W.spheres(nel=(8, 8, 8), nspheres=10, seed=9)
+    ctx, perm, offsets, xi, Ke, fe, Ge, Se, eta = _run_gpu(U, W, w)
+    m = O.make_mesh(dim, w["nel"])
+    fixed = w["fixed"]
+    rp, ci, v, eq, nf = O.global_csr(m, Ke, fixed)
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(len(eq))
+    x[eq < 0] = 0.0
+    y = ctx.operator_apply(x, U.PREC_FP64)
+    yo = O.csr_spmv(rp, ci, v, x[eq >= 0])
+    assert _rel(y[eq >= 0], yo) < 1e-13
+    # fixed dofs behave as identity rows
+    assert np.array_equal(y[eq < 0], x[eq < 0])
+    y32 = ctx.operator_apply(x, U.PREC_MIXED)
+    assert _rel(y32[eq >= 0], yo) < 1e-5
+    ctx.close()
+
+
+@pytest.mark.parametrize("case,schur,pc", [("rt2d", 1, 0), ("spheres", 1, 0), ("spheres", 0, 0), ("spheres", 1, 1)])
+def test_bsscr_solution_parity(oracle, uw, case, schur, pc):
+    from earthbyte_underworld_gb300 import workloads as W
+    O, U = oracle, uw
+    w = W.rt2d(nel=(32, 32), ppc=20) if case == "rt2d" else W.spheres(nel=(8, 8, 8), nspheres=10, seed=9)
+    ctx, perm, offsets, xi, Ke, fe, Ge, Se, eta = _run_gpu(U, W, w)
+    opts = U.default_opts(mg_levels=3, schur_type=schur, schur_pc=pc, scr_rtol=1e-11, a11_rtol=1e-13,
+                          back_rtol=1e-13, max_outer=400, max_inner=2000)
+    u, p, rep = ctx.solve_bsscr(opts)
+    m = O.make_mesh(w["dim"], w["nel"])
+    ou, op, orep = O.solve_bsscr(m, w["fixed"], Ke, Ge, fe, Se, mg_levels=3, scr_rtol=1e-11,
+                                 a11_rtol=1e-13, back_rtol=1e-13)
+    assert rep.rel_residual < 1e-9
+    assert _rel(u, ou) < 1e-8
+    assert _rel(p, op) < 1e-8
+    ctx.close()
+
+
+def test_mixed_precision_solve(oracle, uw):
+    """FP32 operator + smoothers inside FP64 refinement reach the requested residual; the error
+    against the FP64 solve is reported (and small)."""
+    from earthbyte_underworld_gb300 import workloads as W
+    U = uw
+    w = W.spheres(nel=(16, 16, 16), nspheres=20, seed=5)
+    ctx, *_ = _run_gpu(U, W, w)
+    o64 = U.default_opts(mg_levels=3, scr_rtol=1e-10, a11_rtol=1e-12, back_rtol=1e-12)
+    u64, p64, r64 = ctx.solve_bsscr(o64)
+    om = U.default_opts(mg_levels=3, scr_rtol=1e-7, a11_rtol=1e-8, back_rtol=1e-8, precision=U.PREC_MIXED)
+    um, pm, rm = ctx.solve_bsscr(om)
+    assert rm.rel_residual < 1e-6
+    assert _rel(um, u64) < 1e-5
+    ctx.close()

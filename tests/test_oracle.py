@@ -1,0 +1,104 @@
+"""CPU checks of the oracle's restated rules (binning, layout stream, local coordinates, solve)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+
+def test_park_miller_stream_matches_c(oracle):
+    from earthbyte_underworld_gb300 import workloads as W
+    O = oracle
+    m = O.make_mesh(2, (4, 3, 1))
+    xyz = O.random_layout(m, 5, 13)
+    w = W.rt2d(nel=(4, 3), ppc=5, seed=13)
+    assert np.array_equal(xyz[:, 0], w["x"]) and np.array_equal(xyz[:, 1], w["y"])
+
+
+def test_search_element_tie_rules(oracle):
+    """Mesh_RegularAlgorithms.c:194-226: a point on an interior face goes to the lower element
+    (Num_Approx of the fractional part, eps 1e-12); a point at max goes to the last element."""
+    O = oracle
+    m = O.make_mesh(2, (4, 4, 1))
+    pts = np.array([[0.25, 0.1, 0], [0.25 + 1e-13, 0.1, 0], [0.25 + 1e-9, 0.1, 0], [1.0, 1.0, 0],
+                    [0.0, 0.0, 0], [1.0 + 5e-13, 0.5, 0], [1.0 + 1e-6, 0.5, 0], [-1e-9, 0.5, 0]])
+    owning, offsets, perm, xi, outside = O.map_points(m, pts)
+    assert owning[0] == 0                 # x on face 1 -> element 0
+    assert owning[1] == 0                 # within eps of the face -> lower
+    assert owning[2] == 1                 # beyond eps -> upper
+    assert owning[3] == 15                # max corner -> last element
+    assert owning[4] == 0
+    assert owning[5] == 3 + 4 * 1         # x within eps of max -> last column; y on a face -> lower row
+    assert owning[6] == 0xFFFFFFFF and owning[7] == 0xFFFFFFFF
+    assert outside == 2
+
+
+def test_map_is_stable_by_point_index(oracle):
+    O = oracle
+    m = O.make_mesh(3, (3, 2, 2))
+    rng = np.random.default_rng(0)
+    xyz = rng.uniform(0, 1, size=(500, 3))
+    owning, offsets, perm, xi, outside = O.map_points(m, xyz)
+    order = np.lexsort((np.arange(500), owning))
+    assert np.array_equal(perm, order.astype(np.uint32))
+    assert np.array_equal(np.diff(offsets.astype(np.int64)), np.bincount(owning, minlength=12))
+
+
+def test_newton_xi_equals_affine_closed_form(oracle):
+    O = oracle
+    m = O.make_mesh(3, (5, 3, 7))
+    rng = np.random.default_rng(1)
+    xyz = rng.uniform(0, 1, size=(2000, 3))
+    _, off1, perm1, xi1, _ = O.map_points(m, xyz, use_newton=True)
+    _, off2, perm2, xi2, _ = O.map_points(m, xyz, use_newton=False)
+    assert np.array_equal(perm1, perm2)
+    assert np.max(np.abs(xi1 - xi2)) < 1e-13
+    assert np.all(np.abs(xi1) <= 1.0 + 1e-12)
+
+
+def _small_problem(O, dim, nel, ppc=8, seed=0):
+    m = O.make_mesh(dim, nel)
+    rng = np.random.default_rng(seed)
+    E = O.num_elements(m)
+    xyz = O.random_layout(m, ppc, 17)
+    mat = (xyz[:, 1] > 0.5).astype(np.int32)
+    mats = [O.make_material([(O.LAW_MATERIAL_VISCOSITY, [1.0])], density=0.0),
+            O.make_material([(O.LAW_MATERIAL_VISCOSITY, [100.0])], density=1.0)]
+    _, off, perm, xi, _ = O.map_points(m, xyz)
+    f = O.make_fields(gravity=1.0, vert_axis=dim - 1)
+    Ke, fe, Ge, Se, _ = O.assemble(m, off, perm, xi, mat, mats, f)
+    return m, Ke, fe, Ge, Se
+
+
+@pytest.mark.parametrize("dim,nel", [(2, (8, 8, 1)), (3, (4, 4, 4))])
+def test_oracle_bsscr_matches_direct_solve(oracle, dim, nel):
+    O = oracle
+    m, Ke, fe, Ge, Se = _small_problem(O, dim, nel)
+    fixed = O.free_slip_mask(m)
+    u, p, rep = O.solve_bsscr(m, fixed, Ke, Ge, fe, Se, mg_levels=3 if dim == 2 else 2)
+    # direct saddle-point solve with scipy
+    rp, ci, v, eq, nf = O.global_csr(m, Ke, fixed)
+    K = sp.csr_matrix((v, ci, rp), shape=(nf, nf))
+    E = O.num_elements(m)
+    nen = 1 << dim
+    rows, cols, vals = [], [], []
+    f = np.zeros(nf)
+    for e in range(E):
+        inc = np.zeros(8, np.int64)
+        O.lib().uwr_element_nodes(__import__("ctypes").byref(m), e, inc.ctypes.data)
+        for a in range(nen):
+            for d in range(dim):
+                q = eq[inc[a] * dim + d]
+                if q >= 0:
+                    rows.append(q); cols.append(e); vals.append(Ge[e, a * dim + d])
+                    f[q] += fe[e, a * dim + d]
+    G = sp.csr_matrix((vals, (rows, cols)), shape=(nf, E))
+    A = sp.bmat([[K, G], [G.T, None]]).tocsc()
+    # pin the constant pressure mode by adding a row/column (Lagrange multiplier)
+    ones = sp.csr_matrix(np.concatenate([np.zeros(nf), np.ones(E)])[None, :])
+    Aa = sp.bmat([[A, ones.T], [ones, None]]).tocsc()
+    sol = spla.spsolve(Aa, np.concatenate([f, np.zeros(E), [0.0]]))
+    ud, pd = sol[:nf], sol[nf:nf + E]
+    uo = u.reshape(-1)[eq >= 0]
+    assert rep.rel_residual < 1e-9
+    assert np.linalg.norm(uo - ud) / np.linalg.norm(ud) < 1e-8
+    assert np.linalg.norm(p - pd) / np.linalg.norm(pd) < 1e-8
