@@ -1,0 +1,405 @@
+#!/usr/bin/env python
+"""Benchmark of the particle-in-cell Stokes hot path on one GB300 (replicas on N GPUs).
+
+One step = one pass of the hot path over the resident material points:
+    binning + integration-point mapping  ->  rheology + element assembly  ->  BSSCR Stokes
+    solve (Schur-complement FGMRES, A11 FGMRES + 4-level geometric multigrid) to a
+    relative residual of 1e-6.
+Workload (default): 3D Q1-P0 Stokes, 64^3 elements, 27 points per element on a jittered grid,
+50 seeded spheres (viscosity 10^U(-2,3), density U(0,1)), free-slip walls, FP64.
+
+Arms:
+  (default)          this library through its C ABI (ctypes)
+  --impl reference   the reference algorithm restated in C (oracle/uwref.c), timed on the
+                     host cores on a bounded sample of the same workload
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Stokes solve s to 1e-6 rel. residual, mixed+learned vs FP64 GPU; particles/s"
+UNIT = "particles/s"
+
+# DRAM bytes per stencil row measured by ncu for the FP64 / FP32 colour Gauss-Seidel kernel
+# (profiles/gs_colour_spheres.md); scaled by the rows a launch relaxes.
+NCU_TRAFFIC_PER_ROW = {"fp64": None, "fp32": None}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nel", type=int, default=64)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision comparison")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-nel", type=int, default=16, help="mesh of the CPU baseline sample")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self, world, local, use_cuda=True):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if use_cuda and torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            dist.init_process_group(backend=backend)
+            self.dist = dist
+            self.torch = torch
+            self.device = torch.device("cuda", local) if backend == "nccl" else torch.device("cpu")
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, v):
+        if self.world == 1:
+            return v
+        t = self.torch.tensor([float(v)], device=self.device, dtype=self.torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if self.world == 1:
+            return v
+        t = self.torch.tensor([float(v)], device=self.device, dtype=self.torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while running (SM clock, max clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def make_workload(nel, shuffle=True):
+    from earthbyte_underworld_gb300 import workloads as W
+    return W.spheres(nel=(nel, nel, nel), nspheres=50, seed=2024, shuffle=shuffle)
+
+
+# BSSCR options: FGMRES Schur iteration (-scr_ksp_type fgmres) with the scaled BFBt Schur preconditioner
+# (-Q22_pc_type gtkg, Solvers/KSPSolvers/src/BSSCR/pc_ScaledGtKG.c) and FGMRES velocity solves
+# (-A11_ksp_type fgmres, Solvers/SysTest/ConvergenceTests/options-solv-mg.opt); tolerances chosen so
+# that the full Stokes residual reaches 1e-6
+SOLVE_KW = dict(mg_levels=4, smooth_down=2, smooth_up=2, schur_type=1, schur_pc=3, scr_rtol=1e-7, a11_rtol=1e-6,
+                back_rtol=1e-7, restart=30, max_outer=500, max_inner=2000, bfbt_rtol=1e-4, bfbt_max_it=2000)
+
+
+# ------------------------------------------------------------------------------------------
+# CPU leg: the restated reference path on the host cores
+# ------------------------------------------------------------------------------------------
+def cpu_step(O, w, nthreads):
+    import numpy as np
+    m = O.make_mesh(3, w["nel"])
+    xyz = np.stack([w["x"], w["y"], w["z"]], axis=1)
+    t0 = time.perf_counter()
+    _, off, perm, xi, _ = O.map_points(m, xyz)
+    mats = [O.make_material([(mm.laws[0].law, list(mm.laws[0].p))], density=mm.density) for mm in w["materials"]]
+    f = O.make_fields(gravity=w["gravity"], vert_axis=w["vert_axis"])
+    Ke, fe, Ge, Se, _ = O.assemble(m, off, perm, xi, w["material"], mats, f, nthreads=nthreads)
+    t1 = time.perf_counter()
+    levels = 3 if w["nel"][0] % 4 == 0 else 2
+    u, p, rep = O.solve_bsscr(m, w["fixed"], Ke, Ge, fe, Se, mg_levels=levels, smooth=2,
+                              schur_type=SOLVE_KW["schur_type"], schur_pc=SOLVE_KW["schur_pc"],
+                              scr_rtol=SOLVE_KW["scr_rtol"], a11_rtol=SOLVE_KW["a11_rtol"],
+                              back_rtol=SOLVE_KW["back_rtol"], bfbt_rtol=SOLVE_KW["bfbt_rtol"],
+                              bfbt_max_it=SOLVE_KW["bfbt_max_it"], nthreads=nthreads)
+    t2 = time.perf_counter()
+    return t2 - t0, t1 - t0, rep
+
+
+def cpu_baseline(nel, nthreads):
+    from oracle import oracle as O
+    O.lib()
+    w = make_workload(nel)
+    dt, dt_asm, rep = cpu_step(O, w, nthreads)
+    n = w["x"].shape[0]
+    return {"value": n / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"spheres workload at {nel}^3 elements ({n} points, 27/element, 50 spheres), one full "
+                      f"step: map + assemble + BSSCR to 1e-6 (oracle/uwref.c, OpenMP); assembly part "
+                      f"{n / dt_asm:.3e} points/s; solve residual {rep.rel_residual:.1e}",
+            "step_s": dt}
+
+
+def run_reference(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    O.lib()
+    nthreads = os.cpu_count() or 1
+    w = make_workload(args.cpu_nel)
+    n = w["x"].shape[0]
+    for _ in range(args.warmup):
+        cpu_step(O, w, nthreads)
+    times = []
+    res = None
+    for _ in range(args.steps):
+        dt, _, rep = cpu_step(O, w, nthreads)
+        times.append(dt)
+        res = rep.rel_residual
+    tot = sum(times)
+    value = n * args.steps / tot
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"stokes3d_spheres_{args.cpu_nel}cube_27ppc (bounded sample of the 64^3 workload)",
+                      "precision": "fp64", "solver": "BSSCR: Schur FGMRES(scaled BFBt) / A11 FGMRES + GMG (SOR 2+2)", "rel_residual": res},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                            "sample": f"{args.cpu_nel}^3 elements, {n} points, full step per iteration"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from earthbyte_underworld_gb300 import uwgpu as U
+    from earthbyte_underworld_gb300 import workloads as W
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    dist = Dist(world, local)
+    nel = args.nel
+    w = make_workload(nel)
+    npts = w["x"].shape[0]
+    ctx = U.Context(local)
+    W.setup_context(ctx, w)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    flush_buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
+
+    def opts_for(prec):
+        return U.default_opts(precision=U.PREC_MIXED if prec == "mixed" else U.PREC_FP64, **SOLVE_KW)
+
+    def step(opts):
+        ctx.bin_and_map(want=False)
+        ctx.assemble()
+        _, _, rep = ctx.solve_bsscr(opts, want=False)
+        return rep
+
+    def timed(opts, profile):
+        for _ in range(args.warmup):
+            step(opts)
+        torch.cuda.synchronize()
+        dist.barrier()
+        torch.cuda.synchronize()
+        if profile:
+            ctx.profile_enable(True)
+        launches0 = ctx.launch_count()
+        clocks = ClockSampler(local)
+        clocks.start()
+        ev = []
+        reps = []
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush_buf.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            reps.append(step(opts))
+            e1.record(stream)
+            ev.append((e0, e1))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+        clk = clocks.stop()
+        dist.barrier()
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev)
+        launches = ctx.launch_count() - launches0
+        prof = {}
+        if profile:
+            for name, fam in (("assembly", U.KERNEL_ASSEMBLY), ("apply", U.KERNEL_APPLY),
+                              ("smooth", U.KERNEL_SMOOTH), ("binning", U.KERNEL_BINNING)):
+                n, t = ctx.profile_read(fam)
+                b, f = ctx.profile_work(fam)
+                prof[name] = {"launches": n, "ms": t, "bytes": b, "flops": f}
+            ctx.profile_enable(False)
+        return ms, wall, launches, reps, clk, prof
+
+    prec = args.precision
+    ms, wall, launches, reps, clk, prof = timed(opts_for(prec), profile=True)
+    ms_max = dist.max(ms)
+    step_ms = ms_max / args.steps
+    value = dist.sum(npts) / (ms_max / 1e3 / args.steps)
+    rep = reps[-1]
+
+    # roofline of the dominant kernel family
+    peak, peak_kind = measured_peaks()
+    dom = max(prof, key=lambda k: prof[k]["ms"])
+    d = prof[dom]
+    achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9 if d["ms"] > 0 else 0.0
+    fp64_tflops = d["flops"] / (d["ms"] / 1e3) / 1e12 if d["ms"] > 0 else 0.0
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if peak else None, "traffic": None, "kernel": dom,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
+                "avg_launch_us": 1e3 * d["ms"] / max(d["launches"], 1),
+                "algorithmic_bytes_per_launch": d["bytes"] / max(d["launches"], 1),
+                "fp_tflops": fp64_tflops,
+                "note": "algorithmic bytes: stencil blocks, diagonal inverse, rhs and the relaxed rows "
+                        "moved once per launch; FP64 kernels on this part are also limited by its "
+                        "1.2 TFLOP/s FP64 rate (fp_tflops)"}
+    kernels = {k: {"launches": v["launches"], "ms": v["ms"],
+                   "GB_per_s": v["bytes"] / (v["ms"] / 1e3) / 1e9 if v["ms"] > 0 else None,
+                   "TFLOP_per_s": v["flops"] / (v["ms"] / 1e3) / 1e12 if v["ms"] > 0 else None}
+               for k, v in prof.items()}
+
+    # mixed-precision form on the same workload
+    mixed = None
+    if not args.no_mixed and prec == "fp64":
+        ms2, wall2, l2, reps2, clk2, _ = timed(opts_for("mixed"), profile=False)
+        ms2 = dist.max(ms2)
+        mixed = {"value": dist.sum(npts) / (ms2 / 1e3 / args.steps), "ms_per_step": ms2 / args.steps,
+                 "stokes_solve_s": reps2[-1].t_solve_ms / 1e3, "rel_residual": reps2[-1].rel_residual,
+                 "outer_its": reps2[-1].outer_its, "inner_its": reps2[-1].inner_its_total,
+                 "speedup_vs_fp64": (ms_max / args.steps) / (ms2 / args.steps)}
+
+    # end to end through the public API with host buffers (pinned)
+    xs = torch.from_numpy(w["x"]).pin_memory().numpy()
+    ys = torch.from_numpy(w["y"]).pin_memory().numpy()
+    zs = torch.from_numpy(w["z"]).pin_memory().numpy()
+    ms_ = torch.from_numpy(w["material"]).pin_memory().numpy()
+    nn = ctx.nnodes
+    ne = ctx.nelements
+    e2e_times = []
+    opts = opts_for(prec)
+    for it in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.particles_upload(xs, ys, zs, ms_)
+        ctx.bin_and_map(want=False)
+        ctx.assemble()
+        u, p, _ = ctx.solve_bsscr(opts, want=True)
+        torch.cuda.synchronize()
+        if it >= args.warmup:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_s = dist.max(sum(e2e_times))
+    e2e = {"value": dist.sum(npts) / (e2e_s / args.steps), "unit": UNIT,
+           "h2d_bytes_per_step": int(npts * (3 * 8 + 4)), "d2h_bytes_per_step": int(nn * 3 * 8 + ne * 8)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            cpu = cpu_baseline(args.cpu_nel, os.cpu_count() or 1)
+        except Exception as ex:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {ex}"}
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32/f64", "data": "synthetic",
+               "config": {"workload": f"stokes3d_spheres_{nel}cube_27ppc_50spheres", "elements": ne,
+                          "points": npts, "precision": prec, "mg_levels": SOLVE_KW["mg_levels"],
+                          "solver": "BSSCR: Schur FGMRES(scaled BFBt) / A11 FGMRES + GMG (colour block-GS 2+2)",
+                          "target_rel_residual": 1e-6, "rel_residual": rep.rel_residual,
+                          "outer_its": rep.outer_its, "inner_its": rep.inner_its_total, "vcycles": rep.vcycles,
+                          "stokes_solve_s": rep.t_solve_ms / 1e3, "setup_ms": rep.t_setup_ms,
+                          "l2": "256 MB buffer written between timed steps", "parallelism": f"replicas x{world}"},
+               "roofline": roofline, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
+               "gpu_launches": int(launches), "clocks": clk, "mixed": mixed,
+               "wall_s_timed": wall}
+        print(json.dumps(out), flush=True)
+    ctx.close()
+    dist.close()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

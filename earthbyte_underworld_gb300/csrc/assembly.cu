@@ -554,6 +554,12 @@ void assemble(Context& c) {
     A.eta_out = c.seta_out.p;
     A.flags = c.err_count.p;
     {
+        // algorithmic bytes: per point xi + material (+ optional inputs) read, viscosity written;
+        // per element offsets read, packed K_e, f_e, G_e, S_e written
+        double per_point = dim * 8.0 + 4.0 + 8.0 + (c.has_peta ? 8.0 : 0.0) + (c.has_prho ? 8.0 : 0.0);
+        double per_el = 4.0 + packed_size(nd) * 8.0 + 2.0 * nd * 8.0 + 8.0;
+        double flops_point = dim == 3 ? 120.0 : 50.0, flops_el = dim == 3 ? 3600.0 : 300.0;
+        note_work(c, UWGPU_KERNEL_ASSEMBLY, per_point * c.np + per_el * ne, flops_point * c.np + flops_el * ne);
         LaunchScope ls(c, UWGPU_KERNEL_ASSEMBLY);
         if (dim == 3)
             k_assemble<3><<<blocks_for(ne, 128), 128, 0, c.stream>>>(A);

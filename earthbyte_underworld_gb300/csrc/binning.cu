@@ -267,6 +267,16 @@ void bin_and_map(Context& c) {
     UWG_CUDA(cudaMemsetAsync(c.counts.p, 0, ne * sizeof(uint32_t), c.stream));
     UWG_CUDA(cudaMemsetAsync(c.cursor.p, 0, ne * sizeof(uint32_t), c.stream));
     UWG_CUDA(cudaMemsetAsync(c.err_count.p, 0, sizeof(uint32_t), c.stream));
+    {
+        // algorithmic bytes of the whole binning pass: per point coordinates read twice (locate,
+        // map), cell id written/read, count/cursor atomics, unordered and final permutation,
+        // material in, xi and material out (+ optional per-point inputs); per element counts,
+        // cursor and offsets
+        int dim = c.mesh.dim;
+        double extra = (c.has_peta ? 16.0 : 0.0) + (c.has_prho ? 16.0 : 0.0);
+        double per_point = 2 * dim * 8.0 + 8.0 + 16.0 + 12.0 + 8.0 + dim * 8.0 + extra;
+        note_work(c, UWGPU_KERNEL_BINNING, per_point * np + 20.0 * ne, 0.0);
+    }
     if (np > 0) {
         LaunchScope ls(c, UWGPU_KERNEL_BINNING);
         if (c.mesh.dim == 3)

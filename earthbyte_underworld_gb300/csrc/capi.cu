@@ -318,7 +318,7 @@ void uwgpu_solve_opts_default(uwgpu_solve_opts* o) {
     o->mg_levels = 4;
     o->smooth_down = 2;
     o->smooth_up = 2;
-    o->schur_type = UWGPU_SCHUR_FGMRES;
+    o->schur_type = UWGPU_SCHUR_CG;
     o->schur_pc = UWGPU_SCHUR_PC_UW;
     o->restart = 30;
     o->max_outer = 500;
@@ -329,6 +329,8 @@ void uwgpu_solve_opts_default(uwgpu_solve_opts* o) {
     o->remove_const_p = 1;
     o->precision = UWGPU_PREC_FP64;
     o->target_rel_residual = 0.0;
+    o->bfbt_rtol = 1e-2;
+    o->bfbt_max_it = 500;
 }
 
 int uwgpu_solve_bsscr(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, double* u, double* p, uwgpu_report* report) {
@@ -361,6 +363,8 @@ int uwgpu_profile_enable(uwgpu_ctx* ctx, int32_t on) {
             f.used = 0;
             f.launches = 0;
             f.ms = 0.0;
+            f.bytes = 0.0;
+            f.flops = 0.0;
         }
         c.profiling = on != 0;
     });
@@ -384,6 +388,21 @@ int uwgpu_profile_read(uwgpu_ctx* ctx, int32_t which, int64_t* launches, double*
     });
 }
 
+int uwgpu_profile_read_work(uwgpu_ctx* ctx, int32_t which, double* bytes, double* flops) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(which >= 0 && which < UWGPU_KERNEL_COUNT, UWGPU_ERR_ARGUMENT, "bad kernel family");
+        if (bytes) *bytes = c.prof[which].bytes;
+        if (flops) *flops = c.prof[which].flops;
+    });
+}
+
 int64_t uwgpu_launch_count(const uwgpu_ctx* ctx) { return ctx ? ctx->c.launches : 0; }
+
+int uwgpu_get_stream(uwgpu_ctx* ctx, void** stream) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(stream, UWGPU_ERR_ARGUMENT, "null output");
+        *stream = (void*)c.stream;
+    });
+}
 
 }  // extern "C"

@@ -101,6 +101,8 @@ struct ProfileFamily {
     size_t used = 0;
     int64_t launches = 0;
     double ms = 0.0;
+    double bytes = 0.0;   // algorithmic bytes of the profiled launches
+    double flops = 0.0;
 };
 
 struct Context {
@@ -190,6 +192,14 @@ struct LaunchScope {
         if (e1) cudaEventRecord(e1, c.stream);
     }
 };
+
+// Records the algorithmic work of one launch of `family` while profiling.
+inline void note_work(Context& c, int family, double bytes, double flops) {
+    if (c.profiling && family >= 0) {
+        c.prof[family].bytes += bytes;
+        c.prof[family].flops += flops;
+    }
+}
 
 inline void check_launch(const char* what) {
     cudaError_t e = cudaGetLastError();

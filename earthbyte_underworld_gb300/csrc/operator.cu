@@ -18,7 +18,11 @@
 // stencil coupling inside a colour, so a colour is relaxed in parallel without atomics.
 // Coarse element matrices are formed element by element (P_c^T K_c P_c over the 2^dim children),
 // which equals the Galerkin product for this interpolation.
+#include <cooperative_groups.h>
+
 #include "internal.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace uwg {
 
@@ -209,16 +213,10 @@ __global__ void __launch_bounds__(256) k_residual(Grid g, const T* __restrict__ 
     for (int q = 0; q < DIM; ++q) r[(int64_t)q * g.nn + n] = b[(int64_t)q * g.nn + n] - out[q];
 }
 
-// One colour of block Gauss-Seidel: x_n += Dinv_n (b_n - (A x)_n) for nodes of parity `colour`.
+// Block Gauss-Seidel on one node: x_n += Dinv_n (b_n - (A x)_n).
 template <int DIM, typename T>
-__global__ void __launch_bounds__(256) k_gs_colour(Grid g, int colour, const T* __restrict__ A, const T* __restrict__ Dinv,
-                                                   const T* __restrict__ b, T* __restrict__ x) {
-    int px = colour & 1, py = (colour >> 1) & 1, pz = (colour >> 2) & 1;
-    int64_t cx = (g.nx - px + 1) / 2, cy = (g.ny - py + 1) / 2;
-    int64_t cz = DIM == 3 ? (g.nz - pz + 1) / 2 : 1;
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= cx * cy * cz) return;
-    int64_t i = 2 * (t % cx) + px, j = 2 * ((t / cx) % cy) + py, k = DIM == 3 ? 2 * (t / (cx * cy)) + pz : 0;
+__device__ __forceinline__ void gs_relax_node(const Grid& g, int64_t i, int64_t j, int64_t k, const T* __restrict__ A,
+                                              const T* __restrict__ Dinv, const T* __restrict__ b, T* __restrict__ x) {
     int64_t n = i + g.nx * (j + g.ny * k);
     T ax[DIM];
     stencil_row<DIM, T>(g, n, i, j, k, A, x, ax);
@@ -231,6 +229,40 @@ __global__ void __launch_bounds__(256) k_gs_colour(Grid g, int colour, const T* 
 #pragma unroll
         for (int cc = 0; cc < DIM; ++cc) v = fma(Dinv[(int64_t)(r * DIM + cc) * g.nn + n], res[cc], v);
         x[(int64_t)r * g.nn + n] = v;
+    }
+}
+
+constexpr int kGsThreads = 256;
+
+// `sweeps` symmetric multicolour block Gauss-Seidel sweeps (colours ascending, then
+// descending) in one cooperative launch.  Nodes of one parity colour are never stencil
+// neighbours, so a colour is relaxed in parallel; a grid-wide barrier separates colours.
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kGsThreads) k_gs_sweeps(Grid g, const T* __restrict__ A, const T* __restrict__ Dinv,
+                                                          const T* __restrict__ b, T* __restrict__ x, int sweeps,
+                                                          int zero_init) {
+    cg::grid_group grid = cg::this_grid();
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    if (zero_init) {
+        for (int64_t t = tid; t < g.nn * DIM; t += stride) x[t] = (T)0;
+        grid.sync();
+    }
+    constexpr int NCOL = 1 << DIM;
+    for (int s = 0; s < sweeps; ++s) {
+        for (int step = 0; step < 2 * NCOL; ++step) {
+            int col = step < NCOL ? step : 2 * NCOL - 1 - step;
+            int px = col & 1, py = (col >> 1) & 1, pz = (col >> 2) & 1;
+            int64_t cx = (g.nx - px + 1) / 2, cy = (g.ny - py + 1) / 2;
+            int64_t cz = DIM == 3 ? (g.nz - pz + 1) / 2 : 1;
+            int64_t cnt = cx * cy * cz;
+            for (int64_t t = tid; t < cnt; t += stride) {
+                int64_t i = 2 * (t % cx) + px, j = 2 * ((t / cx) % cy) + py;
+                int64_t k = DIM == 3 ? 2 * (t / (cx * cy)) + pz : 0;
+                gs_relax_node<DIM, T>(g, i, j, k, A, Dinv, b, x);
+            }
+            grid.sync();
+        }
     }
 }
 
@@ -592,6 +624,8 @@ const float* dinv_of<float>(const Level& L) { return L.Dinv32.p; }
 template <typename T>
 void level_apply(Context& c, const Level& L, const T* x, T* y) {
     Grid g = grid_of(L.mesh);
+    int D = g.dim, NB = D == 3 ? 27 : 9;
+    note_work(c, UWGPU_KERNEL_APPLY, (double)g.nn * (NB * D * D + 2 * D) * sizeof(T), 2.0 * g.nn * NB * D * D);
     LaunchScope ls(c, UWGPU_KERNEL_APPLY);
     if (g.dim == 3)
         k_apply<3, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, y);
@@ -602,6 +636,8 @@ void level_apply(Context& c, const Level& L, const T* x, T* y) {
 template <typename T>
 void level_residual(Context& c, const Level& L, const T* x, const T* b, T* r) {
     Grid g = grid_of(L.mesh);
+    int D = g.dim, NB = D == 3 ? 27 : 9;
+    note_work(c, UWGPU_KERNEL_APPLY, (double)g.nn * (NB * D * D + 3 * D) * sizeof(T), 2.0 * g.nn * NB * D * D);
     LaunchScope ls(c, UWGPU_KERNEL_APPLY);
     if (g.dim == 3)
         k_residual<3, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, b, r);
@@ -611,22 +647,35 @@ void level_residual(Context& c, const Level& L, const T* x, const T* b, T* r) {
 
 // symmetric sweep: colours ascending then descending
 template <typename T>
-void level_smooth(Context& c, const Level& L, const T* b, T* x, int sweeps) {
+void level_smooth(Context& c, const Level& L, const T* b, T* x, int sweeps, bool zero_init) {
     Grid g = grid_of(L.mesh);
-    int ncol = 1 << g.dim;
-    for (int s = 0; s < sweeps; ++s) {
-        for (int pass = 0; pass < 2; ++pass)
-            for (int k = 0; k < ncol; ++k) {
-                int col = pass == 0 ? k : ncol - 1 - k;
-                int px = col & 1, py = (col >> 1) & 1, pz = (col >> 2) & 1;
-                int64_t cnt = ((g.nx - px + 1) / 2) * ((g.ny - py + 1) / 2) * (g.dim == 3 ? (g.nz - pz + 1) / 2 : 1);
-                LaunchScope ls(c, UWGPU_KERNEL_SMOOTH);
-                if (g.dim == 3)
-                    k_gs_colour<3, T><<<blocks_for(cnt, 256), 256, 0, c.stream>>>(g, col, stencil_of<T>(L), dinv_of<T>(L), b, x);
-                else
-                    k_gs_colour<2, T><<<blocks_for(cnt, 256), 256, 0, c.stream>>>(g, col, stencil_of<T>(L), dinv_of<T>(L), b, x);
-            }
+    int D = g.dim, NB = D == 3 ? 27 : 9;
+    note_work(c, UWGPU_KERNEL_SMOOTH, (double)sweeps * 2.0 * g.nn * (NB * D * D + D * D + 3 * D) * sizeof(T),
+              (double)sweeps * 2.0 * 2.0 * g.nn * (NB * D * D + D * D));
+    // one cooperative launch runs every colour of every sweep with grid-wide barriers between
+    // colours; the grid is sized so that all of its blocks are resident (a requirement of the
+    // cooperative launch), and each thread strides over the nodes of the current colour.
+    static int max_blocks[2][2] = {{0, 0}, {0, 0}};
+    int di = D == 3 ? 1 : 0, ti = sizeof(T) == 8 ? 1 : 0;
+    void* fn = D == 3 ? (void*)k_gs_sweeps<3, T> : (void*)k_gs_sweeps<2, T>;
+    if (max_blocks[di][ti] == 0) {
+        int per_sm = 0, sms = 0, dev = 0;
+        UWG_CUDA(cudaGetDevice(&dev));
+        UWG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        UWG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kGsThreads, 0));
+        UWG_REQUIRE(per_sm > 0, UWGPU_ERR_CUDA, "smoother kernel cannot be made resident");
+        max_blocks[di][ti] = per_sm * sms;
     }
+    int64_t per_colour = (g.nn + (1 << D) - 1) >> D;
+    int64_t want = (per_colour + kGsThreads - 1) / kGsThreads;
+    int blocks = (int)(want < max_blocks[di][ti] ? want : max_blocks[di][ti]);
+    if (blocks < 1) blocks = 1;
+    const T* A = stencil_of<T>(L);
+    const T* Di = dinv_of<T>(L);
+    int zi = zero_init ? 1 : 0;
+    void* args[] = {(void*)&g, (void*)&A, (void*)&Di, (void*)&b, (void*)&x, (void*)&sweeps, (void*)&zi};
+    LaunchScope ls(c, UWGPU_KERNEL_SMOOTH);
+    UWG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kGsThreads), args, 0, c.stream));
 }
 
 template <typename T>
@@ -659,8 +708,8 @@ template void level_apply<double>(Context&, const Level&, const double*, double*
 template void level_apply<float>(Context&, const Level&, const float*, float*);
 template void level_residual<double>(Context&, const Level&, const double*, const double*, double*);
 template void level_residual<float>(Context&, const Level&, const float*, const float*, float*);
-template void level_smooth<double>(Context&, const Level&, const double*, double*, int);
-template void level_smooth<float>(Context&, const Level&, const float*, float*, int);
+template void level_smooth<double>(Context&, const Level&, const double*, double*, int, bool);
+template void level_smooth<float>(Context&, const Level&, const float*, float*, int, bool);
 template void level_restrict<double>(Context&, const Level&, const Level&, const double*, double*);
 template void level_restrict<float>(Context&, const Level&, const Level&, const float*, float*);
 template void level_prolong_add<double>(Context&, const Level&, const Level&, const double*, double*);
@@ -878,6 +927,274 @@ void gather_force(Context& c, double* f) {
         k_gather_force<3><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, c.fe.p, L.mesh.ne, L.fixed.p, f);
     else
         k_gather_force<2><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, c.fe.p, L.mesh.ne, L.fixed.p, f);
+}
+
+// Scaled BFBt weights W = 1/rowmax(K) per velocity dof (fixed dofs 0), pc_ScaledGtKG.c:735-760
+template <int DIM>
+__global__ void k_rowmax_weights(Grid g, const double* __restrict__ A, const uint8_t* __restrict__ fixed,
+                                 double* __restrict__ W) {
+    constexpr int NB = nblocks<DIM>();
+    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.nn) return;
+#pragma unroll
+    for (int r = 0; r < DIM; ++r) {
+        double mx = -1e300;
+        for (int q = 0; q < NB; ++q)
+#pragma unroll
+            for (int cc = 0; cc < DIM; ++cc) {
+                double v = A[((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n];
+                mx = v > mx ? v : mx;
+            }
+        W[(int64_t)r * g.nn + n] = (fixed && fixed[n * DIM + r]) ? 0.0 : 1.0 / mx;
+    }
+}
+
+// diag(G^T W G) per element (Jacobi preconditioner of the inner BFBt solves)
+template <int DIM>
+__global__ void k_gwg_diag(Grid g, GeoArgs geo, const double* __restrict__ W, double* __restrict__ S) {
+    int64_t ne = (int64_t)g.ex * g.ey * g.ez;
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    int64_t ie = e % g.ex, je = (e / g.ex) % g.ey, ke = DIM == 3 ? e / ((int64_t)g.ex * g.ey) : 0;
+    double h[3];
+    element_h<DIM>(geo, ie, je, ke, h);
+    int64_t base = ie + g.nx * (je + g.ny * ke);
+    double acc = 0.0;
+#pragma unroll
+    for (int a = 0; a < (1 << DIM); ++a) {
+        int64_t n = base + (a & 1) + ((a >> 1) & 1) * g.nx + (DIM == 3 ? ((a >> 2) & 1) * g.nx * g.ny : 0);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            double gv = gval<DIM>(h, a, d);
+            acc += gv * gv * W[(int64_t)d * g.nn + n];
+        }
+    }
+    S[e] = acc;
+}
+
+void bfbt_weights(Context& c, double* W) {
+    const Level& L = c.levels[0];
+    Grid g = grid_of(L.mesh);
+    LaunchScope ls(c, -1);
+    if (g.dim == 3)
+        k_rowmax_weights<3><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, L.A64.p, L.fixed.p, W);
+    else
+        k_rowmax_weights<2><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, L.A64.p, L.fixed.p, W);
+}
+
+// ------------------------------------------------------------------------------------------
+// Device-resident Jacobi-preconditioned CG on G^T W G (the inner solves of the scaled BFBt
+// preconditioner).  The scalars live in device memory (double-buffered by iteration parity),
+// so an iteration is four fused kernels with no host round trip; the host reads the residual
+// norm every few iterations to test convergence.
+//   scal[0] = p.q   scal[1], scal[2] = r.z (parity)   scal[3] = r.r   scal[4] = r0.r0
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum(double v, double* sw) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sw[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sw[w];
+    return t;  // valid in thread 0
+}
+
+// s = W (G p)
+template <int DIM>
+__global__ void k_pcg_gp(Grid g, GeoArgs geo, const double* __restrict__ p, const double* __restrict__ W,
+                         const uint8_t* __restrict__ fixed, double* __restrict__ s) {
+    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.nn) return;
+    int64_t idx[3] = {n % g.nx, (n / g.nx) % g.ny, DIM == 3 ? n / (g.nx * g.ny) : 0};
+    int64_t ecount[3] = {g.ex, g.ey, g.ez};
+    double acc[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) acc[d] = 0.0;
+#pragma unroll
+    for (int o = 0; o < (1 << DIM); ++o) {
+        int64_t e3[3] = {0, 0, 0};
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            e3[d] = idx[d] - ((o >> d) & 1);
+            if (e3[d] < 0 || e3[d] >= ecount[d]) ok = false;
+        }
+        if (!ok) continue;
+        int64_t e = e3[0] + (int64_t)g.ex * (e3[1] + (int64_t)g.ey * e3[2]);
+        double h[3];
+        element_h<DIM>(geo, e3[0], e3[1], e3[2], h);
+        double pe = p[e];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) acc[d] += gval<DIM>(h, o, d) * pe;
+    }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+        s[(int64_t)d * g.nn + n] = (fixed && fixed[n * DIM + d]) ? 0.0 : acc[d] * W[(int64_t)d * g.nn + n];
+}
+
+// q = G^T s ; scal[0] += p.q ; also clears the accumulators the next kernel fills
+template <int DIM>
+__global__ void k_pcg_gts(Grid g, GeoArgs geo, const double* __restrict__ s, const double* __restrict__ p,
+                          double* __restrict__ q, double* __restrict__ scal, int parity) {
+    __shared__ double sw[32];
+    int64_t ne = (int64_t)g.ex * g.ey * g.ez;
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double local = 0.0;
+    if (e < ne) {
+        int64_t ie = e % g.ex, je = (e / g.ex) % g.ey, ke = DIM == 3 ? e / ((int64_t)g.ex * g.ey) : 0;
+        double h[3];
+        element_h<DIM>(geo, ie, je, ke, h);
+        int64_t base = ie + g.nx * (je + g.ny * ke);
+        double acc = 0.0;
+#pragma unroll
+        for (int a = 0; a < (1 << DIM); ++a) {
+            int64_t n = base + (a & 1) + ((a >> 1) & 1) * g.nx + (DIM == 3 ? ((a >> 2) & 1) * g.nx * g.ny : 0);
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) acc += gval<DIM>(h, a, d) * s[(int64_t)d * g.nn + n];
+        }
+        q[e] = acc;
+        local = acc * p[e];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        scal[1 + (parity ^ 1)] = 0.0;  // r.z of this iteration (filled by k_pcg_update)
+        scal[3] = 0.0;
+    }
+    double t = block_sum(local, sw);
+    if (threadIdx.x == 0) atomicAdd(&scal[0], t);
+}
+
+// alpha = rz/pq ; x += alpha p ; r -= alpha q ; z = r/d ; scal[rz_new] += r.z ; scal[3] += r.r
+__global__ void k_pcg_update(int64_t ne, const double* __restrict__ p, const double* __restrict__ q,
+                             const double* __restrict__ d, double* __restrict__ x, double* __restrict__ r,
+                             double* __restrict__ z, double* __restrict__ scal, int parity) {
+    __shared__ double sw[32];
+    double alpha = scal[1 + parity] / scal[0];
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double rz = 0.0, rr = 0.0;
+    if (e < ne) {
+        x[e] = fma(alpha, p[e], x[e]);
+        double re = fma(-alpha, q[e], r[e]);
+        r[e] = re;
+        double ze = re / d[e];
+        z[e] = ze;
+        rz = re * ze;
+        rr = re * re;
+    }
+    double t1 = block_sum(rz, sw);
+    __syncthreads();
+    double t2 = block_sum(rr, sw);
+    if (threadIdx.x == 0) {
+        atomicAdd(&scal[1 + (parity ^ 1)], t1);
+        atomicAdd(&scal[3], t2);
+    }
+}
+
+// beta = rz_new/rz ; p = z + beta p ; clears p.q for the next iteration
+__global__ void k_pcg_dir(int64_t ne, const double* __restrict__ z, double* __restrict__ p, double* __restrict__ scal,
+                          int parity) {
+    double beta = scal[1 + (parity ^ 1)] / scal[1 + parity];
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < ne) p[e] = fma(beta, p[e], z[e]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) scal[0] = 0.0;
+}
+
+// initial state: r = b - mean(b) (already projected by the caller), z = r/d, p = z, x = 0,
+// scal[1] = r.z, scal[3] = scal[4] = r.r, scal[0] = 0
+__global__ void k_pcg_init(int64_t ne, const double* __restrict__ b, const double* __restrict__ d,
+                           double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
+                           double* __restrict__ p, double* __restrict__ scal) {
+    __shared__ double sw[32];
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double rz = 0.0, rr = 0.0;
+    if (e < ne) {
+        double re = b[e];
+        double ze = re / d[e];
+        x[e] = 0.0;
+        r[e] = re;
+        z[e] = ze;
+        p[e] = ze;
+        rz = re * ze;
+        rr = re * re;
+    }
+    double t1 = block_sum(rz, sw);
+    __syncthreads();
+    double t2 = block_sum(rr, sw);
+    if (threadIdx.x == 0) {
+        atomicAdd(&scal[1], t1);
+        atomicAdd(&scal[3], t2);
+        atomicAdd(&scal[4], t2);
+    }
+}
+
+// Solves (G^T W G) x = b (b projected off the constant by the caller) to ||r|| <= rtol ||b||.
+// work must hold 4*ne doubles plus 8 scalars; s is a velocity-sized temporary.
+int gwg_pcg(Context& c, const double* W, const double* d, const double* b, double* x, double rtol, int maxit,
+            double* work, double* s) {
+    const Level& L = c.levels[0];
+    Grid g = grid_of(L.mesh);
+    GeoArgs geo = geo_of(L.mesh);
+    int64_t ne = L.mesh.ne;
+    double* r = work;
+    double* z = work + ne;
+    double* p = work + 2 * ne;
+    double* q = work + 3 * ne;
+    double* scal = work + 4 * ne;
+    UWG_CUDA(cudaMemsetAsync(scal, 0, 8 * sizeof(double), c.stream));
+    unsigned eb = blocks_for(ne, 256), nb = blocks_for(g.nn, 256);
+    {
+        LaunchScope ls(c, -1);
+        k_pcg_init<<<eb, 256, 0, c.stream>>>(ne, b, d, x, r, z, p, scal);
+    }
+    double* hs = c.host_scalars;
+    UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+    double r0 = std::sqrt(hs[4]);
+    if (!(r0 > 0.0)) return 0;
+    const int check_every = 8;
+    int it = 0;
+    while (it < maxit) {
+        int parity = it & 1;
+        {
+            LaunchScope ls(c, -1);
+            if (g.dim == 3) k_pcg_gp<3><<<nb, 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
+            else k_pcg_gp<2><<<nb, 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
+        }
+        {
+            LaunchScope ls(c, -1);
+            if (g.dim == 3) k_pcg_gts<3><<<eb, 256, 0, c.stream>>>(g, geo, s, p, q, scal, parity);
+            else k_pcg_gts<2><<<eb, 256, 0, c.stream>>>(g, geo, s, p, q, scal, parity);
+        }
+        {
+            LaunchScope ls(c, -1);
+            k_pcg_update<<<eb, 256, 0, c.stream>>>(ne, p, q, d, x, r, z, scal, parity);
+        }
+        {
+            LaunchScope ls(c, -1);
+            k_pcg_dir<<<eb, 256, 0, c.stream>>>(ne, z, p, scal, parity);
+        }
+        it++;
+        if (it % check_every == 0 || it == maxit) {
+            UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            UWG_CUDA(cudaStreamSynchronize(c.stream));
+            double rn = std::sqrt(hs[3]);
+            if (!std::isfinite(rn)) throw Error(UWGPU_ERR_NAN, "NaN in the BFBt inner solve");
+            if (rn <= rtol * r0) break;
+        }
+    }
+    check_launch("gwg_pcg");
+    return it;
+}
+
+void gwg_diag(Context& c, const double* W, double* S) {
+    const Level& L = c.levels[0];
+    Grid g = grid_of(L.mesh);
+    LaunchScope ls(c, -1);
+    if (g.dim == 3)
+        k_gwg_diag<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), W, S);
+    else
+        k_gwg_diag<2><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), W, S);
 }
 
 void gkgdiag(Context& c, double* S) {

@@ -21,7 +21,7 @@ namespace uwg {
 
 template <typename T> void level_apply(Context&, const Level&, const T*, T*);
 template <typename T> void level_residual(Context&, const Level&, const T*, const T*, T*);
-template <typename T> void level_smooth(Context&, const Level&, const T*, T*, int);
+template <typename T> void level_smooth(Context&, const Level&, const T*, T*, int, bool);
 template <typename T> void level_restrict(Context&, const Level&, const Level&, const T*, T*);
 template <typename T> void level_prolong_add(Context&, const Level&, const Level&, const T*, T*);
 template <typename T> void level_coarse_solve(Context&, const Level&, const T*, T*);
@@ -30,6 +30,10 @@ void op_GT(Context& c, const double* u, double* p);
 void op_GT_unmasked(Context& c, const double* u, double* p);
 void gather_force(Context& c, double* f);
 void gkgdiag(Context& c, double* S);
+void bfbt_weights(Context& c, double* W);
+void gwg_diag(Context& c, const double* W, double* S);
+int gwg_pcg(Context& c, const double* W, const double* d, const double* b, double* x, double rtol, int maxit,
+            double* work, double* s);
 
 // ------------------------------------------------------------------------------------------
 // Vector kernels
@@ -60,6 +64,11 @@ template <typename T>
 __global__ void k_sub_from(int64_t n, const T* __restrict__ x, T* __restrict__ y) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] = x[i] - y[i];
+}
+
+__global__ void k_pointwise_mul(int64_t n, const double* __restrict__ x, const double* __restrict__ d, double* __restrict__ y) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = x[i] * d[i];
 }
 
 __global__ void k_pointwise_div(int64_t n, const double* __restrict__ x, const double* __restrict__ d, double* __restrict__ y) {
@@ -373,6 +382,9 @@ struct Bsscr {
     int64_t nv = 0, npres = 0;
     bool mixed = false;
     DArray<double> f, h, hhat, tu, tu2, t2, Sd, rhs_p, ref_r, ref_d;
+    // scaled BFBt state: weights, G^T W G diagonal, work vectors
+    DArray<double> bw, bd, bt, bt2, bs, bX, pr, pz, pp, pq, ptmp;
+    int64_t bfbt_its = 0;
     DArray<float> r32, d32;
     bool nan = false;
     bool inner_fail = false;
@@ -391,18 +403,14 @@ struct Bsscr {
     template <typename T>
     void vcycle(int l, const T* b, T* x) {
         Level& L = c.levels[l];
-        int64_t n = L.mesh.nn * dim;
         if (l == nlev - 1) {
-            if (nlev > 1) {
+            if (nlev > 1)
                 level_coarse_solve<T>(c, L, b, x);
-            } else {
-                zero<T>(c, n, x);
-                level_smooth<T>(c, L, b, x, o.smooth_down + o.smooth_up);
-            }
+            else
+                level_smooth<T>(c, L, b, x, o.smooth_down + o.smooth_up, true);
             return;
         }
-        zero<T>(c, n, x);
-        level_smooth<T>(c, L, b, x, o.smooth_down);
+        level_smooth<T>(c, L, b, x, o.smooth_down, true);
         T* r = lvl_r<T>(L);
         level_residual<T>(c, L, x, b, r);
         Level& C = c.levels[l + 1];
@@ -411,7 +419,7 @@ struct Bsscr {
         level_restrict<T>(c, L, C, r, bc);
         vcycle<T>(l + 1, bc, xc);
         level_prolong_add<T>(c, L, C, xc, x);
-        level_smooth<T>(c, L, b, x, o.smooth_up);
+        level_smooth<T>(c, L, b, x, o.smooth_up, false);
     }
 
     // ---- velocity (A11) solve: x = K^{-1} b to relative tolerance rtol ----
@@ -475,9 +483,46 @@ struct Bsscr {
         op_GT(c, tu2.p, y);
     }
 
+    void pmul(int64_t n, const double* a, const double* b, double* y) {
+        LaunchScope ls(c, -1);
+        k_pointwise_mul<<<blocks_for(n, 256), 256, 0, c.stream>>>(n, a, b, y);
+    }
+
+    // y = G^T W G x
+    void gwg_apply(const double* x, double* y) {
+        op_G(c, x, bs.p);
+        pmul(nv, bs.p, bw.p, bs.p);
+        op_GT(c, bs.p, y);
+    }
+
+    // Jacobi-preconditioned CG on G^T W G (the inner KSP of the scaled BFBt preconditioner), with
+    // the right-hand side projected off the constant null space (pc_ScaledGtKG.c:266-268)
+    void gwg_solve(const double* b, double* x) {
+        int maxit = o.bfbt_max_it > 0 ? o.bfbt_max_it : 500;
+        double rtol = o.bfbt_rtol > 0 ? o.bfbt_rtol : 1e-4;
+        copy<double>(c, npres, b, pr.p);
+        remove_constant_dev(pr.p);
+        bfbt_its += gwg_pcg(c, bw.p, bd.p, pr.p, x, rtol, maxit, pz.p, bs.p);
+    }
+
+    // pc_ScaledGtKG.c:242-310: y = (G^T W G)^-1 G^T W K W G (G^T W G)^-1 x
+    void bfbt_apply(const double* x, double* y) {
+        gwg_solve(x, bt.p);
+        op_G(c, bt.p, bs.p);
+        pmul(nv, bs.p, bw.p, bs.p);
+        level_apply<double>(c, c.levels[0], bs.p, bX.p);
+        pmul(nv, bX.p, bw.p, bX.p);
+        op_GT(c, bX.p, bt2.p);
+        gwg_solve(bt2.p, y);
+    }
+
+    void remove_constant_dev(double* x);
+
     void schur_pc(const double* v, double* z) {
         if (o.schur_pc == UWGPU_SCHUR_PC_NONE) {
             copy<double>(c, npres, v, z);
+        } else if (o.schur_pc == UWGPU_SCHUR_PC_SCALED_BFBT) {
+            bfbt_apply(v, z);
         } else {
             LaunchScope ls(c, -1);
             k_pointwise_div<<<blocks_for(npres, 256), 256, 0, c.stream>>>(npres, v, Sd.p, z);
@@ -630,6 +675,8 @@ __global__ void k_bc_vector(int64_t nn, const uint8_t* __restrict__ fixed, const
     for (int d = 0; d < DIM; ++d) u[(int64_t)d * nn + n] = fixed[n * DIM + d] ? val[n * DIM + d] : 0.0;
 }
 
+void Bsscr::remove_constant_dev(double* x) { remove_constant(c, npres, x, ptmp); }
+
 void Bsscr::run() {
     auto t0 = std::chrono::steady_clock::now();
     dim = c.mesh.dim;
@@ -690,9 +737,16 @@ void Bsscr::run() {
         op_GT_unmasked(c, ub.p, h.p);
         scale<double>(c, npres, -1.0, h.p, h.p);
     }
-    // Schur preconditioner diagonal
+    // Schur preconditioner
     if (o.schur_pc == UWGPU_SCHUR_PC_UW) copy<double>(c, npres, c.Se.p, Sd.p);
     else if (o.schur_pc == UWGPU_SCHUR_PC_GKGDIAG) gkgdiag(c, Sd.p);
+    else if (o.schur_pc == UWGPU_SCHUR_PC_SCALED_BFBT) {
+        for (auto* v : {&bw, &bs, &bX}) v->ensure(nv);
+        for (auto* v : {&bd, &bt, &bt2, &pr}) v->ensure(npres);
+        pz.ensure(4 * npres + 8);
+        bfbt_weights(c, bw.p);
+        gwg_diag(c, bw.p, bd.p);
+    }
     UWG_CUDA(cudaStreamSynchronize(c.stream));
     auto t1 = std::chrono::steady_clock::now();
     rep.t_setup_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
@@ -730,6 +784,7 @@ void Bsscr::run() {
     rep.backsolve_its = rep.inner_its_total - before;
     if (c.has_bc && c.bc_nonzero) axpy<double>(c, nv, 1.0, ub.p, c.u_sol.p);
     rep.outer_its = outer;
+    rep.pc_inner_its = bfbt_its;
     rep.rel_residual = full_residual(c.u_sol.p, c.p_sol.p);
     UWG_CUDA(cudaStreamSynchronize(c.stream));
     auto t2c = std::chrono::steady_clock::now();
@@ -747,7 +802,7 @@ void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
     UWG_REQUIRE(c.assembled, UWGPU_ERR_STATE, "solve requested before assembly");
     UWG_REQUIRE(o.precision == UWGPU_PREC_FP64 || o.precision == UWGPU_PREC_MIXED, UWGPU_ERR_ARGUMENT, "bad precision");
     UWG_REQUIRE(o.schur_type == UWGPU_SCHUR_CG || o.schur_type == UWGPU_SCHUR_FGMRES, UWGPU_ERR_ARGUMENT, "bad Schur type");
-    UWG_REQUIRE(o.schur_pc >= 0 && o.schur_pc <= 2, UWGPU_ERR_ARGUMENT, "bad Schur preconditioner");
+    UWG_REQUIRE(o.schur_pc >= 0 && o.schur_pc <= 3, UWGPU_ERR_ARGUMENT, "bad Schur preconditioner");
     Bsscr s(c, o, rep);
     s.run();
 }

@@ -33,6 +33,7 @@ SCHUR_FGMRES = 1
 SCHUR_PC_UW = 0
 SCHUR_PC_GKGDIAG = 1
 SCHUR_PC_NONE = 2
+SCHUR_PC_SCALED_BFBT = 3
 
 KERNEL_ASSEMBLY, KERNEL_APPLY, KERNEL_SMOOTH, KERNEL_BINNING = range(4)
 
@@ -57,13 +58,15 @@ class SolveOpts(C.Structure):
                 ("schur_type", C.c_int32), ("schur_pc", C.c_int32), ("restart", C.c_int32),
                 ("max_outer", C.c_int32), ("max_inner", C.c_int32), ("scr_rtol", C.c_double),
                 ("a11_rtol", C.c_double), ("back_rtol", C.c_double), ("remove_const_p", C.c_int32),
-                ("precision", C.c_int32), ("target_rel_residual", C.c_double)]
+                ("precision", C.c_int32), ("target_rel_residual", C.c_double), ("bfbt_rtol", C.c_double),
+                ("bfbt_max_it", C.c_int32), ("pad0", C.c_int32)]
 
 
 class Report(C.Structure):
     _fields_ = [("outer_its", C.c_int32), ("inner_its_total", C.c_int32), ("backsolve_its", C.c_int32),
                 ("vcycles", C.c_int32), ("converged", C.c_int32), ("status", C.c_int32),
-                ("rel_residual", C.c_double), ("t_setup_ms", C.c_double), ("t_solve_ms", C.c_double)]
+                ("rel_residual", C.c_double), ("t_setup_ms", C.c_double), ("t_solve_ms", C.c_double),
+                ("pc_inner_its", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -109,6 +112,8 @@ def load(build_if_missing: bool = True):
         L.uwgpu_solve_opts_default.restype = None
         L.uwgpu_profile_enable.argtypes = [P, C.c_int32]
         L.uwgpu_profile_read.argtypes = [P, C.c_int32, P, P]
+        L.uwgpu_profile_read_work.argtypes = [P, C.c_int32, P, P]
+        L.uwgpu_get_stream.argtypes = [P, P]
         L.uwgpu_launch_count.argtypes = [P]
         L.uwgpu_launch_count.restype = C.c_int64
         _lib = L
@@ -279,6 +284,17 @@ class Context:
         ms = C.c_double()
         self._check(self._L.uwgpu_profile_read(self._h, which, C.byref(n), C.byref(ms)))
         return n.value, ms.value
+
+    def profile_work(self, which):
+        b = C.c_double()
+        f = C.c_double()
+        self._check(self._L.uwgpu_profile_read_work(self._h, which, C.byref(b), C.byref(f)))
+        return b.value, f.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(self._L.uwgpu_get_stream(self._h, C.byref(s)))
+        return s.value or 0
 
     def launch_count(self):
         return int(self._L.uwgpu_launch_count(self._h))

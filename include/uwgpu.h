@@ -72,7 +72,11 @@ typedef struct {
  * (Solvers/KSPSolvers/src/BSSCR/auglag-driver-DGTGD.c, mg.c; StgFEM PETScMGSolver.c). */
 enum { UWGPU_PREC_FP64 = 0, UWGPU_PREC_MIXED = 1 };
 enum { UWGPU_SCHUR_CG = 0, UWGPU_SCHUR_FGMRES = 1 };
-enum { UWGPU_SCHUR_PC_UW = 0, UWGPU_SCHUR_PC_GKGDIAG = 1, UWGPU_SCHUR_PC_NONE = 2 };
+/* Schur preconditioners (-Q22_pc_type): uw = approxS of UzawaPreconditionerTerm; gkgdiag =
+ * diag(G^T diag(K)^-1 G); scaled BFBt = the "gtkg" preconditioner of
+ * Solvers/KSPSolvers/src/BSSCR/pc_ScaledGtKG.c:242-310, (G^T W G)^-1 (G^T W K W G) (G^T W G)^-1 with
+ * W = 1/rowmax(K), whose inner G^T W G solves are Jacobi-preconditioned CG. */
+enum { UWGPU_SCHUR_PC_UW = 0, UWGPU_SCHUR_PC_GKGDIAG = 1, UWGPU_SCHUR_PC_NONE = 2, UWGPU_SCHUR_PC_SCALED_BFBT = 3 };
 
 typedef struct {
     int32_t mg_levels;        /* mgLevels: levels including the fine one (>= 2)          */
@@ -90,6 +94,9 @@ typedef struct {
     int32_t precision;        /* UWGPU_PREC_FP64 or UWGPU_PREC_MIXED                     */
     double target_rel_residual; /* > 0: stop the outer solve once the full Stokes residual
                                    ||[f-Ku-Gp; h-G^T u]|| / ||[f;h]|| is below this value */
+    double bfbt_rtol;         /* inner G^T W G solve tolerance of the scaled BFBt preconditioner */
+    int32_t bfbt_max_it;      /* inner iteration limit of those solves                   */
+    int32_t pad0;
 } uwgpu_solve_opts;
 
 typedef struct {
@@ -102,6 +109,7 @@ typedef struct {
     double rel_residual;      /* ||[f-Ku-Gp; h-G^T u]|| / ||[f;h]|| of the returned u, p  */
     double t_setup_ms;        /* stencil build + multigrid hierarchy                     */
     double t_solve_ms;
+    int64_t pc_inner_its;     /* inner iterations of the Schur preconditioner (scaled BFBt) */
 } uwgpu_report;
 
 typedef struct uwgpu_ctx uwgpu_ctx;
@@ -187,7 +195,9 @@ int uwgpu_operator_apply(uwgpu_ctx* ctx, int32_t precision, const double* x, dou
 int uwgpu_solve_bsscr(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, double* u, double* p,
                       uwgpu_report* report);
 
-/* Default options (mg_levels 4, 2+2 sweeps, FGMRES Schur with the uw preconditioner). */
+/* Default options: the BSSCR driver's defaults (CG Schur iteration, KSPSetType "cg" in
+ * auglag-driver-DGTGD.c:266, with the uw approxS preconditioner, preconditioner.c:137), 4 levels,
+ * 2+2 smoothing sweeps. */
 void uwgpu_solve_opts_default(uwgpu_solve_opts* opts);
 
 /* Kernel timing: when enabled, launches of the kernel family `which` are bracketed by CUDA
@@ -196,8 +206,15 @@ enum { UWGPU_KERNEL_ASSEMBLY = 0, UWGPU_KERNEL_APPLY = 1, UWGPU_KERNEL_SMOOTH = 
        UWGPU_KERNEL_BINNING = 3, UWGPU_KERNEL_COUNT = 4 };
 int uwgpu_profile_enable(uwgpu_ctx* ctx, int32_t on);
 int uwgpu_profile_read(uwgpu_ctx* ctx, int32_t which, int64_t* launches, double* ms);
+/* Algorithmic work of the profiled launches of family `which`: bytes the kernels must move
+ * (each operand read or written once) and floating-point operations, summed on the host at
+ * launch time while profiling is enabled. */
+int uwgpu_profile_read_work(uwgpu_ctx* ctx, int32_t which, double* bytes, double* flops);
 /* Number of library kernel launches issued since the context was created. */
 int64_t uwgpu_launch_count(const uwgpu_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), so callers can order their own work and
+ * record timing events on it. */
+int uwgpu_get_stream(uwgpu_ctx* ctx, void** stream);
 
 #ifdef __cplusplus
 }

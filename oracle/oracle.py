@@ -49,7 +49,7 @@ class SolveOpts(C.Structure):
                 ("schur_type", C.c_int32), ("schur_pc", C.c_int32), ("restart", C.c_int32),
                 ("max_outer", C.c_int32), ("max_inner", C.c_int32), ("scr_rtol", C.c_double),
                 ("a11_rtol", C.c_double), ("back_rtol", C.c_double), ("remove_const_p", C.c_int32),
-                ("nthreads", C.c_int32)]
+                ("nthreads", C.c_int32), ("bfbt_rtol", C.c_double), ("bfbt_max_it", C.c_int32), ("pad", C.c_int32)]
 
 
 class Report(C.Structure):
@@ -243,9 +243,9 @@ def csr_spmv(rowptr, cols, vals, x, nthreads=0):
 
 def solve_bsscr(m, fixed, Ke, Ge, fe, Se, mg_levels=3, smooth=2, schur_type=1, schur_pc=0,
                 scr_rtol=1e-10, a11_rtol=1e-12, back_rtol=1e-12, restart=30, max_outer=500,
-                max_inner=2000, remove_const_p=True, nthreads=0):
+                max_inner=2000, remove_const_p=True, nthreads=0, bfbt_rtol=1e-4, bfbt_max_it=500):
     o = SolveOpts(mg_levels, smooth, smooth, schur_type, schur_pc, restart, max_outer, max_inner,
-                  scr_rtol, a11_rtol, back_rtol, 1 if remove_const_p else 0, nthreads)
+                  scr_rtol, a11_rtol, back_rtol, 1 if remove_const_p else 0, nthreads, bfbt_rtol, bfbt_max_it, 0)
     nn = num_nodes(m)
     E = num_elements(m)
     u = np.zeros((nn, m.dim))

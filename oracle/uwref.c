@@ -874,7 +874,7 @@ static void csr_free(csr* a) {
 }
 
 static void csr_mv(const csr* a, const double* x, double* y) {
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (a->nr > 20000)
     for (int64_t r = 0; r < a->nr; ++r) {
         double s = 0.0;
         for (int64_t k = a->rp[r]; k < a->rp[r + 1]; ++k) s += a->v[k] * x[a->ci[k]];
@@ -1137,7 +1137,7 @@ static void vcycle(mg_t* mg, int l, const double* b, double* x) {
 
 static double dot(int64_t n, const double* a, const double* b) {
     double s = 0.0;
-#pragma omp parallel for reduction(+ : s) schedule(static)
+#pragma omp parallel for reduction(+ : s) schedule(static) if (n > 50000)
     for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
     return s;
 }
@@ -1229,6 +1229,14 @@ typedef struct {
     double* Sdiag;
     double* tu;
     double* tu2;
+    /* scaled BFBt (Solvers/KSPSolvers/src/BSSCR/pc_ScaledGtKG.c:242-310) */
+    int bfbt;
+    double bfbt_rtol;
+    int bfbt_max_it;
+    double* W;      /* 1/rowmax(K), pc_ScaledGtKG.c:735-760 */
+    double* gwgd;   /* diag(G^T W G) */
+    double *pr, *pz, *pp, *pq, *pt, *pt2, *vs, *vX;
+    int64_t bfbt_its;
 } bsscr_t;
 
 static void op_K(void* c, const double* x, double* y) { csr_mv(&((bsscr_t*)c)->K, x, y); }
@@ -1248,8 +1256,54 @@ static void op_S(void* c, const double* v, double* y) {
     a11_solve(s, s->tu, s->tu2, s->a11_rtol);
     csr_mv(&s->GT, s->tu2, y);
 }
+static void gwg_apply(bsscr_t* s, const double* x, double* y) {
+    csr_mv(&s->G, x, s->vs);
+    for (int64_t i = 0; i < s->G.nr; ++i) s->vs[i] *= s->W[i];
+    csr_mv(&s->GT, s->vs, y);
+}
+
+/* inner KSP of the scaled BFBt preconditioner: Jacobi-preconditioned CG on G^T W G, the
+ * right-hand side projected off the constant null space (pc_ScaledGtKG.c:266-268) */
+static void gwg_solve(bsscr_t* s, const double* b, double* x) {
+    int64_t n = s->G.nc;
+    double mean = 0.0;
+    for (int64_t i = 0; i < n; ++i) mean += b[i];
+    mean /= (double)n;
+    for (int64_t i = 0; i < n; ++i) { x[i] = 0.0; s->pr[i] = b[i] - mean; }
+    double r0 = sqrt(dot(n, s->pr, s->pr));
+    if (!(r0 > 0.0)) return;
+    for (int64_t i = 0; i < n; ++i) { s->pz[i] = s->pr[i] / s->gwgd[i]; s->pp[i] = s->pz[i]; }
+    double rz = dot(n, s->pr, s->pz), rn = r0;
+    int it = 0;
+    while (it < s->bfbt_max_it && rn > s->bfbt_rtol * r0) {
+        gwg_apply(s, s->pp, s->pq);
+        double pq = dot(n, s->pp, s->pq);
+        if (!(pq > 0.0)) break;
+        double alpha = rz / pq;
+        for (int64_t i = 0; i < n; ++i) { x[i] += alpha * s->pp[i]; s->pr[i] -= alpha * s->pq[i]; s->pz[i] = s->pr[i] / s->gwgd[i]; }
+        double rz2 = dot(n, s->pr, s->pz);
+        double beta = rz2 / rz;
+        rz = rz2;
+        for (int64_t i = 0; i < n; ++i) s->pp[i] = s->pz[i] + beta * s->pp[i];
+        rn = sqrt(dot(n, s->pr, s->pr));
+        it++;
+    }
+    s->bfbt_its += it;
+}
+
 static void op_Spc(void* c, const double* v, double* y) {
     bsscr_t* s = (bsscr_t*)c;
+    if (s->bfbt) {
+        /* y = (G^T W G)^-1 G^T W K W G (G^T W G)^-1 v */
+        gwg_solve(s, v, s->pt);
+        csr_mv(&s->G, s->pt, s->vs);
+        for (int64_t i = 0; i < s->G.nr; ++i) s->vs[i] *= s->W[i];
+        csr_mv(&s->K, s->vs, s->vX);
+        for (int64_t i = 0; i < s->G.nr; ++i) s->vX[i] *= s->W[i];
+        csr_mv(&s->GT, s->vX, s->pt2);
+        gwg_solve(s, s->pt2, y);
+        return;
+    }
     for (int64_t i = 0; i < s->G.nc; ++i) y[i] = s->Sdiag ? v[i] / s->Sdiag[i] : v[i];
 }
 
@@ -1378,6 +1432,24 @@ int uwr_solve_bsscr(const uwr_mesh* m, const uint8_t* fixed, const double* Ke, c
         s.Sdiag = Sd;
     } else {
         s.Sdiag = NULL;
+        if (o->schur_pc == 3) {
+            s.bfbt = 1;
+            s.bfbt_rtol = o->bfbt_rtol > 0 ? o->bfbt_rtol : 1e-4;
+            s.bfbt_max_it = o->bfbt_max_it > 0 ? o->bfbt_max_it : 500;
+            s.W = (double*)malloc(sizeof(double) * (size_t)nfree);
+            for (int64_t r = 0; r < nfree; ++r) {
+                double mx = -1e300;
+                for (int64_t k = s.K.rp[r]; k < s.K.rp[r + 1]; ++k) mx = s.K.v[k] > mx ? s.K.v[k] : mx;
+                s.W[r] = 1.0 / mx;
+            }
+            s.gwgd = (double*)calloc((size_t)E, sizeof(double));
+            for (int64_t e = 0; e < E; ++e)
+                for (int64_t k = s.GT.rp[e]; k < s.GT.rp[e + 1]; ++k) s.gwgd[e] += s.GT.v[k] * s.GT.v[k] * s.W[s.GT.ci[k]];
+            double** bufs[] = {&s.pr, &s.pz, &s.pp, &s.pq, &s.pt, &s.pt2};
+            for (int b = 0; b < 6; ++b) *bufs[b] = (double*)malloc(sizeof(double) * (size_t)E);
+            s.vs = (double*)malloc(sizeof(double) * (size_t)nfree);
+            s.vX = (double*)malloc(sizeof(double) * (size_t)nfree);
+        }
     }
     s.a11_rtol = o->a11_rtol;
     s.restart = o->restart > 0 ? o->restart : 30;
@@ -1449,6 +1521,10 @@ cleanup:
     free(Sd);
     free(s.tu);
     free(s.tu2);
+    if (s.bfbt) {
+        free(s.W); free(s.gwgd); free(s.pr); free(s.pz); free(s.pp); free(s.pq); free(s.pt); free(s.pt2);
+        free(s.vs); free(s.vX);
+    }
     free(eq);
     return rc;
 }

@@ -114,7 +114,7 @@ typedef struct {
     int32_t mg_levels;        /* total levels incl. fine                          */
     int32_t smooth_down, smooth_up;
     int32_t schur_type;       /* 0 = CG, 1 = FGMRES                               */
-    int32_t schur_pc;         /* 0 = uw (approxS), 1 = gkgdiag, 2 = none           */
+    int32_t schur_pc;         /* 0 = uw (approxS), 1 = gkgdiag, 2 = none, 3 = scaled BFBt */
     int32_t restart;          /* FGMRES restart                                   */
     int32_t max_outer, max_inner;
     double scr_rtol;          /* -scr_ksp_rtol                                    */
@@ -122,6 +122,9 @@ typedef struct {
     double back_rtol;         /* -backsolveA11_ksp_rtol                           */
     int32_t remove_const_p;   /* -remove_constant_pressure_null_space             */
     int32_t nthreads;
+    double bfbt_rtol;         /* inner G^T W G tolerance of the scaled BFBt PC      */
+    int32_t bfbt_max_it;
+    int32_t pad;
 } uwr_solve_opts;
 
 typedef struct {

@@ -122,14 +122,15 @@ def test_operator_apply_matches_csr(oracle, uw, dim):
     ctx.close()
 
 
-@pytest.mark.parametrize("case,schur,pc", [("rt2d", 1, 0), ("spheres", 1, 0), ("spheres", 0, 0), ("spheres", 1, 1)])
+@pytest.mark.parametrize("case,schur,pc", [("rt2d", 1, 0), ("spheres", 1, 0), ("spheres", 0, 0), ("spheres", 1, 1),
+                                           ("spheres", 1, 3), ("rt2d", 1, 3)])
 def test_bsscr_solution_parity(oracle, uw, case, schur, pc):
     from earthbyte_underworld_gb300 import workloads as W
     O, U = oracle, uw
     w = W.rt2d(nel=(32, 32), ppc=20) if case == "rt2d" else W.spheres(nel=(8, 8, 8), nspheres=10, seed=9)
     ctx, perm, offsets, xi, Ke, fe, Ge, Se, eta = _run_gpu(U, W, w)
     opts = U.default_opts(mg_levels=3, schur_type=schur, schur_pc=pc, scr_rtol=1e-11, a11_rtol=1e-13,
-                          back_rtol=1e-13, max_outer=400, max_inner=2000)
+                          back_rtol=1e-13, max_outer=400, max_inner=2000, bfbt_rtol=1e-8, bfbt_max_it=5000)
     u, p, rep = ctx.solve_bsscr(opts)
     m = O.make_mesh(w["dim"], w["nel"])
     ou, op, orep = O.solve_bsscr(m, w["fixed"], Ke, Ge, fe, Se, mg_levels=3, scr_rtol=1e-11,
@@ -147,10 +148,14 @@ def test_mixed_precision_solve(oracle, uw):
     U = uw
     w = W.spheres(nel=(16, 16, 16), nspheres=20, seed=5)
     ctx, *_ = _run_gpu(U, W, w)
-    o64 = U.default_opts(mg_levels=3, scr_rtol=1e-10, a11_rtol=1e-12, back_rtol=1e-12)
+    o64 = U.default_opts(mg_levels=3, schur_type=U.SCHUR_CG, scr_rtol=1e-10, a11_rtol=1e-12, back_rtol=1e-12,
+                         max_outer=2000)
     u64, p64, r64 = ctx.solve_bsscr(o64)
-    om = U.default_opts(mg_levels=3, scr_rtol=1e-7, a11_rtol=1e-8, back_rtol=1e-8, precision=U.PREC_MIXED)
+    om = U.default_opts(mg_levels=3, schur_type=U.SCHUR_CG, scr_rtol=1e-8, a11_rtol=1e-9, back_rtol=1e-9,
+                        precision=U.PREC_MIXED, max_outer=2000)
     um, pm, rm = ctx.solve_bsscr(om)
+    assert r64.rel_residual < 1e-8
     assert rm.rel_residual < 1e-6
+    # error of the mixed-precision solution against the FP64 solve
     assert _rel(um, u64) < 1e-5
     ctx.close()
