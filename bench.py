@@ -39,7 +39,7 @@ NCU_TRAFFIC_PER_ROW = {"fp64": None, "fp32": None}
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nel", type=int, default=64)
@@ -167,7 +167,7 @@ def make_workload(nel, shuffle=True):
 # (-A11_ksp_type fgmres, Solvers/SysTest/ConvergenceTests/options-solv-mg.opt); tolerances chosen so
 # that the full Stokes residual reaches 1e-6
 SOLVE_KW = dict(mg_levels=4, smooth_down=2, smooth_up=2, schur_type=1, schur_pc=3, scr_rtol=1e-7, a11_rtol=1e-6,
-                back_rtol=1e-7, restart=30, max_outer=500, max_inner=2000, bfbt_rtol=1e-4, bfbt_max_it=2000)
+                back_rtol=1e-7, restart=30, max_outer=500, max_inner=2000, bfbt_rtol=1e-2, bfbt_max_it=2000)
 
 
 # ------------------------------------------------------------------------------------------
@@ -267,8 +267,8 @@ def run_ours(args):
         _, _, rep = ctx.solve_bsscr(opts, want=False)
         return rep
 
-    def timed(opts, profile):
-        for _ in range(args.warmup):
+    def timed(opts, profile, warmup=None):
+        for _ in range(args.warmup if warmup is None else warmup):
             step(opts)
         torch.cuda.synchronize()
         dist.barrier()
@@ -337,7 +337,8 @@ def run_ours(args):
     # mixed-precision form on the same workload
     mixed = None
     if not args.no_mixed and prec == "fp64":
-        ms2, wall2, l2, reps2, clk2, _ = timed(opts_for("mixed"), profile=False)
+        # the FP64 leg has warmed every kernel; one extra untimed mixed step suffices
+        ms2, wall2, l2, reps2, clk2, _ = timed(opts_for("mixed"), profile=False, warmup=1)
         ms2 = dist.max(ms2)
         mixed = {"value": dist.sum(npts) / (ms2 / 1e3 / args.steps), "ms_per_step": ms2 / args.steps,
                  "stokes_solve_s": reps2[-1].t_solve_ms / 1e3, "rel_residual": reps2[-1].rel_residual,
@@ -353,7 +354,8 @@ def run_ours(args):
     ne = ctx.nelements
     e2e_times = []
     opts = opts_for(prec)
-    for it in range(args.warmup + args.steps):
+    e2e_warm = 1  # the context is warm from the legs above
+    for it in range(e2e_warm + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ctx.particles_upload(xs, ys, zs, ms_)
@@ -361,7 +363,7 @@ def run_ours(args):
         ctx.assemble()
         u, p, _ = ctx.solve_bsscr(opts, want=True)
         torch.cuda.synchronize()
-        if it >= args.warmup:
+        if it >= e2e_warm:
             e2e_times.append(time.perf_counter() - t0)
     e2e_s = dist.max(sum(e2e_times))
     e2e = {"value": dist.sum(npts) / (e2e_s / args.steps), "unit": UNIT,

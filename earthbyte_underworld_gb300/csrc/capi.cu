@@ -108,6 +108,7 @@ int uwgpu_mesh_q1(uwgpu_ctx* ctx, int32_t dim, const int32_t nel[3], const doubl
         UWG_REQUIRE(m.ne < (int64_t)0x7fffffff, UWGPU_ERR_ARGUMENT, "too many elements");
         c.mesh = m;
         c.has_mesh = true;
+        c.elem_h_for = -1;
         c.has_bc = false;
         c.mapped = false;
         c.assembled = false;

@@ -153,6 +153,10 @@ struct Context {
     DArray<double> Ge;        // entry-major [k][e]
     bool assembled = false;
 
+    // per-axis element widths of the fine mesh (device), and the mesh they belong to
+    DArray<double> elem_h;
+    int64_t elem_h_for = -1;
+
     // solver state
     Level levels[kMaxLevels];
     int nlevels = 0;

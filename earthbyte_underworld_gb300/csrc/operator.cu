@@ -189,62 +189,60 @@ __device__ __forceinline__ void stencil_row(const Grid& g, int64_t n, int64_t i,
     }
 }
 
-template <int DIM, typename T>
-__global__ void __launch_bounds__(256) k_apply(Grid g, const T* __restrict__ A, const T* __restrict__ x, T* __restrict__ y) {
-    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= g.nn) return;
-    int64_t i = n % g.nx, j = (n / g.nx) % g.ny, k = DIM == 3 ? n / (g.nx * g.ny) : 0;
-    T out[DIM];
-    stencil_row<DIM, T>(g, n, i, j, k, A, x, out);
-#pragma unroll
-    for (int r = 0; r < DIM; ++r) y[(int64_t)r * g.nn + n] = out[r];
-}
+// Row-split layout: a block of kRowThreads threads covers kRowThreads/DIM nodes; warp w works on
+// row w % DIM of 32 consecutive nodes (lanes), so every stencil load of a warp is coalesced and a
+// node's DIM rows run on DIM threads (three times the parallelism of one thread per node).
+constexpr int kRowThreads = 192;
 
-// r = b - A x
+// sum_q sum_c A[q][r][c][n] x[c][m(q)] for one row r of node n
 template <int DIM, typename T>
-__global__ void __launch_bounds__(256) k_residual(Grid g, const T* __restrict__ A, const T* __restrict__ x,
-                                                  const T* __restrict__ b, T* __restrict__ r) {
-    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= g.nn) return;
-    int64_t i = n % g.nx, j = (n / g.nx) % g.ny, k = DIM == 3 ? n / (g.nx * g.ny) : 0;
-    T out[DIM];
-    stencil_row<DIM, T>(g, n, i, j, k, A, x, out);
+__device__ __forceinline__ T stencil_row_r(const Grid& g, int64_t n, int64_t i, int64_t j, int64_t k, int r,
+                                           const T* __restrict__ A, const T* __restrict__ x) {
+    constexpr int NB = nblocks<DIM>();
+    T out = (T)0;
 #pragma unroll
-    for (int q = 0; q < DIM; ++q) r[(int64_t)q * g.nn + n] = b[(int64_t)q * g.nn + n] - out[q];
-}
-
-// Block Gauss-Seidel on one node: x_n += Dinv_n (b_n - (A x)_n).
-template <int DIM, typename T>
-__device__ __forceinline__ void gs_relax_node(const Grid& g, int64_t i, int64_t j, int64_t k, const T* __restrict__ A,
-                                              const T* __restrict__ Dinv, const T* __restrict__ b, T* __restrict__ x) {
-    int64_t n = i + g.nx * (j + g.ny * k);
-    T ax[DIM];
-    stencil_row<DIM, T>(g, n, i, j, k, A, x, ax);
-    T res[DIM];
+    for (int q = 0; q < NB; ++q) {
+        int dx = q % 3 - 1, dy = (q / 3) % 3 - 1, dz = DIM == 3 ? q / 9 - 1 : 0;
+        int64_t ii = i + dx, jj = j + dy, kk = k + dz;
+        if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || (DIM == 3 && (kk < 0 || kk >= g.nz))) continue;
+        int64_t m = n + dx + g.nx * (dy + g.ny * dz);
 #pragma unroll
-    for (int r = 0; r < DIM; ++r) res[r] = b[(int64_t)r * g.nn + n] - ax[r];
-#pragma unroll
-    for (int r = 0; r < DIM; ++r) {
-        T v = x[(int64_t)r * g.nn + n];
-#pragma unroll
-        for (int cc = 0; cc < DIM; ++cc) v = fma(Dinv[(int64_t)(r * DIM + cc) * g.nn + n], res[cc], v);
-        x[(int64_t)r * g.nn + n] = v;
+        for (int cc = 0; cc < DIM; ++cc)
+            out = fma(A[((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n], x[(int64_t)cc * g.nn + m], out);
     }
+    return out;
 }
 
-constexpr int kGsThreads = 256;
+// y = A x (or r = b - A x when b is given), row-split
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kRowThreads) k_apply(Grid g, const T* __restrict__ A, const T* __restrict__ x,
+                                                       const T* __restrict__ b, T* __restrict__ y) {
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int r = warp % DIM, grp = warp / DIM;
+    int64_t n = (int64_t)blockIdx.x * (kRowThreads / DIM) + grp * 32 + lane;
+    if (n >= g.nn) return;
+    int64_t i = n % g.nx, j = (n / g.nx) % g.ny, k = DIM == 3 ? n / (g.nx * g.ny) : 0;
+    T v = stencil_row_r<DIM, T>(g, n, i, j, k, r, A, x);
+    y[(int64_t)r * g.nn + n] = b ? b[(int64_t)r * g.nn + n] - v : v;
+}
 
 // `sweeps` symmetric multicolour block Gauss-Seidel sweeps (colours ascending, then
-// descending) in one cooperative launch.  Nodes of one parity colour are never stencil
-// neighbours, so a colour is relaxed in parallel; a grid-wide barrier separates colours.
+// descending) in one cooperative launch: x_n += Dinv_n (b_n - (A x)_n).  Nodes of one parity
+// colour are never stencil neighbours, so a colour is relaxed in parallel; the DIM row
+// residuals of a node meet in shared memory before its update, and a grid-wide barrier
+// separates colours.
 template <int DIM, typename T>
-__global__ void __launch_bounds__(kGsThreads) k_gs_sweeps(Grid g, const T* __restrict__ A, const T* __restrict__ Dinv,
-                                                          const T* __restrict__ b, T* __restrict__ x, int sweeps,
-                                                          int zero_init) {
+__global__ void __launch_bounds__(kRowThreads) k_gs_sweeps(Grid g, const T* __restrict__ A, const T* __restrict__ Dinv,
+                                                           const T* __restrict__ b, T* __restrict__ x, int sweeps,
+                                                           int zero_init) {
+    __shared__ T sres[kRowThreads];
     cg::grid_group grid = cg::this_grid();
-    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    constexpr int NPB = kRowThreads / DIM;
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int r = warp % DIM, grp = warp / DIM;
     if (zero_init) {
+        const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        const int64_t stride = (int64_t)gridDim.x * blockDim.x;
         for (int64_t t = tid; t < g.nn * DIM; t += stride) x[t] = (T)0;
         grid.sync();
     }
@@ -256,10 +254,27 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_sweeps(Grid g, const T* __res
             int64_t cx = (g.nx - px + 1) / 2, cy = (g.ny - py + 1) / 2;
             int64_t cz = DIM == 3 ? (g.nz - pz + 1) / 2 : 1;
             int64_t cnt = cx * cy * cz;
-            for (int64_t t = tid; t < cnt; t += stride) {
-                int64_t i = 2 * (t % cx) + px, j = 2 * ((t / cx) % cy) + py;
-                int64_t k = DIM == 3 ? 2 * (t / (cx * cy)) + pz : 0;
-                gs_relax_node<DIM, T>(g, i, j, k, A, Dinv, b, x);
+            for (int64_t base = (int64_t)blockIdx.x * NPB; base < cnt; base += (int64_t)gridDim.x * NPB) {
+                int64_t t = base + grp * 32 + lane;
+                bool act = t < cnt;
+                int64_t n = 0;
+                T res = (T)0;
+                if (act) {
+                    int64_t i = 2 * (t % cx) + px, j = 2 * ((t / cx) % cy) + py;
+                    int64_t k = DIM == 3 ? 2 * (t / (cx * cy)) + pz : 0;
+                    n = i + g.nx * (j + g.ny * k);
+                    res = b[(int64_t)r * g.nn + n] - stencil_row_r<DIM, T>(g, n, i, j, k, r, A, x);
+                }
+                sres[threadIdx.x] = res;
+                __syncthreads();
+                if (act) {
+                    T v = x[(int64_t)r * g.nn + n];
+#pragma unroll
+                    for (int cc = 0; cc < DIM; ++cc)
+                        v = fma(Dinv[(int64_t)(r * DIM + cc) * g.nn + n], sres[(grp * DIM + cc) * 32 + lane], v);
+                    x[(int64_t)r * g.nn + n] = v;
+                }
+                __syncthreads();
             }
             grid.sync();
         }
@@ -628,9 +643,9 @@ void level_apply(Context& c, const Level& L, const T* x, T* y) {
     note_work(c, UWGPU_KERNEL_APPLY, (double)g.nn * (NB * D * D + 2 * D) * sizeof(T), 2.0 * g.nn * NB * D * D);
     LaunchScope ls(c, UWGPU_KERNEL_APPLY);
     if (g.dim == 3)
-        k_apply<3, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, y);
+        k_apply<3, T><<<blocks_for(g.nn, kRowThreads / 3), kRowThreads, 0, c.stream>>>(g, stencil_of<T>(L), x, nullptr, y);
     else
-        k_apply<2, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, y);
+        k_apply<2, T><<<blocks_for(g.nn, kRowThreads / 2), kRowThreads, 0, c.stream>>>(g, stencil_of<T>(L), x, nullptr, y);
 }
 
 template <typename T>
@@ -640,9 +655,9 @@ void level_residual(Context& c, const Level& L, const T* x, const T* b, T* r) {
     note_work(c, UWGPU_KERNEL_APPLY, (double)g.nn * (NB * D * D + 3 * D) * sizeof(T), 2.0 * g.nn * NB * D * D);
     LaunchScope ls(c, UWGPU_KERNEL_APPLY);
     if (g.dim == 3)
-        k_residual<3, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, b, r);
+        k_apply<3, T><<<blocks_for(g.nn, kRowThreads / 3), kRowThreads, 0, c.stream>>>(g, stencil_of<T>(L), x, b, r);
     else
-        k_residual<2, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, b, r);
+        k_apply<2, T><<<blocks_for(g.nn, kRowThreads / 2), kRowThreads, 0, c.stream>>>(g, stencil_of<T>(L), x, b, r);
 }
 
 // symmetric sweep: colours ascending then descending
@@ -662,12 +677,13 @@ void level_smooth(Context& c, const Level& L, const T* b, T* x, int sweeps, bool
         int per_sm = 0, sms = 0, dev = 0;
         UWG_CUDA(cudaGetDevice(&dev));
         UWG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        UWG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kGsThreads, 0));
+        UWG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kRowThreads, 0));
         UWG_REQUIRE(per_sm > 0, UWGPU_ERR_CUDA, "smoother kernel cannot be made resident");
         max_blocks[di][ti] = per_sm * sms;
     }
     int64_t per_colour = (g.nn + (1 << D) - 1) >> D;
-    int64_t want = (per_colour + kGsThreads - 1) / kGsThreads;
+    int64_t npb = kRowThreads / D;
+    int64_t want = (per_colour + npb - 1) / npb;
     int blocks = (int)(want < max_blocks[di][ti] ? want : max_blocks[di][ti]);
     if (blocks < 1) blocks = 1;
     const T* A = stencil_of<T>(L);
@@ -675,7 +691,7 @@ void level_smooth(Context& c, const Level& L, const T* b, T* x, int sweeps, bool
     int zi = zero_init ? 1 : 0;
     void* args[] = {(void*)&g, (void*)&A, (void*)&Di, (void*)&b, (void*)&x, (void*)&sweeps, (void*)&zi};
     LaunchScope ls(c, UWGPU_KERNEL_SMOOTH);
-    UWG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kGsThreads), args, 0, c.stream));
+    UWG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kRowThreads), args, 0, c.stream));
 }
 
 template <typename T>
@@ -741,17 +757,18 @@ void apply_fine(Context& c, bool fp32, const double* x, double* y) {
 // G_e[a][d] = -s_{d,a} * prod_{q != d} h_q / 2^(dim-1): the 2^dim-point Gauss integral of
 // -dN_a/dx_d over the affine element.
 // ------------------------------------------------------------------------------------------
+// Element widths per axis, precomputed once per mesh (h[off[d] + i] = x_{i+1} - x_i along d), so
+// the kernels do no FP64 division to recover the geometry.
 struct GeoArgs {
-    int nel[3];
-    double min[3], max[3];
+    const double* h;
+    int off[3];
 };
 
 template <int DIM>
 __device__ __forceinline__ void element_h(const GeoArgs& a, int64_t ie, int64_t je, int64_t ke, double h[3]) {
     int64_t idx[3] = {ie, je, ke};
 #pragma unroll
-    for (int d = 0; d < DIM; ++d)
-        h[d] = node_coord_1d(idx[d] + 1, a.nel[d], a.min[d], a.max[d]) - node_coord_1d(idx[d], a.nel[d], a.min[d], a.max[d]);
+    for (int d = 0; d < DIM; ++d) h[d] = __ldg(a.h + a.off[d] + idx[d]);
 }
 
 template <int DIM>
@@ -879,13 +896,22 @@ __global__ void k_gkgdiag(Grid g, GeoArgs geo, const double* __restrict__ A, con
     S[e] = acc;
 }
 
-static GeoArgs geo_of(const MeshDesc& m) {
-    GeoArgs a;
-    for (int d = 0; d < 3; ++d) {
-        a.nel[d] = m.nel[d];
-        a.min[d] = m.min[d];
-        a.max[d] = m.max[d];
+static GeoArgs geo_of(Context& c, const MeshDesc& m) {
+    // widths of the fine mesh, built on first use after the mesh was set
+    if (c.elem_h_for != m.nel[0] + 4096LL * (m.nel[1] + 4096LL * m.nel[2]) || !c.elem_h.p) {
+        std::vector<double> h;
+        for (int d = 0; d < m.dim; ++d)
+            for (int i = 0; i < m.nel[d]; ++i)
+                h.push_back(node_coord_1d(i + 1, m.nel[d], m.min[d], m.max[d]) - node_coord_1d(i, m.nel[d], m.min[d], m.max[d]));
+        c.elem_h.ensure(h.size());
+        UWG_CUDA(cudaMemcpy(c.elem_h.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+        c.elem_h_for = m.nel[0] + 4096LL * (m.nel[1] + 4096LL * m.nel[2]);
     }
+    GeoArgs a;
+    a.h = c.elem_h.p;
+    a.off[0] = 0;
+    a.off[1] = m.nel[0];
+    a.off[2] = m.nel[0] + m.nel[1];
     return a;
 }
 
@@ -894,9 +920,9 @@ void op_G(Context& c, const double* p, double* u) {
     Grid g = grid_of(L.mesh);
     LaunchScope ls(c, -1);
     if (g.dim == 3)
-        k_G<3><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), p, L.fixed.p, u);
+        k_G<3><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), p, L.fixed.p, u);
     else
-        k_G<2><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), p, L.fixed.p, u);
+        k_G<2><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), p, L.fixed.p, u);
 }
 
 void op_GT(Context& c, const double* u, double* p) {
@@ -904,9 +930,9 @@ void op_GT(Context& c, const double* u, double* p) {
     Grid g = grid_of(L.mesh);
     LaunchScope ls(c, -1);
     if (g.dim == 3)
-        k_GT<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), u, L.fixed.p, p);
+        k_GT<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), u, L.fixed.p, p);
     else
-        k_GT<2><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), u, L.fixed.p, p);
+        k_GT<2><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), u, L.fixed.p, p);
 }
 
 void op_GT_unmasked(Context& c, const double* u, double* p) {
@@ -914,9 +940,9 @@ void op_GT_unmasked(Context& c, const double* u, double* p) {
     Grid g = grid_of(L.mesh);
     LaunchScope ls(c, -1);
     if (g.dim == 3)
-        k_GT<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), u, nullptr, p);
+        k_GT<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), u, nullptr, p);
     else
-        k_GT<2><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), u, nullptr, p);
+        k_GT<2><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), u, nullptr, p);
 }
 
 void gather_force(Context& c, double* f) {
@@ -1134,7 +1160,7 @@ int gwg_pcg(Context& c, const double* W, const double* d, const double* b, doubl
             double* work, double* s) {
     const Level& L = c.levels[0];
     Grid g = grid_of(L.mesh);
-    GeoArgs geo = geo_of(L.mesh);
+    GeoArgs geo = geo_of(c, L.mesh);
     int64_t ne = L.mesh.ne;
     double* r = work;
     double* z = work + ne;
@@ -1192,9 +1218,9 @@ void gwg_diag(Context& c, const double* W, double* S) {
     Grid g = grid_of(L.mesh);
     LaunchScope ls(c, -1);
     if (g.dim == 3)
-        k_gwg_diag<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), W, S);
+        k_gwg_diag<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), W, S);
     else
-        k_gwg_diag<2><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), W, S);
+        k_gwg_diag<2><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), W, S);
 }
 
 void gkgdiag(Context& c, double* S) {
@@ -1202,9 +1228,9 @@ void gkgdiag(Context& c, double* S) {
     Grid g = grid_of(L.mesh);
     LaunchScope ls(c, -1);
     if (g.dim == 3)
-        k_gkgdiag<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), L.A64.p, L.fixed.p, S);
+        k_gkgdiag<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), L.A64.p, L.fixed.p, S);
     else
-        k_gkgdiag<2><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(L.mesh), L.A64.p, L.fixed.p, S);
+        k_gkgdiag<2><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), L.A64.p, L.fixed.p, S);
 }
 
 }  // namespace uwg
