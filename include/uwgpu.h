@@ -37,7 +37,8 @@ enum {
     UWGPU_ERR_NOT_CONVERGED = 6, /* a Krylov solve hit its iteration limit                   */
     UWGPU_ERR_NAN = 7,           /* NaN/Inf detected in a residual                           */
     UWGPU_ERR_UNSUPPORTED = 8,   /* rheology law or option not provided by this library      */
-    UWGPU_ERR_BREAKDOWN = 9      /* Krylov breakdown (zero pivot / non-SPD coarse operator)  */
+    UWGPU_ERR_BREAKDOWN = 9,     /* Krylov breakdown (zero pivot / non-SPD coarse operator)  */
+    UWGPU_ERR_TOO_LARGE = 10     /* input larger than the fixed scratch of uwgpu_bin_and_map_noalloc */
 };
 
 /* Rheology laws (one entry of a RheologyMaterial's rheology list, applied in order). */
@@ -215,6 +216,25 @@ int64_t uwgpu_launch_count(const uwgpu_ctx* ctx);
 /* The context's CUDA stream (a cudaStream_t), so callers can order their own work and
  * record timing events on it. */
 int uwgpu_get_stream(uwgpu_ctx* ctx, void** stream);
+
+/* Allocation-free binning + mapping.  This entry point has no counterpart in the reference; it
+ * exists for callers that cannot allocate device memory while they run (a host framework that
+ * owns every device buffer through its own pool, or code where an allocation would synchronise
+ * the device).  It needs no context and calls no allocator: the caller passes device-accessible
+ * inputs (x, y, z coordinates of n points) and outputs (perm: n, offsets: nel+1, xi: dim*n laid
+ * out [d][slot]), and the pass's scratch lives in one fixed __device__ array of about 9 MB that
+ * every device loading the library keeps until the process exits.  Limits: at most
+ * UWGPU_NOALLOC_MAX_POINTS points and UWGPU_NOALLOC_MAX_ELEMENTS elements, else
+ * UWGPU_ERR_TOO_LARGE.  Results equal uwgpu_bin_and_map's.  The first call on a device looks up
+ * the array's device address (make it before any stream capture).  Calls share the array: calls
+ * whose GPU work overlaps race, so order them (e.g. one stream).  Runs on `stream` (NULL: the
+ * default stream) and synchronises it; *outside (optional, host) receives the number of points
+ * outside the mesh, reported as UWGPU_ERR_DOMAIN. */
+#define UWGPU_NOALLOC_MAX_POINTS (1 << 20)
+#define UWGPU_NOALLOC_MAX_ELEMENTS (1 << 17)
+int uwgpu_bin_and_map_noalloc(int32_t dim, const int32_t nel[3], const double min[3], const double max[3],
+                              int64_t n, const double* x, const double* y, const double* z, uint32_t* perm,
+                              uint32_t* offsets, double* xi, void* stream, uint32_t* outside);
 
 #ifdef __cplusplus
 }
