@@ -46,6 +46,10 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--mode", default="step", choices=["step", "kernels"],
+                    help="step: the full hot-path step; kernels: operator apply and smoother only")
+    ap.add_argument("--iters", type=int, default=20, help="launches per kernel in --mode kernels")
     ap.add_argument("--cpu-nel", type=int, default=16, help="mesh of the CPU baseline sample")
     return ap.parse_args()
 
@@ -355,7 +359,7 @@ def run_ours(args):
     e2e_times = []
     opts = opts_for(prec)
     e2e_warm = 1  # the context is warm from the legs above
-    for it in range(e2e_warm + args.steps):
+    for it in range(0 if args.no_e2e else e2e_warm + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ctx.particles_upload(xs, ys, zs, ms_)
@@ -365,9 +369,11 @@ def run_ours(args):
         torch.cuda.synchronize()
         if it >= e2e_warm:
             e2e_times.append(time.perf_counter() - t0)
-    e2e_s = dist.max(sum(e2e_times))
+    e2e_s = dist.max(sum(e2e_times)) if e2e_times else float("nan")
     e2e = {"value": dist.sum(npts) / (e2e_s / args.steps), "unit": UNIT,
            "h2d_bytes_per_step": int(npts * (3 * 8 + 4)), "d2h_bytes_per_step": int(nn * 3 * 8 + ne * 8)}
+
+    operator_rates = kernel_rates(ctx, U, args.iters)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -387,7 +393,7 @@ def run_ours(args):
                           "outer_its": rep.outer_its, "inner_its": rep.inner_its_total, "vcycles": rep.vcycles,
                           "stokes_solve_s": rep.t_solve_ms / 1e3, "setup_ms": rep.t_setup_ms,
                           "l2": "256 MB buffer written between timed steps", "parallelism": f"replicas x{world}"},
-               "roofline": roofline, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
+               "roofline": roofline, "kernels": kernels, "operator": operator_rates, "cpu_baseline": cpu, "e2e": e2e,
                "gpu_launches": int(launches), "clocks": clk, "mixed": mixed,
                "wall_s_timed": wall}
         print(json.dumps(out), flush=True)
@@ -396,10 +402,55 @@ def run_ours(args):
     return 0
 
 
+def kernel_rates(ctx, U, iters):
+    """Fine-level operator apply and smoother, timed back to back on resident vectors, with their
+    algorithmic bytes (stencil 3^d blocks of d x d, diagonal inverse, right-hand side and the
+    row vectors moved once per node)."""
+    nn, dim = ctx.nnodes, ctx.dim
+    nb = 27 if dim == 3 else 9
+    peak, kind = measured_peaks()
+    out = {}
+    for name, prec, size in (("fp64", U.PREC_FP64, 8), ("fp32", U.PREC_MIXED, 4)):
+        ctx.time_apply(prec, 3)
+        ms = ctx.time_apply(prec, iters) / iters
+        apply_bytes = nn * (nb * dim * dim + 2 * dim) * size
+        ctx.time_smooth(prec, 2, 2)
+        sms = ctx.time_smooth(prec, 2, max(iters // 4, 2)) / max(iters // 4, 2)
+        smooth_bytes = 2 * 2 * nn * (nb * dim * dim + dim * dim + 3 * dim) * size + nn * dim * size
+        out[name] = {"apply_ms": ms, "applies_per_s": 1e3 / ms, "apply_GB_per_s": apply_bytes / ms / 1e6,
+                     "apply_frac_hbm": apply_bytes / ms / 1e6 / peak,
+                     "apply_fp_TFLOP_per_s": 2.0 * nn * nb * dim * dim / ms / 1e9,
+                     "smooth2_ms": sms, "smooth2_GB_per_s": smooth_bytes / sms / 1e6,
+                     "smooth2_frac_hbm": smooth_bytes / sms / 1e6 / peak,
+                     "smooth2_fp_TFLOP_per_s": 2 * 2 * 2.0 * nn * (nb + 1) * dim * dim / sms / 1e9}
+    out["peak_GB_per_s"] = peak
+    out["peak_source"] = kind
+    return out
+
+
+def run_kernels(args):
+    import torch
+
+    from earthbyte_underworld_gb300 import uwgpu as U
+    from earthbyte_underworld_gb300 import workloads as W
+    w = make_workload(args.nel)
+    with U.Context(0) as ctx:
+        W.setup_context(ctx, w)
+        ctx.bin_and_map(want=False)
+        ctx.assemble()
+        rates = kernel_rates(ctx, U, args.iters)
+    torch.cuda.synchronize()
+    print(json.dumps({"mode": "kernels", "workload": f"stokes3d_spheres_{args.nel}cube_27ppc_50spheres",
+                      "nodes": (args.nel + 1) ** 3, **rates}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "kernels":
+        return run_kernels(args)
     return run_ours(args)
 
 

@@ -399,6 +399,66 @@ int uwgpu_profile_read_work(uwgpu_ctx* ctx, int32_t which, double* bytes, double
 
 int64_t uwgpu_launch_count(const uwgpu_ctx* ctx) { return ctx ? ctx->c.launches : 0; }
 
+int uwgpu_time_apply(uwgpu_ctx* ctx, int32_t precision, int32_t iterations, double* ms) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(ms && iterations > 0, UWGPU_ERR_ARGUMENT, "bad arguments");
+        bool f32 = precision == UWGPU_PREC_MIXED;
+        if (!c.operator_built || (f32 && !c.operator_has32))
+            uwg::build_operator(c, c.operator_built ? c.operator_levels : 1, f32);
+        uwg::Level& L = c.levels[0];
+        size_t nv = (size_t)L.mesh.nn * L.mesh.dim;
+        cudaEvent_t e0, e1;
+        UWG_CUDA(cudaEventCreate(&e0));
+        UWG_CUDA(cudaEventCreate(&e1));
+        if (f32) {
+            UWG_CUDA(cudaMemsetAsync(L.x32.p, 0, nv * sizeof(float), c.stream));
+            UWG_CUDA(cudaEventRecord(e0, c.stream));
+            for (int i = 0; i < iterations; ++i) uwg::level_apply<float>(c, L, L.x32.p, L.t32.p);
+        } else {
+            UWG_CUDA(cudaMemsetAsync(L.x64.p, 0, nv * sizeof(double), c.stream));
+            UWG_CUDA(cudaEventRecord(e0, c.stream));
+            for (int i = 0; i < iterations; ++i) uwg::level_apply<double>(c, L, L.x64.p, L.t64.p);
+        }
+        UWG_CUDA(cudaEventRecord(e1, c.stream));
+        UWG_CUDA(cudaEventSynchronize(e1));
+        float t = 0.f;
+        UWG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        *ms = t;
+    });
+}
+
+int uwgpu_time_smooth(uwgpu_ctx* ctx, int32_t precision, int32_t sweeps, int32_t iterations, double* ms) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(ms && iterations > 0 && sweeps > 0, UWGPU_ERR_ARGUMENT, "bad arguments");
+        bool f32 = precision == UWGPU_PREC_MIXED;
+        if (!c.operator_built || (f32 && !c.operator_has32))
+            uwg::build_operator(c, c.operator_built ? c.operator_levels : 1, f32);
+        uwg::Level& L = c.levels[0];
+        size_t nv = (size_t)L.mesh.nn * L.mesh.dim;
+        cudaEvent_t e0, e1;
+        UWG_CUDA(cudaEventCreate(&e0));
+        UWG_CUDA(cudaEventCreate(&e1));
+        if (f32) {
+            UWG_CUDA(cudaMemsetAsync(L.b32.p, 0, nv * sizeof(float), c.stream));
+            UWG_CUDA(cudaEventRecord(e0, c.stream));
+            for (int i = 0; i < iterations; ++i) uwg::level_smooth<float>(c, L, L.b32.p, L.x32.p, sweeps, true);
+        } else {
+            UWG_CUDA(cudaMemsetAsync(L.b64.p, 0, nv * sizeof(double), c.stream));
+            UWG_CUDA(cudaEventRecord(e0, c.stream));
+            for (int i = 0; i < iterations; ++i) uwg::level_smooth<double>(c, L, L.b64.p, L.x64.p, sweeps, true);
+        }
+        UWG_CUDA(cudaEventRecord(e1, c.stream));
+        UWG_CUDA(cudaEventSynchronize(e1));
+        float t = 0.f;
+        UWG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        *ms = t;
+    });
+}
+
 int uwgpu_get_stream(uwgpu_ctx* ctx, void** stream) {
     return guarded(ctx, [&](Context& c) {
         UWG_REQUIRE(stream, UWGPU_ERR_ARGUMENT, "null output");

@@ -221,6 +221,8 @@ void assemble(Context& c);
 void build_operator(Context& c, int levels, bool need32);
 void apply_fine(Context& c, bool fp32, const double* x, double* y);  // device SoA vectors
 void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep);
+template <typename T> void level_apply(Context&, const Level&, const T*, T*);
+template <typename T> void level_smooth(Context&, const Level&, const T*, T*, int, bool);
 
 // Number of packed entries of a symmetric nd x nd element matrix.
 __host__ __device__ constexpr int packed_size(int nd) { return nd * (nd + 1) / 2; }

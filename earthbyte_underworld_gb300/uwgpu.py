@@ -114,6 +114,8 @@ def load(build_if_missing: bool = True):
         L.uwgpu_profile_read.argtypes = [P, C.c_int32, P, P]
         L.uwgpu_profile_read_work.argtypes = [P, C.c_int32, P, P]
         L.uwgpu_get_stream.argtypes = [P, P]
+        L.uwgpu_time_apply.argtypes = [P, C.c_int32, C.c_int32, P]
+        L.uwgpu_time_smooth.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, P]
         L.uwgpu_launch_count.argtypes = [P]
         L.uwgpu_launch_count.restype = C.c_int64
         _lib = L
@@ -290,6 +292,16 @@ class Context:
         f = C.c_double()
         self._check(self._L.uwgpu_profile_read_work(self._h, which, C.byref(b), C.byref(f)))
         return b.value, f.value
+
+    def time_apply(self, precision=PREC_FP64, iterations=20):
+        ms = C.c_double()
+        self._check(self._L.uwgpu_time_apply(self._h, precision, iterations, C.byref(ms)))
+        return ms.value
+
+    def time_smooth(self, precision=PREC_FP64, sweeps=2, iterations=10):
+        ms = C.c_double()
+        self._check(self._L.uwgpu_time_smooth(self._h, precision, sweeps, iterations, C.byref(ms)))
+        return ms.value
 
     def stream(self) -> int:
         s = C.c_void_p()

@@ -217,6 +217,14 @@ int64_t uwgpu_launch_count(const uwgpu_ctx* ctx);
  * record timing events on it. */
 int uwgpu_get_stream(uwgpu_ctx* ctx, void** stream);
 
+/* Kernel timing hooks (no reference counterpart; used by the benchmark and the profiles).
+ * Each runs `iterations` back-to-back launches on the fine level, on vectors resident in the
+ * context, and returns the elapsed device time in milliseconds (CUDA events on the context
+ * stream).  uwgpu_time_apply: the operator apply y = K x; uwgpu_time_smooth: one smoothing call
+ * of `sweeps` symmetric colour Gauss-Seidel sweeps.  precision as in uwgpu_operator_apply. */
+int uwgpu_time_apply(uwgpu_ctx* ctx, int32_t precision, int32_t iterations, double* ms);
+int uwgpu_time_smooth(uwgpu_ctx* ctx, int32_t precision, int32_t sweeps, int32_t iterations, double* ms);
+
 /* Allocation-free binning + mapping.  This entry point has no counterpart in the reference; it
  * exists for callers that cannot allocate device memory while they run (a host framework that
  * owns every device buffer through its own pool, or code where an allocation would synchronise
