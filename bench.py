@@ -170,7 +170,7 @@ def make_workload(nel, shuffle=True):
 # (-Q22_pc_type gtkg, Solvers/KSPSolvers/src/BSSCR/pc_ScaledGtKG.c) and FGMRES velocity solves
 # (-A11_ksp_type fgmres, Solvers/SysTest/ConvergenceTests/options-solv-mg.opt); tolerances chosen so
 # that the full Stokes residual reaches 1e-6
-SOLVE_KW = dict(mg_levels=4, smooth_down=2, smooth_up=2, schur_type=1, schur_pc=3, scr_rtol=1e-7, a11_rtol=1e-6,
+SOLVE_KW = dict(mg_levels=4, smooth_down=1, smooth_up=1, schur_type=1, schur_pc=3, scr_rtol=1e-7, a11_rtol=1e-6,
                 back_rtol=1e-7, restart=30, max_outer=500, max_inner=2000, bfbt_rtol=1e-2, bfbt_max_it=2000)
 
 
@@ -188,7 +188,7 @@ def cpu_step(O, w, nthreads):
     Ke, fe, Ge, Se, _ = O.assemble(m, off, perm, xi, w["material"], mats, f, nthreads=nthreads)
     t1 = time.perf_counter()
     levels = 3 if w["nel"][0] % 4 == 0 else 2
-    u, p, rep = O.solve_bsscr(m, w["fixed"], Ke, Ge, fe, Se, mg_levels=levels, smooth=2,
+    u, p, rep = O.solve_bsscr(m, w["fixed"], Ke, Ge, fe, Se, mg_levels=levels, smooth=SOLVE_KW["smooth_down"],
                               schur_type=SOLVE_KW["schur_type"], schur_pc=SOLVE_KW["schur_pc"],
                               scr_rtol=SOLVE_KW["scr_rtol"], a11_rtol=SOLVE_KW["a11_rtol"],
                               back_rtol=SOLVE_KW["back_rtol"], bfbt_rtol=SOLVE_KW["bfbt_rtol"],
@@ -233,7 +233,7 @@ def run_reference(args):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": f"stokes3d_spheres_{args.cpu_nel}cube_27ppc (bounded sample of the 64^3 workload)",
-                      "precision": "fp64", "solver": "BSSCR: Schur FGMRES(scaled BFBt) / A11 FGMRES + GMG (SOR 2+2)", "rel_residual": res},
+                      "precision": "fp64", "solver": "BSSCR: Schur FGMRES(scaled BFBt) / A11 FGMRES + GMG (SOR 1+1)", "rel_residual": res},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                             "sample": f"{args.cpu_nel}^3 elements, {n} points, full step per iteration"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -388,7 +388,7 @@ def run_ours(args):
                "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32/f64", "data": "synthetic",
                "config": {"workload": f"stokes3d_spheres_{nel}cube_27ppc_50spheres", "elements": ne,
                           "points": npts, "precision": prec, "mg_levels": SOLVE_KW["mg_levels"],
-                          "solver": "BSSCR: Schur FGMRES(scaled BFBt) / A11 FGMRES + GMG (colour block-GS 2+2)",
+                          "solver": "BSSCR: Schur FGMRES(scaled BFBt) / A11 FGMRES + GMG (colour block-GS 1+1)",
                           "target_rel_residual": 1e-6, "rel_residual": rep.rel_residual,
                           "outer_its": rep.outer_its, "inner_its": rep.inner_its_total, "vcycles": rep.vcycles,
                           "stokes_solve_s": rep.t_solve_ms / 1e3, "setup_ms": rep.t_setup_ms,

@@ -67,7 +67,25 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: " + r.stdout + r.stderr)
+    build_host()
     return LIB
+
+
+HOST = os.path.join(BUILD, "uw_stokes_host")
+
+
+def build_host() -> str:
+    """Compiles the C host program (host/uw_stokes_host.c) against libuwgpu.so with gcc."""
+    src = os.path.join(HERE, "host", "uw_stokes_host.c")
+    if os.path.exists(HOST) and os.path.getmtime(HOST) >= max(os.path.getmtime(src), os.path.getmtime(LIB)):
+        return HOST
+    cc = shutil.which("gcc") or shutil.which("cc")
+    cmd = [cc, "-O2", "-std=c11", "-Wall", src, "-I", os.path.join(HERE, "..", "include"), "-L", BUILD, "-luwgpu",
+           "-Wl,-rpath,$ORIGIN", "-lm", "-o", HOST]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("host build failed: " + r.stdout + r.stderr)
+    return HOST
 
 
 if __name__ == "__main__":

@@ -156,6 +156,8 @@ struct Context {
     // per-axis element widths of the fine mesh (device), and the mesh they belong to
     DArray<double> elem_h;
     int64_t elem_h_for = -1;
+    DArray<float> elem_h32;
+    int64_t elem_h32_for = -2;
 
     // solver state
     Level levels[kMaxLevels];

@@ -1010,11 +1010,27 @@ void bfbt_weights(Context& c, double* W) {
 
 // ------------------------------------------------------------------------------------------
 // Device-resident Jacobi-preconditioned CG on G^T W G (the inner solves of the scaled BFBt
-// preconditioner).  The scalars live in device memory (double-buffered by iteration parity),
-// so an iteration is four fused kernels with no host round trip; the host reads the residual
-// norm every few iterations to test convergence.
+// preconditioner), in FP64 or FP32 arithmetic (T).  The scalars live in device memory as FP64
+// (double-buffered by iteration parity), so an iteration is four fused kernels with no host
+// round trip; the host reads the residual norm every few iterations to test convergence.
 //   scal[0] = p.q   scal[1], scal[2] = r.z (parity)   scal[3] = r.r   scal[4] = r0.r0
 // ------------------------------------------------------------------------------------------
+template <typename T>
+struct GeoT {
+    const T* h;     // element widths per axis
+    int off[3];
+};
+
+template <int DIM, typename T>
+__device__ __forceinline__ T gvalT(const T h[3], int a, int d) {
+    T area = (T)1;
+#pragma unroll
+    for (int q = 0; q < DIM; ++q)
+        if (q != d) area *= h[q];
+    T s = ((a >> d) & 1) ? (T)1 : (T)-1;
+    return -s * area * (T)(DIM == 3 ? 0.25 : 0.5);
+}
+
 __device__ __forceinline__ double block_sum(double v, double* sw) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -1028,16 +1044,16 @@ __device__ __forceinline__ double block_sum(double v, double* sw) {
 }
 
 // s = W (G p)
-template <int DIM>
-__global__ void k_pcg_gp(Grid g, GeoArgs geo, const double* __restrict__ p, const double* __restrict__ W,
-                         const uint8_t* __restrict__ fixed, double* __restrict__ s) {
+template <int DIM, typename T>
+__global__ void k_pcg_gp(Grid g, GeoT<T> geo, const T* __restrict__ p, const T* __restrict__ W,
+                         const uint8_t* __restrict__ fixed, T* __restrict__ s) {
     int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= g.nn) return;
     int64_t idx[3] = {n % g.nx, (n / g.nx) % g.ny, DIM == 3 ? n / (g.nx * g.ny) : 0};
     int64_t ecount[3] = {g.ex, g.ey, g.ez};
-    double acc[DIM];
+    T acc[DIM];
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) acc[d] = 0.0;
+    for (int d = 0; d < DIM; ++d) acc[d] = (T)0;
 #pragma unroll
     for (int o = 0; o < (1 << DIM); ++o) {
         int64_t e3[3] = {0, 0, 0};
@@ -1049,40 +1065,43 @@ __global__ void k_pcg_gp(Grid g, GeoArgs geo, const double* __restrict__ p, cons
         }
         if (!ok) continue;
         int64_t e = e3[0] + (int64_t)g.ex * (e3[1] + (int64_t)g.ey * e3[2]);
-        double h[3];
-        element_h<DIM>(geo, e3[0], e3[1], e3[2], h);
-        double pe = p[e];
+        T h[3];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) acc[d] += gval<DIM>(h, o, d) * pe;
+        for (int d = 0; d < DIM; ++d) h[d] = __ldg(geo.h + geo.off[d] + e3[d]);
+        T pe = p[e];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) acc[d] = fma(gvalT<DIM, T>(h, o, d), pe, acc[d]);
     }
 #pragma unroll
     for (int d = 0; d < DIM; ++d)
-        s[(int64_t)d * g.nn + n] = (fixed && fixed[n * DIM + d]) ? 0.0 : acc[d] * W[(int64_t)d * g.nn + n];
+        s[(int64_t)d * g.nn + n] = (fixed && fixed[n * DIM + d]) ? (T)0 : acc[d] * W[(int64_t)d * g.nn + n];
 }
 
-// q = G^T s ; scal[0] += p.q ; also clears the accumulators the next kernel fills
-template <int DIM>
-__global__ void k_pcg_gts(Grid g, GeoArgs geo, const double* __restrict__ s, const double* __restrict__ p,
-                          double* __restrict__ q, double* __restrict__ scal, int parity) {
+// q = G^T s ; scal[0] += p.q (when scal is given); clears the accumulators the next kernel fills
+template <int DIM, typename T>
+__global__ void k_pcg_gts(Grid g, GeoT<T> geo, const T* __restrict__ s, const T* __restrict__ p,
+                          T* __restrict__ q, double* __restrict__ scal, int parity) {
     __shared__ double sw[32];
     int64_t ne = (int64_t)g.ex * g.ey * g.ez;
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     double local = 0.0;
     if (e < ne) {
-        int64_t ie = e % g.ex, je = (e / g.ex) % g.ey, ke = DIM == 3 ? e / ((int64_t)g.ex * g.ey) : 0;
-        double h[3];
-        element_h<DIM>(geo, ie, je, ke, h);
-        int64_t base = ie + g.nx * (je + g.ny * ke);
-        double acc = 0.0;
+        int64_t i3[3] = {e % g.ex, (e / g.ex) % g.ey, DIM == 3 ? e / ((int64_t)g.ex * g.ey) : 0};
+        T h[3];
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) h[d] = __ldg(geo.h + geo.off[d] + i3[d]);
+        int64_t base = i3[0] + g.nx * (i3[1] + g.ny * i3[2]);
+        T acc = (T)0;
 #pragma unroll
         for (int a = 0; a < (1 << DIM); ++a) {
             int64_t n = base + (a & 1) + ((a >> 1) & 1) * g.nx + (DIM == 3 ? ((a >> 2) & 1) * g.nx * g.ny : 0);
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) acc += gval<DIM>(h, a, d) * s[(int64_t)d * g.nn + n];
+            for (int d = 0; d < DIM; ++d) acc = fma(gvalT<DIM, T>(h, a, d), s[(int64_t)d * g.nn + n], acc);
         }
         q[e] = acc;
-        local = acc * p[e];
+        if (p) local = (double)acc * (double)p[e];
     }
+    if (!scal) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         scal[1 + (parity ^ 1)] = 0.0;  // r.z of this iteration (filled by k_pcg_update)
         scal[3] = 0.0;
@@ -1092,21 +1111,22 @@ __global__ void k_pcg_gts(Grid g, GeoArgs geo, const double* __restrict__ s, con
 }
 
 // alpha = rz/pq ; x += alpha p ; r -= alpha q ; z = r/d ; scal[rz_new] += r.z ; scal[3] += r.r
-__global__ void k_pcg_update(int64_t ne, const double* __restrict__ p, const double* __restrict__ q,
-                             const double* __restrict__ d, double* __restrict__ x, double* __restrict__ r,
-                             double* __restrict__ z, double* __restrict__ scal, int parity) {
+template <typename T>
+__global__ void k_pcg_update(int64_t ne, const T* __restrict__ p, const T* __restrict__ q, const T* __restrict__ d,
+                             T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, double* __restrict__ scal,
+                             int parity) {
     __shared__ double sw[32];
-    double alpha = scal[1 + parity] / scal[0];
+    T alpha = (T)(scal[1 + parity] / scal[0]);
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     double rz = 0.0, rr = 0.0;
     if (e < ne) {
         x[e] = fma(alpha, p[e], x[e]);
-        double re = fma(-alpha, q[e], r[e]);
+        T re = fma(-alpha, q[e], r[e]);
         r[e] = re;
-        double ze = re / d[e];
+        T ze = re / d[e];
         z[e] = ze;
-        rz = re * ze;
-        rr = re * re;
+        rz = (double)re * (double)ze;
+        rr = (double)re * (double)re;
     }
     double t1 = block_sum(rz, sw);
     __syncthreads();
@@ -1118,31 +1138,32 @@ __global__ void k_pcg_update(int64_t ne, const double* __restrict__ p, const dou
 }
 
 // beta = rz_new/rz ; p = z + beta p ; clears p.q for the next iteration
-__global__ void k_pcg_dir(int64_t ne, const double* __restrict__ z, double* __restrict__ p, double* __restrict__ scal,
+template <typename T>
+__global__ void k_pcg_dir(int64_t ne, const T* __restrict__ z, T* __restrict__ p, double* __restrict__ scal,
                           int parity) {
-    double beta = scal[1 + (parity ^ 1)] / scal[1 + parity];
+    T beta = (T)(scal[1 + (parity ^ 1)] / scal[1 + parity]);
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e < ne) p[e] = fma(beta, p[e], z[e]);
     if (blockIdx.x == 0 && threadIdx.x == 0) scal[0] = 0.0;
 }
 
-// initial state: r = b - mean(b) (already projected by the caller), z = r/d, p = z, x = 0,
-// scal[1] = r.z, scal[3] = scal[4] = r.r, scal[0] = 0
-__global__ void k_pcg_init(int64_t ne, const double* __restrict__ b, const double* __restrict__ d,
-                           double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
-                           double* __restrict__ p, double* __restrict__ scal) {
+// initial state: r = b (projected by the caller), z = r/d, p = z, x = 0, scal[1] = r.z,
+// scal[3] = scal[4] = r.r
+template <typename B, typename T>
+__global__ void k_pcg_init(int64_t ne, const B* __restrict__ b, const T* __restrict__ d, T* __restrict__ x,
+                           T* __restrict__ r, T* __restrict__ z, T* __restrict__ p, double* __restrict__ scal) {
     __shared__ double sw[32];
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     double rz = 0.0, rr = 0.0;
     if (e < ne) {
-        double re = b[e];
-        double ze = re / d[e];
-        x[e] = 0.0;
+        T re = (T)b[e];
+        T ze = re / d[e];
+        x[e] = (T)0;
         r[e] = re;
         z[e] = ze;
         p[e] = ze;
-        rz = re * ze;
-        rr = re * re;
+        rz = (double)re * (double)ze;
+        rr = (double)re * (double)re;
     }
     double t1 = block_sum(rz, sw);
     __syncthreads();
@@ -1154,24 +1175,50 @@ __global__ void k_pcg_init(int64_t ne, const double* __restrict__ b, const doubl
     }
 }
 
+template <typename T>
+static GeoT<T> geo_T(Context& c, const MeshDesc& m);
+template <>
+GeoT<double> geo_T<double>(Context& c, const MeshDesc& m) {
+    GeoArgs a = geo_of(c, m);
+    GeoT<double> g;
+    g.h = a.h;
+    for (int d = 0; d < 3; ++d) g.off[d] = a.off[d];
+    return g;
+}
+template <>
+GeoT<float> geo_T<float>(Context& c, const MeshDesc& m) {
+    GeoArgs a = geo_of(c, m);
+    size_t n = (size_t)m.nel[0] + m.nel[1] + (m.dim == 3 ? m.nel[2] : 0);
+    if (c.elem_h32_for != c.elem_h_for) {
+        c.elem_h32.ensure(n);
+        LaunchScope ls(c, -1);
+        k_convert<double, float><<<blocks_for((int64_t)n, 256), 256, 0, c.stream>>>((int64_t)n, a.h, c.elem_h32.p);
+        c.elem_h32_for = c.elem_h_for;
+    }
+    GeoT<float> g;
+    g.h = c.elem_h32.p;
+    for (int d = 0; d < 3; ++d) g.off[d] = a.off[d];
+    return g;
+}
+
 // Solves (G^T W G) x = b (b projected off the constant by the caller) to ||r|| <= rtol ||b||.
-// work must hold 4*ne doubles plus 8 scalars; s is a velocity-sized temporary.
-int gwg_pcg(Context& c, const double* W, const double* d, const double* b, double* x, double rtol, int maxit,
-            double* work, double* s) {
+// work holds 4*ne values of T; scal 8 doubles; s is a velocity-sized temporary.
+template <typename T>
+static int gwg_pcg_T(Context& c, const T* W, const T* d, const double* b, T* x, double rtol, int maxit, T* work,
+                     T* s, double* scal) {
     const Level& L = c.levels[0];
     Grid g = grid_of(L.mesh);
-    GeoArgs geo = geo_of(c, L.mesh);
+    GeoT<T> geo = geo_T<T>(c, L.mesh);
     int64_t ne = L.mesh.ne;
-    double* r = work;
-    double* z = work + ne;
-    double* p = work + 2 * ne;
-    double* q = work + 3 * ne;
-    double* scal = work + 4 * ne;
+    T* r = work;
+    T* z = work + ne;
+    T* p = work + 2 * ne;
+    T* q = work + 3 * ne;
     UWG_CUDA(cudaMemsetAsync(scal, 0, 8 * sizeof(double), c.stream));
     unsigned eb = blocks_for(ne, 256), nb = blocks_for(g.nn, 256);
     {
         LaunchScope ls(c, -1);
-        k_pcg_init<<<eb, 256, 0, c.stream>>>(ne, b, d, x, r, z, p, scal);
+        k_pcg_init<double, T><<<eb, 256, 0, c.stream>>>(ne, b, d, x, r, z, p, scal);
     }
     double* hs = c.host_scalars;
     UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -1184,21 +1231,21 @@ int gwg_pcg(Context& c, const double* W, const double* d, const double* b, doubl
         int parity = it & 1;
         {
             LaunchScope ls(c, -1);
-            if (g.dim == 3) k_pcg_gp<3><<<nb, 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
-            else k_pcg_gp<2><<<nb, 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
+            if (g.dim == 3) k_pcg_gp<3, T><<<nb, 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
+            else k_pcg_gp<2, T><<<nb, 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
         }
         {
             LaunchScope ls(c, -1);
-            if (g.dim == 3) k_pcg_gts<3><<<eb, 256, 0, c.stream>>>(g, geo, s, p, q, scal, parity);
-            else k_pcg_gts<2><<<eb, 256, 0, c.stream>>>(g, geo, s, p, q, scal, parity);
+            if (g.dim == 3) k_pcg_gts<3, T><<<eb, 256, 0, c.stream>>>(g, geo, s, p, q, scal, parity);
+            else k_pcg_gts<2, T><<<eb, 256, 0, c.stream>>>(g, geo, s, p, q, scal, parity);
         }
         {
             LaunchScope ls(c, -1);
-            k_pcg_update<<<eb, 256, 0, c.stream>>>(ne, p, q, d, x, r, z, scal, parity);
+            k_pcg_update<T><<<eb, 256, 0, c.stream>>>(ne, p, q, d, x, r, z, scal, parity);
         }
         {
             LaunchScope ls(c, -1);
-            k_pcg_dir<<<eb, 256, 0, c.stream>>>(ne, z, p, scal, parity);
+            k_pcg_dir<T><<<eb, 256, 0, c.stream>>>(ne, z, p, scal, parity);
         }
         it++;
         if (it % check_every == 0 || it == maxit) {
@@ -1211,6 +1258,45 @@ int gwg_pcg(Context& c, const double* W, const double* d, const double* b, doubl
     }
     check_launch("gwg_pcg");
     return it;
+}
+
+int gwg_pcg(Context& c, const double* W, const double* d, const double* b, double* x, double rtol, int maxit,
+            double* work, double* s) {
+    return gwg_pcg_T<double>(c, W, d, b, x, rtol, maxit, work, s, work + 4 * c.levels[0].mesh.ne);
+}
+
+int gwg_pcg32(Context& c, const float* W, const float* d, const double* b, float* x, double rtol, int maxit,
+              float* work, float* s, double* scal) {
+    return gwg_pcg_T<float>(c, W, d, b, x, rtol, maxit, work, s, scal);
+}
+
+// FP32 pieces of the scaled BFBt apply: s = W (G p) and q = G^T s
+void op_wg32(Context& c, const float* p, const float* W, float* s) {
+    const Level& L = c.levels[0];
+    Grid g = grid_of(L.mesh);
+    GeoT<float> geo = geo_T<float>(c, L.mesh);
+    LaunchScope ls(c, -1);
+    if (g.dim == 3) k_pcg_gp<3, float><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
+    else k_pcg_gp<2, float><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
+}
+
+void op_gt32(Context& c, const float* s, float* q) {
+    const Level& L = c.levels[0];
+    Grid g = grid_of(L.mesh);
+    GeoT<float> geo = geo_T<float>(c, L.mesh);
+    LaunchScope ls(c, -1);
+    if (g.dim == 3) k_pcg_gts<3, float><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo, s, nullptr, q, nullptr, 0);
+    else k_pcg_gts<2, float><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo, s, nullptr, q, nullptr, 0);
+}
+
+void to_float(Context& c, const double* a, float* b, int64_t n) {
+    LaunchScope ls(c, -1);
+    k_convert<double, float><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, a, b);
+}
+
+void to_double(Context& c, const float* a, double* b, int64_t n) {
+    LaunchScope ls(c, -1);
+    k_convert<float, double><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, a, b);
 }
 
 void gwg_diag(Context& c, const double* W, double* S) {

@@ -34,6 +34,12 @@ void bfbt_weights(Context& c, double* W);
 void gwg_diag(Context& c, const double* W, double* S);
 int gwg_pcg(Context& c, const double* W, const double* d, const double* b, double* x, double rtol, int maxit,
             double* work, double* s);
+int gwg_pcg32(Context& c, const float* W, const float* d, const double* b, float* x, double rtol, int maxit,
+              float* work, float* s, double* scal);
+void op_wg32(Context& c, const float* p, const float* W, float* s);
+void op_gt32(Context& c, const float* s, float* q);
+void to_float(Context& c, const double* a, float* b, int64_t n);
+void to_double(Context& c, const float* a, double* b, int64_t n);
 
 // ------------------------------------------------------------------------------------------
 // Vector kernels
@@ -67,6 +73,11 @@ __global__ void k_sub_from(int64_t n, const T* __restrict__ x, T* __restrict__ y
 }
 
 __global__ void k_pointwise_mul(int64_t n, const double* __restrict__ x, const double* __restrict__ d, double* __restrict__ y) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = x[i] * d[i];
+}
+
+__global__ void k_pointwise_mul32(int64_t n, const float* __restrict__ x, const float* __restrict__ d, float* __restrict__ y) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] = x[i] * d[i];
 }
@@ -384,6 +395,9 @@ struct Bsscr {
     DArray<double> f, h, hhat, tu, tu2, t2, Sd, rhs_p, ref_r, ref_d;
     // scaled BFBt state: weights, G^T W G diagonal, work vectors
     DArray<double> bw, bd, bt, bt2, bs, bX, pr, pz, pp, pq, ptmp;
+    // FP32 copies for the mixed form (the preconditioner runs in FP32 inside the FP64 Schur FGMRES)
+    DArray<float> bw32, bd32, bt32, bt2_32, bs32, bX32, pz32;
+    DArray<double> scal32;
     int64_t bfbt_its = 0;
     DArray<float> r32, d32;
     bool nan = false;
@@ -505,8 +519,32 @@ struct Bsscr {
         bfbt_its += gwg_pcg(c, bw.p, bd.p, pr.p, x, rtol, maxit, pz.p, bs.p);
     }
 
+    // the same preconditioner with FP32 operators, inner solves and vectors (mixed form)
+    void bfbt_apply32(const double* x, double* y) {
+        int maxit = o.bfbt_max_it > 0 ? o.bfbt_max_it : 500;
+        double rtol = o.bfbt_rtol > 0 ? o.bfbt_rtol : 1e-4;
+        copy<double>(c, npres, x, pr.p);
+        remove_constant_dev(pr.p);
+        bfbt_its += gwg_pcg32(c, bw32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, bs32.p, scal32.p);
+        op_wg32(c, bt32.p, bw32.p, bs32.p);
+        level_apply<float>(c, c.levels[0], bs32.p, bX32.p);
+        {
+            LaunchScope ls(c, -1);
+            k_pointwise_mul32<<<blocks_for(nv, 256), 256, 0, c.stream>>>(nv, bX32.p, bw32.p, bX32.p);
+        }
+        op_gt32(c, bX32.p, bt2_32.p);
+        to_double(c, bt2_32.p, pr.p, npres);
+        remove_constant_dev(pr.p);
+        bfbt_its += gwg_pcg32(c, bw32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, bs32.p, scal32.p);
+        to_double(c, bt32.p, y, npres);
+    }
+
     // pc_ScaledGtKG.c:242-310: y = (G^T W G)^-1 G^T W K W G (G^T W G)^-1 x
     void bfbt_apply(const double* x, double* y) {
+        if (mixed) {
+            bfbt_apply32(x, y);
+            return;
+        }
         gwg_solve(x, bt.p);
         op_G(c, bt.p, bs.p);
         pmul(nv, bs.p, bw.p, bs.p);
@@ -746,6 +784,14 @@ void Bsscr::run() {
         pz.ensure(4 * npres + 8);
         bfbt_weights(c, bw.p);
         gwg_diag(c, bw.p, bd.p);
+        if (mixed) {
+            for (auto* v : {&bw32, &bs32, &bX32}) v->ensure(nv);
+            for (auto* v : {&bd32, &bt32, &bt2_32}) v->ensure(npres);
+            pz32.ensure(4 * npres);
+            scal32.ensure(8);
+            to_float(c, bw.p, bw32.p, nv);
+            to_float(c, bd.p, bd32.p, npres);
+        }
     }
     UWG_CUDA(cudaStreamSynchronize(c.stream));
     auto t1 = std::chrono::steady_clock::now();

@@ -36,3 +36,10 @@ def test_create_without_device_fails_cleanly():
     from earthbyte_underworld_gb300 import uwgpu as U
     with pytest.raises(U.UwgpuError):
         U.Context(0)
+
+
+def test_c_host_program_builds_against_the_abi():
+    """The C host side (the reference's own language) compiles and links against libuwgpu.so."""
+    from earthbyte_underworld_gb300 import build
+    build.build()
+    assert os.path.exists(build.build_host())

@@ -159,3 +159,18 @@ def test_mixed_precision_solve(oracle, uw):
     # error of the mixed-precision solution against the FP64 solve
     assert _rel(um, u64) < 1e-5
     ctx.close()
+
+
+def test_c_host_program_solves():
+    """The C host program drives map -> assemble -> BSSCR through the C ABI."""
+    import json
+    import subprocess
+    from earthbyte_underworld_gb300 import build
+    build.build()
+    out = subprocess.run([build.build_host(), "--elementResI=32", "--elementResJ=32", "--mgLevels=3"],
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    rep = json.loads(out.stdout.strip().splitlines()[-1])
+    assert rep["points"] == 32 * 32 * 20
+    assert rep["rel_residual"] < 1e-6
+    assert rep["vmax"] > 0.0
