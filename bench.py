@@ -170,7 +170,7 @@ def make_workload(nel, shuffle=True):
 # (-Q22_pc_type gtkg, Solvers/KSPSolvers/src/BSSCR/pc_ScaledGtKG.c) and FGMRES velocity solves
 # (-A11_ksp_type fgmres, Solvers/SysTest/ConvergenceTests/options-solv-mg.opt); tolerances chosen so
 # that the full Stokes residual reaches 1e-6
-SOLVE_KW = dict(mg_levels=4, smooth_down=1, smooth_up=1, schur_type=1, schur_pc=3, scr_rtol=1e-7, a11_rtol=1e-6,
+SOLVE_KW = dict(mg_levels=4, smooth_down=2, smooth_up=2, smoother=1, schur_type=1, schur_pc=3, scr_rtol=1e-7, a11_rtol=1e-6,
                 back_rtol=1e-7, restart=30, max_outer=500, max_inner=2000, bfbt_rtol=1e-2, bfbt_max_it=2000)
 
 
@@ -271,7 +271,8 @@ def run_ours(args):
         _, _, rep = ctx.solve_bsscr(opts, want=False)
         return rep
 
-    def timed(opts, profile, warmup=None):
+    def timed(opts, profile, warmup=None, steps=None):
+        nsteps = args.steps if steps is None else steps
         for _ in range(args.warmup if warmup is None else warmup):
             step(opts)
         torch.cuda.synchronize()
@@ -285,7 +286,7 @@ def run_ours(args):
         ev = []
         reps = []
         wall0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(nsteps):
             flush_buf.zero_()
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
@@ -304,7 +305,9 @@ def run_ours(args):
         prof = {}
         if profile:
             for name, fam in (("assembly", U.KERNEL_ASSEMBLY), ("apply", U.KERNEL_APPLY),
-                              ("smooth", U.KERNEL_SMOOTH), ("binning", U.KERNEL_BINNING)):
+                              ("smooth", U.KERNEL_SMOOTH), ("binning", U.KERNEL_BINNING),
+                              ("schur_pc", U.KERNEL_SCHUR_PC), ("vector", U.KERNEL_VECTOR),
+                              ("transfer", U.KERNEL_TRANSFER)):
                 n, t = ctx.profile_read(fam)
                 b, f = ctx.profile_work(fam)
                 prof[name] = {"launches": n, "ms": t, "bytes": b, "flops": f}
@@ -312,7 +315,11 @@ def run_ours(args):
         return ms, wall, launches, reps, clk, prof
 
     prec = args.precision
-    ms, wall, launches, reps, clk, prof = timed(opts_for(prec), profile=True)
+    ms, wall, launches, reps, clk, _ = timed(opts_for(prec), profile=False)
+    # One more step of the same workload with every launch of the profiled kernel families
+    # bracketed by CUDA events on the library stream: the per-family times and the roofline come
+    # from it (the events add host work, so the timed steps above run without them).
+    _, _, _, _, _, prof = timed(opts_for(prec), profile=True, warmup=0, steps=1)
     ms_max = dist.max(ms)
     step_ms = ms_max / args.steps
     value = dist.sum(npts) / (ms_max / 1e3 / args.steps)
@@ -320,7 +327,8 @@ def run_ours(args):
 
     # roofline of the dominant kernel family
     peak, peak_kind = measured_peaks()
-    dom = max(prof, key=lambda k: prof[k]["ms"])
+    # the dominant kernel family with an algorithmic byte count (the roofline's subject)
+    dom = max((k for k in prof if prof[k]["bytes"] > 0), key=lambda k: prof[k]["ms"])
     d = prof[dom]
     achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9 if d["ms"] > 0 else 0.0
     fp64_tflops = d["flops"] / (d["ms"] / 1e3) / 1e12 if d["ms"] > 0 else 0.0
@@ -388,7 +396,7 @@ def run_ours(args):
                "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32/f64", "data": "synthetic",
                "config": {"workload": f"stokes3d_spheres_{nel}cube_27ppc_50spheres", "elements": ne,
                           "points": npts, "precision": prec, "mg_levels": SOLVE_KW["mg_levels"],
-                          "solver": "BSSCR: Schur FGMRES(scaled BFBt) / A11 FGMRES + GMG (colour block-GS 1+1)",
+                          "solver": "BSSCR: Schur FGMRES(scaled BFBt) / A11 FGMRES + GMG (Chebyshev block-Jacobi, degree 2+2)",
                           "target_rel_residual": 1e-6, "rel_residual": rep.rel_residual,
                           "outer_its": rep.outer_its, "inner_its": rep.inner_its_total, "vcycles": rep.vcycles,
                           "stokes_solve_s": rep.t_solve_ms / 1e3, "setup_ms": rep.t_setup_ms,

@@ -332,6 +332,7 @@ void uwgpu_solve_opts_default(uwgpu_solve_opts* o) {
     o->target_rel_residual = 0.0;
     o->bfbt_rtol = 1e-2;
     o->bfbt_max_it = 500;
+    o->smoother = UWGPU_SMOOTHER_COLOUR_GS;
 }
 
 int uwgpu_solve_bsscr(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, double* u, double* p, uwgpu_report* report) {

@@ -92,6 +92,7 @@ struct Level {
     DArray<float> r32, x32, b32, t32;
     // coarsest level: dense inverse of the full-dof operator
     DArray<double> Cinv;
+    double lmax = 0.0;       // largest eigenvalue estimate of Dinv A (Chebyshev smoother)
     int64_t ncoarse = 0;
     bool has32 = false;
 };
@@ -170,6 +171,17 @@ struct Context {
 
     bool profiling = false;
     ProfileFamily prof[UWGPU_KERNEL_COUNT];
+
+    // CUDA graphs of the BFBt inner-CG iteration block, one per buffer set
+    struct PcgGraph {
+        const void* key[8];
+        cudaGraphExec_t exec = nullptr;
+    };
+    std::vector<PcgGraph> pcg_graphs;
+    ~Context() {
+        for (auto& g : pcg_graphs)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+    }
 };
 
 // Launch bookkeeping: counts every launch, and brackets the launch with events when the

@@ -20,6 +20,9 @@
 // which equals the Galerkin product for this interpolation.
 #include <cooperative_groups.h>
 
+#include <algorithm>
+#include <iterator>
+
 #include "internal.cuh"
 
 namespace cg = cooperative_groups;
@@ -278,6 +281,55 @@ __global__ void __launch_bounds__(kRowThreads) k_gs_sweeps(Grid g, const T* __re
             }
             grid.sync();
         }
+    }
+}
+
+// One Chebyshev step of the block-Jacobi preconditioned operator D^-1 A (row-split):
+//   z = Dinv (b - A xin);  d = c1 d + c2 z (d = c2 z on the first step);  xout = xin + d.
+// xin == nullptr stands for a zero initial guess.  Every node is relaxed from the old iterate, so
+// no colouring and no grid barrier are needed.
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kRowThreads) k_cheb_step(Grid g, const T* __restrict__ A, const T* __restrict__ Dinv,
+                                                           const T* __restrict__ b, const T* __restrict__ xin,
+                                                           T* __restrict__ xout, T* __restrict__ d, T c1, T c2,
+                                                           int first) {
+    __shared__ T sres[kRowThreads];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int r = warp % DIM, grp = warp / DIM;
+    int64_t n = (int64_t)blockIdx.x * (kRowThreads / DIM) + grp * 32 + lane;
+    bool act = n < g.nn;
+    T res = (T)0;
+    if (act) {
+        int64_t i = n % g.nx, j = (n / g.nx) % g.ny, k = DIM == 3 ? n / (g.nx * g.ny) : 0;
+        res = b[(int64_t)r * g.nn + n];
+        if (xin) res -= stencil_row_r<DIM, T>(g, n, i, j, k, r, A, xin);
+    }
+    sres[threadIdx.x] = res;
+    __syncthreads();
+    if (!act) return;
+    T z = (T)0;
+#pragma unroll
+    for (int cc = 0; cc < DIM; ++cc) z = fma(Dinv[(int64_t)(r * DIM + cc) * g.nn + n], sres[(grp * DIM + cc) * 32 + lane], z);
+    int64_t idx = (int64_t)r * g.nn + n;
+    T dn = first ? c2 * z : fma(c1, d[idx], c2 * z);
+    d[idx] = dn;
+    xout[idx] = (xin ? xin[idx] : (T)0) + dn;
+}
+
+// z = Dinv y (block diagonal)
+template <int DIM, typename T>
+__global__ void k_dinv(Grid g, const T* __restrict__ Dinv, const T* __restrict__ y, T* __restrict__ z) {
+    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.nn) return;
+    T yn[DIM];
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) yn[c] = y[(int64_t)c * g.nn + n];
+#pragma unroll
+    for (int r = 0; r < DIM; ++r) {
+        T v = (T)0;
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) v = fma(Dinv[(int64_t)(r * DIM + c) * g.nn + n], yn[c], v);
+        z[(int64_t)r * g.nn + n] = v;
     }
 }
 
@@ -552,6 +604,10 @@ void build_operator(Context& c, int levels, bool need32) {
     if (levels < 1) levels = 1;
     if (levels > maxlev) levels = maxlev;
     c.nlevels = levels;
+    // captured inner-CG graphs bake in buffer addresses and mesh sizes: drop them on rebuild
+    for (auto& pg : c.pcg_graphs)
+        if (pg.exec) cudaGraphExecDestroy(pg.exec);
+    c.pcg_graphs.clear();
     Level& L0 = c.levels[0];
     L0.mesh = m;
     L0.fixed.ensure((size_t)m.nn * dim);
@@ -597,6 +653,7 @@ void build_operator(Context& c, int levels, bool need32) {
     }
     for (int l = 0; l < levels; ++l) {
         Level& L = c.levels[l];
+        L.lmax = 0.0;
         size_t nv = (size_t)L.mesh.nn * dim;
         L.r64.ensure(nv);
         L.x64.ensure(nv);
@@ -697,7 +754,7 @@ void level_smooth(Context& c, const Level& L, const T* b, T* x, int sweeps, bool
 template <typename T>
 void level_restrict(Context& c, const Level& F, const Level& C, const T* rf, T* rc) {
     Grid gf = grid_of(F.mesh), gc = grid_of(C.mesh);
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_TRANSFER);
     if (gf.dim == 3)
         k_restrict<3, T><<<blocks_for(gc.nn, 256), 256, 0, c.stream>>>(gf, gc, rf, rc, F.fixed.p, C.fixed.p);
     else
@@ -707,7 +764,7 @@ void level_restrict(Context& c, const Level& F, const Level& C, const T* rf, T* 
 template <typename T>
 void level_prolong_add(Context& c, const Level& F, const Level& C, const T* xc, T* xf) {
     Grid gf = grid_of(F.mesh), gc = grid_of(C.mesh);
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_TRANSFER);
     if (gf.dim == 3)
         k_prolong_add<3, T><<<blocks_for(gf.nn, 256), 256, 0, c.stream>>>(gf, gc, xc, xf, F.fixed.p, C.fixed.p);
     else
@@ -716,7 +773,7 @@ void level_prolong_add(Context& c, const Level& F, const Level& C, const T* xc, 
 
 template <typename T>
 void level_coarse_solve(Context& c, const Level& L, const T* b, T* x) {
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_TRANSFER);
     k_gemv<T><<<blocks_for(L.ncoarse * 32, 256), 256, 0, c.stream>>>(L.ncoarse, L.Cinv.p, b, x);
 }
 
@@ -726,6 +783,70 @@ template void level_residual<double>(Context&, const Level&, const double*, cons
 template void level_residual<float>(Context&, const Level&, const float*, const float*, float*);
 template void level_smooth<double>(Context&, const Level&, const double*, double*, int, bool);
 template void level_smooth<float>(Context&, const Level&, const float*, float*, int, bool);
+
+template <typename T>
+static T* tmp_of(Level& L);
+template <>
+double* tmp_of<double>(Level& L) { return L.t64.p; }
+template <>
+float* tmp_of<float>(Level& L) { return L.t32.p; }
+template <typename T>
+static T* dvec_of(Level& L);
+template <>
+double* dvec_of<double>(Level& L) { return L.r64.p; }
+template <>
+float* dvec_of<float>(Level& L) { return L.r32.p; }
+
+// Chebyshev smoothing of `degree` steps on [lmax/10, 1.1 lmax] of D^-1 A (the eigenvalue
+// bounds PETSc's Chebyshev smoother uses by default).  Uses the level's t and r vectors as the
+// alternate iterate and the direction.
+template <typename T>
+void level_cheb(Context& c, Level& L, const T* b, T* x, int degree, bool zero_init) {
+    Grid g = grid_of(L.mesh);
+    int D = g.dim, NB = D == 3 ? 27 : 9;
+    double lmax = 1.1 * L.lmax, lmin = 0.1 * L.lmax;
+    double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+    double sigma = theta / delta, rho = 1.0 / sigma;
+    T* alt = tmp_of<T>(L);
+    T* d = dvec_of<T>(L);
+    note_work(c, UWGPU_KERNEL_SMOOTH, (double)degree * g.nn * (NB * D * D + D * D + 5 * D) * sizeof(T),
+              (double)degree * 2.0 * g.nn * (NB * D * D + D * D));
+    const T* cur = zero_init ? nullptr : x;
+    for (int k = 0; k < degree; ++k) {
+        T* dst = (k % 2 == 0) ? alt : x;
+        double c1 = 0.0, c2;
+        if (k == 0) {
+            c2 = 1.0 / theta;
+        } else {
+            double rho_new = 1.0 / (2.0 * sigma - rho);
+            c1 = rho_new * rho;
+            c2 = 2.0 * rho_new / delta;
+            rho = rho_new;
+        }
+        LaunchScope ls(c, UWGPU_KERNEL_SMOOTH);
+        if (D == 3)
+            k_cheb_step<3, T><<<blocks_for(g.nn, kRowThreads / 3), kRowThreads, 0, c.stream>>>(
+                g, stencil_of<T>(L), dinv_of<T>(L), b, cur, dst, d, (T)c1, (T)c2, k == 0);
+        else
+            k_cheb_step<2, T><<<blocks_for(g.nn, kRowThreads / 2), kRowThreads, 0, c.stream>>>(
+                g, stencil_of<T>(L), dinv_of<T>(L), b, cur, dst, d, (T)c1, (T)c2, k == 0);
+        cur = dst;
+    }
+    if (degree % 2 == 1) UWG_CUDA(cudaMemcpyAsync(x, alt, (size_t)g.nn * D * sizeof(T), cudaMemcpyDeviceToDevice, c.stream));
+    if (degree == 0 && zero_init) UWG_CUDA(cudaMemsetAsync(x, 0, (size_t)g.nn * D * sizeof(T), c.stream));
+}
+
+template <typename T>
+void level_dinv(Context& c, const Level& L, const T* y, T* z) {
+    Grid g = grid_of(L.mesh);
+    LaunchScope ls(c, -1);
+    if (g.dim == 3) k_dinv<3, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, dinv_of<T>(L), y, z);
+    else k_dinv<2, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, dinv_of<T>(L), y, z);
+}
+
+template void level_cheb<double>(Context&, Level&, const double*, double*, int, bool);
+template void level_cheb<float>(Context&, Level&, const float*, float*, int, bool);
+template void level_dinv<double>(Context&, const Level&, const double*, double*);
 template void level_restrict<double>(Context&, const Level&, const Level&, const double*, double*);
 template void level_restrict<float>(Context&, const Level&, const Level&, const float*, float*);
 template void level_prolong_add<double>(Context&, const Level&, const Level&, const double*, double*);
@@ -918,7 +1039,7 @@ static GeoArgs geo_of(Context& c, const MeshDesc& m) {
 void op_G(Context& c, const double* p, double* u) {
     const Level& L = c.levels[0];
     Grid g = grid_of(L.mesh);
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
     if (g.dim == 3)
         k_G<3><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), p, L.fixed.p, u);
     else
@@ -928,7 +1049,7 @@ void op_G(Context& c, const double* p, double* u) {
 void op_GT(Context& c, const double* u, double* p) {
     const Level& L = c.levels[0];
     Grid g = grid_of(L.mesh);
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
     if (g.dim == 3)
         k_GT<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), u, L.fixed.p, p);
     else
@@ -938,7 +1059,7 @@ void op_GT(Context& c, const double* u, double* p) {
 void op_GT_unmasked(Context& c, const double* u, double* p) {
     const Level& L = c.levels[0];
     Grid g = grid_of(L.mesh);
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
     if (g.dim == 3)
         k_GT<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), u, nullptr, p);
     else
@@ -948,7 +1069,7 @@ void op_GT_unmasked(Context& c, const double* u, double* p) {
 void gather_force(Context& c, double* f) {
     const Level& L = c.levels[0];
     Grid g = grid_of(L.mesh);
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
     if (g.dim == 3)
         k_gather_force<3><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, c.fe.p, L.mesh.ne, L.fixed.p, f);
     else
@@ -1217,7 +1338,7 @@ static int gwg_pcg_T(Context& c, const T* W, const T* d, const double* b, T* x, 
     UWG_CUDA(cudaMemsetAsync(scal, 0, 8 * sizeof(double), c.stream));
     unsigned eb = blocks_for(ne, 256), nb = blocks_for(g.nn, 256);
     {
-        LaunchScope ls(c, -1);
+        LaunchScope ls(c, UWGPU_KERNEL_SCHUR_PC);
         k_pcg_init<double, T><<<eb, 256, 0, c.stream>>>(ne, b, d, x, r, z, p, scal);
     }
     double* hs = c.host_scalars;
@@ -1225,36 +1346,45 @@ static int gwg_pcg_T(Context& c, const T* W, const T* d, const double* b, T* x, 
     UWG_CUDA(cudaStreamSynchronize(c.stream));
     double r0 = std::sqrt(hs[4]);
     if (!(r0 > 0.0)) return 0;
-    const int check_every = 8;
+    // Eight iterations (an even number, so the scalar parity repeats) are captured once as a
+    // CUDA graph for this buffer set and replayed; the host tests convergence after each replay.
+    const int block = 8;
+    auto issue = [&](int parity) {
+        if (g.dim == 3) k_pcg_gp<3, T><<<nb, 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
+        else k_pcg_gp<2, T><<<nb, 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
+        if (g.dim == 3) k_pcg_gts<3, T><<<eb, 256, 0, c.stream>>>(g, geo, s, p, q, scal, parity);
+        else k_pcg_gts<2, T><<<eb, 256, 0, c.stream>>>(g, geo, s, p, q, scal, parity);
+        k_pcg_update<T><<<eb, 256, 0, c.stream>>>(ne, p, q, d, x, r, z, scal, parity);
+        k_pcg_dir<T><<<eb, 256, 0, c.stream>>>(ne, z, p, scal, parity);
+    };
+    const void* key[8] = {W, d, x, work, s, scal, (const void*)(intptr_t)ne, (const void*)(intptr_t)sizeof(T)};
+    Context::PcgGraph* pg = nullptr;
+    for (auto& cand : c.pcg_graphs)
+        if (std::equal(std::begin(key), std::end(key), std::begin(cand.key))) pg = &cand;
+    if (!pg) {
+        c.pcg_graphs.emplace_back();
+        pg = &c.pcg_graphs.back();
+        std::copy(std::begin(key), std::end(key), std::begin(pg->key));
+        cudaGraph_t graph;
+        UWG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < block; ++k) issue(k & 1);
+        UWG_CUDA(cudaStreamEndCapture(c.stream, &graph));
+        UWG_CUDA(cudaGraphInstantiate(&pg->exec, graph, 0));
+        UWG_CUDA(cudaGraphDestroy(graph));
+    }
     int it = 0;
     while (it < maxit) {
-        int parity = it & 1;
         {
-            LaunchScope ls(c, -1);
-            if (g.dim == 3) k_pcg_gp<3, T><<<nb, 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
-            else k_pcg_gp<2, T><<<nb, 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
+            LaunchScope ls(c, UWGPU_KERNEL_SCHUR_PC);
+            UWG_CUDA(cudaGraphLaunch(pg->exec, c.stream));
         }
-        {
-            LaunchScope ls(c, -1);
-            if (g.dim == 3) k_pcg_gts<3, T><<<eb, 256, 0, c.stream>>>(g, geo, s, p, q, scal, parity);
-            else k_pcg_gts<2, T><<<eb, 256, 0, c.stream>>>(g, geo, s, p, q, scal, parity);
-        }
-        {
-            LaunchScope ls(c, -1);
-            k_pcg_update<T><<<eb, 256, 0, c.stream>>>(ne, p, q, d, x, r, z, scal, parity);
-        }
-        {
-            LaunchScope ls(c, -1);
-            k_pcg_dir<T><<<eb, 256, 0, c.stream>>>(ne, z, p, scal, parity);
-        }
-        it++;
-        if (it % check_every == 0 || it == maxit) {
-            UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-            UWG_CUDA(cudaStreamSynchronize(c.stream));
-            double rn = std::sqrt(hs[3]);
-            if (!std::isfinite(rn)) throw Error(UWGPU_ERR_NAN, "NaN in the BFBt inner solve");
-            if (rn <= rtol * r0) break;
-        }
+        c.launches += 4 * block - 1;
+        it += block;
+        UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        double rn = std::sqrt(hs[3]);
+        if (!std::isfinite(rn)) throw Error(UWGPU_ERR_NAN, "NaN in the BFBt inner solve");
+        if (rn <= rtol * r0) break;
     }
     check_launch("gwg_pcg");
     return it;
@@ -1275,7 +1405,7 @@ void op_wg32(Context& c, const float* p, const float* W, float* s) {
     const Level& L = c.levels[0];
     Grid g = grid_of(L.mesh);
     GeoT<float> geo = geo_T<float>(c, L.mesh);
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_SCHUR_PC);
     if (g.dim == 3) k_pcg_gp<3, float><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
     else k_pcg_gp<2, float><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
 }
@@ -1284,18 +1414,18 @@ void op_gt32(Context& c, const float* s, float* q) {
     const Level& L = c.levels[0];
     Grid g = grid_of(L.mesh);
     GeoT<float> geo = geo_T<float>(c, L.mesh);
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_SCHUR_PC);
     if (g.dim == 3) k_pcg_gts<3, float><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo, s, nullptr, q, nullptr, 0);
     else k_pcg_gts<2, float><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo, s, nullptr, q, nullptr, 0);
 }
 
 void to_float(Context& c, const double* a, float* b, int64_t n) {
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_SCHUR_PC);
     k_convert<double, float><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, a, b);
 }
 
 void to_double(Context& c, const float* a, double* b, int64_t n) {
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_SCHUR_PC);
     k_convert<float, double><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, a, b);
 }
 

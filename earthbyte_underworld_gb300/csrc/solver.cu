@@ -25,6 +25,8 @@ template <typename T> void level_smooth(Context&, const Level&, const T*, T*, in
 template <typename T> void level_restrict(Context&, const Level&, const Level&, const T*, T*);
 template <typename T> void level_prolong_add(Context&, const Level&, const Level&, const T*, T*);
 template <typename T> void level_coarse_solve(Context&, const Level&, const T*, T*);
+template <typename T> void level_cheb(Context&, Level&, const T*, T*, int, bool);
+template <typename T> void level_dinv(Context&, const Level&, const T*, T*);
 void op_G(Context& c, const double* p, double* u);
 void op_GT(Context& c, const double* u, double* p);
 void op_GT_unmasked(Context& c, const double* u, double* p);
@@ -172,6 +174,12 @@ __global__ void k_combine(int64_t n, const T* __restrict__ Z, int64_t ldz, int m
     x[i] = (X)acc;
 }
 
+// deterministic oscillatory start vector for the power iteration (hash of the index)
+__global__ void k_pattern(int64_t n, double* __restrict__ x) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = (double)(((uint64_t)i * 2654435761ull >> 7) & 1023ull) / 1023.0 - 0.5;
+}
+
 __global__ void k_remove_mean(int64_t n, const double* __restrict__ sum, double* __restrict__ x) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) x[i] -= sum[0] / (double)n;
@@ -191,14 +199,14 @@ struct Reducer {
     template <typename T>
     void multidot(int64_t n, const T* V, int64_t ldv, int m, const T* w, double* host) {
         {
-            LaunchScope ls(c, -1);
+            LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
             if (m <= 1)
                 k_multidot<T, 1><<<kRedBlocks, kRedThreads, 0, c.stream>>>(n, V, ldv, m, w, partial.p);
             else
                 k_multidot<T, 8><<<kRedBlocks, kRedThreads, 0, c.stream>>>(n, V, ldv, m, w, partial.p);
         }
         {
-            LaunchScope ls(c, -1);
+            LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
             k_reduce_partials<<<m, 256, 0, c.stream>>>(m, kRedBlocks, partial.p, out.p);
         }
         if (host) {
@@ -222,12 +230,12 @@ struct Reducer {
 
 template <typename T>
 static void axpy(Context& c, int64_t n, double a, const T* x, T* y) {
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
     k_axpy<T><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, (T)a, x, y);
 }
 template <typename T>
 static void scale(Context& c, int64_t n, double a, const T* x, T* y) {
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
     k_scale<T><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, (T)a, x, y);
 }
 template <typename T>
@@ -240,7 +248,7 @@ static void copy(Context& c, int64_t n, const T* x, T* y) {
 }
 template <typename S, typename D>
 static void cast(Context& c, int64_t n, const S* a, D* b) {
-    LaunchScope ls(c, -1);
+    LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
     k_cast<S, D><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, a, b);
 }
 
@@ -292,7 +300,7 @@ struct Fgmres {
             if (!first) {
                 A(x, w.p);
                 {
-                    LaunchScope ls(c, -1);
+                    LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
                     k_sub_from<T><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, b, w.p);
                 }
                 copy<T>(c, n, w.p, V.p);
@@ -319,7 +327,7 @@ struct Fgmres {
                     red.multidot<T>(n, V.p, n, k + 1, w.p, hcol.data() + 0);
                     UWG_CUDA(cudaMemcpyAsync(dvec.p, hcol.data(), (k + 1) * sizeof(double), cudaMemcpyHostToDevice, c.stream));
                     {
-                        LaunchScope ls(c, -1);
+                        LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
                         k_multi_axpy<T><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, V.p, n, k + 1, dvec.p, w.p, -1.0);
                     }
                     for (int j = 0; j <= k; ++j) {
@@ -370,7 +378,7 @@ struct Fgmres {
             }
             UWG_CUDA(cudaMemcpyAsync(dvec.p, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, c.stream));
             {
-                LaunchScope ls(c, -1);
+                LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
                 k_combine<T, T><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, Z.p, n, k, dvec.p, x);
             }
             beta = std::fabs(g[k]);
@@ -415,16 +423,47 @@ struct Bsscr {
     T* lvl_r(Level& L);
 
     template <typename T>
+    void smooth(Level& L, const T* b, T* x, int sweeps, bool zero_init) {
+        if (o.smoother == UWGPU_SMOOTHER_CHEBYSHEV)
+            level_cheb<T>(c, L, b, x, sweeps, zero_init);
+        else
+            level_smooth<T>(c, L, b, x, sweeps, zero_init);
+    }
+
+    // largest eigenvalue of Dinv A per smoothed level by power iteration (Chebyshev bounds)
+    void estimate_lmax() {
+        for (int l = 0; l < (nlev > 1 ? nlev - 1 : 1); ++l) {
+            Level& L = c.levels[l];
+            if (L.lmax > 0.0) continue;
+            int64_t n = L.mesh.nn * dim;
+            {
+                LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
+                k_pattern<<<blocks_for(n, 256), 256, 0, c.stream>>>(n, L.x64.p);
+            }
+            double nx = red.norm<double>(n, L.x64.p), lam = 1.0;
+            scale<double>(c, n, 1.0 / nx, L.x64.p, L.x64.p);
+            for (int it = 0; it < 15; ++it) {
+                level_apply<double>(c, L, L.x64.p, L.t64.p);
+                level_dinv<double>(c, L, L.t64.p, L.b64.p);
+                lam = red.norm<double>(n, L.b64.p);
+                if (!(lam > 0.0) || !std::isfinite(lam)) { lam = 1.0; break; }
+                scale<double>(c, n, 1.0 / lam, L.b64.p, L.x64.p);
+            }
+            L.lmax = lam;
+        }
+    }
+
+    template <typename T>
     void vcycle(int l, const T* b, T* x) {
         Level& L = c.levels[l];
         if (l == nlev - 1) {
             if (nlev > 1)
                 level_coarse_solve<T>(c, L, b, x);
             else
-                level_smooth<T>(c, L, b, x, o.smooth_down + o.smooth_up, true);
+                smooth<T>(L, b, x, o.smooth_down + o.smooth_up, true);
             return;
         }
-        level_smooth<T>(c, L, b, x, o.smooth_down, true);
+        smooth<T>(L, b, x, o.smooth_down, true);
         T* r = lvl_r<T>(L);
         level_residual<T>(c, L, x, b, r);
         Level& C = c.levels[l + 1];
@@ -433,7 +472,7 @@ struct Bsscr {
         level_restrict<T>(c, L, C, r, bc);
         vcycle<T>(l + 1, bc, xc);
         level_prolong_add<T>(c, L, C, xc, x);
-        level_smooth<T>(c, L, b, x, o.smooth_up, false);
+        smooth<T>(L, b, x, o.smooth_up, false);
     }
 
     // ---- velocity (A11) solve: x = K^{-1} b to relative tolerance rtol ----
@@ -476,7 +515,7 @@ struct Bsscr {
                 its += k;
                 if (nn) { nan = true; break; }
                 {
-                    LaunchScope ls(c, -1);
+                    LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
                     k_cast_add<float, double><<<blocks_for(nv, 256), 256, 0, c.stream>>>(nv, d32.p, x);
                 }
                 level_residual<double>(c, L0, x, b, ref_r.p);
@@ -498,7 +537,7 @@ struct Bsscr {
     }
 
     void pmul(int64_t n, const double* a, const double* b, double* y) {
-        LaunchScope ls(c, -1);
+        LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
         k_pointwise_mul<<<blocks_for(n, 256), 256, 0, c.stream>>>(n, a, b, y);
     }
 
@@ -529,7 +568,7 @@ struct Bsscr {
         op_wg32(c, bt32.p, bw32.p, bs32.p);
         level_apply<float>(c, c.levels[0], bs32.p, bX32.p);
         {
-            LaunchScope ls(c, -1);
+            LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
             k_pointwise_mul32<<<blocks_for(nv, 256), 256, 0, c.stream>>>(nv, bX32.p, bw32.p, bX32.p);
         }
         op_gt32(c, bX32.p, bt2_32.p);
@@ -562,7 +601,7 @@ struct Bsscr {
         } else if (o.schur_pc == UWGPU_SCHUR_PC_SCALED_BFBT) {
             bfbt_apply(v, z);
         } else {
-            LaunchScope ls(c, -1);
+            LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
             k_pointwise_div<<<blocks_for(npres, 256), 256, 0, c.stream>>>(npres, v, Sd.p, z);
         }
     }
@@ -612,12 +651,12 @@ struct Bsscr {
         op_G(c, p, tu.p);
         axpy<double>(c, nv, 1.0, tu.p, t2.p);
         {
-            LaunchScope ls(c, -1);
+            LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
             k_sub_from<double><<<blocks_for(nv, 256), 256, 0, c.stream>>>(nv, f.p, t2.p);
         }
         op_GT(c, u, rhs_p.p);
         {
-            LaunchScope ls(c, -1);
+            LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
             k_sub_from<double><<<blocks_for(npres, 256), 256, 0, c.stream>>>(npres, h.p, rhs_p.p);
         }
         double r2 = red.dot<double>(nv, t2.p, t2.p) + red.dot<double>(npres, rhs_p.p, rhs_p.p);
@@ -653,11 +692,11 @@ static void remove_constant(Context& c, int64_t n, double* x, DArray<double>& tm
     tmp.ensure(1);
     UWG_CUDA(cudaMemsetAsync(tmp.p, 0, sizeof(double), c.stream));
     {
-        LaunchScope ls(c, -1);
+        LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
         k_sum_partial<<<kRedBlocks, kRedThreads, 0, c.stream>>>(n, x, tmp.p);
     }
     {
-        LaunchScope ls(c, -1);
+        LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
         k_remove_mean<<<blocks_for(n, 256), 256, 0, c.stream>>>(n, tmp.p, x);
     }
 }
@@ -724,6 +763,7 @@ void Bsscr::run() {
         build_operator(c, levels, mixed);
     nlev = c.nlevels;
     nv = c.mesh.nn * dim;
+    if (o.smoother == UWGPU_SMOOTHER_CHEBYSHEV) estimate_lmax();
     npres = c.mesh.ne;
     int restart = o.restart > 0 ? o.restart : 30;
     gm64.setup(nv, restart);
@@ -754,7 +794,7 @@ void Bsscr::run() {
         // and for the transposed gradient block h -= G^T u_b
         const MeshDesc& m = c.mesh;
         {
-            LaunchScope ls(c, -1);
+            LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
             if (dim == 3)
                 k_bc_lift<3><<<blocks_for(m.nn, 128), 128, 0, c.stream>>>(m.nnx, m.nny, m.nnz, m.nn, m.nel[0], m.nel[1],
                                                                           m.nel[2], m.ne, c.levels[0].Ke.p, c.fixed.p,
@@ -766,7 +806,7 @@ void Bsscr::run() {
         check_launch("k_bc_lift");
         ub.ensure(nv);
         {
-            LaunchScope ls(c, -1);
+            LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
             if (dim == 3)
                 k_bc_vector<3><<<blocks_for(m.nn, 256), 256, 0, c.stream>>>(m.nn, c.fixed.p, c.bcval.p, ub.p);
             else
@@ -849,6 +889,7 @@ void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
     UWG_REQUIRE(o.precision == UWGPU_PREC_FP64 || o.precision == UWGPU_PREC_MIXED, UWGPU_ERR_ARGUMENT, "bad precision");
     UWG_REQUIRE(o.schur_type == UWGPU_SCHUR_CG || o.schur_type == UWGPU_SCHUR_FGMRES, UWGPU_ERR_ARGUMENT, "bad Schur type");
     UWG_REQUIRE(o.schur_pc >= 0 && o.schur_pc <= 3, UWGPU_ERR_ARGUMENT, "bad Schur preconditioner");
+    UWG_REQUIRE(o.smoother == UWGPU_SMOOTHER_COLOUR_GS || o.smoother == UWGPU_SMOOTHER_CHEBYSHEV, UWGPU_ERR_ARGUMENT, "bad smoother");
     Bsscr s(c, o, rep);
     s.run();
 }

@@ -34,8 +34,10 @@ SCHUR_PC_UW = 0
 SCHUR_PC_GKGDIAG = 1
 SCHUR_PC_NONE = 2
 SCHUR_PC_SCALED_BFBT = 3
+SMOOTHER_COLOUR_GS = 0
+SMOOTHER_CHEBYSHEV = 1
 
-KERNEL_ASSEMBLY, KERNEL_APPLY, KERNEL_SMOOTH, KERNEL_BINNING = range(4)
+KERNEL_ASSEMBLY, KERNEL_APPLY, KERNEL_SMOOTH, KERNEL_BINNING, KERNEL_SCHUR_PC, KERNEL_VECTOR, KERNEL_TRANSFER = range(7)
 
 
 class UwgpuError(RuntimeError):
@@ -59,7 +61,7 @@ class SolveOpts(C.Structure):
                 ("max_outer", C.c_int32), ("max_inner", C.c_int32), ("scr_rtol", C.c_double),
                 ("a11_rtol", C.c_double), ("back_rtol", C.c_double), ("remove_const_p", C.c_int32),
                 ("precision", C.c_int32), ("target_rel_residual", C.c_double), ("bfbt_rtol", C.c_double),
-                ("bfbt_max_it", C.c_int32), ("pad0", C.c_int32)]
+                ("bfbt_max_it", C.c_int32), ("smoother", C.c_int32)]
 
 
 class Report(C.Structure):

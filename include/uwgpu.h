@@ -79,6 +79,12 @@ enum { UWGPU_SCHUR_CG = 0, UWGPU_SCHUR_FGMRES = 1 };
  * W = 1/rowmax(K), whose inner G^T W G solves are Jacobi-preconditioned CG. */
 enum { UWGPU_SCHUR_PC_UW = 0, UWGPU_SCHUR_PC_GKGDIAG = 1, UWGPU_SCHUR_PC_NONE = 2, UWGPU_SCHUR_PC_SCALED_BFBT = 3 };
 
+/* Multigrid smoothers: symmetric multicolour block Gauss-Seidel (the colour-scheduled form of
+ * the reference's Richardson/SOR level smoother, PETScMGSolver.c:674-709), or Chebyshev
+ * iteration on the block-Jacobi preconditioned operator (PETSc KSPCHEBYSHEV, eigenvalue bounds
+ * [0.1, 1.1] x the power-iteration estimate). */
+enum { UWGPU_SMOOTHER_COLOUR_GS = 0, UWGPU_SMOOTHER_CHEBYSHEV = 1 };
+
 typedef struct {
     int32_t mg_levels;        /* mgLevels: levels including the fine one (>= 2)          */
     int32_t smooth_down;      /* downIterations: symmetric colour sweeps before restrict  */
@@ -97,7 +103,8 @@ typedef struct {
                                    ||[f-Ku-Gp; h-G^T u]|| / ||[f;h]|| is below this value */
     double bfbt_rtol;         /* inner G^T W G solve tolerance of the scaled BFBt preconditioner */
     int32_t bfbt_max_it;      /* inner iteration limit of those solves                   */
-    int32_t pad0;
+    int32_t smoother;         /* UWGPU_SMOOTHER_COLOUR_GS (default) or UWGPU_SMOOTHER_CHEBYSHEV:
+                                 smooth_down/up are then polynomial degrees              */
 } uwgpu_solve_opts;
 
 typedef struct {
@@ -204,7 +211,9 @@ void uwgpu_solve_opts_default(uwgpu_solve_opts* opts);
 /* Kernel timing: when enabled, launches of the kernel family `which` are bracketed by CUDA
  * events on the context stream and summed (count, milliseconds). */
 enum { UWGPU_KERNEL_ASSEMBLY = 0, UWGPU_KERNEL_APPLY = 1, UWGPU_KERNEL_SMOOTH = 2,
-       UWGPU_KERNEL_BINNING = 3, UWGPU_KERNEL_COUNT = 4 };
+       UWGPU_KERNEL_BINNING = 3, UWGPU_KERNEL_SCHUR_PC = 4 /* scaled-BFBt inner solves */,
+       UWGPU_KERNEL_VECTOR = 5 /* Krylov vector work, reductions, G and G^T */,
+       UWGPU_KERNEL_TRANSFER = 6 /* restriction, prolongation, coarsest solve */, UWGPU_KERNEL_COUNT = 7 };
 int uwgpu_profile_enable(uwgpu_ctx* ctx, int32_t on);
 int uwgpu_profile_read(uwgpu_ctx* ctx, int32_t which, int64_t* launches, double* ms);
 /* Algorithmic work of the profiled launches of family `which`: bytes the kernels must move

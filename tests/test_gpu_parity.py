@@ -122,15 +122,17 @@ def test_operator_apply_matches_csr(oracle, uw, dim):
     ctx.close()
 
 
-@pytest.mark.parametrize("case,schur,pc", [("rt2d", 1, 0), ("spheres", 1, 0), ("spheres", 0, 0), ("spheres", 1, 1),
-                                           ("spheres", 1, 3), ("rt2d", 1, 3)])
-def test_bsscr_solution_parity(oracle, uw, case, schur, pc):
+@pytest.mark.parametrize("case,schur,pc,smoother", [("rt2d", 1, 0, 0), ("spheres", 1, 0, 0), ("spheres", 0, 0, 0),
+                                                    ("spheres", 1, 1, 0), ("spheres", 1, 3, 0), ("rt2d", 1, 3, 0),
+                                                    ("spheres", 1, 3, 1), ("rt2d", 1, 3, 1)])
+def test_bsscr_solution_parity(oracle, uw, case, schur, pc, smoother):
     from earthbyte_underworld_gb300 import workloads as W
     O, U = oracle, uw
     w = W.rt2d(nel=(32, 32), ppc=20) if case == "rt2d" else W.spheres(nel=(8, 8, 8), nspheres=10, seed=9)
     ctx, perm, offsets, xi, Ke, fe, Ge, Se, eta = _run_gpu(U, W, w)
     opts = U.default_opts(mg_levels=3, schur_type=schur, schur_pc=pc, scr_rtol=1e-11, a11_rtol=1e-13,
-                          back_rtol=1e-13, max_outer=400, max_inner=2000, bfbt_rtol=1e-8, bfbt_max_it=5000)
+                          back_rtol=1e-13, max_outer=400, max_inner=2000, bfbt_rtol=1e-8, bfbt_max_it=5000,
+                          smoother=smoother, smooth_down=2 if smoother else 2, smooth_up=2)
     u, p, rep = ctx.solve_bsscr(opts)
     m = O.make_mesh(w["dim"], w["nel"])
     ou, op, orep = O.solve_bsscr(m, w["fixed"], Ke, Ge, fe, Se, mg_levels=3, scr_rtol=1e-11,
