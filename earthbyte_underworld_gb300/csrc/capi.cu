@@ -358,6 +358,35 @@ int uwgpu_solve_bsscr(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, double* u, d
     });
 }
 
+int uwgpu_solve_picard(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, double tolerance, int32_t max_iterations,
+                       int32_t min_iterations, double* u, double* p, uwgpu_report* report, int32_t* iterations,
+                       double* residual) {
+    return guarded(ctx, [&](Context& c) {
+        uwgpu_solve_opts o;
+        if (opts) o = *opts; else uwgpu_solve_opts_default(&o);
+        uwgpu_report rep;
+        std::memset(&rep, 0, sizeof(rep));
+        int its = 0;
+        double res = 0.0;
+        uwg::solve_picard(c, o, tolerance, max_iterations, min_iterations, rep, its, res);
+        int dim = c.mesh.dim;
+        int64_t nn = c.mesh.nn;
+        if (u) {
+            std::vector<double> soa((size_t)nn * dim);
+            UWG_CUDA(cudaMemcpyAsync(soa.data(), c.u_sol.p, soa.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            UWG_CUDA(cudaStreamSynchronize(c.stream));
+            for (int64_t n = 0; n < nn; ++n)
+                for (int d = 0; d < dim; ++d) u[n * dim + d] = soa[(size_t)d * nn + n];
+        }
+        if (p) UWG_CUDA(cudaMemcpyAsync(p, c.p_sol.p, c.mesh.ne * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        if (report) *report = rep;
+        if (iterations) *iterations = its;
+        if (residual) *residual = res;
+        if (rep.status != UWGPU_OK) throw Error(rep.status, "Picard iteration: a Stokes solve did not converge");
+    });
+}
+
 int uwgpu_profile_enable(uwgpu_ctx* ctx, int32_t on) {
     return guarded(ctx, [&](Context& c) {
         UWG_CUDA(cudaStreamSynchronize(c.stream));

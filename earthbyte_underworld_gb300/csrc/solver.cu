@@ -895,3 +895,53 @@ void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
 }
 
 }  // namespace uwg
+
+namespace uwg {
+
+// SystemLinearEquations_NonLinearExecute (SystemLinearEquations.c:750-935): the residual is the
+// relative change of the velocity solution vector between successive solves.
+void solve_picard(Context& c, const uwgpu_solve_opts& o, double tol, int maxit, int minit, uwgpu_report& rep,
+                  int& iterations, double& residual) {
+    UWG_REQUIRE(c.mapped, UWGPU_ERR_STATE, "Picard iteration requested before bin_and_map");
+    UWG_REQUIRE(maxit >= 1, UWGPU_ERR_ARGUMENT, "max_iterations must be positive");
+    Reducer red(c);
+    int64_t nv = c.mesh.nn * c.mesh.dim;
+    DArray<double> prev;
+    prev.ensure((size_t)nv);
+    residual = 0.0;
+    iterations = 0;
+    uwgpu_report r;
+    for (int it = 0; it < maxit; ++it) {
+        bool have_prev = c.has_solution;
+        if (have_prev) UWG_CUDA(cudaMemcpyAsync(prev.p, c.u_sol.p, nv * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+        assemble(c);
+        std::memset(&r, 0, sizeof(r));
+        solve_bsscr(c, o, r);
+        iterations = it + 1;
+        rep.outer_its += r.outer_its;
+        rep.inner_its_total += r.inner_its_total;
+        rep.backsolve_its += r.backsolve_its;
+        rep.vcycles += r.vcycles;
+        rep.pc_inner_its += r.pc_inner_its;
+        rep.t_setup_ms += r.t_setup_ms;
+        rep.t_solve_ms += r.t_solve_ms;
+        rep.rel_residual = r.rel_residual;
+        rep.status = r.status;
+        rep.converged = r.converged;
+        if (r.status != UWGPU_OK) return;
+        if (!have_prev) continue;
+        {
+            LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
+            k_axpy<double><<<blocks_for(nv, 256), 256, 0, c.stream>>>(nv, -1.0, c.u_sol.p, prev.p);
+        }
+        double dn = red.norm<double>(nv, prev.p), un = red.norm<double>(nv, c.u_sol.p);
+        residual = un > 0.0 ? dn / un : 0.0;
+        if (!std::isfinite(residual)) {
+            rep.status = UWGPU_ERR_NAN;
+            return;
+        }
+        if (residual < tol && iterations >= minit) break;
+    }
+}
+
+}  // namespace uwg

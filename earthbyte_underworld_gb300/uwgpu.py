@@ -110,6 +110,7 @@ def load(build_if_missing: bool = True):
         L.uwgpu_get_point_viscosity.argtypes = [P, P]
         L.uwgpu_operator_apply.argtypes = [P, C.c_int32, P, P]
         L.uwgpu_solve_bsscr.argtypes = [P, P, P, P, P]
+        L.uwgpu_solve_picard.argtypes = [P, P, C.c_double, C.c_int32, C.c_int32, P, P, P, P, P]
         L.uwgpu_solve_opts_default.argtypes = [P]
         L.uwgpu_solve_opts_default.restype = None
         L.uwgpu_profile_enable.argtypes = [P, C.c_int32]
@@ -275,6 +276,20 @@ class Context:
         if check:
             self._check(rc)
         return u, p, rep
+
+    def solve_picard(self, opts: SolveOpts | None = None, tolerance=1e-4, max_iterations=20, min_iterations=1):
+        """Picard iteration (re-assemble with the current solution, re-solve) until the relative
+        velocity change is below `tolerance`.  Returns u, p, report, iterations, residual."""
+        opts = opts or default_opts()
+        rep = Report()
+        u = np.zeros((self.nnodes, self.dim))
+        p = np.zeros(self.nelements)
+        its = C.c_int32()
+        res = C.c_double()
+        self._check(self._L.uwgpu_solve_picard(self._h, C.byref(opts), float(tolerance), int(max_iterations),
+                                               int(min_iterations), _ptr(u), _ptr(p), C.byref(rep), C.byref(its),
+                                               C.byref(res)))
+        return u, p, rep, its.value, res.value
 
     def synchronize(self):
         self._check(self._L.uwgpu_synchronize(self._h))

@@ -127,7 +127,7 @@ def gaussian_random_field(n=256, corr=0.1, seed=7):
     k2 = kx ** 2 + ky ** 2 + kz ** 2
     spec = np.exp(-0.25 * k2 * corr * corr)  # sqrt of the SE power spectrum (up to a constant)
     noise = rng.standard_normal((n, n, n))
-    f = np.fft.irfftn(np.fft.rfftn(noise) * spec, s=(n, n, n))
+    f = np.fft.irfftn(np.fft.rfftn(noise) * spec, s=(n, n, n), axes=(0, 1, 2))
     f -= f.mean()
     f /= np.abs(f).max()
     return f
@@ -179,7 +179,7 @@ def grf(nel=(128, 128, 128), ppc=30, seed=11, grid=256, corr=0.1, shuffle=True):
                 mg_levels=5)
 
 
-def layers(nel=(96, 96, 96), ppc=40, seed=5, nbumps=20):
+def layers(nel=(96, 96, 96), ppc=40, seed=5, nbumps=20, cohesion_scale=1.0):
     """3D nonlinear: 5 horizontal layers (seeded thicknesses), T = 1 - z + sum of 20 Gaussian
     bumps (amplitude 0.1, width 0.05); per layer Arrhenius eta = exp(E/(T+0.1) - E/1.1) with
     E ~ U(5, 15), Drucker-Prager with C ~ U(0.1, 1), mu = 0.6, then a [1e-3, 1e3] limiter."""
@@ -199,10 +199,11 @@ def layers(nel=(96, 96, 96), ppc=40, seed=5, nbumps=20):
     mats = []
     for _ in range(5):
         Ea = rng.uniform(5.0, 15.0)
-        coh = rng.uniform(0.1, 1.0)
+        coh = rng.uniform(0.1, 1.0) * cohesion_scale
+        rho = rng.uniform(0.0, 1.0)   # layer density (seeded; drives the flow)
         mats.append(U.make_material([(U.LAW_ARRHENIUS, [np.exp(-Ea / 1.1), Ea, 0.0, 0.1]),
                                      (U.LAW_DRUCKER_PRAGER, [coh, 0.6, 0.0, 1e-3]),
-                                     (U.LAW_VISCOSITY_LIMITER, [1e3, 1e-3])], density=1.0))
+                                     (U.LAW_VISCOSITY_LIMITER, [1e3, 1e-3])], density=rho))
     centres = rng.uniform(0.0, 1.0, size=(nbumps, 3))
     nn = (nx + 1) * (ny + 1) * (nz + 1)
     idx = np.arange(nn)

@@ -203,6 +203,17 @@ int uwgpu_operator_apply(uwgpu_ctx* ctx, int32_t precision, const double* x, dou
 int uwgpu_solve_bsscr(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, double* u, double* p,
                       uwgpu_report* report);
 
+/* Picard iteration of a nonlinear Stokes system: SystemLinearEquations_NonLinearExecute
+ * (StgFEM/SLE/SystemSetup/src/SystemLinearEquations.c:750-935).  Each iteration re-runs the
+ * rheology and assembly with the current velocity and pressure (strain-rate and pressure
+ * dependent laws; yielding starts after the first solve, YieldRheology.c:210-212) and solves again,
+ * until ||u_k - u_(k-1)|| / ||u_k|| < tolerance (after at least min_iterations) or max_iterations
+ * solves.  Requires uwgpu_bin_and_map first.  *iterations and *residual (optional) report the
+ * solves done and the last relative change; u, p as in uwgpu_solve_bsscr. */
+int uwgpu_solve_picard(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, double tolerance, int32_t max_iterations,
+                       int32_t min_iterations, double* u, double* p, uwgpu_report* report, int32_t* iterations,
+                       double* residual);
+
 /* Default options: the BSSCR driver's defaults (CG Schur iteration, KSPSetType "cg" in
  * auglag-driver-DGTGD.c:266, with the uw approxS preconditioner, preconditioner.c:137), 4 levels,
  * 2+2 smoothing sweeps. */

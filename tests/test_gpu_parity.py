@@ -176,3 +176,36 @@ def test_c_host_program_solves():
     assert rep["points"] == 32 * 32 * 20
     assert rep["rel_residual"] < 1e-6
     assert rep["vmax"] > 0.0
+
+
+def test_picard_nonlinear_parity(oracle, uw):
+    """Picard iteration with Arrhenius + Drucker-Prager + limiter (yielding from the second
+    assembly on, YieldRheology.c:210-212): three solves on the GPU against the same three solves
+    of the oracle (rheology re-evaluated with the previous velocity and pressure)."""
+    from earthbyte_underworld_gb300 import workloads as W
+    O, U = oracle, uw
+    w = W.layers(nel=(6, 6, 8), ppc=20, cohesion_scale=1e-3)
+    opts = U.default_opts(mg_levels=2, schur_type=1, schur_pc=3, scr_rtol=1e-11, a11_rtol=1e-13, back_rtol=1e-13,
+                          max_outer=400, max_inner=2000, bfbt_rtol=1e-8, bfbt_max_it=5000)
+    with U.Context(0) as ctx:
+        W.setup_context(ctx, w)
+        ctx.bin_and_map(want=False)
+        u, p, rep, its, res = ctx.solve_picard(opts, tolerance=0.0, max_iterations=3)
+        eta = ctx.point_viscosity()
+    assert its == 3 and res > 0.0
+    m = O.make_mesh(3, w["nel"])
+    xyz = np.stack([w["x"], w["y"], w["z"]], axis=1)
+    _, off, perm, xi, _ = O.map_points(m, xyz)
+    mats = _mats_oracle(O, w["materials"])
+    ou = op = None
+    for it in range(3):
+        f = O.make_fields(temperature=w["temperature"], velocity=None if ou is None else ou, pressure=op,
+                          previous_solution=ou is not None, gravity=w["gravity"], vert_axis=w["vert_axis"])
+        Ke, fe, Ge, Se, oeta = O.assemble(m, off, perm, xi, w["material"], mats, f, want_eta=True)
+        ou, op, orep = O.solve_bsscr(m, w["fixed"], Ke, Ge, fe, Se, mg_levels=2, schur_type=1, schur_pc=3,
+                                     scr_rtol=1e-11, a11_rtol=1e-13, back_rtol=1e-13, bfbt_rtol=1e-8,
+                                     bfbt_max_it=5000)
+    # yielding happened: some points sit below their Arrhenius/limiter viscosity
+    assert _rel(eta, oeta) < 1e-7
+    assert _rel(u, ou) < 1e-7
+    assert _rel(p, op) < 1e-7
