@@ -197,6 +197,18 @@ def cpu_step(O, w, nthreads):
     return t2 - t0, t1 - t0, rep
 
 
+# what one profiled launch of each kernel family is, and what its algorithmic bytes count
+FAMILY_NOTES = {
+    "smooth": "one Chebyshev step (k_cheb_step): 27 stencil blocks of 3x3, the diagonal-block inverse, rhs "
+              "and the iterate moved once per node; FP64 kernels on this part are also limited by its "
+              "1.2 TFLOP/s FP64 rate (fp_tflops)",
+    "apply": "one operator apply (k_apply): 27 stencil blocks of 3x3 per node, x read and y written once",
+    "schur_pc": "one replay of the BFBt inner-CG graph = 8 iterations of k_gwg_spmv + k_gwg_update + k_gwg_dir: "
+                "the 27-point G^T W G stencil, p and q once per element per iteration, plus the 11 vector "
+                "streams of the update and direction kernels; FP64 rate applies too (fp_tflops)",
+}
+
+
 def cpu_baseline(nel, nthreads):
     from oracle import oracle as O
     O.lib()
@@ -338,9 +350,7 @@ def run_ours(args):
                 "avg_launch_us": 1e3 * d["ms"] / max(d["launches"], 1),
                 "algorithmic_bytes_per_launch": d["bytes"] / max(d["launches"], 1),
                 "fp_tflops": fp64_tflops,
-                "note": "algorithmic bytes: stencil blocks, diagonal inverse, rhs and the relaxed rows "
-                        "moved once per launch; FP64 kernels on this part are also limited by its "
-                        "1.2 TFLOP/s FP64 rate (fp_tflops)"}
+                "note": FAMILY_NOTES.get(dom, "")}
     kernels = {k: {"launches": v["launches"], "ms": v["ms"],
                    "GB_per_s": v["bytes"] / (v["ms"] / 1e3) / 1e9 if v["ms"] > 0 else None,
                    "TFLOP_per_s": v["flops"] / (v["ms"] / 1e3) / 1e12 if v["ms"] > 0 else None}
@@ -351,11 +361,14 @@ def run_ours(args):
     if not args.no_mixed and prec == "fp64":
         # the FP64 leg has warmed every kernel; one extra untimed mixed step suffices
         ms2, wall2, l2, reps2, clk2, _ = timed(opts_for("mixed"), profile=False, warmup=1)
+        _, _, _, _, _, prof2 = timed(opts_for("mixed"), profile=True, warmup=0, steps=1)
         ms2 = dist.max(ms2)
         mixed = {"value": dist.sum(npts) / (ms2 / 1e3 / args.steps), "ms_per_step": ms2 / args.steps,
                  "stokes_solve_s": reps2[-1].t_solve_ms / 1e3, "rel_residual": reps2[-1].rel_residual,
                  "outer_its": reps2[-1].outer_its, "inner_its": reps2[-1].inner_its_total,
-                 "speedup_vs_fp64": (ms_max / args.steps) / (ms2 / args.steps)}
+                 "pc_inner_its": reps2[-1].pc_inner_its,
+                 "speedup_vs_fp64": (ms_max / args.steps) / (ms2 / args.steps),
+                 "kernels": {k: {"launches": v["launches"], "ms": v["ms"]} for k, v in prof2.items()}}
 
     # end to end through the public API with host buffers (pinned)
     xs = torch.from_numpy(w["x"]).pin_memory().numpy()
@@ -399,6 +412,7 @@ def run_ours(args):
                           "solver": "BSSCR: Schur FGMRES(scaled BFBt) / A11 FGMRES + GMG (Chebyshev block-Jacobi, degree 2+2)",
                           "target_rel_residual": 1e-6, "rel_residual": rep.rel_residual,
                           "outer_its": rep.outer_its, "inner_its": rep.inner_its_total, "vcycles": rep.vcycles,
+                          "pc_inner_its": rep.pc_inner_its,
                           "stokes_solve_s": rep.t_solve_ms / 1e3, "setup_ms": rep.t_setup_ms,
                           "l2": "256 MB buffer written between timed steps", "parallelism": f"replicas x{world}"},
                "roofline": roofline, "kernels": kernels, "operator": operator_rates, "cpu_baseline": cpu, "e2e": e2e,

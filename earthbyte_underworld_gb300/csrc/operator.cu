@@ -21,6 +21,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <cstring>
 #include <iterator>
 
 #include "internal.cuh"
@@ -1036,6 +1037,66 @@ static GeoArgs geo_of(Context& c, const MeshDesc& m) {
     return a;
 }
 
+const double* fine_widths(Context& c, int off[3]) {
+    GeoArgs a = geo_of(c, c.levels[0].mesh);
+    for (int d = 0; d < 3; ++d) off[d] = a.off[d];
+    return a.h;
+}
+
+// ||G||_inf over the free velocity rows: max over free dofs (n, d) of sum_e |G_(n,d),e|
+template <int DIM>
+__global__ void k_g_rowsum_max(Grid g, GeoArgs geo, const uint8_t* __restrict__ fixed,
+                               unsigned long long* __restrict__ out) {
+    int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double best = 0.0;
+    if (n < g.nn) {
+        int64_t idx[3] = {n % g.nx, (n / g.nx) % g.ny, DIM == 3 ? n / (g.nx * g.ny) : 0};
+        int64_t ecount[3] = {g.ex, g.ey, g.ez};
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int o = 0; o < (1 << DIM); ++o) {
+            int64_t e3[3] = {0, 0, 0};
+            bool ok = true;
+            for (int d = 0; d < DIM; ++d) {
+                e3[d] = idx[d] - ((o >> d) & 1);
+                if (e3[d] < 0 || e3[d] >= ecount[d]) ok = false;
+            }
+            if (!ok) continue;
+            double h[3];
+            element_h<DIM>(geo, e3[0], e3[1], e3[2], h);
+            for (int d = 0; d < DIM; ++d) acc[d] += fabs(gval<DIM>(h, o, d));
+        }
+        for (int d = 0; d < DIM; ++d)
+            if (!(fixed && fixed[n * DIM + d])) best = fmax(best, acc[d]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_xor_sync(0xffffffffu, best, o));
+    // non-negative doubles order like their bit patterns
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(best));
+}
+
+double g_inf_norm(Context& c) {
+    const Level& L = c.levels[0];
+    Grid g = grid_of(L.mesh);
+    c.scratch.ensure(8);
+    auto* out = reinterpret_cast<unsigned long long*>(c.scratch.p);
+    UWG_CUDA(cudaMemsetAsync(out, 0, sizeof(unsigned long long), c.stream));
+    {
+        LaunchScope ls(c, -1);
+        if (g.dim == 3)
+            k_g_rowsum_max<3><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), L.fixed.p, out);
+        else
+            k_g_rowsum_max<2><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), L.fixed.p, out);
+    }
+    check_launch("k_g_rowsum_max");
+    unsigned long long bits = 0;
+    UWG_CUDA(cudaMemcpyAsync(c.host_scalars, out, sizeof(bits), cudaMemcpyDeviceToHost, c.stream));
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+    std::memcpy(&bits, c.host_scalars, sizeof(bits));
+    double v;
+    std::memcpy(&v, &bits, sizeof(v));
+    return v;
+}
+
 void op_G(Context& c, const double* p, double* u) {
     const Level& L = c.levels[0];
     Grid g = grid_of(L.mesh);
@@ -1096,29 +1157,6 @@ __global__ void k_rowmax_weights(Grid g, const double* __restrict__ A, const uin
     }
 }
 
-// diag(G^T W G) per element (Jacobi preconditioner of the inner BFBt solves)
-template <int DIM>
-__global__ void k_gwg_diag(Grid g, GeoArgs geo, const double* __restrict__ W, double* __restrict__ S) {
-    int64_t ne = (int64_t)g.ex * g.ey * g.ez;
-    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ne) return;
-    int64_t ie = e % g.ex, je = (e / g.ex) % g.ey, ke = DIM == 3 ? e / ((int64_t)g.ex * g.ey) : 0;
-    double h[3];
-    element_h<DIM>(geo, ie, je, ke, h);
-    int64_t base = ie + g.nx * (je + g.ny * ke);
-    double acc = 0.0;
-#pragma unroll
-    for (int a = 0; a < (1 << DIM); ++a) {
-        int64_t n = base + (a & 1) + ((a >> 1) & 1) * g.nx + (DIM == 3 ? ((a >> 2) & 1) * g.nx * g.ny : 0);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-            double gv = gval<DIM>(h, a, d);
-            acc += gv * gv * W[(int64_t)d * g.nn + n];
-        }
-    }
-    S[e] = acc;
-}
-
 void bfbt_weights(Context& c, double* W) {
     const Level& L = c.levels[0];
     Grid g = grid_of(L.mesh);
@@ -1130,11 +1168,8 @@ void bfbt_weights(Context& c, double* W) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Device-resident Jacobi-preconditioned CG on G^T W G (the inner solves of the scaled BFBt
-// preconditioner), in FP64 or FP32 arithmetic (T).  The scalars live in device memory as FP64
-// (double-buffered by iteration parity), so an iteration is four fused kernels with no host
-// round trip; the host reads the residual norm every few iterations to test convergence.
-//   scal[0] = p.q   scal[1], scal[2] = r.z (parity)   scal[3] = r.r   scal[4] = r0.r0
+// FP32 forms of G and G^T for the middle of the scaled BFBt apply in the mixed form
+// (s = W G p, then G^T s); the inner G^T W G solves use its explicit stencil (gwg_stencil.cu).
 // ------------------------------------------------------------------------------------------
 template <typename T>
 struct GeoT {
@@ -1152,21 +1187,9 @@ __device__ __forceinline__ T gvalT(const T h[3], int a, int d) {
     return -s * area * (T)(DIM == 3 ? 0.25 : 0.5);
 }
 
-__device__ __forceinline__ double block_sum(double v, double* sw) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) sw[warp] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (threadIdx.x == 0)
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sw[w];
-    return t;  // valid in thread 0
-}
-
 // s = W (G p)
 template <int DIM, typename T>
-__global__ void k_pcg_gp(Grid g, GeoT<T> geo, const T* __restrict__ p, const T* __restrict__ W,
+__global__ void k_wgp(Grid g, GeoT<T> geo, const T* __restrict__ p, const T* __restrict__ W,
                          const uint8_t* __restrict__ fixed, T* __restrict__ s) {
     int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= g.nn) return;
@@ -1198,116 +1221,28 @@ __global__ void k_pcg_gp(Grid g, GeoT<T> geo, const T* __restrict__ p, const T* 
         s[(int64_t)d * g.nn + n] = (fixed && fixed[n * DIM + d]) ? (T)0 : acc[d] * W[(int64_t)d * g.nn + n];
 }
 
-// q = G^T s ; scal[0] += p.q (when scal is given); clears the accumulators the next kernel fills
+// q = G^T s
 template <int DIM, typename T>
-__global__ void k_pcg_gts(Grid g, GeoT<T> geo, const T* __restrict__ s, const T* __restrict__ p,
-                          T* __restrict__ q, double* __restrict__ scal, int parity) {
-    __shared__ double sw[32];
+__global__ void k_gts(Grid g, GeoT<T> geo, const T* __restrict__ s, T* __restrict__ q) {
     int64_t ne = (int64_t)g.ex * g.ey * g.ez;
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    double local = 0.0;
-    if (e < ne) {
-        int64_t i3[3] = {e % g.ex, (e / g.ex) % g.ey, DIM == 3 ? e / ((int64_t)g.ex * g.ey) : 0};
-        T h[3];
+    if (e >= ne) return;
+    int64_t i3[3] = {e % g.ex, (e / g.ex) % g.ey, DIM == 3 ? e / ((int64_t)g.ex * g.ey) : 0};
+    T h[3];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) h[d] = __ldg(geo.h + geo.off[d] + i3[d]);
-        int64_t base = i3[0] + g.nx * (i3[1] + g.ny * i3[2]);
-        T acc = (T)0;
+    for (int d = 0; d < DIM; ++d) h[d] = __ldg(geo.h + geo.off[d] + i3[d]);
+    int64_t base = i3[0] + g.nx * (i3[1] + g.ny * i3[2]);
+    T acc = (T)0;
 #pragma unroll
-        for (int a = 0; a < (1 << DIM); ++a) {
-            int64_t n = base + (a & 1) + ((a >> 1) & 1) * g.nx + (DIM == 3 ? ((a >> 2) & 1) * g.nx * g.ny : 0);
+    for (int a = 0; a < (1 << DIM); ++a) {
+        int64_t n = base + (a & 1) + ((a >> 1) & 1) * g.nx + (DIM == 3 ? ((a >> 2) & 1) * g.nx * g.ny : 0);
 #pragma unroll
-            for (int d = 0; d < DIM; ++d) acc = fma(gvalT<DIM, T>(h, a, d), s[(int64_t)d * g.nn + n], acc);
-        }
-        q[e] = acc;
-        if (p) local = (double)acc * (double)p[e];
+        for (int d = 0; d < DIM; ++d) acc = fma(gvalT<DIM, T>(h, a, d), s[(int64_t)d * g.nn + n], acc);
     }
-    if (!scal) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        scal[1 + (parity ^ 1)] = 0.0;  // r.z of this iteration (filled by k_pcg_update)
-        scal[3] = 0.0;
-    }
-    double t = block_sum(local, sw);
-    if (threadIdx.x == 0) atomicAdd(&scal[0], t);
+    q[e] = acc;
 }
 
-// alpha = rz/pq ; x += alpha p ; r -= alpha q ; z = r/d ; scal[rz_new] += r.z ; scal[3] += r.r
-template <typename T>
-__global__ void k_pcg_update(int64_t ne, const T* __restrict__ p, const T* __restrict__ q, const T* __restrict__ d,
-                             T* __restrict__ x, T* __restrict__ r, T* __restrict__ z, double* __restrict__ scal,
-                             int parity) {
-    __shared__ double sw[32];
-    T alpha = (T)(scal[1 + parity] / scal[0]);
-    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    double rz = 0.0, rr = 0.0;
-    if (e < ne) {
-        x[e] = fma(alpha, p[e], x[e]);
-        T re = fma(-alpha, q[e], r[e]);
-        r[e] = re;
-        T ze = re / d[e];
-        z[e] = ze;
-        rz = (double)re * (double)ze;
-        rr = (double)re * (double)re;
-    }
-    double t1 = block_sum(rz, sw);
-    __syncthreads();
-    double t2 = block_sum(rr, sw);
-    if (threadIdx.x == 0) {
-        atomicAdd(&scal[1 + (parity ^ 1)], t1);
-        atomicAdd(&scal[3], t2);
-    }
-}
-
-// beta = rz_new/rz ; p = z + beta p ; clears p.q for the next iteration
-template <typename T>
-__global__ void k_pcg_dir(int64_t ne, const T* __restrict__ z, T* __restrict__ p, double* __restrict__ scal,
-                          int parity) {
-    T beta = (T)(scal[1 + (parity ^ 1)] / scal[1 + parity]);
-    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < ne) p[e] = fma(beta, p[e], z[e]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) scal[0] = 0.0;
-}
-
-// initial state: r = b (projected by the caller), z = r/d, p = z, x = 0, scal[1] = r.z,
-// scal[3] = scal[4] = r.r
-template <typename B, typename T>
-__global__ void k_pcg_init(int64_t ne, const B* __restrict__ b, const T* __restrict__ d, T* __restrict__ x,
-                           T* __restrict__ r, T* __restrict__ z, T* __restrict__ p, double* __restrict__ scal) {
-    __shared__ double sw[32];
-    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    double rz = 0.0, rr = 0.0;
-    if (e < ne) {
-        T re = (T)b[e];
-        T ze = re / d[e];
-        x[e] = (T)0;
-        r[e] = re;
-        z[e] = ze;
-        p[e] = ze;
-        rz = (double)re * (double)ze;
-        rr = (double)re * (double)re;
-    }
-    double t1 = block_sum(rz, sw);
-    __syncthreads();
-    double t2 = block_sum(rr, sw);
-    if (threadIdx.x == 0) {
-        atomicAdd(&scal[1], t1);
-        atomicAdd(&scal[3], t2);
-        atomicAdd(&scal[4], t2);
-    }
-}
-
-template <typename T>
-static GeoT<T> geo_T(Context& c, const MeshDesc& m);
-template <>
-GeoT<double> geo_T<double>(Context& c, const MeshDesc& m) {
-    GeoArgs a = geo_of(c, m);
-    GeoT<double> g;
-    g.h = a.h;
-    for (int d = 0; d < 3; ++d) g.off[d] = a.off[d];
-    return g;
-}
-template <>
-GeoT<float> geo_T<float>(Context& c, const MeshDesc& m) {
+static GeoT<float> geo_f32(Context& c, const MeshDesc& m) {
     GeoArgs a = geo_of(c, m);
     size_t n = (size_t)m.nel[0] + m.nel[1] + (m.dim == 3 ? m.nel[2] : 0);
     if (c.elem_h32_for != c.elem_h_for) {
@@ -1322,101 +1257,23 @@ GeoT<float> geo_T<float>(Context& c, const MeshDesc& m) {
     return g;
 }
 
-// Solves (G^T W G) x = b (b projected off the constant by the caller) to ||r|| <= rtol ||b||.
-// work holds 4*ne values of T; scal 8 doubles; s is a velocity-sized temporary.
-template <typename T>
-static int gwg_pcg_T(Context& c, const T* W, const T* d, const double* b, T* x, double rtol, int maxit, T* work,
-                     T* s, double* scal) {
-    const Level& L = c.levels[0];
-    Grid g = grid_of(L.mesh);
-    GeoT<T> geo = geo_T<T>(c, L.mesh);
-    int64_t ne = L.mesh.ne;
-    T* r = work;
-    T* z = work + ne;
-    T* p = work + 2 * ne;
-    T* q = work + 3 * ne;
-    UWG_CUDA(cudaMemsetAsync(scal, 0, 8 * sizeof(double), c.stream));
-    unsigned eb = blocks_for(ne, 256), nb = blocks_for(g.nn, 256);
-    {
-        LaunchScope ls(c, UWGPU_KERNEL_SCHUR_PC);
-        k_pcg_init<double, T><<<eb, 256, 0, c.stream>>>(ne, b, d, x, r, z, p, scal);
-    }
-    double* hs = c.host_scalars;
-    UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-    UWG_CUDA(cudaStreamSynchronize(c.stream));
-    double r0 = std::sqrt(hs[4]);
-    if (!(r0 > 0.0)) return 0;
-    // Eight iterations (an even number, so the scalar parity repeats) are captured once as a
-    // CUDA graph for this buffer set and replayed; the host tests convergence after each replay.
-    const int block = 8;
-    auto issue = [&](int parity) {
-        if (g.dim == 3) k_pcg_gp<3, T><<<nb, 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
-        else k_pcg_gp<2, T><<<nb, 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
-        if (g.dim == 3) k_pcg_gts<3, T><<<eb, 256, 0, c.stream>>>(g, geo, s, p, q, scal, parity);
-        else k_pcg_gts<2, T><<<eb, 256, 0, c.stream>>>(g, geo, s, p, q, scal, parity);
-        k_pcg_update<T><<<eb, 256, 0, c.stream>>>(ne, p, q, d, x, r, z, scal, parity);
-        k_pcg_dir<T><<<eb, 256, 0, c.stream>>>(ne, z, p, scal, parity);
-    };
-    const void* key[8] = {W, d, x, work, s, scal, (const void*)(intptr_t)ne, (const void*)(intptr_t)sizeof(T)};
-    Context::PcgGraph* pg = nullptr;
-    for (auto& cand : c.pcg_graphs)
-        if (std::equal(std::begin(key), std::end(key), std::begin(cand.key))) pg = &cand;
-    if (!pg) {
-        c.pcg_graphs.emplace_back();
-        pg = &c.pcg_graphs.back();
-        std::copy(std::begin(key), std::end(key), std::begin(pg->key));
-        cudaGraph_t graph;
-        UWG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < block; ++k) issue(k & 1);
-        UWG_CUDA(cudaStreamEndCapture(c.stream, &graph));
-        UWG_CUDA(cudaGraphInstantiate(&pg->exec, graph, 0));
-        UWG_CUDA(cudaGraphDestroy(graph));
-    }
-    int it = 0;
-    while (it < maxit) {
-        {
-            LaunchScope ls(c, UWGPU_KERNEL_SCHUR_PC);
-            UWG_CUDA(cudaGraphLaunch(pg->exec, c.stream));
-        }
-        c.launches += 4 * block - 1;
-        it += block;
-        UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-        UWG_CUDA(cudaStreamSynchronize(c.stream));
-        double rn = std::sqrt(hs[3]);
-        if (!std::isfinite(rn)) throw Error(UWGPU_ERR_NAN, "NaN in the BFBt inner solve");
-        if (rn <= rtol * r0) break;
-    }
-    check_launch("gwg_pcg");
-    return it;
-}
-
-int gwg_pcg(Context& c, const double* W, const double* d, const double* b, double* x, double rtol, int maxit,
-            double* work, double* s) {
-    return gwg_pcg_T<double>(c, W, d, b, x, rtol, maxit, work, s, work + 4 * c.levels[0].mesh.ne);
-}
-
-int gwg_pcg32(Context& c, const float* W, const float* d, const double* b, float* x, double rtol, int maxit,
-              float* work, float* s, double* scal) {
-    return gwg_pcg_T<float>(c, W, d, b, x, rtol, maxit, work, s, scal);
-}
-
 // FP32 pieces of the scaled BFBt apply: s = W (G p) and q = G^T s
 void op_wg32(Context& c, const float* p, const float* W, float* s) {
     const Level& L = c.levels[0];
     Grid g = grid_of(L.mesh);
-    GeoT<float> geo = geo_T<float>(c, L.mesh);
+    GeoT<float> geo = geo_f32(c, L.mesh);
     LaunchScope ls(c, UWGPU_KERNEL_SCHUR_PC);
-    if (g.dim == 3) k_pcg_gp<3, float><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
-    else k_pcg_gp<2, float><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
+    if (g.dim == 3) k_wgp<3, float><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
+    else k_wgp<2, float><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, geo, p, W, L.fixed.p, s);
 }
 
 void op_gt32(Context& c, const float* s, float* q) {
     const Level& L = c.levels[0];
     Grid g = grid_of(L.mesh);
-    GeoT<float> geo = geo_T<float>(c, L.mesh);
+    GeoT<float> geo = geo_f32(c, L.mesh);
     LaunchScope ls(c, UWGPU_KERNEL_SCHUR_PC);
-    if (g.dim == 3) k_pcg_gts<3, float><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo, s, nullptr, q, nullptr, 0);
-    else k_pcg_gts<2, float><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo, s, nullptr, q, nullptr, 0);
+    if (g.dim == 3) k_gts<3, float><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo, s, q);
+    else k_gts<2, float><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo, s, q);
 }
 
 void to_float(Context& c, const double* a, float* b, int64_t n) {
@@ -1427,16 +1284,6 @@ void to_float(Context& c, const double* a, float* b, int64_t n) {
 void to_double(Context& c, const float* a, double* b, int64_t n) {
     LaunchScope ls(c, UWGPU_KERNEL_SCHUR_PC);
     k_convert<float, double><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, a, b);
-}
-
-void gwg_diag(Context& c, const double* W, double* S) {
-    const Level& L = c.levels[0];
-    Grid g = grid_of(L.mesh);
-    LaunchScope ls(c, -1);
-    if (g.dim == 3)
-        k_gwg_diag<3><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), W, S);
-    else
-        k_gwg_diag<2><<<blocks_for(L.mesh.ne, 256), 256, 0, c.stream>>>(g, geo_of(c, L.mesh), W, S);
 }
 
 void gkgdiag(Context& c, double* S) {

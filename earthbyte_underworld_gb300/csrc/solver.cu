@@ -33,11 +33,14 @@ void op_GT_unmasked(Context& c, const double* u, double* p);
 void gather_force(Context& c, double* f);
 void gkgdiag(Context& c, double* S);
 void bfbt_weights(Context& c, double* W);
-void gwg_diag(Context& c, const double* W, double* S);
-int gwg_pcg(Context& c, const double* W, const double* d, const double* b, double* x, double rtol, int maxit,
-            double* work, double* s);
-int gwg_pcg32(Context& c, const float* W, const float* d, const double* b, float* x, double rtol, int maxit,
-              float* work, float* s, double* scal);
+void gwg_stencil_build(Context& c, const double* W, double* A, double* dinv);
+void gwg_stencil_fp32(Context& c, const double* A, const double* dinv, float* A32, float* dinv32);
+void gwg_stencil_apply(Context& c, const double* A, const double* x, double* y, double* scal);
+int gwg_cg(Context& c, const double* A, const double* dinv, const double* b, double* x, double rtol, int maxit,
+           double* work, double* scal);
+int gwg_cg32(Context& c, const float* A, const float* dinv, const double* b, float* x, double rtol, int maxit,
+             float* work, double* scal);
+double g_inf_norm(Context& c);
 void op_wg32(Context& c, const float* p, const float* W, float* s);
 void op_gt32(Context& c, const float* s, float* q);
 void to_float(Context& c, const double* a, float* b, int64_t n);
@@ -178,6 +181,16 @@ __global__ void k_combine(int64_t n, const T* __restrict__ Z, int64_t ldz, int m
 __global__ void k_pattern(int64_t n, double* __restrict__ x) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) x[i] = (double)(((uint64_t)i * 2654435761ull >> 7) & 1023ull) / 1023.0 - 0.5;
+}
+
+// element-parity indicators of the P0 pressure grid: t = 1 where i+j+k is even, v = 1 where odd
+// (KSPBuildPressure_CB_Nullspace_BSSCR, ksp_pressure_nullspace.c:23-75)
+__global__ void k_parity_fill(int64_t ex, int64_t ey, int64_t ne, double* __restrict__ t, double* __restrict__ v) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    int64_t par = (e % ex + (e / ex) % ey + e / (ex * ey)) & 1;
+    t[e] = par ? 0.0 : 1.0;
+    v[e] = par ? 1.0 : 0.0;
 }
 
 __global__ void k_remove_mean(int64_t n, const double* __restrict__ sum, double* __restrict__ x) {
@@ -401,12 +414,17 @@ struct Bsscr {
     int64_t nv = 0, npres = 0;
     bool mixed = false;
     DArray<double> f, h, hhat, tu, tu2, t2, Sd, rhs_p, ref_r, ref_d;
-    // scaled BFBt state: weights, G^T W G diagonal, work vectors
-    DArray<double> bw, bd, bt, bt2, bs, bX, pr, pz, pp, pq, ptmp;
+    // scaled BFBt state: weights, G^T W G stencil and inverse diagonal, work vectors
+    DArray<double> bw, bA, bd, bt, bt2, bs, bX, pr, pz, pp, pq, ptmp;
     // FP32 copies for the mixed form (the preconditioner runs in FP32 inside the FP64 Schur FGMRES)
-    DArray<float> bw32, bd32, bt32, bt2_32, bs32, bX32, pz32;
+    DArray<float> bw32, bA32, bd32, bt32, bt2_32, bs32, bX32, pz32;
     DArray<double> scal32;
     int64_t bfbt_its = 0;
+    // pressure null-space vectors (constant, or the two element-parity indicators), each used
+    // only when G maps it to (nearly) zero; and whether G^T W G has the constant null space
+    DArray<double> ns_t, ns_v;
+    bool ns_use_t = false, ns_use_v = false;
+    bool bbt_const = false;
     DArray<float> r32, d32;
     bool nan = false;
     bool inner_fail = false;
@@ -541,21 +559,15 @@ struct Bsscr {
         k_pointwise_mul<<<blocks_for(n, 256), 256, 0, c.stream>>>(n, a, b, y);
     }
 
-    // y = G^T W G x
-    void gwg_apply(const double* x, double* y) {
-        op_G(c, x, bs.p);
-        pmul(nv, bs.p, bw.p, bs.p);
-        op_GT(c, bs.p, y);
-    }
-
     // Jacobi-preconditioned CG on G^T W G (the inner KSP of the scaled BFBt preconditioner), with
-    // the right-hand side projected off the constant null space (pc_ScaledGtKG.c:266-268)
+    // the right-hand side projected off the constant null space when G^T W G has it
+    // (pc_ScaledGtKG.c:266-268, 829-831)
     void gwg_solve(const double* b, double* x) {
         int maxit = o.bfbt_max_it > 0 ? o.bfbt_max_it : 500;
         double rtol = o.bfbt_rtol > 0 ? o.bfbt_rtol : 1e-4;
         copy<double>(c, npres, b, pr.p);
-        remove_constant_dev(pr.p);
-        bfbt_its += gwg_pcg(c, bw.p, bd.p, pr.p, x, rtol, maxit, pz.p, bs.p);
+        if (bbt_const) remove_constant_dev(pr.p);
+        bfbt_its += gwg_cg(c, bA.p, bd.p, pr.p, x, rtol, maxit, pz.p, pz.p + 4 * npres);
     }
 
     // the same preconditioner with FP32 operators, inner solves and vectors (mixed form)
@@ -563,8 +575,8 @@ struct Bsscr {
         int maxit = o.bfbt_max_it > 0 ? o.bfbt_max_it : 500;
         double rtol = o.bfbt_rtol > 0 ? o.bfbt_rtol : 1e-4;
         copy<double>(c, npres, x, pr.p);
-        remove_constant_dev(pr.p);
-        bfbt_its += gwg_pcg32(c, bw32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, bs32.p, scal32.p);
+        if (bbt_const) remove_constant_dev(pr.p);
+        bfbt_its += gwg_cg32(c, bA32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, scal32.p);
         op_wg32(c, bt32.p, bw32.p, bs32.p);
         level_apply<float>(c, c.levels[0], bs32.p, bX32.p);
         {
@@ -573,8 +585,8 @@ struct Bsscr {
         }
         op_gt32(c, bX32.p, bt2_32.p);
         to_double(c, bt2_32.p, pr.p, npres);
-        remove_constant_dev(pr.p);
-        bfbt_its += gwg_pcg32(c, bw32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, bs32.p, scal32.p);
+        if (bbt_const) remove_constant_dev(pr.p);
+        bfbt_its += gwg_cg32(c, bA32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, scal32.p);
         to_double(c, bt32.p, y, npres);
     }
 
@@ -594,6 +606,8 @@ struct Bsscr {
     }
 
     void remove_constant_dev(double* x);
+    void setup_nullspace();
+    void project_nullspace(double* x);
 
     void schur_pc(const double* v, double* z) {
         if (o.schur_pc == UWGPU_SCHUR_PC_NONE) {
@@ -754,6 +768,44 @@ __global__ void k_bc_vector(int64_t nn, const uint8_t* __restrict__ fixed, const
 
 void Bsscr::remove_constant_dev(double* x) { remove_constant(c, npres, x, ptmp); }
 
+// KSPBuildPressure_Const_Nullspace_BSSCR / _CB_Nullspace_BSSCR (ksp_pressure_nullspace.c:23-115):
+// remove_const_p = 1 builds the constant vector, 2 the even and odd element-parity indicators.
+// KSPRemovePressureNullspace_BSSCR (ksp_pressure_nullspace.c:121-176) projects a vector w out
+// only when ||G w|| / ||w|| < nstol ||G||_inf, nstol = 1e-7 (BSSCR.c:391).
+void Bsscr::setup_nullspace() {
+    int mode = o.remove_const_p;
+    ns_use_t = ns_use_v = false;
+    if (mode != 1 && mode != 2) return;
+    const MeshDesc& m = c.mesh;
+    ns_t.ensure(npres);
+    if (mode == 1) {
+        LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
+        k_set<double><<<blocks_for(npres, 256), 256, 0, c.stream>>>(npres, 1.0, ns_t.p);
+    } else {
+        ns_v.ensure(npres);
+        LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
+        k_parity_fill<<<blocks_for(npres, 256), 256, 0, c.stream>>>(m.nel[0], m.nel[1], npres, ns_t.p, ns_v.p);
+    }
+    const double ginf = g_inf_norm(c);
+    auto in_nullspace = [&](const double* w) {
+        op_G(c, w, tu.p);
+        double gn = red.norm<double>(nv, tu.p), wn = red.norm<double>(npres, w);
+        return wn > 0.0 && gn / wn < 1e-7 * ginf;
+    };
+    ns_use_t = in_nullspace(ns_t.p);
+    if (mode == 2) ns_use_v = in_nullspace(ns_v.p);
+}
+
+void Bsscr::project_nullspace(double* x) {
+    for (int k = 0; k < 2; ++k) {
+        bool use = k == 0 ? ns_use_t : ns_use_v;
+        const double* w = k == 0 ? ns_t.p : ns_v.p;
+        if (!use) continue;
+        double a1 = red.dot<double>(npres, w, x), a2 = red.dot<double>(npres, w, w);
+        axpy<double>(c, npres, -a1 / a2, w, x);
+    }
+}
+
 void Bsscr::run() {
     auto t0 = std::chrono::steady_clock::now();
     dim = c.mesh.dim;
@@ -823,14 +875,24 @@ void Bsscr::run() {
         for (auto* v : {&bd, &bt, &bt2, &pr}) v->ensure(npres);
         pz.ensure(4 * npres + 8);
         bfbt_weights(c, bw.p);
-        gwg_diag(c, bw.p, bd.p);
+        bA.ensure((size_t)(dim == 3 ? 27 : 9) * npres);
+        gwg_stencil_build(c, bw.p, bA.p, bd.p);
+        // BSSCR_MatContainsConstNullSpace (Stokes_Nullspace.c:15-46) on G^T W G:
+        // ||A (1/N)||_2 < 1e-7 attaches the constant null space to the inner solves
+        {
+            LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
+            k_set<double><<<blocks_for(npres, 256), 256, 0, c.stream>>>(npres, 1.0 / (double)npres, bt.p);
+        }
+        gwg_stencil_apply(c, bA.p, bt.p, bt2.p, pz.p + 4 * npres);
+        bbt_const = red.norm<double>(npres, bt2.p) < 1e-7;
         if (mixed) {
             for (auto* v : {&bw32, &bs32, &bX32}) v->ensure(nv);
             for (auto* v : {&bd32, &bt32, &bt2_32}) v->ensure(npres);
             pz32.ensure(4 * npres);
             scal32.ensure(8);
             to_float(c, bw.p, bw32.p, nv);
-            to_float(c, bd.p, bd32.p, npres);
+            bA32.ensure((size_t)(dim == 3 ? 27 : 9) * npres);
+            gwg_stencil_fp32(c, bA.p, bd.p, bA32.p, bd32.p);
         }
     }
     UWG_CUDA(cudaStreamSynchronize(c.stream));
@@ -844,8 +906,8 @@ void Bsscr::run() {
     axpy<double>(c, npres, 1.0, h.p, hhat.p);
     // solve (G^T K^{-1} G) p = -h_hat
     scale<double>(c, npres, -1.0, hhat.p, rhs_p.p);
-    DArray<double> tmp;
-    if (o.remove_const_p) remove_constant(c, npres, rhs_p.p, tmp);
+    setup_nullspace();
+    project_nullspace(rhs_p.p);
     int maxo = o.max_outer > 0 ? o.max_outer : 500;
     int outer = 0;
     bool outer_fail = false;
@@ -860,7 +922,7 @@ void Bsscr::run() {
         if (nn) nan = true;
         if (bn > 0 && res > o.scr_rtol * bn * 1.0000001) outer_fail = true;
     }
-    if (o.remove_const_p) remove_constant(c, npres, c.p_sol.p, tmp);
+    project_nullspace(c.p_sol.p);
     // back-solve u = K^{-1} (f - G p)
     op_G(c, c.p_sol.p, t2.p);
     scale<double>(c, nv, -1.0, t2.p, t2.p);
@@ -890,6 +952,7 @@ void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
     UWG_REQUIRE(o.schur_type == UWGPU_SCHUR_CG || o.schur_type == UWGPU_SCHUR_FGMRES, UWGPU_ERR_ARGUMENT, "bad Schur type");
     UWG_REQUIRE(o.schur_pc >= 0 && o.schur_pc <= 3, UWGPU_ERR_ARGUMENT, "bad Schur preconditioner");
     UWG_REQUIRE(o.smoother == UWGPU_SMOOTHER_COLOUR_GS || o.smoother == UWGPU_SMOOTHER_CHEBYSHEV, UWGPU_ERR_ARGUMENT, "bad smoother");
+    UWG_REQUIRE(o.remove_const_p >= 0 && o.remove_const_p <= 2, UWGPU_ERR_ARGUMENT, "bad pressure null-space mode");
     Bsscr s(c, o, rep);
     s.run();
 }

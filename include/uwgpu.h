@@ -97,7 +97,11 @@ typedef struct {
     double scr_rtol;          /* -scr_ksp_rtol                                           */
     double a11_rtol;          /* -A11_ksp_rtol                                           */
     double back_rtol;         /* -backsolveA11_ksp_rtol                                  */
-    int32_t remove_const_p;   /* -remove_constant_pressure_null_space                    */
+    int32_t remove_const_p;   /* pressure null space projected out of the Schur rhs and p:
+                                 0 none, 1 constant (-remove_constant_pressure_null_space),
+                                 2 even/odd element parity (-remove_checkerboard_pressure_null_space);
+                                 a vector is used only when ||G w||/||w|| < 1e-7 ||G||_inf
+                                 (ksp_pressure_nullspace.c:23-176, BSSCR.c:330-347)            */
     int32_t precision;        /* UWGPU_PREC_FP64 or UWGPU_PREC_MIXED                     */
     double target_rel_residual; /* > 0: stop the outer solve once the full Stokes residual
                                    ||[f-Ku-Gp; h-G^T u]|| / ||[f;h]|| is below this value */

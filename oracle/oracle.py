@@ -245,7 +245,7 @@ def solve_bsscr(m, fixed, Ke, Ge, fe, Se, mg_levels=3, smooth=2, schur_type=1, s
                 scr_rtol=1e-10, a11_rtol=1e-12, back_rtol=1e-12, restart=30, max_outer=500,
                 max_inner=2000, remove_const_p=True, nthreads=0, bfbt_rtol=1e-4, bfbt_max_it=500):
     o = SolveOpts(mg_levels, smooth, smooth, schur_type, schur_pc, restart, max_outer, max_inner,
-                  scr_rtol, a11_rtol, back_rtol, 1 if remove_const_p else 0, nthreads, bfbt_rtol, bfbt_max_it, 0)
+                  scr_rtol, a11_rtol, back_rtol, int(remove_const_p), nthreads, bfbt_rtol, bfbt_max_it, 0)
     nn = num_nodes(m)
     E = num_elements(m)
     u = np.zeros((nn, m.dim))

@@ -1237,6 +1237,7 @@ typedef struct {
     double* gwgd;   /* diag(G^T W G) */
     double *pr, *pz, *pp, *pq, *pt, *pt2, *vs, *vX;
     int64_t bfbt_its;
+    int bbt_const;  /* G^T W G has the constant null space (Stokes_Nullspace.c:15-46) */
 } bsscr_t;
 
 static void op_K(void* c, const double* x, double* y) { csr_mv(&((bsscr_t*)c)->K, x, y); }
@@ -1263,12 +1264,15 @@ static void gwg_apply(bsscr_t* s, const double* x, double* y) {
 }
 
 /* inner KSP of the scaled BFBt preconditioner: Jacobi-preconditioned CG on G^T W G, the
- * right-hand side projected off the constant null space (pc_ScaledGtKG.c:266-268) */
+ * right-hand side projected off the constant null space when G^T W G has it
+ * (pc_ScaledGtKG.c:266-268, 829-831) */
 static void gwg_solve(bsscr_t* s, const double* b, double* x) {
     int64_t n = s->G.nc;
     double mean = 0.0;
-    for (int64_t i = 0; i < n; ++i) mean += b[i];
-    mean /= (double)n;
+    if (s->bbt_const) {
+        for (int64_t i = 0; i < n; ++i) mean += b[i];
+        mean /= (double)n;
+    }
     for (int64_t i = 0; i < n; ++i) { x[i] = 0.0; s->pr[i] = b[i] - mean; }
     double r0 = sqrt(dot(n, s->pr, s->pr));
     if (!(r0 > 0.0)) return;
@@ -1339,11 +1343,55 @@ static int pcg(int64_t n, op_fn A, void* actx, op_fn M, void* mctx, const double
     return it;
 }
 
-static void remove_constant(int64_t n, double* v) {
-    double s = 0.0;
-    for (int64_t i = 0; i < n; ++i) s += v[i];
-    s /= (double)n;
-    for (int64_t i = 0; i < n; ++i) v[i] -= s;
+/* Pressure null-space vectors (ksp_pressure_nullspace.c:23-115): mode 1 the constant, mode 2 the
+ * even and odd element-parity indicators (i+j+k even / odd).  A vector is used only when
+ * ||G w|| / ||w|| < nstol ||G||_inf with nstol = 1e-7 (BSSCR.c:391, ksp_pressure_nullspace.c:140-170). */
+typedef struct {
+    int use[2];
+    double* w[2];
+} nullspace_t;
+
+static void nullspace_setup(nullspace_t* ns, const uwr_mesh* m, const csr* G, int mode) {
+    int64_t E = G->nc;
+    memset(ns, 0, sizeof(*ns));
+    if (mode != 1 && mode != 2) return;
+    double ginf = 0.0;
+    for (int64_t r = 0; r < G->nr; ++r) {
+        double a = 0.0;
+        for (int64_t k = G->rp[r]; k < G->rp[r + 1]; ++k) a += fabs(G->v[k]);
+        ginf = a > ginf ? a : ginf;
+    }
+    int nvec = mode == 1 ? 1 : 2;
+    double* gw = (double*)malloc(sizeof(double) * (size_t)(G->nr > 0 ? G->nr : 1));
+    for (int k = 0; k < nvec; ++k) {
+        ns->w[k] = (double*)malloc(sizeof(double) * (size_t)E);
+        for (int64_t e = 0; e < E; ++e) {
+            if (mode == 1) {
+                ns->w[k][e] = 1.0;
+            } else {
+                int64_t i = e % m->nel[0], j = (e / m->nel[0]) % m->nel[1];
+                int64_t l = m->dim == 3 ? e / ((int64_t)m->nel[0] * m->nel[1]) : 0;
+                ns->w[k][e] = ((i + j + l) % 2 == k) ? 1.0 : 0.0;
+            }
+        }
+        csr_mv(G, ns->w[k], gw);
+        double gn = sqrt(dot(G->nr, gw, gw)), wn = sqrt(dot(E, ns->w[k], ns->w[k]));
+        ns->use[k] = wn > 0.0 && gn / wn < 1e-7 * ginf;
+    }
+    free(gw);
+}
+
+static void nullspace_project(const nullspace_t* ns, int64_t n, double* x) {
+    for (int k = 0; k < 2; ++k) {
+        if (!ns->use[k]) continue;
+        double a1 = dot(n, ns->w[k], x), a2 = dot(n, ns->w[k], ns->w[k]);
+        for (int64_t i = 0; i < n; ++i) x[i] -= a1 / a2 * ns->w[k][i];
+    }
+}
+
+static void nullspace_free(nullspace_t* ns) {
+    free(ns->w[0]);
+    free(ns->w[1]);
 }
 
 /* Solvers/KSPSolvers/src/BSSCR/auglag-driver-DGTGD.c:53-441 with penalty 0:
@@ -1449,6 +1497,10 @@ int uwr_solve_bsscr(const uwr_mesh* m, const uint8_t* fixed, const double* Ke, c
             for (int b = 0; b < 6; ++b) *bufs[b] = (double*)malloc(sizeof(double) * (size_t)E);
             s.vs = (double*)malloc(sizeof(double) * (size_t)nfree);
             s.vX = (double*)malloc(sizeof(double) * (size_t)nfree);
+            /* BSSCR_MatContainsConstNullSpace (Stokes_Nullspace.c:15-46): ||A (1/N)||_2 < 1e-7 */
+            for (int64_t e = 0; e < E; ++e) s.pt[e] = 1.0 / (double)E;
+            gwg_apply(&s, s.pt, s.pt2);
+            s.bbt_const = sqrt(dot(E, s.pt2, s.pt2)) < 1e-7;
         }
     }
     s.a11_rtol = o->a11_rtol;
@@ -1469,13 +1521,16 @@ int uwr_solve_bsscr(const uwr_mesh* m, const uint8_t* fixed, const double* Ke, c
         /* solve (G^T K^{-1} G) p = -h_hat */
         double* rhs = (double*)malloc(sizeof(double) * (size_t)E);
         for (int64_t e = 0; e < E; ++e) rhs[e] = -hhat[e];
-        if (o->remove_const_p) remove_constant(E, rhs);
+        nullspace_t ns;
+        nullspace_setup(&ns, m, &s.G, o->remove_const_p);
+        nullspace_project(&ns, E, rhs);
         int outer;
         if (o->schur_type == 0)
             outer = pcg(E, op_S, &s, op_Spc, &s, rhs, p, o->scr_rtol, o->max_outer > 0 ? o->max_outer : 1000);
         else
             outer = fgmres(E, op_S, &s, op_Spc, &s, rhs, p, o->scr_rtol, s.restart, o->max_outer > 0 ? o->max_outer : 1000);
-        if (o->remove_const_p) remove_constant(E, p);
+        nullspace_project(&ns, E, p);
+        nullspace_free(&ns);
         /* back-solve */
         double* t = (double*)malloc(sizeof(double) * (size_t)nfree);
         csr_mv(&s.G, p, t);

@@ -120,7 +120,7 @@ typedef struct {
     double scr_rtol;          /* -scr_ksp_rtol                                    */
     double a11_rtol;          /* -A11_ksp_rtol                                    */
     double back_rtol;         /* -backsolveA11_ksp_rtol                           */
-    int32_t remove_const_p;   /* -remove_constant_pressure_null_space             */
+    int32_t remove_const_p;   /* 1 constant, 2 checkerboard pressure null space     */
     int32_t nthreads;
     double bfbt_rtol;         /* inner G^T W G tolerance of the scaled BFBt PC      */
     int32_t bfbt_max_it;

@@ -209,3 +209,82 @@ def test_picard_nonlinear_parity(oracle, uw):
     assert _rel(eta, oeta) < 1e-7
     assert _rel(u, ou) < 1e-7
     assert _rel(p, op) < 1e-7
+
+
+@pytest.mark.parametrize("case", ["rt2d", "spheres"])
+def test_bfbt_preconditioner_matches_oracle(oracle, uw, case):
+    """The scaled BFBt preconditioner (explicit G^T W G stencil + Jacobi CG on the GPU, matrix-free
+    Jacobi CG in the oracle) gives the Schur FGMRES the same iteration count: with tight inner
+    solves both apply the same operator, so a wrong stencil entry shows up as extra outer
+    iterations.  FP64 and mixed forms."""
+    from earthbyte_underworld_gb300 import workloads as W
+    O, U = oracle, uw
+    w = W.rt2d(nel=(32, 32), ppc=20) if case == "rt2d" else W.spheres(nel=(8, 8, 8), nspheres=10, seed=9)
+    ctx, perm, offsets, xi, Ke, fe, Ge, Se, eta = _run_gpu(U, W, w)
+    m = O.make_mesh(w["dim"], w["nel"])
+    ou, op, orep = O.solve_bsscr(m, w["fixed"], Ke, Ge, fe, Se, mg_levels=3, schur_type=1, schur_pc=3,
+                                 scr_rtol=1e-8, a11_rtol=1e-10, back_rtol=1e-10, bfbt_rtol=1e-8, bfbt_max_it=5000)
+    opts = U.default_opts(mg_levels=3, schur_type=1, schur_pc=3, scr_rtol=1e-8, a11_rtol=1e-10, back_rtol=1e-10,
+                          max_outer=400, max_inner=2000, bfbt_rtol=1e-8, bfbt_max_it=5000)
+    u, p, rep = ctx.solve_bsscr(opts)
+    assert abs(rep.outer_its - orep.outer_its) <= 1, (rep.outer_its, orep.outer_its)
+    assert rep.pc_inner_its > 0
+    assert _rel(u, ou) < 1e-6 and _rel(p, op) < 1e-6
+    om = U.default_opts(mg_levels=3, schur_type=1, schur_pc=3, scr_rtol=1e-6, a11_rtol=1e-8, back_rtol=1e-8,
+                        max_outer=400, max_inner=2000, bfbt_rtol=1e-5, bfbt_max_it=5000, precision=U.PREC_MIXED)
+    um, pm, rm = ctx.solve_bsscr(om)
+    assert rm.rel_residual < 1e-6
+    assert rm.outer_its <= orep.outer_its + 2, (rm.outer_its, orep.outer_its)
+    ctx.close()
+
+
+def _walls(nel, dim, mode):
+    """Dirichlet masks: 'noslip' fixes every component on every wall; 'opentop' fixes the normal
+    component on the side and bottom walls and leaves the top (y = 1 in 2D, z = 1 in 3D) free."""
+    nx, ny = nel[0] + 1, nel[1] + 1
+    nz = nel[2] + 1 if dim == 3 else 1
+    idx = np.arange(nx * ny * nz)
+    i, j, k = idx % nx, (idx // nx) % ny, idx // (nx * ny)
+    fixed = np.zeros((len(idx), dim), np.uint8)
+    if mode == "noslip":
+        wall = (i == 0) | (i == nx - 1) | (j == 0) | (j == ny - 1)
+        if dim == 3:
+            wall |= (k == 0) | (k == nz - 1)
+        fixed[wall, :] = 1
+    else:
+        fixed[(i == 0) | (i == nx - 1), 0] = 1
+        if dim == 2:
+            fixed[j == 0, 1] = 1
+        else:
+            fixed[(j == 0) | (j == ny - 1), 1] = 1
+            fixed[k == 0, 2] = 1
+    return fixed.reshape(-1)
+
+
+@pytest.mark.parametrize("walls,mode,pc", [("opentop", 1, 0), ("opentop", 1, 3), ("noslip", 2, 0), ("noslip", 2, 1)])
+def test_pressure_nullspace_modes(oracle, uw, walls, mode, pc):
+    """Null-space vectors are projected only when G maps them to zero (ksp_pressure_nullspace.c):
+    with an open top the constant is not a null vector and the pressure keeps its level; with
+    no-slip walls in 2D the even/odd element-parity vectors are both null vectors."""
+    from earthbyte_underworld_gb300 import workloads as W
+    O, U = oracle, uw
+    w = W.rt2d(nel=(16, 16), ppc=20)
+    w["fixed"] = _walls(w["nel"], 2, walls)
+    ctx, perm, offsets, xi, Ke, fe, Ge, Se, eta = _run_gpu(U, W, w)
+    opts = U.default_opts(mg_levels=3, schur_type=1, schur_pc=pc, scr_rtol=1e-11, a11_rtol=1e-13, back_rtol=1e-13,
+                          max_outer=400, max_inner=2000, bfbt_rtol=1e-8, bfbt_max_it=5000, remove_const_p=mode)
+    u, p, rep = ctx.solve_bsscr(opts)
+    m = O.make_mesh(2, w["nel"])
+    ou, op, orep = O.solve_bsscr(m, w["fixed"], Ke, Ge, fe, Se, mg_levels=3, schur_type=1, schur_pc=pc,
+                                 scr_rtol=1e-11, a11_rtol=1e-13, back_rtol=1e-13, bfbt_rtol=1e-8,
+                                 bfbt_max_it=5000, remove_const_p=mode)
+    assert rep.rel_residual < 1e-9
+    assert _rel(u, ou) < 1e-8
+    assert _rel(p, op) < 1e-8
+    if walls == "opentop":
+        assert abs(p.mean()) > 1e-3 * np.abs(p).max()   # the level was not projected away
+    else:
+        par = (np.arange(p.size) % 16 + np.arange(p.size) // 16) % 2
+        assert abs(p[par == 0].sum()) < 1e-9 * np.abs(p).sum()
+        assert abs(p[par == 1].sum()) < 1e-9 * np.abs(p).sum()
+    ctx.close()
