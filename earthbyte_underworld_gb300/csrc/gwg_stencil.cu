@@ -33,16 +33,27 @@ struct EGrid {
 template <int DIM>
 __host__ __device__ constexpr int stencil_points() { return DIM == 3 ? 27 : 9; }
 
-__device__ __forceinline__ double block_sum(double v, double* sw) {
+// Block sum: products and the warp shuffle tree in the working precision T (FP64 work is 58x
+// slower than FP32 on this part), the eight warp partials in FP64.
+template <typename T>
+__device__ __forceinline__ double block_sum(T v, double* sw) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) sw[warp] = v;
+    if (lane == 0) sw[warp] = (double)v;
     __syncthreads();
     double t = 0.0;
     if (threadIdx.x == 0)
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sw[w];
     return t;  // valid in thread 0
+}
+
+// ratio of two device scalars, formed once per block (one FP64 division per block, not per thread)
+template <typename T>
+__device__ __forceinline__ T block_ratio(const double* num, const double* den, T* slot) {
+    if (threadIdx.x == 0) *slot = (T)(*num / *den);
+    __syncthreads();
+    return *slot;
 }
 
 // A[q][e] = sum over the nodes n shared by e and f = e + off(q), and the free components d of n,
@@ -122,36 +133,40 @@ __global__ void k_gwg_convert(int64_t n, const S* __restrict__ a, D* __restrict_
     if (i < n) b[i] = (D)a[i];
 }
 
-// q = A p ; scal[0] += p.q ; clears the accumulators that the update kernel fills
+// q = A p ; scal[0] += p.q ; clears the accumulators that the update kernel fills.
+// Entries towards neighbours outside the mesh are stored as 0, so the neighbour index is clamped
+// to the element itself and every load is unconditional (all 2 x 27 loads can be in flight).
+// Index math is 32-bit (the host checks 27 ne < 2^31).
 template <int DIM, typename T>
-__global__ void k_gwg_spmv(EGrid g, const T* __restrict__ A, const T* __restrict__ p, T* __restrict__ q,
-                           double* __restrict__ scal, int parity) {
+__global__ void __launch_bounds__(256) k_gwg_spmv(EGrid g, const T* __restrict__ A, const T* __restrict__ p,
+                                                  T* __restrict__ q, double* __restrict__ scal, int parity) {
     constexpr int NB = stencil_points<DIM>();
     __shared__ double sw[32];
-    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    double local = 0.0;
-    if (e < g.ne) {
-        const int64_t ix = e % g.ex, iy = (e / g.ex) % g.ey, iz = DIM == 3 ? e / (g.ex * g.ey) : 0;
-        const bool okx[3] = {ix > 0, true, ix + 1 < g.ex};
-        const bool oky[3] = {iy > 0, true, iy + 1 < g.ey};
-        const bool okz[3] = {DIM == 3 && iz > 0, true, DIM == 3 && iz + 1 < g.ez};
+    const int ne = (int)g.ne, ex = (int)g.ex, ey = (int)g.ey, ez = (int)g.ez;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    T local = (T)0;
+    if (e < ne) {
+        const int exy = ex * ey;
+        const int ix = e % ex, iy = (e / ex) % ey, iz = DIM == 3 ? e / exy : 0;
+        const int dx[3] = {ix > 0 ? -1 : 0, 0, ix + 1 < ex ? 1 : 0};
+        const int dy[3] = {iy > 0 ? -ex : 0, 0, iy + 1 < ey ? ex : 0};
+        const int dz[3] = {DIM == 3 && iz > 0 ? -exy : 0, 0, DIM == 3 && iz + 1 < ez ? exy : 0};
+        T a[NB], x[NB];
+#pragma unroll
+        for (int k = 0; k < NB; ++k) a[k] = __ldg(A + (size_t)k * ne + e);
+#pragma unroll
+        for (int k = 0; k < NB; ++k) x[k] = __ldg(p + e + dx[k % 3] + dy[(k / 3) % 3] + dz[DIM == 3 ? k / 9 : 1]);
         T acc = (T)0;
 #pragma unroll
-        for (int k = 0; k < NB; ++k) {
-            const int ox = k % 3, oy = (k / 3) % 3, oz = DIM == 3 ? k / 9 : 1;
-            if (okx[ox] && oky[oy] && okz[oz]) {
-                int64_t f = e + (ox - 1) + g.ex * ((oy - 1) + g.ey * (oz - 1));
-                acc = fma(A[(int64_t)k * g.ne + e], p[f], acc);
-            }
-        }
+        for (int k = 0; k < NB; ++k) acc = fma(a[k], x[k], acc);
         q[e] = acc;
-        local = (double)acc * (double)p[e];
+        local = acc * x[NB / 2];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         scal[1 + (parity ^ 1)] = 0.0;
         scal[3] = 0.0;
     }
-    double t = block_sum(local, sw);
+    double t = block_sum<T>(local, sw);
     if (threadIdx.x == 0) atomicAdd(&scal[0], t);
 }
 
@@ -161,21 +176,22 @@ __global__ void k_gwg_update(int64_t ne, const T* __restrict__ p, const T* __res
                              const T* __restrict__ dinv, T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
                              double* __restrict__ scal, int parity) {
     __shared__ double sw[32];
-    T alpha = (T)(scal[1 + parity] / scal[0]);
+    __shared__ T s_alpha;
+    const T alpha = block_ratio<T>(&scal[1 + parity], &scal[0], &s_alpha);
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    double rz = 0.0, rr = 0.0;
+    T rz = (T)0, rr = (T)0;
     if (e < ne) {
         x[e] = fma(alpha, p[e], x[e]);
         T re = fma(-alpha, q[e], r[e]);
         r[e] = re;
         T ze = re * dinv[e];
         z[e] = ze;
-        rz = (double)re * (double)ze;
-        rr = (double)re * (double)re;
+        rz = re * ze;
+        rr = re * re;
     }
-    double t1 = block_sum(rz, sw);
+    double t1 = block_sum<T>(rz, sw);
     __syncthreads();
-    double t2 = block_sum(rr, sw);
+    double t2 = block_sum<T>(rr, sw);
     if (threadIdx.x == 0) {
         atomicAdd(&scal[1 + (parity ^ 1)], t1);
         atomicAdd(&scal[3], t2);
@@ -186,7 +202,8 @@ __global__ void k_gwg_update(int64_t ne, const T* __restrict__ p, const T* __res
 template <typename T>
 __global__ void k_gwg_dir(int64_t ne, const T* __restrict__ z, T* __restrict__ p, double* __restrict__ scal,
                           int parity) {
-    T beta = (T)(scal[1 + (parity ^ 1)] / scal[1 + parity]);
+    __shared__ T s_beta;
+    const T beta = block_ratio<T>(&scal[1 + (parity ^ 1)], &scal[1 + parity], &s_beta);
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e < ne) p[e] = fma(beta, p[e], z[e]);
     if (blockIdx.x == 0 && threadIdx.x == 0) scal[0] = 0.0;
@@ -198,7 +215,7 @@ __global__ void k_gwg_init(int64_t ne, const double* __restrict__ b, const T* __
                            T* __restrict__ r, T* __restrict__ z, T* __restrict__ p, double* __restrict__ scal) {
     __shared__ double sw[32];
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    double rz = 0.0, rr = 0.0;
+    T rz = (T)0, rr = (T)0;
     if (e < ne) {
         T re = (T)b[e];
         T ze = re * dinv[e];
@@ -206,12 +223,12 @@ __global__ void k_gwg_init(int64_t ne, const double* __restrict__ b, const T* __
         r[e] = re;
         z[e] = ze;
         p[e] = ze;
-        rz = (double)re * (double)ze;
-        rr = (double)re * (double)re;
+        rz = re * ze;
+        rr = re * re;
     }
-    double t1 = block_sum(rz, sw);
+    double t1 = block_sum<T>(rz, sw);
     __syncthreads();
-    double t2 = block_sum(rr, sw);
+    double t2 = block_sum<T>(rr, sw);
     if (threadIdx.x == 0) {
         atomicAdd(&scal[1], t1);
         atomicAdd(&scal[3], t2);
@@ -236,6 +253,8 @@ void gwg_stencil_build(Context& c, const double* W, double* A, double* dinv) {
     const Level& L = c.levels[0];
     const MeshDesc& m = L.mesh;
     EGrid g = egrid_of(m);
+    UWG_REQUIRE(g.ne * (m.dim == 3 ? 27 : 9) < (int64_t)1 << 31, UWGPU_ERR_TOO_LARGE,
+                "BFBt stencil: element count too large for 32-bit stencil indexing");
     int off[3];
     const double* h = fine_widths(c, off);
     {

@@ -170,27 +170,36 @@ __global__ void k_convert(int64_t n, const S* __restrict__ a, D* __restrict__ b)
 // ------------------------------------------------------------------------------------------
 // Apply and smoothing.
 // ------------------------------------------------------------------------------------------
-// y_n = sum_q A_q x_{n+off(q)} for one node (T = storage/arithmetic type).
-template <int DIM, typename T>
-__device__ __forceinline__ void stencil_row(const Grid& g, int64_t n, int64_t i, int64_t j, int64_t k,
-                                            const T* __restrict__ A, const T* __restrict__ x, T out[DIM]) {
-    constexpr int NB = nblocks<DIM>();
-#pragma unroll
-    for (int r = 0; r < DIM; ++r) out[r] = (T)0;
-#pragma unroll
-    for (int q = 0; q < NB; ++q) {
-        int dx = q % 3 - 1, dy = (q / 3) % 3 - 1, dz = DIM == 3 ? q / 9 - 1 : 0;
-        int64_t ii = i + dx, jj = j + dy, kk = k + dz;
-        if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || (DIM == 3 && (kk < 0 || kk >= g.nz))) continue;
-        int64_t m = n + dx + g.nx * (dy + g.ny * dz);
-        T xm[DIM];
-#pragma unroll
-        for (int cc = 0; cc < DIM; ++cc) xm[cc] = x[(int64_t)cc * g.nn + m];
-#pragma unroll
-        for (int r = 0; r < DIM; ++r)
-#pragma unroll
-            for (int cc = 0; cc < DIM; ++cc) out[r] = fma(A[((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n], xm[cc], out[r]);
-    }
+// Neighbour offsets of node (i, j, k) per axis, 0 towards a missing neighbour.  Every stencil block
+// towards a neighbour outside the mesh is stored as zero, so a row reads the node itself there
+// and all loads of a row are unconditional (they can all be in flight at once).
+struct NbrOffsets {
+    int64_t dx[3], dy[3], dz[3];
+};
+
+template <int DIM>
+__device__ __forceinline__ NbrOffsets nbr_offsets(const Grid& g, int64_t i, int64_t j, int64_t k) {
+    NbrOffsets o;
+    o.dx[0] = i > 0 ? -1 : 0;
+    o.dx[1] = 0;
+    o.dx[2] = i + 1 < g.nx ? 1 : 0;
+    o.dy[0] = j > 0 ? -g.nx : 0;
+    o.dy[1] = 0;
+    o.dy[2] = j + 1 < g.ny ? g.nx : 0;
+    o.dz[0] = DIM == 3 && k > 0 ? -g.nx * g.ny : 0;
+    o.dz[1] = 0;
+    o.dz[2] = DIM == 3 && k + 1 < g.nz ? g.nx * g.ny : 0;
+    return o;
+}
+
+// (i, j, k) of node n with 32-bit division (node counts stay below 2^32, checked on the host)
+template <int DIM>
+__device__ __forceinline__ void node_ijk(const Grid& g, int64_t n, int64_t& i, int64_t& j, int64_t& k) {
+    const unsigned un = (unsigned)n, nx = (unsigned)g.nx, ny = (unsigned)g.ny;
+    const unsigned q = un / nx;
+    i = un - q * nx;
+    j = DIM == 3 ? q % ny : q;
+    k = DIM == 3 ? q / ny : 0;
 }
 
 // Row-split layout: a block of kRowThreads threads covers kRowThreads/DIM nodes; warp w works on
@@ -203,16 +212,14 @@ template <int DIM, typename T>
 __device__ __forceinline__ T stencil_row_r(const Grid& g, int64_t n, int64_t i, int64_t j, int64_t k, int r,
                                            const T* __restrict__ A, const T* __restrict__ x) {
     constexpr int NB = nblocks<DIM>();
+    const NbrOffsets o = nbr_offsets<DIM>(g, i, j, k);
     T out = (T)0;
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
-        int dx = q % 3 - 1, dy = (q / 3) % 3 - 1, dz = DIM == 3 ? q / 9 - 1 : 0;
-        int64_t ii = i + dx, jj = j + dy, kk = k + dz;
-        if (ii < 0 || ii >= g.nx || jj < 0 || jj >= g.ny || (DIM == 3 && (kk < 0 || kk >= g.nz))) continue;
-        int64_t m = n + dx + g.nx * (dy + g.ny * dz);
+        int64_t m = n + o.dx[q % 3] + o.dy[(q / 3) % 3] + o.dz[DIM == 3 ? q / 9 : 1];
 #pragma unroll
         for (int cc = 0; cc < DIM; ++cc)
-            out = fma(A[((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n], x[(int64_t)cc * g.nn + m], out);
+            out = fma(__ldg(A + ((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n), x[(int64_t)cc * g.nn + m], out);
     }
     return out;
 }
@@ -225,7 +232,8 @@ __global__ void __launch_bounds__(kRowThreads) k_apply(Grid g, const T* __restri
     int r = warp % DIM, grp = warp / DIM;
     int64_t n = (int64_t)blockIdx.x * (kRowThreads / DIM) + grp * 32 + lane;
     if (n >= g.nn) return;
-    int64_t i = n % g.nx, j = (n / g.nx) % g.ny, k = DIM == 3 ? n / (g.nx * g.ny) : 0;
+    int64_t i, j, k;
+    node_ijk<DIM>(g, n, i, j, k);
     T v = stencil_row_r<DIM, T>(g, n, i, j, k, r, A, x);
     y[(int64_t)r * g.nn + n] = b ? b[(int64_t)r * g.nn + n] - v : v;
 }
@@ -301,7 +309,8 @@ __global__ void __launch_bounds__(kRowThreads) k_cheb_step(Grid g, const T* __re
     bool act = n < g.nn;
     T res = (T)0;
     if (act) {
-        int64_t i = n % g.nx, j = (n / g.nx) % g.ny, k = DIM == 3 ? n / (g.nx * g.ny) : 0;
+        int64_t i, j, k;
+        node_ijk<DIM>(g, n, i, j, k);
         res = b[(int64_t)r * g.nn + n];
         if (xin) res -= stencil_row_r<DIM, T>(g, n, i, j, k, r, A, xin);
     }
@@ -590,6 +599,7 @@ void build_operator(Context& c, int levels, bool need32) {
     UWG_REQUIRE(c.assembled, UWGPU_ERR_STATE, "operator requested before assembly");
     const MeshDesc& m = c.mesh;
     int dim = m.dim;
+    UWG_REQUIRE(m.nn < ((int64_t)1 << 32), UWGPU_ERR_TOO_LARGE, "node count beyond 32-bit node indexing");
     // the number of levels the mesh admits (each coarsening halves every axis)
     int maxlev = 1;
     {

@@ -105,28 +105,30 @@ __global__ void k_cast_add(int64_t n, const S* __restrict__ a, D* __restrict__ b
     if (i < n) b[i] += (D)a[i];
 }
 
-// partial[j*G + block] = sum_i V[j*ldv + i] * w[i] for j < m (FP64 accumulation)
+// partial[j*G + block] = sum_i V[j*ldv + i] * w[i] for j < m.  Each thread's few products and
+// the warp tree are in the vectors' precision T (FP64 arithmetic is 58x slower than FP32 on this
+// part, so FP32 Krylov vectors are not widened element by element); warp partials onward in FP64.
 template <typename T, int CH>
 __global__ void __launch_bounds__(kRedThreads) k_multidot(int64_t n, const T* __restrict__ V, int64_t ldv, int m,
                                                           const T* __restrict__ w, double* __restrict__ partial) {
     __shared__ double sred[kRedThreads / 32][CH];
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int j0 = 0; j0 < m; j0 += CH) {
-        double acc[CH];
+        T acc[CH];
 #pragma unroll
-        for (int q = 0; q < CH; ++q) acc[q] = 0.0;
+        for (int q = 0; q < CH; ++q) acc[q] = (T)0;
         for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-            double wi = (double)w[i];
+            T wi = w[i];
 #pragma unroll
             for (int q = 0; q < CH; ++q)
-                if (j0 + q < m) acc[q] = fma((double)V[(int64_t)(j0 + q) * ldv + i], wi, acc[q]);
+                if (j0 + q < m) acc[q] = fma(V[(int64_t)(j0 + q) * ldv + i], wi, acc[q]);
         }
 #pragma unroll
         for (int q = 0; q < CH; ++q) {
-            double v = acc[q];
+            T v = acc[q];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0) sred[warp][q] = v;
+            if (lane == 0) sred[warp][q] = (double)v;
         }
         __syncthreads();
         if (threadIdx.x < CH && j0 + (int)threadIdx.x < m) {
@@ -155,26 +157,41 @@ __global__ void k_reduce_partials(int m, int nb, const double* __restrict__ part
     }
 }
 
-// w -= sum_j h[j] V_j   (h on the device)
+// w += sign * sum_j h[j] V_j  (h on the device).  The coefficients are converted to T once per
+// block in shared memory; the per-element arithmetic is in T.  (Block size >= 64.)
 template <typename T>
 __global__ void k_multi_axpy(int64_t n, const T* __restrict__ V, int64_t ldv, int m, const double* __restrict__ h,
                              T* __restrict__ w, double sign) {
+    __shared__ T sh[64];
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double acc = (double)w[i];
-    for (int j = 0; j < m; ++j) acc = fma(sign * h[j], (double)V[(int64_t)j * ldv + i], acc);
-    w[i] = (T)acc;
+    T acc = i < n ? w[i] : (T)0;
+    for (int j0 = 0; j0 < m; j0 += 64) {
+        __syncthreads();
+        if (threadIdx.x < 64 && j0 + (int)threadIdx.x < m) sh[threadIdx.x] = (T)(sign * h[j0 + threadIdx.x]);
+        __syncthreads();
+        int jn = m - j0 < 64 ? m - j0 : 64;
+        if (i < n)
+            for (int j = 0; j < jn; ++j) acc = fma(sh[j], V[(int64_t)(j0 + j) * ldv + i], acc);
+    }
+    if (i < n) w[i] = acc;
 }
 
-// x += sum_j y[j] Z_j  (y on the device)
-template <typename T, typename X>
+// x += sum_j y[j] Z_j  (y on the device), coefficients staged as in k_multi_axpy
+template <typename T>
 __global__ void k_combine(int64_t n, const T* __restrict__ Z, int64_t ldz, int m, const double* __restrict__ y,
-                          X* __restrict__ x) {
+                          T* __restrict__ x) {
+    __shared__ T sy[64];
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double acc = (double)x[i];
-    for (int j = 0; j < m; ++j) acc = fma(y[j], (double)Z[(int64_t)j * ldz + i], acc);
-    x[i] = (X)acc;
+    T acc = i < n ? x[i] : (T)0;
+    for (int j0 = 0; j0 < m; j0 += 64) {
+        __syncthreads();
+        if (threadIdx.x < 64 && j0 + (int)threadIdx.x < m) sy[threadIdx.x] = (T)y[j0 + threadIdx.x];
+        __syncthreads();
+        int jn = m - j0 < 64 ? m - j0 : 64;
+        if (i < n)
+            for (int j = 0; j < jn; ++j) acc = fma(sy[j], Z[(int64_t)(j0 + j) * ldz + i], acc);
+    }
+    if (i < n) x[i] = acc;
 }
 
 // deterministic oscillatory start vector for the power iteration (hash of the index)
@@ -194,8 +211,11 @@ __global__ void k_parity_fill(int64_t ex, int64_t ey, int64_t ne, double* __rest
 }
 
 __global__ void k_remove_mean(int64_t n, const double* __restrict__ sum, double* __restrict__ x) {
+    __shared__ double mean;
+    if (threadIdx.x == 0) mean = sum[0] / (double)n;   // one division per block
+    __syncthreads();
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) x[i] -= sum[0] / (double)n;
+    if (i < n) x[i] -= mean;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -392,7 +412,7 @@ struct Fgmres {
             UWG_CUDA(cudaMemcpyAsync(dvec.p, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, c.stream));
             {
                 LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
-                k_combine<T, T><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, Z.p, n, k, dvec.p, x);
+                k_combine<T><<<blocks_for(n, 256), 256, 0, c.stream>>>(n, Z.p, n, k, dvec.p, x);
             }
             beta = std::fabs(g[k]);
             if (done || its >= maxit) break;
