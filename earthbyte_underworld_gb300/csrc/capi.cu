@@ -3,6 +3,7 @@
 #include <cstring>
 
 #include "internal.cuh"
+#include "unet.cuh"
 
 using uwg::Context;
 using uwg::Error;
@@ -493,6 +494,79 @@ int uwgpu_get_stream(uwgpu_ctx* ctx, void** stream) {
     return guarded(ctx, [&](Context& c) {
         UWG_REQUIRE(stream, UWGPU_ERR_ARGUMENT, "null output");
         *stream = (void*)c.stream;
+    });
+}
+
+// ---- learned velocity preconditioner ----
+static uwg::unet::Net& net_of(Context& c) {
+    UWG_REQUIRE(c.net != nullptr, UWGPU_ERR_STATE, "no learned preconditioner: call uwgpu_learned_create");
+    return *c.net;
+}
+
+int uwgpu_learned_create(uwgpu_ctx* ctx, int32_t levels, int32_t base_channels, uint64_t seed) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(c.has_mesh, UWGPU_ERR_STATE, "learned preconditioner requested before the mesh");
+        auto* n = new uwg::unet::Net();
+        try {
+            uwg::unet::create(c, *n, levels, base_channels, seed);
+        } catch (...) {
+            delete n;
+            throw;
+        }
+        uwg::unet::destroy(c.net);
+        c.net = n;
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int uwgpu_learned_param_count(uwgpu_ctx* ctx, int64_t* count) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(count, UWGPU_ERR_ARGUMENT, "null count");
+        *count = net_of(c).nparams;
+    });
+}
+
+int uwgpu_learned_get_params(uwgpu_ctx* ctx, float* params) {
+    return guarded(ctx, [&](Context& c) {
+        auto& n = net_of(c);
+        UWG_REQUIRE(params, UWGPU_ERR_ARGUMENT, "null params");
+        UWG_CUDA(cudaMemcpyAsync(params, n.params.p, (size_t)n.nparams * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int uwgpu_learned_set_params(uwgpu_ctx* ctx, const float* params) {
+    return guarded(ctx, [&](Context& c) {
+        auto& n = net_of(c);
+        UWG_REQUIRE(params, UWGPU_ERR_ARGUMENT, "null params");
+        UWG_CUDA(cudaMemcpyAsync(n.params.p, params, (size_t)n.nparams * sizeof(float), cudaMemcpyHostToDevice, c.stream));
+        uwg::unet::pack(c, n);
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int uwgpu_learned_forward(uwgpu_ctx* ctx, const float* input, float* output) {
+    return guarded(ctx, [&](Context& c) {
+        auto& n = net_of(c);
+        UWG_REQUIRE(input && output, UWGPU_ERR_ARGUMENT, "null input or output");
+        uwg::unet::set_input_host(c, n, input);
+        uwg::unet::forward(c, n);
+        uwg::unet::get_output_host(c, n, output);
+    });
+}
+
+int uwgpu_learned_backward(uwgpu_ctx* ctx, const float* grad_output, float* grad_params, float* grad_input) {
+    return guarded(ctx, [&](Context& c) {
+        auto& n = net_of(c);
+        UWG_REQUIRE(grad_output, UWGPU_ERR_ARGUMENT, "null grad_output");
+        uwg::unet::set_grad_output_host(c, n, grad_output);
+        UWG_CUDA(cudaMemsetAsync(n.grads.p, 0, (size_t)n.nparams * sizeof(float), c.stream));
+        uwg::unet::backward(c, n);
+        if (grad_params)
+            UWG_CUDA(cudaMemcpyAsync(grad_params, n.grads.p, (size_t)n.nparams * sizeof(float), cudaMemcpyDeviceToHost,
+                                     c.stream));
+        if (grad_input) uwg::unet::get_input_grad_host(c, n, grad_input);
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
     });
 }
 

@@ -14,6 +14,11 @@
 
 namespace uwg {
 
+namespace unet {
+struct Net;
+void destroy(Net* n);
+}
+
 // Error carried from the internals to the C entry points, which turn it into a status code.
 struct Error : std::runtime_error {
     int code;
@@ -178,7 +183,12 @@ struct Context {
         cudaGraphExec_t exec = nullptr;
     };
     std::vector<PcgGraph> pcg_graphs;
+
+    // learned velocity preconditioner (csrc/unet.cu), created on request
+    unet::Net* net = nullptr;
+
     ~Context() {
+        unet::destroy(net);
         for (auto& g : pcg_graphs)
             if (g.exec) cudaGraphExecDestroy(g.exec);
     }

@@ -1,0 +1,693 @@
+// Learned velocity preconditioner: a 3D U-Net on the nodal grid (BF16 weights and activations,
+// FP32 accumulation and gradients), with its own forward, backward and Adam kernels.
+//
+// Input channels per node: the three components of the residual (scaled to unit RMS) and
+// log10 of the node-averaged viscosity; output: a three-component velocity correction.  The node
+// grid (nel+1 per axis) is zero-padded to a multiple of 2^(levels-1).  Level l has base * 2^l
+// channels; each level is two 3x3x3 convolutions with ReLU, levels are joined by 2x2x2 average
+// pooling on the way down and nearest upsampling + concatenation with the skip on the way up, and
+// a 1x1x1 convolution maps the finest decoder output to the three velocity components.
+//
+// Layout: channels-last (voxel-major, channel fastest) so that one 16-byte load brings eight BF16
+// channels of a voxel.  Weights of a 3x3x3 layer are W[tap][cin][cout]; the data-gradient pass
+// runs the forward kernel on W'[tap][cout][cin] = W[26 - tap][cin][cout].
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+#include "unet.cuh"
+
+namespace uwg {
+namespace unet {
+
+typedef __nv_bfloat16 bf16;
+
+// ------------------------------------------------------------------------------------------
+// Kernels
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void load8(const bf16* p, float v[8]) {
+    uint4 raw = *reinterpret_cast<const uint4*>(p);
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&raw);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float2 f = __bfloat1622float2(h[k]);
+        v[2 * k] = f.x;
+        v[2 * k + 1] = f.y;
+    }
+}
+__device__ __forceinline__ void load8(const float* p, float v[8]) {
+    float4 a = *reinterpret_cast<const float4*>(p);
+    float4 b = *reinterpret_cast<const float4*>(p + 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void store8(bf16* p, const float v[8]) {
+    uint4 raw;
+    __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&raw);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) h[k] = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+    *reinterpret_cast<uint4*>(p) = raw;
+}
+__device__ __forceinline__ void store8(float* p, const float v[8]) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    *reinterpret_cast<float4*>(p + 4) = make_float4(v[4], v[5], v[6], v[7]);
+}
+
+// 3x3x3 convolution, zero padding, eight output channels per thread (one voxel per thread):
+//   out[v][co] = act(bias[co] + sum_{t, ci} W[t][ci][co] in[v + off(t)][ci])
+// The block's slice W[.][.][co0 .. co0+8) is staged in shared memory (BF16).
+// cin and cout are multiples of 8.
+template <typename TI, typename TO>
+__global__ void __launch_bounds__(128) k_conv3(Vol g, int cin, int cout, const TI* __restrict__ in,
+                                               const bf16* __restrict__ W, const float* __restrict__ bias,
+                                               TO* __restrict__ out, int relu) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bf16* sw = reinterpret_cast<bf16*>(smem_raw);   // [27][cin][8]
+    const int co0 = blockIdx.y * 8;
+    for (int idx = threadIdx.x; idx < 27 * cin; idx += blockDim.x)
+        *reinterpret_cast<uint4*>(sw + (size_t)idx * 8) = *reinterpret_cast<const uint4*>(W + (size_t)idx * cout + co0);
+    __syncthreads();
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= g.nv) return;
+    const int x = (int)(v % g.px), y = (int)((v / g.px) % g.py), z = (int)(v / ((int64_t)g.px * g.py));
+    float acc[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[k] = bias ? bias[co0 + k] : 0.0f;
+    for (int t = 0; t < 27; ++t) {
+        const int xx = x + t % 3 - 1, yy = y + (t / 3) % 3 - 1, zz = z + t / 9 - 1;
+        if (xx < 0 || xx >= g.px || yy < 0 || yy >= g.py || zz < 0 || zz >= g.pz) continue;
+        const TI* row = in + ((int64_t)xx + (int64_t)g.px * (yy + (int64_t)g.py * zz)) * cin;
+        const bf16* wt = sw + (size_t)t * cin * 8;
+        for (int c8 = 0; c8 < cin; c8 += 8) {
+            float xv[8];
+            load8(row + c8, xv);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                float wv[8];
+                load8(wt + (size_t)(c8 + c) * 8, wv);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) acc[k] = fmaf(xv[c], wv[k], acc[k]);
+            }
+        }
+    }
+    if (relu) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) acc[k] = fmaxf(acc[k], 0.0f);
+    }
+    store8(out + v * cout + co0, acc);
+}
+
+// dW[t][ci][co] += sum_v in[v + off(t)][ci] g[v][co]  (in: BF16 activations, g: FP32 gradient of
+// the pre-activation).  grid = (voxel slices, 27 taps); each block accumulates its slice in
+// registers (output o = threadIdx.x + 256 k) and adds it to dW once.
+constexpr int kWgThreads = 256;
+constexpr int kWgMaxPer = 64;   // cin * cout <= 256 * 64
+constexpr int kWgTile = 32;     // voxels staged per round
+__global__ void __launch_bounds__(kWgThreads) k_conv3_wgrad(Vol g, int cin, int cout, int taps,
+                                                            const bf16* __restrict__ in,
+                                                            const float* __restrict__ gout, float* __restrict__ dW,
+                                                            int64_t vslice) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sx = reinterpret_cast<float*>(smem_raw);   // [kWgTile][cin]
+    float* sg = sx + kWgTile * cin;                    // [kWgTile][cout]
+    const int t = blockIdx.y;
+    const int dx = taps == 27 ? t % 3 - 1 : 0, dy = taps == 27 ? (t / 3) % 3 - 1 : 0, dz = taps == 27 ? t / 9 - 1 : 0;
+    const int nout = cin * cout;
+    float acc[kWgMaxPer];
+#pragma unroll
+    for (int k = 0; k < kWgMaxPer; ++k) acc[k] = 0.0f;
+    const int64_t v0 = (int64_t)blockIdx.x * vslice;
+    const int64_t v1 = v0 + vslice < g.nv ? v0 + vslice : g.nv;
+    for (int64_t vb = v0; vb < v1; vb += kWgTile) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < kWgTile * cin; idx += blockDim.x) {
+            const int vt = idx / cin, c = idx % cin;
+            const int64_t v = vb + vt;
+            float val = 0.0f;
+            if (v < v1) {
+                const int x = (int)(v % g.px) + dx, y = (int)((v / g.px) % g.py) + dy,
+                          z = (int)(v / ((int64_t)g.px * g.py)) + dz;
+                if (x >= 0 && x < g.px && y >= 0 && y < g.py && z >= 0 && z < g.pz)
+                    val = __bfloat162float(in[((int64_t)x + (int64_t)g.px * (y + (int64_t)g.py * z)) * cin + c]);
+            }
+            sx[idx] = val;
+        }
+        for (int idx = threadIdx.x; idx < kWgTile * cout; idx += blockDim.x) {
+            const int vt = idx / cout, c = idx % cout;
+            const int64_t v = vb + vt;
+            sg[idx] = v < v1 ? gout[v * cout + c] : 0.0f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kWgMaxPer; ++k) {
+            const int o = threadIdx.x + k * kWgThreads;
+            if (o < nout) {
+                const int ci = o / cout, co = o % cout;
+                float a = acc[k];
+#pragma unroll 8
+                for (int vt = 0; vt < kWgTile; ++vt) a = fmaf(sx[vt * cin + ci], sg[vt * cout + co], a);
+                acc[k] = a;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kWgMaxPer; ++k) {
+        const int o = threadIdx.x + k * kWgThreads;
+        if (o < nout) atomicAdd(&dW[(int64_t)t * nout + o], acc[k]);
+    }
+}
+
+// db[co] += sum_v g[v][co]
+__global__ void k_bias_grad(int64_t nv, int cout, const float* __restrict__ gout, float* __restrict__ db) {
+    // thread t covers channel t % cout of voxels (t / cout) + k * (threads / cout) of the block's slice
+    const int lanes = blockDim.x / cout;
+    const int co = threadIdx.x % cout, sub = threadIdx.x / cout;
+    if (sub >= lanes) return;
+    float a = 0.0f;
+    for (int64_t v = (int64_t)blockIdx.x * lanes + sub; v < nv; v += (int64_t)gridDim.x * lanes) a += gout[v * cout + co];
+    atomicAdd(&db[co], a);
+}
+
+// g = g * (y > 0): gradient through ReLU, y the stored BF16 output of the layer
+__global__ void k_relu_bwd(int64_t n, const bf16* __restrict__ y, float* __restrict__ g) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && !(__bfloat162float(y[i]) > 0.0f)) g[i] = 0.0f;
+}
+
+// 2x2x2 average pooling (fine -> coarse), BF16
+__global__ void k_pool(Vol f, Vol c, int ch, const bf16* __restrict__ in, bf16* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.nv * ch) return;
+    const int64_t V = i / ch;
+    const int cc = (int)(i % ch);
+    const int X = (int)(V % c.px), Y = (int)((V / c.px) % c.py), Z = (int)(V / ((int64_t)c.px * c.py));
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int x = 2 * X + (k & 1), y = 2 * Y + ((k >> 1) & 1), z = 2 * Z + (k >> 2);
+        s += __bfloat162float(in[((int64_t)x + (int64_t)f.px * (y + (int64_t)f.py * z)) * ch + cc]);
+    }
+    out[i] = __float2bfloat16_rn(0.125f * s);
+}
+
+// gradient of the pooling, added: gf[v][c] += gc[parent(v)][c] / 8
+__global__ void k_pool_bwd_add(Vol f, Vol c, int ch, const float* __restrict__ gc, float* __restrict__ gf) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= f.nv * ch) return;
+    const int64_t v = i / ch;
+    const int cc = (int)(i % ch);
+    const int x = (int)(v % f.px), y = (int)((v / f.px) % f.py), z = (int)(v / ((int64_t)f.px * f.py));
+    const int64_t V = (x / 2) + (int64_t)c.px * ((y / 2) + (int64_t)c.py * (z / 2));
+    gf[i] += 0.125f * gc[V * ch + cc];
+}
+
+// decoder input: out[v] = [ up(coarse)[v] (cu channels) | skip[v] (cs channels) ]
+__global__ void k_up_concat(Vol f, Vol c, int cu, int cs, const bf16* __restrict__ coarse,
+                            const bf16* __restrict__ skip, bf16* __restrict__ out) {
+    const int ct = cu + cs;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= f.nv * ct) return;
+    const int64_t v = i / ct;
+    const int cc = (int)(i % ct);
+    if (cc < cu) {
+        const int x = (int)(v % f.px), y = (int)((v / f.px) % f.py), z = (int)(v / ((int64_t)f.px * f.py));
+        const int64_t V = (x / 2) + (int64_t)c.px * ((y / 2) + (int64_t)c.py * (z / 2));
+        out[i] = coarse[V * cu + cc];
+    } else {
+        out[i] = skip[v * cs + (cc - cu)];
+    }
+}
+
+// gradient of k_up_concat: gc[V][c] = sum over the 8 children of g[v][c] (c < cu);
+// gskip[v][c] += g[v][cu + c]
+__global__ void k_up_concat_bwd_coarse(Vol f, Vol c, int cu, int cs, const float* __restrict__ g,
+                                       float* __restrict__ gc) {
+    const int ct = cu + cs;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.nv * cu) return;
+    const int64_t V = i / cu;
+    const int cc = (int)(i % cu);
+    const int X = (int)(V % c.px), Y = (int)((V / c.px) % c.py), Z = (int)(V / ((int64_t)c.px * c.py));
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int x = 2 * X + (k & 1), y = 2 * Y + ((k >> 1) & 1), z = 2 * Z + (k >> 2);
+        s += g[((int64_t)x + (int64_t)f.px * (y + (int64_t)f.py * z)) * ct + cc];
+    }
+    gc[i] = s;
+}
+__global__ void k_up_concat_bwd_skip(Vol f, int cu, int cs, const float* __restrict__ g, float* __restrict__ gs) {
+    const int ct = cu + cs;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= f.nv * cs) return;
+    const int64_t v = i / cs;
+    const int cc = (int)(i % cs);
+    gs[i] += g[v * ct + cu + cc];
+}
+
+// head: out[d][v] = b[d] + sum_c W[c][d] x[v][c]   (d < 3, out SoA FP32)
+__global__ void k_head(int64_t nv, int cin, const bf16* __restrict__ x, const float* __restrict__ W,
+                       const float* __restrict__ b, float* __restrict__ out) {
+    int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    float a0 = b[0], a1 = b[1], a2 = b[2];
+    for (int c8 = 0; c8 < cin; c8 += 8) {
+        float xv[8];
+        load8(x + v * cin + c8, xv);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const float* w = W + (c8 + c) * 3;
+            a0 = fmaf(xv[c], w[0], a0);
+            a1 = fmaf(xv[c], w[1], a1);
+            a2 = fmaf(xv[c], w[2], a2);
+        }
+    }
+    out[v] = a0;
+    out[nv + v] = a1;
+    out[2 * nv + v] = a2;
+}
+
+// head backward: gx[v][c] = sum_d W[c][d] g[d][v]; dW[c][d] += sum_v x[v][c] g[d][v]; db[d] += sum_v g[d][v]
+// (warp sums first, then one shared-memory add per warp, then one global add per block)
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__global__ void k_head_bwd(int64_t nv, int cin, const bf16* __restrict__ x, const float* __restrict__ W,
+                           const float* __restrict__ g, float* __restrict__ gx, float* __restrict__ dW,
+                           float* __restrict__ db) {
+    extern __shared__ float sacc[];   // [cin * 3 + 3]
+    for (int k = threadIdx.x; k < cin * 3 + 3; k += blockDim.x) sacc[k] = 0.0f;
+    __syncthreads();
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = v < nv;
+    const float g0 = act ? g[v] : 0.0f, g1 = act ? g[nv + v] : 0.0f, g2 = act ? g[2 * nv + v] : 0.0f;
+    const bool lead = (threadIdx.x & 31) == 0;
+    for (int c = 0; c < cin; ++c) {
+        const float* w = W + c * 3;
+        const float xv = act ? __bfloat162float(x[v * cin + c]) : 0.0f;
+        if (act) gx[v * cin + c] = w[0] * g0 + w[1] * g1 + w[2] * g2;
+        const float s0 = warp_sum(xv * g0), s1 = warp_sum(xv * g1), s2 = warp_sum(xv * g2);
+        if (lead) {
+            atomicAdd(&sacc[c * 3 + 0], s0);
+            atomicAdd(&sacc[c * 3 + 1], s1);
+            atomicAdd(&sacc[c * 3 + 2], s2);
+        }
+    }
+    const float t0 = warp_sum(g0), t1 = warp_sum(g1), t2 = warp_sum(g2);
+    if (lead) {
+        atomicAdd(&sacc[cin * 3 + 0], t0);
+        atomicAdd(&sacc[cin * 3 + 1], t1);
+        atomicAdd(&sacc[cin * 3 + 2], t2);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < cin * 3; k += blockDim.x) atomicAdd(&dW[k], sacc[k]);
+    for (int k = threadIdx.x; k < 3; k += blockDim.x) atomicAdd(&db[k], sacc[cin * 3 + k]);
+}
+
+// FP32 master weights -> BF16 W[t][ci][co] and the flipped transpose W'[t][co][ci] = W[26-t][ci][co]
+__global__ void k_pack(int taps, int cin, int cout, const float* __restrict__ w, bf16* __restrict__ w16,
+                       bf16* __restrict__ wflip) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)taps * cin * cout;
+    if (i >= n) return;
+    const int t = (int)(i / ((int64_t)cin * cout));
+    const int rem = (int)(i % ((int64_t)cin * cout));
+    const int ci = rem / cout, co = rem % cout;
+    const bf16 b = __float2bfloat16_rn(w[i]);
+    w16[i] = b;
+    if (wflip) wflip[((int64_t)(taps - 1 - t) * cout + co) * cin + ci] = b;
+}
+
+// Adam (Kingma & Ba 2015) with bias correction; bc1 = 1 - beta1^t, bc2 = 1 - beta2^t
+__global__ void k_adam(int64_t n, float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, float lr, float b1, float b2, float eps, float bc1, float bc2,
+                       float gscale) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i] * gscale;
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+}
+
+// ------------------------------------------------------------------------------------------
+// Host side
+// ------------------------------------------------------------------------------------------
+static unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+static size_t conv_smem(int cin) { return (size_t)27 * cin * 8 * sizeof(bf16); }
+static size_t wgrad_smem(int cin, int cout) { return (size_t)kWgTile * (cin + cout) * sizeof(float); }
+
+template <typename TI, typename TO>
+static void conv_launch(Context& c, const Vol& g, int cin, int cout, const TI* in, const bf16* W, const float* bias,
+                        TO* out, bool relu) {
+    const size_t smem = conv_smem(cin);
+    static bool attr_set = false;   // per instantiation; the attribute is per device function
+    if (!attr_set) {
+        UWG_CUDA(cudaFuncSetAttribute(k_conv3<TI, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        attr_set = true;
+    }
+    UWG_REQUIRE(smem <= 200 * 1024, UWGPU_ERR_ARGUMENT, "U-Net layer too wide for the convolution kernel");
+    dim3 grid(nblk(g.nv, 128), cout / 8);
+    LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+    k_conv3<TI, TO><<<grid, 128, smem, c.stream>>>(g, cin, cout, in, W, bias, out, relu ? 1 : 0);
+    note_work(c, UWGPU_KERNEL_LEARNED, (double)g.nv * (cin * sizeof(TI) + cout * sizeof(TO)),
+              2.0 * 27.0 * cin * cout * (double)g.nv);
+}
+
+static void wgrad_launch(Context& c, const Vol& g, int cin, int cout, const bf16* in, const float* gout, float* dW) {
+    UWG_REQUIRE((int64_t)cin * cout <= (int64_t)kWgThreads * kWgMaxPer, UWGPU_ERR_ARGUMENT,
+                "U-Net layer too wide for the weight-gradient kernel");
+    static bool attr_set = false;
+    if (!attr_set) {
+        UWG_CUDA(cudaFuncSetAttribute(k_conv3_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+        attr_set = true;
+    }
+    const int slices = 16;
+    const int64_t vslice = (g.nv + slices - 1) / slices;
+    LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+    k_conv3_wgrad<<<dim3(slices, 27), kWgThreads, wgrad_smem(cin, cout), c.stream>>>(g, cin, cout, 27, in, gout, dW,
+                                                                                     vslice);
+    note_work(c, UWGPU_KERNEL_LEARNED, (double)g.nv * 27.0 * (cin * 2 + cout * 4), 2.0 * 27.0 * cin * cout * (double)g.nv);
+}
+
+static void bias_grad_launch(Context& c, int64_t nv, int cout, const float* gout, float* db) {
+    LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+    k_bias_grad<<<152, (256 / cout) * cout, 0, c.stream>>>(nv, cout, gout, db);
+}
+
+static void relu_bwd(Context& c, int64_t n, const bf16* y, float* g) {
+    LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+    k_relu_bwd<<<nblk(n, 256), 256, 0, c.stream>>>(n, y, g);
+}
+
+// splitmix64 (Steele, Lea and Flood 2014) for reproducible initial weights
+static uint64_t splitmix(uint64_t& s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+void destroy(Net* n) { delete n; }
+
+void create(Context& c, Net& n, int levels, int base, uint64_t seed) {
+    const MeshDesc& m = c.mesh;
+    UWG_REQUIRE(m.dim == 3, UWGPU_ERR_UNSUPPORTED, "the learned preconditioner is built for 3D meshes");
+    UWG_REQUIRE(levels >= 1 && levels <= kMaxLevels, UWGPU_ERR_ARGUMENT, "U-Net levels must be 1..6");
+    UWG_REQUIRE(base >= 8 && base % 8 == 0 && (base << (levels - 1)) <= 256, UWGPU_ERR_ARGUMENT,
+                "U-Net base channels must be a multiple of 8, at most 256 at the coarsest level");
+    n.levels = levels;
+    n.base = base;
+    n.nnx = m.nnx;
+    n.nny = m.nny;
+    n.nnz = m.nnz;
+    n.nn = m.nn;
+    const int64_t mult = (int64_t)1 << (levels - 1);
+    Vol v0;
+    v0.px = (int)((m.nnx + mult - 1) / mult * mult);
+    v0.py = (int)((m.nny + mult - 1) / mult * mult);
+    v0.pz = (int)((m.nnz + mult - 1) / mult * mult);
+    for (int l = 0; l < levels; ++l) {
+        Vol v;
+        v.px = v0.px >> l;
+        v.py = v0.py >> l;
+        v.pz = v0.pz >> l;
+        v.nv = (int64_t)v.px * v.py * v.pz;
+        n.vol[l] = v;
+        n.ch[l] = base << l;
+    }
+    // layers and parameter offsets
+    {
+        std::vector<Conv> fresh((size_t)(2 * levels + 2 * (levels - 1)));   // Conv owns device arrays: no copies
+        n.convs.swap(fresh);
+    }
+    int64_t off = 0;
+    auto add = [&](Conv& cv, int cin, int cout) {
+        cv.cin = cin;
+        cv.cout = cout;
+        cv.w_off = off;
+        off += (int64_t)27 * cin * cout;
+        cv.b_off = off;
+        off += cout;
+    };
+    for (int l = 0; l < levels; ++l) {
+        add(n.convs[n.enc(l, 0)], n.cin_of_level(l), n.ch[l]);
+        add(n.convs[n.enc(l, 1)], n.ch[l], n.ch[l]);
+    }
+    for (int l = 0; l + 1 < levels; ++l) {
+        add(n.convs[n.dec(l, 0)], n.ch[l + 1] + n.ch[l], n.ch[l]);
+        add(n.convs[n.dec(l, 1)], n.ch[l], n.ch[l]);
+    }
+    n.head_w = off;
+    off += (int64_t)n.ch[0] * 3;
+    n.head_b = off;
+    off += 3;
+    n.nparams = off;
+    // He-uniform initial weights, zero biases, zero head (the untrained net adds nothing)
+    std::vector<float> h((size_t)n.nparams, 0.0f);
+    uint64_t s = seed;
+    for (auto& cv : n.convs) {
+        const float a = std::sqrt(6.0f / (27.0f * cv.cin));
+        for (int64_t i = 0; i < (int64_t)27 * cv.cin * cv.cout; ++i) {
+            const double u = (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0);
+            h[(size_t)(cv.w_off + i)] = (float)((2.0 * u - 1.0) * a);
+        }
+    }
+    for (auto* a : {&n.params, &n.grads, &n.adam_m, &n.adam_v}) a->ensure((size_t)n.nparams);
+    UWG_CUDA(cudaMemcpy(n.params.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+    UWG_CUDA(cudaMemset(n.grads.p, 0, h.size() * sizeof(float)));
+    UWG_CUDA(cudaMemset(n.adam_m.p, 0, h.size() * sizeof(float)));
+    UWG_CUDA(cudaMemset(n.adam_v.p, 0, h.size() * sizeof(float)));
+    n.adam_t = 0;
+    n.out_scale = 1.0f;
+    // activations and gradients
+    const Vol& f = n.vol[0];
+    n.x0.ensure((size_t)f.nv * kInChannels);
+    UWG_CUDA(cudaMemset(n.x0.p, 0, (size_t)f.nv * kInChannels * sizeof(bf16)));
+    n.out.ensure((size_t)f.nv * 3);
+    n.gout.ensure((size_t)f.nv * 3);
+    for (int l = 0; l < levels; ++l) {
+        const int64_t nv = n.vol[l].nv;
+        const int C = n.ch[l];
+        n.enc_a[l].ensure((size_t)nv * C);
+        n.enc_b[l].ensure((size_t)nv * C);
+        n.g_enc_a[l].ensure((size_t)nv * C);
+        n.g_enc_b[l].ensure((size_t)nv * C);
+        n.g_in[l].ensure((size_t)nv * n.cin_of_level(l));
+        if (l + 1 < levels) {
+            n.pool[l].ensure((size_t)n.vol[l + 1].nv * C);
+            const int ct = n.ch[l + 1] + C;
+            n.dec_cat[l].ensure((size_t)nv * ct);
+            n.dec_a[l].ensure((size_t)nv * C);
+            n.dec_b[l].ensure((size_t)nv * C);
+            n.g_cat[l].ensure((size_t)nv * ct);
+            n.g_dec_a[l].ensure((size_t)nv * C);
+            n.g_dec_b[l].ensure((size_t)nv * C);
+        }
+    }
+    for (auto& cv : n.convs) {
+        cv.w16.ensure((size_t)27 * cv.cin * cv.cout);
+        cv.wflip.ensure((size_t)27 * cv.cin * cv.cout);
+    }
+    pack(c, n);
+}
+
+void pack(Context& c, Net& n) {
+    for (auto& cv : n.convs) {
+        const int64_t nw = (int64_t)27 * cv.cin * cv.cout;
+        LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+        k_pack<<<nblk(nw, 256), 256, 0, c.stream>>>(27, cv.cin, cv.cout, n.params.p + cv.w_off, cv.w16.p, cv.wflip.p);
+    }
+    check_launch("k_pack");
+}
+
+void forward(Context& c, Net& n) {
+    const int L = n.levels;
+    for (int l = 0; l < L; ++l) {
+        const Vol& g = n.vol[l];
+        const Conv& a = n.convs[n.enc(l, 0)];
+        const Conv& b = n.convs[n.enc(l, 1)];
+        const bf16* in = l == 0 ? n.x0.p : n.pool[l - 1].p;
+        conv_launch<bf16, bf16>(c, g, a.cin, a.cout, in, a.w16.p, n.params.p + a.b_off, n.enc_a[l].p, true);
+        conv_launch<bf16, bf16>(c, g, b.cin, b.cout, n.enc_a[l].p, b.w16.p, n.params.p + b.b_off, n.enc_b[l].p, true);
+        if (l + 1 < L) {
+            const int64_t cnt = n.vol[l + 1].nv * n.ch[l];
+            LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+            k_pool<<<nblk(cnt, 256), 256, 0, c.stream>>>(g, n.vol[l + 1], n.ch[l], n.enc_b[l].p, n.pool[l].p);
+        }
+    }
+    for (int l = L - 2; l >= 0; --l) {
+        const Vol& g = n.vol[l];
+        const int cu = n.ch[l + 1], cs = n.ch[l];
+        const bf16* coarse = l == L - 2 ? n.enc_b[L - 1].p : n.dec_b[l + 1].p;
+        {
+            const int64_t cnt = g.nv * (cu + cs);
+            LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+            k_up_concat<<<nblk(cnt, 256), 256, 0, c.stream>>>(g, n.vol[l + 1], cu, cs, coarse, n.enc_b[l].p,
+                                                              n.dec_cat[l].p);
+        }
+        const Conv& a = n.convs[n.dec(l, 0)];
+        const Conv& b = n.convs[n.dec(l, 1)];
+        conv_launch<bf16, bf16>(c, g, a.cin, a.cout, n.dec_cat[l].p, a.w16.p, n.params.p + a.b_off, n.dec_a[l].p, true);
+        conv_launch<bf16, bf16>(c, g, b.cin, b.cout, n.dec_a[l].p, b.w16.p, n.params.p + b.b_off, n.dec_b[l].p, true);
+    }
+    const bf16* fin = L == 1 ? n.enc_b[0].p : n.dec_b[0].p;
+    {
+        LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+        k_head<<<nblk(n.vol[0].nv, 256), 256, 0, c.stream>>>(n.vol[0].nv, n.ch[0], fin, n.params.p + n.head_w,
+                                                              n.params.p + n.head_b, n.out.p);
+    }
+    check_launch("unet forward");
+}
+
+// gradient of one conv layer: g (pre-activation gradient, FP32, [nv][cout]) -> dW, db, and the
+// gradient of its input (post-activation of the layer below) into gin
+static void conv_backward(Context& c, Net& n, const Vol& g, const Conv& cv, const bf16* in, const float* gpre,
+                          float* gin) {
+    wgrad_launch(c, g, cv.cin, cv.cout, in, gpre, n.grads.p + cv.w_off);
+    bias_grad_launch(c, g.nv, cv.cout, gpre, n.grads.p + cv.b_off);
+    conv_launch<float, float>(c, g, cv.cout, cv.cin, gpre, cv.wflip.p, nullptr, gin, false);
+}
+
+void backward(Context& c, Net& n) {
+    const int L = n.levels;
+    const Vol& f = n.vol[0];
+    const bf16* fin = L == 1 ? n.enc_b[0].p : n.dec_b[0].p;
+    float* gfin = L == 1 ? n.g_enc_b[0].p : n.g_dec_b[0].p;
+    {
+        LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+        k_head_bwd<<<nblk(f.nv, 256), 256, (size_t)(n.ch[0] * 3 + 3) * sizeof(float), c.stream>>>(
+            f.nv, n.ch[0], fin, n.params.p + n.head_w, n.gout.p, gfin, n.grads.p + n.head_w, n.grads.p + n.head_b);
+    }
+    // skip gradients start at zero; the decoder adds into them
+    for (int l = 0; l + 1 < L; ++l)
+        UWG_CUDA(cudaMemsetAsync(n.g_enc_b[l].p, 0, (size_t)n.vol[l].nv * n.ch[l] * sizeof(float), c.stream));
+    for (int l = 0; l + 1 < L; ++l) {
+        const Vol& g = n.vol[l];
+        const int cu = n.ch[l + 1], cs = n.ch[l];
+        relu_bwd(c, g.nv * cs, n.dec_b[l].p, n.g_dec_b[l].p);
+        conv_backward(c, n, g, n.convs[n.dec(l, 1)], n.dec_a[l].p, n.g_dec_b[l].p, n.g_dec_a[l].p);
+        relu_bwd(c, g.nv * cs, n.dec_a[l].p, n.g_dec_a[l].p);
+        conv_backward(c, n, g, n.convs[n.dec(l, 0)], n.dec_cat[l].p, n.g_dec_a[l].p, n.g_cat[l].p);
+        float* gcoarse = l + 1 == L - 1 ? n.g_enc_b[L - 1].p : n.g_dec_b[l + 1].p;
+        {
+            LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+            k_up_concat_bwd_coarse<<<nblk(n.vol[l + 1].nv * cu, 256), 256, 0, c.stream>>>(g, n.vol[l + 1], cu, cs,
+                                                                                           n.g_cat[l].p, gcoarse);
+        }
+        {
+            LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+            k_up_concat_bwd_skip<<<nblk(g.nv * cs, 256), 256, 0, c.stream>>>(g, cu, cs, n.g_cat[l].p, n.g_enc_b[l].p);
+        }
+    }
+    for (int l = L - 1; l >= 0; --l) {
+        const Vol& g = n.vol[l];
+        const int C = n.ch[l];
+        if (l + 1 < L) {
+            LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+            k_pool_bwd_add<<<nblk(g.nv * C, 256), 256, 0, c.stream>>>(g, n.vol[l + 1], C, n.g_in[l + 1].p,
+                                                                      n.g_enc_b[l].p);
+        }
+        relu_bwd(c, g.nv * C, n.enc_b[l].p, n.g_enc_b[l].p);
+        conv_backward(c, n, g, n.convs[n.enc(l, 1)], n.enc_a[l].p, n.g_enc_b[l].p, n.g_enc_a[l].p);
+        relu_bwd(c, g.nv * C, n.enc_a[l].p, n.g_enc_a[l].p);
+        const bf16* in = l == 0 ? n.x0.p : n.pool[l - 1].p;
+        conv_backward(c, n, g, n.convs[n.enc(l, 0)], in, n.g_enc_a[l].p, n.g_in[l].p);
+    }
+    check_launch("unet backward");
+}
+
+// node (i, j, k) of the mesh sits at voxel (i, j, k) of the padded level-0 grid
+__global__ void k_input_from_host_layout(int64_t nnx, int64_t nny, int64_t nn, Vol g, const float* __restrict__ in4,
+                                         bf16* __restrict__ x0) {
+    int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nn) return;
+    const int64_t i = node % nnx, j = (node / nnx) % nny, k = node / (nnx * nny);
+    const int64_t v = i + (int64_t)g.px * (j + (int64_t)g.py * k);
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) x0[v * kInChannels + ch] = __float2bfloat16_rn(in4[(int64_t)ch * nn + node]);
+}
+
+__global__ void k_output_to_node_layout(int64_t nnx, int64_t nny, int64_t nn, Vol g, const float* __restrict__ out,
+                                        float* __restrict__ o3) {
+    int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nn) return;
+    const int64_t i = node % nnx, j = (node / nnx) % nny, k = node / (nnx * nny);
+    const int64_t v = i + (int64_t)g.px * (j + (int64_t)g.py * k);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) o3[(int64_t)d * nn + node] = out[(int64_t)d * g.nv + v];
+}
+
+void set_input_host(Context& c, Net& n, const float* input) {
+    DArray<float> tmp;
+    tmp.ensure((size_t)n.nn * 4);
+    UWG_CUDA(cudaMemcpyAsync(tmp.p, input, (size_t)n.nn * 4 * sizeof(float), cudaMemcpyHostToDevice, c.stream));
+    UWG_CUDA(cudaMemsetAsync(n.x0.p, 0, (size_t)n.vol[0].nv * kInChannels * sizeof(bf16), c.stream));
+    LaunchScope ls(c, -1);
+    k_input_from_host_layout<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], tmp.p, n.x0.p);
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+void get_output_host(Context& c, Net& n, float* output) {
+    DArray<float> tmp;
+    tmp.ensure((size_t)n.nn * 3);
+    {
+        LaunchScope ls(c, -1);
+        k_output_to_node_layout<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], n.out.p, tmp.p);
+    }
+    UWG_CUDA(cudaMemcpyAsync(output, tmp.p, (size_t)n.nn * 3 * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+__global__ void k_grad_from_node_layout(int64_t nnx, int64_t nny, int64_t nn, Vol g, const float* __restrict__ g3,
+                                        float* __restrict__ gout) {
+    int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nn) return;
+    const int64_t i = node % nnx, j = (node / nnx) % nny, k = node / (nnx * nny);
+    const int64_t v = i + (int64_t)g.px * (j + (int64_t)g.py * k);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) gout[(int64_t)d * g.nv + v] = g3[(int64_t)d * nn + node];
+}
+
+__global__ void k_input_grad_to_node_layout(int64_t nnx, int64_t nny, int64_t nn, Vol g, const float* __restrict__ gin,
+                                            float* __restrict__ g4) {
+    int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nn) return;
+    const int64_t i = node % nnx, j = (node / nnx) % nny, k = node / (nnx * nny);
+    const int64_t v = i + (int64_t)g.px * (j + (int64_t)g.py * k);
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) g4[(int64_t)ch * nn + node] = gin[v * kInChannels + ch];
+}
+
+void set_grad_output_host(Context& c, Net& n, const float* grad) {
+    DArray<float> tmp;
+    tmp.ensure((size_t)n.nn * 3);
+    UWG_CUDA(cudaMemcpyAsync(tmp.p, grad, (size_t)n.nn * 3 * sizeof(float), cudaMemcpyHostToDevice, c.stream));
+    UWG_CUDA(cudaMemsetAsync(n.gout.p, 0, (size_t)n.vol[0].nv * 3 * sizeof(float), c.stream));
+    LaunchScope ls(c, -1);
+    k_grad_from_node_layout<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], tmp.p, n.gout.p);
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+void get_input_grad_host(Context& c, Net& n, float* grad_input) {
+    DArray<float> tmp;
+    tmp.ensure((size_t)n.nn * 4);
+    {
+        LaunchScope ls(c, -1);
+        k_input_grad_to_node_layout<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], n.g_in[0].p,
+                                                                            tmp.p);
+    }
+    UWG_CUDA(cudaMemcpyAsync(grad_input, tmp.p, (size_t)n.nn * 4 * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+}  // namespace unet
+}  // namespace uwg

@@ -37,7 +37,8 @@ SCHUR_PC_SCALED_BFBT = 3
 SMOOTHER_COLOUR_GS = 0
 SMOOTHER_CHEBYSHEV = 1
 
-KERNEL_ASSEMBLY, KERNEL_APPLY, KERNEL_SMOOTH, KERNEL_BINNING, KERNEL_SCHUR_PC, KERNEL_VECTOR, KERNEL_TRANSFER = range(7)
+KERNEL_ASSEMBLY, KERNEL_APPLY, KERNEL_SMOOTH, KERNEL_BINNING, KERNEL_SCHUR_PC, KERNEL_VECTOR, KERNEL_TRANSFER, \
+    KERNEL_LEARNED = range(8)
 
 
 class UwgpuError(RuntimeError):
@@ -121,6 +122,12 @@ def load(build_if_missing: bool = True):
         L.uwgpu_time_smooth.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, P]
         L.uwgpu_launch_count.argtypes = [P]
         L.uwgpu_launch_count.restype = C.c_int64
+        L.uwgpu_learned_create.argtypes = [P, C.c_int32, C.c_int32, C.c_uint64]
+        L.uwgpu_learned_param_count.argtypes = [P, P]
+        L.uwgpu_learned_get_params.argtypes = [P, P]
+        L.uwgpu_learned_set_params.argtypes = [P, P]
+        L.uwgpu_learned_forward.argtypes = [P, P, P]
+        L.uwgpu_learned_backward.argtypes = [P, P, P, P]
         _lib = L
         return _lib
 
@@ -327,6 +334,40 @@ class Context:
 
     def launch_count(self):
         return int(self._L.uwgpu_launch_count(self._h))
+
+    # ---- learned velocity preconditioner ----
+    def learned_create(self, levels=3, base=8, seed=1):
+        self._check(self._L.uwgpu_learned_create(self._h, levels, base, seed))
+
+    def learned_param_count(self):
+        n = C.c_int64()
+        self._check(self._L.uwgpu_learned_param_count(self._h, C.byref(n)))
+        return n.value
+
+    def learned_params(self):
+        p = np.zeros(self.learned_param_count(), np.float32)
+        self._check(self._L.uwgpu_learned_get_params(self._h, _ptr(p)))
+        return p
+
+    def learned_set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        assert p.size == self.learned_param_count()
+        self._check(self._L.uwgpu_learned_set_params(self._h, _ptr(p)))
+
+    def learned_forward(self, inp):
+        """inp: (4, nn) float32 (residual components, log10 viscosity) -> (3, nn) float32"""
+        x = np.ascontiguousarray(inp, dtype=np.float32).reshape(4, self.nnodes)
+        out = np.zeros((3, self.nnodes), np.float32)
+        self._check(self._L.uwgpu_learned_forward(self._h, _ptr(x), _ptr(out)))
+        return out
+
+    def learned_backward(self, grad_out):
+        """after learned_forward: gradient of the output (3, nn) -> (parameter gradient, input gradient (4, nn))"""
+        g = np.ascontiguousarray(grad_out, dtype=np.float32).reshape(3, self.nnodes)
+        gp = np.zeros(self.learned_param_count(), np.float32)
+        gi = np.zeros((4, self.nnodes), np.float32)
+        self._check(self._L.uwgpu_learned_backward(self._h, _ptr(g), _ptr(gp), _ptr(gi)))
+        return gp, gi
 
 
 def free_slip_mask(dim, nel):

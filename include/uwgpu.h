@@ -228,7 +228,8 @@ void uwgpu_solve_opts_default(uwgpu_solve_opts* opts);
 enum { UWGPU_KERNEL_ASSEMBLY = 0, UWGPU_KERNEL_APPLY = 1, UWGPU_KERNEL_SMOOTH = 2,
        UWGPU_KERNEL_BINNING = 3, UWGPU_KERNEL_SCHUR_PC = 4 /* scaled-BFBt inner solves */,
        UWGPU_KERNEL_VECTOR = 5 /* Krylov vector work, reductions, G and G^T */,
-       UWGPU_KERNEL_TRANSFER = 6 /* restriction, prolongation, coarsest solve */, UWGPU_KERNEL_COUNT = 7 };
+       UWGPU_KERNEL_TRANSFER = 6 /* restriction, prolongation, coarsest solve */,
+       UWGPU_KERNEL_LEARNED = 7 /* U-Net preconditioner: forward, backward, Adam */, UWGPU_KERNEL_COUNT = 8 };
 int uwgpu_profile_enable(uwgpu_ctx* ctx, int32_t on);
 int uwgpu_profile_read(uwgpu_ctx* ctx, int32_t which, int64_t* launches, double* ms);
 /* Algorithmic work of the profiled launches of family `which`: bytes the kernels must move
@@ -267,6 +268,26 @@ int uwgpu_time_smooth(uwgpu_ctx* ctx, int32_t precision, int32_t sweeps, int32_t
 int uwgpu_bin_and_map_noalloc(int32_t dim, const int32_t nel[3], const double min[3], const double max[3],
                               int64_t n, const double* x, const double* y, const double* z, uint32_t* perm,
                               uint32_t* offsets, double* xi, void* stream, uint32_t* outside);
+
+/* ---- Learned velocity preconditioner ------------------------------------------------------
+ * A 3D U-Net (BF16 weights and activations, FP32 accumulation) that maps the velocity residual
+ * and log10 viscosity on the node grid to a velocity correction.  It has no counterpart in the
+ * reference: it augments the multigrid preconditioner of the velocity solve (BSSCR/mg.c:42-132,
+ * PCMG) inside the flexible Krylov iteration, with plain multigrid as its fallback.  3D only. */
+
+/* Builds the network for the context's mesh: `levels` resolution levels (1..6), `base_channels`
+ * channels at the finest level (multiple of 8), doubling per level; weights from `seed`. */
+int uwgpu_learned_create(uwgpu_ctx* ctx, int32_t levels, int32_t base_channels, uint64_t seed);
+int uwgpu_learned_param_count(uwgpu_ctx* ctx, int64_t* count);
+/* Parameters (FP32 master copy, layout: per 3x3x3 layer W[27][cin][cout] then bias[cout], encoder
+ * layers by level, then decoder layers by level, then the 1x1x1 head W[cin][3], bias[3]). */
+int uwgpu_learned_get_params(uwgpu_ctx* ctx, float* params);
+int uwgpu_learned_set_params(uwgpu_ctx* ctx, const float* params);
+/* Test hooks: one forward pass on host input[4][nn] (channels: three residual components,
+ * log10 viscosity; node order of the mesh) -> output[3][nn]; then the backward pass of
+ * grad_output[3][nn] -> grad_params[param_count] (overwritten) and grad_input[4][nn]. */
+int uwgpu_learned_forward(uwgpu_ctx* ctx, const float* input, float* output);
+int uwgpu_learned_backward(uwgpu_ctx* ctx, const float* grad_output, float* grad_params, float* grad_input);
 
 #ifdef __cplusplus
 }
