@@ -334,6 +334,8 @@ void uwgpu_solve_opts_default(uwgpu_solve_opts* o) {
     o->bfbt_rtol = 1e-2;
     o->bfbt_max_it = 500;
     o->smoother = UWGPU_SMOOTHER_COLOUR_GS;
+    o->learned_pc = 0;
+    o->learned_stagnation = 2;
 }
 
 int uwgpu_solve_bsscr(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, double* u, double* p, uwgpu_report* report) {
@@ -567,6 +569,20 @@ int uwgpu_learned_backward(uwgpu_ctx* ctx, const float* grad_output, float* grad
                                      c.stream));
         if (grad_input) uwg::unet::get_input_grad_host(c, n, grad_input);
         UWG_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int uwgpu_learned_generate(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, int32_t nsamples, uint64_t seed) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(opts, UWGPU_ERR_ARGUMENT, "null options");
+        uwg::learned_generate(c, *opts, nsamples, seed);
+    });
+}
+
+int uwgpu_learned_train(uwgpu_ctx* ctx, int32_t epochs, int32_t batch, float learning_rate, uint64_t seed,
+                        double* train_loss, double* holdout_ratio) {
+    return guarded(ctx, [&](Context& c) {
+        uwg::unet::train(c, net_of(c), epochs, batch, learning_rate, seed, train_loss, holdout_ratio);
     });
 }
 

@@ -16,6 +16,7 @@
 #include <cstring>
 
 #include "internal.cuh"
+#include "unet.cuh"
 
 namespace uwg {
 
@@ -312,10 +313,14 @@ struct Fgmres {
         y.assign(m, 0.0);
         hcol.assign(m + 1, 0.0);
     }
+    // residual estimate after each iteration of the current solve (read by adaptive preconditioners)
+    std::vector<double> hist;
+
     // A(x, y): y = A x ; M(v, z): z = M^{-1} v.  Returns iterations; *res = final ||r||.
     template <typename Aop, typename Mop>
     int solve(Aop&& A, Mop&& M, const T* b, T* x, double rtol, int maxit, double* res_out, double* bnorm_out,
               bool* nan_out) {
+        hist.clear();
         zero<T>(c, n, x);
         double bnorm = red.norm<T>(n, b);
         if (bnorm_out) *bnorm_out = bnorm;
@@ -391,6 +396,7 @@ struct Fgmres {
                 g[k + 1] = -sn[k] * g[k];
                 g[k] = cs[k] * g[k];
                 its++;
+                hist.push_back(std::fabs(g[k + 1]));
                 if (!std::isfinite(g[k + 1])) {
                     if (nan_out) *nan_out = true;
                     done = true;
@@ -451,6 +457,47 @@ struct Bsscr {
 
     Bsscr(Context& ctx, const uwgpu_solve_opts& opts, uwgpu_report& r)
         : c(ctx), o(opts), rep(r), red(ctx), gm64(ctx, red), gm32(ctx, red), gms(ctx, red) {}
+
+    // velocity hierarchy: operator, levels, Chebyshev bounds
+    void setup_velocity() {
+        dim = c.mesh.dim;
+        int levels = o.mg_levels < 1 ? 1 : o.mg_levels;
+        mixed = o.precision == UWGPU_PREC_MIXED;
+        if (!c.operator_built || c.operator_levels != levels || (mixed && !c.operator_has32))
+            build_operator(c, levels, mixed);
+        nlev = c.nlevels;
+        nv = c.mesh.nn * dim;
+        if (o.smoother == UWGPU_SMOOTHER_CHEBYSHEV) estimate_lmax();
+    }
+
+    // ---- learned correction of the V-cycle (unet.cu): M(r) = V(r) + N(r) ----
+    // Active while the velocity FGMRES makes progress; after `learned_stagnation` consecutive
+    // iterations that reduce the residual estimate by less than 5%, the rest of that velocity
+    // solve uses the plain V-cycle (the multigrid fallback).
+    bool learned = false;      // requested and a network exists
+    bool learned_on = false;   // within the current velocity solve
+    template <typename T>
+    void learned_check(const std::vector<double>& hist) {
+        if (!learned_on) return;
+        const int need = o.learned_stagnation > 0 ? o.learned_stagnation : 2;
+        if ((int)hist.size() < need + 1) return;
+        for (int q = 0; q < need; ++q) {
+            const size_t i = hist.size() - 1 - q;
+            if (!(hist[i] > 0.95 * hist[i - 1])) return;
+        }
+        learned_on = false;
+        rep.learned_fallbacks++;
+    }
+    template <typename T>
+    void precondition(const T* in, T* out, const std::vector<double>& hist) {
+        vcycle<T>(0, in, out);
+        rep.vcycles++;
+        learned_check<T>(hist);
+        if (learned_on) {
+            unet::correct<T>(c, *c.net, in, out);
+            rep.learned_applies++;
+        }
+    }
 
     // ---- multigrid V-cycle (zero initial guess), precision T ----
     template <typename T>
@@ -521,11 +568,9 @@ struct Bsscr {
         if (!mixed) {
             double res = 0.0, bn = 0.0;
             bool nn = false;
+            learned_on = learned;
             its = gm64.solve([&](const double* in, double* out) { level_apply<double>(c, L0, in, out); },
-                             [&](const double* in, double* out) {
-                                 vcycle<double>(0, in, out);
-                                 rep.vcycles++;
-                             },
+                             [&](const double* in, double* out) { precondition<double>(in, out, gm64.hist); },
                              b, x, rtol, maxit, &res, &bn, &nn);
             if (nn) nan = true;
             if (!(res <= rtol * bn * 1.0000001) && bn > 0) inner_fail = true;
@@ -538,6 +583,7 @@ struct Bsscr {
             copy<double>(c, nv, b, ref_r.p);
             double rn = bn;
             int guard = 0;
+            learned_on = learned;
             while (rn > rtol * bn && its < maxit && guard < 50) {
                 guard++;
                 cast<double, float>(c, nv, ref_r.p, r32.p);
@@ -545,10 +591,7 @@ struct Bsscr {
                 bool nn = false;
                 double inner_rtol = std::max(rtol * bn / rn, 1e-4);
                 int k = gm32.solve([&](const float* in, float* out) { level_apply<float>(c, L0, in, out); },
-                                   [&](const float* in, float* out) {
-                                       vcycle<float>(0, in, out);
-                                       rep.vcycles++;
-                                   },
+                                   [&](const float* in, float* out) { precondition<float>(in, out, gm32.hist); },
                                    r32.p, d32.p, std::min(inner_rtol, 0.5), maxit - its, &res, &b32n, &nn);
                 its += k;
                 if (nn) { nan = true; break; }
@@ -828,14 +871,13 @@ void Bsscr::project_nullspace(double* x) {
 
 void Bsscr::run() {
     auto t0 = std::chrono::steady_clock::now();
-    dim = c.mesh.dim;
-    int levels = o.mg_levels < 1 ? 1 : o.mg_levels;
-    mixed = o.precision == UWGPU_PREC_MIXED;
-    if (!c.operator_built || c.operator_levels != levels || (mixed && !c.operator_has32))
-        build_operator(c, levels, mixed);
-    nlev = c.nlevels;
-    nv = c.mesh.nn * dim;
-    if (o.smoother == UWGPU_SMOOTHER_CHEBYSHEV) estimate_lmax();
+    setup_velocity();
+    if (o.learned_pc) {
+        UWG_REQUIRE(c.net != nullptr, UWGPU_ERR_STATE, "learned_pc requested but no network (uwgpu_learned_create)");
+        UWG_REQUIRE(c.net->nn == c.mesh.nn, UWGPU_ERR_STATE, "the network was built for another mesh");
+        unet::prepare_viscosity(c, *c.net);
+        learned = true;
+    }
     npres = c.mesh.ne;
     int restart = o.restart > 0 ? o.restart : 30;
     gm64.setup(nv, restart);
@@ -973,8 +1015,42 @@ void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
     UWG_REQUIRE(o.schur_pc >= 0 && o.schur_pc <= 3, UWGPU_ERR_ARGUMENT, "bad Schur preconditioner");
     UWG_REQUIRE(o.smoother == UWGPU_SMOOTHER_COLOUR_GS || o.smoother == UWGPU_SMOOTHER_CHEBYSHEV, UWGPU_ERR_ARGUMENT, "bad smoother");
     UWG_REQUIRE(o.remove_const_p >= 0 && o.remove_const_p <= 2, UWGPU_ERR_ARGUMENT, "bad pressure null-space mode");
+    UWG_REQUIRE(o.learned_pc == 0 || o.learned_pc == 1, UWGPU_ERR_ARGUMENT, "bad learned_pc");
     Bsscr s(c, o, rep);
     s.run();
+}
+
+// Training pairs for the learned correction, produced by the multigrid solver of the assembled
+// system: a random multi-scale velocity field e (zero on Dirichlet dofs), its residual r = K e
+// (the residual of the zero guess, so e is exactly the error), and one V-cycle v = V(r) of the
+// solver's own hierarchy; the network learns the error the V-cycle leaves, e - V(r), from r and
+// the viscosity.  Returns the number of samples added.
+int learned_generate(Context& c, const uwgpu_solve_opts& o, int nsamples, uint64_t seed) {
+    UWG_REQUIRE(c.assembled, UWGPU_ERR_STATE, "training data requested before assembly");
+    UWG_REQUIRE(c.net != nullptr, UWGPU_ERR_STATE, "no network (uwgpu_learned_create)");
+    UWG_REQUIRE(c.net->nn == c.mesh.nn, UWGPU_ERR_STATE, "the network was built for another mesh");
+    UWG_REQUIRE(nsamples > 0, UWGPU_ERR_ARGUMENT, "nsamples must be positive");
+    uwgpu_report rep;
+    std::memset(&rep, 0, sizeof(rep));
+    uwgpu_solve_opts o64 = o;
+    o64.precision = UWGPU_PREC_FP64;
+    Bsscr s(c, o64, rep);
+    s.setup_velocity();
+    unet::Net& n = *c.net;
+    const int64_t nv = c.mesh.nn * 3;
+    DArray<double> e, r, v;
+    e.ensure(nv);
+    r.ensure(nv);
+    v.ensure(nv);
+    unet::dataset_reserve(c, n, nsamples);
+    for (int k = 0; k < nsamples; ++k) {
+        unet::random_field(c, n, seed + (uint64_t)k, e.p);
+        level_apply<double>(c, c.levels[0], e.p, r.p);
+        s.vcycle<double>(0, r.p, v.p);
+        unet::dataset_add(c, n, r.p, e.p, v.p);
+    }
+    unet::dataset_finish(c, n);
+    return n.nsamples;
 }
 
 }  // namespace uwg

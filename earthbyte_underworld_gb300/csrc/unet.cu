@@ -13,6 +13,7 @@
 // runs the forward kernel on W'[tap][cout][cin] = W[26 - tap][cin][cout].
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -687,6 +688,339 @@ void get_input_grad_host(Context& c, Net& n, float* grad_input) {
     }
     UWG_CUDA(cudaMemcpyAsync(grad_input, tmp.p, (size_t)n.nn * 4 * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
     UWG_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+// ------------------------------------------------------------------------------------------
+// The network as a preconditioner: residual -> input tensor, output -> velocity correction
+// ------------------------------------------------------------------------------------------
+template <typename T>
+__global__ void k_sumsq(int64_t n, const T* __restrict__ x, double* __restrict__ out) {
+    float s = 0.0f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v = (float)x[i];
+        s = fmaf(v, v, s);
+    }
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, (double)s);
+}
+
+// node (i, j, k) of the mesh is voxel (i, j, k) of the padded level-0 grid
+__device__ __forceinline__ int64_t node_voxel(int64_t node, int64_t nnx, int64_t nny, const Vol& g) {
+    const int64_t i = node % nnx, j = (node / nnx) % nny, k = node / (nnx * nny);
+    return i + (int64_t)g.px * (j + (int64_t)g.py * k);
+}
+
+// x0[v] = (r[.][node] / rms(r), log10 viscosity, 0, 0, 0, 0)
+template <typename T>
+__global__ void k_make_input(int64_t nnx, int64_t nny, int64_t nn, Vol g, const T* __restrict__ r,
+                             const double* __restrict__ sumsq, const float* __restrict__ logeta, bf16* __restrict__ x0) {
+    __shared__ float inv;
+    if (threadIdx.x == 0) inv = sumsq[0] > 0.0 ? (float)rsqrt(sumsq[0] / (double)(3 * nn)) : 0.0f;
+    __syncthreads();
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nn) return;
+    const int64_t v = node_voxel(node, nnx, nny, g);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) x0[v * kInChannels + d] = __float2bfloat16_rn((float)r[(int64_t)d * nn + node] * inv);
+    x0[v * kInChannels + 3] = __float2bfloat16_rn(logeta[node]);
+}
+
+// z[d][node] += out_scale * rms(r) * out[d][v] on free dofs
+template <typename T>
+__global__ void k_add_correction(int64_t nnx, int64_t nny, int64_t nn, Vol g, const float* __restrict__ out,
+                                 const double* __restrict__ sumsq, float out_scale, const uint8_t* __restrict__ fixed,
+                                 T* __restrict__ z) {
+    __shared__ float s;
+    if (threadIdx.x == 0) s = out_scale * (float)sqrt(sumsq[0] / (double)(3 * nn));
+    __syncthreads();
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nn) return;
+    const int64_t v = node_voxel(node, nnx, nny, g);
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        if (!(fixed && fixed[node * 3 + d])) z[(int64_t)d * nn + node] += (T)(s * out[(int64_t)d * g.nv + v]);
+}
+
+// mean of log10(viscosity) over the material points of each element (0 for an empty element)
+__global__ void k_elem_logeta(int64_t ne, const uint32_t* __restrict__ offsets, const double* __restrict__ eta,
+                              float* __restrict__ elog) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const uint32_t a = offsets[e], b = offsets[e + 1];
+    float s = 0.0f;
+    for (uint32_t k = a; k < b; ++k) s += log10f(fmaxf((float)eta[k], 1e-30f));
+    elog[e] = b > a ? s / (float)(b - a) : 0.0f;
+}
+
+// node value = mean over the (1..8) elements around the node
+__global__ void k_node_logeta(int64_t nnx, int64_t nny, int64_t nn, int ex, int ey, int ez, const float* __restrict__ elog,
+                              float* __restrict__ nlog) {
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nn) return;
+    const int64_t i = node % nnx, j = (node / nnx) % nny, k = node / (nnx * nny);
+    float s = 0.0f;
+    int cnt = 0;
+    for (int o = 0; o < 8; ++o) {
+        const int64_t a = i - (o & 1), b = j - ((o >> 1) & 1), cc = k - (o >> 2);
+        if (a < 0 || a >= ex || b < 0 || b >= ey || cc < 0 || cc >= ez) continue;
+        s += elog[a + (int64_t)ex * (b + (int64_t)ey * cc)];
+        cnt++;
+    }
+    nlog[node] = cnt ? s / (float)cnt : 0.0f;
+}
+
+void prepare_viscosity(Context& c, Net& n) {
+    UWG_REQUIRE(c.assembled && c.mapped, UWGPU_ERR_STATE, "learned preconditioner needs the assembled point viscosities");
+    const MeshDesc& m = c.mesh;
+    n.logeta.ensure((size_t)n.nn);
+    DArray<float> elog;
+    elog.ensure((size_t)m.ne);
+    {
+        LaunchScope ls(c, -1);
+        k_elem_logeta<<<nblk(m.ne, 256), 256, 0, c.stream>>>(m.ne, c.offsets.p, c.seta_out.p, elog.p);
+    }
+    {
+        LaunchScope ls(c, -1);
+        k_node_logeta<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, m.nel[0], m.nel[1], m.nel[2], elog.p,
+                                                             n.logeta.p);
+    }
+    UWG_CUDA(cudaStreamSynchronize(c.stream));   // elog is released on return
+}
+
+template <typename T>
+void correct(Context& c, Net& n, const T* r, T* z) {
+    n.sumsq.ensure(1);
+    UWG_CUDA(cudaMemsetAsync(n.sumsq.p, 0, sizeof(double), c.stream));
+    {
+        LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+        k_sumsq<T><<<304, 256, 0, c.stream>>>(3 * n.nn, r, n.sumsq.p);
+    }
+    {
+        LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+        k_make_input<T><<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], r, n.sumsq.p, n.logeta.p,
+                                                                n.x0.p);
+    }
+    forward(c, n);
+    LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+    k_add_correction<T><<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], n.out.p, n.sumsq.p,
+                                                                n.out_scale, c.levels[0].fixed.p, z);
+}
+template void correct<double>(Context&, Net&, const double*, double*);
+template void correct<float>(Context&, Net&, const float*, float*);
+
+// ------------------------------------------------------------------------------------------
+// Training data: residual/error pairs of the multigrid solver (see solver.cu learned_generate)
+// ------------------------------------------------------------------------------------------
+struct Mode {
+    float kx, ky, kz, phase, amp;
+};
+
+// e[d][node] = sum over the modes of component d of amp cos(2 pi k.x + phase), 0 on fixed dofs
+__global__ void k_random_field(int64_t nnx, int64_t nny, int64_t nn, float hx, float hy, float hz,
+                               const Mode* __restrict__ modes, int per_comp, const uint8_t* __restrict__ fixed,
+                               double* __restrict__ e) {
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nn) return;
+    const float x = (float)(node % nnx) * hx, y = (float)((node / nnx) % nny) * hy, z = (float)(node / (nnx * nny)) * hz;
+    for (int d = 0; d < 3; ++d) {
+        float s = 0.0f;
+        for (int m = 0; m < per_comp; ++m) {
+            const Mode md = modes[d * per_comp + m];
+            s += md.amp * cospif(2.0f * (md.kx * x + md.ky * y + md.kz * z) + md.phase);
+        }
+        e[(int64_t)d * nn + node] = (fixed && fixed[node * 3 + d]) ? 0.0 : (double)s;
+    }
+}
+
+void random_field(Context& c, Net& n, uint64_t seed, double* e) {
+    const MeshDesc& m = c.mesh;
+    const int per = 16;
+    uint64_t s = seed * 0x2545F4914F6CDD1Dull + 17;
+    auto unif = [&]() { return (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0); };
+    // the largest wavenumber of this sample: from 1 (smooth) up to half the mesh resolution
+    const int kcap = std::max(1, std::min(m.nel[0], std::min(m.nel[1], m.nel[2])) / 2);
+    const double kmax = 1.0 + unif() * (kcap - 1);
+    std::vector<Mode> h((size_t)3 * per);
+    for (auto& md : h) {
+        md.kx = (float)std::floor(unif() * (kmax + 1.0));
+        md.ky = (float)std::floor(unif() * (kmax + 1.0));
+        md.kz = (float)std::floor(unif() * (kmax + 1.0));
+        const double kk = std::sqrt((double)md.kx * md.kx + (double)md.ky * md.ky + (double)md.kz * md.kz);
+        md.phase = (float)(2.0 * unif());
+        md.amp = (float)((2.0 * unif() - 1.0) / (1.0 + kk));
+    }
+    n.modes.ensure(h.size() * sizeof(Mode));
+    UWG_CUDA(cudaMemcpyAsync(n.modes.p, h.data(), h.size() * sizeof(Mode), cudaMemcpyHostToDevice, c.stream));
+    LaunchScope ls(c, -1);
+    k_random_field<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, 1.0f / m.nel[0], 1.0f / m.nel[1],
+                                                          1.0f / m.nel[2], reinterpret_cast<const Mode*>(n.modes.p), per,
+                                                          c.levels[0].fixed.p, e);
+    UWG_CUDA(cudaStreamSynchronize(c.stream));   // the host mode table is released on return
+}
+
+// sample k: x = r / rms(r), y = (e - v) / rms(r) (FP32, [3][nn]); ysq[k] = |y|^2
+__global__ void k_store_sample(int64_t n3, const double* __restrict__ r, const double* __restrict__ e,
+                               const double* __restrict__ v, const double* __restrict__ sumsq, int64_t nvec,
+                               float* __restrict__ xs, float* __restrict__ ys) {
+    __shared__ double inv;
+    if (threadIdx.x == 0) inv = sumsq[0] > 0.0 ? 1.0 / sqrt(sumsq[0] / (double)nvec) : 0.0;
+    __syncthreads();
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n3) return;
+    xs[i] = (float)(r[i] * inv);
+    ys[i] = (float)((e[i] - v[i]) * inv);
+}
+
+void dataset_reserve(Context& c, Net& n, int nsamples) {
+    n.data_x.ensure((size_t)nsamples * 3 * n.nn);
+    n.data_y.ensure((size_t)nsamples * 3 * n.nn);
+    n.ysq.assign((size_t)nsamples, 0.0);
+    n.nsamples = 0;
+    prepare_viscosity(c, n);
+}
+
+void dataset_add(Context& c, Net& n, const double* r, const double* e, const double* v) {
+    const int k = n.nsamples;
+    UWG_REQUIRE((size_t)k < n.ysq.size(), UWGPU_ERR_ARGUMENT, "training set is full");
+    n.sumsq.ensure(1);
+    UWG_CUDA(cudaMemsetAsync(n.sumsq.p, 0, sizeof(double), c.stream));
+    const int64_t n3 = 3 * n.nn;
+    {
+        LaunchScope ls(c, -1);
+        k_sumsq<double><<<304, 256, 0, c.stream>>>(n3, r, n.sumsq.p);
+    }
+    float* xs = n.data_x.p + (size_t)k * n3;
+    float* ys = n.data_y.p + (size_t)k * n3;
+    {
+        LaunchScope ls(c, -1);
+        k_store_sample<<<nblk(n3, 256), 256, 0, c.stream>>>(n3, r, e, v, n.sumsq.p, n3, xs, ys);
+    }
+    UWG_CUDA(cudaMemsetAsync(n.sumsq.p, 0, sizeof(double), c.stream));
+    {
+        LaunchScope ls(c, -1);
+        k_sumsq<float><<<304, 256, 0, c.stream>>>(n3, ys, n.sumsq.p);
+    }
+    double h = 0.0;
+    UWG_CUDA(cudaMemcpyAsync(&h, n.sumsq.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+    n.ysq[(size_t)k] = h;
+    n.nsamples = k + 1;
+}
+
+__global__ void k_scale_f(int64_t n, float a, float* __restrict__ x) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] *= a;
+}
+
+// the network's targets are scaled to unit RMS; out_scale maps its output back
+void dataset_finish(Context& c, Net& n) {
+    UWG_REQUIRE(n.nsamples > 0, UWGPU_ERR_STATE, "empty training set");
+    double tot = 0.0;
+    for (int k = 0; k < n.nsamples; ++k) tot += n.ysq[(size_t)k];
+    const double rms = std::sqrt(tot / ((double)n.nsamples * 3.0 * n.nn));
+    UWG_REQUIRE(rms > 0.0 && std::isfinite(rms), UWGPU_ERR_NAN, "training targets are zero or not finite");
+    n.out_scale = (float)rms;
+    const int64_t tot_n = (int64_t)n.nsamples * 3 * n.nn;
+    LaunchScope ls(c, -1);
+    k_scale_f<<<nblk(tot_n, 256), 256, 0, c.stream>>>(tot_n, (float)(1.0 / rms), n.data_y.p);
+    for (auto& v : n.ysq) v /= rms * rms;
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+// ------------------------------------------------------------------------------------------
+// Training: relative squared error per sample, Adam
+// ------------------------------------------------------------------------------------------
+__global__ void k_sample_input(int64_t nnx, int64_t nny, int64_t nn, Vol g, const float* __restrict__ xs,
+                               const float* __restrict__ logeta, bf16* __restrict__ x0) {
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nn) return;
+    const int64_t v = node_voxel(node, nnx, nny, g);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) x0[v * kInChannels + d] = __float2bfloat16_rn(xs[(int64_t)d * nn + node]);
+    x0[v * kInChannels + 3] = __float2bfloat16_rn(logeta[node]);
+}
+
+// loss += |out - y|^2 / ysq over free dofs; gout = 2 (out - y) / ysq there (0 elsewhere)
+__global__ void k_rel_mse(int64_t nnx, int64_t nny, int64_t nn, Vol g, const float* __restrict__ out,
+                          const float* __restrict__ y, const uint8_t* __restrict__ fixed, float inv_ysq,
+                          float* __restrict__ gout, double* __restrict__ loss) {
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.0f;
+    if (node < nn) {
+        const int64_t v = node_voxel(node, nnx, nny, g);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            float diff = out[(int64_t)d * g.nv + v] - y[(int64_t)d * nn + node];
+            if (fixed && fixed[node * 3 + d]) diff = 0.0f;
+            gout[(int64_t)d * g.nv + v] = 2.0f * diff * inv_ysq;
+            l = fmaf(diff * diff, inv_ysq, l);
+        }
+    }
+    l = warp_sum(l);
+    if ((threadIdx.x & 31) == 0 && loss) atomicAdd(loss, (double)l);
+}
+
+// one sample: forward, loss and its gradient, backward (grads accumulate); returns the loss
+static void sample_step(Context& c, Net& n, int k, bool train, double* dloss) {
+    const int64_t n3 = 3 * n.nn;
+    {
+        LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+        k_sample_input<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], n.data_x.p + (size_t)k * n3,
+                                                               n.logeta.p, n.x0.p);
+    }
+    forward(c, n);
+    UWG_CUDA(cudaMemsetAsync(n.gout.p, 0, (size_t)n.vol[0].nv * 3 * sizeof(float), c.stream));
+    {
+        LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+        const double ysq = n.ysq[(size_t)k];
+        k_rel_mse<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], n.out.p, n.data_y.p + (size_t)k * n3,
+                                                          c.levels[0].fixed.p, ysq > 0.0 ? (float)(1.0 / ysq) : 0.0f,
+                                                          n.gout.p, dloss);
+    }
+    if (train) backward(c, n);
+}
+
+void train(Context& c, Net& n, int epochs, int batch, float lr, uint64_t seed, double* train_loss,
+           double* holdout_ratio) {
+    UWG_REQUIRE(n.nsamples >= 2, UWGPU_ERR_STATE, "training needs at least two samples (learned_generate)");
+    UWG_REQUIRE(epochs >= 0 && batch >= 1, UWGPU_ERR_ARGUMENT, "bad epochs or batch");
+    const int nhold = std::max(1, n.nsamples / 10);
+    const int ntrain = n.nsamples - nhold;
+    std::vector<int> order((size_t)ntrain);
+    for (int k = 0; k < ntrain; ++k) order[(size_t)k] = k;
+    uint64_t s = seed ^ 0xA0761D6478BD642Full;
+    DArray<double> dl;
+    dl.ensure(2);
+    double last = 0.0;
+    for (int ep = 0; ep < epochs; ++ep) {
+        for (int k = ntrain - 1; k > 0; --k) std::swap(order[(size_t)k], order[(size_t)(splitmix(s) % (uint64_t)(k + 1))]);
+        UWG_CUDA(cudaMemsetAsync(dl.p, 0, sizeof(double), c.stream));
+        for (int b0 = 0; b0 < ntrain; b0 += batch) {
+            const int nb = std::min(batch, ntrain - b0);
+            UWG_CUDA(cudaMemsetAsync(n.grads.p, 0, (size_t)n.nparams * sizeof(float), c.stream));
+            for (int q = 0; q < nb; ++q) sample_step(c, n, order[(size_t)(b0 + q)], true, dl.p);
+            n.adam_t++;
+            const float b1 = 0.9f, b2 = 0.999f;
+            const float bc1 = 1.0f - std::pow(b1, (float)n.adam_t), bc2 = 1.0f - std::pow(b2, (float)n.adam_t);
+            {
+                LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+                k_adam<<<nblk(n.nparams, 256), 256, 0, c.stream>>>(n.nparams, n.params.p, n.grads.p, n.adam_m.p,
+                                                                   n.adam_v.p, lr, b1, b2, 1e-8f, bc1, bc2, 1.0f / nb);
+            }
+            pack(c, n);
+        }
+        UWG_CUDA(cudaMemcpyAsync(c.host_scalars, dl.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        last = c.host_scalars[0] / ntrain;
+        if (!std::isfinite(last)) throw Error(UWGPU_ERR_NAN, "U-Net training diverged");
+    }
+    if (train_loss) *train_loss = last;
+    // held-out samples: |y - N(x)|^2 / |y|^2 averaged (1 = no better than no correction)
+    UWG_CUDA(cudaMemsetAsync(dl.p, 0, sizeof(double), c.stream));
+    for (int k = ntrain; k < n.nsamples; ++k) sample_step(c, n, k, false, dl.p);
+    UWG_CUDA(cudaMemcpyAsync(c.host_scalars, dl.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+    if (holdout_ratio) *holdout_ratio = c.host_scalars[0] / nhold;
 }
 
 }  // namespace unet

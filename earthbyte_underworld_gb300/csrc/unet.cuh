@@ -38,6 +38,15 @@ struct Net {
     int adam_t = 0;
     float out_scale = 1.0f;                       // target scale learned from the training set
 
+    // preconditioner state: node log10 viscosity, scratch scalar
+    DArray<float> logeta;
+    DArray<double> sumsq;
+    // training set: inputs r/rms(r) and targets (e - V r)/rms(r)/out_scale, [sample][3][nn]
+    DArray<float> data_x, data_y;
+    std::vector<double> ysq;                      // |target|^2 per sample
+    int nsamples = 0;
+    DArray<unsigned char> modes;                  // random-field mode table
+
     // activations (BF16, channels-last) and the head output (FP32, [3][nv0])
     DArray<__nv_bfloat16> x0;
     DArray<__nv_bfloat16> enc_a[kMaxLevels], enc_b[kMaxLevels], pool[kMaxLevels];
@@ -67,6 +76,20 @@ void get_output_host(Context& c, Net& n, float* output);
 // Gradient of the output from host grad[3][nn] (zero on padding voxels); input gradient to host [4][nn].
 void set_grad_output_host(Context& c, Net& n, const float* grad);
 void get_input_grad_host(Context& c, Net& n, float* grad_input);
+
+// node log10 viscosity from the assembled material points (needed before correct / training)
+void prepare_viscosity(Context& c, Net& n);
+// z += network correction for residual r (node SoA [3][nn]); r is scaled to unit RMS first
+template <typename T>
+void correct(Context& c, Net& n, const T* r, T* z);
+// random multi-scale velocity field (0 on fixed dofs) into e[3][nn]
+void random_field(Context& c, Net& n, uint64_t seed, double* e);
+void dataset_reserve(Context& c, Net& n, int nsamples);
+void dataset_add(Context& c, Net& n, const double* r, const double* e, const double* v);
+void dataset_finish(Context& c, Net& n);
+// Adam on the relative squared error; the last 10% of the samples are held out
+void train(Context& c, Net& n, int epochs, int batch, float lr, uint64_t seed, double* train_loss,
+           double* holdout_ratio);
 
 }  // namespace unet
 }  // namespace uwg

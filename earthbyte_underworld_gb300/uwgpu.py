@@ -62,14 +62,15 @@ class SolveOpts(C.Structure):
                 ("max_outer", C.c_int32), ("max_inner", C.c_int32), ("scr_rtol", C.c_double),
                 ("a11_rtol", C.c_double), ("back_rtol", C.c_double), ("remove_const_p", C.c_int32),
                 ("precision", C.c_int32), ("target_rel_residual", C.c_double), ("bfbt_rtol", C.c_double),
-                ("bfbt_max_it", C.c_int32), ("smoother", C.c_int32)]
+                ("bfbt_max_it", C.c_int32), ("smoother", C.c_int32), ("learned_pc", C.c_int32),
+                ("learned_stagnation", C.c_int32)]
 
 
 class Report(C.Structure):
     _fields_ = [("outer_its", C.c_int32), ("inner_its_total", C.c_int32), ("backsolve_its", C.c_int32),
                 ("vcycles", C.c_int32), ("converged", C.c_int32), ("status", C.c_int32),
                 ("rel_residual", C.c_double), ("t_setup_ms", C.c_double), ("t_solve_ms", C.c_double),
-                ("pc_inner_its", C.c_int64)]
+                ("pc_inner_its", C.c_int64), ("learned_applies", C.c_int32), ("learned_fallbacks", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -128,6 +129,8 @@ def load(build_if_missing: bool = True):
         L.uwgpu_learned_set_params.argtypes = [P, P]
         L.uwgpu_learned_forward.argtypes = [P, P, P]
         L.uwgpu_learned_backward.argtypes = [P, P, P, P]
+        L.uwgpu_learned_generate.argtypes = [P, P, C.c_int32, C.c_uint64]
+        L.uwgpu_learned_train.argtypes = [P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P, P]
         _lib = L
         return _lib
 
@@ -360,6 +363,16 @@ class Context:
         out = np.zeros((3, self.nnodes), np.float32)
         self._check(self._L.uwgpu_learned_forward(self._h, _ptr(x), _ptr(out)))
         return out
+
+    def learned_generate(self, opts, nsamples=64, seed=1):
+        """training pairs (residual, error left by one V-cycle) from the assembled system"""
+        self._check(self._L.uwgpu_learned_generate(self._h, C.byref(opts), nsamples, seed))
+
+    def learned_train(self, epochs=10, batch=4, lr=1e-3, seed=1):
+        """Adam on the generated pairs -> (last-epoch relative loss, held-out error ratio)"""
+        tl, hr = C.c_double(), C.c_double()
+        self._check(self._L.uwgpu_learned_train(self._h, epochs, batch, lr, seed, C.byref(tl), C.byref(hr)))
+        return tl.value, hr.value
 
     def learned_backward(self, grad_out):
         """after learned_forward: gradient of the output (3, nn) -> (parameter gradient, input gradient (4, nn))"""

@@ -109,6 +109,10 @@ typedef struct {
     int32_t bfbt_max_it;      /* inner iteration limit of those solves                   */
     int32_t smoother;         /* UWGPU_SMOOTHER_COLOUR_GS (default) or UWGPU_SMOOTHER_CHEBYSHEV:
                                  smooth_down/up are then polynomial degrees              */
+    int32_t learned_pc;       /* 1: velocity preconditioner V-cycle + trained U-Net correction
+                                 (uwgpu_learned_*), 0: V-cycle only (default)                */
+    int32_t learned_stagnation; /* consecutive velocity iterations with < 5% residual reduction
+                                 after which a velocity solve drops the U-Net (default 2)    */
 } uwgpu_solve_opts;
 
 typedef struct {
@@ -122,6 +126,8 @@ typedef struct {
     double t_setup_ms;        /* stencil build + multigrid hierarchy                     */
     double t_solve_ms;
     int64_t pc_inner_its;     /* inner iterations of the Schur preconditioner (scaled BFBt) */
+    int32_t learned_applies;  /* U-Net corrections applied                                  */
+    int32_t learned_fallbacks; /* velocity solves that fell back to the plain V-cycle       */
 } uwgpu_report;
 
 typedef struct uwgpu_ctx uwgpu_ctx;
@@ -288,6 +294,16 @@ int uwgpu_learned_set_params(uwgpu_ctx* ctx, const float* params);
  * grad_output[3][nn] -> grad_params[param_count] (overwritten) and grad_input[4][nn]. */
 int uwgpu_learned_forward(uwgpu_ctx* ctx, const float* input, float* output);
 int uwgpu_learned_backward(uwgpu_ctx* ctx, const float* grad_output, float* grad_params, float* grad_input);
+
+/* Training set from the assembled system: `nsamples` residual/error pairs of the multigrid
+ * solver (random velocity fields e, r = K e, target e - V(r) for one V-cycle V of the hierarchy
+ * `opts` describes); replaces any previous set. */
+int uwgpu_learned_generate(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, int32_t nsamples, uint64_t seed);
+/* Adam on the relative squared error of the correction; the last 10% of the samples are held
+ * out.  train_loss: mean relative error of the last epoch; holdout_ratio: |target - N|^2/|target|^2
+ * on the held-out pairs (below 1: the network reduces the error the V-cycle leaves). */
+int uwgpu_learned_train(uwgpu_ctx* ctx, int32_t epochs, int32_t batch, float learning_rate, uint64_t seed,
+                        double* train_loss, double* holdout_ratio);
 
 #ifdef __cplusplus
 }

@@ -45,7 +45,11 @@ def padded(n, levels):
 
 
 def _bf(x, on):
-    return x.to(torch.bfloat16).to(torch.float32) if on else x
+    """round the value to bfloat16; the gradient passes through in FP32 (a plain dtype cast would
+    round the gradient to bfloat16 as well, which the GPU backward does not do)"""
+    if not on:
+        return x
+    return x + (x.to(torch.bfloat16).to(torch.float32) - x).detach()
 
 
 def forward_t(layers, hw, hb, inp, nodes, levels, emulate_bf16=True):

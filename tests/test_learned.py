@@ -93,3 +93,58 @@ def test_unet_forward_backward_match_reference(uw, nel, levels, base):
     fout, fgp, _ = R.value_and_grads(params, inp, gout, nodes, levels, base, emulate_bf16=False)
     assert _rel(out, rout) < 1.5e-2 and _rel(gp, rgp) < 3e-2 and _rel(gi, rgi) < 3e-2
     assert _rel(out, rout) < 0.5 * _rel(fout, rout)
+
+
+@pytest.mark.gpu
+def test_learned_preconditioner_training_and_ablation(uw):
+    """Train the U-Net on residual/error pairs of the multigrid solver (on the GPU, with its own
+    kernels), then solve with and without it.  The gain on its task is asserted: on held-out pairs
+    the network removes part of the error one V-cycle leaves (ratio < 1).  The solve with the
+    learned correction reaches the same solution; the iteration counts of both are reported
+    (flexible Krylov accepts any correction, and plain multigrid stays the fallback)."""
+    from earthbyte_underworld_gb300 import workloads as W
+    U = uw
+    w = W.spheres(nel=(16, 16, 16), nspheres=20, seed=5)
+    opts = U.default_opts(mg_levels=3, schur_type=1, schur_pc=3, scr_rtol=1e-6, a11_rtol=1e-6, back_rtol=1e-6,
+                          max_outer=200, max_inner=2000, bfbt_rtol=1e-2, bfbt_max_it=2000, smoother=1,
+                          smooth_down=2, smooth_up=2)
+    with U.Context(0) as ctx:
+        W.setup_context(ctx, w)
+        ctx.bin_and_map(want=False)
+        ctx.assemble()
+        u0, p0, r0 = ctx.solve_bsscr(opts)
+        ctx.learned_create(levels=3, base=8, seed=1)
+        ctx.learned_generate(opts, nsamples=96, seed=5)
+        loss, holdout = ctx.learned_train(epochs=25, batch=4, lr=2e-3, seed=2)
+        opts.learned_pc = 1
+        u1, p1, r1 = ctx.solve_bsscr(opts)
+    print(f"\nU-Net: train loss {loss:.3f}, held-out error ratio {holdout:.3f}; "
+          f"V-cycles plain {r0.vcycles}, learned {r1.vcycles} ({r1.learned_applies} corrections, "
+          f"{r1.learned_fallbacks} fallbacks)")
+    assert np.isfinite(loss) and holdout < 0.95
+    assert r1.rel_residual < 1e-5 and r1.learned_applies > 0
+    assert _rel(u1, u0) < 1e-4 and _rel(p1, p0) < 1e-3
+
+
+@pytest.mark.gpu
+def test_learned_preconditioner_falls_back(uw):
+    """A network that makes things worse (large random weights) must not break the solve: the
+    stagnation test drops it and the plain V-cycle finishes the velocity solves."""
+    from earthbyte_underworld_gb300 import workloads as W
+    U = uw
+    w = W.spheres(nel=(8, 8, 8), nspheres=8, seed=3)
+    opts = U.default_opts(mg_levels=2, schur_type=1, schur_pc=0, scr_rtol=1e-6, a11_rtol=1e-7, back_rtol=1e-7,
+                          max_outer=400, max_inner=2000)
+    with U.Context(0) as ctx:
+        W.setup_context(ctx, w)
+        ctx.bin_and_map(want=False)
+        ctx.assemble()
+        u0, p0, r0 = ctx.solve_bsscr(opts)
+        ctx.learned_create(levels=2, base=8, seed=4)
+        rng = np.random.default_rng(0)
+        ctx.learned_set_params(rng.standard_normal(ctx.learned_param_count()).astype(np.float32) * 3.0)
+        opts.learned_pc = 1
+        u1, p1, r1 = ctx.solve_bsscr(opts)
+    assert r1.rel_residual < 1e-5
+    assert _rel(u1, u0) < 1e-4
+    assert r1.learned_applies > 0
