@@ -1,8 +1,9 @@
 // Learned velocity preconditioner: a 3D U-Net on the nodal grid (BF16 weights and activations,
 // FP32 accumulation and gradients), with its own forward, backward and Adam kernels.
 //
-// Input channels per node: the three components of the residual (scaled to unit RMS) and
-// log10 of the node-averaged viscosity; output: a three-component velocity correction.  The node
+// Input channels per node: the three components of the residual r and of the multigrid
+// V-cycle's answer V(r) (each scaled to unit RMS), and log10 of the node-averaged viscosity;
+// output: the correction to add to V(r), in units of RMS(V(r)).  The node
 // grid (nel+1 per axis) is zero-padded to a multiple of 2^(levels-1).  Level l has base * 2^l
 // channels; each level is two 3x3x3 convolutions with ReLU, levels are joined by 2x2x2 average
 // pooling on the way down and nearest upsampling + concatenation with the skip on the way up, and
@@ -614,7 +615,7 @@ __global__ void k_input_from_host_layout(int64_t nnx, int64_t nny, int64_t nn, V
     const int64_t i = node % nnx, j = (node / nnx) % nny, k = node / (nnx * nny);
     const int64_t v = i + (int64_t)g.px * (j + (int64_t)g.py * k);
 #pragma unroll
-    for (int ch = 0; ch < 4; ++ch) x0[v * kInChannels + ch] = __float2bfloat16_rn(in4[(int64_t)ch * nn + node]);
+    for (int ch = 0; ch < kUsedChannels; ++ch) x0[v * kInChannels + ch] = __float2bfloat16_rn(in4[(int64_t)ch * nn + node]);
 }
 
 __global__ void k_output_to_node_layout(int64_t nnx, int64_t nny, int64_t nn, Vol g, const float* __restrict__ out,
@@ -629,8 +630,9 @@ __global__ void k_output_to_node_layout(int64_t nnx, int64_t nny, int64_t nn, Vo
 
 void set_input_host(Context& c, Net& n, const float* input) {
     DArray<float> tmp;
-    tmp.ensure((size_t)n.nn * 4);
-    UWG_CUDA(cudaMemcpyAsync(tmp.p, input, (size_t)n.nn * 4 * sizeof(float), cudaMemcpyHostToDevice, c.stream));
+    tmp.ensure((size_t)n.nn * kUsedChannels);
+    UWG_CUDA(cudaMemcpyAsync(tmp.p, input, (size_t)n.nn * kUsedChannels * sizeof(float), cudaMemcpyHostToDevice,
+                             c.stream));
     UWG_CUDA(cudaMemsetAsync(n.x0.p, 0, (size_t)n.vol[0].nv * kInChannels * sizeof(bf16), c.stream));
     LaunchScope ls(c, -1);
     k_input_from_host_layout<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], tmp.p, n.x0.p);
@@ -665,7 +667,7 @@ __global__ void k_input_grad_to_node_layout(int64_t nnx, int64_t nny, int64_t nn
     const int64_t i = node % nnx, j = (node / nnx) % nny, k = node / (nnx * nny);
     const int64_t v = i + (int64_t)g.px * (j + (int64_t)g.py * k);
 #pragma unroll
-    for (int ch = 0; ch < 4; ++ch) g4[(int64_t)ch * nn + node] = gin[v * kInChannels + ch];
+    for (int ch = 0; ch < kUsedChannels; ++ch) g4[(int64_t)ch * nn + node] = gin[v * kInChannels + ch];
 }
 
 void set_grad_output_host(Context& c, Net& n, const float* grad) {
@@ -680,13 +682,14 @@ void set_grad_output_host(Context& c, Net& n, const float* grad) {
 
 void get_input_grad_host(Context& c, Net& n, float* grad_input) {
     DArray<float> tmp;
-    tmp.ensure((size_t)n.nn * 4);
+    tmp.ensure((size_t)n.nn * kUsedChannels);
     {
         LaunchScope ls(c, -1);
         k_input_grad_to_node_layout<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], n.g_in[0].p,
                                                                             tmp.p);
     }
-    UWG_CUDA(cudaMemcpyAsync(grad_input, tmp.p, (size_t)n.nn * 4 * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+    UWG_CUDA(cudaMemcpyAsync(grad_input, tmp.p, (size_t)n.nn * kUsedChannels * sizeof(float), cudaMemcpyDeviceToHost,
+                             c.stream));
     UWG_CUDA(cudaStreamSynchronize(c.stream));
 }
 
@@ -710,28 +713,33 @@ __device__ __forceinline__ int64_t node_voxel(int64_t node, int64_t nnx, int64_t
     return i + (int64_t)g.px * (j + (int64_t)g.py * k);
 }
 
-// x0[v] = (r[.][node] / rms(r), log10 viscosity, 0, 0, 0, 0)
+// x0[v] = (r / rms(r), v / rms(v), log10 viscosity, 0) at node voxels; sumsq = (|r|^2, |v|^2)
 template <typename T>
 __global__ void k_make_input(int64_t nnx, int64_t nny, int64_t nn, Vol g, const T* __restrict__ r,
-                             const double* __restrict__ sumsq, const float* __restrict__ logeta, bf16* __restrict__ x0) {
-    __shared__ float inv;
-    if (threadIdx.x == 0) inv = sumsq[0] > 0.0 ? (float)rsqrt(sumsq[0] / (double)(3 * nn)) : 0.0f;
+                             const T* __restrict__ vc, const double* __restrict__ sumsq,
+                             const float* __restrict__ logeta, bf16* __restrict__ x0) {
+    __shared__ float inv[2];
+    if (threadIdx.x < 2)
+        inv[threadIdx.x] = sumsq[threadIdx.x] > 0.0 ? (float)rsqrt(sumsq[threadIdx.x] / (double)(3 * nn)) : 0.0f;
     __syncthreads();
     const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= nn) return;
     const int64_t v = node_voxel(node, nnx, nny, g);
 #pragma unroll
-    for (int d = 0; d < 3; ++d) x0[v * kInChannels + d] = __float2bfloat16_rn((float)r[(int64_t)d * nn + node] * inv);
-    x0[v * kInChannels + 3] = __float2bfloat16_rn(logeta[node]);
+    for (int d = 0; d < 3; ++d) {
+        x0[v * kInChannels + d] = __float2bfloat16_rn((float)r[(int64_t)d * nn + node] * inv[0]);
+        x0[v * kInChannels + 3 + d] = __float2bfloat16_rn((float)vc[(int64_t)d * nn + node] * inv[1]);
+    }
+    x0[v * kInChannels + 6] = __float2bfloat16_rn(logeta[node]);
 }
 
-// z[d][node] += out_scale * rms(r) * out[d][v] on free dofs
+// z[d][node] += out_scale * rms(V(r)) * out[d][v] on free dofs (sumsq[1] = |V(r)|^2)
 template <typename T>
 __global__ void k_add_correction(int64_t nnx, int64_t nny, int64_t nn, Vol g, const float* __restrict__ out,
                                  const double* __restrict__ sumsq, float out_scale, const uint8_t* __restrict__ fixed,
                                  T* __restrict__ z) {
     __shared__ float s;
-    if (threadIdx.x == 0) s = out_scale * (float)sqrt(sumsq[0] / (double)(3 * nn));
+    if (threadIdx.x == 0) s = out_scale * (float)sqrt(sumsq[1] / (double)(3 * nn));
     __syncthreads();
     const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= nn) return;
@@ -789,16 +797,20 @@ void prepare_viscosity(Context& c, Net& n) {
 
 template <typename T>
 void correct(Context& c, Net& n, const T* r, T* z) {
-    n.sumsq.ensure(1);
-    UWG_CUDA(cudaMemsetAsync(n.sumsq.p, 0, sizeof(double), c.stream));
+    n.sumsq.ensure(2);
+    UWG_CUDA(cudaMemsetAsync(n.sumsq.p, 0, 2 * sizeof(double), c.stream));
     {
         LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
         k_sumsq<T><<<304, 256, 0, c.stream>>>(3 * n.nn, r, n.sumsq.p);
     }
     {
         LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
-        k_make_input<T><<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], r, n.sumsq.p, n.logeta.p,
-                                                                n.x0.p);
+        k_sumsq<T><<<304, 256, 0, c.stream>>>(3 * n.nn, z, n.sumsq.p + 1);
+    }
+    {
+        LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+        k_make_input<T><<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], r, z, n.sumsq.p,
+                                                                n.logeta.p, n.x0.p);
     }
     forward(c, n);
     LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
@@ -858,21 +870,23 @@ void random_field(Context& c, Net& n, uint64_t seed, double* e) {
     UWG_CUDA(cudaStreamSynchronize(c.stream));   // the host mode table is released on return
 }
 
-// sample k: x = r / rms(r), y = (e - v) / rms(r) (FP32, [3][nn]); ysq[k] = |y|^2
+// sample k: xs = (r / rms(r), v / rms(v)) (FP32, [6][nn]), ys = (e - v) / rms(v) ([3][nn])
 __global__ void k_store_sample(int64_t n3, const double* __restrict__ r, const double* __restrict__ e,
                                const double* __restrict__ v, const double* __restrict__ sumsq, int64_t nvec,
                                float* __restrict__ xs, float* __restrict__ ys) {
-    __shared__ double inv;
-    if (threadIdx.x == 0) inv = sumsq[0] > 0.0 ? 1.0 / sqrt(sumsq[0] / (double)nvec) : 0.0;
+    __shared__ double inv[2];
+    if (threadIdx.x < 2)
+        inv[threadIdx.x] = sumsq[threadIdx.x] > 0.0 ? 1.0 / sqrt(sumsq[threadIdx.x] / (double)nvec) : 0.0;
     __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n3) return;
-    xs[i] = (float)(r[i] * inv);
-    ys[i] = (float)((e[i] - v[i]) * inv);
+    xs[i] = (float)(r[i] * inv[0]);
+    xs[n3 + i] = (float)(v[i] * inv[1]);
+    ys[i] = (float)((e[i] - v[i]) * inv[1]);
 }
 
 void dataset_reserve(Context& c, Net& n, int nsamples) {
-    n.data_x.ensure((size_t)nsamples * 3 * n.nn);
+    n.data_x.ensure((size_t)nsamples * 6 * n.nn);
     n.data_y.ensure((size_t)nsamples * 3 * n.nn);
     n.ysq.assign((size_t)nsamples, 0.0);
     n.nsamples = 0;
@@ -882,14 +896,15 @@ void dataset_reserve(Context& c, Net& n, int nsamples) {
 void dataset_add(Context& c, Net& n, const double* r, const double* e, const double* v) {
     const int k = n.nsamples;
     UWG_REQUIRE((size_t)k < n.ysq.size(), UWGPU_ERR_ARGUMENT, "training set is full");
-    n.sumsq.ensure(1);
-    UWG_CUDA(cudaMemsetAsync(n.sumsq.p, 0, sizeof(double), c.stream));
+    n.sumsq.ensure(2);
+    UWG_CUDA(cudaMemsetAsync(n.sumsq.p, 0, 2 * sizeof(double), c.stream));
     const int64_t n3 = 3 * n.nn;
     {
         LaunchScope ls(c, -1);
         k_sumsq<double><<<304, 256, 0, c.stream>>>(n3, r, n.sumsq.p);
+        k_sumsq<double><<<304, 256, 0, c.stream>>>(n3, v, n.sumsq.p + 1);
     }
-    float* xs = n.data_x.p + (size_t)k * n3;
+    float* xs = n.data_x.p + (size_t)k * 2 * n3;
     float* ys = n.data_y.p + (size_t)k * n3;
     {
         LaunchScope ls(c, -1);
@@ -936,8 +951,8 @@ __global__ void k_sample_input(int64_t nnx, int64_t nny, int64_t nn, Vol g, cons
     if (node >= nn) return;
     const int64_t v = node_voxel(node, nnx, nny, g);
 #pragma unroll
-    for (int d = 0; d < 3; ++d) x0[v * kInChannels + d] = __float2bfloat16_rn(xs[(int64_t)d * nn + node]);
-    x0[v * kInChannels + 3] = __float2bfloat16_rn(logeta[node]);
+    for (int d = 0; d < 6; ++d) x0[v * kInChannels + d] = __float2bfloat16_rn(xs[(int64_t)d * nn + node]);
+    x0[v * kInChannels + 6] = __float2bfloat16_rn(logeta[node]);
 }
 
 // loss += |out - y|^2 / ysq over free dofs; gout = 2 (out - y) / ysq there (0 elsewhere)
@@ -965,7 +980,7 @@ static void sample_step(Context& c, Net& n, int k, bool train, double* dloss) {
     const int64_t n3 = 3 * n.nn;
     {
         LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
-        k_sample_input<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], n.data_x.p + (size_t)k * n3,
+        k_sample_input<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], n.data_x.p + (size_t)k * 2 * n3,
                                                                n.logeta.p, n.x0.p);
     }
     forward(c, n);

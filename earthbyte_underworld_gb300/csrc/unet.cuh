@@ -12,7 +12,8 @@ namespace uwg {
 namespace unet {
 
 constexpr int kMaxLevels = 6;
-constexpr int kInChannels = 8;   // residual (3), log10 viscosity (1), zero padding to 8
+constexpr int kInChannels = 8;     // residual (3), V-cycle answer (3), log10 viscosity (1), zero (1)
+constexpr int kUsedChannels = 7;   // channels the test hooks exchange with the host
 
 // zero-padded voxel grid of one level (channels-last tensors of nv voxels)
 struct Vol {
@@ -41,7 +42,8 @@ struct Net {
     // preconditioner state: node log10 viscosity, scratch scalar
     DArray<float> logeta;
     DArray<double> sumsq;
-    // training set: inputs r/rms(r) and targets (e - V r)/rms(r)/out_scale, [sample][3][nn]
+    // training set: inputs (r/rms(r), V(r)/rms(V(r))) [sample][6][nn] and targets
+    // (e - V(r))/rms(V(r))/out_scale [sample][3][nn]
     DArray<float> data_x, data_y;
     std::vector<double> ysq;                      // |target|^2 per sample
     int nsamples = 0;
@@ -70,16 +72,16 @@ void forward(Context& c, Net& n);
 // Backward pass from n.gout (gradient of the head output, [3][nv0]); adds into n.grads.
 // n.g_in[0] receives the gradient of the input tensor.
 void backward(Context& c, Net& n);
-// Input tensor from host node arrays input[4][nn] (test hook); output back to out[3][nn].
+// Input tensor from host node arrays input[7][nn] (test hook); output back to out[3][nn].
 void set_input_host(Context& c, Net& n, const float* input);
 void get_output_host(Context& c, Net& n, float* output);
-// Gradient of the output from host grad[3][nn] (zero on padding voxels); input gradient to host [4][nn].
+// Gradient of the output from host grad[3][nn] (zero on padding voxels); input gradient to host [7][nn].
 void set_grad_output_host(Context& c, Net& n, const float* grad);
 void get_input_grad_host(Context& c, Net& n, float* grad_input);
 
 // node log10 viscosity from the assembled material points (needed before correct / training)
 void prepare_viscosity(Context& c, Net& n);
-// z += network correction for residual r (node SoA [3][nn]); r is scaled to unit RMS first
+// z += network correction for residual r, z holding the V-cycle's answer V(r) (node SoA [3][nn])
 template <typename T>
 void correct(Context& c, Net& n, const T* r, T* z);
 // random multi-scale velocity field (0 on fixed dofs) into e[3][nn]

@@ -358,8 +358,8 @@ class Context:
         self._check(self._L.uwgpu_learned_set_params(self._h, _ptr(p)))
 
     def learned_forward(self, inp):
-        """inp: (4, nn) float32 (residual components, log10 viscosity) -> (3, nn) float32"""
-        x = np.ascontiguousarray(inp, dtype=np.float32).reshape(4, self.nnodes)
+        """inp: (7, nn) float32 (residual, V-cycle answer, log10 viscosity) -> (3, nn) float32"""
+        x = np.ascontiguousarray(inp, dtype=np.float32).reshape(7, self.nnodes)
         out = np.zeros((3, self.nnodes), np.float32)
         self._check(self._L.uwgpu_learned_forward(self._h, _ptr(x), _ptr(out)))
         return out
@@ -375,10 +375,10 @@ class Context:
         return tl.value, hr.value
 
     def learned_backward(self, grad_out):
-        """after learned_forward: gradient of the output (3, nn) -> (parameter gradient, input gradient (4, nn))"""
+        """after learned_forward: gradient of the output (3, nn) -> (parameter gradient, input gradient (7, nn))"""
         g = np.ascontiguousarray(grad_out, dtype=np.float32).reshape(3, self.nnodes)
         gp = np.zeros(self.learned_param_count(), np.float32)
-        gi = np.zeros((4, self.nnodes), np.float32)
+        gi = np.zeros((7, self.nnodes), np.float32)
         self._check(self._L.uwgpu_learned_backward(self._h, _ptr(g), _ptr(gp), _ptr(gi)))
         return gp, gi
 

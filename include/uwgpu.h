@@ -276,8 +276,9 @@ int uwgpu_bin_and_map_noalloc(int32_t dim, const int32_t nel[3], const double mi
                               uint32_t* offsets, double* xi, void* stream, uint32_t* outside);
 
 /* ---- Learned velocity preconditioner ------------------------------------------------------
- * A 3D U-Net (BF16 weights and activations, FP32 accumulation) that maps the velocity residual
- * and log10 viscosity on the node grid to a velocity correction.  It has no counterpart in the
+ * A 3D U-Net (BF16 weights and activations, FP32 accumulation) that maps the velocity residual,
+ * the multigrid V-cycle's answer to it and log10 viscosity on the node grid to a correction of
+ * that answer.  It has no counterpart in the
  * reference: it augments the multigrid preconditioner of the velocity solve (BSSCR/mg.c:42-132,
  * PCMG) inside the flexible Krylov iteration, with plain multigrid as its fallback.  3D only. */
 
@@ -289,15 +290,16 @@ int uwgpu_learned_param_count(uwgpu_ctx* ctx, int64_t* count);
  * layers by level, then decoder layers by level, then the 1x1x1 head W[cin][3], bias[3]). */
 int uwgpu_learned_get_params(uwgpu_ctx* ctx, float* params);
 int uwgpu_learned_set_params(uwgpu_ctx* ctx, const float* params);
-/* Test hooks: one forward pass on host input[4][nn] (channels: three residual components,
- * log10 viscosity; node order of the mesh) -> output[3][nn]; then the backward pass of
- * grad_output[3][nn] -> grad_params[param_count] (overwritten) and grad_input[4][nn]. */
+/* Test hooks: one forward pass on host input[7][nn] (channels: three residual components, three
+ * components of the V-cycle's answer, log10 viscosity; node order of the mesh) -> output[3][nn];
+ * then the backward pass of grad_output[3][nn] -> grad_params[param_count] (overwritten) and
+ * grad_input[7][nn]. */
 int uwgpu_learned_forward(uwgpu_ctx* ctx, const float* input, float* output);
 int uwgpu_learned_backward(uwgpu_ctx* ctx, const float* grad_output, float* grad_params, float* grad_input);
 
 /* Training set from the assembled system: `nsamples` residual/error pairs of the multigrid
- * solver (random velocity fields e, r = K e, target e - V(r) for one V-cycle V of the hierarchy
- * `opts` describes); replaces any previous set. */
+ * solver (random velocity fields e, r = K e, inputs r and V(r), target e - V(r) for one V-cycle V
+ * of the hierarchy `opts` describes); replaces any previous set. */
 int uwgpu_learned_generate(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, int32_t nsamples, uint64_t seed);
 /* Adam on the relative squared error of the correction; the last 10% of the samples are held
  * out.  train_loss: mean relative error of the last epoch; holdout_ratio: |target - N|^2/|target|^2

@@ -54,13 +54,14 @@ def _bf(x, on):
 
 def forward_t(layers, hw, hb, inp, nodes, levels, emulate_bf16=True):
     """layers: [(conv3d weight [cout][cin][3][3][3], bias)], head (hw [cin][3], hb [3]);
-    inp (4, nn) tensor, node order x fastest; nodes = (nnx, nny, nnz) -> (3, nn)"""
+    inp (7, nn) tensor (residual, V-cycle answer, log10 viscosity), node order x fastest;
+    nodes = (nnx, nny, nnz) -> (3, nn)"""
     nnx, nny, nnz = nodes
     px, py, pz = (padded(n, levels) for n in nodes)
     bfon = emulate_bf16
-    grid = inp.reshape(4, nnz, nny, nnx)
+    grid = inp.reshape(7, nnz, nny, nnx)
     x = torch.cat([F.pad(grid, (0, px - nnx, 0, py - nny, 0, pz - nnz)).unsqueeze(0),
-                   torch.zeros(1, IN_CHANNELS - 4, pz, py, px)], dim=1)
+                   torch.zeros(1, IN_CHANNELS - 7, pz, py, px)], dim=1)
     x = _bf(x, bfon)
 
     def conv(t, k):
@@ -85,7 +86,7 @@ def forward_t(layers, hw, hb, inp, nodes, levels, emulate_bf16=True):
 
 
 def value_and_grads(params, inp, grad_out, nodes, levels, base, emulate_bf16=True):
-    """(output (3, nn), parameter gradient (flat), input gradient (4, nn)) of <output, grad_out>"""
+    """(output (3, nn), parameter gradient (flat), input gradient (7, nn)) of <output, grad_out>"""
     p = torch.tensor(np.asarray(params, dtype=np.float32), requires_grad=True)
     x = torch.tensor(np.asarray(inp, dtype=np.float32), requires_grad=True)
     ch, shapes = layer_shapes(levels, base)

@@ -68,7 +68,7 @@ def test_unet_forward_backward_match_reference(uw, nel, levels, base):
     rng = np.random.default_rng(11)
     # (a) quantized
     params = _quantized_params(R, levels, base, rng)
-    inp = (rng.integers(-3, 4, (4, nn)) / 2.0).astype(np.float32)
+    inp = (rng.integers(-3, 4, (7, nn)) / 2.0).astype(np.float32)
     gout = (rng.integers(-3, 4, (3, nn)) / 4.0).astype(np.float32)
     p0, out, gp, gi = _gpu_pass(U, nel, levels, base, params, inp, gout)
     assert p0.size == R.param_count(levels, base)
@@ -86,7 +86,7 @@ def test_unet_forward_backward_match_reference(uw, nel, levels, base):
     # (b) random FP32 data, He-scaled weights
     params = p0.copy()
     params[-3 * base - 3:] = rng.standard_normal(3 * base + 3).astype(np.float32) * 0.3
-    inp = rng.standard_normal((4, nn)).astype(np.float32)
+    inp = rng.standard_normal((7, nn)).astype(np.float32)
     gout = rng.standard_normal((3, nn)).astype(np.float32)
     _, out, gp, gi = _gpu_pass(U, nel, levels, base, params, inp, gout)
     rout, rgp, rgi = R.value_and_grads(params, inp, gout, nodes, levels, base, emulate_bf16=True)
@@ -114,8 +114,8 @@ def test_learned_preconditioner_training_and_ablation(uw):
         ctx.assemble()
         u0, p0, r0 = ctx.solve_bsscr(opts)
         ctx.learned_create(levels=3, base=8, seed=1)
-        ctx.learned_generate(opts, nsamples=96, seed=5)
-        loss, holdout = ctx.learned_train(epochs=25, batch=4, lr=2e-3, seed=2)
+        ctx.learned_generate(opts, nsamples=160, seed=5)
+        loss, holdout = ctx.learned_train(epochs=40, batch=8, lr=2e-3, seed=2)
         opts.learned_pc = 1
         u1, p1, r1 = ctx.solve_bsscr(opts)
     print(f"\nU-Net: train loss {loss:.3f}, held-out error ratio {holdout:.3f}; "
