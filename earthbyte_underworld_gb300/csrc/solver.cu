@@ -1021,10 +1021,12 @@ void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
 }
 
 // Training pairs for the learned correction, produced by the multigrid solver of the assembled
-// system: a random multi-scale velocity field e (zero on Dirichlet dofs), its residual r = K e
-// (the residual of the zero guess, so e is exactly the error), and one V-cycle v = V(r) of the
-// solver's own hierarchy; the network learns the error the V-cycle leaves, e - V(r), from r and
-// the viscosity.  Returns the number of samples added.
+// system.  For each right-hand side b (the assembled buoyancy force first, then random
+// multi-scale fields, zero on Dirichlet dofs) the exact solution u* is computed by a tight
+// FGMRES solve, and the plain multigrid iteration u <- u + V(b - K u) is run from u = 0.  Every
+// iterate gives one pair: inputs the residual r = b - K u and the V-cycle's answer V(r), target
+// the error left after that cycle, u* - u - V(r).  Late iterates carry the slowly converging
+// modes that a velocity solve spends its iterations on.  Returns the number of pairs.
 int learned_generate(Context& c, const uwgpu_solve_opts& o, int nsamples, uint64_t seed) {
     UWG_REQUIRE(c.assembled, UWGPU_ERR_STATE, "training data requested before assembly");
     UWG_REQUIRE(c.net != nullptr, UWGPU_ERR_STATE, "no network (uwgpu_learned_create)");
@@ -1034,20 +1036,39 @@ int learned_generate(Context& c, const uwgpu_solve_opts& o, int nsamples, uint64
     std::memset(&rep, 0, sizeof(rep));
     uwgpu_solve_opts o64 = o;
     o64.precision = UWGPU_PREC_FP64;
+    o64.learned_pc = 0;
     Bsscr s(c, o64, rep);
     s.setup_velocity();
+    s.gm64.setup(s.nv, o64.restart > 0 ? o64.restart : 30);
     unet::Net& n = *c.net;
-    const int64_t nv = c.mesh.nn * 3;
-    DArray<double> e, r, v;
-    e.ensure(nv);
-    r.ensure(nv);
-    v.ensure(nv);
+    const int64_t nv = s.nv;
+    const int per_rhs = 12;   // multigrid iterates per right-hand side
+    DArray<double> b, us, u, r, v, e;
+    for (auto* a : {&b, &us, &u, &r, &v, &e}) a->ensure(nv);
     unet::dataset_reserve(c, n, nsamples);
-    for (int k = 0; k < nsamples; ++k) {
-        unet::random_field(c, n, seed + (uint64_t)k, e.p);
-        level_apply<double>(c, c.levels[0], e.p, r.p);
-        s.vcycle<double>(0, r.p, v.p);
-        unet::dataset_add(c, n, r.p, e.p, v.p);
+    const Level& L0 = c.levels[0];
+    for (int src = 0; n.nsamples < nsamples; ++src) {
+        if (src == 0) gather_force(c, b.p);
+        else unet::random_field(c, n, seed + (uint64_t)src, b.p);
+        double res = 0.0, bn = 0.0;
+        bool nanflag = false;
+        s.gm64.solve([&](const double* in, double* out) { level_apply<double>(c, L0, in, out); },
+                     [&](const double* in, double* out) { s.vcycle<double>(0, in, out); }, b.p, us.p, 1e-11,
+                     o64.max_inner > 0 ? o64.max_inner : 500, &res, &bn, &nanflag);
+        UWG_REQUIRE(!nanflag, UWGPU_ERR_NAN, "NaN while generating training pairs");
+        if (!(bn > 0.0)) continue;
+        zero<double>(c, nv, u.p);
+        const double un = s.red.norm<double>(nv, us.p);
+        for (int k = 0; k < per_rhs && n.nsamples < nsamples; ++k) {
+            level_residual<double>(c, L0, u.p, b.p, r.p);
+            s.vcycle<double>(0, r.p, v.p);
+            // e = u* - u (error before the cycle); the stored target is e - V(r)
+            copy<double>(c, nv, us.p, e.p);
+            axpy<double>(c, nv, -1.0, u.p, e.p);
+            unet::dataset_add(c, n, r.p, e.p, v.p);
+            axpy<double>(c, nv, 1.0, v.p, u.p);
+            if (s.red.norm<double>(nv, e.p) <= 1e-8 * un) break;
+        }
     }
     unet::dataset_finish(c, n);
     return n.nsamples;
