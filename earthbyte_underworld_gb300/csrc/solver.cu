@@ -313,8 +313,10 @@ struct Fgmres {
         y.assign(m, 0.0);
         hcol.assign(m + 1, 0.0);
     }
-    // residual estimate after each iteration of the current solve (read by adaptive preconditioners)
+    // residual estimate after each iteration of the current solve, and the position of the
+    // current iteration in its restart cycle (read by adaptive preconditioners)
     std::vector<double> hist;
+    int cycle_k = 0;
 
     // A(x, y): y = A x ; M(v, z): z = M^{-1} v.  Returns iterations; *res = final ||r||.
     template <typename Aop, typename Mop>
@@ -358,6 +360,7 @@ struct Fgmres {
             for (; k < m && its < maxit; ++k) {
                 T* vk = V.p + (int64_t)k * n;
                 T* zk = Z.p + (int64_t)k * n;
+                cycle_k = k;
                 M(vk, zk);
                 A(zk, w.p);
                 // CGS2
@@ -470,10 +473,13 @@ struct Bsscr {
         if (o.smoother == UWGPU_SMOOTHER_CHEBYSHEV) estimate_lmax();
     }
 
-    // ---- learned correction of the V-cycle (unet.cu): M(r) = V(r) + N(r) ----
-    // Active while the velocity FGMRES makes progress; after `learned_stagnation` consecutive
-    // iterations that reduce the residual estimate by less than 5%, the rest of that velocity
-    // solve uses the plain V-cycle (the multigrid fallback).
+    // ---- learned correction of the V-cycle (unet.cu): M(r) = V(r) + N(r, V(r)) ----
+    // The network is trained on residuals of the multigrid iteration, so it is applied where
+    // FGMRES hands the preconditioner a true (scaled) residual: the first iteration of each
+    // restart cycle; the other Krylov directions get the plain V-cycle.  It stays active while
+    // the velocity FGMRES makes progress; after `learned_stagnation` consecutive iterations that
+    // reduce the residual estimate by less than 5%, the rest of that velocity solve uses the
+    // plain V-cycle (the multigrid fallback).
     bool learned = false;      // requested and a network exists
     bool learned_on = false;   // within the current velocity solve
     template <typename T>
@@ -489,11 +495,11 @@ struct Bsscr {
         rep.learned_fallbacks++;
     }
     template <typename T>
-    void precondition(const T* in, T* out, const std::vector<double>& hist) {
+    void precondition(const T* in, T* out, const std::vector<double>& hist, int cycle_k) {
         vcycle<T>(0, in, out);
         rep.vcycles++;
         learned_check<T>(hist);
-        if (learned_on) {
+        if (learned_on && cycle_k == 0) {
             unet::correct<T>(c, *c.net, in, out);
             rep.learned_applies++;
         }
@@ -570,7 +576,7 @@ struct Bsscr {
             bool nn = false;
             learned_on = learned;
             its = gm64.solve([&](const double* in, double* out) { level_apply<double>(c, L0, in, out); },
-                             [&](const double* in, double* out) { precondition<double>(in, out, gm64.hist); },
+                             [&](const double* in, double* out) { precondition<double>(in, out, gm64.hist, gm64.cycle_k); },
                              b, x, rtol, maxit, &res, &bn, &nn);
             if (nn) nan = true;
             if (!(res <= rtol * bn * 1.0000001) && bn > 0) inner_fail = true;
@@ -591,7 +597,7 @@ struct Bsscr {
                 bool nn = false;
                 double inner_rtol = std::max(rtol * bn / rn, 1e-4);
                 int k = gm32.solve([&](const float* in, float* out) { level_apply<float>(c, L0, in, out); },
-                                   [&](const float* in, float* out) { precondition<float>(in, out, gm32.hist); },
+                                   [&](const float* in, float* out) { precondition<float>(in, out, gm32.hist, gm32.cycle_k); },
                                    r32.p, d32.p, std::min(inner_rtol, 0.5), maxit - its, &res, &b32n, &nn);
                 its += k;
                 if (nn) { nan = true; break; }
