@@ -1049,8 +1049,8 @@ int learned_generate(Context& c, const uwgpu_solve_opts& o, int nsamples, uint64
     unet::Net& n = *c.net;
     const int64_t nv = s.nv;
     const int per_rhs = 12;   // multigrid iterates per right-hand side
-    DArray<double> b, us, u, r, v, e, kv;
-    for (auto* a : {&b, &us, &u, &r, &v, &e, &kv}) a->ensure(nv);
+    DArray<double> b, us, u, r, v, e;
+    for (auto* a : {&b, &us, &u, &r, &v, &e}) a->ensure(nv);
     unet::dataset_reserve(c, n, nsamples);
     const Level& L0 = c.levels[0];
     for (int src = 0; n.nsamples < nsamples; ++src) {
@@ -1071,8 +1071,7 @@ int learned_generate(Context& c, const uwgpu_solve_opts& o, int nsamples, uint64
             // e = u* - u (error before the cycle); the stored target is e - V(r)
             copy<double>(c, nv, us.p, e.p);
             axpy<double>(c, nv, -1.0, u.p, e.p);
-            level_apply<double>(c, L0, v.p, kv.p);
-            unet::dataset_add(c, n, r.p, e.p, v.p, kv.p);
+            unet::dataset_add(c, n, r.p, e.p, v.p);
             axpy<double>(c, nv, 1.0, v.p, u.p);
             if (s.red.norm<double>(nv, e.p) <= 1e-8 * un) break;
         }

@@ -870,21 +870,6 @@ void random_field(Context& c, Net& n, uint64_t seed, double* e) {
     UWG_CUDA(cudaStreamSynchronize(c.stream));   // the host mode table is released on return
 }
 
-// sum of ((a - b) / rms)^2 with rms^2 = sumsq_v[0] / n (the RMS of the V-cycle answer)
-__global__ void k_diff_sumsq(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
-                             const double* __restrict__ sumsq_v, double* __restrict__ out) {
-    __shared__ float inv2;
-    if (threadIdx.x == 0) inv2 = sumsq_v[0] > 0.0 ? (float)((double)n / sumsq_v[0]) : 0.0f;
-    __syncthreads();
-    float s = 0.0f;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float d = (float)(a[i] - b[i]);
-        s = fmaf(d, d, s);
-    }
-    s = warp_sum(s) * inv2;
-    if ((threadIdx.x & 31) == 0) atomicAdd(out, (double)s);
-}
-
 // sample k: xs = (r / rms(r), v / rms(v)) (FP32, [6][nn]), ys = (e - v) / rms(v) ([3][nn])
 __global__ void k_store_sample(int64_t n3, const double* __restrict__ r, const double* __restrict__ e,
                                const double* __restrict__ v, const double* __restrict__ sumsq, int64_t nvec,
@@ -908,7 +893,7 @@ void dataset_reserve(Context& c, Net& n, int nsamples) {
     prepare_viscosity(c, n);
 }
 
-void dataset_add(Context& c, Net& n, const double* r, const double* e, const double* v, const double* kv) {
+void dataset_add(Context& c, Net& n, const double* r, const double* e, const double* v) {
     const int k = n.nsamples;
     UWG_REQUIRE((size_t)k < n.ysq.size(), UWGPU_ERR_ARGUMENT, "training set is full");
     n.sumsq.ensure(2);
@@ -925,11 +910,10 @@ void dataset_add(Context& c, Net& n, const double* r, const double* e, const dou
         LaunchScope ls(c, -1);
         k_store_sample<<<nblk(n3, 256), 256, 0, c.stream>>>(n3, r, e, v, n.sumsq.p, n3, xs, ys);
     }
-    // |K y|^2 with K y = (r - K v) / rms(v): the residual the plain cycle leaves, scaled
     UWG_CUDA(cudaMemsetAsync(n.sumsq.p, 0, sizeof(double), c.stream));
     {
         LaunchScope ls(c, -1);
-        k_diff_sumsq<<<304, 256, 0, c.stream>>>(n3, r, kv, n.sumsq.p + 1, n.sumsq.p);
+        k_sumsq<float><<<304, 256, 0, c.stream>>>(n3, ys, n.sumsq.p);
     }
     double h = 0.0;
     UWG_CUDA(cudaMemcpyAsync(&h, n.sumsq.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -946,18 +930,9 @@ __global__ void k_scale_f(int64_t n, float a, float* __restrict__ x) {
 // the network's targets are scaled to unit RMS; out_scale maps its output back
 void dataset_finish(Context& c, Net& n) {
     UWG_REQUIRE(n.nsamples > 0, UWGPU_ERR_STATE, "empty training set");
-    DArray<double> acc;
-    acc.ensure(1);
-    UWG_CUDA(cudaMemsetAsync(acc.p, 0, sizeof(double), c.stream));
-    const int64_t all = (int64_t)n.nsamples * 3 * n.nn;
-    {
-        LaunchScope ls(c, -1);
-        k_sumsq<float><<<608, 256, 0, c.stream>>>(all, n.data_y.p, acc.p);
-    }
     double tot = 0.0;
-    UWG_CUDA(cudaMemcpyAsync(&tot, acc.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-    UWG_CUDA(cudaStreamSynchronize(c.stream));
-    const double rms = std::sqrt(tot / (double)all);
+    for (int k = 0; k < n.nsamples; ++k) tot += n.ysq[(size_t)k];
+    const double rms = std::sqrt(tot / ((double)n.nsamples * 3.0 * n.nn));
     UWG_REQUIRE(rms > 0.0 && std::isfinite(rms), UWGPU_ERR_NAN, "training targets are zero or not finite");
     n.out_scale = (float)rms;
     const int64_t tot_n = (int64_t)n.nsamples * 3 * n.nn;
@@ -980,35 +955,23 @@ __global__ void k_sample_input(int64_t nnx, int64_t nny, int64_t nn, Vol g, cons
     x0[v * kInChannels + 6] = __float2bfloat16_rn(logeta[node]);
 }
 
-// d = out - y at node dofs (0 on fixed dofs), node layout [3][nn]
-__global__ void k_out_minus_target(int64_t nnx, int64_t nny, int64_t nn, Vol g, const float* __restrict__ out,
-                                   const float* __restrict__ y, const uint8_t* __restrict__ fixed,
-                                   float* __restrict__ d) {
-    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (node >= nn) return;
-    const int64_t v = node_voxel(node, nnx, nny, g);
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-        d[(int64_t)c * nn + node] =
-            (fixed && fixed[node * 3 + c]) ? 0.0f : out[(int64_t)c * g.nv + v] - y[(int64_t)c * nn + node];
-}
-
-// loss += scale |kd|^2 ; gout (voxel layout) = 2 scale kkd at node voxels
-__global__ void k_residual_loss(int64_t nnx, int64_t nny, int64_t nn, Vol g, const float* __restrict__ kd,
-                                const float* __restrict__ kkd, float scale, float* __restrict__ gout,
-                                double* __restrict__ loss) {
+// loss += |out - y|^2 / ysq over free dofs; gout = 2 (out - y) / ysq there (0 elsewhere)
+__global__ void k_rel_mse(int64_t nnx, int64_t nny, int64_t nn, Vol g, const float* __restrict__ out,
+                          const float* __restrict__ y, const uint8_t* __restrict__ fixed, float inv_ysq,
+                          float* __restrict__ gout, double* __restrict__ loss) {
     const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     float l = 0.0f;
     if (node < nn) {
         const int64_t v = node_voxel(node, nnx, nny, g);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const float a = kd[(int64_t)c * nn + node];
-            l = fmaf(a, a, l);
-            gout[(int64_t)c * g.nv + v] = 2.0f * scale * kkd[(int64_t)c * nn + node];
+        for (int d = 0; d < 3; ++d) {
+            float diff = out[(int64_t)d * g.nv + v] - y[(int64_t)d * nn + node];
+            if (fixed && fixed[node * 3 + d]) diff = 0.0f;
+            gout[(int64_t)d * g.nv + v] = 2.0f * diff * inv_ysq;
+            l = fmaf(diff * diff, inv_ysq, l);
         }
     }
-    l = warp_sum(l) * scale;
+    l = warp_sum(l);
     if ((threadIdx.x & 31) == 0 && loss) atomicAdd(loss, (double)l);
 }
 
@@ -1021,21 +984,13 @@ static void sample_step(Context& c, Net& n, int k, bool train, double* dloss) {
                                                                n.logeta.p, n.x0.p);
     }
     forward(c, n);
-    // the residual the corrected cycle leaves, relative to the plain cycle's: |K(out - y)|^2 / |K y|^2
     UWG_CUDA(cudaMemsetAsync(n.gout.p, 0, (size_t)n.vol[0].nv * 3 * sizeof(float), c.stream));
-    const Level& L0 = c.levels[0];
     {
         LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
-        k_out_minus_target<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], n.out.p,
-                                                                   n.data_y.p + (size_t)k * n3, L0.fixed.p, n.dnode.p);
-    }
-    level_apply<float>(c, L0, n.dnode.p, n.kd.p);
-    level_apply<float>(c, L0, n.kd.p, n.kkd.p);   // K is symmetric: the gradient of |K d|^2 is 2 K K d
-    {
-        LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
-        const double ksq = n.ysq[(size_t)k];
-        k_residual_loss<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], n.kd.p, n.kkd.p,
-                                                                ksq > 0.0 ? (float)(1.0 / ksq) : 0.0f, n.gout.p, dloss);
+        const double ysq = n.ysq[(size_t)k];
+        k_rel_mse<<<nblk(n.nn, 256), 256, 0, c.stream>>>(n.nnx, n.nny, n.nn, n.vol[0], n.out.p, n.data_y.p + (size_t)k * n3,
+                                                          c.levels[0].fixed.p, ysq > 0.0 ? (float)(1.0 / ysq) : 0.0f,
+                                                          n.gout.p, dloss);
     }
     if (train) backward(c, n);
 }
@@ -1043,9 +998,6 @@ static void sample_step(Context& c, Net& n, int k, bool train, double* dloss) {
 void train(Context& c, Net& n, int epochs, int batch, float lr, uint64_t seed, double* train_loss,
            double* holdout_ratio) {
     UWG_REQUIRE(n.nsamples >= 2, UWGPU_ERR_STATE, "training needs at least two samples (learned_generate)");
-    UWG_REQUIRE(c.operator_built, UWGPU_ERR_STATE, "training needs the velocity operator (learned_generate)");
-    if (!c.operator_has32) build_operator(c, c.operator_levels, true);   // FP32 K for the loss
-    for (auto* a : {&n.dnode, &n.kd, &n.kkd}) a->ensure((size_t)3 * n.nn);
     UWG_REQUIRE(epochs >= 0 && batch >= 1, UWGPU_ERR_ARGUMENT, "bad epochs or batch");
     const int nhold = std::max(1, n.nsamples / 10);
     const int ntrain = n.nsamples - nhold;

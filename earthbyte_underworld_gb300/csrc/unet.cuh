@@ -45,8 +45,7 @@ struct Net {
     // training set: inputs (r/rms(r), V(r)/rms(V(r))) [sample][6][nn] and targets
     // (e - V(r))/rms(V(r))/out_scale [sample][3][nn]
     DArray<float> data_x, data_y;
-    std::vector<double> ysq;                      // |K target|^2 per sample (residual of the plain cycle)
-    DArray<float> dnode, kd, kkd;                 // loss scratch: out - target, K of it, K K of it
+    std::vector<double> ysq;                      // |target|^2 per sample
     int nsamples = 0;
     DArray<unsigned char> modes;                  // random-field mode table
 
@@ -88,10 +87,9 @@ void correct(Context& c, Net& n, const T* r, T* z);
 // random multi-scale velocity field (0 on fixed dofs) into e[3][nn]
 void random_field(Context& c, Net& n, uint64_t seed, double* e);
 void dataset_reserve(Context& c, Net& n, int nsamples);
-void dataset_add(Context& c, Net& n, const double* r, const double* e, const double* v, const double* kv);
+void dataset_add(Context& c, Net& n, const double* r, const double* e, const double* v);
 void dataset_finish(Context& c, Net& n);
-// Adam on |K (target - N)|^2 / |K target|^2, the residual the corrected V-cycle leaves relative to
-// the plain V-cycle's; the last 10% of the samples are held out
+// Adam on the relative squared error; the last 10% of the samples are held out
 void train(Context& c, Net& n, int epochs, int batch, float lr, uint64_t seed, double* train_loss,
            double* holdout_ratio);
 

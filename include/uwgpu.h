@@ -301,10 +301,9 @@ int uwgpu_learned_backward(uwgpu_ctx* ctx, const float* grad_output, float* grad
  * solver (random velocity fields e, r = K e, inputs r and V(r), target e - V(r) for one V-cycle V
  * of the hierarchy `opts` describes); replaces any previous set. */
 int uwgpu_learned_generate(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, int32_t nsamples, uint64_t seed);
-/* Adam on |K(target - N)|^2 / |K target|^2 per pair: the squared residual the corrected cycle
- * V + N leaves relative to the plain V-cycle's.  The last 10% of the pairs are held out.
- * train_loss: that ratio averaged over the last epoch; holdout_ratio: the same on the held-out
- * pairs (below 1: the corrected cycle leaves a smaller residual than the plain V-cycle). */
+/* Adam on the relative squared error of the correction; the last 10% of the samples are held
+ * out.  train_loss: mean relative error of the last epoch; holdout_ratio: |target - N|^2/|target|^2
+ * on the held-out pairs (below 1: the network reduces the error the V-cycle leaves). */
 int uwgpu_learned_train(uwgpu_ctx* ctx, int32_t epochs, int32_t batch, float learning_rate, uint64_t seed,
                         double* train_loss, double* holdout_ratio);
 
