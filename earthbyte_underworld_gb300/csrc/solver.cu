@@ -473,7 +473,7 @@ struct Bsscr {
         if (o.smoother == UWGPU_SMOOTHER_CHEBYSHEV) estimate_lmax();
     }
 
-    // ---- learned correction of the V-cycle (unet.cu): M(r) = V(r) + N(r, V(r)) ----
+    // ---- learned correction of the V-cycle (unet.cu): M(r) = S(V(r) + N(r, V(r))) ----
     // The network is trained on residuals of the multigrid iteration, so it is applied where
     // FGMRES hands the preconditioner a true (scaled) residual: the first iteration of each
     // restart cycle; the other Krylov directions get the plain V-cycle.  It stays active while
@@ -501,6 +501,13 @@ struct Bsscr {
         learned_check<T>(hist);
         if (learned_on && cycle_k == 0) {
             unet::correct<T>(c, *c.net, in, out);
+            // post-smoothing on the new residual, as after a coarse-grid correction: the rough
+            // part of the network's error (its BF16 activations included) would otherwise be
+            // amplified by K; the fine level's b and x buffers are free once the V-cycle is done
+            Level& L0 = c.levels[0];
+            level_residual<T>(c, L0, out, in, lvl_b<T>(L0));
+            smooth<T>(L0, lvl_b<T>(L0), lvl_x<T>(L0), o.smooth_up > 0 ? o.smooth_up : 1, true);
+            axpy<T>(c, nv, 1.0, lvl_x<T>(L0), out);
             rep.learned_applies++;
         }
     }
