@@ -462,6 +462,39 @@ int uwgpu_time_apply(uwgpu_ctx* ctx, int32_t precision, int32_t iterations, doub
     });
 }
 
+int uwgpu_time_chebyshev(uwgpu_ctx* ctx, int32_t precision, int32_t degree, int32_t iterations, double* ms) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(ms && iterations > 0 && degree > 0, UWGPU_ERR_ARGUMENT, "bad arguments");
+        const bool f32 = precision == UWGPU_PREC_MIXED;
+        uwgpu_solve_opts o;
+        uwgpu_solve_opts_default(&o);
+        o.mg_levels = c.operator_built ? c.operator_levels : 1;
+        o.precision = f32 ? UWGPU_PREC_MIXED : UWGPU_PREC_FP64;
+        uwg::estimate_fine_lmax(c, o);
+        uwg::Level& L = c.levels[0];
+        const size_t nv = (size_t)L.mesh.nn * L.mesh.dim;
+        cudaEvent_t e0, e1;
+        UWG_CUDA(cudaEventCreate(&e0));
+        UWG_CUDA(cudaEventCreate(&e1));
+        if (f32) {
+            UWG_CUDA(cudaMemsetAsync(L.b32.p, 0, nv * sizeof(float), c.stream));
+            UWG_CUDA(cudaEventRecord(e0, c.stream));
+            for (int i = 0; i < iterations; ++i) uwg::level_cheb<float>(c, L, L.b32.p, L.x32.p, degree, true);
+        } else {
+            UWG_CUDA(cudaMemsetAsync(L.b64.p, 0, nv * sizeof(double), c.stream));
+            UWG_CUDA(cudaEventRecord(e0, c.stream));
+            for (int i = 0; i < iterations; ++i) uwg::level_cheb<double>(c, L, L.b64.p, L.x64.p, degree, true);
+        }
+        UWG_CUDA(cudaEventRecord(e1, c.stream));
+        UWG_CUDA(cudaEventSynchronize(e1));
+        float t = 0.f;
+        UWG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        *ms = t;
+    });
+}
+
 int uwgpu_time_smooth(uwgpu_ctx* ctx, int32_t precision, int32_t sweeps, int32_t iterations, double* ms) {
     return guarded(ctx, [&](Context& c) {
         UWG_REQUIRE(ms && iterations > 0 && sweeps > 0, UWGPU_ERR_ARGUMENT, "bad arguments");

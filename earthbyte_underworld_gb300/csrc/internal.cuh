@@ -245,6 +245,8 @@ void assemble(Context& c);
 void build_operator(Context& c, int levels, bool need32);
 void apply_fine(Context& c, bool fp32, const double* x, double* y);  // device SoA vectors
 void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep);
+void estimate_fine_lmax(Context& c, const uwgpu_solve_opts& o);
+template <typename T> void level_cheb(Context&, Level&, const T*, T*, int, bool);
 int learned_generate(Context& c, const uwgpu_solve_opts& o, int nsamples, uint64_t seed);
 void solve_picard(Context& c, const uwgpu_solve_opts& o, double tol, int maxit, int minit, uwgpu_report& rep,
                   int& iterations, double& residual);

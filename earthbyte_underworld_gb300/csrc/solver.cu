@@ -1033,6 +1033,16 @@ void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
     s.run();
 }
 
+// Largest eigenvalue of Dinv A on the fine level for the Chebyshev smoother (timing hooks).
+void estimate_fine_lmax(Context& c, const uwgpu_solve_opts& o) {
+    uwgpu_report rep;
+    std::memset(&rep, 0, sizeof(rep));
+    uwgpu_solve_opts oc = o;
+    oc.smoother = UWGPU_SMOOTHER_CHEBYSHEV;
+    Bsscr s(c, oc, rep);
+    s.setup_velocity();
+}
+
 // Training pairs for the learned correction, produced by the multigrid solver of the assembled
 // system.  For each right-hand side b (the assembled buoyancy force first, then random
 // multi-scale fields, zero on Dirichlet dofs) the exact solution u* is computed by a tight

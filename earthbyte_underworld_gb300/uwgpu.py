@@ -121,6 +121,7 @@ def load(build_if_missing: bool = True):
         L.uwgpu_get_stream.argtypes = [P, P]
         L.uwgpu_time_apply.argtypes = [P, C.c_int32, C.c_int32, P]
         L.uwgpu_time_smooth.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, P]
+        L.uwgpu_time_chebyshev.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, P]
         L.uwgpu_launch_count.argtypes = [P]
         L.uwgpu_launch_count.restype = C.c_int64
         L.uwgpu_learned_create.argtypes = [P, C.c_int32, C.c_int32, C.c_uint64]
@@ -328,6 +329,11 @@ class Context:
     def time_smooth(self, precision=PREC_FP64, sweeps=2, iterations=10):
         ms = C.c_double()
         self._check(self._L.uwgpu_time_smooth(self._h, precision, sweeps, iterations, C.byref(ms)))
+        return ms.value
+
+    def time_chebyshev(self, precision=PREC_FP64, degree=2, iterations=10):
+        ms = C.c_double()
+        self._check(self._L.uwgpu_time_chebyshev(self._h, precision, degree, iterations, C.byref(ms)))
         return ms.value
 
     def stream(self) -> int:

@@ -248,6 +248,10 @@ int64_t uwgpu_launch_count(const uwgpu_ctx* ctx);
  * record timing events on it. */
 int uwgpu_get_stream(uwgpu_ctx* ctx, void** stream);
 
+/* Timing hook (no reference counterpart): `iterations` Chebyshev smoothing calls of `degree`
+ * steps on the fine level (k_cheb_step, zero initial guess), total ms by CUDA events. */
+int uwgpu_time_chebyshev(uwgpu_ctx* ctx, int32_t precision, int32_t degree, int32_t iterations, double* ms);
+
 /* Kernel timing hooks (no reference counterpart; used by the benchmark and the profiles).
  * Each runs `iterations` back-to-back launches on the fine level, on vectors resident in the
  * context, and returns the elapsed device time in milliseconds (CUDA events on the context
