@@ -170,6 +170,11 @@ __global__ void __launch_bounds__(256) k_gwg_spmv(EGrid g, const T* __restrict__
     if (threadIdx.x == 0) atomicAdd(&scal[0], t);
 }
 
+// Elements per thread of the vector kernels: the block reduction (a shuffle tree, FP64 in the
+// FP64 form) is paid once per kEpt elements.  Element k of a thread is base + k * blockDim.x,
+// so every access stays coalesced.
+constexpr int kEpt = 4;
+
 // alpha = rz/pq ; x += alpha p ; r -= alpha q ; z = dinv r ; scal[rz_new] += r.z ; scal[3] += r.r
 template <typename T>
 __global__ void k_gwg_update(int64_t ne, const T* __restrict__ p, const T* __restrict__ q,
@@ -178,16 +183,20 @@ __global__ void k_gwg_update(int64_t ne, const T* __restrict__ p, const T* __res
     __shared__ double sw[32];
     __shared__ T s_alpha;
     const T alpha = block_ratio<T>(&scal[1 + parity], &scal[0], &s_alpha);
-    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t base = (int64_t)blockIdx.x * blockDim.x * kEpt + threadIdx.x;
     T rz = (T)0, rr = (T)0;
-    if (e < ne) {
-        x[e] = fma(alpha, p[e], x[e]);
-        T re = fma(-alpha, q[e], r[e]);
-        r[e] = re;
-        T ze = re * dinv[e];
-        z[e] = ze;
-        rz = re * ze;
-        rr = re * re;
+#pragma unroll
+    for (int k = 0; k < kEpt; ++k) {
+        const int64_t e = base + (int64_t)k * blockDim.x;
+        if (e < ne) {
+            x[e] = fma(alpha, p[e], x[e]);
+            T re = fma(-alpha, q[e], r[e]);
+            r[e] = re;
+            T ze = re * dinv[e];
+            z[e] = ze;
+            rz = fma(re, ze, rz);
+            rr = fma(re, re, rr);
+        }
     }
     double t1 = block_sum<T>(rz, sw);
     __syncthreads();
@@ -204,8 +213,12 @@ __global__ void k_gwg_dir(int64_t ne, const T* __restrict__ z, T* __restrict__ p
                           int parity) {
     __shared__ T s_beta;
     const T beta = block_ratio<T>(&scal[1 + (parity ^ 1)], &scal[1 + parity], &s_beta);
-    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < ne) p[e] = fma(beta, p[e], z[e]);
+    const int64_t base = (int64_t)blockIdx.x * blockDim.x * kEpt + threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < kEpt; ++k) {
+        const int64_t e = base + (int64_t)k * blockDim.x;
+        if (e < ne) p[e] = fma(beta, p[e], z[e]);
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) scal[0] = 0.0;
 }
 
@@ -306,7 +319,7 @@ static int gwg_cg_T(Context& c, const T* A, const T* dinv, const double* b, T* x
     T* p = work + 2 * ne;
     T* q = work + 3 * ne;
     UWG_CUDA(cudaMemsetAsync(scal, 0, 8 * sizeof(double), c.stream));
-    const unsigned eb = blocks_for(ne, 256);
+    const unsigned eb = blocks_for(ne, 256), eb4 = blocks_for(ne, 256 * kEpt);
     {
         LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
         k_gwg_init<T><<<eb, 256, 0, c.stream>>>(ne, b, dinv, x, r, z, p, scal);
@@ -322,8 +335,8 @@ static int gwg_cg_T(Context& c, const T* A, const T* dinv, const double* b, T* x
     auto issue = [&](int parity) {
         if (m.dim == 3) k_gwg_spmv<3, T><<<eb, 256, 0, c.stream>>>(g, A, p, q, scal, parity);
         else k_gwg_spmv<2, T><<<eb, 256, 0, c.stream>>>(g, A, p, q, scal, parity);
-        k_gwg_update<T><<<eb, 256, 0, c.stream>>>(ne, p, q, dinv, x, r, z, scal, parity);
-        k_gwg_dir<T><<<eb, 256, 0, c.stream>>>(ne, z, p, scal, parity);
+        k_gwg_update<T><<<eb4, 256, 0, c.stream>>>(ne, p, q, dinv, x, r, z, scal, parity);
+        k_gwg_dir<T><<<eb4, 256, 0, c.stream>>>(ne, z, p, scal, parity);
     };
     const void* key[8] = {A, dinv, x, work, scal, (const void*)(intptr_t)ne, (const void*)(intptr_t)sizeof(T),
                           (const void*)(intptr_t)m.dim};
