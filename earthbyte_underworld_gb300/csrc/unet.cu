@@ -102,12 +102,14 @@ __global__ void __launch_bounds__(128) k_conv3(Vol g, int cin, int cout, const T
     store8(out + v * cout + co0, acc);
 }
 
-// dW[t][ci][co] += sum_v in[v + off(t)][ci] g[v][co]  (in: BF16 activations, g: FP32 gradient of
-// the pre-activation).  grid = (voxel slices, 27 taps); each block accumulates its slice in
-// registers (output o = threadIdx.x + 256 k) and adds it to dW once.
+// part[slice][t][ci][co] = sum over the slice's voxels v of in[v + off(t)][ci] g[v][co]  (in: BF16
+// activations, g: FP32 gradient of the pre-activation).  grid = (voxel slices, 27 taps); each
+// block accumulates its slice in registers (output o = threadIdx.x + 256 k).  The slices are
+// summed in a fixed order afterwards (k_sum_slices), so the gradient is deterministic.
 constexpr int kWgThreads = 256;
 constexpr int kWgMaxPer = 64;   // cin * cout <= 256 * 64
 constexpr int kWgTile = 32;     // voxels staged per round
+constexpr int kWgSlices = 16;   // voxel slices (blocks per tap)
 __global__ void __launch_bounds__(kWgThreads) k_conv3_wgrad(Vol g, int cin, int cout, int taps,
                                                             const bf16* __restrict__ in,
                                                             const float* __restrict__ gout, float* __restrict__ dW,
@@ -155,22 +157,38 @@ __global__ void __launch_bounds__(kWgThreads) k_conv3_wgrad(Vol g, int cin, int 
             }
         }
     }
+    float* part = dW + ((int64_t)blockIdx.x * taps + t) * nout;
 #pragma unroll
     for (int k = 0; k < kWgMaxPer; ++k) {
         const int o = threadIdx.x + k * kWgThreads;
-        if (o < nout) atomicAdd(&dW[(int64_t)t * nout + o], acc[k]);
+        if (o < nout) part[o] = acc[k];
     }
 }
 
-// db[co] += sum_v g[v][co]
-__global__ void k_bias_grad(int64_t nv, int cout, const float* __restrict__ gout, float* __restrict__ db) {
-    // thread t covers channel t % cout of voxels (t / cout) + k * (threads / cout) of the block's slice
+// dst[i] += sum_s part[s][i], s ascending
+__global__ void k_sum_slices(int64_t n, int slices, const float* __restrict__ part, float* __restrict__ dst) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float a = 0.0f;
+    for (int sl = 0; sl < slices; ++sl) a += part[(int64_t)sl * n + i];
+    dst[i] += a;
+}
+
+// part[block][co] = sum over the block's voxels of g[v][co] (thread t covers channel t % cout of
+// voxels t / cout + k * lanes); the lanes are combined in shared memory in a fixed order
+__global__ void k_bias_grad(int64_t nv, int cout, const float* __restrict__ gout, float* __restrict__ part) {
+    __shared__ float sp[256];
     const int lanes = blockDim.x / cout;
     const int co = threadIdx.x % cout, sub = threadIdx.x / cout;
-    if (sub >= lanes) return;
     float a = 0.0f;
     for (int64_t v = (int64_t)blockIdx.x * lanes + sub; v < nv; v += (int64_t)gridDim.x * lanes) a += gout[v * cout + co];
-    atomicAdd(&db[co], a);
+    sp[threadIdx.x] = a;
+    __syncthreads();
+    if (threadIdx.x < cout) {
+        float b = 0.0f;
+        for (int l = 0; l < lanes; ++l) b += sp[l * cout + threadIdx.x];
+        part[(int64_t)blockIdx.x * cout + threadIdx.x] = b;
+    }
 }
 
 // g = g * (y > 0): gradient through ReLU, y the stored BF16 output of the layer
@@ -279,12 +297,12 @@ __device__ __forceinline__ float warp_sum(float v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+// part[block][0 .. 3 cin) = block sums of x[v][c] g[d][v], part[block][3 cin .. 3 cin + 3) = of g[d][v]
+// (warp sums, then the warps in a fixed order); gx[v][c] = sum_d W[c][d] g[d][v]
 __global__ void k_head_bwd(int64_t nv, int cin, const bf16* __restrict__ x, const float* __restrict__ W,
-                           const float* __restrict__ g, float* __restrict__ gx, float* __restrict__ dW,
-                           float* __restrict__ db) {
-    extern __shared__ float sacc[];   // [cin * 3 + 3]
-    for (int k = threadIdx.x; k < cin * 3 + 3; k += blockDim.x) sacc[k] = 0.0f;
-    __syncthreads();
+                           const float* __restrict__ g, float* __restrict__ gx, float* __restrict__ part) {
+    extern __shared__ float swarp[];   // [warps][cin * 3 + 3]
+    const int nq = cin * 3 + 3, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool act = v < nv;
     const float g0 = act ? g[v] : 0.0f, g1 = act ? g[nv + v] : 0.0f, g2 = act ? g[2 * nv + v] : 0.0f;
@@ -295,20 +313,23 @@ __global__ void k_head_bwd(int64_t nv, int cin, const bf16* __restrict__ x, cons
         if (act) gx[v * cin + c] = w[0] * g0 + w[1] * g1 + w[2] * g2;
         const float s0 = warp_sum(xv * g0), s1 = warp_sum(xv * g1), s2 = warp_sum(xv * g2);
         if (lead) {
-            atomicAdd(&sacc[c * 3 + 0], s0);
-            atomicAdd(&sacc[c * 3 + 1], s1);
-            atomicAdd(&sacc[c * 3 + 2], s2);
+            swarp[warp * nq + c * 3 + 0] = s0;
+            swarp[warp * nq + c * 3 + 1] = s1;
+            swarp[warp * nq + c * 3 + 2] = s2;
         }
     }
     const float t0 = warp_sum(g0), t1 = warp_sum(g1), t2 = warp_sum(g2);
     if (lead) {
-        atomicAdd(&sacc[cin * 3 + 0], t0);
-        atomicAdd(&sacc[cin * 3 + 1], t1);
-        atomicAdd(&sacc[cin * 3 + 2], t2);
+        swarp[warp * nq + cin * 3 + 0] = t0;
+        swarp[warp * nq + cin * 3 + 1] = t1;
+        swarp[warp * nq + cin * 3 + 2] = t2;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < cin * 3; k += blockDim.x) atomicAdd(&dW[k], sacc[k]);
-    for (int k = threadIdx.x; k < 3; k += blockDim.x) atomicAdd(&db[k], sacc[cin * 3 + k]);
+    for (int k = threadIdx.x; k < nq; k += blockDim.x) {
+        float a = 0.0f;
+        for (int w = 0; w < nw; ++w) a += swarp[w * nq + k];
+        part[(int64_t)blockIdx.x * nq + k] = a;
+    }
 }
 
 // FP32 master weights -> BF16 W[t][ci][co] and the flipped transpose W'[t][co][ci] = W[26-t][ci][co]
@@ -364,7 +385,8 @@ static void conv_launch(Context& c, const Vol& g, int cin, int cout, const TI* i
               2.0 * 27.0 * cin * cout * (double)g.nv);
 }
 
-static void wgrad_launch(Context& c, const Vol& g, int cin, int cout, const bf16* in, const float* gout, float* dW) {
+static void wgrad_launch(Context& c, const Vol& g, int cin, int cout, const bf16* in, const float* gout, float* dW,
+                         DArray<float>& part) {
     UWG_REQUIRE((int64_t)cin * cout <= (int64_t)kWgThreads * kWgMaxPer, UWGPU_ERR_ARGUMENT,
                 "U-Net layer too wide for the weight-gradient kernel");
     static bool attr_set = false;
@@ -372,17 +394,29 @@ static void wgrad_launch(Context& c, const Vol& g, int cin, int cout, const bf16
         UWG_CUDA(cudaFuncSetAttribute(k_conv3_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
         attr_set = true;
     }
-    const int slices = 16;
+    const int slices = kWgSlices;
     const int64_t vslice = (g.nv + slices - 1) / slices;
+    const int64_t nw = (int64_t)27 * cin * cout;
+    part.ensure((size_t)slices * nw);
+    {
+        LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+        k_conv3_wgrad<<<dim3(slices, 27), kWgThreads, wgrad_smem(cin, cout), c.stream>>>(g, cin, cout, 27, in, gout,
+                                                                                         part.p, vslice);
+    }
     LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
-    k_conv3_wgrad<<<dim3(slices, 27), kWgThreads, wgrad_smem(cin, cout), c.stream>>>(g, cin, cout, 27, in, gout, dW,
-                                                                                     vslice);
+    k_sum_slices<<<nblk(nw, 256), 256, 0, c.stream>>>(nw, slices, part.p, dW);
     note_work(c, UWGPU_KERNEL_LEARNED, (double)g.nv * 27.0 * (cin * 2 + cout * 4), 2.0 * 27.0 * cin * cout * (double)g.nv);
 }
 
-static void bias_grad_launch(Context& c, int64_t nv, int cout, const float* gout, float* db) {
+static void bias_grad_launch(Context& c, int64_t nv, int cout, const float* gout, float* db, DArray<float>& part) {
+    const int blocks = 152;
+    part.ensure((size_t)blocks * cout);
+    {
+        LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+        k_bias_grad<<<blocks, (256 / cout) * cout, 0, c.stream>>>(nv, cout, gout, part.p);
+    }
     LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
-    k_bias_grad<<<152, (256 / cout) * cout, 0, c.stream>>>(nv, cout, gout, db);
+    k_sum_slices<<<nblk(cout, 256), 256, 0, c.stream>>>(cout, blocks, part.p, db);
 }
 
 static void relu_bwd(Context& c, int64_t n, const bf16* y, float* g) {
@@ -554,8 +588,8 @@ void forward(Context& c, Net& n) {
 // gradient of its input (post-activation of the layer below) into gin
 static void conv_backward(Context& c, Net& n, const Vol& g, const Conv& cv, const bf16* in, const float* gpre,
                           float* gin) {
-    wgrad_launch(c, g, cv.cin, cv.cout, in, gpre, n.grads.p + cv.w_off);
-    bias_grad_launch(c, g.nv, cv.cout, gpre, n.grads.p + cv.b_off);
+    wgrad_launch(c, g, cv.cin, cv.cout, in, gpre, n.grads.p + cv.w_off, n.part);
+    bias_grad_launch(c, g.nv, cv.cout, gpre, n.grads.p + cv.b_off, n.part);
     conv_launch<float, float>(c, g, cv.cout, cv.cin, gpre, cv.wflip.p, nullptr, gin, false);
 }
 
@@ -565,9 +599,17 @@ void backward(Context& c, Net& n) {
     const bf16* fin = L == 1 ? n.enc_b[0].p : n.dec_b[0].p;
     float* gfin = L == 1 ? n.g_enc_b[0].p : n.g_dec_b[0].p;
     {
+        const int nq = n.ch[0] * 3 + 3;
+        const unsigned hb = nblk(f.nv, 256);
+        n.part.ensure((size_t)hb * nq);
+        {
+            LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+            k_head_bwd<<<hb, 256, (size_t)8 * nq * sizeof(float), c.stream>>>(f.nv, n.ch[0], fin, n.params.p + n.head_w,
+                                                                              n.gout.p, gfin, n.part.p);
+        }
+        // head_w and head_b are adjacent in the parameter vector: one ordered sum for both
         LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
-        k_head_bwd<<<nblk(f.nv, 256), 256, (size_t)(n.ch[0] * 3 + 3) * sizeof(float), c.stream>>>(
-            f.nv, n.ch[0], fin, n.params.p + n.head_w, n.gout.p, gfin, n.grads.p + n.head_w, n.grads.p + n.head_b);
+        k_sum_slices<<<nblk(nq, 256), 256, 0, c.stream>>>(nq, (int)hb, n.part.p, n.grads.p + n.head_w);
     }
     // skip gradients start at zero; the decoder adds into them
     for (int l = 0; l + 1 < L; ++l)
@@ -696,15 +738,25 @@ void get_input_grad_host(Context& c, Net& n, float* grad_input) {
 // ------------------------------------------------------------------------------------------
 // The network as a preconditioner: residual -> input tensor, output -> velocity correction
 // ------------------------------------------------------------------------------------------
+// out[0] += sum x^2, in a fixed order: launched as one block of 1024 threads (deterministic)
 template <typename T>
-__global__ void k_sumsq(int64_t n, const T* __restrict__ x, double* __restrict__ out) {
-    float s = 0.0f;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(1024) k_sumsq(int64_t n, const T* __restrict__ x, double* __restrict__ out) {
+    __shared__ double sw[32];
+    float sf = 0.0f;   // each thread's strided partial in FP32 (fixed order), the tree in FP64
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
         const float v = (float)x[i];
-        s = fmaf(v, v, s);
+        sf = fmaf(v, v, sf);
     }
-    s = warp_sum(s);
-    if ((threadIdx.x & 31) == 0) atomicAdd(out, (double)s);
+    double s = sf;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sw[w];
+        out[0] += t;
+    }
 }
 
 // node (i, j, k) of the mesh is voxel (i, j, k) of the padded level-0 grid
@@ -801,11 +853,11 @@ void correct(Context& c, Net& n, const T* r, T* z) {
     UWG_CUDA(cudaMemsetAsync(n.sumsq.p, 0, 2 * sizeof(double), c.stream));
     {
         LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
-        k_sumsq<T><<<304, 256, 0, c.stream>>>(3 * n.nn, r, n.sumsq.p);
+        k_sumsq<T><<<1, 1024, 0, c.stream>>>(3 * n.nn, r, n.sumsq.p);
     }
     {
         LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
-        k_sumsq<T><<<304, 256, 0, c.stream>>>(3 * n.nn, z, n.sumsq.p + 1);
+        k_sumsq<T><<<1, 1024, 0, c.stream>>>(3 * n.nn, z, n.sumsq.p + 1);
     }
     {
         LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
@@ -901,8 +953,8 @@ void dataset_add(Context& c, Net& n, const double* r, const double* e, const dou
     const int64_t n3 = 3 * n.nn;
     {
         LaunchScope ls(c, -1);
-        k_sumsq<double><<<304, 256, 0, c.stream>>>(n3, r, n.sumsq.p);
-        k_sumsq<double><<<304, 256, 0, c.stream>>>(n3, v, n.sumsq.p + 1);
+        k_sumsq<double><<<1, 1024, 0, c.stream>>>(n3, r, n.sumsq.p);
+        k_sumsq<double><<<1, 1024, 0, c.stream>>>(n3, v, n.sumsq.p + 1);
     }
     float* xs = n.data_x.p + (size_t)k * 2 * n3;
     float* ys = n.data_y.p + (size_t)k * n3;
@@ -913,7 +965,7 @@ void dataset_add(Context& c, Net& n, const double* r, const double* e, const dou
     UWG_CUDA(cudaMemsetAsync(n.sumsq.p, 0, sizeof(double), c.stream));
     {
         LaunchScope ls(c, -1);
-        k_sumsq<float><<<304, 256, 0, c.stream>>>(n3, ys, n.sumsq.p);
+        k_sumsq<float><<<1, 1024, 0, c.stream>>>(n3, ys, n.sumsq.p);
     }
     double h = 0.0;
     UWG_CUDA(cudaMemcpyAsync(&h, n.sumsq.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));

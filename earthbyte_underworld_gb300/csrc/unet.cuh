@@ -57,6 +57,7 @@ struct Net {
     // gradients (FP32)
     DArray<float> gout, g_enc_a[kMaxLevels], g_enc_b[kMaxLevels], g_in[kMaxLevels];
     DArray<float> g_dec_a[kMaxLevels], g_dec_b[kMaxLevels], g_cat[kMaxLevels];
+    DArray<float> part;                           // per-block partial gradients (ordered sums)
 
     int enc(int l, int k) const { return 2 * l + k; }
     int dec(int l, int k) const { return 2 * levels + 2 * l + k; }

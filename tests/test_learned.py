@@ -115,7 +115,7 @@ def test_learned_preconditioner_training_and_ablation(uw):
         u0, p0, r0 = ctx.solve_bsscr(opts)
         ctx.learned_create(levels=3, base=8, seed=1)
         ctx.learned_generate(opts, nsamples=192, seed=5)
-        loss, holdout = ctx.learned_train(epochs=40, batch=8, lr=2e-3, seed=2)
+        loss, holdout = ctx.learned_train(epochs=60, batch=8, lr=1e-3, seed=2)
         opts.learned_pc = 1
         u1, p1, r1 = ctx.solve_bsscr(opts)
     print(f"\nU-Net: train loss {loss:.3f}, held-out error ratio {holdout:.3f}; "
