@@ -121,7 +121,7 @@ def test_learned_preconditioner_training_and_ablation(uw):
     print(f"\nU-Net: train loss {loss:.3f}, held-out error ratio {holdout:.3f}; "
           f"V-cycles plain {r0.vcycles}, learned {r1.vcycles} ({r1.learned_applies} corrections, "
           f"{r1.learned_fallbacks} fallbacks)")
-    assert np.isfinite(loss) and holdout < 0.95
+    assert np.isfinite(loss) and holdout < 0.6   # deterministic training: 0.33 measured
     assert r1.rel_residual < 1e-5 and r1.learned_applies > 0
     assert _rel(u1, u0) < 1e-4 and _rel(p1, p0) < 1e-3
 
