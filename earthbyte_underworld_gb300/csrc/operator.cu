@@ -21,7 +21,6 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
-#include <type_traits>
 #include <cstring>
 #include <iterator>
 
@@ -237,76 +236,6 @@ __global__ void __launch_bounds__(kRowThreads) k_apply(Grid g, const T* __restri
     node_ijk<DIM>(g, n, i, j, k);
     T v = stencil_row_r<DIM, T>(g, n, i, j, k, r, A, x);
     y[(int64_t)r * g.nn + n] = b ? b[(int64_t)r * g.nn + n] - v : v;
-}
-
-// Node form for FP32: one thread per node computes all DIM rows, so each neighbour's DIM values of
-// x are gathered once per node instead of once per row (the row-split form gathers them DIM
-// times, which is the right trade in FP64, where the FP64 pipe is the limit and the extra threads
-// hide its latency; in FP32 the gathers are the cost).  Lanes are consecutive nodes, so every
-// stencil load of a warp is still one coalesced 128-byte line.
-template <int DIM, typename T>
-__device__ __forceinline__ void stencil_node(const Grid& g, int64_t n, int64_t i, int64_t j, int64_t k,
-                                             const T* __restrict__ A, const T* __restrict__ x, T out[DIM]) {
-    constexpr int NB = nblocks<DIM>();
-    const NbrOffsets o = nbr_offsets<DIM>(g, i, j, k);
-#pragma unroll
-    for (int r = 0; r < DIM; ++r) out[r] = (T)0;
-#pragma unroll
-    for (int q = 0; q < NB; ++q) {
-        const int64_t m = n + o.dx[q % 3] + o.dy[(q / 3) % 3] + o.dz[DIM == 3 ? q / 9 : 1];
-        T xm[DIM];
-#pragma unroll
-        for (int cc = 0; cc < DIM; ++cc) xm[cc] = x[(int64_t)cc * g.nn + m];
-#pragma unroll
-        for (int r = 0; r < DIM; ++r)
-#pragma unroll
-            for (int cc = 0; cc < DIM; ++cc)
-                out[r] = fma(__ldg(A + ((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n), xm[cc], out[r]);
-    }
-}
-
-// y = A x (or r = b - A x when b is given), node form
-template <int DIM, typename T>
-__global__ void __launch_bounds__(256) k_apply_node(Grid g, const T* __restrict__ A, const T* __restrict__ x,
-                                                    const T* __restrict__ b, T* __restrict__ y) {
-    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= g.nn) return;
-    int64_t i, j, k;
-    node_ijk<DIM>(g, n, i, j, k);
-    T out[DIM];
-    stencil_node<DIM, T>(g, n, i, j, k, A, x, out);
-#pragma unroll
-    for (int r = 0; r < DIM; ++r) y[(int64_t)r * g.nn + n] = b ? b[(int64_t)r * g.nn + n] - out[r] : out[r];
-}
-
-// Chebyshev step, node form (see k_cheb_step): the DIM row residuals stay in registers
-template <int DIM, typename T>
-__global__ void __launch_bounds__(256) k_cheb_node(Grid g, const T* __restrict__ A, const T* __restrict__ Dinv,
-                                                   const T* __restrict__ b, const T* __restrict__ xin,
-                                                   T* __restrict__ xout, T* __restrict__ d, T c1, T c2, int first) {
-    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= g.nn) return;
-    T res[DIM];
-#pragma unroll
-    for (int r = 0; r < DIM; ++r) res[r] = b[(int64_t)r * g.nn + n];
-    if (xin) {
-        int64_t i, j, k;
-        node_ijk<DIM>(g, n, i, j, k);
-        T ax[DIM];
-        stencil_node<DIM, T>(g, n, i, j, k, A, xin, ax);
-#pragma unroll
-        for (int r = 0; r < DIM; ++r) res[r] -= ax[r];
-    }
-#pragma unroll
-    for (int r = 0; r < DIM; ++r) {
-        T z = (T)0;
-#pragma unroll
-        for (int cc = 0; cc < DIM; ++cc) z = fma(Dinv[(int64_t)(r * DIM + cc) * g.nn + n], res[cc], z);
-        const int64_t idx = (int64_t)r * g.nn + n;
-        const T dn = first ? c2 * z : fma(c1, d[idx], c2 * z);
-        d[idx] = dn;
-        xout[idx] = (xin ? xin[idx] : (T)0) + dn;
-    }
 }
 
 // `sweeps` symmetric multicolour block Gauss-Seidel sweeps (colours ascending, then
@@ -781,14 +710,10 @@ void level_apply(Context& c, const Level& L, const T* x, T* y) {
     int D = g.dim, NB = D == 3 ? 27 : 9;
     note_work(c, UWGPU_KERNEL_APPLY, (double)g.nn * (NB * D * D + 2 * D) * sizeof(T), 2.0 * g.nn * NB * D * D);
     LaunchScope ls(c, UWGPU_KERNEL_APPLY);
-    if (std::is_same<T, float>::value) {
-        if (g.dim == 3) k_apply_node<3, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, nullptr, y);
-        else k_apply_node<2, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, nullptr, y);
-    } else if (g.dim == 3) {
+    if (g.dim == 3)
         k_apply<3, T><<<blocks_for(g.nn, kRowThreads / 3), kRowThreads, 0, c.stream>>>(g, stencil_of<T>(L), x, nullptr, y);
-    } else {
+    else
         k_apply<2, T><<<blocks_for(g.nn, kRowThreads / 2), kRowThreads, 0, c.stream>>>(g, stencil_of<T>(L), x, nullptr, y);
-    }
 }
 
 template <typename T>
@@ -797,14 +722,10 @@ void level_residual(Context& c, const Level& L, const T* x, const T* b, T* r) {
     int D = g.dim, NB = D == 3 ? 27 : 9;
     note_work(c, UWGPU_KERNEL_APPLY, (double)g.nn * (NB * D * D + 3 * D) * sizeof(T), 2.0 * g.nn * NB * D * D);
     LaunchScope ls(c, UWGPU_KERNEL_APPLY);
-    if (std::is_same<T, float>::value) {
-        if (g.dim == 3) k_apply_node<3, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, b, r);
-        else k_apply_node<2, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), x, b, r);
-    } else if (g.dim == 3) {
+    if (g.dim == 3)
         k_apply<3, T><<<blocks_for(g.nn, kRowThreads / 3), kRowThreads, 0, c.stream>>>(g, stencil_of<T>(L), x, b, r);
-    } else {
+    else
         k_apply<2, T><<<blocks_for(g.nn, kRowThreads / 2), kRowThreads, 0, c.stream>>>(g, stencil_of<T>(L), x, b, r);
-    }
 }
 
 // symmetric sweep: colours ascending then descending
@@ -914,20 +835,12 @@ void level_cheb(Context& c, Level& L, const T* b, T* x, int degree, bool zero_in
             rho = rho_new;
         }
         LaunchScope ls(c, UWGPU_KERNEL_SMOOTH);
-        if (std::is_same<T, float>::value) {
-            if (D == 3)
-                k_cheb_node<3, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), dinv_of<T>(L), b, cur,
-                                                                              dst, d, (T)c1, (T)c2, k == 0);
-            else
-                k_cheb_node<2, T><<<blocks_for(g.nn, 256), 256, 0, c.stream>>>(g, stencil_of<T>(L), dinv_of<T>(L), b, cur,
-                                                                              dst, d, (T)c1, (T)c2, k == 0);
-        } else if (D == 3) {
+        if (D == 3)
             k_cheb_step<3, T><<<blocks_for(g.nn, kRowThreads / 3), kRowThreads, 0, c.stream>>>(
                 g, stencil_of<T>(L), dinv_of<T>(L), b, cur, dst, d, (T)c1, (T)c2, k == 0);
-        } else {
+        else
             k_cheb_step<2, T><<<blocks_for(g.nn, kRowThreads / 2), kRowThreads, 0, c.stream>>>(
                 g, stencil_of<T>(L), dinv_of<T>(L), b, cur, dst, d, (T)c1, (T)c2, k == 0);
-        }
         cur = dst;
     }
     if (degree % 2 == 1) UWG_CUDA(cudaMemcpyAsync(x, alt, (size_t)g.nn * D * sizeof(T), cudaMemcpyDeviceToDevice, c.stream));
