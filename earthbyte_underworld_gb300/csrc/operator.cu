@@ -212,14 +212,27 @@ template <int DIM, typename T>
 __device__ __forceinline__ T stencil_row_r(const Grid& g, int64_t n, int64_t i, int64_t j, int64_t k, int r,
                                            const T* __restrict__ A, const T* __restrict__ x) {
     constexpr int NB = nblocks<DIM>();
+    // Loads are issued in batches of QB neighbours (all stencil and x values of the batch before
+    // its FMAs), so that enough bytes are in flight per thread to cover the memory latency:
+    // 9 neighbours in FP32, 3 in FP64 (which is limited by the FP64 pipe, not by latency).
+    constexpr int QB = sizeof(T) == 4 ? 9 : 3;
     const NbrOffsets o = nbr_offsets<DIM>(g, i, j, k);
     T out = (T)0;
 #pragma unroll
-    for (int q = 0; q < NB; ++q) {
-        int64_t m = n + o.dx[q % 3] + o.dy[(q / 3) % 3] + o.dz[DIM == 3 ? q / 9 : 1];
+    for (int q0 = 0; q0 < NB; q0 += QB) {
+        T a[QB * DIM], xv[QB * DIM];
 #pragma unroll
-        for (int cc = 0; cc < DIM; ++cc)
-            out = fma(__ldg(A + ((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n), x[(int64_t)cc * g.nn + m], out);
+        for (int qq = 0; qq < QB; ++qq) {
+            const int q = q0 + qq;
+            const int64_t m = n + o.dx[q % 3] + o.dy[(q / 3) % 3] + o.dz[DIM == 3 ? q / 9 : 1];
+#pragma unroll
+            for (int cc = 0; cc < DIM; ++cc) {
+                a[qq * DIM + cc] = __ldg(A + ((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n);
+                xv[qq * DIM + cc] = x[(int64_t)cc * g.nn + m];
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < QB * DIM; ++t) out = fma(a[t], xv[t], out);
     }
     return out;
 }
