@@ -170,7 +170,7 @@ def make_workload(nel, shuffle=True):
 # (-Q22_pc_type gtkg, Solvers/KSPSolvers/src/BSSCR/pc_ScaledGtKG.c) and FGMRES velocity solves
 # (-A11_ksp_type fgmres, Solvers/SysTest/ConvergenceTests/options-solv-mg.opt); tolerances chosen so
 # that the full Stokes residual reaches 1e-6
-SOLVE_KW = dict(mg_levels=4, smooth_down=2, smooth_up=2, smoother=1, schur_type=1, schur_pc=3, scr_rtol=1e-7, a11_rtol=1e-6,
+SOLVE_KW = dict(mg_levels=4, smooth_down=2, smooth_up=2, smoother=1, schur_type=1, schur_pc=3, scr_rtol=1e-6, a11_rtol=5e-7,
                 back_rtol=1e-7, restart=30, max_outer=500, max_inner=2000, bfbt_rtol=1e-2, bfbt_max_it=2000)
 
 

@@ -103,8 +103,9 @@ typedef struct {
                                  a vector is used only when ||G w||/||w|| < 1e-7 ||G||_inf
                                  (ksp_pressure_nullspace.c:23-176, BSSCR.c:330-347)            */
     int32_t precision;        /* UWGPU_PREC_FP64 or UWGPU_PREC_MIXED                     */
-    double target_rel_residual; /* > 0: stop the outer solve once the full Stokes residual
-                                   ||[f-Ku-Gp; h-G^T u]|| / ||[f;h]|| is below this value */
+    double target_rel_residual; /* > 0: the report's status is UWGPU_ERR_NOT_CONVERGED when the
+                                   full Stokes residual ||[f-Ku-Gp; h-G^T u]|| / ||[f;h]|| after
+                                   the solve is above this value (a check, not a stopping rule) */
     double bfbt_rtol;         /* inner G^T W G solve tolerance of the scaled BFBt preconditioner */
     int32_t bfbt_max_it;      /* inner iteration limit of those solves                   */
     int32_t smoother;         /* UWGPU_SMOOTHER_COLOUR_GS (default) or UWGPU_SMOOTHER_CHEBYSHEV:
