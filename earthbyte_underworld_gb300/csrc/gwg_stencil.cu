@@ -9,10 +9,14 @@
 // (A[q][e], entry-major, q = neighbour offset) and an iteration is then 27 FMAs per element
 // with coalesced stencil reads; the 57 MB FP64 stencil of a 64^3 mesh can stay in L2.
 //
-// CG state lives in device memory (scalars double-buffered by iteration parity), an iteration is
-// three kernels, eight iterations are captured once as a CUDA graph and replayed; the host reads
-// the residual norm after each replay.
-//   scal[0] = p.q   scal[1], scal[2] = r.z (parity)   scal[3] = r.r   scal[4] = r0.r0
+// CG state lives in device memory and an iteration k is two kernels:
+//   k_cg_update:   alpha = rz_k / pq_k; x += alpha p; r -= alpha q; z = Dinv r; rz_{k+1}, rr
+//   k_cg_spmv_dir: beta = rz_{k+1} / rz_k; p = z + beta p; q = A z + beta q (= A p); pq_{k+1}
+// (q = A p by linearity, so the direction update needs no neighbour of p and fuses into the spmv).
+// The scalars are buffered so that no kernel clears a slot another block may still read:
+//   scal[0..2] = rz (k mod 3)   scal[3..4] = pq (k mod 2)   scal[5..6] = rr (k mod 2)   scal[7] = r0.r0
+// Six iterations (so both patterns repeat) are captured once as a CUDA graph and replayed; the
+// host reads the residual norm after each replay.
 #include <algorithm>
 #include <cmath>
 #include <iterator>
@@ -170,24 +174,67 @@ __global__ void __launch_bounds__(256) k_gwg_spmv(EGrid g, const T* __restrict__
     if (threadIdx.x == 0) atomicAdd(&scal[0], t);
 }
 
+__device__ __forceinline__ double* rz_slot(double* scal, int k) { return scal + ((k % 3) + 3) % 3; }
+__device__ __forceinline__ double* pq_slot(double* scal, int k) { return scal + 3 + (((k % 2) + 2) % 2); }
+__device__ __forceinline__ double* rr_slot(double* scal, int k) { return scal + 5 + (((k % 2) + 2) % 2); }
+
+// iteration k, second kernel: p = z + beta p; q = A z + beta q; pq_{k+1} += p.q.  With first != 0
+// (before iteration 0): p = z, q = A z, pq_0.  Clears rr_{k+1}'s slot.
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) k_cg_spmv_dir(EGrid g, const T* __restrict__ A, const T* __restrict__ z,
+                                                     T* __restrict__ p, T* __restrict__ q, double* __restrict__ scal,
+                                                     int k, int first) {
+    constexpr int NB = stencil_points<DIM>();
+    __shared__ double sw[32];
+    __shared__ T s_beta;
+    const T beta = first ? (T)0 : block_ratio<T>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
+    const int ne = (int)g.ne, ex = (int)g.ex, ey = (int)g.ey, ez = (int)g.ez;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    T local = (T)0;
+    if (e < ne) {
+        const int exy = ex * ey;
+        const int ix = e % ex, iy = (e / ex) % ey, iz = DIM == 3 ? e / exy : 0;
+        const int dx[3] = {ix > 0 ? -1 : 0, 0, ix + 1 < ex ? 1 : 0};
+        const int dy[3] = {iy > 0 ? -ex : 0, 0, iy + 1 < ey ? ex : 0};
+        const int dz[3] = {DIM == 3 && iz > 0 ? -exy : 0, 0, DIM == 3 && iz + 1 < ez ? exy : 0};
+        T a[NB], x[NB];
+#pragma unroll
+        for (int t = 0; t < NB; ++t) a[t] = __ldg(A + (size_t)t * ne + e);
+#pragma unroll
+        for (int t = 0; t < NB; ++t) x[t] = __ldg(z + e + dx[t % 3] + dy[(t / 3) % 3] + dz[DIM == 3 ? t / 9 : 1]);
+        T az = (T)0;
+#pragma unroll
+        for (int t = 0; t < NB; ++t) az = fma(a[t], x[t], az);
+        const T pe = first ? x[NB / 2] : fma(beta, p[e], x[NB / 2]);
+        const T qe = first ? az : fma(beta, q[e], az);
+        p[e] = pe;
+        q[e] = qe;
+        local = pe * qe;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *rr_slot(scal, k + 1) = 0.0;
+    double t = block_sum<T>(local, sw);
+    if (threadIdx.x == 0) atomicAdd(pq_slot(scal, k + 1), t);
+}
+
 // Elements per thread of the vector kernels: the block reduction (a shuffle tree, FP64 in the
 // FP64 form) is paid once per kEpt elements.  Element k of a thread is base + k * blockDim.x,
 // so every access stays coalesced.
-constexpr int kEpt = 4;
+constexpr int kEpt = 2;
 
-// alpha = rz/pq ; x += alpha p ; r -= alpha q ; z = dinv r ; scal[rz_new] += r.z ; scal[3] += r.r
+// iteration k, first kernel: alpha = rz_k / pq_k; x += alpha p; r -= alpha q; z = dinv r;
+// rz_{k+1} += r.z; rr_k += r.r.  Clears the slots of rz_{k+2} and pq_{k+1}.
 template <typename T>
-__global__ void k_gwg_update(int64_t ne, const T* __restrict__ p, const T* __restrict__ q,
-                             const T* __restrict__ dinv, T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
-                             double* __restrict__ scal, int parity) {
+__global__ void k_cg_update(int64_t ne, const T* __restrict__ p, const T* __restrict__ q,
+                            const T* __restrict__ dinv, T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
+                            double* __restrict__ scal, int k) {
     __shared__ double sw[32];
     __shared__ T s_alpha;
-    const T alpha = block_ratio<T>(&scal[1 + parity], &scal[0], &s_alpha);
+    const T alpha = block_ratio<T>(rz_slot(scal, k), pq_slot(scal, k), &s_alpha);
     const int64_t base = (int64_t)blockIdx.x * blockDim.x * kEpt + threadIdx.x;
     T rz = (T)0, rr = (T)0;
 #pragma unroll
-    for (int k = 0; k < kEpt; ++k) {
-        const int64_t e = base + (int64_t)k * blockDim.x;
+    for (int m = 0; m < kEpt; ++m) {
+        const int64_t e = base + (int64_t)m * blockDim.x;
         if (e < ne) {
             x[e] = fma(alpha, p[e], x[e]);
             T re = fma(-alpha, q[e], r[e]);
@@ -198,34 +245,24 @@ __global__ void k_gwg_update(int64_t ne, const T* __restrict__ p, const T* __res
             rr = fma(re, re, rr);
         }
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *rz_slot(scal, k + 2) = 0.0;
+        *pq_slot(scal, k + 1) = 0.0;
+    }
     double t1 = block_sum<T>(rz, sw);
     __syncthreads();
     double t2 = block_sum<T>(rr, sw);
     if (threadIdx.x == 0) {
-        atomicAdd(&scal[1 + (parity ^ 1)], t1);
-        atomicAdd(&scal[3], t2);
+        atomicAdd(rz_slot(scal, k + 1), t1);
+        atomicAdd(rr_slot(scal, k), t2);
     }
 }
 
-// beta = rz_new/rz ; p = z + beta p ; clears p.q for the next iteration
-template <typename T>
-__global__ void k_gwg_dir(int64_t ne, const T* __restrict__ z, T* __restrict__ p, double* __restrict__ scal,
-                          int parity) {
-    __shared__ T s_beta;
-    const T beta = block_ratio<T>(&scal[1 + (parity ^ 1)], &scal[1 + parity], &s_beta);
-    const int64_t base = (int64_t)blockIdx.x * blockDim.x * kEpt + threadIdx.x;
-#pragma unroll
-    for (int k = 0; k < kEpt; ++k) {
-        const int64_t e = base + (int64_t)k * blockDim.x;
-        if (e < ne) p[e] = fma(beta, p[e], z[e]);
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) scal[0] = 0.0;
-}
-
-// r = b, z = dinv r, p = z, x = 0 ; scal[1] = r.z, scal[3] = scal[4] = r.r (scal zeroed before)
+// r = b, z = dinv r, x = 0 ; rz_0 (scal[0]) = r.z, scal[7] = r0.r0 (scal zeroed before; p and q
+// are formed by the first k_cg_spmv_dir)
 template <typename T>
 __global__ void k_gwg_init(int64_t ne, const double* __restrict__ b, const T* __restrict__ dinv, T* __restrict__ x,
-                           T* __restrict__ r, T* __restrict__ z, T* __restrict__ p, double* __restrict__ scal) {
+                           T* __restrict__ r, T* __restrict__ z, double* __restrict__ scal) {
     __shared__ double sw[32];
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     T rz = (T)0, rr = (T)0;
@@ -235,7 +272,6 @@ __global__ void k_gwg_init(int64_t ne, const double* __restrict__ b, const T* __
         x[e] = (T)0;
         r[e] = re;
         z[e] = ze;
-        p[e] = ze;
         rz = re * ze;
         rr = re * re;
     }
@@ -243,9 +279,8 @@ __global__ void k_gwg_init(int64_t ne, const double* __restrict__ b, const T* __
     __syncthreads();
     double t2 = block_sum<T>(rr, sw);
     if (threadIdx.x == 0) {
-        atomicAdd(&scal[1], t1);
-        atomicAdd(&scal[3], t2);
-        atomicAdd(&scal[4], t2);
+        atomicAdd(&scal[0], t1);
+        atomicAdd(&scal[7], t2);
     }
 }
 
@@ -319,27 +354,31 @@ static int gwg_cg_T(Context& c, const T* A, const T* dinv, const double* b, T* x
     T* p = work + 2 * ne;
     T* q = work + 3 * ne;
     UWG_CUDA(cudaMemsetAsync(scal, 0, 8 * sizeof(double), c.stream));
-    const unsigned eb = blocks_for(ne, 256), eb4 = blocks_for(ne, 256 * kEpt);
+    const unsigned eb = blocks_for(ne, 256), ebv = blocks_for(ne, 256 * kEpt);
     {
         LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
-        k_gwg_init<T><<<eb, 256, 0, c.stream>>>(ne, b, dinv, x, r, z, p, scal);
+        k_gwg_init<T><<<eb, 256, 0, c.stream>>>(ne, b, dinv, x, r, z, scal);
+    }
+    {
+        LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
+        if (m.dim == 3) k_cg_spmv_dir<3, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, -1, 1);
+        else k_cg_spmv_dir<2, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, -1, 1);
     }
     double* hs = c.host_scalars;
     UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     UWG_CUDA(cudaStreamSynchronize(c.stream));
-    const double r0 = std::sqrt(hs[4]);
+    const double r0 = std::sqrt(hs[7]);
     if (!(r0 > 0.0)) return 0;
-    // Eight iterations (an even number, so the scalar parity repeats) form one CUDA graph per
-    // buffer set, replayed until converged.
-    const int block = 8;
-    auto issue = [&](int parity) {
-        if (m.dim == 3) k_gwg_spmv<3, T><<<eb, 256, 0, c.stream>>>(g, A, p, q, scal, parity);
-        else k_gwg_spmv<2, T><<<eb, 256, 0, c.stream>>>(g, A, p, q, scal, parity);
-        k_gwg_update<T><<<eb4, 256, 0, c.stream>>>(ne, p, q, dinv, x, r, z, scal, parity);
-        k_gwg_dir<T><<<eb4, 256, 0, c.stream>>>(ne, z, p, scal, parity);
+    // Six iterations (the rz slots cycle with period 3, pq and rr with period 2) form one CUDA
+    // graph per buffer set, replayed until converged.
+    const int block = 6;
+    auto issue = [&](int k) {
+        k_cg_update<T><<<ebv, 256, 0, c.stream>>>(ne, p, q, dinv, x, r, z, scal, k);
+        if (m.dim == 3) k_cg_spmv_dir<3, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, 0);
+        else k_cg_spmv_dir<2, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, 0);
     };
     const void* key[8] = {A, dinv, x, work, scal, (const void*)(intptr_t)ne, (const void*)(intptr_t)sizeof(T),
-                          (const void*)(intptr_t)m.dim};
+                          (const void*)(intptr_t)(m.dim + 16)};
     Context::PcgGraph* pg = nullptr;
     for (auto& cand : c.pcg_graphs)
         if (std::equal(std::begin(key), std::end(key), std::begin(cand.key))) pg = &cand;
@@ -349,15 +388,15 @@ static int gwg_cg_T(Context& c, const T* A, const T* dinv, const double* b, T* x
         std::copy(std::begin(key), std::end(key), std::begin(pg->key));
         cudaGraph_t graph;
         UWG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < block; ++k) issue(k & 1);
+        for (int k = 0; k < block; ++k) issue(k);
         UWG_CUDA(cudaStreamEndCapture(c.stream, &graph));
         UWG_CUDA(cudaGraphInstantiate(&pg->exec, graph, 0));
         UWG_CUDA(cudaGraphDestroy(graph));
     }
-    // algorithmic traffic of one iteration: the stencil and p once, q written, the update's
-    // eight vector streams and the direction update's three
-    const double it_bytes = (double)ne * sizeof(T) * (nb + 2 + 8 + 3);
-    const double it_flops = (double)ne * (2.0 * nb + 12.0);
+    // algorithmic traffic of one iteration: update (p, q, dinv, x, r read; x, r, z written) and
+    // spmv+direction (the stencil, z, p, q read; p, q written)
+    const double it_bytes = (double)ne * sizeof(T) * (8 + nb + 5);
+    const double it_flops = (double)ne * (2.0 * nb + 14.0);
     int it = 0;
     while (it < maxit) {
         {
@@ -365,11 +404,11 @@ static int gwg_cg_T(Context& c, const T* A, const T* dinv, const double* b, T* x
             UWG_CUDA(cudaGraphLaunch(pg->exec, c.stream));
         }
         note_work(c, UWGPU_KERNEL_SCHUR_PC, block * it_bytes, block * it_flops);
-        c.launches += 3 * block - 1;
+        c.launches += 2 * block - 1;
         it += block;
         UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         UWG_CUDA(cudaStreamSynchronize(c.stream));
-        const double rn = std::sqrt(hs[3]);
+        const double rn = std::sqrt(hs[6]);   // rr of the last iteration of the block (k = 5: slot 5 + 1)
         if (!std::isfinite(rn)) throw Error(UWGPU_ERR_NAN, "NaN in the BFBt inner solve");
         if (rn <= rtol * r0) break;
     }
