@@ -15,7 +15,7 @@
 // (q = A p by linearity, so the direction update needs no neighbour of p and fuses into the spmv).
 // The scalars are buffered so that no kernel clears a slot another block may still read:
 //   scal[0..2] = rz (k mod 3)   scal[3..4] = pq (k mod 2)   scal[5..6] = rr (k mod 2)   scal[7] = r0.r0
-// Six iterations (so both patterns repeat) are captured once as a CUDA graph and replayed; the
+// Twelve iterations (so both patterns repeat) are captured once as a CUDA graph and replayed; the
 // host reads the residual norm after each replay.
 #include <algorithm>
 #include <cmath>
@@ -369,9 +369,9 @@ static int gwg_cg_T(Context& c, const T* A, const T* dinv, const double* b, T* x
     UWG_CUDA(cudaStreamSynchronize(c.stream));
     const double r0 = std::sqrt(hs[7]);
     if (!(r0 > 0.0)) return 0;
-    // Six iterations (the rz slots cycle with period 3, pq and rr with period 2) form one CUDA
-    // graph per buffer set, replayed until converged.
-    const int block = 6;
+    // Twelve iterations (the rz slots cycle with period 3, pq and rr with period 2) form one CUDA
+    // graph per buffer set, replayed until converged; the host checks the residual once per replay.
+    const int block = 12;
     auto issue = [&](int k) {
         k_cg_update<T><<<ebv, 256, 0, c.stream>>>(ne, p, q, dinv, x, r, z, scal, k);
         if (m.dim == 3) k_cg_spmv_dir<3, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, 0);
@@ -408,7 +408,7 @@ static int gwg_cg_T(Context& c, const T* A, const T* dinv, const double* b, T* x
         it += block;
         UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         UWG_CUDA(cudaStreamSynchronize(c.stream));
-        const double rn = std::sqrt(hs[6]);   // rr of the last iteration of the block (k = 5: slot 5 + 1)
+        const double rn = std::sqrt(hs[6]);   // rr of the block's last iteration (k = 11: slot 5 + 1)
         if (!std::isfinite(rn)) throw Error(UWGPU_ERR_NAN, "NaN in the BFBt inner solve");
         if (rn <= rtol * r0) break;
     }
