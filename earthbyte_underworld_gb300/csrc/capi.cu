@@ -476,14 +476,17 @@ int uwgpu_time_chebyshev(uwgpu_ctx* ctx, int32_t precision, int32_t degree, int3
         cudaEvent_t e0, e1;
         UWG_CUDA(cudaEventCreate(&e0));
         UWG_CUDA(cudaEventCreate(&e1));
+        // from the current iterate (not a zero guess), so every step applies the stencil
         if (f32) {
             UWG_CUDA(cudaMemsetAsync(L.b32.p, 0, nv * sizeof(float), c.stream));
+            UWG_CUDA(cudaMemsetAsync(L.x32.p, 0, nv * sizeof(float), c.stream));
             UWG_CUDA(cudaEventRecord(e0, c.stream));
-            for (int i = 0; i < iterations; ++i) uwg::level_cheb<float>(c, L, L.b32.p, L.x32.p, degree, true);
+            for (int i = 0; i < iterations; ++i) uwg::level_cheb<float>(c, L, L.b32.p, L.x32.p, degree, false);
         } else {
             UWG_CUDA(cudaMemsetAsync(L.b64.p, 0, nv * sizeof(double), c.stream));
+            UWG_CUDA(cudaMemsetAsync(L.x64.p, 0, nv * sizeof(double), c.stream));
             UWG_CUDA(cudaEventRecord(e0, c.stream));
-            for (int i = 0; i < iterations; ++i) uwg::level_cheb<double>(c, L, L.b64.p, L.x64.p, degree, true);
+            for (int i = 0; i < iterations; ++i) uwg::level_cheb<double>(c, L, L.b64.p, L.x64.p, degree, false);
         }
         UWG_CUDA(cudaEventRecord(e1, c.stream));
         UWG_CUDA(cudaEventSynchronize(e1));

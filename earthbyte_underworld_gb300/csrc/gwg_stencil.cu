@@ -222,11 +222,12 @@ __global__ void __launch_bounds__(256) k_cg_spmv_dir(EGrid g, const T* __restric
 constexpr int kEpt = 2;
 
 // iteration k, first kernel: alpha = rz_k / pq_k; x += alpha p; r -= alpha q; z = dinv r;
-// rz_{k+1} += r.z; rr_k += r.r.  Clears the slots of rz_{k+2} and pq_{k+1}.
+// rz_{k+1} += r.z; and, when want_rr (the host's convergence check follows), rr_k += r.r.
+// Clears the slots of rz_{k+2} and pq_{k+1}.
 template <typename T>
 __global__ void k_cg_update(int64_t ne, const T* __restrict__ p, const T* __restrict__ q,
                             const T* __restrict__ dinv, T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
-                            double* __restrict__ scal, int k) {
+                            double* __restrict__ scal, int k, int want_rr) {
     __shared__ double sw[32];
     __shared__ T s_alpha;
     const T alpha = block_ratio<T>(rz_slot(scal, k), pq_slot(scal, k), &s_alpha);
@@ -250,11 +251,11 @@ __global__ void k_cg_update(int64_t ne, const T* __restrict__ p, const T* __rest
         *pq_slot(scal, k + 1) = 0.0;
     }
     double t1 = block_sum<T>(rz, sw);
-    __syncthreads();
-    double t2 = block_sum<T>(rr, sw);
-    if (threadIdx.x == 0) {
-        atomicAdd(rz_slot(scal, k + 1), t1);
-        atomicAdd(rr_slot(scal, k), t2);
+    if (threadIdx.x == 0) atomicAdd(rz_slot(scal, k + 1), t1);
+    if (want_rr) {
+        __syncthreads();
+        double t2 = block_sum<T>(rr, sw);
+        if (threadIdx.x == 0) atomicAdd(rr_slot(scal, k), t2);
     }
 }
 
@@ -373,7 +374,7 @@ static int gwg_cg_T(Context& c, const T* A, const T* dinv, const double* b, T* x
     // graph per buffer set, replayed until converged; the host checks the residual once per replay.
     const int block = 12;
     auto issue = [&](int k) {
-        k_cg_update<T><<<ebv, 256, 0, c.stream>>>(ne, p, q, dinv, x, r, z, scal, k);
+        k_cg_update<T><<<ebv, 256, 0, c.stream>>>(ne, p, q, dinv, x, r, z, scal, k, k == block - 1);
         if (m.dim == 3) k_cg_spmv_dir<3, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, 0);
         else k_cg_spmv_dir<2, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, 0);
     };
