@@ -570,6 +570,14 @@ struct Bsscr {
         level_restrict<T>(c, L, C, r, bc);
         vcycle<T>(l + 1, bc, xc);
         level_prolong_add<T>(c, L, C, xc, x);
+        // W-cycle: a second coarse correction on the residual left by the first
+        // (PCMG's -pc_mg_cycle_type w); the coarsest solve is exact, so it is not repeated there
+        if (o.mg_cycle == 2 && l + 1 < nlev - 1) {
+            level_residual<T>(c, L, x, b, r);
+            level_restrict<T>(c, L, C, r, bc);
+            vcycle<T>(l + 1, bc, xc);
+            level_prolong_add<T>(c, L, C, xc, x);
+        }
         smooth<T>(L, b, x, o.smooth_up, false);
     }
 
@@ -1029,6 +1037,7 @@ void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
     UWG_REQUIRE(o.smoother == UWGPU_SMOOTHER_COLOUR_GS || o.smoother == UWGPU_SMOOTHER_CHEBYSHEV, UWGPU_ERR_ARGUMENT, "bad smoother");
     UWG_REQUIRE(o.remove_const_p >= 0 && o.remove_const_p <= 2, UWGPU_ERR_ARGUMENT, "bad pressure null-space mode");
     UWG_REQUIRE(o.learned_pc == 0 || o.learned_pc == 1, UWGPU_ERR_ARGUMENT, "bad learned_pc");
+    UWG_REQUIRE(o.mg_cycle == 1 || o.mg_cycle == 2, UWGPU_ERR_ARGUMENT, "mg_cycle must be 1 (V) or 2 (W)");
     Bsscr s(c, o, rep);
     s.run();
 }

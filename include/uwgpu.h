@@ -114,6 +114,9 @@ typedef struct {
                                  (uwgpu_learned_*), 0: V-cycle only (default)                */
     int32_t learned_stagnation; /* consecutive velocity iterations with < 5% residual reduction
                                  after which a velocity solve drops the U-Net (default 2)    */
+    int32_t mg_cycle;         /* coarse corrections per level visit: 1 V-cycle (default), 2 W-cycle
+                                 (-pc_mg_cycle_type v|w of the velocity PCMG)                */
+    int32_t pad0;
 } uwgpu_solve_opts;
 
 typedef struct {
@@ -250,7 +253,8 @@ int64_t uwgpu_launch_count(const uwgpu_ctx* ctx);
 int uwgpu_get_stream(uwgpu_ctx* ctx, void** stream);
 
 /* Timing hook (no reference counterpart): `iterations` Chebyshev smoothing calls of `degree`
- * steps on the fine level (k_cheb_step, zero initial guess), total ms by CUDA events. */
+ * steps on the fine level (k_cheb_step, each step a full stencil pass from the current iterate),
+ * total ms by CUDA events. */
 int uwgpu_time_chebyshev(uwgpu_ctx* ctx, int32_t precision, int32_t degree, int32_t iterations, double* ms);
 
 /* Kernel timing hooks (no reference counterpart; used by the benchmark and the profiles).
