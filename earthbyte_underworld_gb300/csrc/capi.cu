@@ -221,6 +221,28 @@ int uwgpu_particles_upload(uwgpu_ctx* ctx, int64_t n, const double* x, const dou
     });
 }
 
+int uwgpu_advect_particles(uwgpu_ctx* ctx, double dt, int32_t order, int32_t allow_first_order_fallback,
+                           uint32_t* fell_back, uint32_t* left_mesh) {
+    return guarded(ctx, [&](Context& c) {
+        uint32_t fb = 0, lm = 0;
+        uwg::advect_particles(c, dt, order, allow_first_order_fallback != 0, fb, lm);
+        if (fell_back) *fell_back = fb;
+        if (left_mesh) *left_mesh = lm;
+    });
+}
+
+int uwgpu_particles_download(uwgpu_ctx* ctx, double* x, double* y, double* z) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(c.has_points, UWGPU_ERR_STATE, "no particles");
+        const size_t n = (size_t)c.np;
+        if (x && n) UWG_CUDA(cudaMemcpyAsync(x, c.px.p, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        if (y && n) UWG_CUDA(cudaMemcpyAsync(y, c.py.p, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        if (z && n && c.mesh.dim == 3)
+            UWG_CUDA(cudaMemcpyAsync(z, c.pz.p, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
 int uwgpu_bin_and_map(uwgpu_ctx* ctx, uint32_t* perm, uint32_t* offsets, double* xi) {
     return guarded(ctx, [&](Context& c) {
         uwg::bin_and_map(c);

@@ -140,6 +140,7 @@ struct Context {
     // material points
     int64_t np = 0;
     DArray<double> px, py, pz;
+    DArray<double> qx, qy, qz;    // second coordinate set for advection (swapped in on success)
     DArray<int32_t> pmat;
     DArray<double> peta, prho;
     bool has_peta = false, has_prho = false;
@@ -246,6 +247,7 @@ void build_operator(Context& c, int levels, bool need32);
 void apply_fine(Context& c, bool fp32, const double* x, double* y);  // device SoA vectors
 void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep);
 void estimate_fine_lmax(Context& c, const uwgpu_solve_opts& o);
+void advect_particles(Context& c, double dt, int order, bool fallback, uint32_t& fell_back, uint32_t& left_mesh);
 template <typename T> void level_cheb(Context&, Level&, const T*, T*, int, bool);
 int learned_generate(Context& c, const uwgpu_solve_opts& o, int nsamples, uint64_t seed);
 void solve_picard(Context& c, const uwgpu_solve_opts& o, double tol, int maxit, int minit, uwgpu_report& rep,

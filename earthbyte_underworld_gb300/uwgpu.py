@@ -130,6 +130,8 @@ def load(build_if_missing: bool = True):
         L.uwgpu_learned_set_params.argtypes = [P, P]
         L.uwgpu_learned_forward.argtypes = [P, P, P]
         L.uwgpu_learned_backward.argtypes = [P, P, P, P]
+        L.uwgpu_advect_particles.argtypes = [P, C.c_double, C.c_int32, C.c_int32, P, P]
+        L.uwgpu_particles_download.argtypes = [P, P, P, P]
         L.uwgpu_learned_generate.argtypes = [P, P, C.c_int32, C.c_uint64]
         L.uwgpu_learned_train.argtypes = [P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P, P]
         _lib = L
@@ -243,6 +245,20 @@ class Context:
                                                    _ptr(eta), _ptr(rho)))
 
     # ---- hot path ----
+    def advect(self, dt, order=2, allow_fallback=False):
+        """advect the material points with the current velocity -> (fallbacks, points that left the mesh)"""
+        fb, lm = C.c_uint32(), C.c_uint32()
+        self._check(self._L.uwgpu_advect_particles(self._h, dt, order, 1 if allow_fallback else 0, C.byref(fb),
+                                                   C.byref(lm)))
+        return fb.value, lm.value
+
+    def particles(self):
+        """current coordinates (x, y, z) of the material points"""
+        n = self.npoints
+        x, y, z = (np.zeros(n) for _ in range(3))
+        self._check(self._L.uwgpu_particles_download(self._h, _ptr(x), _ptr(y), _ptr(z) if self.dim == 3 else None))
+        return x, y, z
+
     def bin_and_map(self, want=True):
         if not want:
             self._check(self._L.uwgpu_bin_and_map(self._h, None, None, None))

@@ -185,6 +185,20 @@ int uwgpu_particles_upload(uwgpu_ctx* ctx, int64_t n, const double* x, const dou
  * (nel+1) and xi (3 per slot).  Returns UWGPU_ERR_DOMAIN if points lie outside the mesh. */
 int uwgpu_bin_and_map(uwgpu_ctx* ctx, uint32_t* perm, uint32_t* offsets, double* xi);
 
+/* Material-point advection with the current velocity solution: _SwarmAdvector_TimeDeriv
+ * (PICellerator/MaterialPoints/src/SwarmAdvector.c:288-314) integrated by TimeIntegrand_FirstOrder
+ * (order 1) or TimeIntegrand_SecondOrder (order 2, StgDomain/Utils/src/TimeIntegrand.c:221-337).
+ * A point with no velocity (outside the mesh; with order 2 also a predictor outside the mesh
+ * unless allow_first_order_fallback) makes the call return UWGPU_ERR_DOMAIN and leaves every
+ * point where it was.  fell_back: points updated to first order; left_mesh: points now outside
+ * the mesh (the next uwgpu_bin_and_map refuses them).  The positions change on the device: the
+ * next uwgpu_bin_and_map redoes the ownership (SwarmAdvector_AdvectionFinish,
+ * SwarmAdvector.c:375-382). */
+int uwgpu_advect_particles(uwgpu_ctx* ctx, double dt, int32_t order, int32_t allow_first_order_fallback,
+                           uint32_t* fell_back, uint32_t* left_mesh);
+/* Current particle coordinates to host arrays (n each; z ignored in 2D). */
+int uwgpu_particles_download(uwgpu_ctx* ctx, double* x, double* y, double* z);
+
 /* Element assembly of every element: replaces the StiffnessMatrix assemble entry point
  * (StgFEM/SLE/SystemSetup/src/StiffnessMatrix.c:799-1017) for the terms
  * ConstitutiveMatrixCartesian (Underworld/Rheology/src/ConstitutiveMatrixCartesian.c:202-412),

@@ -260,6 +260,16 @@ def solve_bsscr(m, fixed, Ke, Ge, fe, Se, mg_levels=3, smooth=2, schur_type=1, s
     return u, p, rep
 
 
+def advect(m, u_nodal, xyz, dt, order=2, allow_fallback=False):
+    """SwarmAdvector step (first or second order) -> (new positions (n, 3), failed, fallbacks)"""
+    out = np.ascontiguousarray(xyz, dtype=np.float64).copy()
+    fb = C.c_int64()
+    lib().uwr_advect.restype = C.c_int64
+    failed = lib().uwr_advect(C.byref(m), _p(np.ascontiguousarray(u_nodal, dtype=np.float64)), out.shape[0], _p(out),
+                              C.c_double(dt), order, 1 if allow_fallback else 0, C.byref(fb))
+    return out, int(failed), fb.value
+
+
 def free_slip_mask(m):
     """Free-slip walls: the normal velocity component is fixed on every wall."""
     nn = num_nodes(m)

@@ -175,6 +175,62 @@ int uwr_search_element(const uwr_mesh* m, const double* pt, uint32_t* el) {
     return 1;
 }
 
+/* Velocity at a point: FieldVariable_InterpolateValueAt -> _FeVariable_InterpolateValueAt
+ * (StgFEM/Discretisation/src/FeVariable.c:773-800): element search, global->local (Newton), Q1
+ * shape functions on the element's nodal values.  u_nodal is node-major (node * dim + d). */
+static int velocity_at(const uwr_mesh* m, const double* u_nodal, const double* pt, double* v) {
+    uint32_t e;
+    if (!uwr_search_element(m, pt, &e)) return 0;
+    double xi[3] = {0, 0, 0}, N[8];
+    int64_t inc[8];
+    uwr_global_to_local(m, e, pt, xi);
+    uwr_shape(m->dim, xi, N);
+    uwr_element_nodes(m, e, inc);
+    int nen = m->dim == 3 ? 8 : 4;
+    for (int d = 0; d < m->dim; ++d) {
+        v[d] = 0.0;
+        for (int a = 0; a < nen; ++a) v[d] += N[a] * u_nodal[inc[a] * m->dim + d];
+    }
+    return 1;
+}
+
+/* Particle advection: _SwarmAdvector_TimeDeriv (PICellerator/MaterialPoints/src/SwarmAdvector.c:
+ * 288-314) in TimeIntegrand_FirstOrder (StgDomain/Utils/src/TimeIntegrand.c:221-265,
+ * x = x0 + dt v(x0)) or TimeIntegrand_SecondOrder (:267-337: predictor x0 + dt/2 v(x0), then
+ * x0 + dt v(predictor); a predictor outside the mesh falls back to the first-order update when
+ * allowed).  Points are independent.  Returns the number of points whose velocity could not be
+ * found (the reference stops there); such points are left unmoved. */
+int64_t uwr_advect(const uwr_mesh* m, const double* u_nodal, int64_t n, double* xyz, double dt, int32_t order,
+                   int32_t allow_fallback, int64_t* fallbacks) {
+    int64_t failed = 0, fb = 0;
+    for (int64_t p = 0; p < n; ++p) {
+        double x0[3] = {xyz[p * 3], xyz[p * 3 + 1], xyz[p * 3 + 2]}, v0[3] = {0, 0, 0}, v1[3] = {0, 0, 0};
+        if (!velocity_at(m, u_nodal, x0, v0)) {
+            failed++;
+            continue;
+        }
+        double x1[3] = {x0[0], x0[1], x0[2]};
+        if (order == 1) {
+            for (int d = 0; d < m->dim; ++d) x1[d] = x0[d] + dt * v0[d];
+        } else {
+            double xm[3] = {x0[0], x0[1], x0[2]};
+            for (int d = 0; d < m->dim; ++d) xm[d] = x0[d] + 0.5 * dt * v0[d];
+            if (velocity_at(m, u_nodal, xm, v1)) {
+                for (int d = 0; d < m->dim; ++d) x1[d] = x0[d] + dt * v1[d];
+            } else if (allow_fallback) {
+                for (int d = 0; d < m->dim; ++d) x1[d] = x0[d] + dt * v0[d];
+                fb++;
+            } else {
+                failed++;
+                continue;
+            }
+        }
+        for (int d = 0; d < m->dim; ++d) xyz[p * 3 + d] = x1[d];
+    }
+    if (fallbacks) *fallbacks = fb;
+    return failed;
+}
+
 /* PICellerator/MaterialPoints/src/CoincidentMapper.c:176-242 with
  * StgDomain/Swarm/src/SwarmClass.c:1155-1184 (append => ascending point order per cell),
  * StgFEM/Discretisation/src/ElementType.c:227-350 for xi. */

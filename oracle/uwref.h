@@ -81,6 +81,8 @@ int64_t uwr_map(const uwr_mesh* m, int64_t n, const double* xyz /* n*3 */,
                 double* xi /* n*3, in perm order */, int32_t use_newton);
 
 /* Shape functions ---------------------------------------------------------------------- */
+int64_t uwr_advect(const uwr_mesh* m, const double* u_nodal /* nnode*dim */, int64_t n, double* xyz /* n*3, in/out */,
+                   double dt, int32_t order, int32_t allow_fallback, int64_t* fallbacks);
 void uwr_shape(int dim, const double* xi, double* N);
 void uwr_shape_local_derivs(int dim, const double* xi, double* GNi /* dim*nen */);
 void uwr_global_to_local(const uwr_mesh* m, int64_t e, const double* x, double* xi);
