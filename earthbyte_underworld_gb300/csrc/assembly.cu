@@ -56,8 +56,9 @@ struct AssemblyArgs {
 // is carried as its viscosity (D[3][3] in 3D, D[2][2] in 2D).
 template <int DIM>
 __device__ __forceinline__ double run_rheology(const uwgpu_material& m, const double* N, const double* Tn,
-                                               bool hasT, double yglobal, double ymax, double point_eta,
+                                               bool hasT, const double* xg, double ymax, double point_eta,
                                                const double (*L)[3], double pressure, int prev) {
+    const double yglobal = xg[1];
     double eta = 0.0;
     for (int l = 0; l < m.n_laws; ++l) {
         const uwgpu_law& law = m.laws[l];
@@ -134,6 +135,35 @@ __device__ __forceinline__ double run_rheology(const uwgpu_material& m, const do
         case UWGPU_LAW_PARTICLE_VISCOSITY:
             eta = point_eta;
             break;
+        case UWGPU_LAW_LINEAR_VISCOSITY:
+            eta = law.p[1] * xg[0] + law.p[2] * xg[1] + law.p[4] * xg[0] * xg[1] + law.p[0];
+            if (DIM == 3)
+                eta += law.p[3] * xg[2] + law.p[5] * xg[0] * xg[2] + law.p[6] * xg[1] * xg[2] +
+                       law.p[7] * xg[0] * xg[1] * xg[2];
+            break;
+        case UWGPU_LAW_DEPTH_DEPENDENT: {
+            const int axis = (int)law.p[3];
+            eta = law.p[0] * exp(law.p[1] * (xg[axis < 0 ? 0 : (axis > 2 ? 2 : axis)] - law.p[2]));
+            break;
+        }
+        case UWGPU_LAW_NON_NEWTONIAN: {
+            // strain-rate invariant of the previous solution at the point (TensorMath.c:430-458)
+            double sri = law.p[1];
+            if (prev) {
+                if (DIM == 3) {
+                    double e3 = 0.5 * (L[0][1] + L[1][0]), e4 = 0.5 * (L[0][2] + L[2][0]), e5 = 0.5 * (L[1][2] + L[2][1]);
+                    sri = sqrt(0.5 * (L[0][0] * L[0][0] + L[1][1] * L[1][1] + L[2][2] * L[2][2]) + e3 * e3 + e4 * e4 +
+                               e5 * e5);
+                } else {
+                    double e2 = 0.5 * (L[0][1] + L[1][0]);
+                    sri = sqrt(0.5 * (L[0][0] * L[0][0] + L[1][1] * L[1][1]) + e2 * e2);
+                }
+            }
+            const double n = law.p[0];
+            if (sri == 0.0 || fabs(n - 1.0) < 1.0e-10) break;
+            eta = pow(2.0 * sri, 1.0 / n - 1.0) * pow(eta, 1.0 / n);
+            break;
+        }
         default:
             break;
         }
@@ -241,9 +271,12 @@ __global__ void __launch_bounds__(128) k_assemble(AssemblyArgs A) {
                     for (int j = 0; j < DIM; ++j) L[i][j] += gx[j] * un[i][a];
             }
         }
-        double yglobal = x0[1] + 0.5 * h[1] * (xi[1] + 1.0);
+        // global coordinate of the point (FeMesh_CoordLocalToGlobal on the affine element)
+        double xg[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) xg[d] = x0[d] + 0.5 * h[d] * (xi[d] + 1.0);
         double peta = A.seta_in ? A.seta_in[s] : 0.0;
-        double eta = run_rheology<DIM>(m, N, Tn, hasT, yglobal, A.max[1], peta, L, pressure, A.previous_solution);
+        double eta = run_rheology<DIM>(m, N, Tn, hasT, xg, A.max[1], peta, L, pressure, A.previous_solution);
         if (A.eta_out) A.eta_out[s] = eta;
         double rho0 = A.srho_in ? A.srho_in[s] : m.density;
         double T = 0.0;

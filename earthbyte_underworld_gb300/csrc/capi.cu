@@ -149,9 +149,14 @@ int uwgpu_materials_set(uwgpu_ctx* ctx, int32_t n, const uwgpu_material* mats) {
                         "material needs 1..4 rheology laws");
             for (int l = 0; l < mats[i].n_laws; ++l) {
                 int law = mats[i].laws[l].law;
-                UWG_REQUIRE(law >= UWGPU_LAW_MATERIAL_VISCOSITY && law <= UWGPU_LAW_PARTICLE_VISCOSITY,
+                UWG_REQUIRE(law >= UWGPU_LAW_MATERIAL_VISCOSITY && law <= UWGPU_LAW_NON_NEWTONIAN,
                             UWGPU_ERR_UNSUPPORTED,
                             "rheology law " + std::to_string(law) + " is not provided by this library");
+                if (law == UWGPU_LAW_DEPTH_DEPENDENT) {
+                    const double axis = mats[i].laws[l].p[3];
+                    UWG_REQUIRE(axis == 0.0 || axis == 1.0 || axis == 2.0, UWGPU_ERR_ARGUMENT,
+                                "DepthDependentViscosity variationAxis must be 0, 1 or 2");
+                }
             }
         }
         upload(c.mats, mats, (size_t)n, c.stream);

@@ -25,6 +25,9 @@ LAW_FRANK_KAMENETSKII = 3
 LAW_VISCOSITY_LIMITER = 4
 LAW_DRUCKER_PRAGER = 5
 LAW_PARTICLE_VISCOSITY = 6
+LAW_LINEAR_VISCOSITY = 7
+LAW_DEPTH_DEPENDENT = 8
+LAW_NON_NEWTONIAN = 9
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -48,7 +51,7 @@ class UwgpuError(RuntimeError):
 
 
 class Law(C.Structure):
-    _fields_ = [("law", C.c_int32), ("pad", C.c_int32), ("p", C.c_double * 6)]
+    _fields_ = [("law", C.c_int32), ("pad", C.c_int32), ("p", C.c_double * 8)]
 
 
 class Material(C.Structure):

@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define UWGPU_ABI_VERSION 1
+#define UWGPU_ABI_VERSION 2
 
 /* Status codes. */
 enum {
@@ -49,13 +49,20 @@ enum {
     UWGPU_LAW_VISCOSITY_LIMITER = 4,  /* Underworld/Rheology/src/ViscosityLimiter.c:106   p0=maxViscosity p1=minViscosity */
     UWGPU_LAW_DRUCKER_PRAGER = 5,     /* Underworld/Rheology/src/DruckerPrager.c:236 via YieldRheology.c:198, VonMises.c:232
                                          p0=cohesion p1=frictionCoefficient p2=minimumYieldStress p3=minimumViscosity */
-    UWGPU_LAW_PARTICLE_VISCOSITY = 6  /* eta taken from the per-point viscosity array passed to uwgpu_particles_upload */
+    UWGPU_LAW_PARTICLE_VISCOSITY = 6, /* eta taken from the per-point viscosity array passed to uwgpu_particles_upload */
+    UWGPU_LAW_LINEAR_VISCOSITY = 7,   /* Underworld/Rheology/src/LinearViscosity.c:154-190  eta = C + X x + Y y + XY x y
+                                         (+ Z z + XZ x z + YZ y z + XYZ x y z in 3D); p0..p7 = C X Y Z XY XZ YZ XYZ */
+    UWGPU_LAW_DEPTH_DEPENDENT = 8,    /* Underworld/Rheology/src/DepthDependentViscosity.c:165-188  eta = eta0 exp(gamma (x_axis - referencePoint));
+                                         p0=eta0 p1=gamma p2=referencePoint p3=variationAxis (0, 1, 2) */
+    UWGPU_LAW_NON_NEWTONIAN = 9       /* Underworld/Rheology/src/NonNewtonian.c:139-171  eta = (2 e_II)^(1/n - 1) eta^(1/n), e_II the point's
+                                         strain-rate invariant (defaultStrainRateInvariant before the first solve);
+                                         p0=stressExponent p1=defaultStrainRateInvariant */
 };
 
 typedef struct {
     int32_t law;
     int32_t pad;
-    double p[6];
+    double p[8];
 } uwgpu_law;
 
 /* One RheologyMaterial (Underworld/Rheology/src/RheologyMaterial.c:240-270) plus the

@@ -31,7 +31,7 @@ class Mesh(C.Structure):
 
 
 class Law(C.Structure):
-    _fields_ = [("law", C.c_int32), ("pad", C.c_int32), ("p", C.c_double * 6)]
+    _fields_ = [("law", C.c_int32), ("pad", C.c_int32), ("p", C.c_double * 8)]
 
 
 class Material(C.Structure):

@@ -529,6 +529,35 @@ static double stress_invariant(const rheo_point* rp, double eta) {
     }
 }
 
+/* global coordinate of the point: FeMesh_CoordLocalToGlobal = sum_a N_a(xi) x_a */
+static void point_coord(const rheo_point* rp, double* x) {
+    int nen = (rp->m->dim == 3) ? 8 : 4;
+    for (int d = 0; d < 3; ++d) {
+        x[d] = 0.0;
+        for (int a = 0; a < nen; ++a) x[d] += rp->N[a] * rp->nodes[a][d];
+    }
+}
+
+/* second invariant of the strain rate at the point (StrainRateInvariantField:
+ * TensorMath.c:430-458 on the symmetric velocity gradient) */
+static double strain_rate_invariant(const rheo_point* rp) {
+    int dim = rp->m->dim, nen = (dim == 3) ? 8 : 4;
+    double L[3][3] = {{0}};
+    if (rp->f->velocity) {
+        for (int a = 0; a < nen; ++a)
+            for (int i = 0; i < dim; ++i)
+                for (int j = 0; j < dim; ++j)
+                    L[i][j] += rp->GNx[j * nen + a] * rp->f->velocity[rp->inc[a] * dim + i];
+    }
+    if (dim == 3) {
+        double e0 = L[0][0], e1 = L[1][1], e2 = L[2][2], e3 = 0.5 * (L[0][1] + L[1][0]), e4 = 0.5 * (L[0][2] + L[2][0]),
+               e5 = 0.5 * (L[1][2] + L[2][1]);
+        return sqrt(0.5 * (e0 * e0 + e1 * e1 + e2 * e2) + e3 * e3 + e4 * e4 + e5 * e5);
+    }
+    double e0 = L[0][0], e1 = L[1][1], e2 = 0.5 * (L[0][1] + L[1][0]);
+    return sqrt(0.5 * (e0 * e0 + e1 * e1) + e2 * e2);
+}
+
 /* The rheology list of a RheologyMaterial (Underworld/Rheology/src/Rheology_Register.c:61-77).
  * Every law in scope keeps D isotropic, so the constitutive matrix is tracked by eta:
  * SetIsotropicViscosity (ConstitutiveMatrix.c:362-367) sets it, IsotropicCorrection adds to it. */
@@ -593,6 +622,29 @@ static double run_rheologies(const uwr_material* mat, const rheo_point* rp) {
         case UWR_LAW_PARTICLE_VISCOSITY:
             eta = rp->point_eta;
             break;
+        case UWR_LAW_LINEAR_VISCOSITY: { /* LinearViscosity.c:154-190, coordinate by FeMesh_CoordLocalToGlobal */
+            double x[3];
+            point_coord(rp, x);
+            eta = law->p[1] * x[0] + law->p[2] * x[1] + law->p[4] * x[0] * x[1] + law->p[0];
+            if (dim == 3)
+                eta += law->p[3] * x[2] + law->p[5] * x[0] * x[2] + law->p[6] * x[1] * x[2] + law->p[7] * x[0] * x[1] * x[2];
+            break;
+        }
+        case UWR_LAW_DEPTH_DEPENDENT: { /* DepthDependentViscosity.c:165-188 */
+            double x[3];
+            point_coord(rp, x);
+            int axis = (int)law->p[3];
+            eta = law->p[0] * exp(law->p[1] * (x[axis] - law->p[2]));
+            break;
+        }
+        case UWR_LAW_NON_NEWTONIAN: { /* NonNewtonian.c:139-171 */
+            double sri = rp->f->previous_solution ? strain_rate_invariant(rp) : law->p[1];
+            if (sri == 0) break;
+            double n = law->p[0];
+            if (fabs(n - 1.0) < 1.0e-10) break;
+            eta = pow(2.0 * sri, 1.0 / n - 1.0) * pow(eta, 1.0 / n);
+            break;
+        }
         default:
             break;
         }

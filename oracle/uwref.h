@@ -34,13 +34,16 @@ enum {
     UWR_LAW_FRANK_KAMENETSKII = 3,    /* p[0]=eta0 p[1]=theta                              */
     UWR_LAW_VISCOSITY_LIMITER = 4,    /* p[0]=maxViscosity p[1]=minViscosity               */
     UWR_LAW_DRUCKER_PRAGER = 5,       /* p[0]=cohesion p[1]=frictionCoefficient p[2]=minimumYieldStress p[3]=minimumViscosity */
-    UWR_LAW_PARTICLE_VISCOSITY = 6    /* eta = per-point viscosity input                   */
+    UWR_LAW_PARTICLE_VISCOSITY = 6,   /* eta = per-point viscosity input                   */
+    UWR_LAW_LINEAR_VISCOSITY = 7,     /* p0..p7 = C X Y Z XY XZ YZ XYZ                      */
+    UWR_LAW_DEPTH_DEPENDENT = 8,      /* p0=eta0 p1=gamma p2=referencePoint p3=axis         */
+    UWR_LAW_NON_NEWTONIAN = 9         /* p0=stressExponent p1=defaultStrainRateInvariant    */
 };
 
 typedef struct {
     int32_t law;
     int32_t pad;
-    double p[6];
+    double p[8];
 } uwr_law;
 
 typedef struct {

@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol():
     lib = ctypes.CDLL(lib_path)
     missing = [s for s in declared_symbols() if not hasattr(lib, s)]
     assert not missing, missing
-    assert lib.uwgpu_abi_version() == 1
+    assert lib.uwgpu_abi_version() == 2
 
 
 def test_create_without_device_fails_cleanly():
