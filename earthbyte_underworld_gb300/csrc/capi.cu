@@ -364,7 +364,7 @@ void uwgpu_solve_opts_default(uwgpu_solve_opts* o) {
     o->learned_pc = 0;
     o->learned_stagnation = 2;
     o->mg_cycle = 1;
-    o->pad0 = 0;
+    o->bfbt_inner_pc = 0;
 }
 
 int uwgpu_solve_bsscr(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, double* u, double* p, uwgpu_report* report) {

@@ -174,6 +174,7 @@ __global__ void __launch_bounds__(256) k_gwg_spmv(EGrid g, const T* __restrict__
     if (threadIdx.x == 0) atomicAdd(&scal[0], t);
 }
 
+static double* rz_slot_host(double* scal, int k) { return scal + ((k % 3) + 3) % 3; }
 __device__ __forceinline__ double* rz_slot(double* scal, int k) { return scal + ((k % 3) + 3) % 3; }
 __device__ __forceinline__ double* pq_slot(double* scal, int k) { return scal + 3 + (((k % 2) + 2) % 2); }
 __device__ __forceinline__ double* rr_slot(double* scal, int k) { return scal + 5 + (((k % 2) + 2) % 2); }
@@ -283,6 +284,208 @@ __global__ void k_gwg_init(int64_t ne, const double* __restrict__ b, const T* __
         atomicAdd(&scal[0], t1);
         atomicAdd(&scal[7], t2);
     }
+}
+
+// ------------------------------------------------------------------------------------------
+// Multigrid preconditioner for the inner solves (option bfbt_inner_pc = 1): the element grid is
+// coarsened 2:1 per axis by aggregation (a coarse element is the union of its 2^dim children;
+// prolongation copies the parent's value, restriction sums the children), the coarse operator
+// is the Galerkin product P^T A P (again a 3^dim element stencil), smoothing is Chebyshev on
+// Dinv A (degree 2 before and after the coarse correction, the same polynomial, so the V-cycle
+// is symmetric), and the coarsest level is a dense inverse (with the constant projector added
+// when the operator has the constant null space).
+// ------------------------------------------------------------------------------------------
+
+// Ac[Q][E] = sum over the children e of E and their entries q whose neighbour's parent is at
+// offset Q from E of Af[q][e]
+template <int DIM>
+__global__ void k_gmg_coarsen(EGrid f, EGrid c, const double* __restrict__ Af, double* __restrict__ Ac) {
+    constexpr int NB = stencil_points<DIM>();
+    const int64_t E = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (E >= c.ne) return;
+    const int64_t Ei[3] = {E % c.ex, (E / c.ex) % c.ey, DIM == 3 ? E / (c.ex * c.ey) : 0};
+    const int64_t fc[3] = {f.ex, f.ey, f.ez};
+    double acc[NB];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) acc[q] = 0.0;
+    for (int ch = 0; ch < (1 << DIM); ++ch) {
+        const int64_t fi[3] = {2 * Ei[0] + (ch & 1), 2 * Ei[1] + ((ch >> 1) & 1), DIM == 3 ? 2 * Ei[2] + ((ch >> 2) & 1) : 0};
+        const int64_t e = fi[0] + f.ex * (fi[1] + f.ey * fi[2]);
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            const int o[3] = {q % 3 - 1, (q / 3) % 3 - 1, DIM == 3 ? q / 9 - 1 : 0};
+            int Q = 0, mul = 1;
+            bool valid = true;
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) {
+                const int64_t nb = fi[d] + o[d];
+                valid = valid && nb >= 0 && nb < fc[d];
+                const int64_t P = nb >= 0 ? nb / 2 : -1;   // parent of the neighbour (floor)
+                Q += (int)(P - Ei[d] + 1) * mul;
+                mul *= 3;
+            }
+            if (valid) acc[Q] += Af[(int64_t)q * f.ne + e];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NB; ++q) Ac[(int64_t)q * c.ne + E] = acc[q];
+}
+
+__global__ void k_gmg_dinv(int64_t ne, int center, const double* __restrict__ A, double* __restrict__ dinv) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < ne) dinv[e] = 1.0 / A[(int64_t)center * ne + e];
+}
+
+// (A x)_e with clamped neighbour indices (entries towards missing neighbours are 0)
+template <int DIM, typename T>
+__device__ __forceinline__ T gmg_row(const EGrid& g, int64_t e, const T* __restrict__ A, const T* __restrict__ x) {
+    constexpr int NB = stencil_points<DIM>();
+    const int64_t exy = g.ex * g.ey;
+    const int64_t ix = e % g.ex, iy = (e / g.ex) % g.ey, iz = DIM == 3 ? e / exy : 0;
+    const int64_t dx[3] = {ix > 0 ? -1 : 0, 0, ix + 1 < g.ex ? 1 : 0};
+    const int64_t dy[3] = {iy > 0 ? -g.ex : 0, 0, iy + 1 < g.ey ? g.ex : 0};
+    const int64_t dz[3] = {DIM == 3 && iz > 0 ? -exy : 0, 0, DIM == 3 && iz + 1 < g.ez ? exy : 0};
+    T a[NB], xv[NB];
+#pragma unroll
+    for (int t = 0; t < NB; ++t) a[t] = __ldg(A + (size_t)t * g.ne + e);
+#pragma unroll
+    for (int t = 0; t < NB; ++t) xv[t] = x[e + dx[t % 3] + dy[(t / 3) % 3] + dz[DIM == 3 ? t / 9 : 1]];
+    T acc = (T)0;
+#pragma unroll
+    for (int t = 0; t < NB; ++t) acc = fma(a[t], xv[t], acc);
+    return acc;
+}
+
+// r = b - A x
+template <int DIM, typename T>
+__global__ void k_gmg_resid(EGrid g, const T* __restrict__ A, const T* __restrict__ x, const T* __restrict__ b,
+                            T* __restrict__ r) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < g.ne) r[e] = b[e] - gmg_row<DIM, T>(g, e, A, x);
+}
+
+// Chebyshev step on Dinv A: z = dinv (b - A xin); d = c1 d + c2 z (c2 z first); xout = xin + d
+// (xin == nullptr: zero guess)
+template <int DIM, typename T>
+__global__ void k_gmg_cheb(EGrid g, const T* __restrict__ A, const T* __restrict__ dinv, const T* __restrict__ b,
+                           const T* __restrict__ xin, T* __restrict__ xout, T* __restrict__ d, T c1, T c2, int first) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= g.ne) return;
+    T res = b[e];
+    if (xin) res -= gmg_row<DIM, T>(g, e, A, xin);
+    const T z = res * dinv[e];
+    const T dn = first ? c2 * z : fma(c1, d[e], c2 * z);
+    d[e] = dn;
+    xout[e] = (xin ? xin[e] : (T)0) + dn;
+}
+
+// y = dinv (A x) (power iteration for the Chebyshev bounds)
+template <int DIM>
+__global__ void k_gmg_dax(EGrid g, const double* __restrict__ A, const double* __restrict__ dinv,
+                          const double* __restrict__ x, double* __restrict__ y) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < g.ne) y[e] = dinv[e] * gmg_row<DIM, double>(g, e, A, x);
+}
+
+template <int DIM, typename T>
+__global__ void k_gmg_restrict(EGrid f, EGrid c, const T* __restrict__ rf, T* __restrict__ bc) {
+    const int64_t E = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (E >= c.ne) return;
+    const int64_t Ei[3] = {E % c.ex, (E / c.ex) % c.ey, DIM == 3 ? E / (c.ex * c.ey) : 0};
+    T acc = (T)0;
+#pragma unroll
+    for (int ch = 0; ch < (1 << DIM); ++ch) {
+        const int64_t e = (2 * Ei[0] + (ch & 1)) +
+                          f.ex * ((2 * Ei[1] + ((ch >> 1) & 1)) + f.ey * (DIM == 3 ? 2 * Ei[2] + ((ch >> 2) & 1) : 0));
+        acc += rf[e];
+    }
+    bc[E] = acc;
+}
+
+template <int DIM, typename T>
+__global__ void k_gmg_prolong_add(EGrid f, EGrid c, const T* __restrict__ xc, T* __restrict__ xf) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= f.ne) return;
+    const int64_t ix = e % f.ex, iy = (e / f.ex) % f.ey, iz = DIM == 3 ? e / (f.ex * f.ey) : 0;
+    xf[e] += xc[(ix / 2) + c.ex * ((iy / 2) + c.ey * (iz / 2))];
+}
+
+// dense coarsest matrix from the stencil, plus `shift` in every entry (the constant projector)
+template <int DIM>
+__global__ void k_gmg_dense(EGrid g, const double* __restrict__ A, double shift, double* __restrict__ M) {
+    constexpr int NB = stencil_points<DIM>();
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= g.ne) return;
+    for (int64_t j = 0; j < g.ne; ++j) M[e * g.ne + j] = shift;
+    const int64_t ix = e % g.ex, iy = (e / g.ex) % g.ey, iz = DIM == 3 ? e / (g.ex * g.ey) : 0;
+    for (int q = 0; q < NB; ++q) {
+        const int ox = q % 3 - 1, oy = (q / 3) % 3 - 1, oz = DIM == 3 ? q / 9 - 1 : 0;
+        if (ix + ox < 0 || ix + ox >= g.ex || iy + oy < 0 || iy + oy >= g.ey ||
+            (DIM == 3 && (iz + oz < 0 || iz + oz >= g.ez)))
+            continue;
+        M[e * g.ne + e + ox + g.ex * (oy + g.ey * oz)] += A[(int64_t)q * g.ne + e];
+    }
+}
+
+// CG kernels with the multigrid preconditioner: the update leaves z to the V-cycle; the dot
+// kernel accumulates rz_{k+1} = r.z afterwards
+template <typename T>
+__global__ void k_cgm_update(int64_t ne, const T* __restrict__ p, const T* __restrict__ q, T* __restrict__ x,
+                             T* __restrict__ r, double* __restrict__ scal, int k, int want_rr) {
+    __shared__ double sw[32];
+    __shared__ T s_alpha;
+    const T alpha = block_ratio<T>(rz_slot(scal, k), pq_slot(scal, k), &s_alpha);
+    const int64_t base = (int64_t)blockIdx.x * blockDim.x * kEpt + threadIdx.x;
+    T rr = (T)0;
+#pragma unroll
+    for (int m = 0; m < kEpt; ++m) {
+        const int64_t e = base + (int64_t)m * blockDim.x;
+        if (e < ne) {
+            x[e] = fma(alpha, p[e], x[e]);
+            const T re = fma(-alpha, q[e], r[e]);
+            r[e] = re;
+            rr = fma(re, re, rr);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *rz_slot(scal, k + 2) = 0.0;
+        *pq_slot(scal, k + 1) = 0.0;
+    }
+    if (want_rr) {
+        double t = block_sum<T>(rr, sw);
+        if (threadIdx.x == 0) atomicAdd(rr_slot(scal, k), t);
+    }
+}
+
+template <typename T>
+__global__ void k_cgm_dot(int64_t ne, const T* __restrict__ r, const T* __restrict__ z, double* __restrict__ out) {
+    __shared__ double sw[32];
+    const int64_t base = (int64_t)blockIdx.x * blockDim.x * kEpt + threadIdx.x;
+    T rz = (T)0;
+#pragma unroll
+    for (int m = 0; m < kEpt; ++m) {
+        const int64_t e = base + (int64_t)m * blockDim.x;
+        if (e < ne) rz = fma(r[e], z[e], rz);
+    }
+    double t = block_sum<T>(rz, sw);
+    if (threadIdx.x == 0) atomicAdd(out, t);
+}
+
+// r = b (copied, T), x = 0 ; scal[7] = r0.r0
+template <typename T>
+__global__ void k_cgm_init(int64_t ne, const double* __restrict__ b, T* __restrict__ x, T* __restrict__ r,
+                           double* __restrict__ scal) {
+    __shared__ double sw[32];
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    T rr = (T)0;
+    if (e < ne) {
+        const T re = (T)b[e];
+        x[e] = (T)0;
+        r[e] = re;
+        rr = re * re;
+    }
+    double t = block_sum<T>(rr, sw);
+    if (threadIdx.x == 0) atomicAdd(&scal[7], t);
 }
 
 EGrid egrid_of(const MeshDesc& m) {
@@ -425,6 +628,291 @@ int gwg_cg(Context& c, const double* A, const double* dinv, const double* b, dou
 int gwg_cg32(Context& c, const float* A, const float* dinv, const double* b, float* x, double rtol, int maxit,
              float* work, double* scal) {
     return gwg_cg_T<float>(c, A, dinv, b, x, rtol, maxit, work, scal);
+}
+
+// ---- multigrid hierarchy for G^T W G ----------------------------------------------------
+void dense_inverse(Context& c, double* M, int64_t n);                      // operator.cu
+template <typename T> void dense_apply(Context& c, const double* M, int64_t n, const T* b, T* x);
+
+static EGrid egrid_level(const Context::GwgLevel& L) {
+    EGrid g;
+    g.ex = L.ex;
+    g.ey = L.ey;
+    g.ez = L.ez;
+    g.ne = L.ne;
+    return g;
+}
+
+// Builds the coarse levels, Chebyshev bounds and the coarsest inverse for the fine stencil A0
+// (its inverse diagonal dinv0).  Returns false when the mesh does not coarsen to a dense size
+// that fits (the caller keeps the Jacobi preconditioner then).
+bool gwg_mg_build(Context& c, const double* A0, const double* dinv0, bool need32, bool const_null) {
+    const MeshDesc& m = c.levels[0].mesh;
+    // captured V-cycles carry this hierarchy's Chebyshev coefficients: drop them
+    for (auto it = c.pcg_graphs.begin(); it != c.pcg_graphs.end();) {
+        if ((intptr_t)it->key[7] >= 32) {
+            if (it->exec) cudaGraphExecDestroy(it->exec);
+            it = c.pcg_graphs.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    const int dim = m.dim, nb = dim == 3 ? 27 : 9;
+    EGrid g = egrid_of(m);
+    int nlev = 1;
+    {
+        auto& L0 = c.gwg[0];
+        L0.ex = g.ex;
+        L0.ey = g.ey;
+        L0.ez = g.ez;
+        L0.ne = g.ne;
+    }
+    while (nlev < kMaxLevels) {
+        const auto& F = c.gwg[nlev - 1];
+        const bool even = F.ex % 2 == 0 && F.ey % 2 == 0 && (dim == 2 || F.ez % 2 == 0);
+        if (!even || F.ne <= 512) break;
+        auto& C = c.gwg[nlev];
+        C.ex = F.ex / 2;
+        C.ey = F.ey / 2;
+        C.ez = dim == 3 ? F.ez / 2 : 1;
+        C.ne = C.ex * C.ey * C.ez;
+        nlev++;
+    }
+    const auto& Lc = c.gwg[nlev - 1];
+    if (Lc.ne > 4096) return false;
+    c.gwg_nlev = nlev;
+    // coarse stencils (FP64)
+    for (int l = 1; l < nlev; ++l) {
+        auto& C = c.gwg[l];
+        C.A64.ensure((size_t)nb * C.ne);
+        C.dinv64.ensure((size_t)C.ne);
+        const double* Af = l == 1 ? A0 : c.gwg[l - 1].A64.p;
+        LaunchScope ls(c, -1);
+        if (dim == 3) k_gmg_coarsen<3><<<blocks_for(C.ne, 128), 128, 0, c.stream>>>(egrid_level(c.gwg[l - 1]), egrid_level(C), Af, C.A64.p);
+        else k_gmg_coarsen<2><<<blocks_for(C.ne, 128), 128, 0, c.stream>>>(egrid_level(c.gwg[l - 1]), egrid_level(C), Af, C.A64.p);
+        k_gmg_dinv<<<blocks_for(C.ne, 256), 256, 0, c.stream>>>(C.ne, nb / 2, C.A64.p, C.dinv64.p);
+        c.launches++;
+    }
+    check_launch("k_gmg_coarsen");
+    // work vectors
+    for (int l = 0; l < nlev; ++l) {
+        auto& L = c.gwg[l];
+        for (auto* a : {&L.b64, &L.x64, &L.r64, &L.t64, &L.d64}) a->ensure((size_t)L.ne);
+        if (need32)
+            for (auto* a : {&L.b32, &L.x32, &L.r32, &L.t32, &L.d32}) a->ensure((size_t)L.ne);
+    }
+    // Chebyshev bounds: largest eigenvalue of Dinv A per smoothed level (power iteration)
+    for (int l = 0; l + 1 < nlev; ++l) {
+        auto& L = c.gwg[l];
+        const double* A = l == 0 ? A0 : L.A64.p;
+        const double* dinv = l == 0 ? dinv0 : L.dinv64.p;
+        const EGrid gl = egrid_level(L);
+        std::vector<double> h((size_t)L.ne);
+        for (int64_t e = 0; e < L.ne; ++e) h[(size_t)e] = (double)((e * 2654435761ull >> 7) & 1023ull) / 1023.0 - 0.5;
+        UWG_CUDA(cudaMemcpyAsync(L.x64.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        double lam = 1.0;
+        for (int it = 0; it < 12; ++it) {
+            {
+                LaunchScope ls(c, -1);
+                if (dim == 3) k_gmg_dax<3><<<blocks_for(L.ne, 256), 256, 0, c.stream>>>(gl, A, dinv, L.x64.p, L.t64.p);
+                else k_gmg_dax<2><<<blocks_for(L.ne, 256), 256, 0, c.stream>>>(gl, A, dinv, L.x64.p, L.t64.p);
+            }
+            UWG_CUDA(cudaMemcpyAsync(h.data(), L.t64.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            UWG_CUDA(cudaStreamSynchronize(c.stream));
+            double nrm = 0.0;
+            for (double v : h) nrm += v * v;
+            nrm = std::sqrt(nrm);
+            if (!(nrm > 0.0) || !std::isfinite(nrm)) break;
+            lam = nrm;
+            for (double& v : h) v /= nrm;
+            UWG_CUDA(cudaMemcpyAsync(L.x64.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        }
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        L.lmax = lam;
+    }
+    // coarsest: dense inverse of A (+ mean diagonal / n in every entry for the constant mode)
+    {
+        const auto& C = c.gwg[nlev - 1];
+        const double* Ac = nlev == 1 ? A0 : C.A64.p;
+        const int64_t n = C.ne;
+        double shift = 0.0;
+        if (const_null) {
+            std::vector<double> dg((size_t)n);
+            UWG_CUDA(cudaMemcpy(dg.data(), Ac + (size_t)(nb / 2) * n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+            double sdg = 0.0;
+            for (double v : dg) sdg += v;
+            shift = sdg / n / n;
+        }
+        c.gwg_Cinv.ensure((size_t)(n * n));
+        c.gwg_ncoarse = n;
+        {
+            LaunchScope ls(c, -1);
+            if (dim == 3) k_gmg_dense<3><<<blocks_for(n, 128), 128, 0, c.stream>>>(egrid_level(C), Ac, shift, c.gwg_Cinv.p);
+            else k_gmg_dense<2><<<blocks_for(n, 128), 128, 0, c.stream>>>(egrid_level(C), Ac, shift, c.gwg_Cinv.p);
+        }
+        check_launch("k_gmg_dense");
+        dense_inverse(c, c.gwg_Cinv.p, n);
+    }
+    // FP32 copies of the coarse levels (level 0's FP32 stencil belongs to the solve)
+    if (need32)
+        for (int l = 1; l < nlev; ++l) {
+            auto& L = c.gwg[l];
+            L.A32.ensure((size_t)nb * L.ne);
+            L.dinv32.ensure((size_t)L.ne);
+            LaunchScope ls(c, -1);
+            k_gwg_convert<double, float><<<blocks_for((int64_t)nb * L.ne, 256), 256, 0, c.stream>>>((int64_t)nb * L.ne, L.A64.p, L.A32.p);
+            k_gwg_convert<double, float><<<blocks_for(L.ne, 256), 256, 0, c.stream>>>(L.ne, L.dinv64.p, L.dinv32.p);
+            c.launches++;
+        }
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+    return true;
+}
+
+// the level array of precision T
+template <typename T> static T* lv(DArray<double>& a64, DArray<float>& a32);
+template <> double* lv<double>(DArray<double>& a64, DArray<float>&) { return a64.p; }
+template <> float* lv<float>(DArray<double>&, DArray<float>& a32) { return a32.p; }
+
+// degree-2 Chebyshev smoothing on level l (xin == nullptr: zero guess); result in x (x may be xin)
+template <typename T>
+static void gmg_smooth(Context& c, int l, const T* A, const T* dinv, const T* b, const T* xin, T* x) {
+    auto& L = c.gwg[l];
+    const EGrid g = egrid_level(L);
+    const double lmax = 1.1 * L.lmax, lmin = 0.1 * L.lmax;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
+    const double rho0 = 1.0 / sigma, rho1 = 1.0 / (2.0 * sigma - rho0);
+    const double c2a = 1.0 / theta, c1b = rho1 * rho0, c2b = 2.0 * rho1 / delta;
+    T* t = lv<T>(L.t64, L.t32);
+    T* d = lv<T>(L.d64, L.d32);
+    const unsigned nbk = blocks_for(L.ne, 256);
+    if (c.mesh.dim == 3) {
+        k_gmg_cheb<3, T><<<nbk, 256, 0, c.stream>>>(g, A, dinv, b, xin, t, d, (T)0, (T)c2a, 1);
+        k_gmg_cheb<3, T><<<nbk, 256, 0, c.stream>>>(g, A, dinv, b, t, x, d, (T)c1b, (T)c2b, 0);
+    } else {
+        k_gmg_cheb<2, T><<<nbk, 256, 0, c.stream>>>(g, A, dinv, b, xin, t, d, (T)0, (T)c2a, 1);
+        k_gmg_cheb<2, T><<<nbk, 256, 0, c.stream>>>(g, A, dinv, b, t, x, d, (T)c1b, (T)c2b, 0);
+    }
+}
+
+// V-cycle x = M b on level l (zero initial guess); level 0 uses the solve's stencil A0 / dinv0
+template <typename T>
+static void gmg_vcycle(Context& c, int l, const T* A0, const T* dinv0, const T* b, T* x) {
+    auto& L = c.gwg[l];
+    if (l == c.gwg_nlev - 1) {
+        dense_apply<T>(c, c.gwg_Cinv.p, c.gwg_ncoarse, b, x);
+        return;
+    }
+    const T* A = l == 0 ? A0 : lv<T>(L.A64, L.A32);
+    const T* dinv = l == 0 ? dinv0 : lv<T>(L.dinv64, L.dinv32);
+    const EGrid g = egrid_level(L);
+    auto& C = c.gwg[l + 1];
+    const EGrid gc = egrid_level(C);
+    T* r = lv<T>(L.r64, L.r32);
+    T* bc = lv<T>(C.b64, C.b32);
+    T* xc = lv<T>(C.x64, C.x32);
+    gmg_smooth<T>(c, l, A, dinv, b, nullptr, x);
+    const unsigned nbk = blocks_for(L.ne, 256), nbc = blocks_for(C.ne, 256);
+    if (c.mesh.dim == 3) {
+        k_gmg_resid<3, T><<<nbk, 256, 0, c.stream>>>(g, A, x, b, r);
+        k_gmg_restrict<3, T><<<nbc, 256, 0, c.stream>>>(g, gc, r, bc);
+    } else {
+        k_gmg_resid<2, T><<<nbk, 256, 0, c.stream>>>(g, A, x, b, r);
+        k_gmg_restrict<2, T><<<nbc, 256, 0, c.stream>>>(g, gc, r, bc);
+    }
+    gmg_vcycle<T>(c, l + 1, A0, dinv0, bc, xc);
+    if (c.mesh.dim == 3) k_gmg_prolong_add<3, T><<<nbk, 256, 0, c.stream>>>(g, gc, xc, x);
+    else k_gmg_prolong_add<2, T><<<nbk, 256, 0, c.stream>>>(g, gc, xc, x);
+    // post-smoothing from x with the same polynomial; in place is safe: the first step reads x and
+    // writes t, the second reads t and writes x
+    gmg_smooth<T>(c, l, A, dinv, b, x, x);
+}
+
+// CG on A x = b preconditioned by the V-cycle; work holds 4*ne values of T, scal 8 doubles
+template <typename T>
+static int gwg_cg_mg_T(Context& c, const T* A, const T* dinv, const double* b, T* x, double rtol, int maxit,
+                       T* work, double* scal) {
+    const MeshDesc& m = c.levels[0].mesh;
+    EGrid g = egrid_of(m);
+    const int64_t ne = g.ne;
+    const int nb = m.dim == 3 ? 27 : 9;
+    T* r = work;
+    T* z = work + ne;
+    T* p = work + 2 * ne;
+    T* q = work + 3 * ne;
+    UWG_CUDA(cudaMemsetAsync(scal, 0, 8 * sizeof(double), c.stream));
+    const unsigned eb = blocks_for(ne, 256), ebv = blocks_for(ne, 256 * kEpt);
+    {
+        LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
+        k_cgm_init<T><<<eb, 256, 0, c.stream>>>(ne, b, x, r, scal);
+    }
+    gmg_vcycle<T>(c, 0, A, dinv, r, z);
+    k_cgm_dot<T><<<ebv, 256, 0, c.stream>>>(ne, r, z, scal);   // rz_0 -> scal[0]
+    if (m.dim == 3) k_cg_spmv_dir<3, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, -1, 1);
+    else k_cg_spmv_dir<2, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, -1, 1);
+    check_launch("gwg_cg_mg init");
+    double* hs = c.host_scalars;
+    UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+    const double r0 = std::sqrt(hs[7]);
+    if (!(r0 > 0.0)) return 0;
+    // four iterations per graph (the rz slots cycle with period 3, pq / rr with 2: 12 would be
+    // the period, but each iteration carries a V-cycle, so the host checks more often)
+    const int block = 6;
+    auto issue = [&](int k) {
+        k_cgm_update<T><<<ebv, 256, 0, c.stream>>>(ne, p, q, x, r, scal, k, k == block - 1);
+        gmg_vcycle<T>(c, 0, A, dinv, r, z);
+        k_cgm_dot<T><<<ebv, 256, 0, c.stream>>>(ne, r, z, rz_slot_host(scal, k + 1));
+        if (m.dim == 3) k_cg_spmv_dir<3, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, 0);
+        else k_cg_spmv_dir<2, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, 0);
+    };
+    const void* key[8] = {A, dinv, x, work, scal, (const void*)(intptr_t)ne, (const void*)(intptr_t)sizeof(T),
+                          (const void*)(intptr_t)(m.dim + 32)};
+    Context::PcgGraph* pg = nullptr;
+    for (auto& cand : c.pcg_graphs)
+        if (std::equal(std::begin(key), std::end(key), std::begin(cand.key))) pg = &cand;
+    if (!pg) {
+        c.pcg_graphs.emplace_back();
+        pg = &c.pcg_graphs.back();
+        std::copy(std::begin(key), std::end(key), std::begin(pg->key));
+        cudaGraph_t graph;
+        UWG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < block; ++k) issue(k);
+        UWG_CUDA(cudaStreamEndCapture(c.stream, &graph));
+        UWG_CUDA(cudaGraphInstantiate(&pg->exec, graph, 0));
+        UWG_CUDA(cudaGraphDestroy(graph));
+    }
+    // algorithmic traffic of one iteration: the two CG kernels, two smoothing steps before and two
+    // after the coarse correction and the residual on every level (stencil + vectors)
+    double lev_bytes = 0.0;
+    for (int l = 0; l + 1 < c.gwg_nlev; ++l) lev_bytes += (double)c.gwg[l].ne * sizeof(T) * 5.0 * (nb + 4);
+    const double it_bytes = (double)ne * sizeof(T) * (8 + nb + 5 + 2) + lev_bytes;
+    const double it_flops = (double)ne * (2.0 * nb + 16.0) * 6.0;
+    int it = 0;
+    while (it < maxit) {
+        {
+            LaunchScope ls(c, UWGPU_KERNEL_SCHUR_PC);
+            UWG_CUDA(cudaGraphLaunch(pg->exec, c.stream));
+        }
+        note_work(c, UWGPU_KERNEL_SCHUR_PC, block * it_bytes, block * it_flops);
+        it += block;
+        UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        const double rn = std::sqrt(hs[6]);   // rr of the block's last iteration (k = 5: slot 5 + 1)
+        if (!std::isfinite(rn)) throw Error(UWGPU_ERR_NAN, "NaN in the BFBt inner solve");
+        if (rn <= rtol * r0) break;
+    }
+    check_launch("gwg_cg_mg");
+    return it;
+}
+
+int gwg_cg_mg(Context& c, const double* A, const double* dinv, const double* b, double* x, double rtol, int maxit,
+              double* work, double* scal) {
+    return gwg_cg_mg_T<double>(c, A, dinv, b, x, rtol, maxit, work, scal);
+}
+
+int gwg_cg_mg32(Context& c, const float* A, const float* dinv, const double* b, float* x, double rtol, int maxit,
+                float* work, double* scal) {
+    return gwg_cg_mg_T<float>(c, A, dinv, b, x, rtol, maxit, work, scal);
 }
 
 }  // namespace uwg

@@ -178,6 +178,20 @@ struct Context {
     bool profiling = false;
     ProfileFamily prof[UWGPU_KERNEL_COUNT];
 
+    // multigrid hierarchy of the BFBt operator G^T W G (gwg_stencil.cu): element grids coarsened
+    // 2:1 by aggregation; level 0's stencil belongs to the solve, the others live here, as do the
+    // work vectors of every level (stable addresses for the captured CG graphs)
+    struct GwgLevel {
+        int64_t ex = 0, ey = 0, ez = 0, ne = 0;
+        DArray<double> A64, dinv64, b64, x64, r64, t64, d64;
+        DArray<float> A32, dinv32, b32, x32, r32, t32, d32;
+        double lmax = 0.0;
+    };
+    GwgLevel gwg[kMaxLevels];
+    int gwg_nlev = 0;
+    DArray<double> gwg_Cinv;     // dense inverse on the coarsest level
+    int64_t gwg_ncoarse = 0;
+
     // CUDA graphs of the BFBt inner-CG iteration block, one per buffer set
     struct PcgGraph {
         const void* key[8];

@@ -574,6 +574,33 @@ static void to_fp32(Context& c, const DArray<double>& a, DArray<float>& b) {
     check_launch("k_convert");
 }
 
+// In-place Gauss-Jordan inverse of an SPD dense n x n matrix (no pivoting), on the stream.
+void dense_inverse(Context& c, double* M, int64_t n) {
+    DArray<double> row, col;
+    row.ensure((size_t)n);
+    col.ensure((size_t)n);
+    for (int64_t k = 0; k < n; ++k) {
+        {
+            LaunchScope ls(c, -1);
+            k_gj_save<<<blocks_for(n, 256), 256, 0, c.stream>>>(n, k, M, row.p, col.p);
+        }
+        {
+            LaunchScope ls(c, -1);
+            k_gj_update<<<blocks_for(n * n, 256), 256, 0, c.stream>>>(n, k, M, row.p, col.p);
+        }
+    }
+    check_launch("k_gj_update");
+    UWG_CUDA(cudaStreamSynchronize(c.stream));   // row and col are released on return
+}
+
+// x = M b with a dense FP64 n x n matrix (one warp per row), vectors of type T
+template <typename T>
+void dense_apply(Context& c, const double* M, int64_t n, const T* b, T* x) {
+    k_gemv<T><<<blocks_for(n * 32, 256), 256, 0, c.stream>>>(n, M, b, x);
+}
+template void dense_apply<double>(Context&, const double*, int64_t, const double*, double*);
+template void dense_apply<float>(Context&, const double*, int64_t, const float*, float*);
+
 static void coarse_inverse(Context& c, Level& L) {
     Grid g = grid_of(L.mesh);
     int dim = L.mesh.dim;
@@ -591,21 +618,7 @@ static void coarse_inverse(Context& c, Level& L) {
             k_dense_from_stencil<2><<<blocks_for(g.nn, 128), 128, 0, c.stream>>>(g, L.A64.p, L.Cinv.p);
     }
     check_launch("k_dense_from_stencil");
-    DArray<double> row, col;
-    row.ensure((size_t)n);
-    col.ensure((size_t)n);
-    for (int64_t k = 0; k < n; ++k) {
-        {
-            LaunchScope ls(c, -1);
-            k_gj_save<<<blocks_for(n, 256), 256, 0, c.stream>>>(n, k, L.Cinv.p, row.p, col.p);
-        }
-        {
-            LaunchScope ls(c, -1);
-            k_gj_update<<<blocks_for(n * n, 256), 256, 0, c.stream>>>(n, k, L.Cinv.p, row.p, col.p);
-        }
-    }
-    check_launch("k_gj_update");
-    UWG_CUDA(cudaStreamSynchronize(c.stream));
+    dense_inverse(c, L.Cinv.p, n);
 }
 
 void build_operator(Context& c, int levels, bool need32) {

@@ -42,6 +42,11 @@ int gwg_cg(Context& c, const double* A, const double* dinv, const double* b, dou
 int gwg_cg32(Context& c, const float* A, const float* dinv, const double* b, float* x, double rtol, int maxit,
              float* work, double* scal);
 double g_inf_norm(Context& c);
+bool gwg_mg_build(Context& c, const double* A0, const double* dinv0, bool need32, bool const_null);
+int gwg_cg_mg(Context& c, const double* A, const double* dinv, const double* b, double* x, double rtol, int maxit,
+              double* work, double* scal);
+int gwg_cg_mg32(Context& c, const float* A, const float* dinv, const double* b, float* x, double rtol, int maxit,
+                float* work, double* scal);
 void op_wg32(Context& c, const float* p, const float* W, float* s);
 void op_gt32(Context& c, const float* s, float* q);
 void to_float(Context& c, const double* a, float* b, int64_t n);
@@ -454,6 +459,7 @@ struct Bsscr {
     DArray<double> ns_t, ns_v;
     bool ns_use_t = false, ns_use_v = false;
     bool bbt_const = false;
+    bool bfbt_mg = false;      // the inner solves use the multigrid preconditioner
     DArray<float> r32, d32;
     bool nan = false;
     bool inner_fail = false;
@@ -651,7 +657,8 @@ struct Bsscr {
         double rtol = o.bfbt_rtol > 0 ? o.bfbt_rtol : 1e-4;
         copy<double>(c, npres, b, pr.p);
         if (bbt_const) remove_constant_dev(pr.p);
-        bfbt_its += gwg_cg(c, bA.p, bd.p, pr.p, x, rtol, maxit, pz.p, pz.p + 4 * npres);
+        bfbt_its += bfbt_mg ? gwg_cg_mg(c, bA.p, bd.p, pr.p, x, rtol, maxit, pz.p, pz.p + 4 * npres)
+                            : gwg_cg(c, bA.p, bd.p, pr.p, x, rtol, maxit, pz.p, pz.p + 4 * npres);
     }
 
     // the same preconditioner with FP32 operators, inner solves and vectors (mixed form)
@@ -660,7 +667,8 @@ struct Bsscr {
         double rtol = o.bfbt_rtol > 0 ? o.bfbt_rtol : 1e-4;
         copy<double>(c, npres, x, pr.p);
         if (bbt_const) remove_constant_dev(pr.p);
-        bfbt_its += gwg_cg32(c, bA32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, scal32.p);
+        bfbt_its += bfbt_mg ? gwg_cg_mg32(c, bA32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, scal32.p)
+                            : gwg_cg32(c, bA32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, scal32.p);
         op_wg32(c, bt32.p, bw32.p, bs32.p);
         level_apply<float>(c, c.levels[0], bs32.p, bX32.p);
         {
@@ -670,7 +678,8 @@ struct Bsscr {
         op_gt32(c, bX32.p, bt2_32.p);
         to_double(c, bt2_32.p, pr.p, npres);
         if (bbt_const) remove_constant_dev(pr.p);
-        bfbt_its += gwg_cg32(c, bA32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, scal32.p);
+        bfbt_its += bfbt_mg ? gwg_cg_mg32(c, bA32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, scal32.p)
+                            : gwg_cg32(c, bA32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, scal32.p);
         to_double(c, bt32.p, y, npres);
     }
 
@@ -977,6 +986,7 @@ void Bsscr::run() {
             bA32.ensure((size_t)(dim == 3 ? 27 : 9) * npres);
             gwg_stencil_fp32(c, bA.p, bd.p, bA32.p, bd32.p);
         }
+        if (o.bfbt_inner_pc == 1) bfbt_mg = gwg_mg_build(c, bA.p, bd.p, mixed, bbt_const);
     }
     UWG_CUDA(cudaStreamSynchronize(c.stream));
     auto t1 = std::chrono::steady_clock::now();
@@ -1038,6 +1048,7 @@ void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
     UWG_REQUIRE(o.remove_const_p >= 0 && o.remove_const_p <= 2, UWGPU_ERR_ARGUMENT, "bad pressure null-space mode");
     UWG_REQUIRE(o.learned_pc == 0 || o.learned_pc == 1, UWGPU_ERR_ARGUMENT, "bad learned_pc");
     UWG_REQUIRE(o.mg_cycle == 1 || o.mg_cycle == 2, UWGPU_ERR_ARGUMENT, "mg_cycle must be 1 (V) or 2 (W)");
+    UWG_REQUIRE(o.bfbt_inner_pc == 0 || o.bfbt_inner_pc == 1, UWGPU_ERR_ARGUMENT, "bfbt_inner_pc must be 0 or 1");
     Bsscr s(c, o, rep);
     s.run();
 }

@@ -66,7 +66,7 @@ class SolveOpts(C.Structure):
                 ("a11_rtol", C.c_double), ("back_rtol", C.c_double), ("remove_const_p", C.c_int32),
                 ("precision", C.c_int32), ("target_rel_residual", C.c_double), ("bfbt_rtol", C.c_double),
                 ("bfbt_max_it", C.c_int32), ("smoother", C.c_int32), ("learned_pc", C.c_int32),
-                ("learned_stagnation", C.c_int32), ("mg_cycle", C.c_int32), ("pad0", C.c_int32)]
+                ("learned_stagnation", C.c_int32), ("mg_cycle", C.c_int32), ("bfbt_inner_pc", C.c_int32)]
 
 
 class Report(C.Structure):

@@ -123,7 +123,8 @@ typedef struct {
                                  after which a velocity solve drops the U-Net (default 2)    */
     int32_t mg_cycle;         /* coarse corrections per level visit: 1 V-cycle (default), 2 W-cycle
                                  (-pc_mg_cycle_type v|w of the velocity PCMG)                */
-    int32_t pad0;
+    int32_t bfbt_inner_pc;    /* preconditioner of the scaled BFBt inner G^T W G solves: 0 Jacobi (default,
+                                 as the reference's KSP), 1 aggregation multigrid V-cycle      */
 } uwgpu_solve_opts;
 
 typedef struct {

@@ -211,12 +211,12 @@ def test_picard_nonlinear_parity(oracle, uw):
     assert _rel(p, op) < 1e-7
 
 
-@pytest.mark.parametrize("case", ["rt2d", "spheres"])
-def test_bfbt_preconditioner_matches_oracle(oracle, uw, case):
-    """The scaled BFBt preconditioner (explicit G^T W G stencil + Jacobi CG on the GPU, matrix-free
-    Jacobi CG in the oracle) gives the Schur FGMRES the same iteration count: with tight inner
-    solves both apply the same operator, so a wrong stencil entry shows up as extra outer
-    iterations.  FP64 and mixed forms."""
+@pytest.mark.parametrize("case,inner_pc", [("rt2d", 0), ("spheres", 0), ("rt2d", 1), ("spheres", 1)])
+def test_bfbt_preconditioner_matches_oracle(oracle, uw, case, inner_pc):
+    """The scaled BFBt preconditioner (explicit G^T W G stencil + Jacobi or multigrid-preconditioned
+    CG on the GPU, matrix-free Jacobi CG in the oracle) gives the Schur FGMRES the same iteration
+    count: with tight inner solves both apply the same operator, so a wrong stencil entry (or a
+    wrong inner preconditioner) shows up as extra outer iterations.  FP64 and mixed forms."""
     from earthbyte_underworld_gb300 import workloads as W
     O, U = oracle, uw
     w = W.rt2d(nel=(32, 32), ppc=20) if case == "rt2d" else W.spheres(nel=(8, 8, 8), nspheres=10, seed=9)
@@ -225,13 +225,14 @@ def test_bfbt_preconditioner_matches_oracle(oracle, uw, case):
     ou, op, orep = O.solve_bsscr(m, w["fixed"], Ke, Ge, fe, Se, mg_levels=3, schur_type=1, schur_pc=3,
                                  scr_rtol=1e-8, a11_rtol=1e-10, back_rtol=1e-10, bfbt_rtol=1e-8, bfbt_max_it=5000)
     opts = U.default_opts(mg_levels=3, schur_type=1, schur_pc=3, scr_rtol=1e-8, a11_rtol=1e-10, back_rtol=1e-10,
-                          max_outer=400, max_inner=2000, bfbt_rtol=1e-8, bfbt_max_it=5000)
+                          max_outer=400, max_inner=2000, bfbt_rtol=1e-8, bfbt_max_it=5000, bfbt_inner_pc=inner_pc)
     u, p, rep = ctx.solve_bsscr(opts)
     assert abs(rep.outer_its - orep.outer_its) <= 1, (rep.outer_its, orep.outer_its)
     assert rep.pc_inner_its > 0
     assert _rel(u, ou) < 1e-6 and _rel(p, op) < 1e-6
     om = U.default_opts(mg_levels=3, schur_type=1, schur_pc=3, scr_rtol=1e-6, a11_rtol=1e-8, back_rtol=1e-8,
-                        max_outer=400, max_inner=2000, bfbt_rtol=1e-5, bfbt_max_it=5000, precision=U.PREC_MIXED)
+                        max_outer=400, max_inner=2000, bfbt_rtol=1e-5, bfbt_max_it=5000, precision=U.PREC_MIXED,
+                        bfbt_inner_pc=inner_pc)
     um, pm, rm = ctx.solve_bsscr(om)
     assert rm.rel_residual < 1e-6
     assert rm.outer_its <= orep.outer_its + 2, (rm.outer_its, orep.outer_its)
