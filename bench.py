@@ -486,6 +486,17 @@ def kernel_rates(ctx, U, iters):
                      "smooth2_ms": sms, "smooth2_GB_per_s": smooth_bytes / sms / 1e6,
                      "smooth2_frac_hbm": smooth_bytes / sms / 1e6 / peak,
                      "smooth2_fp_TFLOP_per_s": 2 * 2 * 2.0 * nn * (nb + 1) * dim * dim / sms / 1e9})
+    # the scaled BFBt inner operator (one value per element): the CG's direction kernel with p = z,
+    # q = A z; algorithmic bytes: z read and p, q written, plus the 3^d stencil coefficients
+    # (stencil forms) or the nodal W of about one node per element (matrix-free FP32 form)
+    ne = ctx.nelements
+    for name, form, per_elem in (("fp64", 0, (nb + 3) * 8), ("fp32", 1, (dim + 3) * 4),
+                                 ("fp32_stencil", 2, (nb + 3) * 4)):
+        ctx.time_bfbt_apply(form, 3)
+        bms = ctx.time_bfbt_apply(form, iters) / iters
+        gbs = ne * per_elem / bms / 1e6
+        out.setdefault(name, {}).update({"bfbt_dir_ms": bms, "bfbt_dir_GB_per_s": gbs,
+                                         "bfbt_dir_frac_hbm": gbs / peak, "bfbt_dir_bytes": ne * per_elem})
     out["peak_GB_per_s"] = peak
     out["peak_source"] = kind
     return out

@@ -461,6 +461,20 @@ int uwgpu_profile_read_work(uwgpu_ctx* ctx, int32_t which, double* bytes, double
 
 int64_t uwgpu_launch_count(const uwgpu_ctx* ctx) { return ctx ? ctx->c.launches : 0; }
 
+int uwgpu_bfbt_operator_apply(uwgpu_ctx* ctx, int32_t form, const double* x, double* y) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(x && y, UWGPU_ERR_ARGUMENT, "x and y are required");
+        uwg::bfbt_operator_hook(c, form, x, y, 0, nullptr);
+    });
+}
+
+int uwgpu_time_bfbt_apply(uwgpu_ctx* ctx, int32_t form, int32_t iterations, double* ms) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(ms && iterations > 0, UWGPU_ERR_ARGUMENT, "bad arguments");
+        uwg::bfbt_operator_hook(c, form, nullptr, nullptr, iterations, ms);
+    });
+}
+
 int uwgpu_time_apply(uwgpu_ctx* ctx, int32_t precision, int32_t iterations, double* ms) {
     return guarded(ctx, [&](Context& c) {
         UWG_REQUIRE(ms && iterations > 0, UWGPU_ERR_ARGUMENT, "bad arguments");

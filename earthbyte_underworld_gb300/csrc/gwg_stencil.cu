@@ -20,13 +20,19 @@
 #include <algorithm>
 #include <cmath>
 #include <iterator>
+#include <type_traits>
 
 #include "internal.cuh"
 
 namespace uwg {
 
-// fine-mesh element widths h[off[d] + i] (operator.cu)
+// fine-mesh element widths h[off[d] + i] (operator.cu), FP64 and FP32
 const double* fine_widths(Context& c, int off[3]);
+const float* fine_widths32(Context& c, int off[3]);
+void bfbt_weights(Context& c, double* W);
+void to_float(Context& c, const double* a, float* b, int64_t n);
+void to_double(Context& c, const float* a, double* b, int64_t n);
+void gwg_stencil_build(Context& c, const double* W, double* A, double* dinv);
 
 namespace {
 
@@ -287,6 +293,167 @@ __global__ void k_gwg_init(int64_t ne, const double* __restrict__ b, const T* __
 }
 
 // ------------------------------------------------------------------------------------------
+// Matrix-free FP32 apply (mixed form).  In FP32 the G, W, G^T chain is cheap arithmetic (FP32
+// issues at 58x the FP64 rate), so the mixed form applies G^T W G without the stencil.  A block
+// takes a tile of kMfX x kMfY x TZ elements (kMfX x kMfY in 2D), stages z on the tile and its
+// one-element halo in shared memory, forms y = W G z at the tile's nodes (shared memory), then
+// (G^T y)_e for its elements, fused with the direction update of k_cg_spmv_dir.  Per element it
+// streams z, p, q (read), p, q (written) and about one node's W instead of 27 stencil
+// coefficients; on a 128^3 mesh every array an iteration touches fits in L2 together.
+// G_(n,d),f = -s prod_{k != d} h_k(f) / 2^(dim-1), s = +1 when n is on the upper side of f along d
+// (the convention of k_gwg_build); W is zero on fixed velocity components.
+// ------------------------------------------------------------------------------------------
+constexpr int kMfX = 32, kMfY = 8;
+
+template <int DIM, int TZ>
+__global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf_dir(EGrid g, int64_t nnx, int64_t nny, int64_t nn,
+                                                           const float* __restrict__ h, int off1, int off2,
+                                                           const float* __restrict__ W, const float* __restrict__ z,
+                                                           float* __restrict__ p, float* __restrict__ q,
+                                                           double* __restrict__ scal, int k, int first) {
+    constexpr int HX = kMfX + 2, HY = kMfY + 2, HZ = DIM == 3 ? TZ + 2 : 1;   // element halo
+    constexpr int NX = kMfX + 1, NY = kMfY + 1, NZ = DIM == 3 ? TZ + 1 : 1;   // tile nodes
+    constexpr int NN = NX * NY * NZ;
+    constexpr int EZ = DIM == 3 ? TZ : 1;                                     // elements per thread
+    __shared__ float zs[HZ * HY * HX];
+    __shared__ float ys[DIM * NN];
+    __shared__ float hw[HX + HY + HZ];   // widths of the halo elements per axis (0 outside the mesh)
+    __shared__ double sw[32];
+    __shared__ float s_beta;
+    const float beta = first ? 0.f : block_ratio<float>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
+    const int ex = (int)g.ex, ey = (int)g.ey, ez = (int)g.ez;
+    const int ntx = (ex + kMfX - 1) / kMfX, nty = (ey + kMfY - 1) / kMfY;
+    int bi = blockIdx.x;
+    const int x0 = (bi % ntx) * kMfX;
+    bi /= ntx;
+    const int y0 = (bi % nty) * kMfY;
+    bi /= nty;
+    const int z0 = DIM == 3 ? bi * TZ : 0;
+    const int tid = threadIdx.x;
+    for (int i = tid; i < HX + HY + HZ; i += blockDim.x) {
+        int idx, n, o;
+        if (i < HX) {
+            idx = x0 - 1 + i, n = ex, o = 0;
+        } else if (i < HX + HY) {
+            idx = y0 - 1 + (i - HX), n = ey, o = off1;
+        } else {
+            idx = z0 - 1 + (i - HX - HY), n = DIM == 3 ? ez : 0, o = off2;
+        }
+        hw[i] = idx >= 0 && idx < n ? h[o + idx] : 0.f;
+    }
+    for (int i = tid; i < HZ * HY * HX; i += blockDim.x) {
+        const int gx = x0 - 1 + i % HX, gy = y0 - 1 + (i / HX) % HY, gz = DIM == 3 ? z0 - 1 + i / (HX * HY) : 0;
+        zs[i] = (gx >= 0 && gx < ex && gy >= 0 && gy < ey && gz >= 0 && gz < ez) ? z[gx + ex * (gy + ey * gz)] : 0.f;
+    }
+    __syncthreads();
+    const float* hx = hw;
+    const float* hy = hw + HX;
+    const float* hz = hw + HX + HY;
+    const float sc = DIM == 3 ? 0.25f : 0.5f;
+    // y_(n,d) = W_(n,d) sum over the 2^dim elements f = n - 1 + a of G_(n,d),f z_f
+    for (int i = tid; i < NN; i += blockDim.x) {
+        const int nx = i % NX, ny = (i / NX) % NY, nz = DIM == 3 ? i / (NX * NY) : 0;
+        const int gx = x0 + nx, gy = y0 + ny, gz = z0 + nz;
+        float acc[3] = {0.f, 0.f, 0.f};
+        const bool inside = gx <= ex && gy <= ey && (DIM == 2 || gz <= ez);
+        if (inside) {
+#pragma unroll
+            for (int a = 0; a < (1 << DIM); ++a) {
+                const int ax = a & 1, ay = (a >> 1) & 1, az = (a >> 2) & 1;
+                const float zv = zs[(DIM == 3 ? (nz + az) * HY * HX : 0) + (ny + ay) * HX + nx + ax];
+                const float wx = hx[nx + ax], wy = hy[ny + ay];
+                if (DIM == 3) {
+                    const float wz = hz[nz + az];
+                    acc[0] += (ax ? sc : -sc) * (wy * wz) * zv;
+                    acc[1] += (ay ? sc : -sc) * (wx * wz) * zv;
+                    acc[2] += (az ? sc : -sc) * (wx * wy) * zv;
+                } else {
+                    acc[0] += (ax ? sc : -sc) * wy * zv;
+                    acc[1] += (ay ? sc : -sc) * wx * zv;
+                }
+            }
+        }
+        const int64_t node = inside ? gx + nnx * (gy + nny * gz) : 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) ys[d * NN + i] = inside ? W[(int64_t)d * nn + node] * acc[d] : 0.f;
+    }
+    __syncthreads();
+    // (G^T y)_e over the corners b of e, then p = z + beta p, q = A z + beta q, pq_{k+1}
+    const int lx = tid % kMfX, ly = tid / kMfX;
+    float local = 0.f;
+#pragma unroll
+    for (int lz = 0; lz < EZ; ++lz) {
+        const int gx = x0 + lx, gy = y0 + ly, gz = z0 + lz;
+        if (gx < ex && gy < ey && gz < (DIM == 3 ? ez : 1)) {
+            const float wx = hx[lx + 1], wy = hy[ly + 1], wz = DIM == 3 ? hz[lz + 1] : 1.f;
+            const float a0 = sc * (DIM == 3 ? wy * wz : wy), a1 = sc * (DIM == 3 ? wx * wz : wx), a2 = sc * wx * wy;
+            float out = 0.f;
+#pragma unroll
+            for (int b = 0; b < (1 << DIM); ++b) {
+                const int bx = b & 1, by = (b >> 1) & 1, bz = (b >> 2) & 1;
+                const int ni = ((DIM == 3 ? lz + bz : 0) * NY + ly + by) * NX + lx + bx;
+                out = fmaf(bx ? -a0 : a0, ys[ni], out);
+                out = fmaf(by ? -a1 : a1, ys[NN + ni], out);
+                if (DIM == 3) out = fmaf(bz ? -a2 : a2, ys[2 * NN + ni], out);
+            }
+            const int e = gx + ex * (gy + ey * gz);
+            const float ze = zs[((DIM == 3 ? lz + 1 : 0) * HY + ly + 1) * HX + lx + 1];
+            const float pe = first ? ze : fmaf(beta, p[e], ze);
+            const float qe = first ? out : fmaf(beta, q[e], out);
+            p[e] = pe;
+            q[e] = qe;
+            local = fmaf(pe, qe, local);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *rr_slot(scal, k + 1) = 0.0;
+    double t = block_sum<float>(local, sw);
+    if (threadIdx.x == 0) atomicAdd(pq_slot(scal, k + 1), t);
+}
+
+// the launch of the matrix-free direction kernel: tile depth 4 when that still gives four tiles
+// per SM, else 2 (3D)
+struct MfLaunch {
+    EGrid g;
+    int64_t nnx, nny, nn;
+    const float* h;
+    int off1, off2;
+    const float* W;
+    int dim, tz;
+    unsigned blocks;
+};
+
+static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* h, const int off[3], const float* W, int sms) {
+    MfLaunch L;
+    L.g = g;
+    L.nnx = m.nnx;
+    L.nny = m.nny;
+    L.nn = m.nn;
+    L.h = h;
+    L.off1 = off[1];
+    L.off2 = off[2];
+    L.W = W;
+    L.dim = m.dim;
+    const int64_t txy = ((g.ex + kMfX - 1) / kMfX) * ((g.ey + kMfY - 1) / kMfY);
+    L.tz = m.dim == 3 && txy * ((g.ez + 3) / 4) >= 4 * (int64_t)sms ? 4 : 2;
+    L.blocks = (unsigned)(m.dim == 3 ? txy * ((g.ez + L.tz - 1) / L.tz) : txy);
+    return L;
+}
+
+static void mf_dir(const MfLaunch& L, cudaStream_t st, const float* z, float* p, float* q, double* scal, int k,
+                   int first) {
+    const unsigned nt = kMfX * kMfY;
+    if (L.dim == 2)
+        k_cg_mf_dir<2, 1><<<L.blocks, nt, 0, st>>>(L.g, L.nnx, L.nny, L.nn, L.h, L.off1, L.off2, L.W, z, p, q, scal, k,
+                                                   first);
+    else if (L.tz == 4)
+        k_cg_mf_dir<3, 4><<<L.blocks, nt, 0, st>>>(L.g, L.nnx, L.nny, L.nn, L.h, L.off1, L.off2, L.W, z, p, q, scal, k,
+                                                   first);
+    else
+        k_cg_mf_dir<3, 2><<<L.blocks, nt, 0, st>>>(L.g, L.nnx, L.nny, L.nn, L.h, L.off1, L.off2, L.W, z, p, q, scal, k,
+                                                   first);
+}
+
+// ------------------------------------------------------------------------------------------
 // Multigrid preconditioner for the inner solves (option bfbt_inner_pc = 1): the element grid is
 // coarsened 2:1 per axis by aggregation (a coarse element is the union of its 2^dim children;
 // prolongation copies the parent's value, restriction sums the children), the coarse operator
@@ -521,12 +688,12 @@ void gwg_stencil_build(Context& c, const double* W, double* A, double* dinv) {
     check_launch("k_gwg_build");
 }
 
-// FP32 copies of the stencil and the inverse diagonal (mixed form)
+// FP32 copies of the stencil (skipped when A32 is null) and the inverse diagonal (mixed form)
 void gwg_stencil_fp32(Context& c, const double* A, const double* dinv, float* A32, float* dinv32) {
     const MeshDesc& m = c.levels[0].mesh;
     int64_t ne = m.ne, na = ne * (m.dim == 3 ? 27 : 9);
     LaunchScope ls(c, -1);
-    k_gwg_convert<double, float><<<blocks_for(na, 256), 256, 0, c.stream>>>(na, A, A32);
+    if (A32) k_gwg_convert<double, float><<<blocks_for(na, 256), 256, 0, c.stream>>>(na, A, A32);
     k_gwg_convert<double, float><<<blocks_for(ne, 256), 256, 0, c.stream>>>(ne, dinv, dinv32);
     c.launches++;
     check_launch("k_gwg_convert");
@@ -545,28 +712,46 @@ void gwg_stencil_apply(Context& c, const double* A, const double* x, double* y, 
 
 // Solves A x = b (b projected off the constant by the caller when A has it) to
 // ||r|| <= rtol ||b|| by Jacobi-preconditioned CG.  work holds 4*ne values of T, scal 8 doubles.
+// With Wmf (FP32 only) A is applied matrix-free from the nodal weights instead of the stencil.
 // Returns the iterations taken.
 template <typename T>
-static int gwg_cg_T(Context& c, const T* A, const T* dinv, const double* b, T* x, double rtol, int maxit, T* work,
-                    double* scal) {
+static int gwg_cg_T(Context& c, const T* A, const float* Wmf, const T* dinv, const double* b, T* x, double rtol,
+                    int maxit, T* work, double* scal) {
     const MeshDesc& m = c.levels[0].mesh;
     EGrid g = egrid_of(m);
     const int64_t ne = g.ne;
     const int nb = m.dim == 3 ? 27 : 9;
+    MfLaunch mf{};
+    if (Wmf) {
+        int off[3], sms = 0;
+        const float* h = fine_widths32(c, off);
+        UWG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
+        mf = mf_launch(m, g, h, off, Wmf, sms);
+    }
     T* r = work;
     T* z = work + ne;
     T* p = work + 2 * ne;
     T* q = work + 3 * ne;
-    UWG_CUDA(cudaMemsetAsync(scal, 0, 8 * sizeof(double), c.stream));
     const unsigned eb = blocks_for(ne, 256), ebv = blocks_for(ne, 256 * kEpt);
+    // direction kernel of iteration k: p = z + beta p, q = A z + beta q, pq_{k+1}
+    auto dir = [&](int k, int first) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (Wmf) {
+                mf_dir(mf, c.stream, z, p, q, scal, k, first);
+                return;
+            }
+        }
+        if (m.dim == 3) k_cg_spmv_dir<3, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, first);
+        else k_cg_spmv_dir<2, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, first);
+    };
+    UWG_CUDA(cudaMemsetAsync(scal, 0, 8 * sizeof(double), c.stream));
     {
         LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
         k_gwg_init<T><<<eb, 256, 0, c.stream>>>(ne, b, dinv, x, r, z, scal);
     }
     {
         LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
-        if (m.dim == 3) k_cg_spmv_dir<3, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, -1, 1);
-        else k_cg_spmv_dir<2, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, -1, 1);
+        dir(-1, 1);
     }
     double* hs = c.host_scalars;
     UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -578,11 +763,10 @@ static int gwg_cg_T(Context& c, const T* A, const T* dinv, const double* b, T* x
     const int block = 12;
     auto issue = [&](int k) {
         k_cg_update<T><<<ebv, 256, 0, c.stream>>>(ne, p, q, dinv, x, r, z, scal, k, k == block - 1);
-        if (m.dim == 3) k_cg_spmv_dir<3, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, 0);
-        else k_cg_spmv_dir<2, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, 0);
+        dir(k, 0);
     };
-    const void* key[8] = {A, dinv, x, work, scal, (const void*)(intptr_t)ne, (const void*)(intptr_t)sizeof(T),
-                          (const void*)(intptr_t)(m.dim + 16)};
+    const void* key[8] = {Wmf ? (const void*)Wmf : (const void*)A, dinv, x, work, scal, (const void*)(intptr_t)ne,
+                          (const void*)(intptr_t)sizeof(T), (const void*)(intptr_t)(m.dim + (Wmf ? 48 : 16))};
     Context::PcgGraph* pg = nullptr;
     for (auto& cand : c.pcg_graphs)
         if (std::equal(std::begin(key), std::end(key), std::begin(cand.key))) pg = &cand;
@@ -598,9 +782,10 @@ static int gwg_cg_T(Context& c, const T* A, const T* dinv, const double* b, T* x
         UWG_CUDA(cudaGraphDestroy(graph));
     }
     // algorithmic traffic of one iteration: update (p, q, dinv, x, r read; x, r, z written) and
-    // spmv+direction (the stencil, z, p, q read; p, q written)
-    const double it_bytes = (double)ne * sizeof(T) * (8 + nb + 5);
-    const double it_flops = (double)ne * (2.0 * nb + 14.0);
+    // spmv+direction (the stencil, z, p, q read; p, q written; matrix-free: the dim nodal
+    // weights of about one node per element in place of the stencil)
+    const double it_bytes = (double)ne * sizeof(T) * (8 + (Wmf ? m.dim : nb) + 5);
+    const double it_flops = Wmf ? (double)ne * (m.dim == 3 ? 110.0 : 46.0) : (double)ne * (2.0 * nb + 14.0);
     int it = 0;
     while (it < maxit) {
         {
@@ -622,12 +807,95 @@ static int gwg_cg_T(Context& c, const T* A, const T* dinv, const double* b, T* x
 
 int gwg_cg(Context& c, const double* A, const double* dinv, const double* b, double* x, double rtol, int maxit,
            double* work, double* scal) {
-    return gwg_cg_T<double>(c, A, dinv, b, x, rtol, maxit, work, scal);
+    return gwg_cg_T<double>(c, A, nullptr, dinv, b, x, rtol, maxit, work, scal);
 }
 
 int gwg_cg32(Context& c, const float* A, const float* dinv, const double* b, float* x, double rtol, int maxit,
              float* work, double* scal) {
-    return gwg_cg_T<float>(c, A, dinv, b, x, rtol, maxit, work, scal);
+    return gwg_cg_T<float>(c, A, nullptr, dinv, b, x, rtol, maxit, work, scal);
+}
+
+// the mixed form's inner solve: G^T W G applied matrix-free from W32 (FP32 nodal weights, zero on
+// fixed components)
+int gwg_cg32_mf(Context& c, const float* W32, const float* dinv, const double* b, float* x, double rtol, int maxit,
+                float* work, double* scal) {
+    return gwg_cg_T<float>(c, nullptr, W32, dinv, b, x, rtol, maxit, work, scal);
+}
+
+// Test and timing hook on the inner operator of the current fine velocity operator: W, the FP64
+// stencil and (form 2) its FP32 copy are built here, then the direction kernel of the inner CG
+// runs with p = z, q = A z in the given form (0: FP64 stencil, 1: FP32 matrix-free, 2: FP32
+// stencil).  With xh, y = A x is returned in yh; with iterations > 0 the kernel is launched that
+// many times back to back and the elapsed device time is returned in ms.
+void bfbt_operator_hook(Context& c, int form, const double* xh, double* yh, int iterations, double* ms) {
+    UWG_REQUIRE(c.operator_built, UWGPU_ERR_STATE, "the fine velocity operator is not built (solve first)");
+    UWG_REQUIRE(form >= 0 && form <= 2, UWGPU_ERR_ARGUMENT, "form must be 0, 1 or 2");
+    const MeshDesc& m = c.levels[0].mesh;
+    const EGrid g = egrid_of(m);
+    const int nb = m.dim == 3 ? 27 : 9;
+    const int64_t ne = g.ne, nv = m.nn * m.dim;
+    UWG_REQUIRE(ne * nb < (int64_t)1 << 31, UWGPU_ERR_TOO_LARGE, "BFBt stencil: element count too large");
+    DArray<double> W, A, dinv, x, pq, scal;
+    DArray<float> W32, A32, x32, pq32;
+    W.ensure((size_t)nv);
+    A.ensure((size_t)nb * ne);
+    dinv.ensure((size_t)ne);
+    x.ensure((size_t)ne);
+    pq.ensure((size_t)2 * ne);
+    scal.ensure(8);
+    bfbt_weights(c, W.p);
+    gwg_stencil_build(c, W.p, A.p, dinv.p);
+    if (xh) UWG_CUDA(cudaMemcpyAsync(x.p, xh, (size_t)ne * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    else UWG_CUDA(cudaMemsetAsync(x.p, 0, (size_t)ne * sizeof(double), c.stream));
+    MfLaunch mf{};
+    if (form != 0) {
+        x32.ensure((size_t)ne);
+        pq32.ensure((size_t)2 * ne);
+        to_float(c, x.p, x32.p, ne);
+        if (form == 1) {
+            W32.ensure((size_t)nv);
+            to_float(c, W.p, W32.p, nv);
+            int off[3], sms = 0;
+            const float* h = fine_widths32(c, off);
+            UWG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
+            mf = mf_launch(m, g, h, off, W32.p, sms);
+        } else {
+            A32.ensure((size_t)nb * ne);
+            to_float(c, A.p, A32.p, (int64_t)nb * ne);
+        }
+    }
+    auto launch = [&]() {
+        const unsigned eb = blocks_for(ne, 256);
+        if (form == 1) mf_dir(mf, c.stream, x32.p, pq32.p, pq32.p + ne, scal.p, -1, 1);
+        else if (form == 2 && m.dim == 3) k_cg_spmv_dir<3, float><<<eb, 256, 0, c.stream>>>(g, A32.p, x32.p, pq32.p, pq32.p + ne, scal.p, -1, 1);
+        else if (form == 2) k_cg_spmv_dir<2, float><<<eb, 256, 0, c.stream>>>(g, A32.p, x32.p, pq32.p, pq32.p + ne, scal.p, -1, 1);
+        else if (m.dim == 3) k_cg_spmv_dir<3, double><<<eb, 256, 0, c.stream>>>(g, A.p, x.p, pq.p, pq.p + ne, scal.p, -1, 1);
+        else k_cg_spmv_dir<2, double><<<eb, 256, 0, c.stream>>>(g, A.p, x.p, pq.p, pq.p + ne, scal.p, -1, 1);
+    };
+    UWG_CUDA(cudaMemsetAsync(scal.p, 0, 8 * sizeof(double), c.stream));
+    launch();
+    check_launch("bfbt operator hook");
+    if (yh) {
+        if (form != 0) to_double(c, pq32.p + ne, pq.p + ne, ne);
+        UWG_CUDA(cudaMemcpyAsync(yh, pq.p + ne, (size_t)ne * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    }
+    if (iterations > 0 && ms) {
+        cudaEvent_t e0, e1;
+        UWG_CUDA(cudaEventCreate(&e0));
+        UWG_CUDA(cudaEventCreate(&e1));
+        UWG_CUDA(cudaEventRecord(e0, c.stream));
+        for (int i = 0; i < iterations; ++i) launch();
+        UWG_CUDA(cudaEventRecord(e1, c.stream));
+        UWG_CUDA(cudaEventSynchronize(e1));
+        float t = 0.f;
+        UWG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        check_launch("bfbt operator hook timing");
+        *ms = t;
+        c.launches += iterations;
+    }
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
 }
 
 // ---- multigrid hierarchy for G^T W G ----------------------------------------------------
@@ -650,7 +918,7 @@ bool gwg_mg_build(Context& c, const double* A0, const double* dinv0, bool need32
     const MeshDesc& m = c.levels[0].mesh;
     // captured V-cycles carry this hierarchy's Chebyshev coefficients: drop them
     for (auto it = c.pcg_graphs.begin(); it != c.pcg_graphs.end();) {
-        if ((intptr_t)it->key[7] >= 32) {
+        if ((intptr_t)it->key[7] >= 32 && (intptr_t)it->key[7] < 48) {
             if (it->exec) cudaGraphExecDestroy(it->exec);
             it = c.pcg_graphs.erase(it);
         } else {
@@ -855,8 +1123,8 @@ static int gwg_cg_mg_T(Context& c, const T* A, const T* dinv, const double* b, T
     UWG_CUDA(cudaStreamSynchronize(c.stream));
     const double r0 = std::sqrt(hs[7]);
     if (!(r0 > 0.0)) return 0;
-    // four iterations per graph (the rz slots cycle with period 3, pq / rr with 2: 12 would be
-    // the period, but each iteration carries a V-cycle, so the host checks more often)
+    // six iterations per graph: the rz slots cycle with period 3 and the pq / rr slots with 2, so
+    // every launch of the graph finds its slots where the previous one left them
     const int block = 6;
     auto issue = [&](int k) {
         k_cgm_update<T><<<ebv, 256, 0, c.stream>>>(ne, p, q, x, r, scal, k, k == block - 1);

@@ -261,6 +261,7 @@ void build_operator(Context& c, int levels, bool need32);
 void apply_fine(Context& c, bool fp32, const double* x, double* y);  // device SoA vectors
 void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep);
 void estimate_fine_lmax(Context& c, const uwgpu_solve_opts& o);
+void bfbt_operator_hook(Context& c, int form, const double* xh, double* yh, int iterations, double* ms);
 void advect_particles(Context& c, double dt, int order, bool fallback, uint32_t& fell_back, uint32_t& left_mesh);
 template <typename T> void level_cheb(Context&, Level&, const T*, T*, int, bool);
 int learned_generate(Context& c, const uwgpu_solve_opts& o, int nsamples, uint64_t seed);

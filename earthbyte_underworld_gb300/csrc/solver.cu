@@ -47,6 +47,8 @@ int gwg_cg_mg(Context& c, const double* A, const double* dinv, const double* b, 
               double* work, double* scal);
 int gwg_cg_mg32(Context& c, const float* A, const float* dinv, const double* b, float* x, double rtol, int maxit,
                 float* work, double* scal);
+int gwg_cg32_mf(Context& c, const float* W32, const float* dinv, const double* b, float* x, double rtol, int maxit,
+                float* work, double* scal);
 void op_wg32(Context& c, const float* p, const float* W, float* s);
 void op_gt32(Context& c, const float* s, float* q);
 void to_float(Context& c, const double* a, float* b, int64_t n);
@@ -661,14 +663,21 @@ struct Bsscr {
                             : gwg_cg(c, bA.p, bd.p, pr.p, x, rtol, maxit, pz.p, pz.p + 4 * npres);
     }
 
-    // the same preconditioner with FP32 operators, inner solves and vectors (mixed form)
-    void bfbt_apply32(const double* x, double* y) {
+    // FP32 inner solve of G^T W G into bt32: multigrid-preconditioned on the FP32 stencil, Jacobi
+    // on the stencil (bfbt_inner_pc = 2), or Jacobi with the matrix-free apply (default)
+    int inner32(const double* b) {
         int maxit = o.bfbt_max_it > 0 ? o.bfbt_max_it : 500;
         double rtol = o.bfbt_rtol > 0 ? o.bfbt_rtol : 1e-4;
+        if (bfbt_mg) return gwg_cg_mg32(c, bA32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
+        if (o.bfbt_inner_pc == 2) return gwg_cg32(c, bA32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
+        return gwg_cg32_mf(c, bw32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
+    }
+
+    // the same preconditioner with FP32 operators, inner solves and vectors (mixed form)
+    void bfbt_apply32(const double* x, double* y) {
         copy<double>(c, npres, x, pr.p);
         if (bbt_const) remove_constant_dev(pr.p);
-        bfbt_its += bfbt_mg ? gwg_cg_mg32(c, bA32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, scal32.p)
-                            : gwg_cg32(c, bA32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, scal32.p);
+        bfbt_its += inner32(pr.p);
         op_wg32(c, bt32.p, bw32.p, bs32.p);
         level_apply<float>(c, c.levels[0], bs32.p, bX32.p);
         {
@@ -678,8 +687,7 @@ struct Bsscr {
         op_gt32(c, bX32.p, bt2_32.p);
         to_double(c, bt2_32.p, pr.p, npres);
         if (bbt_const) remove_constant_dev(pr.p);
-        bfbt_its += bfbt_mg ? gwg_cg_mg32(c, bA32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, scal32.p)
-                            : gwg_cg32(c, bA32.p, bd32.p, pr.p, bt32.p, rtol, maxit, pz32.p, scal32.p);
+        bfbt_its += inner32(pr.p);
         to_double(c, bt32.p, y, npres);
     }
 
@@ -982,9 +990,12 @@ void Bsscr::run() {
             for (auto* v : {&bd32, &bt32, &bt2_32}) v->ensure(npres);
             pz32.ensure(4 * npres);
             scal32.ensure(8);
-            to_float(c, bw.p, bw32.p, nv);
-            bA32.ensure((size_t)(dim == 3 ? 27 : 9) * npres);
-            gwg_stencil_fp32(c, bA.p, bd.p, bA32.p, bd32.p);
+            to_float(c, bw.p, bw32.p, nv);   // zero on fixed components: the matrix-free inner operator's W
+            // the explicit FP32 stencil only where the inner solve reads it (multigrid levels, or
+            // the stencil form asked for); the default mixed inner solve is matrix-free
+            const bool want_stencil32 = o.bfbt_inner_pc != 0;
+            if (want_stencil32) bA32.ensure((size_t)(dim == 3 ? 27 : 9) * npres);
+            gwg_stencil_fp32(c, bA.p, bd.p, want_stencil32 ? bA32.p : nullptr, bd32.p);
         }
         if (o.bfbt_inner_pc == 1) bfbt_mg = gwg_mg_build(c, bA.p, bd.p, mixed, bbt_const);
     }
@@ -1048,7 +1059,7 @@ void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
     UWG_REQUIRE(o.remove_const_p >= 0 && o.remove_const_p <= 2, UWGPU_ERR_ARGUMENT, "bad pressure null-space mode");
     UWG_REQUIRE(o.learned_pc == 0 || o.learned_pc == 1, UWGPU_ERR_ARGUMENT, "bad learned_pc");
     UWG_REQUIRE(o.mg_cycle == 1 || o.mg_cycle == 2, UWGPU_ERR_ARGUMENT, "mg_cycle must be 1 (V) or 2 (W)");
-    UWG_REQUIRE(o.bfbt_inner_pc == 0 || o.bfbt_inner_pc == 1, UWGPU_ERR_ARGUMENT, "bfbt_inner_pc must be 0 or 1");
+    UWG_REQUIRE(o.bfbt_inner_pc >= 0 && o.bfbt_inner_pc <= 2, UWGPU_ERR_ARGUMENT, "bfbt_inner_pc must be 0, 1 or 2");
     Bsscr s(c, o, rep);
     s.run();
 }

@@ -125,6 +125,8 @@ def load(build_if_missing: bool = True):
         L.uwgpu_time_apply.argtypes = [P, C.c_int32, C.c_int32, P]
         L.uwgpu_time_smooth.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, P]
         L.uwgpu_time_chebyshev.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, P]
+        L.uwgpu_bfbt_operator_apply.argtypes = [P, C.c_int32, P, P]
+        L.uwgpu_time_bfbt_apply.argtypes = [P, C.c_int32, C.c_int32, P]
         L.uwgpu_launch_count.argtypes = [P]
         L.uwgpu_launch_count.restype = C.c_int64
         L.uwgpu_learned_create.argtypes = [P, C.c_int32, C.c_int32, C.c_uint64]
@@ -348,6 +350,19 @@ class Context:
     def time_smooth(self, precision=PREC_FP64, sweeps=2, iterations=10):
         ms = C.c_double()
         self._check(self._L.uwgpu_time_smooth(self._h, precision, sweeps, iterations, C.byref(ms)))
+        return ms.value
+
+    def bfbt_operator_apply(self, x, form=0):
+        """y = G^T W G x, the scaled BFBt inner operator of the current fine operator (form 0: FP64
+        stencil, 1: FP32 matrix-free, 2: FP32 stencil)"""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty_like(x)
+        self._check(self._L.uwgpu_bfbt_operator_apply(self._h, form, _ptr(x), _ptr(y)))
+        return y
+
+    def time_bfbt_apply(self, form=1, iterations=20):
+        ms = C.c_double()
+        self._check(self._L.uwgpu_time_bfbt_apply(self._h, form, iterations, C.byref(ms)))
         return ms.value
 
     def time_chebyshev(self, precision=PREC_FP64, degree=2, iterations=10):

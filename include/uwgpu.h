@@ -124,7 +124,9 @@ typedef struct {
     int32_t mg_cycle;         /* coarse corrections per level visit: 1 V-cycle (default), 2 W-cycle
                                  (-pc_mg_cycle_type v|w of the velocity PCMG)                */
     int32_t bfbt_inner_pc;    /* preconditioner of the scaled BFBt inner G^T W G solves: 0 Jacobi (default,
-                                 as the reference's KSP), 1 aggregation multigrid V-cycle      */
+                                 as the reference's KSP; the mixed form applies G^T W G
+                                 matrix-free in FP32), 1 aggregation multigrid V-cycle, 2 Jacobi
+                                 on the explicit FP32 stencil in the mixed form                */
 } uwgpu_solve_opts;
 
 typedef struct {
@@ -286,6 +288,15 @@ int uwgpu_time_chebyshev(uwgpu_ctx* ctx, int32_t precision, int32_t degree, int3
  * of `sweeps` symmetric colour Gauss-Seidel sweeps.  precision as in uwgpu_operator_apply. */
 int uwgpu_time_apply(uwgpu_ctx* ctx, int32_t precision, int32_t iterations, double* ms);
 int uwgpu_time_smooth(uwgpu_ctx* ctx, int32_t precision, int32_t sweeps, int32_t iterations, double* ms);
+
+/* Test and timing hooks on the inner operator of the scaled BFBt preconditioner, G^T W G with
+ * W = 1/rowmax(K) of the current fine velocity operator (pc_ScaledGtKG.c:735-760; built by a
+ * previous solve, else UWGPU_ERR_STATE).  form 0: the FP64 element stencil; 1: the FP32
+ * matrix-free apply of the mixed form; 2: the FP32 stencil.  uwgpu_bfbt_operator_apply: y = A x
+ * (host arrays of one value per element).  uwgpu_time_bfbt_apply: `iterations` launches of the
+ * inner CG's operator kernel in that form, elapsed device milliseconds in ms. */
+int uwgpu_bfbt_operator_apply(uwgpu_ctx* ctx, int32_t form, const double* x, double* y);
+int uwgpu_time_bfbt_apply(uwgpu_ctx* ctx, int32_t form, int32_t iterations, double* ms);
 
 /* Allocation-free binning + mapping.  This entry point has no counterpart in the reference; it
  * exists for callers that cannot allocate device memory while they run (a host framework that
