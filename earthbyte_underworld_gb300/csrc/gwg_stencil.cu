@@ -311,16 +311,17 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf_dir(EGrid g, int64_t nnx,
                                                            const float* __restrict__ W, const float* __restrict__ z,
                                                            float* __restrict__ p, float* __restrict__ q,
                                                            double* __restrict__ scal, int k, int first) {
+    constexpr int NT = kMfX * kMfY;                                            // threads
     constexpr int HX = kMfX + 2, HY = kMfY + 2, HZ = DIM == 3 ? TZ + 2 : 1;   // element halo
     constexpr int NX = kMfX + 1, NY = kMfY + 1, NZ = DIM == 3 ? TZ + 1 : 1;   // tile nodes
     constexpr int NN = NX * NY * NZ;
+    constexpr int NPT = (NN + NT - 1) / NT;                                   // nodes per thread
     constexpr int EZ = DIM == 3 ? TZ : 1;                                     // elements per thread
     __shared__ float zs[HZ * HY * HX];
     __shared__ float ys[DIM * NN];
     __shared__ float hw[HX + HY + HZ];   // widths of the halo elements per axis (0 outside the mesh)
     __shared__ double sw[32];
     __shared__ float s_beta;
-    const float beta = first ? 0.f : block_ratio<float>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
     const int ex = (int)g.ex, ey = (int)g.ey, ez = (int)g.ez;
     const int ntx = (ex + kMfX - 1) / kMfX, nty = (ey + kMfY - 1) / kMfY;
     int bi = blockIdx.x;
@@ -330,7 +331,30 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf_dir(EGrid g, int64_t nnx,
     bi /= nty;
     const int z0 = DIM == 3 ? bi * TZ : 0;
     const int tid = threadIdx.x;
-    for (int i = tid; i < HX + HY + HZ; i += blockDim.x) {
+    const int lx = tid % kMfX, ly = tid / kMfX;
+    // every global load of the block is issued before the first barrier: this thread's nodal
+    // weights and (after the first iteration) its elements' p and q, then the z halo
+    float wv[NPT][DIM];
+#pragma unroll
+    for (int j = 0; j < NPT; ++j) {
+        const int i = tid + j * NT;
+        const int nx = i % NX, ny = (i / NX) % NY, nz = DIM == 3 ? i / (NX * NY) : 0;
+        const int gx = x0 + nx, gy = y0 + ny, gz = z0 + nz;
+        const bool inside = i < NN && gx <= ex && gy <= ey && (DIM == 2 || gz <= ez);
+        const int64_t node = inside ? gx + nnx * (gy + nny * gz) : 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) wv[j][d] = inside ? __ldg(W + (int64_t)d * nn + node) : 0.f;
+    }
+    float pv[EZ], qv[EZ];
+#pragma unroll
+    for (int lz = 0; lz < EZ; ++lz) {
+        const int gx = x0 + lx, gy = y0 + ly, gz = z0 + lz;
+        const bool valid = !first && gx < ex && gy < ey && gz < (DIM == 3 ? ez : 1);
+        const int e = valid ? gx + ex * (gy + ey * gz) : 0;
+        pv[lz] = valid ? p[e] : 0.f;
+        qv[lz] = valid ? q[e] : 0.f;
+    }
+    for (int i = tid; i < HX + HY + HZ; i += NT) {
         int idx, n, o;
         if (i < HX) {
             idx = x0 - 1 + i, n = ex, o = 0;
@@ -339,29 +363,32 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf_dir(EGrid g, int64_t nnx,
         } else {
             idx = z0 - 1 + (i - HX - HY), n = DIM == 3 ? ez : 0, o = off2;
         }
-        hw[i] = idx >= 0 && idx < n ? h[o + idx] : 0.f;
+        hw[i] = idx >= 0 && idx < n ? __ldg(h + o + idx) : 0.f;
     }
-    for (int i = tid; i < HZ * HY * HX; i += blockDim.x) {
+    for (int i = tid; i < HZ * HY * HX; i += NT) {
         const int gx = x0 - 1 + i % HX, gy = y0 - 1 + (i / HX) % HY, gz = DIM == 3 ? z0 - 1 + i / (HX * HY) : 0;
-        zs[i] = (gx >= 0 && gx < ex && gy >= 0 && gy < ey && gz >= 0 && gz < ez) ? z[gx + ex * (gy + ey * gz)] : 0.f;
+        zs[i] = (gx >= 0 && gx < ex && gy >= 0 && gy < ey && gz >= 0 && gz < ez) ? __ldg(z + gx + ex * (gy + ey * gz))
+                                                                                 : 0.f;
     }
+    const float beta = first ? 0.f : block_ratio<float>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
     __syncthreads();
     const float* hx = hw;
     const float* hy = hw + HX;
     const float* hz = hw + HX + HY;
     const float sc = DIM == 3 ? 0.25f : 0.5f;
     // y_(n,d) = W_(n,d) sum over the 2^dim elements f = n - 1 + a of G_(n,d),f z_f
-    for (int i = tid; i < NN; i += blockDim.x) {
-        const int nx = i % NX, ny = (i / NX) % NY, nz = DIM == 3 ? i / (NX * NY) : 0;
-        const int gx = x0 + nx, gy = y0 + ny, gz = z0 + nz;
-        float acc[3] = {0.f, 0.f, 0.f};
-        const bool inside = gx <= ex && gy <= ey && (DIM == 2 || gz <= ez);
-        if (inside) {
+#pragma unroll
+    for (int j = 0; j < NPT; ++j) {
+        const int i = tid + j * NT;
+        if (i < NN) {
+            const int nx = i % NX, ny = (i / NX) % NY, nz = DIM == 3 ? i / (NX * NY) : 0;
+            float acc[3] = {0.f, 0.f, 0.f};
+            const float wx0 = hx[nx], wx1 = hx[nx + 1], wy0 = hy[ny], wy1 = hy[ny + 1];
 #pragma unroll
             for (int a = 0; a < (1 << DIM); ++a) {
                 const int ax = a & 1, ay = (a >> 1) & 1, az = (a >> 2) & 1;
                 const float zv = zs[(DIM == 3 ? (nz + az) * HY * HX : 0) + (ny + ay) * HX + nx + ax];
-                const float wx = hx[nx + ax], wy = hy[ny + ay];
+                const float wx = ax ? wx1 : wx0, wy = ay ? wy1 : wy0;
                 if (DIM == 3) {
                     const float wz = hz[nz + az];
                     acc[0] += (ax ? sc : -sc) * (wy * wz) * zv;
@@ -372,34 +399,60 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf_dir(EGrid g, int64_t nnx,
                     acc[1] += (ay ? sc : -sc) * wx * zv;
                 }
             }
-        }
-        const int64_t node = inside ? gx + nnx * (gy + nny * gz) : 0;
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) ys[d * NN + i] = inside ? W[(int64_t)d * nn + node] * acc[d] : 0.f;
+            for (int d = 0; d < DIM; ++d) ys[d * NN + i] = wv[j][d] * acc[d];
+        }
     }
     __syncthreads();
-    // (G^T y)_e over the corners b of e, then p = z + beta p, q = A z + beta q, pq_{k+1}
-    const int lx = tid % kMfX, ly = tid / kMfX;
+    // (G^T y)_e over the corners of e, marching up the thread's column of elements (the upper
+    // corner values of one element are the lower ones of the next), then p = z + beta p,
+    // q = A z + beta q and pq_{k+1}
+    const float wx = hx[lx + 1], wy = hy[ly + 1];
+    float lo[DIM][4];
+#pragma unroll
+    for (int c4 = 0; c4 < 4; ++c4) {
+        const int ni = (ly + (c4 >> 1)) * NX + lx + (c4 & 1);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) lo[d][c4] = ys[d * NN + ni];
+    }
     float local = 0.f;
 #pragma unroll
     for (int lz = 0; lz < EZ; ++lz) {
+        float out = 0.f;
+        if (DIM == 3) {
+            float hi[DIM][4];
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4) {
+                const int ni = ((lz + 1) * NY + ly + (c4 >> 1)) * NX + lx + (c4 & 1);
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) hi[d][c4] = ys[d * NN + ni];
+            }
+            const float wz = hz[lz + 1];
+            const float a0 = sc * wy * wz, a1 = sc * wx * wz, a2 = sc * wx * wy;
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4) {
+                out = fmaf((c4 & 1) ? -a0 : a0, lo[0][c4] + hi[0][c4], out);
+                out = fmaf((c4 >> 1) ? -a1 : a1, lo[1][c4] + hi[1][c4], out);
+                out = fmaf(a2, lo[DIM - 1][c4] - hi[DIM - 1][c4], out);
+            }
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4)
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) lo[d][c4] = hi[d][c4];
+        } else {
+            const float a0 = sc * wy, a1 = sc * wx;
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4) {
+                out = fmaf((c4 & 1) ? -a0 : a0, lo[0][c4], out);
+                out = fmaf((c4 >> 1) ? -a1 : a1, lo[1][c4], out);
+            }
+        }
         const int gx = x0 + lx, gy = y0 + ly, gz = z0 + lz;
         if (gx < ex && gy < ey && gz < (DIM == 3 ? ez : 1)) {
-            const float wx = hx[lx + 1], wy = hy[ly + 1], wz = DIM == 3 ? hz[lz + 1] : 1.f;
-            const float a0 = sc * (DIM == 3 ? wy * wz : wy), a1 = sc * (DIM == 3 ? wx * wz : wx), a2 = sc * wx * wy;
-            float out = 0.f;
-#pragma unroll
-            for (int b = 0; b < (1 << DIM); ++b) {
-                const int bx = b & 1, by = (b >> 1) & 1, bz = (b >> 2) & 1;
-                const int ni = ((DIM == 3 ? lz + bz : 0) * NY + ly + by) * NX + lx + bx;
-                out = fmaf(bx ? -a0 : a0, ys[ni], out);
-                out = fmaf(by ? -a1 : a1, ys[NN + ni], out);
-                if (DIM == 3) out = fmaf(bz ? -a2 : a2, ys[2 * NN + ni], out);
-            }
             const int e = gx + ex * (gy + ey * gz);
             const float ze = zs[((DIM == 3 ? lz + 1 : 0) * HY + ly + 1) * HX + lx + 1];
-            const float pe = first ? ze : fmaf(beta, p[e], ze);
-            const float qe = first ? out : fmaf(beta, q[e], out);
+            const float pe = first ? ze : fmaf(beta, pv[lz], ze);
+            const float qe = first ? out : fmaf(beta, qv[lz], out);
             p[e] = pe;
             q[e] = qe;
             local = fmaf(pe, qe, local);
