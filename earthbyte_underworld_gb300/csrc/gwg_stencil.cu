@@ -28,7 +28,6 @@ namespace uwg {
 
 // fine-mesh element widths h[off[d] + i] (operator.cu), FP64 and FP32
 const double* fine_widths(Context& c, int off[3]);
-const float* fine_widths32(Context& c, int off[3]);
 void bfbt_weights(Context& c, double* W);
 void to_float(Context& c, const double* a, float* b, int64_t n);
 void to_double(Context& c, const float* a, double* b, int64_t n);
@@ -294,216 +293,265 @@ __global__ void k_gwg_init(int64_t ne, const double* __restrict__ b, const T* __
 
 // ------------------------------------------------------------------------------------------
 // Matrix-free FP32 apply (mixed form).  In FP32 the G, W, G^T chain is cheap arithmetic (FP32
-// issues at 58x the FP64 rate), so the mixed form applies G^T W G without the stencil.  A block
-// takes a tile of kMfX x kMfY x TZ elements (kMfX x kMfY in 2D), stages z on the tile and its
-// one-element halo in shared memory, forms y = W G z at the tile's nodes (shared memory), then
-// (G^T y)_e for its elements, fused with the direction update of k_cg_spmv_dir.  Per element it
-// streams z, p, q (read), p, q (written) and about one node's W instead of 27 stencil
+// issues at 58x the FP64 rate), so the mixed form applies G^T W G without the stencil and streams
+// z, p, q (read), p, q (written) and about one node's W per element instead of 27 stencil
 // coefficients; on a 128^3 mesh every array an iteration touches fits in L2 together.
-// G_(n,d),f = -s prod_{k != d} h_k(f) / 2^(dim-1), s = +1 when n is on the upper side of f along d
-// (the convention of k_gwg_build); W is zero on fixed velocity components.
+// The mesh is uniform, so G_(n,d),f = -s a_d with s = +1 when n is on the upper side of f along d
+// and a_d = prod_{k != d} h_k / 2^(dim-1) (the convention of k_gwg_build).  With the folded
+// weights Wc_(n,d) = a_d^2 W_(n,d) (zero on fixed components):
+//   y_(n,d) = Wc_(n,d) D_d(n),  D_d(n) = sum over the 2^dim elements f around n of
+//             (+1 if f is above n along d, else -1) z_f
+//   (A z)_e = sum over the corners b of e and the components d of (-1 if b is the upper corner
+//             along d, else +1) y_(n_b,d)
 // ------------------------------------------------------------------------------------------
 constexpr int kMfX = 32, kMfY = 8;
 
-template <int DIM, int TZ>
-__global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf_dir(EGrid g, int64_t nnx, int64_t nny, int64_t nn,
-                                                           const float* __restrict__ h, int off1, int off2,
-                                                           const float* __restrict__ W, const float* __restrict__ z,
-                                                           float* __restrict__ p, float* __restrict__ q,
-                                                           double* __restrict__ scal, int k, int first) {
-    constexpr int NT = kMfX * kMfY;                                            // threads
-    constexpr int HX = kMfX + 2, HY = kMfY + 2, HZ = DIM == 3 ? TZ + 2 : 1;   // element halo
-    constexpr int NX = kMfX + 1, NY = kMfY + 1, NZ = DIM == 3 ? TZ + 1 : 1;   // tile nodes
-    constexpr int NN = NX * NY * NZ;
-    constexpr int NPT = (NN + NT - 1) / NT;                                   // nodes per thread
-    constexpr int EZ = DIM == 3 ? TZ : 1;                                     // elements per thread
-    __shared__ float zs[HZ * HY * HX];
-    __shared__ float ys[DIM * NN];
-    __shared__ float hw[HX + HY + HZ];   // widths of the halo elements per axis (0 outside the mesh)
+// 2D: one kMfX x kMfY tile of elements per block; z with its one-element halo and the tile's
+// nodes staged in shared memory; fused with the direction update of k_cg_spmv_dir
+__global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf2_dir(int ex, int ey, int64_t nnx, int64_t nn,
+                                                            const float* __restrict__ Wc, const float* __restrict__ z,
+                                                            float* __restrict__ p, float* __restrict__ q,
+                                                            double* __restrict__ scal, int k, int first) {
+    constexpr int NT = kMfX * kMfY;
+    constexpr int HX = kMfX + 2, HY = kMfY + 2, NX = kMfX + 1, NY = kMfY + 1, NN = NX * NY;
+    __shared__ float zs[HY * HX];
+    __shared__ float ys[2 * NN];
     __shared__ double sw[32];
     __shared__ float s_beta;
-    const int ex = (int)g.ex, ey = (int)g.ey, ez = (int)g.ez;
-    const int ntx = (ex + kMfX - 1) / kMfX, nty = (ey + kMfY - 1) / kMfY;
-    int bi = blockIdx.x;
-    const int x0 = (bi % ntx) * kMfX;
-    bi /= ntx;
-    const int y0 = (bi % nty) * kMfY;
-    bi /= nty;
-    const int z0 = DIM == 3 ? bi * TZ : 0;
-    const int tid = threadIdx.x;
-    const int lx = tid % kMfX, ly = tid / kMfX;
-    // every global load of the block is issued before the first barrier: this thread's nodal
-    // weights and (after the first iteration) its elements' p and q, then the z halo
-    float wv[NPT][DIM];
-#pragma unroll
-    for (int j = 0; j < NPT; ++j) {
-        const int i = tid + j * NT;
-        const int nx = i % NX, ny = (i / NX) % NY, nz = DIM == 3 ? i / (NX * NY) : 0;
-        const int gx = x0 + nx, gy = y0 + ny, gz = z0 + nz;
-        const bool inside = i < NN && gx <= ex && gy <= ey && (DIM == 2 || gz <= ez);
-        const int64_t node = inside ? gx + nnx * (gy + nny * gz) : 0;
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) wv[j][d] = inside ? __ldg(W + (int64_t)d * nn + node) : 0.f;
-    }
-    float pv[EZ], qv[EZ];
-#pragma unroll
-    for (int lz = 0; lz < EZ; ++lz) {
-        const int gx = x0 + lx, gy = y0 + ly, gz = z0 + lz;
-        const bool valid = !first && gx < ex && gy < ey && gz < (DIM == 3 ? ez : 1);
-        const int e = valid ? gx + ex * (gy + ey * gz) : 0;
-        pv[lz] = valid ? p[e] : 0.f;
-        qv[lz] = valid ? q[e] : 0.f;
-    }
-    for (int i = tid; i < HX + HY + HZ; i += NT) {
-        int idx, n, o;
-        if (i < HX) {
-            idx = x0 - 1 + i, n = ex, o = 0;
-        } else if (i < HX + HY) {
-            idx = y0 - 1 + (i - HX), n = ey, o = off1;
-        } else {
-            idx = z0 - 1 + (i - HX - HY), n = DIM == 3 ? ez : 0, o = off2;
-        }
-        hw[i] = idx >= 0 && idx < n ? __ldg(h + o + idx) : 0.f;
-    }
-    for (int i = tid; i < HZ * HY * HX; i += NT) {
-        const int gx = x0 - 1 + i % HX, gy = y0 - 1 + (i / HX) % HY, gz = DIM == 3 ? z0 - 1 + i / (HX * HY) : 0;
-        zs[i] = (gx >= 0 && gx < ex && gy >= 0 && gy < ey && gz >= 0 && gz < ez) ? __ldg(z + gx + ex * (gy + ey * gz))
-                                                                                 : 0.f;
+    const int ntx = (ex + kMfX - 1) / kMfX;
+    const int x0 = (blockIdx.x % ntx) * kMfX, y0 = (blockIdx.x / ntx) * kMfY;
+    const int tid = threadIdx.x, lx = tid % kMfX, ly = tid / kMfX;
+    for (int i = tid; i < HY * HX; i += NT) {
+        const int gx = x0 - 1 + i % HX, gy = y0 - 1 + i / HX;
+        zs[i] = (gx >= 0 && gx < ex && gy >= 0 && gy < ey) ? __ldg(z + gx + ex * gy) : 0.f;
     }
     const float beta = first ? 0.f : block_ratio<float>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
     __syncthreads();
-    const float* hx = hw;
-    const float* hy = hw + HX;
-    const float* hz = hw + HX + HY;
-    const float sc = DIM == 3 ? 0.25f : 0.5f;
-    // y_(n,d) = W_(n,d) sum over the 2^dim elements f = n - 1 + a of G_(n,d),f z_f
-#pragma unroll
-    for (int j = 0; j < NPT; ++j) {
-        const int i = tid + j * NT;
-        if (i < NN) {
-            const int nx = i % NX, ny = (i / NX) % NY, nz = DIM == 3 ? i / (NX * NY) : 0;
-            float acc[3] = {0.f, 0.f, 0.f};
-            const float wx0 = hx[nx], wx1 = hx[nx + 1], wy0 = hy[ny], wy1 = hy[ny + 1];
-#pragma unroll
-            for (int a = 0; a < (1 << DIM); ++a) {
-                const int ax = a & 1, ay = (a >> 1) & 1, az = (a >> 2) & 1;
-                const float zv = zs[(DIM == 3 ? (nz + az) * HY * HX : 0) + (ny + ay) * HX + nx + ax];
-                const float wx = ax ? wx1 : wx0, wy = ay ? wy1 : wy0;
-                if (DIM == 3) {
-                    const float wz = hz[nz + az];
-                    acc[0] += (ax ? sc : -sc) * (wy * wz) * zv;
-                    acc[1] += (ay ? sc : -sc) * (wx * wz) * zv;
-                    acc[2] += (az ? sc : -sc) * (wx * wy) * zv;
-                } else {
-                    acc[0] += (ax ? sc : -sc) * wy * zv;
-                    acc[1] += (ay ? sc : -sc) * wx * zv;
-                }
-            }
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) ys[d * NN + i] = wv[j][d] * acc[d];
+    for (int i = tid; i < NN; i += NT) {
+        const int nx = i % NX, ny = i / NX, gx = x0 + nx, gy = y0 + ny;
+        float y0v = 0.f, y1v = 0.f;
+        if (gx <= ex && gy <= ey) {
+            const int b = ny * HX + nx;
+            const float z00 = zs[b], z10 = zs[b + 1], z01 = zs[b + HX], z11 = zs[b + HX + 1];
+            const int64_t node = gx + nnx * gy;
+            y0v = __ldg(Wc + node) * ((z10 - z00) + (z11 - z01));
+            y1v = __ldg(Wc + nn + node) * ((z01 - z00) + (z11 - z10));
         }
+        ys[i] = y0v;
+        ys[NN + i] = y1v;
     }
     __syncthreads();
-    // (G^T y)_e over the corners of e, marching up the thread's column of elements (the upper
-    // corner values of one element are the lower ones of the next), then p = z + beta p,
-    // q = A z + beta q and pq_{k+1}
-    const float wx = hx[lx + 1], wy = hy[ly + 1];
-    float lo[DIM][4];
-#pragma unroll
-    for (int c4 = 0; c4 < 4; ++c4) {
-        const int ni = (ly + (c4 >> 1)) * NX + lx + (c4 & 1);
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) lo[d][c4] = ys[d * NN + ni];
-    }
     float local = 0.f;
-#pragma unroll
-    for (int lz = 0; lz < EZ; ++lz) {
-        float out = 0.f;
-        if (DIM == 3) {
-            float hi[DIM][4];
-#pragma unroll
-            for (int c4 = 0; c4 < 4; ++c4) {
-                const int ni = ((lz + 1) * NY + ly + (c4 >> 1)) * NX + lx + (c4 & 1);
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) hi[d][c4] = ys[d * NN + ni];
-            }
-            const float wz = hz[lz + 1];
-            const float a0 = sc * wy * wz, a1 = sc * wx * wz, a2 = sc * wx * wy;
-#pragma unroll
-            for (int c4 = 0; c4 < 4; ++c4) {
-                out = fmaf((c4 & 1) ? -a0 : a0, lo[0][c4] + hi[0][c4], out);
-                out = fmaf((c4 >> 1) ? -a1 : a1, lo[1][c4] + hi[1][c4], out);
-                out = fmaf(a2, lo[DIM - 1][c4] - hi[DIM - 1][c4], out);
-            }
-#pragma unroll
-            for (int c4 = 0; c4 < 4; ++c4)
-#pragma unroll
-                for (int d = 0; d < DIM; ++d) lo[d][c4] = hi[d][c4];
-        } else {
-            const float a0 = sc * wy, a1 = sc * wx;
-#pragma unroll
-            for (int c4 = 0; c4 < 4; ++c4) {
-                out = fmaf((c4 & 1) ? -a0 : a0, lo[0][c4], out);
-                out = fmaf((c4 >> 1) ? -a1 : a1, lo[1][c4], out);
-            }
-        }
-        const int gx = x0 + lx, gy = y0 + ly, gz = z0 + lz;
-        if (gx < ex && gy < ey && gz < (DIM == 3 ? ez : 1)) {
-            const int e = gx + ex * (gy + ey * gz);
-            const float ze = zs[((DIM == 3 ? lz + 1 : 0) * HY + ly + 1) * HX + lx + 1];
-            const float pe = first ? ze : fmaf(beta, pv[lz], ze);
-            const float qe = first ? out : fmaf(beta, qv[lz], out);
-            p[e] = pe;
-            q[e] = qe;
-            local = fmaf(pe, qe, local);
-        }
+    const int gx = x0 + lx, gy = y0 + ly;
+    if (gx < ex && gy < ey) {
+        const int b = ly * NX + lx;
+        const float out = (ys[b] - ys[b + 1] + ys[b + NX] - ys[b + NX + 1]) +
+                          (ys[NN + b] + ys[NN + b + 1] - ys[NN + b + NX] - ys[NN + b + NX + 1]);
+        const int e = gx + ex * gy;
+        const float ze = zs[(ly + 1) * HX + lx + 1];
+        const float pe = first ? ze : fmaf(beta, p[e], ze);
+        const float qe = first ? out : fmaf(beta, q[e], out);
+        p[e] = pe;
+        q[e] = qe;
+        local = pe * qe;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) *rr_slot(scal, k + 1) = 0.0;
     double t = block_sum<float>(local, sw);
     if (threadIdx.x == 0) atomicAdd(pq_slot(scal, k + 1), t);
 }
 
-// the launch of the matrix-free direction kernel: tile depth 4 when that still gives four tiles
-// per SM, else 2 (3D)
-struct MfLaunch {
-    EGrid g;
+// 3D: a block owns a column of kMfX x kMfY elements over zc element planes and marches up z.  Step
+// t stages element plane kk = zlo - 1 + t (with its one-element xy halo), forms node plane kk
+// from element planes kk - 1 and kk, then element plane kk - 1 from node planes kk - 1 and kk.
+// The next plane's z, W, p and q are loaded into registers while the current one is computed.
+// Element planes rotate through three buffers and node planes through two, so that no thread
+// overwrites a plane another thread may still read (two barriers per step).
+struct Mf3 {
+    int ex, ey, ez, zc;
     int64_t nnx, nny, nn;
-    const float* h;
-    int off1, off2;
-    const float* W;
-    int dim, tz;
+};
+
+__global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* __restrict__ Wc,
+                                                            const float* __restrict__ z, float* __restrict__ p,
+                                                            float* __restrict__ q, double* __restrict__ scal, int k,
+                                                            int first) {
+    constexpr int NT = kMfX * kMfY;
+    constexpr int HX = kMfX + 2, HY = kMfY + 2, HP = HX * HY;   // element plane with halo
+    constexpr int NX = kMfX + 1, NY = kMfY + 1, NP = NX * NY;   // node plane
+    static_assert(HP <= 2 * NT && NP <= 2 * NT, "two slots per thread cover a plane");
+    __shared__ float zb[3][HP];
+    __shared__ float yb[2][3][NP];
+    __shared__ double sw[32];
+    __shared__ float s_beta;
+    const int ex = a.ex, ey = a.ey, ez = a.ez;
+    const int ntx = (ex + kMfX - 1) / kMfX, nty = (ey + kMfY - 1) / kMfY;
+    int bi = blockIdx.x;
+    const int x0 = (bi % ntx) * kMfX;
+    bi /= ntx;
+    const int y0 = (bi % nty) * kMfY;
+    bi /= nty;
+    const int zlo = bi * a.zc, zhi = min(zlo + a.zc, ez);
+    const int tid = threadIdx.x, tx = tid % kMfX, ty = tid / kMfX;
+    const int64_t exy = (int64_t)ex * ey, nxy = a.nnx * a.nny;
+    // this thread's two element-halo slots and two node slots of a plane (offsets within a plane)
+    int zo[2], nbase[2];
+    bool zok[2], nok[2];
+    int64_t no[2];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const int i = tid + s * NT;
+        const int hx = i % HX, hy = i / HX, gx = x0 - 1 + hx, gy = y0 - 1 + hy;
+        zok[s] = i < HP && gx >= 0 && gx < ex && gy >= 0 && gy < ey;
+        zo[s] = zok[s] ? gx + ex * gy : 0;
+        const int nx = i % NX, ny = i / NX;
+        nok[s] = i < NP && x0 + nx <= ex && y0 + ny <= ey;
+        no[s] = nok[s] ? (x0 + nx) + a.nnx * (y0 + ny) : 0;
+        nbase[s] = ny * HX + nx;   // the node's lower-left element in the halo plane
+    }
+    const bool eok = x0 + tx < ex && y0 + ty < ey;
+    const int eo = eok ? (x0 + tx) + ex * (y0 + ty) : 0;
+    float zr[2], wr[2][3], pn = 0.f, qn = 0.f;
+    auto load_z = [&](int plane) {
+#pragma unroll
+        for (int s = 0; s < 2; ++s)
+            zr[s] = zok[s] && plane >= 0 && plane < ez ? __ldg(z + plane * exy + zo[s]) : 0.f;
+    };
+    auto load_w = [&](int plane) {
+#pragma unroll
+        for (int s = 0; s < 2; ++s)
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                wr[s][d] = nok[s] && plane <= ez ? __ldg(Wc + d * a.nn + plane * nxy + no[s]) : 0.f;
+    };
+    auto load_pq = [&](int plane) {
+        const bool ok = !first && eok && plane < zhi;
+        pn = ok ? p[plane * exy + eo] : 0.f;
+        qn = ok ? q[plane * exy + eo] : 0.f;
+    };
+    const float beta = first ? 0.f : block_ratio<float>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
+    // prologue: element plane zlo - 1 into buffer 0; registers for plane zlo
+    load_z(zlo - 1);
+#pragma unroll
+    for (int s = 0; s < 2; ++s)
+        if (tid + s * NT < HP) zb[0][tid + s * NT] = zr[s];
+    load_z(zlo);
+    load_w(zlo);
+    float lo[3][4], hi[3][4];
+    float local = 0.f;
+    const int ybase = ty * NX + tx;
+    for (int t = 1; t <= zhi - zlo + 1; ++t) {
+        const int kk = zlo - 1 + t;
+        float* zc = zb[t % 3];
+        const float* zp = zb[(t + 2) % 3];   // element plane kk - 1
+#pragma unroll
+        for (int s = 0; s < 2; ++s)
+            if (tid + s * NT < HP) zc[tid + s * NT] = zr[s];
+        float wc[2][3];
+#pragma unroll
+        for (int s = 0; s < 2; ++s)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) wc[s][d] = wr[s][d];
+        const float pc = pn, qc = qn;
+        load_z(kk + 1);
+        load_w(kk + 1);
+        load_pq(kk);   // element plane kk, computed in the next step
+        __syncthreads();
+        float* yc = yb[t & 1][0];
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const int i = tid + s * NT;
+            if (i < NP) {
+                const int b = nbase[s];
+                const float z000 = zp[b], z100 = zp[b + 1], z010 = zp[b + HX], z110 = zp[b + HX + 1];
+                const float z001 = zc[b], z101 = zc[b + 1], z011 = zc[b + HX], z111 = zc[b + HX + 1];
+                const float dx = (z100 - z000) + (z110 - z010) + (z101 - z001) + (z111 - z011);
+                const float dy = (z010 - z000) + (z110 - z100) + (z011 - z001) + (z111 - z101);
+                const float dz = (z001 - z000) + (z101 - z100) + (z011 - z010) + (z111 - z110);
+                yc[i] = wc[s][0] * dx;
+                yc[NP + i] = wc[s][1] * dy;
+                yc[2 * NP + i] = wc[s][2] * dz;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c4 = 0; c4 < 4; ++c4) {
+            const int ni = ybase + (c4 >> 1) * NX + (c4 & 1);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) hi[d][c4] = yc[d * NP + ni];
+        }
+        if (t >= 2 && eok) {
+            // element plane kk - 1: corners (bx, by) on node planes kk - 1 (lo) and kk (hi)
+            float out = 0.f;
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4) {
+                out += (c4 & 1) ? -(lo[0][c4] + hi[0][c4]) : (lo[0][c4] + hi[0][c4]);
+                out += (c4 >> 1) ? -(lo[1][c4] + hi[1][c4]) : (lo[1][c4] + hi[1][c4]);
+                out += lo[2][c4] - hi[2][c4];
+            }
+            const int64_t e = (int64_t)(kk - 1) * exy + eo;
+            const float ze = zp[(ty + 1) * HX + tx + 1];
+            const float pe = first ? ze : fmaf(beta, pc, ze);
+            const float qe = first ? out : fmaf(beta, qc, out);
+            p[e] = pe;
+            q[e] = qe;
+            local = fmaf(pe, qe, local);
+        }
+#pragma unroll
+        for (int c4 = 0; c4 < 4; ++c4)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) lo[d][c4] = hi[d][c4];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *rr_slot(scal, k + 1) = 0.0;
+    double t = block_sum<float>(local, sw);
+    if (threadIdx.x == 0) atomicAdd(pq_slot(scal, k + 1), t);
+}
+
+// Wc_(n,d) = a_d^2 W_(n,d) in FP32 (the weights of the matrix-free apply)
+__global__ void k_mf_weights(int64_t nn, int dim, double a0, double a1, double a2, const double* __restrict__ W,
+                             float* __restrict__ Wc) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    Wc[n] = (float)(a0 * a0 * W[n]);
+    Wc[nn + n] = (float)(a1 * a1 * W[nn + n]);
+    if (dim == 3) Wc[2 * nn + n] = (float)(a2 * a2 * W[2 * nn + n]);
+}
+
+// the launch of the matrix-free direction kernel: in 3D the deepest column chunk (up to 16
+// element planes) that still gives four blocks per SM, at least 2 planes
+struct MfLaunch {
+    int dim;
+    int ex, ey;
+    int64_t nnx, nn;
+    Mf3 a3;
+    const float* Wc;
     unsigned blocks;
 };
 
-static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* h, const int off[3], const float* W, int sms) {
-    MfLaunch L;
-    L.g = g;
-    L.nnx = m.nnx;
-    L.nny = m.nny;
-    L.nn = m.nn;
-    L.h = h;
-    L.off1 = off[1];
-    L.off2 = off[2];
-    L.W = W;
+static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* Wc, int sms) {
+    MfLaunch L{};
     L.dim = m.dim;
+    L.ex = (int)g.ex;
+    L.ey = (int)g.ey;
+    L.nnx = m.nnx;
+    L.nn = m.nn;
+    L.Wc = Wc;
     const int64_t txy = ((g.ex + kMfX - 1) / kMfX) * ((g.ey + kMfY - 1) / kMfY);
-    L.tz = m.dim == 3 && txy * ((g.ez + 3) / 4) >= 4 * (int64_t)sms ? 4 : 2;
-    L.blocks = (unsigned)(m.dim == 3 ? txy * ((g.ez + L.tz - 1) / L.tz) : txy);
+    if (m.dim == 2) {
+        L.blocks = (unsigned)txy;
+        return L;
+    }
+    int zc = 16;
+    while (zc > 2 && txy * ((g.ez + zc - 1) / zc) < 4 * (int64_t)sms) zc /= 2;
+    L.a3 = Mf3{(int)g.ex, (int)g.ey, (int)g.ez, zc, m.nnx, m.nny, m.nn};
+    L.blocks = (unsigned)(txy * ((g.ez + zc - 1) / zc));
     return L;
 }
 
 static void mf_dir(const MfLaunch& L, cudaStream_t st, const float* z, float* p, float* q, double* scal, int k,
                    int first) {
     const unsigned nt = kMfX * kMfY;
-    if (L.dim == 2)
-        k_cg_mf_dir<2, 1><<<L.blocks, nt, 0, st>>>(L.g, L.nnx, L.nny, L.nn, L.h, L.off1, L.off2, L.W, z, p, q, scal, k,
-                                                   first);
-    else if (L.tz == 4)
-        k_cg_mf_dir<3, 4><<<L.blocks, nt, 0, st>>>(L.g, L.nnx, L.nny, L.nn, L.h, L.off1, L.off2, L.W, z, p, q, scal, k,
-                                                   first);
-    else
-        k_cg_mf_dir<3, 2><<<L.blocks, nt, 0, st>>>(L.g, L.nnx, L.nny, L.nn, L.h, L.off1, L.off2, L.W, z, p, q, scal, k,
-                                                   first);
+    if (L.dim == 2) k_cg_mf2_dir<<<L.blocks, nt, 0, st>>>(L.ex, L.ey, L.nnx, L.nn, L.Wc, z, p, q, scal, k, first);
+    else k_cg_mf3_dir<<<L.blocks, nt, 0, st>>>(L.a3, L.Wc, z, p, q, scal, k, first);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -776,10 +824,9 @@ static int gwg_cg_T(Context& c, const T* A, const float* Wmf, const T* dinv, con
     const int nb = m.dim == 3 ? 27 : 9;
     MfLaunch mf{};
     if (Wmf) {
-        int off[3], sms = 0;
-        const float* h = fine_widths32(c, off);
+        int sms = 0;
         UWG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
-        mf = mf_launch(m, g, h, off, Wmf, sms);
+        mf = mf_launch(m, g, Wmf, sms);
     }
     T* r = work;
     T* z = work + ne;
@@ -868,11 +915,29 @@ int gwg_cg32(Context& c, const float* A, const float* dinv, const double* b, flo
     return gwg_cg_T<float>(c, A, nullptr, dinv, b, x, rtol, maxit, work, scal);
 }
 
-// the mixed form's inner solve: G^T W G applied matrix-free from W32 (FP32 nodal weights, zero on
-// fixed components)
-int gwg_cg32_mf(Context& c, const float* W32, const float* dinv, const double* b, float* x, double rtol, int maxit,
+// the mixed form's inner solve: G^T W G applied matrix-free from the folded weights Wc
+// (gwg_mf_weights)
+int gwg_cg32_mf(Context& c, const float* Wc, const float* dinv, const double* b, float* x, double rtol, int maxit,
                 float* work, double* scal) {
-    return gwg_cg_T<float>(c, nullptr, W32, dinv, b, x, rtol, maxit, work, scal);
+    return gwg_cg_T<float>(c, nullptr, Wc, dinv, b, x, rtol, maxit, work, scal);
+}
+
+// the folded weights of the matrix-free apply, Wc_(n,d) = a_d^2 W_(n,d) (FP32), for the uniform
+// mesh's a_d = prod_{k != d} h_k / 2^(dim-1)
+void gwg_mf_weights(Context& c, const double* W, float* Wc) {
+    const MeshDesc& m = c.levels[0].mesh;
+    double h[3] = {1.0, 1.0, 1.0};
+    for (int d = 0; d < m.dim; ++d) h[d] = (m.max[d] - m.min[d]) / m.nel[d];
+    const double sc = m.dim == 3 ? 0.25 : 0.5;
+    double a[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < m.dim; ++d) {
+        a[d] = sc;
+        for (int k = 0; k < m.dim; ++k)
+            if (k != d) a[d] *= h[k];
+    }
+    LaunchScope ls(c, -1);
+    k_mf_weights<<<blocks_for(m.nn, 256), 256, 0, c.stream>>>(m.nn, m.dim, a[0], a[1], a[2], W, Wc);
+    check_launch("k_mf_weights");
 }
 
 // Test and timing hook on the inner operator of the current fine velocity operator: W, the FP64
@@ -907,11 +972,10 @@ void bfbt_operator_hook(Context& c, int form, const double* xh, double* yh, int 
         to_float(c, x.p, x32.p, ne);
         if (form == 1) {
             W32.ensure((size_t)nv);
-            to_float(c, W.p, W32.p, nv);
-            int off[3], sms = 0;
-            const float* h = fine_widths32(c, off);
+            gwg_mf_weights(c, W.p, W32.p);
+            int sms = 0;
             UWG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
-            mf = mf_launch(m, g, h, off, W32.p, sms);
+            mf = mf_launch(m, g, W32.p, sms);
         } else {
             A32.ensure((size_t)nb * ne);
             to_float(c, A.p, A32.p, (int64_t)nb * ne);

@@ -1293,12 +1293,6 @@ static GeoT<float> geo_f32(Context& c, const MeshDesc& m) {
     return g;
 }
 
-const float* fine_widths32(Context& c, int off[3]) {
-    GeoT<float> g = geo_f32(c, c.levels[0].mesh);
-    for (int d = 0; d < 3; ++d) off[d] = g.off[d];
-    return g.h;
-}
-
 // FP32 pieces of the scaled BFBt apply: s = W (G p) and q = G^T s
 void op_wg32(Context& c, const float* p, const float* W, float* s) {
     const Level& L = c.levels[0];

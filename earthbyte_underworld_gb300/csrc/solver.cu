@@ -47,8 +47,9 @@ int gwg_cg_mg(Context& c, const double* A, const double* dinv, const double* b, 
               double* work, double* scal);
 int gwg_cg_mg32(Context& c, const float* A, const float* dinv, const double* b, float* x, double rtol, int maxit,
                 float* work, double* scal);
-int gwg_cg32_mf(Context& c, const float* W32, const float* dinv, const double* b, float* x, double rtol, int maxit,
+int gwg_cg32_mf(Context& c, const float* Wc, const float* dinv, const double* b, float* x, double rtol, int maxit,
                 float* work, double* scal);
+void gwg_mf_weights(Context& c, const double* W, float* Wc);
 void op_wg32(Context& c, const float* p, const float* W, float* s);
 void op_gt32(Context& c, const float* s, float* q);
 void to_float(Context& c, const double* a, float* b, int64_t n);
@@ -453,7 +454,7 @@ struct Bsscr {
     // scaled BFBt state: weights, G^T W G stencil and inverse diagonal, work vectors
     DArray<double> bw, bA, bd, bt, bt2, bs, bX, pr, pz, pp, pq, ptmp;
     // FP32 copies for the mixed form (the preconditioner runs in FP32 inside the FP64 Schur FGMRES)
-    DArray<float> bw32, bA32, bd32, bt32, bt2_32, bs32, bX32, pz32;
+    DArray<float> bw32, bA32, bd32, bt32, bt2_32, bs32, bX32, pz32, bwc32;
     DArray<double> scal32;
     int64_t bfbt_its = 0;
     // pressure null-space vectors (constant, or the two element-parity indicators), each used
@@ -670,7 +671,7 @@ struct Bsscr {
         double rtol = o.bfbt_rtol > 0 ? o.bfbt_rtol : 1e-4;
         if (bfbt_mg) return gwg_cg_mg32(c, bA32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
         if (o.bfbt_inner_pc == 2) return gwg_cg32(c, bA32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
-        return gwg_cg32_mf(c, bw32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
+        return gwg_cg32_mf(c, bwc32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
     }
 
     // the same preconditioner with FP32 operators, inner solves and vectors (mixed form)
@@ -990,7 +991,9 @@ void Bsscr::run() {
             for (auto* v : {&bd32, &bt32, &bt2_32}) v->ensure(npres);
             pz32.ensure(4 * npres);
             scal32.ensure(8);
-            to_float(c, bw.p, bw32.p, nv);   // zero on fixed components: the matrix-free inner operator's W
+            to_float(c, bw.p, bw32.p, nv);
+            bwc32.ensure(nv);
+            gwg_mf_weights(c, bw.p, bwc32.p);   // the matrix-free inner operator's folded weights
             // the explicit FP32 stencil only where the inner solve reads it (multigrid levels, or
             // the stencil form asked for); the default mixed inner solve is matrix-free
             const bool want_stencil32 = o.bfbt_inner_pc != 0;
