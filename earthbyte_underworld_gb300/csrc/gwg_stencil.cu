@@ -360,129 +360,105 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf2_dir(int ex, int ey, int6
     if (threadIdx.x == 0) atomicAdd(pq_slot(scal, k + 1), t);
 }
 
-// 3D: a block owns a column of kMfX x (kMfY ROWS) elements over zc element planes and marches up z;
-// a thread owns ROWS adjacent elements along y in every plane (they share a row of corner nodes).
-// Step t stages element plane kk = zlo - 1 + t (with its one-element xy halo), forms node plane kk
+// 3D: a block owns a column of kMfX x kMfY elements over zc element planes and marches up z.  Step
+// t stages element plane kk = zlo - 1 + t (with its one-element xy halo), forms node plane kk
 // from element planes kk - 1 and kk, then element plane kk - 1 from node planes kk - 1 and kk.
 // The next plane's z, W, p and q are loaded into registers while the current one is computed.
 // Element planes rotate through three buffers and node planes through two, so that no thread
-// overwrites a plane another thread may still read (two barriers per step).  Offsets within a
-// plane are 32-bit (the host checks 3 nn < 2^31).
+// overwrites a plane another thread may still read (two barriers per step).
 struct Mf3 {
     int ex, ey, ez, zc;
-    int nnx, nny, nn;
+    int64_t nnx, nny, nn;
 };
 
-template <int ROWS>
-__global__ void __launch_bounds__(kMfX * kMfY, 3) k_cg_mf3_dir(Mf3 a, const float* __restrict__ Wc,
+__global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* __restrict__ Wc,
                                                             const float* __restrict__ z, float* __restrict__ p,
                                                             float* __restrict__ q, double* __restrict__ scal, int k,
                                                             int first) {
-    constexpr int NT = kMfX * kMfY, TY = kMfY * ROWS;
-    constexpr int HX = kMfX + 2, HY = TY + 2, HP = HX * HY;   // element plane with halo
-    constexpr int NX = kMfX + 1, NY = TY + 1, NP = NX * NY;   // node plane
-    constexpr int SZ = (HP + NT - 1) / NT, SN = (NP + NT - 1) / NT;   // slots per thread
+    constexpr int NT = kMfX * kMfY;
+    constexpr int HX = kMfX + 2, HY = kMfY + 2, HP = HX * HY;   // element plane with halo
+    constexpr int NX = kMfX + 1, NY = kMfY + 1, NP = NX * NY;   // node plane
+    static_assert(HP <= 2 * NT && NP <= 2 * NT, "two slots per thread cover a plane");
     __shared__ float zb[3][HP];
     __shared__ float yb[2][3][NP];
     __shared__ double sw[32];
     __shared__ float s_beta;
     const int ex = a.ex, ey = a.ey, ez = a.ez;
-    const int ntx = (ex + kMfX - 1) / kMfX, nty = (ey + TY - 1) / TY;
+    const int ntx = (ex + kMfX - 1) / kMfX, nty = (ey + kMfY - 1) / kMfY;
     int bi = blockIdx.x;
     const int x0 = (bi % ntx) * kMfX;
     bi /= ntx;
-    const int y0 = (bi % nty) * TY;
+    const int y0 = (bi % nty) * kMfY;
     bi /= nty;
     const int zlo = bi * a.zc, zhi = min(zlo + a.zc, ez);
     const int tid = threadIdx.x, tx = tid % kMfX, ty = tid / kMfX;
-    const int exy = ex * ey, nxy = a.nnx * a.nny;
-    // this thread's element-halo slots and node slots of a plane (offsets within a plane)
-    int zo[SZ], nbase[SN], no[SN];
-    bool zok[SZ], nok[SN];
+    const int64_t exy = (int64_t)ex * ey, nxy = a.nnx * a.nny;
+    // this thread's two element-halo slots and two node slots of a plane (offsets within a plane)
+    int zo[2], nbase[2];
+    bool zok[2], nok[2];
+    int64_t no[2];
 #pragma unroll
-    for (int s = 0; s < SZ; ++s) {
+    for (int s = 0; s < 2; ++s) {
         const int i = tid + s * NT;
-        const int gx = x0 - 1 + i % HX, gy = y0 - 1 + i / HX;
+        const int hx = i % HX, hy = i / HX, gx = x0 - 1 + hx, gy = y0 - 1 + hy;
         zok[s] = i < HP && gx >= 0 && gx < ex && gy >= 0 && gy < ey;
         zo[s] = zok[s] ? gx + ex * gy : 0;
-    }
-#pragma unroll
-    for (int s = 0; s < SN; ++s) {
-        const int i = tid + s * NT;
         const int nx = i % NX, ny = i / NX;
         nok[s] = i < NP && x0 + nx <= ex && y0 + ny <= ey;
         no[s] = nok[s] ? (x0 + nx) + a.nnx * (y0 + ny) : 0;
         nbase[s] = ny * HX + nx;   // the node's lower-left element in the halo plane
     }
-    bool eok[ROWS];
-    int eo[ROWS];
-#pragma unroll
-    for (int r = 0; r < ROWS; ++r) {
-        const int gx = x0 + tx, gy = y0 + ty * ROWS + r;
-        eok[r] = gx < ex && gy < ey;
-        eo[r] = eok[r] ? gx + ex * gy : 0;
-    }
-    float zr[SZ], wr[SN][3], pn[ROWS], qn[ROWS];
+    const bool eok = x0 + tx < ex && y0 + ty < ey;
+    const int eo = eok ? (x0 + tx) + ex * (y0 + ty) : 0;
+    float zr[2], wr[2][3], pn = 0.f, qn = 0.f;
     auto load_z = [&](int plane) {
-        const bool pok = plane >= 0 && plane < ez;
-        const float* zp = z + (int64_t)(pok ? plane : 0) * exy;
 #pragma unroll
-        for (int s = 0; s < SZ; ++s) zr[s] = zok[s] && pok ? __ldg(zp + zo[s]) : 0.f;
+        for (int s = 0; s < 2; ++s)
+            zr[s] = zok[s] && plane >= 0 && plane < ez ? __ldg(z + plane * exy + zo[s]) : 0.f;
     };
     auto load_w = [&](int plane) {
-        const bool pok = plane <= ez;
-        const float* wp = Wc + (int64_t)(pok ? plane : 0) * nxy;
 #pragma unroll
-        for (int s = 0; s < SN; ++s)
+        for (int s = 0; s < 2; ++s)
 #pragma unroll
-            for (int d = 0; d < 3; ++d) wr[s][d] = nok[s] && pok ? __ldg(wp + d * a.nn + no[s]) : 0.f;
+            for (int d = 0; d < 3; ++d)
+                wr[s][d] = nok[s] && plane <= ez ? __ldg(Wc + d * a.nn + plane * nxy + no[s]) : 0.f;
     };
     auto load_pq = [&](int plane) {
-        const bool pok = !first && plane < zhi;
-        const int64_t off = (int64_t)(pok ? plane : 0) * exy;
-#pragma unroll
-        for (int r = 0; r < ROWS; ++r) {
-            pn[r] = pok && eok[r] ? p[off + eo[r]] : 0.f;
-            qn[r] = pok && eok[r] ? q[off + eo[r]] : 0.f;
-        }
+        const bool ok = !first && eok && plane < zhi;
+        pn = ok ? p[plane * exy + eo] : 0.f;
+        qn = ok ? q[plane * exy + eo] : 0.f;
     };
     const float beta = first ? 0.f : block_ratio<float>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
     // prologue: element plane zlo - 1 into buffer 0; registers for plane zlo
     load_z(zlo - 1);
 #pragma unroll
-    for (int s = 0; s < SZ; ++s)
+    for (int s = 0; s < 2; ++s)
         if (tid + s * NT < HP) zb[0][tid + s * NT] = zr[s];
     load_z(zlo);
     load_w(zlo);
-    // corner values of the thread's elements: node rows ty ROWS + j (j = 0..ROWS), columns tx, tx + 1
-    float lo[3][ROWS + 1][2], hi[3][ROWS + 1][2];
+    float lo[3][4], hi[3][4];
     float local = 0.f;
-    const int ybase = ty * ROWS * NX + tx;
-#pragma unroll(ROWS == 1 ? 2 : 1)
+    const int ybase = ty * NX + tx;
     for (int t = 1; t <= zhi - zlo + 1; ++t) {
         const int kk = zlo - 1 + t;
         float* zc = zb[t % 3];
         const float* zp = zb[(t + 2) % 3];   // element plane kk - 1
 #pragma unroll
-        for (int s = 0; s < SZ; ++s)
+        for (int s = 0; s < 2; ++s)
             if (tid + s * NT < HP) zc[tid + s * NT] = zr[s];
-        float wc[SN][3], pc[ROWS], qc[ROWS];
+        float wc[2][3];
 #pragma unroll
-        for (int s = 0; s < SN; ++s)
+        for (int s = 0; s < 2; ++s)
 #pragma unroll
             for (int d = 0; d < 3; ++d) wc[s][d] = wr[s][d];
-#pragma unroll
-        for (int r = 0; r < ROWS; ++r) {
-            pc[r] = pn[r];
-            qc[r] = qn[r];
-        }
+        const float pc = pn, qc = qn;
         load_z(kk + 1);
         load_w(kk + 1);
         load_pq(kk);   // element plane kk, computed in the next step
         __syncthreads();
         float* yc = yb[t & 1][0];
 #pragma unroll
-        for (int s = 0; s < SN; ++s) {
+        for (int s = 0; s < 2; ++s) {
             const int i = tid + s * NT;
             if (i < NP) {
                 const int b = nbase[s];
@@ -498,42 +474,32 @@ __global__ void __launch_bounds__(kMfX * kMfY, 3) k_cg_mf3_dir(Mf3 a, const floa
         }
         __syncthreads();
 #pragma unroll
-        for (int j = 0; j <= ROWS; ++j)
+        for (int c4 = 0; c4 < 4; ++c4) {
+            const int ni = ybase + (c4 >> 1) * NX + (c4 & 1);
 #pragma unroll
-            for (int c = 0; c < 2; ++c)
+            for (int d = 0; d < 3; ++d) hi[d][c4] = yc[d * NP + ni];
+        }
+        if (t >= 2 && eok) {
+            // element plane kk - 1: corners (bx, by) on node planes kk - 1 (lo) and kk (hi)
+            float out = 0.f;
 #pragma unroll
-                for (int d = 0; d < 3; ++d) hi[d][j][c] = yc[d * NP + ybase + j * NX + c];
-        if (t >= 2) {
-            // element plane kk - 1: corners (c, row j) on node planes kk - 1 (lo) and kk (hi)
-            const int64_t off = (int64_t)(kk - 1) * exy;
-#pragma unroll
-            for (int r = 0; r < ROWS; ++r) {
-                if (!eok[r]) continue;
-                float out = 0.f;
-#pragma unroll
-                for (int jj = 0; jj < 2; ++jj)
-#pragma unroll
-                    for (int c = 0; c < 2; ++c) {
-                        const int j = r + jj;
-                        const float sx = lo[0][j][c] + hi[0][j][c], sy = lo[1][j][c] + hi[1][j][c];
-                        out += c ? -sx : sx;
-                        out += jj ? -sy : sy;
-                        out += lo[2][j][c] - hi[2][j][c];
-                    }
-                const float ze = zp[(ty * ROWS + r + 1) * HX + tx + 1];
-                const float pe = first ? ze : fmaf(beta, pc[r], ze);
-                const float qe = first ? out : fmaf(beta, qc[r], out);
-                p[off + eo[r]] = pe;
-                q[off + eo[r]] = qe;
-                local = fmaf(pe, qe, local);
+            for (int c4 = 0; c4 < 4; ++c4) {
+                out += (c4 & 1) ? -(lo[0][c4] + hi[0][c4]) : (lo[0][c4] + hi[0][c4]);
+                out += (c4 >> 1) ? -(lo[1][c4] + hi[1][c4]) : (lo[1][c4] + hi[1][c4]);
+                out += lo[2][c4] - hi[2][c4];
             }
+            const int64_t e = (int64_t)(kk - 1) * exy + eo;
+            const float ze = zp[(ty + 1) * HX + tx + 1];
+            const float pe = first ? ze : fmaf(beta, pc, ze);
+            const float qe = first ? out : fmaf(beta, qc, out);
+            p[e] = pe;
+            q[e] = qe;
+            local = fmaf(pe, qe, local);
         }
 #pragma unroll
-        for (int j = 0; j <= ROWS; ++j)
+        for (int c4 = 0; c4 < 4; ++c4)
 #pragma unroll
-            for (int c = 0; c < 2; ++c)
-#pragma unroll
-                for (int d = 0; d < 3; ++d) lo[d][j][c] = hi[d][j][c];
+            for (int d = 0; d < 3; ++d) lo[d][c4] = hi[d][c4];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) *rr_slot(scal, k + 1) = 0.0;
     double t = block_sum<float>(local, sw);
@@ -550,11 +516,10 @@ __global__ void k_mf_weights(int64_t nn, int dim, double a0, double a1, double a
     if (dim == 3) Wc[2 * nn + n] = (float)(a2 * a2 * W[2 * nn + n]);
 }
 
-// the launch of the matrix-free direction kernel.  3D: two element rows per thread and the
-// deepest column chunk (up to 16 element planes, at least 2) that keeps three blocks per SM;
-// where even 2-plane chunks of two-row columns leave fewer, one row per thread.
+// the launch of the matrix-free direction kernel: in 3D the deepest column chunk (up to 16
+// element planes) that still gives four blocks per SM, at least 2 planes
 struct MfLaunch {
-    int dim, rows;
+    int dim;
     int ex, ey;
     int64_t nnx, nn;
     Mf3 a3;
@@ -570,21 +535,15 @@ static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* Wc, int sms) 
     L.nnx = m.nnx;
     L.nn = m.nn;
     L.Wc = Wc;
+    const int64_t txy = ((g.ex + kMfX - 1) / kMfX) * ((g.ey + kMfY - 1) / kMfY);
     if (m.dim == 2) {
-        L.blocks = (unsigned)(((g.ex + kMfX - 1) / kMfX) * ((g.ey + kMfY - 1) / kMfY));
+        L.blocks = (unsigned)txy;
         return L;
     }
-    UWG_REQUIRE(3 * m.nn < ((int64_t)1 << 31), UWGPU_ERR_TOO_LARGE, "matrix-free BFBt apply: mesh too large");
-    const int64_t want = 3 * (int64_t)sms;
-    for (int rows = 2; rows >= 1; --rows) {
-        const int64_t txy = ((g.ex + kMfX - 1) / kMfX) * ((g.ey + kMfY * rows - 1) / (kMfY * rows));
-        int zc = 16;
-        while (zc > 2 && txy * ((g.ez + zc - 1) / zc) < want) zc /= 2;
-        L.rows = rows;
-        L.a3 = Mf3{(int)g.ex, (int)g.ey, (int)g.ez, zc, (int)m.nnx, (int)m.nny, (int)m.nn};
-        L.blocks = (unsigned)(txy * ((g.ez + zc - 1) / zc));
-        if ((int64_t)L.blocks >= want) break;
-    }
+    int zc = 16;
+    while (zc > 2 && txy * ((g.ez + zc - 1) / zc) < 4 * (int64_t)sms) zc /= 2;
+    L.a3 = Mf3{(int)g.ex, (int)g.ey, (int)g.ez, zc, m.nnx, m.nny, m.nn};
+    L.blocks = (unsigned)(txy * ((g.ez + zc - 1) / zc));
     return L;
 }
 
@@ -592,8 +551,7 @@ static void mf_dir(const MfLaunch& L, cudaStream_t st, const float* z, float* p,
                    int first) {
     const unsigned nt = kMfX * kMfY;
     if (L.dim == 2) k_cg_mf2_dir<<<L.blocks, nt, 0, st>>>(L.ex, L.ey, L.nnx, L.nn, L.Wc, z, p, q, scal, k, first);
-    else if (L.rows == 2) k_cg_mf3_dir<2><<<L.blocks, nt, 0, st>>>(L.a3, L.Wc, z, p, q, scal, k, first);
-    else k_cg_mf3_dir<1><<<L.blocks, nt, 0, st>>>(L.a3, L.Wc, z, p, q, scal, k, first);
+    else k_cg_mf3_dir<<<L.blocks, nt, 0, st>>>(L.a3, L.Wc, z, p, q, scal, k, first);
 }
 
 // ------------------------------------------------------------------------------------------
