@@ -463,6 +463,7 @@ struct Bsscr {
     bool ns_use_t = false, ns_use_v = false;
     bool bbt_const = false;
     bool bfbt_mg = false;      // the inner solves use the multigrid preconditioner
+    bool stencil32 = false;    // the mixed form's Jacobi inner solves read the FP32 stencil
     DArray<float> r32, d32;
     bool nan = false;
     bool inner_fail = false;
@@ -664,13 +665,13 @@ struct Bsscr {
                             : gwg_cg(c, bA.p, bd.p, pr.p, x, rtol, maxit, pz.p, pz.p + 4 * npres);
     }
 
-    // FP32 inner solve of G^T W G into bt32: multigrid-preconditioned on the FP32 stencil, Jacobi
-    // on the stencil (bfbt_inner_pc = 2), or Jacobi with the matrix-free apply (default)
+    // FP32 inner solve of G^T W G into bt32: multigrid-preconditioned on the FP32 stencil, or
+    // Jacobi on the FP32 stencil or with the matrix-free apply
     int inner32(const double* b) {
         int maxit = o.bfbt_max_it > 0 ? o.bfbt_max_it : 500;
         double rtol = o.bfbt_rtol > 0 ? o.bfbt_rtol : 1e-4;
         if (bfbt_mg) return gwg_cg_mg32(c, bA32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
-        if (o.bfbt_inner_pc == 2) return gwg_cg32(c, bA32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
+        if (stencil32) return gwg_cg32(c, bA32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
         return gwg_cg32_mf(c, bwc32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
     }
 
@@ -994,9 +995,15 @@ void Bsscr::run() {
             to_float(c, bw.p, bw32.p, nv);
             bwc32.ensure(nv);
             gwg_mf_weights(c, bw.p, bwc32.p);   // the matrix-free inner operator's folded weights
-            // the explicit FP32 stencil only where the inner solve reads it (multigrid levels, or
-            // the stencil form asked for); the default mixed inner solve is matrix-free
-            const bool want_stencil32 = o.bfbt_inner_pc != 0;
+            // Jacobi inner solves: the FP32 stencil while it and the CG vectors take at most half
+            // of L2 (streamed from L2 it is the faster form), else the matrix-free apply, which
+            // moves about a fifth of the bytes; bfbt_inner_pc 2 / 3 force one form.  The
+            // multigrid levels start from the FP32 stencil.
+            int l2 = 0;
+            UWG_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c.device));
+            const double st_bytes = (double)npres * 4.0 * ((dim == 3 ? 27 : 9) + 6);
+            stencil32 = o.bfbt_inner_pc == 2 || (o.bfbt_inner_pc == 0 && st_bytes <= 0.5 * l2);
+            const bool want_stencil32 = stencil32 || o.bfbt_inner_pc == 1;
             if (want_stencil32) bA32.ensure((size_t)(dim == 3 ? 27 : 9) * npres);
             gwg_stencil_fp32(c, bA.p, bd.p, want_stencil32 ? bA32.p : nullptr, bd32.p);
         }
@@ -1062,7 +1069,7 @@ void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
     UWG_REQUIRE(o.remove_const_p >= 0 && o.remove_const_p <= 2, UWGPU_ERR_ARGUMENT, "bad pressure null-space mode");
     UWG_REQUIRE(o.learned_pc == 0 || o.learned_pc == 1, UWGPU_ERR_ARGUMENT, "bad learned_pc");
     UWG_REQUIRE(o.mg_cycle == 1 || o.mg_cycle == 2, UWGPU_ERR_ARGUMENT, "mg_cycle must be 1 (V) or 2 (W)");
-    UWG_REQUIRE(o.bfbt_inner_pc >= 0 && o.bfbt_inner_pc <= 2, UWGPU_ERR_ARGUMENT, "bfbt_inner_pc must be 0, 1 or 2");
+    UWG_REQUIRE(o.bfbt_inner_pc >= 0 && o.bfbt_inner_pc <= 3, UWGPU_ERR_ARGUMENT, "bfbt_inner_pc must be 0..3");
     Bsscr s(c, o, rep);
     s.run();
 }

@@ -124,9 +124,10 @@ typedef struct {
     int32_t mg_cycle;         /* coarse corrections per level visit: 1 V-cycle (default), 2 W-cycle
                                  (-pc_mg_cycle_type v|w of the velocity PCMG)                */
     int32_t bfbt_inner_pc;    /* preconditioner of the scaled BFBt inner G^T W G solves: 0 Jacobi (default,
-                                 as the reference's KSP; the mixed form applies G^T W G
-                                 matrix-free in FP32), 1 aggregation multigrid V-cycle, 2 Jacobi
-                                 on the explicit FP32 stencil in the mixed form                */
+                                 as the reference's KSP; the mixed form reads the FP32 stencil
+                                 while it fits in half of L2, else applies G^T W G matrix-free),
+                                 1 aggregation multigrid V-cycle, 2 Jacobi on the FP32 stencil,
+                                 3 Jacobi with the matrix-free FP32 apply (2, 3: mixed form)     */
 } uwgpu_solve_opts;
 
 typedef struct {

@@ -211,7 +211,8 @@ def test_picard_nonlinear_parity(oracle, uw):
     assert _rel(p, op) < 1e-7
 
 
-@pytest.mark.parametrize("case,inner_pc", [("rt2d", 0), ("spheres", 0), ("rt2d", 1), ("spheres", 1), ("spheres16", 1)])
+@pytest.mark.parametrize("case,inner_pc", [("rt2d", 0), ("spheres", 0), ("rt2d", 1), ("spheres", 1), ("spheres16", 1),
+                                           ("rt2d", 3), ("spheres16", 3)])
 def test_bfbt_preconditioner_matches_oracle(oracle, uw, case, inner_pc):
     """The scaled BFBt preconditioner (explicit G^T W G stencil + Jacobi or multigrid-preconditioned
     CG on the GPU, matrix-free Jacobi CG in the oracle) gives the Schur FGMRES the same iteration
@@ -220,7 +221,7 @@ def test_bfbt_preconditioner_matches_oracle(oracle, uw, case, inner_pc):
     from earthbyte_underworld_gb300 import workloads as W
     O, U = oracle, uw
     # with inner_pc = 1: 32x32 coarsens once (V-cycle to a dense 16x16), 8^3 is solved densely,
-    # 16^3 coarsens once in 3D
+    # 16^3 coarsens once in 3D; inner_pc = 3: the mixed form's matrix-free inner operator
     w = {"rt2d": lambda: W.rt2d(nel=(32, 32), ppc=20),
          "spheres": lambda: W.spheres(nel=(8, 8, 8), nspheres=10, seed=9),
          "spheres16": lambda: W.spheres(nel=(16, 16, 16), nspheres=20, seed=5)}[case]()
