@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
-    ap.add_argument("--mode", default="step", choices=["step", "kernels"],
+    ap.add_argument("--mode", default="step", choices=["step", "kernels", "bfbt"],
                     help="step: the full hot-path step; kernels: operator apply and smoother only")
     ap.add_argument("--iters", type=int, default=20, help="launches per kernel in --mode kernels")
     ap.add_argument("--cpu-nel", type=int, default=16, help="mesh of the CPU baseline sample")
@@ -519,10 +519,44 @@ def run_kernels(args):
     return 0
 
 
+def run_bfbt(args):
+    """The scaled BFBt inner operator's kernel in its three forms (FP64 stencil, FP32 matrix-free,
+    FP32 stencil) on a GRF-viscosity mesh of nel^3 elements (4 points per element: the operator
+    depends on the viscosity field, not on the point count), timed back to back with CUDA events."""
+    import numpy as np
+    import torch
+
+    from earthbyte_underworld_gb300 import uwgpu as U
+    from earthbyte_underworld_gb300 import workloads as W
+    n = args.nel
+    w = W.grf(nel=(n, n, n), ppc=4, grid=64, corr=0.1)
+    out = {"mode": "bfbt", "workload": f"grf_{n}cube_4ppc", "elements": n ** 3}
+    peak, kind = measured_peaks()
+    with U.Context(0) as ctx:
+        W.setup_context(ctx, w)
+        ctx.bin_and_map(want=False)
+        ctx.assemble()
+        ctx.operator_apply(np.zeros(ctx.nnodes * 3))
+        for name, form, per_elem in (("fp64_stencil", 0, 30 * 8), ("fp32_matrix_free", 1, 6 * 4),
+                                     ("fp32_stencil", 2, 30 * 4)):
+            ctx.time_bfbt_apply(form, 3)
+            ms = ctx.time_bfbt_apply(form, args.iters) / args.iters
+            gbs = n ** 3 * per_elem / ms / 1e6
+            out[name] = {"us": 1e3 * ms, "algorithmic_bytes": n ** 3 * per_elem, "GB_per_s": gbs,
+                         "frac_hbm": gbs / peak}
+    torch.cuda.synchronize()
+    out["peak_GB_per_s"] = peak
+    out["peak_source"] = kind
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "bfbt":
+        return run_bfbt(args)
     if args.mode == "kernels":
         return run_kernels(args)
     return run_ours(args)
