@@ -7,7 +7,8 @@
 //   eta  the RheologyMaterial law list (Rheology_Register.c:61-77): MaterialViscosity.c:119-139,
 //        Arrhenius.c:156-200, FrankKamenetskii.c:134-152, ViscosityLimiter.c:106-126,
 //        YieldRheology.c:198-243 + VonMises.c:206-269 + DruckerPrager.c:236-345
-//   w    ConstantWeights.c:180-189 (cellLocalVolume 2^dim / count, WeightsCalculator.c:83)
+//   w    ConstantWeights.c:180-189 (cellLocalVolume 2^dim / count, WeightsCalculator.c:83), or
+//        the discrete Voronoi weights and centroids of weights.cu (DVCWeights.c)
 //   f_e  PICellerator/Utils/src/BuoyancyForceTerm.c:310-452
 //   G_e  StgFEM/Assembly/src/GradientStiffnessMatrixTerm.c:160-250 on the 2^dim Gauss swarm
 //   S_e  StgFEM/SLE/ProvidedSystems/StokesFlow/src/UzawaPreconditionerTerm.c:155-238
@@ -32,6 +33,7 @@ struct AssemblyArgs {
     int64_t ne, nslots;
     const uint32_t* offsets;
     const double* sxi;       // [d][slot]
+    const double* sw;        // per-slot weights, or null: 2^dim / count
     const int32_t* smat;
     const double* seta_in;   // optional
     const double* srho_in;   // optional
@@ -286,8 +288,9 @@ __global__ void __launch_bounds__(128) k_assemble(AssemblyArgs A) {
         }
         double rho = rho0 * (1.0 - m.alpha * (T - m.ref_temp));
 
-        double c = w * eta;
-        double r = w * rho;
+        const double ws = A.sw ? A.sw[s] : w;
+        double c = ws * eta;
+        double r = ws * rho;
         if (DIM == 3) {
             double x1 = xi[0], y1 = xi[1], z1 = xi[2];
             double x2 = x1 * x1;
@@ -565,7 +568,7 @@ void assemble(Context& c) {
     A.ne = ne;
     A.nslots = c.np;
     A.offsets = c.offsets.p;
-    A.sxi = c.sxi.p;
+    integration_points(c, &A.sxi, &A.sw);
     A.smat = c.smat.p;
     A.seta_in = c.has_peta ? c.seta_in.p : nullptr;
     A.srho_in = c.has_prho ? c.srho_in.p : nullptr;
@@ -589,7 +592,8 @@ void assemble(Context& c) {
     {
         // algorithmic bytes: per point xi + material (+ optional inputs) read, viscosity written;
         // per element offsets read, packed K_e, f_e, G_e, S_e written
-        double per_point = dim * 8.0 + 4.0 + 8.0 + (c.has_peta ? 8.0 : 0.0) + (c.has_prho ? 8.0 : 0.0);
+        double per_point = dim * 8.0 + 4.0 + 8.0 + (c.has_peta ? 8.0 : 0.0) + (c.has_prho ? 8.0 : 0.0) +
+                           (A.sw ? 8.0 : 0.0);
         double per_el = 4.0 + packed_size(nd) * 8.0 + 2.0 * nd * 8.0 + 8.0;
         double flops_point = dim == 3 ? 120.0 : 50.0, flops_el = dim == 3 ? 3600.0 : 300.0;
         note_work(c, UWGPU_KERNEL_ASSEMBLY, per_point * c.np + per_el * ne, flops_point * c.np + flops_el * ne);

@@ -266,6 +266,14 @@ int uwgpu_bin_and_map(uwgpu_ctx* ctx, uint32_t* perm, uint32_t* offsets, double*
     });
 }
 
+int uwgpu_weights_set(uwgpu_ctx* ctx, int32_t kind, const int32_t res[3]) {
+    return guarded(ctx, [&](Context& c) { uwg::weights_set(c, kind, res); });
+}
+
+int uwgpu_integration_points(uwgpu_ctx* ctx, double* xi, double* w) {
+    return guarded(ctx, [&](Context& c) { uwg::integration_points_download(c, xi, w); });
+}
+
 int uwgpu_assemble(uwgpu_ctx* ctx) {
     return guarded(ctx, [&](Context& c) { uwg::assemble(c); });
 }

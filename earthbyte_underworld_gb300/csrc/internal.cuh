@@ -150,6 +150,12 @@ struct Context {
     DArray<uint32_t> cell, counts, offsets, cursor, perm, tmp_perm, block_sums;
     DArray<uint32_t> err_count;
     DArray<double> sxi;       // [d][slot]
+    // integration weights: constant 2^dim / count, or discrete Voronoi cells of dvc_res cells
+    // per axis (centroids dvc_xi [d][slot], volumes dvc_w [slot], boundary sets dvc_bnd)
+    int weights_kind = 0;
+    int dvc_res[3] = {10, 10, 10};
+    DArray<double> dvc_xi, dvc_w;
+    DArray<uint32_t> dvc_bnd;
     DArray<int32_t> smat;
     DArray<double> seta_in, srho_in, seta_out;
     bool mapped = false;
@@ -261,6 +267,9 @@ void build_operator(Context& c, int levels, bool need32);
 void apply_fine(Context& c, bool fp32, const double* x, double* y);  // device SoA vectors
 void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep);
 void estimate_fine_lmax(Context& c, const uwgpu_solve_opts& o);
+void weights_set(Context& c, int kind, const int32_t res[3]);
+void integration_points(Context& c, const double** xi, const double** w);
+void integration_points_download(Context& c, double* xi, double* w);
 void bfbt_operator_hook(Context& c, int form, const double* xh, double* yh, int iterations, double* ms);
 void advect_particles(Context& c, double dt, int order, bool fallback, uint32_t& fell_back, uint32_t& left_mesh);
 template <typename T> void level_cheb(Context&, Level&, const T*, T*, int, bool);

@@ -43,6 +43,9 @@ SMOOTHER_CHEBYSHEV = 1
 KERNEL_ASSEMBLY, KERNEL_APPLY, KERNEL_SMOOTH, KERNEL_BINNING, KERNEL_SCHUR_PC, KERNEL_VECTOR, KERNEL_TRANSFER, \
     KERNEL_LEARNED = range(8)
 
+WEIGHTS_CONSTANT = 0
+WEIGHTS_DVC = 1
+
 
 class UwgpuError(RuntimeError):
     def __init__(self, code, msg):
@@ -126,6 +129,8 @@ def load(build_if_missing: bool = True):
         L.uwgpu_time_smooth.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, P]
         L.uwgpu_time_chebyshev.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, P]
         L.uwgpu_bfbt_operator_apply.argtypes = [P, C.c_int32, P, P]
+        L.uwgpu_weights_set.argtypes = [P, C.c_int32, P]
+        L.uwgpu_integration_points.argtypes = [P, P, P]
         L.uwgpu_time_bfbt_apply.argtypes = [P, C.c_int32, C.c_int32, P]
         L.uwgpu_launch_count.argtypes = [P]
         L.uwgpu_launch_count.restype = C.c_int64
@@ -351,6 +356,19 @@ class Context:
         ms = C.c_double()
         self._check(self._L.uwgpu_time_smooth(self._h, precision, sweeps, iterations, C.byref(ms)))
         return ms.value
+
+    def weights_set(self, kind=0, res=(10, 10, 10)):
+        """WEIGHTS_CONSTANT (2^dim / count) or WEIGHTS_DVC (discrete Voronoi cells, res per axis)."""
+        r = np.ascontiguousarray(list(res) + [1] * (3 - len(res)), dtype=np.int32)
+        self._check(self._L.uwgpu_weights_set(self._h, kind, _ptr(r)))
+
+    def integration_points(self):
+        """(local coordinates [slot][3], weights [slot]) the last assembly integrated with."""
+        n = self.npoints
+        xi = np.zeros((n, 3))
+        w = np.zeros(n)
+        self._check(self._L.uwgpu_integration_points(self._h, _ptr(xi), _ptr(w)))
+        return xi, w
 
     def bfbt_operator_apply(self, x, form=0):
         """y = G^T W G x, the scaled BFBt inner operator of the current fine operator (form 0: FP64

@@ -210,6 +210,19 @@ int uwgpu_advect_particles(uwgpu_ctx* ctx, double dt, int32_t order, int32_t all
 /* Current particle coordinates to host arrays (n each; z ignored in 2D). */
 int uwgpu_particles_download(uwgpu_ctx* ctx, double* x, double* y, double* z);
 
+/* Integration weights of the next assemblies (the WeightsCalculator of the integration swarm).
+ * UWGPU_WEIGHTS_CONSTANT (default): ConstantWeights, 2^dim / points in the element
+ * (PICellerator/Weights/src/ConstantWeights.c:180-189).  UWGPU_WEIGHTS_DVC: DVCWeights
+ * (PICellerator/Weights/src/DVCWeights.c:763-942) on res[0] x res[1] (x res[2]) cells over the
+ * element's local coordinates (the component's resolutionX/Y/Z, default 10 each; at most 32 per
+ * axis and 1024 cells per element): every integration point moves to the centroid of its
+ * discrete Voronoi region and weighs that region's volume.  res is ignored for CONSTANT. */
+enum { UWGPU_WEIGHTS_CONSTANT = 0, UWGPU_WEIGHTS_DVC = 1 };
+int uwgpu_weights_set(uwgpu_ctx* ctx, int32_t kind, const int32_t res[3]);
+/* Local coordinates ([slot][3], z = 0 in 2D) and weights (slot order) of the integration points
+ * the last assembly used.  Either output may be NULL. */
+int uwgpu_integration_points(uwgpu_ctx* ctx, double* xi, double* w);
+
 /* Element assembly of every element: replaces the StiffnessMatrix assemble entry point
  * (StgFEM/SLE/SystemSetup/src/StiffnessMatrix.c:799-1017) for the terms
  * ConstitutiveMatrixCartesian (Underworld/Rheology/src/ConstitutiveMatrixCartesian.c:202-412),

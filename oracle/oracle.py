@@ -78,7 +78,9 @@ def lib():
             L.uwr_map.restype = C.c_int64
             L.uwr_map.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32]
             L.uwr_random_layout.argtypes = [P, C.c_int32, C.c_uint32, P]
-            L.uwr_assemble.argtypes = [P, C.c_int64, P, P, P, P, P, P, C.c_int32, P, P, P, P, P, P, P, C.c_int32]
+            L.uwr_assemble.argtypes = [P, C.c_int64, P, P, P, P, P, P, C.c_int32, P, P, P, P, P, P, P, P, C.c_int32]
+            L.uwr_dvc_element.argtypes = [C.c_int, P, C.c_int32, P, P, P]
+            L.uwr_dvc_weights.argtypes = [P, P, P, P, P, P, C.c_int32]
             L.uwr_assemble_gauss.argtypes = [P, C.c_int32, P, P, P, P]
             L.uwr_eqnum.restype = C.c_int64
             L.uwr_eqnum.argtypes = [P, P, P]
@@ -179,7 +181,9 @@ def make_fields(temperature=None, velocity=None, pressure=None, previous_solutio
 
 
 def assemble(m, offsets, perm, xi, material, mats, fields, point_eta=None, point_rho=None,
-             nthreads=0, want_eta=False):
+             nthreads=0, want_eta=False, weights=None):
+    """Element matrices from the points in slot order (xi [slot][3]); weights: per-slot
+    integration weights (e.g. dvc_weights), else the constant 2^dim / count."""
     dim = m.dim
     nen = 8 if dim == 3 else 4
     nd = nen * dim
@@ -193,13 +197,39 @@ def assemble(m, offsets, perm, xi, material, mats, fields, point_eta=None, point
     material = None if material is None else np.ascontiguousarray(material, dtype=np.int32)
     point_eta = None if point_eta is None else np.ascontiguousarray(point_eta, dtype=np.float64)
     point_rho = None if point_rho is None else np.ascontiguousarray(point_rho, dtype=np.float64)
+    weights = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
     arr = materials_array(mats)
     rc = lib().uwr_assemble(C.byref(m), n, _p(offsets), _p(perm), _p(np.ascontiguousarray(xi)),
                             _p(material), _p(point_eta), _p(point_rho), len(mats), arr,
-                            C.byref(fields), _p(Ke), _p(fe), _p(Ge), _p(Se), _p(eta), nthreads)
+                            C.byref(fields), _p(Ke), _p(fe), _p(Ge), _p(Se), _p(eta), _p(weights), nthreads)
     if rc != 0:
         raise RuntimeError("oracle assembly failed (material index out of range)")
     return Ke, fe, Ge, Se, eta
+
+
+def dvc_element(dim, res, xi):
+    """Discrete Voronoi weights of one element: xi (nump, dim) local coordinates -> (centroids
+    (nump, dim), weights (nump,), growth passes)."""
+    xi = np.ascontiguousarray(xi, dtype=np.float64).reshape(-1, dim)
+    r = np.ascontiguousarray(list(res) + [1] * (3 - len(res)), dtype=np.int32)
+    cxi = np.zeros_like(xi)
+    w = np.zeros(xi.shape[0])
+    passes = lib().uwr_dvc_element(dim, _p(r), xi.shape[0], _p(xi), _p(cxi), _p(w))
+    if passes < 0:
+        raise ValueError("DVC resolution out of range")
+    return cxi, w, passes
+
+
+def dvc_weights(m, res, offsets, xi, nthreads=0):
+    """Discrete Voronoi weights of every element, points in slot order: xi [slot][3] ->
+    (centroids [slot][3], weights [slot])."""
+    xi = np.ascontiguousarray(xi, dtype=np.float64).reshape(-1, 3)
+    r = np.ascontiguousarray(list(res) + [1] * (3 - len(res)), dtype=np.int32)
+    cxi = np.zeros_like(xi)
+    w = np.zeros(xi.shape[0])
+    lib().uwr_dvc_weights(C.byref(m), _p(r), _p(np.ascontiguousarray(offsets, dtype=np.uint32)), _p(xi), _p(cxi),
+                          _p(w), nthreads)
+    return cxi, w
 
 
 def assemble_gauss(m, mats, el_material, fields):

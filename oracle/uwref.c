@@ -720,7 +720,7 @@ int uwr_assemble(const uwr_mesh* m, int64_t n, const uint32_t* offsets, const ui
                  const double* xi, const int32_t* material, const double* point_eta,
                  const double* point_rho, int32_t nmat, const uwr_material* mats,
                  const uwr_fields* f, double* Ke, double* fe, double* Ge, double* Se,
-                 double* eta_out, int32_t nthreads) {
+                 double* eta_out, const double* slot_weight, int32_t nthreads) {
     (void)n;
     set_threads(nthreads);
     int dim = m->dim, nen = (dim == 3) ? 8 : 4, nd = nen * dim;
@@ -749,6 +749,7 @@ int uwr_assemble(const uwr_mesh* m, int64_t n, const uint32_t* offsets, const ui
         for (uint32_t s = beg; s < end; ++s) {
             uint32_t p = perm[s];
             const double* x = xi + 3 * (int64_t)s;
+            if (slot_weight) weight = slot_weight[s];
             double detJ, GNx[24], N[8];
             global_derivs_nodes(dim, rp.nodes, x, &detJ, GNx);
             uwr_shape(dim, x, N);
@@ -782,6 +783,161 @@ int uwr_assemble(const uwr_mesh* m, int64_t n, const uint32_t* offsets, const ui
         }
     }
     return bad ? -1 : 0;
+}
+
+/* ---- discrete Voronoi cell weights (PICellerator/Weights/src/DVCWeights.c) --------------------
+ * An element's local square / cube [-1, 1]^dim carries a fixed grid of res[0] x res[1] (x res[2])
+ * cells, x fastest (_DVCWeights_ConstructGrid, :500-594: the cell centres are accumulated from
+ * -1 - h/2 by repeated additions of h = 2 / res, as below).  Every point first claims the cell
+ * that holds it (cell index = (int)((xi + 1) / h), the upper face folded into the last cell; a
+ * later point in the same cell takes it over).  Then the points grow their regions in passes
+ * (_DVCWeights_CreateVoronoi, :668-714): in point order, each point tries the cells of its
+ * boundary (_DVCWeights_ClaimCells, :261-317).  It takes a free cell, and a cell held by another
+ * point when it is strictly nearer to the cell's centre by _DVCWeights_DistanceTest (:604-609,
+ * evaluated in the same order: (x1 + x2 - x0 - x0)(x1 - x2) + ... > 0, owner 1, challenger 2,
+ * centre 0).  Its boundary becomes the face neighbours of the cells it has just taken that it
+ * does not hold (_DVCWeights_UpdateBchain, :395-446).  The passes end when one takes no cell.
+ * Weight = cells held x cell volume; the new local coordinate is the mean of the held cells'
+ * centres, summed in cell order (_DVCWeights_GetCentroids, :203-231); a point that holds no
+ * cell keeps weight 0 and coordinate 0. */
+static void dvc_centres(int n, double* c) {
+    const double h = 2.0 / n;
+    double x = -1.0 - h / 2.0;
+    for (int i = 0; i < n; ++i) {
+        x = x + h;
+        c[i] = x;
+    }
+}
+
+static double dvc_contest(int dim, const double* c0, const double* p1, const double* p2) {
+    double t = (p1[0] + p2[0] - c0[0] - c0[0]) * (p1[0] - p2[0]) + (p1[1] + p2[1] - c0[1] - c0[1]) * (p1[1] - p2[1]);
+    if (dim == 3) t = t + (p1[2] + p2[2] - c0[2] - c0[2]) * (p1[2] - p2[2]);
+    return t;
+}
+
+int uwr_dvc_element(int dim, const int32_t res[3], int32_t nump, const double* xi, double* cxi, double* w) {
+    const int nx = res[0], ny = res[1], nz = dim == 3 ? res[2] : 1;
+    const int nc = nx * ny * nz;
+    if (nx < 1 || ny < 1 || nz < 1 || nx > 64 || ny > 64 || nz > 64 || nc > 4096) return -1;
+    double cen[3][64];
+    dvc_centres(nx, cen[0]);
+    dvc_centres(ny, cen[1]);
+    if (dim == 3) dvc_centres(nz, cen[2]);
+    const double h[3] = {2.0 / nx, 2.0 / ny, dim == 3 ? 2.0 / nz : 1.0};
+    int* owner = (int*)malloc(sizeof(int) * (size_t)nc);
+    unsigned char* mark = (unsigned char*)calloc((size_t)nc, 1);
+    int* bnd = (int*)malloc(sizeof(int) * (size_t)nc * (size_t)(nump > 0 ? nump : 1));
+    int* nbnd = (int*)calloc((size_t)(nump > 0 ? nump : 1), sizeof(int));
+    int* took = (int*)malloc(sizeof(int) * (size_t)nc);
+    for (int c = 0; c < nc; ++c) owner[c] = -1;
+    /* the boundary of p after it took the cells took[0..ntook) */
+#define DVC_BOUNDARY(p, ntook)                                                                       \
+    do {                                                                                             \
+        int* B = bnd + (size_t)(p) * nc;                                                             \
+        int nb = 0;                                                                                  \
+        for (int t_ = 0; t_ < (ntook); ++t_) {                                                       \
+            const int c = took[t_];                                                                  \
+            const int x = c % nx, y = (c / nx) % ny, z = c / (nx * ny);                              \
+            int q[6], nq = 0;                                                                        \
+            if (y > 0) q[nq++] = c - nx;                                                             \
+            if (y < ny - 1) q[nq++] = c + nx;                                                        \
+            if (x < nx - 1) q[nq++] = c + 1;                                                         \
+            if (x > 0) q[nq++] = c - 1;                                                              \
+            if (z < nz - 1) q[nq++] = c + nx * ny;                                                   \
+            if (z > 0) q[nq++] = c - nx * ny;                                                        \
+            for (int k_ = 0; k_ < nq; ++k_)                                                          \
+                if (owner[q[k_]] != (p) && !mark[q[k_]]) {                                           \
+                    mark[q[k_]] = 1;                                                                 \
+                    B[nb++] = q[k_];                                                                 \
+                }                                                                                    \
+        }                                                                                            \
+        for (int k_ = 0; k_ < nb; ++k_) mark[B[k_]] = 0;                                             \
+        nbnd[p] = nb;                                                                                \
+    } while (0)
+    for (int p = 0; p < nump; ++p) {
+        int idx[3] = {0, 0, 0};
+        for (int d = 0; d < dim; ++d) {
+            const int n = d == 0 ? nx : (d == 1 ? ny : nz);
+            idx[d] = (int)((xi[p * dim + d] - -1.0) / h[d]);
+            if (idx[d] == n) idx[d]--;
+        }
+        const int c = idx[0] + nx * (idx[1] + ny * idx[2]);
+        owner[c] = p;
+        took[0] = c;
+        DVC_BOUNDARY(p, 1);
+    }
+    int passes = 0, taken = nump > 0;
+    while (taken) {
+        taken = 0;
+        ++passes;
+        for (int p = 0; p < nump; ++p) {
+            const int* B = bnd + (size_t)p * nc;
+            int ntook = 0;
+            for (int k = 0; k < nbnd[p]; ++k) {
+                const int c = B[k];
+                int take = 0;
+                if (owner[c] == -1) {
+                    take = 1;
+                } else if (owner[c] != p) {
+                    const double c0[3] = {cen[0][c % nx], cen[1][(c / nx) % ny], dim == 3 ? cen[2][c / (nx * ny)] : 0.0};
+                    take = dvc_contest(dim, c0, xi + (size_t)owner[c] * dim, xi + (size_t)p * dim) > 0.0;
+                }
+                if (take) {
+                    owner[c] = p;
+                    took[ntook++] = c;
+                }
+            }
+            taken += ntook;
+            DVC_BOUNDARY(p, ntook);
+        }
+    }
+#undef DVC_BOUNDARY
+    const double da = dim == 3 ? h[0] * h[1] * h[2] : h[0] * h[1];
+    int* count = (int*)calloc((size_t)(nump > 0 ? nump : 1), sizeof(int));
+    for (int p = 0; p < nump * dim; ++p) cxi[p] = 0.0;
+    for (int c = 0; c < nc; ++c) {
+        const int p = owner[c];
+        if (p < 0) continue;
+        cxi[p * dim + 0] += cen[0][c % nx];
+        cxi[p * dim + 1] += cen[1][(c / nx) % ny];
+        if (dim == 3) cxi[p * dim + 2] += cen[2][c / (nx * ny)];
+        count[p]++;
+    }
+    for (int p = 0; p < nump; ++p) {
+        w[p] = count[p] * da;
+        if (count[p] != 0)
+            for (int d = 0; d < dim; ++d) cxi[p * dim + d] /= count[p];
+    }
+    free(count);
+    free(took);
+    free(nbnd);
+    free(bnd);
+    free(mark);
+    free(owner);
+    return passes;
+}
+
+void uwr_dvc_weights(const uwr_mesh* m, const int32_t res[3], const uint32_t* offsets, const double* xi,
+                     double* cxi, double* w, int32_t nthreads) {
+    set_threads(nthreads);
+    const int dim = m->dim;
+    const int64_t E = uwr_num_elements(m);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t e = 0; e < E; ++e) {
+        const uint32_t beg = offsets[e], n = offsets[e + 1] - beg;
+        double pin[3 * 512], pout[3 * 512];
+        double* a = n <= 512 ? pin : (double*)malloc(sizeof(double) * 3 * n);
+        double* b = n <= 512 ? pout : (double*)malloc(sizeof(double) * 3 * n);
+        for (uint32_t i = 0; i < n; ++i)
+            for (int d = 0; d < dim; ++d) a[i * dim + d] = xi[3 * (int64_t)(beg + i) + d];
+        uwr_dvc_element(dim, res, (int32_t)n, a, b, w + beg);
+        for (uint32_t i = 0; i < n; ++i) {
+            for (int d = 0; d < dim; ++d) cxi[3 * (int64_t)(beg + i) + d] = b[i * dim + d];
+            if (dim == 2) cxi[3 * (int64_t)(beg + i) + 2] = 0.0;
+        }
+        if (a != pin) free(a);
+        if (b != pout) free(b);
+    }
 }
 
 int uwr_assemble_gauss(const uwr_mesh* m, int32_t nmat, const uwr_material* mats,

@@ -98,7 +98,18 @@ int uwr_assemble(const uwr_mesh* m, int64_t n, const uint32_t* offsets, const ui
                  const double* xi, const int32_t* material, const double* point_eta,
                  const double* point_rho, int32_t nmat, const uwr_material* mats,
                  const uwr_fields* f, double* Ke, double* fe, double* Ge, double* Se,
-                 double* eta_out, int32_t nthreads);
+                 double* eta_out, const double* slot_weight /* NULL: constant weights */,
+                 int32_t nthreads);
+
+/* Discrete Voronoi cell weights (PICellerator/Weights/src/DVCWeights.c) --------------------- */
+/* One element: nump points at local coordinates xi[p*dim + d]; res[d] cells per axis
+ * (res[0]*res[1](*res[2]) <= 4096).  Out: the new local coordinates (the centroids of the
+ * points' discrete Voronoi regions) cxi[p*dim + d] and the weights w[p] (region volume in local
+ * coordinates).  Returns the number of growth passes. */
+int uwr_dvc_element(int dim, const int32_t res[3], int32_t nump, const double* xi, double* cxi, double* w);
+/* Every element of the mesh, points in slot order: xi and cxi are [slot][3] (z unused in 2D). */
+void uwr_dvc_weights(const uwr_mesh* m, const int32_t res[3], const uint32_t* offsets, const double* xi,
+                     double* cxi, double* w, int32_t nthreads);
 
 /* Gauss-swarm element matrices (2^dim Gauss points, unit weights). */
 void uwr_gauss_G(const uwr_mesh* m, int64_t e, double* Ge /* nd */);
