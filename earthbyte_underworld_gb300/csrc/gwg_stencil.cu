@@ -65,6 +65,29 @@ __device__ __forceinline__ T block_ratio(const double* num, const double* den, T
     return *slot;
 }
 
+// Programmatic dependent launch between the CG kernels: a kernel waits for the grid before it
+// (griddepcontrol.wait: that grid has completed and its writes are visible) before it reads
+// anything, and lets the next grid start launching once all its own writes are issued, so the
+// next kernel's blocks are resident when this one ends.  Without a programmatic predecessor the
+// wait returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kern)(KArgs...), unsigned grid, unsigned block, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    UWG_CUDA(cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
+}
+
 // A[q][e] = sum over the nodes n shared by e and f = e + off(q), and the free components d of n,
 //           G_(n,d),e W_(n,d) G_(n,d),f   with  G_(n,d),e = -s prod_{k != d} h_k / 2^(dim-1),
 // s = +1 when n is on the upper side of e along d (the P0 divergence term of the Q1 element,
@@ -193,6 +216,7 @@ __global__ void __launch_bounds__(256) k_cg_spmv_dir(EGrid g, const T* __restric
     constexpr int NB = stencil_points<DIM>();
     __shared__ double sw[32];
     __shared__ T s_beta;
+    pdl_wait();
     const T beta = first ? (T)0 : block_ratio<T>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
     const int ne = (int)g.ne, ex = (int)g.ex, ey = (int)g.ey, ez = (int)g.ez;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -220,6 +244,7 @@ __global__ void __launch_bounds__(256) k_cg_spmv_dir(EGrid g, const T* __restric
     if (blockIdx.x == 0 && threadIdx.x == 0) *rr_slot(scal, k + 1) = 0.0;
     double t = block_sum<T>(local, sw);
     if (threadIdx.x == 0) atomicAdd(pq_slot(scal, k + 1), t);
+    pdl_trigger();
 }
 
 // Elements per thread of the vector kernels: the block reduction (a shuffle tree, FP64 in the
@@ -236,6 +261,7 @@ __global__ void k_cg_update(int64_t ne, const T* __restrict__ p, const T* __rest
                             double* __restrict__ scal, int k, int want_rr) {
     __shared__ double sw[32];
     __shared__ T s_alpha;
+    pdl_wait();
     const T alpha = block_ratio<T>(rz_slot(scal, k), pq_slot(scal, k), &s_alpha);
     const int64_t base = (int64_t)blockIdx.x * blockDim.x * kEpt + threadIdx.x;
     T rz = (T)0, rr = (T)0;
@@ -263,6 +289,7 @@ __global__ void k_cg_update(int64_t ne, const T* __restrict__ p, const T* __rest
         double t2 = block_sum<T>(rr, sw);
         if (threadIdx.x == 0) atomicAdd(rr_slot(scal, k), t2);
     }
+    pdl_trigger();
 }
 
 // r = b, z = dinv r, x = 0 ; rz_0 (scal[0]) = r.z, scal[7] = r0.r0 (scal zeroed before; p and q
@@ -321,6 +348,7 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf2_dir(int ex, int ey, int6
     const int ntx = (ex + kMfX - 1) / kMfX;
     const int x0 = (blockIdx.x % ntx) * kMfX, y0 = (blockIdx.x / ntx) * kMfY;
     const int tid = threadIdx.x, lx = tid % kMfX, ly = tid / kMfX;
+    pdl_wait();
     for (int i = tid; i < HY * HX; i += NT) {
         const int gx = x0 - 1 + i % HX, gy = y0 - 1 + i / HX;
         zs[i] = (gx >= 0 && gx < ex && gy >= 0 && gy < ey) ? __ldg(z + gx + ex * gy) : 0.f;
@@ -358,6 +386,7 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf2_dir(int ex, int ey, int6
     if (blockIdx.x == 0 && threadIdx.x == 0) *rr_slot(scal, k + 1) = 0.0;
     double t = block_sum<float>(local, sw);
     if (threadIdx.x == 0) atomicAdd(pq_slot(scal, k + 1), t);
+    pdl_trigger();
 }
 
 // 3D: a block owns a column of kMfX x kMfY elements over zc element planes and marches up z.  Step
@@ -428,6 +457,7 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* 
         pn = ok ? p[plane * exy + eo] : 0.f;
         qn = ok ? q[plane * exy + eo] : 0.f;
     };
+    pdl_wait();
     const float beta = first ? 0.f : block_ratio<float>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
     // prologue: element plane zlo - 1 into buffer 0; registers for plane zlo
     load_z(zlo - 1);
@@ -504,6 +534,7 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* 
     if (blockIdx.x == 0 && threadIdx.x == 0) *rr_slot(scal, k + 1) = 0.0;
     double t = block_sum<float>(local, sw);
     if (threadIdx.x == 0) atomicAdd(pq_slot(scal, k + 1), t);
+    pdl_trigger();
 }
 
 // Wc_(n,d) = a_d^2 W_(n,d) in FP32 (the weights of the matrix-free apply)
@@ -550,8 +581,8 @@ static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* Wc, int sms) 
 static void mf_dir(const MfLaunch& L, cudaStream_t st, const float* z, float* p, float* q, double* scal, int k,
                    int first) {
     const unsigned nt = kMfX * kMfY;
-    if (L.dim == 2) k_cg_mf2_dir<<<L.blocks, nt, 0, st>>>(L.ex, L.ey, L.nnx, L.nn, L.Wc, z, p, q, scal, k, first);
-    else k_cg_mf3_dir<<<L.blocks, nt, 0, st>>>(L.a3, L.Wc, z, p, q, scal, k, first);
+    if (L.dim == 2) launch_pdl(k_cg_mf2_dir, L.blocks, nt, st, L.ex, L.ey, L.nnx, L.nn, L.Wc, z, p, q, scal, k, first);
+    else launch_pdl(k_cg_mf3_dir, L.blocks, nt, st, L.a3, L.Wc, z, p, q, scal, k, first);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -841,8 +872,8 @@ static int gwg_cg_T(Context& c, const T* A, const float* Wmf, const T* dinv, con
                 return;
             }
         }
-        if (m.dim == 3) k_cg_spmv_dir<3, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, first);
-        else k_cg_spmv_dir<2, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, first);
+        if (m.dim == 3) launch_pdl(k_cg_spmv_dir<3, T>, eb, 256, c.stream, g, A, z, p, q, scal, k, first);
+        else launch_pdl(k_cg_spmv_dir<2, T>, eb, 256, c.stream, g, A, z, p, q, scal, k, first);
     };
     UWG_CUDA(cudaMemsetAsync(scal, 0, 8 * sizeof(double), c.stream));
     {
@@ -862,7 +893,7 @@ static int gwg_cg_T(Context& c, const T* A, const float* Wmf, const T* dinv, con
     // graph per buffer set, replayed until converged; the host checks the residual once per replay.
     const int block = 12;
     auto issue = [&](int k) {
-        k_cg_update<T><<<ebv, 256, 0, c.stream>>>(ne, p, q, dinv, x, r, z, scal, k, k == block - 1);
+        launch_pdl(k_cg_update<T>, ebv, 256, c.stream, ne, p, q, dinv, x, r, z, scal, k, (int)(k == block - 1));
         dir(k, 0);
     };
     const void* key[8] = {Wmf ? (const void*)Wmf : (const void*)A, dinv, x, work, scal, (const void*)(intptr_t)ne,
