@@ -22,8 +22,6 @@
 #include <iterator>
 #include <type_traits>
 
-#include <math_constants.h>
-
 #include "internal.cuh"
 
 namespace uwg {
@@ -539,248 +537,6 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* 
     pdl_trigger();
 }
 
-// ------------------------------------------------------------------------------------------
-// One-reduction CG for the mixed form's 3D inner solves (Chronopoulos and Gear's arrangement of
-// Jacobi-preconditioned CG: the same iterates as CG in exact arithmetic, one grid reduction per
-// iteration instead of two).  Iteration i, one kernel:
-//   beta = g_i / g_(i-1), alpha = g_i / (d_i - beta g_i / alpha_(i-1))   (i = 0: beta = 0, alpha = g_0 / d_0)
-//   p = u + beta p,  s = w + beta s,  x += alpha p,  r -= alpha s,  u = Dinv r,  w = A u,
-//   g_(i+1) = r.u,  d_(i+1) = w.u  (and r.r for the convergence test)
-// w = A u needs u on the tile's halo: the kernel forms it there from r, w, s and Dinv, which are
-// double-buffered (iteration i reads set i mod 2 and writes the other), so no block overwrites
-// what another block still reads; u, p and x are touched only by their own element's thread.
-// The march over z planes is that of k_cg_mf3_dir; the staging thread of an element of the
-// block's own tile also writes its new s and r.  Each new value is formed once, with explicit
-// fmaf, and read back from shared memory where it is needed again.
-// Scalars: g by iteration mod 4 (scal[0..3]), d mod 4 (scal[4..7]), alpha mod 2 (scal[8..9]),
-// r.r mod 2 (scal[10..11]), r0.r0 scal[12]; iteration i clears g, d of i + 2 and r.r of i + 1.
-// INIT (before iteration 0): r = b, s = 0, p = 0, x = 0, u = Dinv b, w = A u, g_0, d_0, r0.r0,
-// g_(-1) = inf, alpha_(-1) = 1.
-// ------------------------------------------------------------------------------------------
-__device__ __forceinline__ double* cgc_g(double* scal, int i) { return scal + (i & 3); }
-__device__ __forceinline__ double* cgc_d(double* scal, int i) { return scal + 4 + (i & 3); }
-__device__ __forceinline__ double* cgc_a(double* scal, int i) { return scal + 8 + (i & 1); }
-__device__ __forceinline__ double* cgc_rr(double* scal, int i) { return scal + 10 + (i & 1); }
-
-struct CgcVec {
-    float *x, *p, *u;
-    const float* r_in;
-    const float* w_in;
-    const float* s_in;
-    float *r_out, *w_out, *s_out;
-    const float* dinv;
-    const double* b;   // INIT only
-};
-
-template <bool INIT>
-__global__ void __launch_bounds__(kMfX * kMfY) k_cgc_mf3(Mf3 a, const float* __restrict__ Wc, CgcVec v,
-                                                         double* __restrict__ scal, int it, int want_rr) {
-    constexpr int NT = kMfX * kMfY;
-    constexpr int HX = kMfX + 2, HY = kMfY + 2, HP = HX * HY;
-    constexpr int NX = kMfX + 1, NY = kMfY + 1, NP = NX * NY;
-    static_assert(HP <= 2 * NT && NP <= 2 * NT, "two slots per thread cover a plane");
-    __shared__ float zb[3][HP];   // new u on the element planes (with halo)
-    __shared__ float rb[3][HP];   // new r on the element planes (with halo)
-    __shared__ float yb[2][3][NP];
-    __shared__ double sw[32];
-    __shared__ float s_ab[2];
-    const int ex = a.ex, ey = a.ey, ez = a.ez;
-    const int ntx = (ex + kMfX - 1) / kMfX, nty = (ey + kMfY - 1) / kMfY;
-    int bi = blockIdx.x;
-    const int x0 = (bi % ntx) * kMfX;
-    bi /= ntx;
-    const int y0 = (bi % nty) * kMfY;
-    bi /= nty;
-    const int zlo = bi * a.zc, zhi = min(zlo + a.zc, ez);
-    const int tid = threadIdx.x, tx = tid % kMfX, ty = tid / kMfX;
-    const int64_t exy = (int64_t)ex * ey, nxy = a.nnx * a.nny;
-    int zo[2], nbase[2];
-    bool zok[2], zown[2], nok[2];
-    int64_t no[2];
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-        const int i = tid + s * NT;
-        const int hx = i % HX, hy = i / HX, gx = x0 - 1 + hx, gy = y0 - 1 + hy;
-        zok[s] = i < HP && gx >= 0 && gx < ex && gy >= 0 && gy < ey;
-        zown[s] = zok[s] && hx >= 1 && hx <= kMfX && hy >= 1 && hy <= kMfY;   // in this block's tile
-        zo[s] = zok[s] ? gx + ex * gy : 0;
-        const int nx = i % NX, ny = i / NX;
-        nok[s] = i < NP && x0 + nx <= ex && y0 + ny <= ey;
-        no[s] = nok[s] ? (x0 + nx) + a.nnx * (y0 + ny) : 0;
-        nbase[s] = ny * HX + nx;
-    }
-    const bool eok = x0 + tx < ex && y0 + ty < ey;
-    const int eo = eok ? (x0 + tx) + ex * (y0 + ty) : 0;
-    // staging inputs of the next plane: (w, s, r, dinv) per slot; INIT: (b, dinv)
-    float in_w[2], in_s[2], in_r[2], in_d[2], wr[2][3], pn = 0.f, xn = 0.f, un = 0.f;
-    auto load_in = [&](int plane) {
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const bool ok = zok[s] && plane >= 0 && plane < ez;
-            const int64_t f = plane * exy + zo[s];
-            if (INIT) {
-                in_r[s] = ok ? (float)v.b[ok ? f : 0] : 0.f;
-                in_w[s] = 0.f;
-                in_s[s] = 0.f;
-            } else {
-                in_w[s] = ok ? __ldg(v.w_in + f) : 0.f;
-                in_s[s] = ok ? __ldg(v.s_in + f) : 0.f;
-                in_r[s] = ok ? __ldg(v.r_in + f) : 0.f;
-            }
-            in_d[s] = ok ? __ldg(v.dinv + f) : 0.f;
-        }
-    };
-    auto load_w = [&](int plane) {
-#pragma unroll
-        for (int s = 0; s < 2; ++s)
-#pragma unroll
-            for (int d = 0; d < 3; ++d)
-                wr[s][d] = nok[s] && plane <= ez ? __ldg(Wc + d * a.nn + plane * nxy + no[s]) : 0.f;
-    };
-    auto load_own = [&](int plane) {
-        const bool ok = !INIT && eok && plane < zhi;
-        const int64_t e = plane * exy + eo;
-        un = ok ? v.u[e] : 0.f;
-        pn = ok ? v.p[e] : 0.f;
-        xn = ok ? v.x[e] : 0.f;
-    };
-    pdl_wait();
-    float alpha = 0.f, beta = 0.f;
-    if (!INIT) {
-        if (threadIdx.x == 0) {
-            // before the first iteration INIT leaves g_(-1) = inf and alpha_(-1) = 1, so that the
-            // general form gives beta = 0 and alpha = g_0 / d_0
-            const double g = *cgc_g(scal, it), dd = *cgc_d(scal, it);
-            const double be = g / *cgc_g(scal, it - 1);
-            const double al = g / (dd - be * g / *cgc_a(scal, it - 1));
-            s_ab[0] = (float)al;
-            s_ab[1] = (float)be;
-            if (blockIdx.x == 0) {
-                *cgc_a(scal, it) = al;
-                *cgc_g(scal, it + 2) = 0.0;
-                *cgc_d(scal, it + 2) = 0.0;
-                *cgc_rr(scal, it + 1) = 0.0;
-            }
-        }
-        __syncthreads();
-        alpha = s_ab[0];
-        beta = s_ab[1];
-    }
-    // stage a plane: s = w + beta s, r = r - alpha s, u = Dinv r on every slot; the block's own
-    // elements also get their new s and r written
-    auto stage = [&](int plane, float* zdst, float* rdst) {
-        const bool own_plane = plane >= zlo && plane < zhi;
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const int i = tid + s * NT;
-            if (i < HP) {
-                const float sn = INIT ? 0.f : fmaf(beta, in_s[s], in_w[s]);
-                const float rn = INIT ? in_r[s] : fmaf(-alpha, sn, in_r[s]);
-                const float u_ = rn * in_d[s];
-                zdst[i] = u_;
-                rdst[i] = rn;
-                if (zown[s] && own_plane) {
-                    const int64_t f = plane * exy + zo[s];
-                    v.s_out[f] = sn;
-                    v.r_out[f] = rn;
-                }
-            }
-        }
-    };
-    load_in(zlo - 1);
-    stage(zlo - 1, zb[0], rb[0]);
-    load_in(zlo);
-    load_w(zlo);
-    float lo[3][4], hi[3][4];
-    float gsum = 0.f, dsum = 0.f, rsum = 0.f;
-    const int ybase = ty * NX + tx;
-    for (int t = 1; t <= zhi - zlo + 1; ++t) {
-        const int kk = zlo - 1 + t;
-        float* zc = zb[t % 3];
-        const float* zp = zb[(t + 2) % 3];   // element plane kk - 1
-        const float* rp = rb[(t + 2) % 3];
-        stage(kk, zc, rb[t % 3]);
-        float wc[2][3];
-#pragma unroll
-        for (int s = 0; s < 2; ++s)
-#pragma unroll
-            for (int d = 0; d < 3; ++d) wc[s][d] = wr[s][d];
-        const float uc = un, pc = pn, xc = xn;
-        load_in(kk + 1);
-        load_w(kk + 1);
-        load_own(kk);   // element plane kk, updated in the next step
-        __syncthreads();
-        float* yc = yb[t & 1][0];
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const int i = tid + s * NT;
-            if (i < NP) {
-                const int b = nbase[s];
-                const float z000 = zp[b], z100 = zp[b + 1], z010 = zp[b + HX], z110 = zp[b + HX + 1];
-                const float z001 = zc[b], z101 = zc[b + 1], z011 = zc[b + HX], z111 = zc[b + HX + 1];
-                const float dx = (z100 - z000) + (z110 - z010) + (z101 - z001) + (z111 - z011);
-                const float dy = (z010 - z000) + (z110 - z100) + (z011 - z001) + (z111 - z101);
-                const float dz = (z001 - z000) + (z101 - z100) + (z011 - z010) + (z111 - z110);
-                yc[i] = wc[s][0] * dx;
-                yc[NP + i] = wc[s][1] * dy;
-                yc[2 * NP + i] = wc[s][2] * dz;
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int c4 = 0; c4 < 4; ++c4) {
-            const int ni = ybase + (c4 >> 1) * NX + (c4 & 1);
-#pragma unroll
-            for (int d = 0; d < 3; ++d) hi[d][c4] = yc[d * NP + ni];
-        }
-        if (t >= 2 && eok) {
-            float wn = 0.f;
-#pragma unroll
-            for (int c4 = 0; c4 < 4; ++c4) {
-                wn += (c4 & 1) ? -(lo[0][c4] + hi[0][c4]) : (lo[0][c4] + hi[0][c4]);
-                wn += (c4 >> 1) ? -(lo[1][c4] + hi[1][c4]) : (lo[1][c4] + hi[1][c4]);
-                wn += lo[2][c4] - hi[2][c4];
-            }
-            const int64_t e = (int64_t)(kk - 1) * exy + eo;
-            const int ci = (ty + 1) * HX + tx + 1;
-            const float u_ = zp[ci], rn = rp[ci];
-            if (INIT) {
-                v.p[e] = 0.f;
-                v.x[e] = 0.f;
-            } else {
-                const float pe = fmaf(beta, pc, uc);
-                v.p[e] = pe;
-                v.x[e] = fmaf(alpha, pe, xc);
-            }
-            v.u[e] = u_;
-            v.w_out[e] = wn;
-            gsum = fmaf(rn, u_, gsum);
-            dsum = fmaf(wn, u_, dsum);
-            rsum = fmaf(rn, rn, rsum);
-        }
-#pragma unroll
-        for (int c4 = 0; c4 < 4; ++c4)
-#pragma unroll
-            for (int d = 0; d < 3; ++d) lo[d][c4] = hi[d][c4];
-    }
-    if (INIT && blockIdx.x == 0 && threadIdx.x == 0) {
-        *cgc_g(scal, -1) = CUDART_INF;
-        *cgc_a(scal, -1) = 1.0;
-    }
-    const int nx_it = INIT ? 0 : it + 1;
-    double t1 = block_sum<float>(gsum, sw);
-    if (threadIdx.x == 0) atomicAdd(cgc_g(scal, nx_it), t1);
-    __syncthreads();
-    double t2 = block_sum<float>(dsum, sw);
-    if (threadIdx.x == 0) atomicAdd(cgc_d(scal, nx_it), t2);
-    if (INIT || want_rr) {
-        __syncthreads();
-        double t3 = block_sum<float>(rsum, sw);
-        if (threadIdx.x == 0) atomicAdd(INIT ? scal + 12 : cgc_rr(scal, it), t3);
-    }
-    pdl_trigger();
-}
-
 // Wc_(n,d) = a_d^2 W_(n,d) in FP32 (the weights of the matrix-free apply)
 __global__ void k_mf_weights(int64_t nn, int dim, double a0, double a1, double a2, const double* __restrict__ W,
                              float* __restrict__ Wc) {
@@ -1213,93 +969,6 @@ void gwg_mf_weights(Context& c, const double* W, float* Wc) {
     LaunchScope ls(c, -1);
     k_mf_weights<<<blocks_for(m.nn, 256), 256, 0, c.stream>>>(m.nn, m.dim, a[0], a[1], a[2], W, Wc);
     check_launch("k_mf_weights");
-}
-
-// The mixed form's 3D inner solve with the matrix-free operator as one-reduction CG (k_cgc_mf3):
-// work holds 8 ne floats (p, u and two sets of r, w, s), scal 16 doubles.  Twelve iterations per
-// CUDA graph (the scalar slots repeat with period 4, the vector sets with period 2).
-int gwg_cg32_cgc(Context& c, const float* Wc, const float* dinv, const double* b, float* x, double rtol, int maxit,
-                 float* work, double* scal) {
-    const MeshDesc& m = c.levels[0].mesh;
-    UWG_REQUIRE(m.dim == 3, UWGPU_ERR_ARGUMENT, "one-reduction inner CG is 3D");
-    EGrid g = egrid_of(m);
-    const int64_t ne = g.ne;
-    int sms = 0;
-    UWG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
-    const MfLaunch mf = mf_launch(m, g, Wc, sms);
-    float* p = work;
-    float* u = work + ne;
-    float* rs[2] = {work + 2 * ne, work + 3 * ne};
-    float* ws[2] = {work + 4 * ne, work + 5 * ne};
-    float* ss[2] = {work + 6 * ne, work + 7 * ne};
-    auto vec = [&](int set) {
-        CgcVec v;
-        v.x = x;
-        v.p = p;
-        v.u = u;
-        v.r_in = rs[set];
-        v.w_in = ws[set];
-        v.s_in = ss[set];
-        v.r_out = rs[set ^ 1];
-        v.w_out = ws[set ^ 1];
-        v.s_out = ss[set ^ 1];
-        v.dinv = dinv;
-        v.b = b;
-        return v;
-    };
-    UWG_CUDA(cudaMemsetAsync(scal, 0, 16 * sizeof(double), c.stream));
-    {
-        // INIT writes set 0 (its "out" set) for iteration 0 to read
-        CgcVec v = vec(1);
-        LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
-        launch_pdl(k_cgc_mf3<true>, mf.blocks, kMfX * kMfY, c.stream, mf.a3, Wc, v, scal, 0, 1);
-    }
-    double* hs = c.host_scalars;
-    UWG_CUDA(cudaMemcpyAsync(hs, scal, 16 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-    UWG_CUDA(cudaStreamSynchronize(c.stream));
-    check_launch("k_cgc_mf3 init");
-    const double r0 = std::sqrt(hs[12]);
-    if (!(r0 > 0.0)) return 0;
-    const int block = 12;
-    const void* key[8] = {Wc, dinv, x, work, scal, (const void*)(intptr_t)ne, (const void*)(intptr_t)sizeof(float),
-                          (const void*)(intptr_t)(m.dim + 64)};
-    Context::PcgGraph* pg = nullptr;
-    for (auto& cand : c.pcg_graphs)
-        if (std::equal(std::begin(key), std::end(key), std::begin(cand.key))) pg = &cand;
-    if (!pg) {
-        c.pcg_graphs.emplace_back();
-        pg = &c.pcg_graphs.back();
-        std::copy(std::begin(key), std::end(key), std::begin(pg->key));
-        cudaGraph_t graph;
-        UWG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
-        for (int k = 0; k < block; ++k)
-            launch_pdl(k_cgc_mf3<false>, mf.blocks, kMfX * kMfY, c.stream, mf.a3, Wc, vec(k & 1), scal, k,
-                       (int)(k == block - 1));
-        UWG_CUDA(cudaStreamEndCapture(c.stream, &graph));
-        UWG_CUDA(cudaGraphInstantiate(&pg->exec, graph, 0));
-        UWG_CUDA(cudaGraphDestroy(graph));
-    }
-    // algorithmic traffic of one iteration: r, w, s, Dinv, u, p, x read, r, w, s, u, p, x written
-    // per element, and the nodal weights of about one node per element
-    const double it_bytes = (double)ne * 4.0 * (7 + 6 + 3);
-    const double it_flops = (double)ne * 60.0;
-    int it = 0;
-    while (it < maxit) {
-        {
-            LaunchScope ls(c, UWGPU_KERNEL_SCHUR_PC);
-            UWG_CUDA(cudaGraphLaunch(pg->exec, c.stream));
-        }
-        note_work(c, UWGPU_KERNEL_SCHUR_PC, block * it_bytes, block * it_flops);
-        c.launches += block - 1;
-        it += block;
-        UWG_CUDA(cudaMemcpyAsync(hs, scal, 16 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-        UWG_CUDA(cudaStreamSynchronize(c.stream));
-        const double rn = std::sqrt(hs[10 + ((block - 1) & 1)]);   // r.r after the block's last iteration
-        if (!std::isfinite(rn)) throw Error(UWGPU_ERR_NAN, "NaN in the BFBt inner solve");
-        if (rn <= rtol * r0) break;
-    }
-    check_launch("gwg_cg32_cgc");
-    return it;
 }
 
 // Test and timing hook on the inner operator of the current fine velocity operator: W, the FP64

@@ -49,8 +49,6 @@ int gwg_cg_mg32(Context& c, const float* A, const float* dinv, const double* b, 
                 float* work, double* scal);
 int gwg_cg32_mf(Context& c, const float* Wc, const float* dinv, const double* b, float* x, double rtol, int maxit,
                 float* work, double* scal);
-int gwg_cg32_cgc(Context& c, const float* Wc, const float* dinv, const double* b, float* x, double rtol, int maxit,
-                 float* work, double* scal);
 void gwg_mf_weights(Context& c, const double* W, float* Wc);
 void op_wg32(Context& c, const float* p, const float* W, float* s);
 void op_gt32(Context& c, const float* s, float* q);
@@ -668,13 +666,12 @@ struct Bsscr {
     }
 
     // FP32 inner solve of G^T W G into bt32: multigrid-preconditioned on the FP32 stencil, or
-    // Jacobi on the FP32 stencil or with the matrix-free apply (in 3D as one-reduction CG)
+    // Jacobi on the FP32 stencil or with the matrix-free apply
     int inner32(const double* b) {
         int maxit = o.bfbt_max_it > 0 ? o.bfbt_max_it : 500;
         double rtol = o.bfbt_rtol > 0 ? o.bfbt_rtol : 1e-4;
         if (bfbt_mg) return gwg_cg_mg32(c, bA32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
         if (stencil32) return gwg_cg32(c, bA32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
-        if (c.mesh.dim == 3) return gwg_cg32_cgc(c, bwc32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
         return gwg_cg32_mf(c, bwc32.p, bd32.p, b, bt32.p, rtol, maxit, pz32.p, scal32.p);
     }
 
@@ -993,8 +990,8 @@ void Bsscr::run() {
         if (mixed) {
             for (auto* v : {&bw32, &bs32, &bX32}) v->ensure(nv);
             for (auto* v : {&bd32, &bt32, &bt2_32}) v->ensure(npres);
-            pz32.ensure(8 * npres);   // the one-reduction CG keeps 8 vectors
-            scal32.ensure(16);
+            pz32.ensure(4 * npres);
+            scal32.ensure(8);
             to_float(c, bw.p, bw32.p, nv);
             bwc32.ensure(nv);
             gwg_mf_weights(c, bw.p, bwc32.p);   // the matrix-free inner operator's folded weights
