@@ -35,6 +35,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Stokes solve s to 1e-6 rel. residual, mixed+learned vs FP64 GPU; particles/s"
+# FP64 FMA throughput of this part (an FMA-chain micro-benchmark on the GB300), TFLOP/s
+FP64_TFLOPS = 1.19
 UNIT = "particles/s"
 
 # DRAM bytes per stencil row measured by ncu for the FP64 / FP32 colour Gauss-Seidel kernel
@@ -377,6 +379,18 @@ def run_ours(args):
               "achieved_GB_per_s": d["bytes"] / (d["ms"] / 1e3) / 1e9 if d["ms"] > 0 else 0.0,
               "fp_TFLOP_per_s": d["flops"] / (d["ms"] / 1e3) / 1e12 if d["ms"] > 0 else 0.0,
               "note": FAMILY_NOTES.get(dom, "")}
+    # assembly (rheology + K_e, f_e, G_e, S_e; the DVC pass too when selected): points assembled per
+    # second, and the kernel's place against HBM and against the FP64 rate, which bounds it
+    a_ = prof.get("assembly", {})
+    assembly = None
+    if a_.get("ms", 0) > 0:
+        assembly = {"points_per_s": npts / (a_["ms"] / 1e3), "ms": a_["ms"],
+                    "GB_per_s": a_["bytes"] / (a_["ms"] / 1e3) / 1e9,
+                    "frac_hbm": a_["bytes"] / (a_["ms"] / 1e3) / 1e9 / peak,
+                    "fp64_TFLOP_per_s": a_["flops"] / (a_["ms"] / 1e3) / 1e12,
+                    "frac_fp64": a_["flops"] / (a_["ms"] / 1e3) / 1e12 / FP64_TFLOPS,
+                    "note": f"FP64 work (moment accumulation per point, moment contraction per element) is bound "
+                            f"by the {FP64_TFLOPS} TFLOP/s FP64 rate measured on this part, not by HBM"}
     kernels = {k: {"launches": v["launches"], "ms": v["ms"],
                    "GB_per_s": v["bytes"] / (v["ms"] / 1e3) / 1e9 if v["ms"] > 0 else None,
                    "TFLOP_per_s": v["flops"] / (v["ms"] / 1e3) / 1e12 if v["ms"] > 0 else None}
@@ -452,7 +466,8 @@ def run_ours(args):
                           "pc_inner_its": rep.pc_inner_its,
                           "stokes_solve_s": rep.t_solve_ms / 1e3, "setup_ms": rep.t_setup_ms,
                           "l2": "256 MB buffer written between timed steps", "parallelism": f"replicas x{world}"},
-               "roofline": roofline, "kernels": kernels, "operator": operator_rates, "cpu_baseline": cpu, "e2e": e2e,
+               "roofline": roofline, "assembly": assembly, "kernels": kernels, "operator": operator_rates,
+               "cpu_baseline": cpu, "e2e": e2e,
                "gpu_launches": int(launches), "clocks": clk, "comparison": comparison,
                "wall_s_timed": wall}
         print(json.dumps(out), flush=True)
