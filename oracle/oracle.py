@@ -81,6 +81,7 @@ def lib():
             L.uwr_assemble.argtypes = [P, C.c_int64, P, P, P, P, P, P, C.c_int32, P, P, P, P, P, P, P, P, C.c_int32]
             L.uwr_dvc_element.argtypes = [C.c_int, P, C.c_int32, P, P, P]
             L.uwr_dvc_weights.argtypes = [P, P, P, P, P, P, C.c_int32]
+            L.uwr_dvc_grid.argtypes = [C.c_int, P, P, P]
             L.uwr_assemble_gauss.argtypes = [P, C.c_int32, P, P, P, P]
             L.uwr_eqnum.restype = C.c_int64
             L.uwr_eqnum.argtypes = [P, P, P]
@@ -218,6 +219,16 @@ def dvc_element(dim, res, xi):
     if passes < 0:
         raise ValueError("DVC resolution out of range")
     return cxi, w, passes
+
+
+def dvc_grid(dim, res):
+    """(cell centres (nc, dim), face neighbours (nc, 2 dim): N, S, E, W[, U, D], -2 at the border)."""
+    r = np.ascontiguousarray(list(res) + [1] * (3 - len(res)), dtype=np.int32)
+    nc = int(np.prod(r[:dim]))
+    centre = np.zeros((nc, dim))
+    nbr = np.zeros((nc, 2 * dim), np.int32)
+    lib().uwr_dvc_grid(dim, _p(r), _p(centre), _p(nbr))
+    return centre, nbr
 
 
 def dvc_weights(m, res, offsets, xi, nthreads=0):

@@ -809,6 +809,34 @@ static void dvc_centres(int n, double* c) {
     }
 }
 
+/* face neighbours of cell c in the order N (y + 1), S (y - 1), E (x + 1), W (x - 1), U (z + 1),
+ * D (z - 1); -2 where the grid ends (_DVCWeights_ConstructGrid's links, :510-580) */
+static void dvc_neighbours(int c, int nx, int ny, int nz, int q[6]) {
+    const int x = c % nx, y = (c / nx) % ny, z = c / (nx * ny);
+    q[0] = y < ny - 1 ? c + nx : -2;
+    q[1] = y > 0 ? c - nx : -2;
+    q[2] = x < nx - 1 ? c + 1 : -2;
+    q[3] = x > 0 ? c - 1 : -2;
+    q[4] = z < nz - 1 ? c + nx * ny : -2;
+    q[5] = z > 0 ? c - nx * ny : -2;
+}
+
+void uwr_dvc_grid(int dim, const int32_t res[3], double* centre /* nc*dim */, int32_t* nbr /* nc*2dim */) {
+    const int nx = res[0], ny = res[1], nz = dim == 3 ? res[2] : 1;
+    double cen[3][64];
+    dvc_centres(nx, cen[0]);
+    dvc_centres(ny, cen[1]);
+    if (dim == 3) dvc_centres(nz, cen[2]);
+    for (int c = 0; c < nx * ny * nz; ++c) {
+        int q[6];
+        dvc_neighbours(c, nx, ny, nz, q);
+        for (int k = 0; k < 2 * dim; ++k) nbr[c * 2 * dim + k] = q[k];
+        centre[c * dim + 0] = cen[0][c % nx];
+        centre[c * dim + 1] = cen[1][(c / nx) % ny];
+        if (dim == 3) centre[c * dim + 2] = cen[2][c / (nx * ny)];
+    }
+}
+
 static double dvc_contest(int dim, const double* c0, const double* p1, const double* p2) {
     double t = (p1[0] + p2[0] - c0[0] - c0[0]) * (p1[0] - p2[0]) + (p1[1] + p2[1] - c0[1] - c0[1]) * (p1[1] - p2[1]);
     if (dim == 3) t = t + (p1[2] + p2[2] - c0[2] - c0[2]) * (p1[2] - p2[2]);
@@ -836,17 +864,10 @@ int uwr_dvc_element(int dim, const int32_t res[3], int32_t nump, const double* x
         int* B = bnd + (size_t)(p) * nc;                                                             \
         int nb = 0;                                                                                  \
         for (int t_ = 0; t_ < (ntook); ++t_) {                                                       \
-            const int c = took[t_];                                                                  \
-            const int x = c % nx, y = (c / nx) % ny, z = c / (nx * ny);                              \
-            int q[6], nq = 0;                                                                        \
-            if (y > 0) q[nq++] = c - nx;                                                             \
-            if (y < ny - 1) q[nq++] = c + nx;                                                        \
-            if (x < nx - 1) q[nq++] = c + 1;                                                         \
-            if (x > 0) q[nq++] = c - 1;                                                              \
-            if (z < nz - 1) q[nq++] = c + nx * ny;                                                   \
-            if (z > 0) q[nq++] = c - nx * ny;                                                        \
-            for (int k_ = 0; k_ < nq; ++k_)                                                          \
-                if (owner[q[k_]] != (p) && !mark[q[k_]]) {                                           \
+            int q[6];                                                                                \
+            dvc_neighbours(took[t_], nx, ny, nz, q);                                                 \
+            for (int k_ = 0; k_ < 6; ++k_)                                                           \
+                if (q[k_] >= 0 && owner[q[k_]] != (p) && !mark[q[k_]]) {                             \
                     mark[q[k_]] = 1;                                                                 \
                     B[nb++] = q[k_];                                                                 \
                 }                                                                                    \

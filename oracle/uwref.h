@@ -107,6 +107,9 @@ int uwr_assemble(const uwr_mesh* m, int64_t n, const uint32_t* offsets, const ui
  * points' discrete Voronoi regions) cxi[p*dim + d] and the weights w[p] (region volume in local
  * coordinates).  Returns the number of growth passes. */
 int uwr_dvc_element(int dim, const int32_t res[3], int32_t nump, const double* xi, double* cxi, double* w);
+/* The cell grid: centres (nc*dim, accumulated as the reference does) and face neighbours
+ * (nc*2*dim: N, S, E, W[, U, D], -2 where the grid ends). */
+void uwr_dvc_grid(int dim, const int32_t res[3], double* centre, int32_t* nbr);
 /* Every element of the mesh, points in slot order: xi and cxi are [slot][3] (z unused in 2D). */
 void uwr_dvc_weights(const uwr_mesh* m, const int32_t res[3], const uint32_t* offsets, const double* xi,
                      double* cxi, double* w, int32_t nthreads);

@@ -2,9 +2,11 @@
 
 Reads PICellerator/Weights/tests/DVCWeightsSuite.c (the ten 3D and ten 2D point coordinates that
 _DVCWeightsSuite_InitialiseParticleCoords / ...2D assign, on a 10 x 10 (x 10) grid over
-[-1, 1]^dim) and the expected centroids and weights the suite compares against
+[-1, 1]^dim), the expected centroids and weights the suite compares against
 (PICellerator/Weights/tests/expected/DVCWeightsSuite_testGetCentroids.txt, ...2D.txt, printed
-with six decimals), from the read-only reference tree, and writes tests/golden/dvc_golden.json.
+with six decimals) and the expected cell grids (links and centres,
+DVCWeightsSuite_testConstructGrid.txt, ...2D.txt), from the read-only reference tree, and writes
+tests/golden/dvc_golden.json.
 Run once in a checkout that has the reference tree; the fixture is committed.
 """
 import json
@@ -36,6 +38,18 @@ def expected(path, dim):
     return [[float(v) for v in c.split(",")][:dim] for c in cen], [float(v) for v in wts]
 
 
+def grid(path, dim):
+    """cell links (N, S, E, W[, U, D]) and centres of _DVCWeights_ConstructGrid{,2D} as the suite's
+    expected file prints them"""
+    txt = open(path).read()
+    keys = "NSEWUD"[:2 * dim]
+    pat = r"Values: \(" + ", ".join(k + r": (-?\d+)" for k in keys) + r"\)"
+    links = [[int(v) for v in m] for m in re.findall(pat, txt)]
+    cen = [[float(v) for v in c.split(",")] for c in re.findall(r"Coords: \(([^)]*)\)", txt)]
+    assert len(links) == len(cen)
+    return links, cen
+
+
 def main():
     src = open(SUITE).read()
     c3 = coords(src, "void _DVCWeightsSuite_InitialiseParticleCoords(", "pList")
@@ -49,6 +63,11 @@ def main():
                "centroids": cen3, "weights": w3},
         "2d": {"res": [10, 10], "xi": [list(p) for p in zip(c2["x"], c2["y"])], "centroids": cen2, "weights": w2},
     }
+    l3, g3 = grid(os.path.join(EXPECTED, "DVCWeightsSuite_testConstructGrid.txt"), 3)
+    l2, g2 = grid(os.path.join(EXPECTED, "DVCWeightsSuite_testConstructGrid2D.txt"), 2)
+    out["grid3d"] = {"res": [10, 10, 10], "links": l3, "centres": g3}
+    out["grid2d"] = {"res": [10, 10], "links": l2, "centres": g2}
+    assert len(l3) == 1000 and len(l2) == 100
     assert len(out["3d"]["xi"]) == len(cen3) == len(w3) == 10
     assert len(out["2d"]["xi"]) == len(cen2) == len(w2) == 10
     with open(OUT, "w") as f:

@@ -20,6 +20,16 @@ def test_dvc_matches_reference_known_answers(oracle, key, dim):
     assert passes > 1
 
 
+@pytest.mark.parametrize("key,dim", [("grid3d", 3), ("grid2d", 2)])
+def test_dvc_grid_matches_reference_construction(oracle, key, dim):
+    """Cell links and centres equal _DVCWeights_ConstructGrid{,2D}'s (the suite's expected grid
+    files: links exactly, centres to their six printed decimals)."""
+    g = json.load(open(GOLDEN))[key]
+    centre, nbr = oracle.dvc_grid(dim, g["res"])
+    assert np.array_equal(nbr, np.array(g["links"], dtype=np.int32))
+    assert np.abs(centre - np.array(g["centres"])).max() < 1e-6
+
+
 @pytest.mark.parametrize("dim,res", [(3, (10, 10, 10)), (2, (10, 10)), (3, (8, 6, 5)), (2, (32, 32))])
 def test_dvc_partition_invariants(oracle, dim, res):
     """The regions tile the element: weights sum to 2^dim, every weight is a whole number of
