@@ -148,6 +148,11 @@ typedef struct {
 typedef struct uwgpu_ctx uwgpu_ctx;
 
 /* Lifetime ------------------------------------------------------------------------------ */
+/* The GPU components create their context in their Build phase and free it in their Destroy
+ * phase (Stg_Component_Build / Stg_Component_Destroy, StGermain/Base/Automation/src/
+ * Stg_Component.c:228,339); the last error message is what they pass to Journal_Firewall
+ * (StGermain/Base/IO/src/Journal.c:519).  uwgpu_abi_version and uwgpu_synchronize have no
+ * reference counterpart. */
 int uwgpu_abi_version(void);
 /* Creates a context on `device` with its own stream. */
 int uwgpu_create(int32_t device, uwgpu_ctx** out);
@@ -207,7 +212,8 @@ int uwgpu_bin_and_map(uwgpu_ctx* ctx, uint32_t* perm, uint32_t* offsets, double*
  * SwarmAdvector.c:375-382). */
 int uwgpu_advect_particles(uwgpu_ctx* ctx, double dt, int32_t order, int32_t allow_first_order_fallback,
                            uint32_t* fell_back, uint32_t* left_mesh);
-/* Current particle coordinates to host arrays (n each; z ignored in 2D). */
+/* Current particle coordinates to host arrays (n each; z ignored in 2D): the host copy of
+ * GlobalParticle.coord (StgDomain/Swarm/src/StandardParticle.h:77) for output and analysis. */
 int uwgpu_particles_download(uwgpu_ctx* ctx, double* x, double* y, double* z);
 
 /* Integration weights of the next assemblies (the WeightsCalculator of the integration swarm).
@@ -220,7 +226,9 @@ int uwgpu_particles_download(uwgpu_ctx* ctx, double* x, double* y, double* z);
 enum { UWGPU_WEIGHTS_CONSTANT = 0, UWGPU_WEIGHTS_DVC = 1 };
 int uwgpu_weights_set(uwgpu_ctx* ctx, int32_t kind, const int32_t res[3]);
 /* Local coordinates ([slot][3], z = 0 in 2D) and weights (slot order) of the integration points
- * the last assembly used.  Either output may be NULL. */
+ * the last assembly used: IntegrationPoint.xi and .weight (StgDomain/Swarm/src/
+ * IntegrationPoint.h:47, StandardParticle.h:70) for CPU readers of the integration swarm.
+ * Either output may be NULL. */
 int uwgpu_integration_points(uwgpu_ctx* ctx, double* xi, double* w);
 
 /* Element assembly of every element: replaces the StiffnessMatrix assemble entry point
@@ -238,7 +246,9 @@ int uwgpu_assemble(uwgpu_ctx* ctx);
  * fe, Ge: count*nd; Se: count.  Any output may be NULL. */
 int uwgpu_get_element_matrices(uwgpu_ctx* ctx, int64_t first, int64_t count, double* Ke,
                                double* fe, double* Ge, double* Se);
-/* Viscosity evaluated at every integration slot by the last assembly (n, slot order). */
+/* Viscosity evaluated at every integration slot by the last assembly (n, slot order): the
+ * isotropic viscosity the constitutive matrix holds per point (ConstitutiveMatrixCartesian.c:332,
+ * matrixData[2][2] in 2D) for output and tests. */
 int uwgpu_get_point_viscosity(uwgpu_ctx* ctx, double* eta);
 
 /* Velocity-block operator y = K x on nodal vectors (nnode*dim, fixed dofs act as identity):
@@ -278,6 +288,7 @@ enum { UWGPU_KERNEL_ASSEMBLY = 0, UWGPU_KERNEL_APPLY = 1, UWGPU_KERNEL_SMOOTH = 
        UWGPU_KERNEL_VECTOR = 5 /* Krylov vector work, reductions, G and G^T */,
        UWGPU_KERNEL_TRANSFER = 6 /* restriction, prolongation, coarsest solve */,
        UWGPU_KERNEL_LEARNED = 7 /* U-Net preconditioner: forward, backward, Adam */, UWGPU_KERNEL_COUNT = 8 };
+/* (Measurement hooks, no reference counterpart.) */
 int uwgpu_profile_enable(uwgpu_ctx* ctx, int32_t on);
 int uwgpu_profile_read(uwgpu_ctx* ctx, int32_t which, int64_t* launches, double* ms);
 /* Algorithmic work of the profiled launches of family `which`: bytes the kernels must move
