@@ -7,7 +7,11 @@
 // about 75 FP64 instructions per node and 50 per element, which on this part (FP64 at 1/58 of
 // the FP32 rate) makes every CG iteration FP64-issue bound.  The stencil is built once per solve
 // (A[q][e], entry-major, q = neighbour offset) and an iteration is then 27 FMAs per element
-// with coalesced stencil reads; the 57 MB FP64 stencil of a 64^3 mesh can stay in L2.
+// with coalesced stencil reads; the 57 MB FP64 stencil of a 64^3 mesh can stay in L2.  In FP32
+// the matrix-free chain is cheap, so the mixed form applies G^T W G matrix-free (k_cg_mf3_dir,
+// k_cg_mf2_dir below) once its FP32 stencil would no longer fit in L2.
+// Further down: the aggregation multigrid option for the inner solves, and the test and timing
+// hooks on the inner operator.
 //
 // CG state lives in device memory and an iteration k is two kernels:
 //   k_cg_update:   alpha = rz_k / pq_k; x += alpha p; r -= alpha q; z = Dinv r; rz_{k+1}, rr
@@ -16,7 +20,9 @@
 // The scalars are buffered so that no kernel clears a slot another block may still read:
 //   scal[0..2] = rz (k mod 3)   scal[3..4] = pq (k mod 2)   scal[5..6] = rr (k mod 2)   scal[7] = r0.r0
 // Twelve iterations (so both patterns repeat) are captured once as a CUDA graph and replayed; the
-// host reads the residual norm after each replay.
+// host reads the residual norm after each replay.  The two kernels are launched with programmatic
+// dependent launch (pdl_wait / pdl_trigger), so each one's blocks are resident when the previous
+// one ends.
 #include <algorithm>
 #include <cmath>
 #include <iterator>
