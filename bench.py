@@ -39,10 +39,6 @@ METRIC = "Stokes solve s to 1e-6 rel. residual, mixed+learned vs FP64 GPU; parti
 FP64_TFLOPS = 1.19
 UNIT = "particles/s"
 
-# DRAM bytes per stencil row measured by ncu for the FP64 / FP32 colour Gauss-Seidel kernel
-# (profiles/gs_colour_spheres.md); scaled by the rows a launch relaxes.
-NCU_TRAFFIC_PER_ROW = {"fp64": None, "fp32": None}
-
 
 def parse():
     ap = argparse.ArgumentParser()

@@ -16,8 +16,10 @@
 //
 // Host code cannot use the array's name as a device address (on the host it names a stand-in
 // object); its device address is looked up once per device with cudaGetSymbolAddress, on the
-// first call made while that device is current.  That first call should therefore come before
-// any stream capture.
+// first call made while that device is current.
+//
+// Every call ends by copying the outside-point count to the host and synchronising its stream,
+// so no call can be made while that stream is being captured into a CUDA graph.
 #include <mutex>
 
 #include "internal.cuh"
@@ -84,38 +86,44 @@ __global__ void k_na_locate(int64_t n, const double* __restrict__ x, const doubl
     atomicAdd(&s[kOffCount + e], 1u);
 }
 
-// Exclusive scan of the counts into offsets[0..ne] by one block (ne <= kMaxElements).
+// Exclusive scan of the counts into offsets[0..ne] by one block (ne <= kMaxElements): the counts
+// are read in tiles of blockDim.x consecutive words (one per thread, coalesced), each tile is
+// scanned in the block and carried into the next.
 __global__ void k_na_scan(int64_t ne, const uint32_t* __restrict__ s, uint32_t* __restrict__ offsets) {
     __shared__ uint32_t warp_tot[32];
-    const int64_t per = (ne + blockDim.x - 1) / blockDim.x;
-    const int64_t beg = threadIdx.x * per;
-    uint32_t sum = 0;
-    for (int64_t i = beg; i < beg + per && i < ne; ++i) sum += s[kOffCount + i];
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t incl = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-    }
-    if (lane == 31) warp_tot[warp] = incl;
+    __shared__ uint32_t carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    if (threadIdx.x == 0) carry = 0u;
     __syncthreads();
-    if (warp == 0) {
-        uint32_t w = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0u;
+    for (int64_t t = 0; t < ne; t += blockDim.x) {
+        const int64_t i = t + threadIdx.x;
+        const uint32_t v = i < ne ? s[kOffCount + i] : 0u;
+        uint32_t incl = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t v = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += v;
+            uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
         }
-        warp_tot[lane] = w;
+        if (lane == 31) warp_tot[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = lane < nwarps ? warp_tot[lane] : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t u = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += u;
+            }
+            warp_tot[lane] = w;
+        }
+        __syncthreads();
+        const uint32_t base = carry;
+        const uint32_t excl = base + (warp ? warp_tot[warp - 1] : 0u) + incl - v;
+        if (i < ne) offsets[i] = excl;
+        __syncthreads();   // every thread has read carry and warp_tot
+        if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+        __syncthreads();
     }
-    __syncthreads();
-    uint32_t run = (warp ? warp_tot[warp - 1] : 0u) + incl - sum;
-    for (int64_t i = beg; i < beg + per && i < ne; ++i) {
-        offsets[i] = run;
-        run += s[kOffCount + i];
-    }
-    if (threadIdx.x == blockDim.x - 1) offsets[ne] = run;
+    if (threadIdx.x == 0) offsets[ne] = carry;
 }
 
 __global__ void k_na_scatter(int64_t n, const uint32_t* __restrict__ offsets, uint32_t* __restrict__ s) {
@@ -127,8 +135,23 @@ __global__ void k_na_scatter(int64_t n, const uint32_t* __restrict__ offsets, ui
     s[kOffTmp + slot] = (uint32_t)p;
 }
 
+// Local coordinate of point v in element e along every axis, written to slot `slot` (SoA [d][slot]).
+template <int DIM>
+__device__ __forceinline__ void na_map_point(const int64_t idx[3], const MeshP& mp, uint32_t v, uint32_t slot, int64_t n,
+                                             const double* __restrict__ x, const double* __restrict__ y,
+                                             const double* __restrict__ z, double* __restrict__ xi) {
+    double pt[3] = {x[v], y[v], DIM == 3 ? z[v] : 0.0};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        double x0 = uwg::node_coord_1d(idx[d], mp.nel[d], mp.min[d], mp.max[d]);
+        double h = uwg::node_coord_1d(idx[d] + 1, mp.nel[d], mp.min[d], mp.max[d]) - x0;
+        xi[(int64_t)d * n + slot] = (2.0 * (pt[d] - x0) - h) / h;
+    }
+}
+
 // One warp per element: rank the element's points by index (the reference's append order),
-// write the permutation and the local coordinates (SoA [d][slot]).
+// write the permutation and the local coordinates.  Elements with at most 32 points rank in
+// registers (one point per lane, exchanged by shuffles); fuller elements re-read their run.
 template <int DIM>
 __global__ void k_na_sort_map(int64_t ne, int64_t n, MeshP mp, const uint32_t* __restrict__ offsets,
                               const uint32_t* __restrict__ s, const double* __restrict__ x,
@@ -139,21 +162,23 @@ __global__ void k_na_sort_map(int64_t ne, int64_t n, MeshP mp, const uint32_t* _
     if (e >= ne) return;
     uint32_t beg = offsets[e], cnt = offsets[e + 1] - beg;
     int64_t idx[3] = {e % mp.nel[0], (e / mp.nel[0]) % mp.nel[1], DIM == 3 ? e / ((int64_t)mp.nel[0] * mp.nel[1]) : 0};
-    for (uint32_t i = lane; i < ((cnt + 31u) & ~31u); i += 32) {
-        uint32_t v = i < cnt ? s[kOffTmp + beg + i] : 0xffffffffu;
+    if (cnt <= 32u) {
+        uint32_t v = lane < (int)cnt ? s[kOffTmp + beg + lane] : 0xffffffffu;
+        uint32_t rank = 0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) rank += (__shfl_sync(0xffffffffu, v, j) < v) ? 1u : 0u;
+        if (lane < (int)cnt) {
+            perm[beg + rank] = v;
+            na_map_point<DIM>(idx, mp, v, beg + rank, n, x, y, z, xi);
+        }
+        return;
+    }
+    for (uint32_t i = lane; i < cnt; i += 32) {
+        uint32_t v = s[kOffTmp + beg + i];
         uint32_t rank = 0;
         for (uint32_t j = 0; j < cnt; ++j) rank += (s[kOffTmp + beg + j] < v) ? 1u : 0u;
-        if (i < cnt) {
-            uint32_t slot = beg + rank;
-            perm[slot] = v;
-            double pt[3] = {x[v], y[v], DIM == 3 ? z[v] : 0.0};
-#pragma unroll
-            for (int d = 0; d < DIM; ++d) {
-                double x0 = uwg::node_coord_1d(idx[d], mp.nel[d], mp.min[d], mp.max[d]);
-                double h = uwg::node_coord_1d(idx[d] + 1, mp.nel[d], mp.min[d], mp.max[d]) - x0;
-                xi[(int64_t)d * n + slot] = (2.0 * (pt[d] - x0) - h) / h;
-            }
-        }
+        perm[beg + rank] = v;
+        na_map_point<DIM>(idx, mp, v, beg + rank, n, x, y, z, xi);
     }
 }
 
@@ -165,6 +190,12 @@ static uint32_t* scratch_address(int dev) {
         g_addr[dev] = (uint32_t*)ptr;
     }
     return g_addr[dev];
+}
+
+// Launches `fn` and returns the launch's own status (cudaLaunchKernel reports a bad
+// configuration of this launch rather than an error left pending by earlier, unrelated work).
+static cudaError_t launch(const void* fn, unsigned blocks, unsigned threads, cudaStream_t st, void** args) {
+    return cudaLaunchKernel(fn, dim3(blocks), dim3(threads), args, 0, st);
 }
 
 }  // namespace uwg_noalloc
@@ -183,6 +214,8 @@ extern "C" int uwgpu_bin_and_map_noalloc(int32_t dim, const int32_t nel[3], cons
         mp.min[d] = min[d];
         mp.max[d] = max[d];
         if (d < dim && (nel[d] < 1 || !(max[d] > min[d]))) return UWGPU_ERR_ARGUMENT;
+        // checked one factor at a time, so that the product cannot overflow
+        if (mp.nel[d] > kMaxElements / ne) return UWGPU_ERR_TOO_LARGE;
         ne *= mp.nel[d];
     }
     if (n > kMaxPoints || ne > kMaxElements) return UWGPU_ERR_TOO_LARGE;
@@ -195,18 +228,22 @@ extern "C" int uwgpu_bin_and_map_noalloc(int32_t dim, const int32_t nel[3], cons
     if (cudaMemsetAsync(s + kOffCount, 0, (size_t)(kOffFlag + 1 - kOffCount) * sizeof(uint32_t), st) != cudaSuccess)
         return UWGPU_ERR_CUDA;
     if (n > 0) {
-        unsigned b = (unsigned)((n + 255) / 256);
-        if (dim == 3) k_na_locate<3><<<b, 256, 0, st>>>(n, x, y, z, mp, s);
-        else k_na_locate<2><<<b, 256, 0, st>>>(n, x, y, z, mp, s);
+        void* args[] = {&n, (void*)&x, (void*)&y, (void*)&z, &mp, &s};
+        const void* fn = dim == 3 ? (const void*)k_na_locate<3> : (const void*)k_na_locate<2>;
+        if (launch(fn, (unsigned)((n + 255) / 256), 256, st, args) != cudaSuccess) return UWGPU_ERR_CUDA;
     }
-    k_na_scan<<<1, 1024, 0, st>>>(ne, s, offsets);
+    {
+        void* args[] = {&ne, &s, &offsets};
+        if (launch((const void*)k_na_scan, 1, 1024, st, args) != cudaSuccess) return UWGPU_ERR_CUDA;
+    }
     if (n > 0) {
-        k_na_scatter<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, offsets, s);
-        unsigned b = (unsigned)((ne * 32 + 255) / 256);
-        if (dim == 3) k_na_sort_map<3><<<b, 256, 0, st>>>(ne, n, mp, offsets, s, x, y, z, perm, xi);
-        else k_na_sort_map<2><<<b, 256, 0, st>>>(ne, n, mp, offsets, s, x, y, z, perm, xi);
+        void* sargs[] = {&n, &offsets, &s};
+        if (launch((const void*)k_na_scatter, (unsigned)((n + 255) / 256), 256, st, sargs) != cudaSuccess)
+            return UWGPU_ERR_CUDA;
+        void* margs[] = {&ne, &n, &mp, &offsets, &s, (void*)&x, (void*)&y, (void*)&z, &perm, &xi};
+        const void* fn = dim == 3 ? (const void*)k_na_sort_map<3> : (const void*)k_na_sort_map<2>;
+        if (launch(fn, (unsigned)((ne * 32 + 255) / 256), 256, st, margs) != cudaSuccess) return UWGPU_ERR_CUDA;
     }
-    if (cudaGetLastError() != cudaSuccess) return UWGPU_ERR_CUDA;
     uint32_t out = 0;
     if (cudaMemcpyAsync(&out, s + kOffFlag, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)

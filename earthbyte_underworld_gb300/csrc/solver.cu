@@ -1143,7 +1143,10 @@ int learned_generate(Context& c, const uwgpu_solve_opts& o, int nsamples, uint64
 namespace uwg {
 
 // SystemLinearEquations_NonLinearExecute (SystemLinearEquations.c:750-935): the residual is the
-// relative change of the velocity solution vector between successive solves.
+// relative change of the velocity solution vector between successive solves.  With tol > 0, a
+// loop that ends at max_iterations without reaching it reports UWGPU_ERR_NOT_CONVERGED (the
+// reference's "Failed to converge" branch, SystemLinearEquations.c:908-914); tol <= 0 runs
+// exactly max_iterations solves.
 void solve_picard(Context& c, const uwgpu_solve_opts& o, double tol, int maxit, int minit, uwgpu_report& rep,
                   int& iterations, double& residual) {
     UWG_REQUIRE(c.mapped, UWGPU_ERR_STATE, "Picard iteration requested before bin_and_map");
@@ -1154,6 +1157,7 @@ void solve_picard(Context& c, const uwgpu_solve_opts& o, double tol, int maxit, 
     prev.ensure((size_t)nv);
     residual = 0.0;
     iterations = 0;
+    bool converged = false;
     uwgpu_report r;
     for (int it = 0; it < maxit; ++it) {
         bool have_prev = c.has_solution;
@@ -1184,7 +1188,14 @@ void solve_picard(Context& c, const uwgpu_solve_opts& o, double tol, int maxit, 
             rep.status = UWGPU_ERR_NAN;
             return;
         }
-        if (residual < tol && iterations >= minit) break;
+        if (residual < tol && iterations >= minit) {
+            converged = true;
+            break;
+        }
+    }
+    if (tol > 0.0 && !converged) {
+        rep.status = UWGPU_ERR_NOT_CONVERGED;
+        rep.converged = 0;
     }
 }
 

@@ -8,8 +8,8 @@
  *       ForceVector assemble entry points
  *   ExecuteSolver -> StokesBlockKSPInterface / BSSCR   -> uwgpu_solve_bsscr
  * and reads its parameters the way Underworld's main reads command-line overrides
- * (`--key=value`, Underworld/src/main.c:77-79).  The three gpu_* functions below are what the
- * StGermain component shim of INTEGRATION.md calls; main() runs them on a generated
+ * (`--key=value`, Underworld/src/main.c:77-79).  The three gpu_* functions below are what a
+ * StGermain component shim (the GPU mapper, assembly hook and SLE solver) calls; main() runs them on a generated
  * Rayleigh-Taylor style layout so that the binding can be exercised without StGermain.
  *
  * Build: earthbyte_underworld_gb300/build.py (gcc -O2 ... -luwgpu -lm, rpath next to libuwgpu.so)

@@ -314,18 +314,23 @@ class Context:
             self._check(rc)
         return u, p, rep
 
-    def solve_picard(self, opts: SolveOpts | None = None, tolerance=1e-4, max_iterations=20, min_iterations=1):
+    def solve_picard(self, opts: SolveOpts | None = None, tolerance=1e-4, max_iterations=20, min_iterations=1,
+                     check=True):
         """Picard iteration (re-assemble with the current solution, re-solve) until the relative
-        velocity change is below `tolerance`.  Returns u, p, report, iterations, residual."""
+        velocity change is below `tolerance` (tolerance <= 0: exactly max_iterations solves).
+        Returns u, p, report, iterations, residual; with check=False a status other than OK is
+        left in report.status instead of raised."""
         opts = opts or default_opts()
         rep = Report()
         u = np.zeros((self.nnodes, self.dim))
         p = np.zeros(self.nelements)
         its = C.c_int32()
         res = C.c_double()
-        self._check(self._L.uwgpu_solve_picard(self._h, C.byref(opts), float(tolerance), int(max_iterations),
-                                               int(min_iterations), _ptr(u), _ptr(p), C.byref(rep), C.byref(its),
-                                               C.byref(res)))
+        rc = self._L.uwgpu_solve_picard(self._h, C.byref(opts), float(tolerance), int(max_iterations),
+                                        int(min_iterations), _ptr(u), _ptr(p), C.byref(rep), C.byref(its),
+                                        C.byref(res))
+        if check:
+            self._check(rc)
         return u, p, rep, its.value, res.value
 
     def synchronize(self):

@@ -218,11 +218,44 @@ def layers(nel=(96, 96, 96), ppc=40, seed=5, nbumps=20, cohesion_scale=1.0):
                 temperature=T, mg_levels=4)
 
 
+def driven_walls(dim, nel, kind="lid"):
+    """Non-zero Dirichlet conditions of two driven models, as (fixed mask, values), node-major
+    (node * dim + component):
+      lid        free-slip walls, and on the top wall (y = 1 in 2D, z = 1 in 3D) the x velocity
+                 fixed to 4 x (1 - x) (zero at the corners, so no net flux through any wall)
+      extension  x walls pulled apart (u_x = -0.5 at x = 0, +0.5 at x = 1), the other side walls
+                 and the bottom free-slip, the top open"""
+    nx, ny = nel[0] + 1, nel[1] + 1
+    nz = nel[2] + 1 if dim == 3 else 1
+    idx = np.arange(nx * ny * nz)
+    i, j, k = idx % nx, (idx // nx) % ny, idx // (nx * ny)
+    X = _node_coord(i, nel[0])
+    fixed = np.zeros((idx.size, dim), np.uint8)
+    val = np.zeros((idx.size, dim))
+    top = (j == ny - 1) if dim == 2 else (k == nz - 1)
+    if kind == "lid":
+        fixed[:] = U.free_slip_mask(dim, nel).reshape(-1, dim)
+        fixed[top, 0] = 1
+        val[top, 0] = 4.0 * X[top] * (1.0 - X[top])
+    elif kind == "extension":
+        fixed[(i == 0) | (i == nx - 1), 0] = 1
+        val[i == 0, 0] = -0.5
+        val[i == nx - 1, 0] = 0.5
+        if dim == 2:
+            fixed[j == 0, 1] = 1
+        else:
+            fixed[(j == 0) | (j == ny - 1), 1] = 1
+            fixed[k == 0, 2] = 1
+    else:
+        raise ValueError(kind)
+    return fixed.reshape(-1), val.reshape(-1)
+
+
 def setup_context(ctx: U.Context, w: dict):
     """Load a workload into a device context (mesh, BCs, materials, fields, points)."""
     dim = w["dim"]
     ctx.mesh_q1(dim, w["nel"])
-    ctx.bc_set(w["fixed"])
+    ctx.bc_set(w["fixed"], w.get("bcval"))
     ctx.materials_set(w["materials"])
     ctx.fields_set(w.get("temperature"), w.get("gravity", 0.0), w.get("vert_axis", dim - 1))
     ctx.particles_upload(w["x"], w["y"], w["z"], w["material"], w.get("eta"), w.get("rho"))

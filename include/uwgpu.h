@@ -271,7 +271,10 @@ int uwgpu_solve_bsscr(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, double* u, d
  * dependent laws; yielding starts after the first solve, YieldRheology.c:210-212) and solves again,
  * until ||u_k - u_(k-1)|| / ||u_k|| < tolerance (after at least min_iterations) or max_iterations
  * solves.  Requires uwgpu_bin_and_map first.  *iterations and *residual (optional) report the
- * solves done and the last relative change; u, p as in uwgpu_solve_bsscr. */
+ * solves done and the last relative change; u, p as in uwgpu_solve_bsscr.  With tolerance > 0,
+ * reaching max_iterations without meeting it returns UWGPU_ERR_NOT_CONVERGED (the reference's
+ * "Failed to converge", SystemLinearEquations.c:908-914); tolerance <= 0 runs exactly
+ * max_iterations solves. */
 int uwgpu_solve_picard(uwgpu_ctx* ctx, const uwgpu_solve_opts* opts, double tolerance, int32_t max_iterations,
                        int32_t min_iterations, double* u, double* p, uwgpu_report* report, int32_t* iterations,
                        double* residual);
@@ -332,10 +335,11 @@ int uwgpu_time_bfbt_apply(uwgpu_ctx* ctx, int32_t form, int32_t iterations, doub
  * every device loading the library keeps until the process exits.  Limits: at most
  * UWGPU_NOALLOC_MAX_POINTS points and UWGPU_NOALLOC_MAX_ELEMENTS elements, else
  * UWGPU_ERR_TOO_LARGE.  Results equal uwgpu_bin_and_map's.  The first call on a device looks up
- * the array's device address (make it before any stream capture).  Calls share the array: calls
- * whose GPU work overlaps race, so order them (e.g. one stream).  Runs on `stream` (NULL: the
- * default stream) and synchronises it; *outside (optional, host) receives the number of points
- * outside the mesh, reported as UWGPU_ERR_DOMAIN. */
+ * the array's device address.  Calls share the array: calls whose GPU work overlaps race, so
+ * order them (e.g. one stream).  Runs on `stream` (NULL: the default stream) and synchronises it
+ * to read the outside-point count, so it cannot be called while that stream is being captured;
+ * *outside (optional, host) receives the number of points outside the mesh, reported as
+ * UWGPU_ERR_DOMAIN. */
 #define UWGPU_NOALLOC_MAX_POINTS (1 << 20)
 #define UWGPU_NOALLOC_MAX_ELEMENTS (1 << 17)
 int uwgpu_bin_and_map_noalloc(int32_t dim, const int32_t nel[3], const double min[3], const double max[3],

@@ -79,6 +79,8 @@ def lib():
             L.uwr_map.argtypes = [P, C.c_int64, P, P, P, P, P, C.c_int32]
             L.uwr_random_layout.argtypes = [P, C.c_int32, C.c_uint32, P]
             L.uwr_assemble.argtypes = [P, C.c_int64, P, P, P, P, P, P, C.c_int32, P, P, P, P, P, P, P, P, C.c_int32]
+            L.uwr_assemble_range.argtypes = [P, C.c_int64, C.c_int64, C.c_int64, P, P, P, P, P, P, C.c_int32, P, P,
+                                             P, P, P, P, P, P, C.c_int32]
             L.uwr_dvc_element.argtypes = [C.c_int, P, C.c_int32, P, P, P]
             L.uwr_dvc_weights.argtypes = [P, P, P, P, P, P, C.c_int32]
             L.uwr_dvc_grid.argtypes = [C.c_int, P, P, P]
@@ -90,6 +92,7 @@ def lib():
             L.uwr_csr_fill.argtypes = [P, P, C.c_int64, P, P, P, P, C.c_int32]
             L.uwr_csr_spmv.argtypes = [C.c_int64, P, P, P, P, P, C.c_int32]
             L.uwr_solve_bsscr.argtypes = [P, P, P, P, P, P, P, P, P, P]
+            L.uwr_solve_bsscr_bc.argtypes = [P, P, P, P, P, P, P, P, P, P, P]
             L.uwr_node_coords.argtypes = [P, P]
             L.uwr_global_to_local.argtypes = [P, C.c_int64, P, P]
             _lib = L
@@ -208,6 +211,28 @@ def assemble(m, offsets, perm, xi, material, mats, fields, point_eta=None, point
     return Ke, fe, Ge, Se, eta
 
 
+def assemble_range(m, first, count, offsets, perm, xi, material, mats, fields, point_eta=None, point_rho=None,
+                   nthreads=0):
+    """Element matrices of elements [first, first + count) only (points in slot order, as in
+    assemble): returns Ke (count, nd, nd), fe, Ge (count, nd), Se (count,)."""
+    dim = m.dim
+    nd = (8 if dim == 3 else 4) * dim
+    Ke = np.zeros((count, nd, nd))
+    fe = np.zeros((count, nd))
+    Ge = np.zeros((count, nd))
+    Se = np.zeros(count)
+    material = None if material is None else np.ascontiguousarray(material, dtype=np.int32)
+    point_eta = None if point_eta is None else np.ascontiguousarray(point_eta, dtype=np.float64)
+    point_rho = None if point_rho is None else np.ascontiguousarray(point_rho, dtype=np.float64)
+    arr = materials_array(mats)
+    rc = lib().uwr_assemble_range(C.byref(m), int(first), int(count), perm.shape[0], _p(offsets), _p(perm),
+                                  _p(np.ascontiguousarray(xi)), _p(material), _p(point_eta), _p(point_rho), len(mats),
+                                  arr, C.byref(fields), _p(Ke), _p(fe), _p(Ge), _p(Se), None, None, nthreads)
+    if rc != 0:
+        raise RuntimeError(f"oracle assembly of a range failed ({rc})")
+    return Ke, fe, Ge, Se
+
+
 def dvc_element(dim, res, xi):
     """Discrete Voronoi weights of one element: xi (nump, dim) local coordinates -> (centroids
     (nump, dim), weights (nump,), growth passes)."""
@@ -284,7 +309,9 @@ def csr_spmv(rowptr, cols, vals, x, nthreads=0):
 
 def solve_bsscr(m, fixed, Ke, Ge, fe, Se, mg_levels=3, smooth=2, schur_type=1, schur_pc=0,
                 scr_rtol=1e-10, a11_rtol=1e-12, back_rtol=1e-12, restart=30, max_outer=500,
-                max_inner=2000, remove_const_p=True, nthreads=0, bfbt_rtol=1e-4, bfbt_max_it=500):
+                max_inner=2000, remove_const_p=True, nthreads=0, bfbt_rtol=1e-4, bfbt_max_it=500, bcval=None):
+    """BSSCR solve; bcval (nn*dim, read where fixed) gives non-zero Dirichlet values, lifted into
+    the right-hand sides as the reference's assembly does (None: homogeneous conditions)."""
     o = SolveOpts(mg_levels, smooth, smooth, schur_type, schur_pc, restart, max_outer, max_inner,
                   scr_rtol, a11_rtol, back_rtol, int(remove_const_p), nthreads, bfbt_rtol, bfbt_max_it, 0)
     nn = num_nodes(m)
@@ -293,9 +320,10 @@ def solve_bsscr(m, fixed, Ke, Ge, fe, Se, mg_levels=3, smooth=2, schur_type=1, s
     p = np.zeros(E)
     rep = Report()
     fx = np.ascontiguousarray(fixed, dtype=np.uint8)
-    rc = lib().uwr_solve_bsscr(C.byref(m), _p(fx), _p(np.ascontiguousarray(Ke)), _p(np.ascontiguousarray(Ge)),
-                               _p(np.ascontiguousarray(fe)), _p(np.ascontiguousarray(Se)), C.byref(o),
-                               _p(u), _p(p), C.byref(rep))
+    bv = None if bcval is None else np.ascontiguousarray(bcval, dtype=np.float64).reshape(-1)
+    rc = lib().uwr_solve_bsscr_bc(C.byref(m), _p(fx), _p(bv), _p(np.ascontiguousarray(Ke)),
+                                  _p(np.ascontiguousarray(Ge)), _p(np.ascontiguousarray(fe)),
+                                  _p(np.ascontiguousarray(Se)), C.byref(o), _p(u), _p(p), C.byref(rep))
     if rc != 0:
         raise RuntimeError("oracle BSSCR setup failed (coarse factorisation)")
     return u, p, rep

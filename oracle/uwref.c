@@ -721,15 +721,29 @@ int uwr_assemble(const uwr_mesh* m, int64_t n, const uint32_t* offsets, const ui
                  const double* point_rho, int32_t nmat, const uwr_material* mats,
                  const uwr_fields* f, double* Ke, double* fe, double* Ge, double* Se,
                  double* eta_out, const double* slot_weight, int32_t nthreads) {
+    return uwr_assemble_range(m, 0, uwr_num_elements(m), n, offsets, perm, xi, material, point_eta, point_rho,
+                              nmat, mats, f, Ke, fe, Ge, Se, eta_out, slot_weight, nthreads);
+}
+
+/* uwr_assemble restricted to elements [first, first + count): outputs Ke, fe, Ge, Se are indexed
+ * from `first` (element first + i at position i); eta_out stays indexed by slot.  Lets a caller
+ * check a large mesh chunk by chunk with bounded memory. */
+int uwr_assemble_range(const uwr_mesh* m, int64_t first, int64_t count, int64_t n, const uint32_t* offsets,
+                       const uint32_t* perm, const double* xi, const int32_t* material, const double* point_eta,
+                       const double* point_rho, int32_t nmat, const uwr_material* mats,
+                       const uwr_fields* f, double* Ke, double* fe, double* Ge, double* Se,
+                       double* eta_out, const double* slot_weight, int32_t nthreads) {
     (void)n;
     set_threads(nthreads);
     int dim = m->dim, nen = (dim == 3) ? 8 : 4, nd = nen * dim;
     int64_t E = uwr_num_elements(m);
+    if (first < 0 || count < 0 || first + count > E) return -2;
     /* WeightsCalculator.c:83 cellLocalVolume = 2^dim; ConstantWeights.c:180-189 */
     const double cellVolume = pow(2.0, (double)dim);
     int bad = 0;
 #pragma omp parallel for schedule(dynamic, 64) reduction(| : bad)
-    for (int64_t e = 0; e < E; ++e) {
+    for (int64_t e = first; e < first + count; ++e) {
+        const int64_t eo = e - first;   /* output position */
         int64_t inc[8];
         uwr_element_nodes(m, e, inc);
         rheo_point rp;
@@ -738,7 +752,7 @@ int uwr_assemble(const uwr_mesh* m, int64_t n, const uint32_t* offsets, const ui
         rp.e = e;
         rp.inc = inc;
         element_node_xyz(m, e, rp.nodes);
-        double* K = Ke ? Ke + e * nd * nd : NULL;
+        double* K = Ke ? Ke + eo * nd * nd : NULL;
         double Kloc[576];
         if (!K) K = Kloc;
         memset(K, 0, sizeof(double) * nd * nd);
@@ -773,13 +787,13 @@ int uwr_assemble(const uwr_mesh* m, int64_t n, const uint32_t* offsets, const ui
         }
         double G[24];
         uwr_gauss_G(m, e, G);
-        if (fe) memcpy(fe + e * nd, floc, sizeof(double) * nd);
-        if (Ge) memcpy(Ge + e * nd, G, sizeof(double) * nd);
+        if (fe) memcpy(fe + eo * nd, floc, sizeof(double) * nd);
+        if (Ge) memcpy(Ge + eo * nd, G, sizeof(double) * nd);
         if (Se) {
             /* StgFEM/SLE/ProvidedSystems/StokesFlow/src/UzawaPreconditionerTerm.c:194-214 */
             double s = 0.0;
             for (int v = 0; v < nd; ++v) s += G[v] * (G[v] / K[v * nd + v]);
-            Se[e] = s;
+            Se[eo] = s;
         }
     }
     return bad ? -1 : 0;
@@ -1685,6 +1699,19 @@ static void nullspace_free(nullspace_t* ns) {
 int uwr_solve_bsscr(const uwr_mesh* m, const uint8_t* fixed, const double* Ke, const double* Ge,
                     const double* fe, const double* Se, const uwr_solve_opts* o,
                     double* u_nodal, double* p, uwr_report* rep) {
+    return uwr_solve_bsscr_bc(m, fixed, NULL, Ke, Ge, fe, Se, o, u_nodal, p, rep);
+}
+
+/* BSSCR solve with Dirichlet values bcval (nn*dim, read where fixed; NULL: homogeneous).  The
+ * element loop lifts the fixed values into both right-hand sides the way __StiffnessMatrix_NewAssemble
+ * does (StgFEM/SLE/SystemSetup/src/StiffnessMatrix.c:900-925): for the velocity block
+ * f_row -= K_e[row][col] bc_col over free rows and fixed columns; for the gradient block, whose
+ * transposed right-hand side is the continuity equation's h, h_e -= G_e[row] bc_row over fixed
+ * rows.  The Schur right-hand side is then G^T K^-1 f - h, the residual includes h - G^T u, and
+ * the returned nodal velocity carries the fixed values. */
+int uwr_solve_bsscr_bc(const uwr_mesh* m, const uint8_t* fixed, const double* bcval, const double* Ke,
+                       const double* Ge, const double* fe, const double* Se, const uwr_solve_opts* o,
+                       double* u_nodal, double* p, uwr_report* rep) {
     set_threads(o->nthreads);
     double t0 = now_s();
     int dim = m->dim, nen = (dim == 3) ? 8 : 4, nd = nen * dim;
@@ -1745,6 +1772,27 @@ int uwr_solve_bsscr(const uwr_mesh* m, const uint8_t* fixed, const double* Ke, c
                 if (q >= 0) f[q] += fe[e * nd + a * dim + d];
             }
     }
+    double* h = (double*)calloc((size_t)(E > 0 ? E : 1), sizeof(double));
+    if (bcval) {
+        for (int64_t e = 0; e < E; ++e) {
+            int64_t inc[8];
+            uwr_element_nodes(m, e, inc);
+            const double* K = Ke + (size_t)e * nd * nd;
+            for (int b = 0; b < nen; ++b)
+                for (int d2 = 0; d2 < dim; ++d2) {
+                    int64_t gc = inc[b] * dim + d2;
+                    if (eq[gc] >= 0) continue;
+                    double bc = bcval[gc];
+                    int col = b * dim + d2;
+                    for (int a = 0; a < nen; ++a)
+                        for (int d = 0; d < dim; ++d) {
+                            int64_t q = eq[inc[a] * dim + d];
+                            if (q >= 0) f[q] -= bc * K[(a * dim + d) * nd + col];
+                        }
+                    h[e] -= bc * Ge[e * nd + col];
+                }
+        }
+    }
     /* Schur preconditioner diagonal */
     double* Sd = (double*)malloc(sizeof(double) * (size_t)E);
     if (o->schur_pc == 0) {
@@ -1801,8 +1849,8 @@ int uwr_solve_bsscr(const uwr_mesh* m, const uint8_t* fixed, const double* Ke, c
         double* utmp = (double*)malloc(sizeof(double) * (size_t)nfree);
         double* hhat = (double*)malloc(sizeof(double) * (size_t)E);
         a11_solve(&s, f, utmp, o->a11_rtol);
-        csr_mv(&s.GT, utmp, hhat);   /* D K^{-1} f; h = 0 */
-        for (int64_t e = 0; e < E; ++e) hhat[e] = -hhat[e];
+        csr_mv(&s.GT, utmp, hhat);   /* h_hat = h - G^T K^{-1} f */
+        for (int64_t e = 0; e < E; ++e) hhat[e] = h[e] - hhat[e];
         /* solve (G^T K^{-1} G) p = -h_hat */
         double* rhs = (double*)malloc(sizeof(double) * (size_t)E);
         for (int64_t e = 0; e < E; ++e) rhs[e] = -hhat[e];
@@ -1827,13 +1875,14 @@ int uwr_solve_bsscr(const uwr_mesh* m, const uint8_t* fixed, const double* Ke, c
         double* gtu = (double*)malloc(sizeof(double) * (size_t)E);
         csr_mv(&s.K, utmp, ku);
         csr_mv(&s.G, p, t);
-        double r2 = 0.0, b2 = dot(nfree, f, f);
+        double r2 = 0.0, b2 = dot(nfree, f, f) + dot(E, h, h);
         for (int64_t r = 0; r < nfree; ++r) { double d = f[r] - ku[r] - t[r]; r2 += d * d; }
         csr_mv(&s.GT, utmp, gtu);
-        r2 += dot(E, gtu, gtu);
+        for (int64_t e = 0; e < E; ++e) { double d = h[e] - gtu[e]; r2 += d * d; }
         memset(u_nodal, 0, sizeof(double) * (size_t)(nn * dim));
         for (int64_t k = 0; k < nn * dim; ++k)
             if (eq[k] >= 0) u_nodal[k] = utmp[eq[k]];
+            else if (bcval) u_nodal[k] = bcval[k];
         if (rep) {
             rep->outer_its = outer;
             rep->backsolve_its = (int32_t)(s.inner_its - before);
@@ -1858,6 +1907,7 @@ cleanup:
     csr_free(&s.G);
     csr_free(&s.GT);
     free(f);
+    free(h);
     free(Sd);
     free(s.tu);
     free(s.tu2);

@@ -100,6 +100,12 @@ int uwr_assemble(const uwr_mesh* m, int64_t n, const uint32_t* offsets, const ui
                  const uwr_fields* f, double* Ke, double* fe, double* Ge, double* Se,
                  double* eta_out, const double* slot_weight /* NULL: constant weights */,
                  int32_t nthreads);
+/* uwr_assemble over elements [first, first + count) only; Ke, fe, Ge, Se indexed from first. */
+int uwr_assemble_range(const uwr_mesh* m, int64_t first, int64_t count, int64_t n, const uint32_t* offsets,
+                       const uint32_t* perm, const double* xi, const int32_t* material, const double* point_eta,
+                       const double* point_rho, int32_t nmat, const uwr_material* mats,
+                       const uwr_fields* f, double* Ke, double* fe, double* Ge, double* Se,
+                       double* eta_out, const double* slot_weight, int32_t nthreads);
 
 /* Discrete Voronoi cell weights (PICellerator/Weights/src/DVCWeights.c) --------------------- */
 /* One element: nump points at local coordinates xi[p*dim + d]; res[d] cells per axis
@@ -155,6 +161,11 @@ typedef struct {
 int uwr_solve_bsscr(const uwr_mesh* m, const uint8_t* fixed, const double* Ke, const double* Ge,
                     const double* fe, const double* Se, const uwr_solve_opts* o,
                     double* u_nodal /* nnode*dim */, double* p /* E */, uwr_report* rep);
+/* The same with non-zero Dirichlet values (bcval: nn*dim, read where fixed), lifted into f and h as
+ * StgFEM/SLE/SystemSetup/src/StiffnessMatrix.c:900-925 does. */
+int uwr_solve_bsscr_bc(const uwr_mesh* m, const uint8_t* fixed, const double* bcval, const double* Ke,
+                       const double* Ge, const double* fe, const double* Se, const uwr_solve_opts* o,
+                       double* u_nodal, double* p, uwr_report* rep);
 
 /* Sparse kernels used by the CPU baseline timing. */
 void uwr_csr_spmv(int64_t nrows, const int64_t* rowptr, const int64_t* cols, const double* vals,

@@ -7,14 +7,16 @@ _DVCWeightsSuite_InitialiseParticleCoords / ...2D assign, on a 10 x 10 (x 10) gr
 with six decimals) and the expected cell grids (links and centres,
 DVCWeightsSuite_testConstructGrid.txt, ...2D.txt), from the read-only reference tree, and writes
 tests/golden/dvc_golden.json.
-Run once in a checkout that has the reference tree; the fixture is committed.
+Run once with the reference tree's path as the only argument; the fixture is committed.
 """
 import json
 import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit(f"usage: python {os.path.basename(__file__)} <path of the Underworld 1.x source tree>")
+REF = sys.argv[1]
 SUITE = os.path.join(REF, "PICellerator/Weights/tests/DVCWeightsSuite.c")
 EXPECTED = os.path.join(REF, "PICellerator/Weights/tests/expected")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "dvc_golden.json")

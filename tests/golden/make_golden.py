@@ -3,7 +3,7 @@
 Reads the PETSc-binary AIJ files that Underworld/Rheology/tests/ViscousSuite.c compares against
 (Underworld/Rheology/tests/expected/test*2D.matrix, testArrheniusWithLimiter.matrix) from the
 read-only reference tree and writes them as CSR arrays to tests/golden/viscous_golden.npz.
-Run once in a checkout that has the reference tree; the fixtures are committed.
+Run once with the reference tree's path as the only argument; the fixtures are committed.
 
 PETSc binary layout (big-endian): int32 MAT_FILE_CLASSID (1211216), int32 rows, int32 cols,
 int32 total nnz, int32 row lengths[rows], int32 column indices[nnz], float64 values[nnz].
@@ -13,7 +13,9 @@ import sys
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit(f"usage: python {os.path.basename(__file__)} <path of the Underworld 1.x source tree>")
+REF = sys.argv[1]
 SRC = os.path.join(REF, "Underworld/Rheology/tests/expected")
 NAMES = ["testMaterialViscosity2D", "testArrhenius2D", "testArrheniusWithLimiter", "testFrankKamenetskii2D"]
 

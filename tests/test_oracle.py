@@ -102,3 +102,62 @@ def test_oracle_bsscr_matches_direct_solve(oracle, dim, nel):
     assert rep.rel_residual < 1e-9
     assert np.linalg.norm(uo - ud) / np.linalg.norm(ud) < 1e-8
     assert np.linalg.norm(p - pd) / np.linalg.norm(pd) < 1e-8
+
+
+def _full_saddle(O, m, Ke, Ge, fe):
+    """K over every velocity dof, G (dofs x elements) and f assembled directly from the element
+    matrices (independent of the oracle's own assembly and lift)."""
+    import ctypes
+    dim = m.dim
+    nen = 1 << dim
+    nd = nen * dim
+    nn, E = O.num_nodes(m), O.num_elements(m)
+    rows, cols, vals, grows, gcols, gvals = [], [], [], [], [], []
+    f = np.zeros(nn * dim)
+    for e in range(E):
+        inc = np.zeros(8, np.int64)
+        O.lib().uwr_element_nodes(ctypes.byref(m), e, inc.ctypes.data)
+        dofs = (inc[:nen, None] * dim + np.arange(dim)[None, :]).reshape(-1)
+        rows.append(np.repeat(dofs, nd)); cols.append(np.tile(dofs, nd)); vals.append(Ke[e].reshape(-1))
+        grows.append(dofs); gcols.append(np.full(nd, e)); gvals.append(Ge[e])
+        np.add.at(f, dofs, fe[e])
+    K = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(nn * dim, nn * dim))
+    G = sp.csr_matrix((np.concatenate(gvals), (np.concatenate(grows), np.concatenate(gcols))), shape=(nn * dim, E))
+    return K, G, f
+
+
+@pytest.mark.parametrize("dim,nel,kind", [(2, (8, 8, 1), "lid"), (2, (8, 6, 1), "extension"),
+                                          (3, (4, 4, 4), "lid"), (3, (4, 6, 4), "extension")])
+def test_oracle_bc_lift_matches_direct_solve(oracle, dim, nel, kind):
+    """Non-zero Dirichlet values (StiffnessMatrix.c:900-925 lift): the oracle's BSSCR solution
+    equals a direct solve of K_ff u_f + G_f p = f_f - K_fc u_c, G_f^T u_f = -G_c^T u_c, and its
+    velocity carries the fixed values."""
+    from earthbyte_underworld_gb300 import workloads as W
+    O = oracle
+    m, Ke, fe, Ge, Se = _small_problem(O, dim, nel)
+    fixed, bcval = W.driven_walls(dim, nel[:dim], kind)
+    u, p, rep = O.solve_bsscr(m, fixed, Ke, Ge, fe, Se, mg_levels=2, scr_rtol=1e-12, a11_rtol=1e-13,
+                              back_rtol=1e-13, bcval=bcval)
+    K, G, f = _full_saddle(O, m, Ke, Ge, fe)
+    free = fixed == 0
+    uc = np.where(free, 0.0, bcval)
+    Kff = K[free][:, free]
+    Gf = G[free]
+    E = O.num_elements(m)
+    rhs = np.concatenate([f[free] - K[free] @ uc, -(G.T @ uc)])
+    A = sp.bmat([[Kff, Gf], [Gf.T, None]]).tocsc()
+    closed = kind == "lid"
+    if closed:   # constant pressure in the null space: pin its mean
+        ones = sp.csr_matrix(np.concatenate([np.zeros(Kff.shape[0]), np.ones(E)])[None, :])
+        A = sp.bmat([[A, ones.T], [ones, None]]).tocsc()
+        rhs = np.concatenate([rhs, [0.0]])
+    sol = spla.spsolve(A, rhs)
+    ud = uc.copy()
+    ud[free] = sol[:Kff.shape[0]]
+    pd = sol[Kff.shape[0]:Kff.shape[0] + E]
+    if closed:
+        p = p - p.mean()
+    assert rep.rel_residual < 1e-9
+    assert np.array_equal(u.reshape(-1)[~free], bcval[~free])
+    assert np.linalg.norm(u.reshape(-1) - ud) / np.linalg.norm(ud) < 1e-8
+    assert np.linalg.norm(p - pd) / np.linalg.norm(pd) < 1e-8
