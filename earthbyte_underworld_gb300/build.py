@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libuwgpu.so")
-SOURCES = ["capi.cu", "binning.cu", "assembly.cu", "operator.cu", "solver.cu", "gwg_stencil.cu", "unet.cu", "advect.cu", "noalloc.cu", "weights.cu"]
+SOURCES = ["capi.cu", "binning.cu", "assembly.cu", "operator.cu", "solver.cu", "gwg_stencil.cu", "unet.cu", "advect.cu", "noalloc.cu", "weights.cu", "tc_check.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -35,7 +35,7 @@ def _flags(extra=()):
 def _stale(obj, src):
     if not os.path.exists(obj):
         return True
-    deps = [src, os.path.join(CSRC, "internal.cuh"), os.path.join(HERE, "..", "include", "uwgpu.h")]
+    deps = [src, os.path.join(CSRC, "internal.cuh"), os.path.join(CSRC, "tc.cuh"), os.path.join(HERE, "..", "include", "uwgpu.h")]
     t = os.path.getmtime(obj)
     return any(os.path.getmtime(d) > t for d in deps)
 

@@ -22,7 +22,10 @@
 // needs ~50 FP64 operations per point instead of the ~1000 of the per-point B^T D B loop,
 // which matters on a part whose FP64 rate is 1/58 of its FP32 rate.  K_e, f_e, G_e are
 // written entry-major ([entry][element]) so a warp's stores coalesce.
+#include <cuda_fp16.h>
+
 #include "internal.cuh"
+#include "tc.cuh"
 
 namespace uwg {
 
@@ -52,7 +55,18 @@ struct AssemblyArgs {
     double* Se;
     double* eta_out;
     uint32_t* flags;  // bit0: empty element, bit1: bad material index
+    double* mom;      // 3D, tensor-core contraction: moments out ([27][e]) instead of K_e and S_e
 };
+
+// G_e entry of node a, component d on a 3D element of widths h: the integral of -dN_a/dx_d
+// (exact for the 2x2x2 Gauss rule)
+__host__ __device__ inline double ge_entry(const double h[3], int a, int d) {
+    double area = 1.0;
+    for (int q = 0; q < 3; ++q)
+        if (q != d) area *= h[q];
+    const double sa = ((a >> d) & 1) ? 1.0 : -1.0;
+    return -sa * area * 0.25;
+}
 
 // Per-point rheology chain.  Every law in scope keeps D isotropic, so the constitutive matrix
 // is carried as its viscosity (D[3][3] in 3D, D[2][2] in 2D).
@@ -181,6 +195,130 @@ __device__ __constant__ double kL[2][2] = {{1.0, 1.0}, {1.0, -1.0}};
 
 __device__ __forceinline__ int qtype(int si, int sj) { return si == sj ? (si > 0 ? 0 : 1) : 2; }
 __device__ __forceinline__ int ltype(int s) { return s > 0 ? 0 : 1; }
+
+// The 63 pair tables of a 3D element: same-axis tables Dkk[t1][t2] (the node-pair types of the two
+// other axes) and mixed-axis tables Mkl[t_k][t_l][t_other], each an integer combination of the 27
+// moments mu[a][b][c] (a, b, c: powers of xi, eta, zeta).
+struct Tables3 {
+    double Dxx[3][3], Dyy[3][3], Dzz[3][3];
+    double Mxy[2][2][3], Mxz[2][2][3], Myz[2][2][3];
+};
+
+// Coefficient of moment m = 9a + 3b + c in table q (the ordering of Tables3 flattened:
+// Dxx, Dyy, Dzz as [t1][t2], then Mxy, Mxz, Myz as [ta][tb][to]); the same combinations
+// tables_from_moments forms.  Values are 0, +-1, +-2, +-4.
+__host__ __device__ inline int table_coefficient(int q, int m) {
+    const int Q[3][3] = {{1, 2, 1}, {1, -2, 1}, {1, 0, -1}};
+    const int L[2][2] = {{1, 1}, {1, -1}};
+    const int a = m / 9, b = (m / 3) % 3, c = m % 3;
+    if (q < 27) {
+        const int axis = q / 9, t1 = (q % 9) / 3, t2 = q % 3;
+        // the axis of the table carries power 0; (u, v) the powers of the two other axes in order
+        int zero, u, v;
+        if (axis == 0) { zero = a; u = b; v = c; }
+        else if (axis == 1) { zero = b; u = a; v = c; }
+        else { zero = c; u = a; v = b; }
+        return zero == 0 ? Q[t1][u] * Q[t2][v] : 0;
+    }
+    if (q >= 63) return 0;
+    const int r = q - 27, pair = r / 12, ta = (r % 12) / 6, tb = (r % 6) / 3, to = r % 3;
+    int u, v, o;   // powers of the pair's first axis, second axis, and the other axis
+    if (pair == 0) { u = a; v = b; o = c; }        // xy
+    else if (pair == 1) { u = a; v = c; o = b; }   // xz
+    else { u = b; v = c; o = a; }                  // yz
+    if (u > 1 || v > 1) return 0;
+    return L[ta][u] * L[tb][v] * Q[to][o];
+}
+
+__device__ __forceinline__ void tables_from_moments(const double* mu, Tables3& T) {
+#pragma unroll
+    for (int t1 = 0; t1 < 3; ++t1)
+#pragma unroll
+        for (int t2 = 0; t2 < 3; ++t2) {
+            double sx = 0.0, sy = 0.0, sz = 0.0;
+#pragma unroll
+            for (int u = 0; u < 3; ++u)
+#pragma unroll
+                for (int v = 0; v < 3; ++v) {
+                    double q = kQ[t1][u] * kQ[t2][v];
+                    sx += q * mu[0 * 9 + u * 3 + v];   // axes y (u), z (v)
+                    sy += q * mu[u * 9 + 0 * 3 + v];   // axes x (u), z (v)
+                    sz += q * mu[u * 9 + v * 3 + 0];   // axes x (u), y (v)
+                }
+            T.Dxx[t1][t2] = sx;
+            T.Dyy[t1][t2] = sy;
+            T.Dzz[t1][t2] = sz;
+        }
+#pragma unroll
+    for (int ta = 0; ta < 2; ++ta)
+#pragma unroll
+        for (int tb = 0; tb < 2; ++tb)
+#pragma unroll
+            for (int to = 0; to < 3; ++to) {
+                double sxy = 0.0, sxz = 0.0, syz = 0.0;
+#pragma unroll
+                for (int u = 0; u < 2; ++u)
+#pragma unroll
+                    for (int v = 0; v < 2; ++v) {
+                        double l2 = kL[ta][u] * kL[tb][v];
+#pragma unroll
+                        for (int o = 0; o < 3; ++o) {
+                            double q = l2 * kQ[to][o];
+                            sxy += q * mu[u * 9 + v * 3 + o];   // x^u y^v z^o
+                            sxz += q * mu[u * 9 + o * 3 + v];   // x^u z^v y^o
+                            syz += q * mu[o * 9 + u * 3 + v];   // y^u z^v x^o
+                        }
+                    }
+                T.Mxy[ta][tb][to] = sxy;
+                T.Mxz[ta][tb][to] = sxz;
+                T.Myz[ta][tb][to] = syz;
+            }
+}
+
+// Packed K_e (entry-major) of element e from its tables; diag receives the 24 diagonal entries.
+__device__ __forceinline__ void ke_from_tables(const Tables3& T, double detJ, const double g[3], int64_t e, int64_t ne,
+                                               double* __restrict__ Ke, double diag[24]) {
+    constexpr int NEN = 8, ND = 24;
+    const double inv64 = 1.0 / 64.0;
+    // M_kl[i][j] for node pair (i, j)
+    auto Mkl = [&](int k, int l, int i, int j) -> double {
+        int si[3] = {((i & 1) << 1) - 1, (((i >> 1) & 1) << 1) - 1, (((i >> 2) & 1) << 1) - 1};
+        int sj[3] = {((j & 1) << 1) - 1, (((j >> 1) & 1) << 1) - 1, (((j >> 2) & 1) << 1) - 1};
+        double sc = detJ * g[k] * g[l] * inv64 * (double)(si[k] * sj[l]);
+        if (k == l) {
+            if (k == 0) return sc * T.Dxx[qtype(si[1], sj[1])][qtype(si[2], sj[2])];
+            if (k == 1) return sc * T.Dyy[qtype(si[0], sj[0])][qtype(si[2], sj[2])];
+            return sc * T.Dzz[qtype(si[0], sj[0])][qtype(si[1], sj[1])];
+        }
+        // k < l: derivative axis k on node i, l on node j
+        if (k > l) {
+            // M_kl[i][j] = M_lk[j][i]
+            int t = k; k = l; l = t;
+            int tmp[3] = {si[0], si[1], si[2]};
+            for (int q = 0; q < 3; ++q) { si[q] = sj[q]; sj[q] = tmp[q]; }
+        }
+        if (k == 0 && l == 1) return sc * T.Mxy[ltype(sj[0])][ltype(si[1])][qtype(si[2], sj[2])];
+        if (k == 0 && l == 2) return sc * T.Mxz[ltype(sj[0])][ltype(si[2])][qtype(si[1], sj[1])];
+        return sc * T.Myz[ltype(sj[1])][ltype(si[2])][qtype(si[0], sj[0])];
+    };
+#pragma unroll
+    for (int i = 0; i < NEN; ++i)
+#pragma unroll
+        for (int j = i; j < NEN; ++j) {
+            double tr = Mkl(0, 0, i, j) + Mkl(1, 1, i, j) + Mkl(2, 2, i, j);
+#pragma unroll
+            for (int al = 0; al < 3; ++al)
+#pragma unroll
+                for (int be = 0; be < 3; ++be) {
+                    int r = i * 3 + al, cix = j * 3 + be;
+                    if (r > cix) continue;
+                    // K[(i,al),(j,be)] = delta * tr + M_{be,al}[i][j]
+                    double v = Mkl(be, al, i, j) + (al == be ? tr : 0.0);
+                    Ke[(int64_t)packed_index(ND, r, cix) * ne + e] = v;
+                    if (r == cix) diag[r] = v;
+                }
+        }
+}
 
 template <int DIM>
 __global__ void __launch_bounds__(128) k_assemble(AssemblyArgs A) {
@@ -351,109 +489,28 @@ __global__ void __launch_bounds__(128) k_assemble(AssemblyArgs A) {
     const double inv64 = DIM == 3 ? 1.0 / 64.0 : 1.0 / 16.0;
 
     if (DIM == 3) {
-        // same-axis pair tables: Dkk[t1][t2] over the two other axes
-        double Dxx[3][3], Dyy[3][3], Dzz[3][3];
-#pragma unroll
-        for (int t1 = 0; t1 < 3; ++t1)
-#pragma unroll
-            for (int t2 = 0; t2 < 3; ++t2) {
-                double sx = 0.0, sy = 0.0, sz = 0.0;
-#pragma unroll
-                for (int u = 0; u < 3; ++u)
-#pragma unroll
-                    for (int v = 0; v < 3; ++v) {
-                        double q = kQ[t1][u] * kQ[t2][v];
-                        sx += q * mu[0 * 9 + u * 3 + v];   // axes y (u), z (v)
-                        sy += q * mu[u * 9 + 0 * 3 + v];   // axes x (u), z (v)
-                        sz += q * mu[u * 9 + v * 3 + 0];   // axes x (u), y (v)
-                    }
-                Dxx[t1][t2] = sx;
-                Dyy[t1][t2] = sy;
-                Dzz[t1][t2] = sz;
-            }
-        // mixed pairs (k < l): Mkl[tk_j][tl_i][t_other]
-        double Mxy[2][2][3], Mxz[2][2][3], Myz[2][2][3];
-#pragma unroll
-        for (int ta = 0; ta < 2; ++ta)
-#pragma unroll
-            for (int tb = 0; tb < 2; ++tb)
-#pragma unroll
-                for (int to = 0; to < 3; ++to) {
-                    double sxy = 0.0, sxz = 0.0, syz = 0.0;
-#pragma unroll
-                    for (int u = 0; u < 2; ++u)
-#pragma unroll
-                        for (int v = 0; v < 2; ++v) {
-                            double l2 = kL[ta][u] * kL[tb][v];
-#pragma unroll
-                            for (int o = 0; o < 3; ++o) {
-                                double q = l2 * kQ[to][o];
-                                sxy += q * mu[u * 9 + v * 3 + o];   // x^u y^v z^o
-                                sxz += q * mu[u * 9 + o * 3 + v];   // x^u z^v y^o
-                                syz += q * mu[o * 9 + u * 3 + v];   // y^u z^v x^o
-                            }
-                        }
-                    Mxy[ta][tb][to] = sxy;
-                    Mxz[ta][tb][to] = sxz;
-                    Myz[ta][tb][to] = syz;
-                }
-        // M_kl[i][j] for node pair (i, j)
-        auto Mkl = [&](int k, int l, int i, int j) -> double {
-            int si[3] = {((i & 1) << 1) - 1, (((i >> 1) & 1) << 1) - 1, (((i >> 2) & 1) << 1) - 1};
-            int sj[3] = {((j & 1) << 1) - 1, (((j >> 1) & 1) << 1) - 1, (((j >> 2) & 1) << 1) - 1};
-            double sc = detJ * g[k] * g[l] * inv64 * (double)(si[k] * sj[l]);
-            if (k == l) {
-                if (k == 0) return sc * Dxx[qtype(si[1], sj[1])][qtype(si[2], sj[2])];
-                if (k == 1) return sc * Dyy[qtype(si[0], sj[0])][qtype(si[2], sj[2])];
-                return sc * Dzz[qtype(si[0], sj[0])][qtype(si[1], sj[1])];
-            }
-            // k < l: derivative axis k on node i, l on node j
-            if (k > l) {
-                // M_kl[i][j] = M_lk[j][i]
-                int t = k; k = l; l = t;
-                int tmp[3] = {si[0], si[1], si[2]};
-                for (int q = 0; q < 3; ++q) { si[q] = sj[q]; sj[q] = tmp[q]; }
-            }
-            if (k == 0 && l == 1) return sc * Mxy[ltype(sj[0])][ltype(si[1])][qtype(si[2], sj[2])];
-            if (k == 0 && l == 2) return sc * Mxz[ltype(sj[0])][ltype(si[2])][qtype(si[1], sj[1])];
-            return sc * Myz[ltype(sj[1])][ltype(si[2])][qtype(si[0], sj[0])];
-        };
         const int64_t ne = A.ne;
         double diag[ND];
+        if (A.mom) {
+            // moments out; K_e and S_e come from the tensor-core contraction (k_contract_tc)
 #pragma unroll
-        for (int i = 0; i < NEN; ++i)
-#pragma unroll
-            for (int j = i; j < NEN; ++j) {
-                double tr = Mkl(0, 0, i, j) + Mkl(1, 1, i, j) + Mkl(2, 2, i, j);
-#pragma unroll
-                for (int al = 0; al < 3; ++al)
-#pragma unroll
-                    for (int be = 0; be < 3; ++be) {
-                        int r = i * 3 + al, cix = j * 3 + be;
-                        if (r > cix) continue;
-                        // K[(i,al),(j,be)] = delta * tr + M_{be,al}[i][j]
-                        double v = Mkl(be, al, i, j) + (al == be ? tr : 0.0);
-                        A.Ke[(int64_t)packed_index(ND, r, cix) * ne + e] = v;
-                        if (r == cix) diag[r] = v;
-                    }
-            }
+            for (int m = 0; m < NM; ++m) A.mom[(int64_t)m * ne + e] = mu[m];
+        } else {
+            Tables3 T;
+            tables_from_moments(mu, T);
+            ke_from_tables(T, detJ, g, e, ne, A.Ke, diag);
+        }
         // G_e: integral of -dN_a/dx_d over the element (exact for the 2x2x2 Gauss rule)
-        double Gl[ND];
         double s = 0.0;
 #pragma unroll
         for (int a = 0; a < NEN; ++a)
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                double area = 1.0;
-#pragma unroll
-                for (int q = 0; q < 3; ++q)
-                    if (q != d) area *= h[q];
-                double sa = ((a >> d) & 1) ? 1.0 : -1.0;
-                Gl[a * 3 + d] = -sa * area * 0.25;
-                A.Ge[(int64_t)(a * 3 + d) * ne + e] = Gl[a * 3 + d];
-                s += Gl[a * 3 + d] * (Gl[a * 3 + d] / diag[a * 3 + d]);
+                const double G = ge_entry(h, a, d);
+                A.Ge[(int64_t)(a * 3 + d) * ne + e] = G;
+                if (!A.mom) s += G * (G / diag[a * 3 + d]);
             }
-        A.Se[e] = s;
+        if (!A.mom) A.Se[e] = s;
         // f_e: -g detJ sum_p w rho N_a on the vertical component
         double fs = -A.gravity * detJ * 0.125;
 #pragma unroll
@@ -542,6 +599,179 @@ __global__ void __launch_bounds__(128) k_assemble(AssemblyArgs A) {
     }
 }
 
+// ---- tensor-core contraction of the 3D moments into K_e -------------------------------------
+// The 63 pair tables are integer combinations of the 27 moments (table_coefficient), so for a
+// tile of 128 elements they form one product Tab = Mom C^T with C (63 x 27) of small integers.
+// It runs on the tensor core in FP16 with FP64 accuracy by the error-free splitting of Ozaki,
+// Ogita, Oishi and Rump ("Error-free transformations of matrix multiplication by using fast
+// routines of matrix multiplication and its applications", Numer. Algorithms 59, 2012): each
+// element's moments are scaled by a power of two s_e >= max |mu| and cut into five slices of 11
+// bits, mu = s_e sum_j a_j 2^(-11 (j+1)) with integers |a_j| < 2^11 (exact in FP16).  A slice
+// times C is an integer below 27 * 2^11 * 4 < 2^24, exact in the FP32 accumulator, so the only
+// error is the truncation after 55 bits (relative 2^-55 of the element's largest moment) and the
+// FP64 sum of the five slice products.  The epilogue forms K_e and S_e from the tables in FP64
+// (ke_from_tables, as the FP64 path does).
+constexpr int kSlices = 5;
+constexpr int kTabN = 64;   // 63 tables + a zero row
+constexpr int kMomK = 32;   // 27 moments + zero columns
+
+struct ContractArgs {
+    int nel[3];
+    double min[3], max[3];
+    int64_t ne;
+    const double* mom;   // [27][e]
+    double* Ke;          // packed, entry-major
+    double* Se;
+    uint32_t* err;
+};
+
+__global__ void __launch_bounds__(128, 1) k_contract_tc(ContractArgs A) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    unsigned char* sB = smem;                                   // 64 x 32 FP16, K-major
+    unsigned char* sA = smem + kTabN * kMomK * 2;               // kSlices x (128 x 32 FP16)
+    const uint32_t bytesA = 128 * kMomK * 2;
+    constexpr uint32_t kCols = 512;                             // 5 x 64 accumulator columns
+    if (warp == 0) {
+        tc::tmem_alloc(&tbase, kCols);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) tc::mbar_init(&bar, 1);
+    for (int idx = tid; idx < kTabN * kMomK; idx += 128) {
+        const int q = idx / kMomK, m = idx % kMomK;
+        const float v = m < 27 ? (float)table_coefficient(q, m) : 0.0f;
+        *reinterpret_cast<__half*>(sB + tc::k_major_offset(q, m, kMomK)) = __float2half_rn(v);
+    }
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t taddr = tbase;
+    const uint32_t idesc = tc::idesc_f16(128, kTabN, tc::kFmtF16, 0, 0);
+    const int64_t ne = A.ne;
+    const int64_t ntiles = (ne + 127) / 128;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t e = tile * 128 + tid;
+        const bool live = e < ne;
+        // this element's moments, scaled by 2^-ex so that |t| < 1, cut into five 11-bit slices
+        double t[27];
+        double mx = 0.0;
+#pragma unroll
+        for (int m = 0; m < 27; ++m) {
+            t[m] = live ? A.mom[(int64_t)m * ne + e] : 0.0;
+            mx = fmax(mx, fabs(t[m]));
+        }
+        int ex = 0;
+        frexp(mx, &ex);   // mx < 2^ex
+#pragma unroll
+        for (int m = 0; m < 27; ++m) t[m] = ldexp(t[m], -ex);
+#pragma unroll
+        for (int j = 0; j < kSlices; ++j) {
+#pragma unroll
+            for (int c8 = 0; c8 < kMomK / 8; ++c8) {
+                uint4 chunk;
+                __half* hv = reinterpret_cast<__half*>(&chunk);
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const int m = c8 * 8 + i;
+                    float a = 0.0f;
+                    if (m < 27) {
+                        const double u = t[m] * 2048.0;
+                        const double w = trunc(u);
+                        t[m] = u - w;
+                        a = (float)w;
+                    }
+                    hv[i] = __float2half_rn(a);
+                }
+                *reinterpret_cast<uint4*>(sA + j * bytesA + tc::k_major_offset(tid, c8 * 8, kMomK)) = chunk;
+            }
+        }
+        tc::fence_proxy_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (tid == 0) {
+            const uint32_t b = tc::smem_u32(sB), a0 = tc::smem_u32(sA);
+#pragma unroll
+            for (int j = 0; j < kSlices; ++j)
+#pragma unroll
+                for (int s = 0; s < kMomK / 16; ++s)
+                    tc::mma_f16(taddr + (uint32_t)(j * kTabN), tc::k_major_desc(a0 + j * bytesA, s, kMomK),
+                                tc::k_major_desc(b, s, kMomK), idesc, s > 0 ? 1u : 0u);
+            tc::mma_commit(&bar);
+        }
+        ok = tc::mbar_wait(&bar, phase) && ok;
+        phase ^= 1u;
+        ok = __syncthreads_and(ok) != 0;
+        if (!ok) break;
+        tc::fence_after_sync();
+        // tables = 2^ex sum_j D_j 2^(-11 (j+1)), each D_j an exact integer in FP32
+        double T[kTabN];
+#pragma unroll
+        for (int q = 0; q < kTabN; ++q) T[q] = 0.0;
+#pragma unroll
+        for (int j = 0; j < kSlices; ++j) {
+            const double sc = ldexp(1.0, ex - 11 * (j + 1));
+#pragma unroll
+            for (int c = 0; c < kTabN; c += 16) {
+                uint32_t r[16];
+                tc::tmem_ld16(tc::tmem_addr(taddr, 32 * warp, j * kTabN + c), r);
+                tc::tmem_wait_ld();
+#pragma unroll
+                for (int i = 0; i < 16; ++i) T[c + i] = fma((double)__uint_as_float(r[i]), sc, T[c + i]);
+            }
+        }
+        tc::fence_before_sync();
+        if (live) {
+            Tables3 tb;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                tb.Dxx[i / 3][i % 3] = T[i];
+                tb.Dyy[i / 3][i % 3] = T[9 + i];
+                tb.Dzz[i / 3][i % 3] = T[18 + i];
+            }
+#pragma unroll
+            for (int i = 0; i < 12; ++i) {
+                tb.Mxy[i / 6][(i / 3) % 2][i % 3] = T[27 + i];
+                tb.Mxz[i / 6][(i / 3) % 2][i % 3] = T[39 + i];
+                tb.Myz[i / 6][(i / 3) % 2][i % 3] = T[51 + i];
+            }
+            const int64_t ie = e % A.nel[0], je = (e / A.nel[0]) % A.nel[1], ke = e / ((int64_t)A.nel[0] * A.nel[1]);
+            const int64_t idx[3] = {ie, je, ke};
+            double h[3], g[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const double x0 = node_coord_1d(idx[d], A.nel[d], A.min[d], A.max[d]);
+                h[d] = node_coord_1d(idx[d] + 1, A.nel[d], A.min[d], A.max[d]) - x0;
+                g[d] = 2.0 / h[d];
+            }
+            const double detJ = (0.5 * h[0]) * (0.5 * h[1]) * (0.5 * h[2]);
+            double diag[24];
+            ke_from_tables(tb, detJ, g, e, ne, A.Ke, diag);
+            double s = 0.0;
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const double G = ge_entry(h, a, d);
+                    s += G * (G / diag[a * 3 + d]);
+                }
+            A.Se[e] = s;
+        }
+    }
+    if (!ok && tid == 0) atomicOr(A.err, 4u);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(taddr, kCols);
+    }
+}
+
 void assemble(Context& c) {
     UWG_REQUIRE(c.mapped, UWGPU_ERR_STATE, "assemble called before bin_and_map");
     UWG_REQUIRE(c.nmat > 0, UWGPU_ERR_STATE, "materials not set");
@@ -589,12 +819,20 @@ void assemble(Context& c) {
     A.Se = c.Se.p;
     A.eta_out = c.seta_out.p;
     A.flags = c.err_count.p;
+    const bool tcpath = dim == 3 && c.assembly_mode == UWGPU_ASSEMBLY_TENSOR;
+    A.mom = nullptr;
+    if (tcpath) {
+        c.mom.ensure((size_t)27 * ne);
+        A.mom = c.mom.p;
+    }
     {
         // algorithmic bytes: per point xi + material (+ optional inputs) read, viscosity written;
         // per element offsets read, packed K_e, f_e, G_e, S_e written
         double per_point = dim * 8.0 + 4.0 + 8.0 + (c.has_peta ? 8.0 : 0.0) + (c.has_prho ? 8.0 : 0.0) +
                            (A.sw ? 8.0 : 0.0);
-        double per_el = 4.0 + packed_size(nd) * 8.0 + 2.0 * nd * 8.0 + 8.0;
+        // (the tensor-core form writes the 27 moments instead of K_e and S_e, and its contraction
+        // kernel reads them back: 2 x 216 B more per element)
+        double per_el = 4.0 + packed_size(nd) * 8.0 + 2.0 * nd * 8.0 + 8.0 + (tcpath ? 2.0 * 27 * 8.0 : 0.0);
         double flops_point = dim == 3 ? 120.0 : 50.0, flops_el = dim == 3 ? 3600.0 : 300.0;
         note_work(c, UWGPU_KERNEL_ASSEMBLY, per_point * c.np + per_el * ne, flops_point * c.np + flops_el * ne);
         LaunchScope ls(c, UWGPU_KERNEL_ASSEMBLY);
@@ -604,11 +842,38 @@ void assemble(Context& c) {
             k_assemble<2><<<blocks_for(ne, 128), 128, 0, c.stream>>>(A);
     }
     check_launch("k_assemble");
+    if (tcpath) {
+        ContractArgs C;
+        for (int d = 0; d < 3; ++d) {
+            C.nel[d] = m.nel[d];
+            C.min[d] = m.min[d];
+            C.max[d] = m.max[d];
+        }
+        C.ne = ne;
+        C.mom = c.mom.p;
+        C.Ke = L0.Ke.p;
+        C.Se = c.Se.p;
+        C.err = c.err_count.p;
+        static bool attr_set = false;
+        if (!attr_set) {
+            UWG_CUDA(cudaFuncSetAttribute(k_contract_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+            attr_set = true;
+        }
+        // 512 TMEM columns per CTA: request enough shared memory that one CTA fills an SM
+        const size_t smem = 120 * 1024;
+        int nsm = 1;
+        UWG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
+        const int64_t ntiles = (ne + 127) / 128;
+        LaunchScope ls(c, UWGPU_KERNEL_ASSEMBLY);
+        k_contract_tc<<<(unsigned)(ntiles < nsm ? ntiles : nsm), 128, smem, c.stream>>>(C);
+    }
+    check_launch("k_contract_tc");
     uint32_t flags = 0;
     UWG_CUDA(cudaMemcpyAsync(&flags, c.err_count.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream));
     UWG_CUDA(cudaStreamSynchronize(c.stream));
     c.assembled = true;
     c.operator_built = false;
+    if (flags & 4u) throw Error(UWGPU_ERR_CUDA, "tensor-core contraction: an MMA did not complete in time");
     if (flags & 2u) throw Error(UWGPU_ERR_ARGUMENT, "material index out of range");
     if (flags & 1u)
         throw Error(UWGPU_ERR_ARGUMENT,

@@ -476,6 +476,21 @@ int uwgpu_bfbt_operator_apply(uwgpu_ctx* ctx, int32_t form, const double* x, dou
     });
 }
 
+int uwgpu_assembly_set(uwgpu_ctx* ctx, int32_t mode) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(mode == UWGPU_ASSEMBLY_FP64 || mode == UWGPU_ASSEMBLY_TENSOR, UWGPU_ERR_ARGUMENT, "bad assembly mode");
+        c.assembly_mode = mode;
+    });
+}
+
+int uwgpu_tc_check(uwgpu_ctx* ctx, int32_t layout, int32_t format, int32_t n, int32_t k, const uint16_t* a,
+                   const uint16_t* b, float* d) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(a && b && d, UWGPU_ERR_ARGUMENT, "a, b and d are required");
+        uwg::tc_check(layout, format, n, k, a, b, d);
+    });
+}
+
 int uwgpu_time_bfbt_apply(uwgpu_ctx* ctx, int32_t form, int32_t iterations, double* ms) {
     return guarded(ctx, [&](Context& c) {
         UWG_REQUIRE(ms && iterations > 0, UWGPU_ERR_ARGUMENT, "bad arguments");

@@ -165,6 +165,8 @@ struct Context {
     DArray<double> Se;
     DArray<double> Ge;        // entry-major [k][e]
     bool assembled = false;
+    int assembly_mode = UWGPU_ASSEMBLY_FP64;
+    DArray<double> mom;       // 3D moments [27][e] of the tensor-core contraction
 
     // per-axis element widths of the fine mesh (device), and the mesh they belong to
     DArray<double> elem_h;
@@ -271,6 +273,7 @@ void weights_set(Context& c, int kind, const int32_t res[3]);
 void integration_points(Context& c, const double** xi, const double** w);
 void integration_points_download(Context& c, double* xi, double* w);
 void bfbt_operator_hook(Context& c, int form, const double* xh, double* yh, int iterations, double* ms);
+int tc_check(int layout, int fmt, int N, int K, const uint16_t* A, const uint16_t* B, float* D);
 void advect_particles(Context& c, double dt, int order, bool fallback, uint32_t& fell_back, uint32_t& left_mesh);
 template <typename T> void level_cheb(Context&, Level&, const T*, T*, int, bool);
 int learned_generate(Context& c, const uwgpu_solve_opts& o, int nsamples, uint64_t seed);

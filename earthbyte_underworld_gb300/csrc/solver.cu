@@ -1044,20 +1044,22 @@ void Bsscr::run() {
     int before = rep.inner_its_total;
     a11(t2.p, c.u_sol.p, o.back_rtol);
     rep.backsolve_its = rep.inner_its_total - before;
-    if (c.has_bc && c.bc_nonzero) axpy<double>(c, nv, 1.0, ub.p, c.u_sol.p);
     rep.outer_its = outer;
     rep.pc_inner_its = bfbt_its;
+    // the residual of the lifted system, on the free dofs (before the fixed values are added)
     rep.rel_residual = full_residual(c.u_sol.p, c.p_sol.p);
+    if (c.has_bc && c.bc_nonzero) axpy<double>(c, nv, 1.0, ub.p, c.u_sol.p);
     UWG_CUDA(cudaStreamSynchronize(c.stream));
+    if (learned) unet::check_errors(c, *c.net);
     auto t2c = std::chrono::steady_clock::now();
     rep.t_solve_ms = std::chrono::duration<double, std::milli>(t2c - t1).count();
     c.has_solution = true;
-    rep.converged = !(nan || outer_fail || inner_fail) ? 1 : 0;
     if (nan || !std::isfinite(rep.rel_residual)) rep.status = UWGPU_ERR_NAN;
     else if (outer_fail) rep.status = UWGPU_ERR_NOT_CONVERGED;
     else rep.status = UWGPU_OK;
     if (o.target_rel_residual > 0 && rep.rel_residual > o.target_rel_residual && rep.status == UWGPU_OK)
         rep.status = UWGPU_ERR_NOT_CONVERGED;
+    rep.converged = rep.status == UWGPU_OK && !inner_fail ? 1 : 0;
 }
 
 void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "internal.cuh"
+#include "tc.cuh"
 #include "unet.cuh"
 
 namespace uwg {
@@ -58,110 +59,308 @@ __device__ __forceinline__ void store8(float* p, const float v[8]) {
     *reinterpret_cast<float4*>(p + 4) = make_float4(v[4], v[5], v[6], v[7]);
 }
 
-// 3x3x3 convolution, zero padding, eight output channels per thread (one voxel per thread):
-//   out[v][co] = act(bias[co] + sum_{t, ci} W[t][ci][co] in[v + off(t)][ci])
-// The block's slice W[.][.][co0 .. co0+8) is staged in shared memory (BF16).
-// cin and cout are multiples of 8.
-template <typename TI, typename TO>
-__global__ void __launch_bounds__(128) k_conv3(Vol g, int cin, int cout, const TI* __restrict__ in,
-                                               const bf16* __restrict__ W, const float* __restrict__ bias,
-                                               TO* __restrict__ out, int relu) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    bf16* sw = reinterpret_cast<bf16*>(smem_raw);   // [27][cin][8]
-    const int co0 = blockIdx.y * 8;
-    for (int idx = threadIdx.x; idx < 27 * cin; idx += blockDim.x)
-        *reinterpret_cast<uint4*>(sw + (size_t)idx * 8) = *reinterpret_cast<const uint4*>(W + (size_t)idx * cout + co0);
-    __syncthreads();
-    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= g.nv) return;
-    const int x = (int)(v % g.px), y = (int)((v / g.px) % g.py), z = (int)(v / ((int64_t)g.px * g.py));
-    float acc[8];
+// ---- tensor-core (tcgen05) forms of the 3x3x3 convolution --------------------------------------
+// FP32 values enter a BF16 product as two parts, hi = bf16(x) and lo = bf16(x - hi), whose sum
+// carries about 16 significant bits (the split of Henry, Tang and Heinecke, "Leveraging the
+// bfloat16 artificial intelligence datatype for higher-precision computations", ARITH 2019);
+// both parts are multiplied on the tensor core and accumulated in FP32.
+__device__ __forceinline__ void split8(const float* p, uint4& hi, uint4& lo) {
+    float v[8];
+    load8(p, v);
+    __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&hi);
+    __nv_bfloat162* l = reinterpret_cast<__nv_bfloat162*>(&lo);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) acc[k] = bias ? bias[co0 + k] : 0.0f;
-    for (int t = 0; t < 27; ++t) {
-        const int xx = x + t % 3 - 1, yy = y + (t / 3) % 3 - 1, zz = z + t / 9 - 1;
-        if (xx < 0 || xx >= g.px || yy < 0 || yy >= g.py || zz < 0 || zz >= g.pz) continue;
-        const TI* row = in + ((int64_t)xx + (int64_t)g.px * (yy + (int64_t)g.py * zz)) * cin;
-        const bf16* wt = sw + (size_t)t * cin * 8;
-        for (int c8 = 0; c8 < cin; c8 += 8) {
-            float xv[8];
-            load8(row + c8, xv);
-#pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                float wv[8];
-                load8(wt + (size_t)(c8 + c) * 8, wv);
-#pragma unroll
-                for (int k = 0; k < 8; ++k) acc[k] = fmaf(xv[c], wv[k], acc[k]);
-            }
-        }
+    for (int k = 0; k < 4; ++k) {
+        const __nv_bfloat162 a = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+        const float2 af = __bfloat1622float2(a);
+        h[k] = a;
+        l[k] = __floats2bfloat162_rn(v[2 * k] - af.x, v[2 * k + 1] - af.y);
     }
-    if (relu) {
-#pragma unroll
-        for (int k = 0; k < 8; ++k) acc[k] = fmaxf(acc[k], 0.0f);
-    }
-    store8(out + v * cout + co0, acc);
 }
 
-// part[slice][t][ci][co] = sum over the slice's voxels v of in[v + off(t)][ci] g[v][co]  (in: BF16
-// activations, g: FP32 gradient of the pre-activation).  grid = (voxel slices, 27 taps); each
-// block accumulates its slice in registers (output o = threadIdx.x + 256 k).  The slices are
-// summed in a fixed order afterwards (k_sum_slices), so the gradient is deterministic.
-constexpr int kWgThreads = 256;
-constexpr int kWgMaxPer = 64;   // cin * cout <= 256 * 64
-constexpr int kWgTile = 32;     // voxels staged per round
-constexpr int kWgSlices = 16;   // voxel slices (blocks per tap)
-__global__ void __launch_bounds__(kWgThreads) k_conv3_wgrad(Vol g, int cin, int cout, int taps,
-                                                            const bf16* __restrict__ in,
-                                                            const float* __restrict__ gout, float* __restrict__ dW,
-                                                            int64_t vslice) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float* sx = reinterpret_cast<float*>(smem_raw);   // [kWgTile][cin]
-    float* sg = sx + kWgTile * cin;                    // [kWgTile][cout]
-    const int t = blockIdx.y;
-    const int dx = taps == 27 ? t % 3 - 1 : 0, dy = taps == 27 ? (t / 3) % 3 - 1 : 0, dz = taps == 27 ? t / 9 - 1 : 0;
-    const int nout = cin * cout;
-    float acc[kWgMaxPer];
-#pragma unroll
-    for (int k = 0; k < kWgMaxPer; ++k) acc[k] = 0.0f;
-    const int64_t v0 = (int64_t)blockIdx.x * vslice;
-    const int64_t v1 = v0 + vslice < g.nv ? v0 + vslice : g.nv;
-    for (int64_t vb = v0; vb < v1; vb += kWgTile) {
-        __syncthreads();
-        for (int idx = threadIdx.x; idx < kWgTile * cin; idx += blockDim.x) {
-            const int vt = idx / cin, c = idx % cin;
-            const int64_t v = vb + vt;
-            float val = 0.0f;
-            if (v < v1) {
-                const int x = (int)(v % g.px) + dx, y = (int)((v / g.px) % g.py) + dy,
-                          z = (int)(v / ((int64_t)g.px * g.py)) + dz;
-                if (x >= 0 && x < g.px && y >= 0 && y < g.py && z >= 0 && z < g.pz)
-                    val = __bfloat162float(in[((int64_t)x + (int64_t)g.px * (y + (int64_t)g.py * z)) * cin + c]);
-            }
-            sx[idx] = val;
-        }
-        for (int idx = threadIdx.x; idx < kWgTile * cout; idx += blockDim.x) {
-            const int vt = idx / cout, c = idx % cout;
-            const int64_t v = vb + vt;
-            sg[idx] = v < v1 ? gout[v * cout + c] : 0.0f;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < kWgMaxPer; ++k) {
-            const int o = threadIdx.x + k * kWgThreads;
-            if (o < nout) {
-                const int ci = o / cout, co = o % cout;
-                float a = acc[k];
-#pragma unroll 8
-                for (int vt = 0; vt < kWgTile; ++vt) a = fmaf(sx[vt * cin + ci], sg[vt * cout + co], a);
-                acc[k] = a;
-            }
-        }
+constexpr int kTcSmemBudget = 200 * 1024;   // dynamic shared memory a tensor-core conv kernel may use
+
+// Shared-memory plan of k_conv3_tc: B (the weights) for all 27 taps when they fit, else two tap
+// buffers; A double-buffered per tap, with a second (lo) part for FP32 inputs.
+struct ConvTcPlan {
+    int Kp, Np;
+    int resident;
+    size_t bytesB, bytesA, smem;
+};
+__host__ __device__ inline ConvTcPlan conv_tc_plan(int K, int N, bool split) {
+    ConvTcPlan p;
+    p.Kp = (K + 15) / 16 * 16;
+    p.Np = (N + 15) / 16 * 16;
+    p.bytesB = (size_t)p.Np * p.Kp * 2;
+    p.bytesA = (size_t)128 * p.Kp * 2;
+    const size_t a_total = 2 * (split ? 2 : 1) * p.bytesA;
+    p.resident = 27 * p.bytesB + a_total <= (size_t)kTcSmemBudget ? 1 : 0;
+    p.smem = (p.resident ? 27 : 2) * p.bytesB + a_total;
+    return p;
+}
+
+// 3x3x3 convolution as an implicit GEMM on the tensor core: for a tile of 128 consecutive voxels
+// (rows, M = 128) and all N output channels, D = sum over the 27 taps t of A_t B_t^T, with
+// A_t[m][k] = in[v_m + off(t)][k] (zero outside the grid) and B_t[n][k] = W_t[k][n], read from the
+// layer's other packing Wrev[26 - t][n][k] (for the forward pass the flipped transpose, for the
+// data gradient the plain weights).  Operands are K-major in shared memory; the accumulator
+// (128 x N FP32) lives in TMEM; one thread issues the MMAs of a tap while all threads stage the
+// next tap into the other buffer.  The epilogue adds the bias, applies ReLU and stores BF16 (or
+// FP32) rows.  CTAs are persistent over the voxel tiles.  FP32 inputs (gradients) enter as
+// hi + lo BF16 parts (two MMAs per K step).
+template <typename TI, typename TO>
+__global__ void __launch_bounds__(128, 1) k_conv3_tc(Vol g, int K, int N, ConvTcPlan P, const TI* __restrict__ in,
+                                                     const bf16* __restrict__ Wrev, const float* __restrict__ bias,
+                                                     TO* __restrict__ out, int relu, uint32_t* __restrict__ err) {
+    constexpr bool kSplit = sizeof(TI) == 4;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t bar[2];
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int Kp = P.Kp, Np = P.Np, kc8 = Kp / 8;
+    unsigned char* sB = smem;
+    unsigned char* sA = smem + (P.resident ? 27 : 2) * P.bytesB;   // [buf][part] of bytesA each
+    const uint32_t ncols = tc::tmem_cols(Np);
+    if (warp == 0) {
+        tc::tmem_alloc(&tbase, ncols);
+        tc::tmem_relinquish();
     }
-    float* part = dW + ((int64_t)blockIdx.x * taps + t) * nout;
+    if (tid == 0) {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+    }
+    // B of tap t into `dst` (K-major, zero beyond N and K)
+    auto stage_b = [&](int t, unsigned char* dst) {
+        const bf16* src = Wrev + (size_t)(26 - t) * N * K;
+        for (int idx = tid; idx < Np * kc8; idx += 128) {
+            const int n = idx % Np, c8 = idx / Np;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (n < N && c8 * 8 < K) v = __ldg(reinterpret_cast<const uint4*>(src + (size_t)n * K + c8 * 8));
+            *reinterpret_cast<uint4*>(dst + tc::k_major_offset(n, c8 * 8, Kp)) = v;
+        }
+    };
+    if (P.resident)
+        for (int t = 0; t < 27; ++t) stage_b(t, sB + (size_t)t * P.bytesB);
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t taddr = tbase;
+    const uint32_t idesc = tc::idesc_f16(128, Np, tc::kFmtBF16, 0, 0);
+    uint32_t phase[2] = {0u, 0u}, pend[2] = {0u, 0u};
+    bool ok = true;
+    auto wait_buf = [&](int b) {
+        if (pend[b]) {
+            ok = tc::mbar_wait(&bar[b], phase[b]) && ok;
+            phase[b] ^= 1u;
+            pend[b] = 0u;
+        }
+    };
+    const int64_t ntiles = (g.nv + 127) / 128;
+    const int64_t pxy = (int64_t)g.px * g.py;
+    for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int64_t v = tile * 128 + tid;   // this thread's row
+        const bool vin = v < g.nv;
+        const int x = (int)(v % g.px), y = (int)((v / g.px) % g.py), z = (int)(v / pxy);
+        for (int t = 0; t < 27; ++t) {
+            const int b = t & 1;
+            wait_buf(b);
+            unsigned char* a0 = sA + (size_t)b * (kSplit ? 2 : 1) * P.bytesA;
+            const int xx = x + t % 3 - 1, yy = y + (t / 3) % 3 - 1, zz = z + t / 9 - 1;
+            const bool nb = vin && xx >= 0 && xx < g.px && yy >= 0 && yy < g.py && zz >= 0 && zz < g.pz;
+            const TI* row = in + ((int64_t)xx + (int64_t)g.px * (yy + (int64_t)g.py * zz)) * K;
+            for (int c8 = 0; c8 < kc8; ++c8) {
+                const uint32_t off = tc::k_major_offset(tid, c8 * 8, Kp);
+                const bool live = nb && c8 * 8 < K;
+                if (kSplit) {
+                    uint4 hi = make_uint4(0, 0, 0, 0), lo = make_uint4(0, 0, 0, 0);
+                    if (live) split8(reinterpret_cast<const float*>(row) + c8 * 8, hi, lo);
+                    *reinterpret_cast<uint4*>(a0 + off) = hi;
+                    *reinterpret_cast<uint4*>(a0 + P.bytesA + off) = lo;
+                } else {
+                    uint4 val = make_uint4(0, 0, 0, 0);
+                    if (live) val = __ldg(reinterpret_cast<const uint4*>(reinterpret_cast<const bf16*>(row) + c8 * 8));
+                    *reinterpret_cast<uint4*>(a0 + off) = val;
+                }
+            }
+            unsigned char* bt = P.resident ? sB + (size_t)t * P.bytesB : sB + (size_t)b * P.bytesB;
+            if (!P.resident) stage_b(t, bt);
+            tc::fence_proxy_async();
+            tc::fence_before_sync();
+            ok = __syncthreads_and(ok) != 0;
+            if (!ok) break;
+            tc::fence_after_sync();
+            if (tid == 0) {
+                const uint32_t sa = tc::smem_u32(a0), sb = tc::smem_u32(bt);
+                for (int s = 0; s < Kp / 16; ++s) {
+                    const uint64_t db = tc::k_major_desc(sb, s, Kp);
+                    tc::mma_f16(taddr, tc::k_major_desc(sa, s, Kp), db, idesc, (t > 0 || s > 0) ? 1u : 0u);
+                    if (kSplit) tc::mma_f16(taddr, tc::k_major_desc(sa + (uint32_t)P.bytesA, s, Kp), db, idesc, 1u);
+                }
+                tc::mma_commit(&bar[b]);
+            }
+            pend[b] = 1u;
+        }
+        wait_buf(0);
+        wait_buf(1);
+        ok = __syncthreads_and(ok) != 0;
+        if (!ok) break;
+        tc::fence_after_sync();
+        // epilogue: this thread's row, 16 columns at a time
+        for (int c = 0; c < Np; c += 16) {
+            uint32_t r[16];
+            tc::tmem_ld16(tc::tmem_addr(taddr, 32 * warp, c), r);
+            tc::tmem_wait_ld();
+            if (!vin) continue;
 #pragma unroll
-    for (int k = 0; k < kWgMaxPer; ++k) {
-        const int o = threadIdx.x + k * kWgThreads;
-        if (o < nout) part[o] = acc[k];
+            for (int h = 0; h < 2; ++h) {
+                const int c0 = c + 8 * h;
+                if (c0 >= N) break;
+                float o[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    float val = __uint_as_float(r[8 * h + j]) + (bias ? bias[c0 + j] : 0.0f);
+                    o[j] = relu ? fmaxf(val, 0.0f) : val;
+                }
+                store8(out + v * N + c0, o);
+            }
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+    }
+    if (!ok) {
+        if (tid == 0) atomicOr(err, 1u);
+        // give MMAs still in flight a bounded time to finish before the TMEM is released
+        for (int b = 0; b < 2; ++b)
+            if (pend[b]) tc::mbar_wait(&bar[b], phase[b], 1u << 16);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(taddr, ncols);
+    }
+}
+
+// Weight gradient on the tensor core: part[slice][t][ci][co] = sum over the slice's voxels v of
+// in[v + off(t)][ci] g[v][co].  Rows M are the (tap, input channel) pairs, 128 per CTA (grid.x);
+// N the output channels; K the voxels, 64 per stage, double-buffered.  Both operands are
+// MN-major in shared memory: a 16-byte chunk holds 8 consecutive channels of one voxel, as the
+// channels-last tensors store them.  The FP32 gradient enters as hi + lo BF16 parts.  Each CTA
+// (grid.y) owns a fixed voxel slice, and the slices are summed in a fixed order afterwards, so the
+// gradient is deterministic.
+constexpr int kWgK = 64;   // voxels per stage
+__host__ __device__ inline size_t wgrad_tc_smem(int Np) {
+    return 2 * ((size_t)128 * kWgK * 2 + 2 * (size_t)Np * kWgK * 2);
+}
+__global__ void __launch_bounds__(128, 1) k_conv3_wgrad_tc(Vol g, int cin, int cout, int Np, int64_t vslice,
+                                                           const bf16* __restrict__ in, const float* __restrict__ gout,
+                                                           float* __restrict__ part, uint32_t* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t bar[2];
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int rows = 27 * cin;
+    const int r0 = blockIdx.x * 128;
+    const size_t bytesA = (size_t)128 * kWgK * 2, bytesB = (size_t)Np * kWgK * 2;
+    const size_t stage_bytes = bytesA + 2 * bytesB;
+    const uint32_t ncols = tc::tmem_cols(Np);
+    if (warp == 0) {
+        tc::tmem_alloc(&tbase, ncols);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t taddr = tbase;
+    const uint32_t idesc = tc::idesc_f16(128, Np, tc::kFmtBF16, 1, 1);
+    const int64_t v0 = (int64_t)blockIdx.y * vslice;
+    const int64_t v1 = v0 + vslice < g.nv ? v0 + vslice : g.nv;
+    const int64_t pxy = (int64_t)g.px * g.py;
+    uint32_t phase[2] = {0u, 0u}, pend[2] = {0u, 0u};
+    bool ok = true;
+    int step = 0;
+    for (int64_t vb = v0; vb < v1; vb += kWgK, ++step) {
+        const int b = step & 1;
+        if (pend[b]) {
+            ok = tc::mbar_wait(&bar[b], phase[b]) && ok;
+            phase[b] ^= 1u;
+            pend[b] = 0u;
+        }
+        unsigned char* sa = smem + (size_t)b * stage_bytes;
+        unsigned char* sbh = sa + bytesA;
+        unsigned char* sbl = sbh + bytesB;
+        // A: 16 row groups (8 channels of one tap) x 64 voxels
+        for (int idx = tid; idx < 16 * kWgK; idx += 128) {
+            const int k = idx % kWgK, mg = idx / kWgK;   // consecutive threads: consecutive voxels
+            const int r = r0 + mg * 8;
+            const int64_t v = vb + k;
+            uint4 val = make_uint4(0, 0, 0, 0);
+            if (r < rows && v < v1) {
+                const int t = r / cin, ci = r % cin;
+                const int x = (int)(v % g.px) + t % 3 - 1, y = (int)((v / g.px) % g.py) + (t / 3) % 3 - 1,
+                          z = (int)(v / pxy) + t / 9 - 1;
+                if (x >= 0 && x < g.px && y >= 0 && y < g.py && z >= 0 && z < g.pz)
+                    val = __ldg(reinterpret_cast<const uint4*>(in + ((int64_t)x + (int64_t)g.px * (y + (int64_t)g.py * z)) * cin + ci));
+            }
+            *reinterpret_cast<uint4*>(sa + tc::mn_major_offset(mg * 8, k, 128)) = val;
+        }
+        // B: Np / 8 groups of output channels x 64 voxels, hi and lo parts
+        for (int idx = tid; idx < (Np / 8) * kWgK; idx += 128) {
+            const int k = idx % kWgK, ng = idx / kWgK;
+            const int64_t v = vb + k;
+            uint4 hi = make_uint4(0, 0, 0, 0), lo = make_uint4(0, 0, 0, 0);
+            if (ng * 8 < cout && v < v1) split8(gout + v * cout + ng * 8, hi, lo);
+            const uint32_t off = tc::mn_major_offset(ng * 8, k, Np);
+            *reinterpret_cast<uint4*>(sbh + off) = hi;
+            *reinterpret_cast<uint4*>(sbl + off) = lo;
+        }
+        tc::fence_proxy_async();
+        tc::fence_before_sync();
+        ok = __syncthreads_and(ok) != 0;
+        if (!ok) break;
+        tc::fence_after_sync();
+        if (tid == 0) {
+            const uint32_t a = tc::smem_u32(sa), bh = tc::smem_u32(sbh), bl = tc::smem_u32(sbl);
+            for (int s = 0; s < kWgK / 16; ++s) {
+                const uint64_t da = tc::mn_major_desc(a, s, 128);
+                tc::mma_f16(taddr, da, tc::mn_major_desc(bh, s, Np), idesc, (step > 0 || s > 0) ? 1u : 0u);
+                tc::mma_f16(taddr, da, tc::mn_major_desc(bl, s, Np), idesc, 1u);
+            }
+            tc::mma_commit(&bar[b]);
+        }
+        pend[b] = 1u;
+    }
+    for (int b = 0; b < 2; ++b)
+        if (pend[b]) {
+            ok = tc::mbar_wait(&bar[b], phase[b]) && ok;
+            phase[b] ^= 1u;
+            pend[b] = 0u;
+        }
+    ok = __syncthreads_and(ok) != 0;
+    tc::fence_after_sync();
+    const int r = r0 + tid;
+    float* dst = part + ((int64_t)blockIdx.y * rows + r) * cout;
+    for (int c = 0; c < Np && ok; c += 16) {
+        uint32_t v[16];
+        tc::tmem_ld16(tc::tmem_addr(taddr, 32 * warp, c), v);
+        tc::tmem_wait_ld();
+        if (r >= rows) continue;
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            if (c + j < cout) dst[c + j] = step > 0 ? __uint_as_float(v[j]) : 0.0f;
+    }
+    if (!ok && tid == 0) atomicOr(err, 1u);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(taddr, ncols);
     }
 }
 
@@ -365,47 +564,91 @@ __global__ void k_adam(int64_t n, float* __restrict__ p, const float* __restrict
 // ------------------------------------------------------------------------------------------
 static unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
-static size_t conv_smem(int cin) { return (size_t)27 * cin * 8 * sizeof(bf16); }
-static size_t wgrad_smem(int cin, int cout) { return (size_t)kWgTile * (cin + cout) * sizeof(float); }
-
-template <typename TI, typename TO>
-static void conv_launch(Context& c, const Vol& g, int cin, int cout, const TI* in, const bf16* W, const float* bias,
-                        TO* out, bool relu) {
-    const size_t smem = conv_smem(cin);
-    static bool attr_set = false;   // per instantiation; the attribute is per device function
-    if (!attr_set) {
-        UWG_CUDA(cudaFuncSetAttribute(k_conv3<TI, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        attr_set = true;
-    }
-    UWG_REQUIRE(smem <= 200 * 1024, UWGPU_ERR_ARGUMENT, "U-Net layer too wide for the convolution kernel");
-    dim3 grid(nblk(g.nv, 128), cout / 8);
-    LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
-    k_conv3<TI, TO><<<grid, 128, smem, c.stream>>>(g, cin, cout, in, W, bias, out, relu ? 1 : 0);
-    note_work(c, UWGPU_KERNEL_LEARNED, (double)g.nv * (cin * sizeof(TI) + cout * sizeof(TO)),
-              2.0 * 27.0 * cin * cout * (double)g.nv);
+static int sm_count(Context& c) {
+    int n = 0;
+    UWG_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, c.device));
+    return n > 0 ? n : 1;
 }
 
-static void wgrad_launch(Context& c, const Vol& g, int cin, int cout, const bf16* in, const float* gout, float* dW,
-                         DArray<float>& part) {
-    UWG_REQUIRE((int64_t)cin * cout <= (int64_t)kWgThreads * kWgMaxPer, UWGPU_ERR_ARGUMENT,
-                "U-Net layer too wide for the weight-gradient kernel");
-    static bool attr_set = false;
+constexpr size_t kSmemPerSm = 227 * 1024;   // dynamic shared memory one CTA may use
+
+// Dynamic shared memory to request so that at most 512 / ncols CTAs of a kernel share an SM: the
+// SM's 512 TMEM columns then cover every resident CTA's allocation, and no CTA waits for another
+// one's columns.  Returns the request and the number of CTAs per SM it allows.
+static size_t tmem_safe_smem(size_t need, uint32_t ncols, int* per_sm) {
+    const int max_cta = (int)(512 / ncols) < 16 ? (int)(512 / ncols) : 16;
+    size_t req = need;
+    const size_t floor_bytes = kSmemPerSm / (size_t)(max_cta + 1) + 1024;
+    if (req < floor_bytes) req = floor_bytes;
+    int fit = (int)(kSmemPerSm / req);
+    *per_sm = fit < max_cta ? (fit > 0 ? fit : 1) : max_cta;
+    return req;
+}
+
+void check_errors(Context& c, Net& n) {
+    if (!n.tc_err.p) return;
+    uint32_t e = 0;
+    UWG_CUDA(cudaMemcpyAsync(&e, n.tc_err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream));
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+    if (e) {
+        UWG_CUDA(cudaMemsetAsync(n.tc_err.p, 0, sizeof(uint32_t), c.stream));
+        throw Error(UWGPU_ERR_CUDA, "U-Net tensor-core kernel: an MMA did not complete in time");
+    }
+}
+
+// 3x3x3 convolution on the tensor core (k_conv3_tc).  W: the layer's weights as the convolution
+// reads them ([27][K][N]); Wrev: the layer's other packing ([27][N][K] in reverse tap order).
+template <typename TI, typename TO>
+static void conv_launch_tc(Context& c, Net& n, const Vol& g, int K, int N, const TI* in, const bf16* Wrev,
+                           const float* bias, TO* out, bool relu) {
+    const ConvTcPlan P = conv_tc_plan(K, N, sizeof(TI) == 4);
+    UWG_REQUIRE(P.smem <= kSmemPerSm && P.Np <= 256, UWGPU_ERR_ARGUMENT, "U-Net layer too wide for the tensor-core convolution");
+    static bool attr_set = false;   // per instantiation
     if (!attr_set) {
-        UWG_CUDA(cudaFuncSetAttribute(k_conv3_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+        UWG_CUDA(cudaFuncSetAttribute(k_conv3_tc<TI, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemPerSm));
         attr_set = true;
     }
-    const int slices = kWgSlices;
-    const int64_t vslice = (g.nv + slices - 1) / slices;
-    const int64_t nw = (int64_t)27 * cin * cout;
+    int per_sm = 1;
+    const size_t smem = tmem_safe_smem(P.smem, tc::tmem_cols(P.Np), &per_sm);
+    const int64_t ntiles = (g.nv + 127) / 128;
+    const int64_t cap = (int64_t)sm_count(c) * per_sm;
+    const unsigned grid = (unsigned)(ntiles < cap ? ntiles : cap);
+    LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
+    k_conv3_tc<TI, TO><<<grid, 128, smem, c.stream>>>(g, K, N, P, in, Wrev, bias, out, relu ? 1 : 0, n.tc_err.p);
+    note_work(c, UWGPU_KERNEL_LEARNED, (double)g.nv * (K * sizeof(TI) + N * sizeof(TO)),
+              2.0 * 27.0 * K * N * (double)g.nv * (sizeof(TI) == 4 ? 2.0 : 1.0));
+}
+
+static void wgrad_launch_tc(Context& c, Net& n, const Vol& g, int cin, int cout, const bf16* in, const float* gout,
+                            float* dW, DArray<float>& part) {
+    const int Np = (cout + 15) / 16 * 16;
+    UWG_REQUIRE(Np <= 256, UWGPU_ERR_ARGUMENT, "U-Net layer too wide for the tensor-core weight gradient");
+    static bool attr_set = false;
+    if (!attr_set) {
+        UWG_CUDA(cudaFuncSetAttribute(k_conv3_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemPerSm));
+        attr_set = true;
+    }
+    int per_sm = 1;
+    const size_t smem = tmem_safe_smem(wgrad_tc_smem(Np), tc::tmem_cols(Np), &per_sm);
+    const int rows = 27 * cin;
+    const int mtiles = (rows + 127) / 128;
+    int64_t slices = (2LL * sm_count(c) + mtiles - 1) / mtiles;
+    const int64_t max_slices = (g.nv + 511) / 512;
+    if (slices > max_slices) slices = max_slices;
+    if (slices < 1) slices = 1;
+    int64_t vslice = (g.nv + slices - 1) / slices;
+    vslice = (vslice + kWgK - 1) / kWgK * kWgK;
+    slices = (g.nv + vslice - 1) / vslice;
+    const int64_t nw = (int64_t)rows * cout;
     part.ensure((size_t)slices * nw);
     {
         LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
-        k_conv3_wgrad<<<dim3(slices, 27), kWgThreads, wgrad_smem(cin, cout), c.stream>>>(g, cin, cout, 27, in, gout,
-                                                                                         part.p, vslice);
+        k_conv3_wgrad_tc<<<dim3(mtiles, (unsigned)slices), 128, smem, c.stream>>>(g, cin, cout, Np, vslice, in, gout,
+                                                                                 part.p, n.tc_err.p);
     }
     LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
-    k_sum_slices<<<nblk(nw, 256), 256, 0, c.stream>>>(nw, slices, part.p, dW);
-    note_work(c, UWGPU_KERNEL_LEARNED, (double)g.nv * 27.0 * (cin * 2 + cout * 4), 2.0 * 27.0 * cin * cout * (double)g.nv);
+    k_sum_slices<<<nblk(nw, 256), 256, 0, c.stream>>>(nw, (int)slices, part.p, dW);
+    note_work(c, UWGPU_KERNEL_LEARNED, (double)g.nv * 27.0 * (cin * 2 + cout * 4), 4.0 * 27.0 * cin * cout * (double)g.nv);
 }
 
 static void bias_grad_launch(Context& c, int64_t nv, int cout, const float* gout, float* db, DArray<float>& part) {
@@ -533,6 +776,8 @@ void create(Context& c, Net& n, int levels, int base, uint64_t seed) {
         cv.w16.ensure((size_t)27 * cv.cin * cv.cout);
         cv.wflip.ensure((size_t)27 * cv.cin * cv.cout);
     }
+    n.tc_err.ensure(1);
+    UWG_CUDA(cudaMemset(n.tc_err.p, 0, sizeof(uint32_t)));
     pack(c, n);
 }
 
@@ -552,8 +797,9 @@ void forward(Context& c, Net& n) {
         const Conv& a = n.convs[n.enc(l, 0)];
         const Conv& b = n.convs[n.enc(l, 1)];
         const bf16* in = l == 0 ? n.x0.p : n.pool[l - 1].p;
-        conv_launch<bf16, bf16>(c, g, a.cin, a.cout, in, a.w16.p, n.params.p + a.b_off, n.enc_a[l].p, true);
-        conv_launch<bf16, bf16>(c, g, b.cin, b.cout, n.enc_a[l].p, b.w16.p, n.params.p + b.b_off, n.enc_b[l].p, true);
+        conv_launch_tc<bf16, bf16>(c, n, g, a.cin, a.cout, in, a.wflip.p, n.params.p + a.b_off, n.enc_a[l].p, true);
+        conv_launch_tc<bf16, bf16>(c, n, g, b.cin, b.cout, n.enc_a[l].p, b.wflip.p, n.params.p + b.b_off, n.enc_b[l].p,
+                                   true);
         if (l + 1 < L) {
             const int64_t cnt = n.vol[l + 1].nv * n.ch[l];
             LaunchScope ls(c, UWGPU_KERNEL_LEARNED);
@@ -572,8 +818,10 @@ void forward(Context& c, Net& n) {
         }
         const Conv& a = n.convs[n.dec(l, 0)];
         const Conv& b = n.convs[n.dec(l, 1)];
-        conv_launch<bf16, bf16>(c, g, a.cin, a.cout, n.dec_cat[l].p, a.w16.p, n.params.p + a.b_off, n.dec_a[l].p, true);
-        conv_launch<bf16, bf16>(c, g, b.cin, b.cout, n.dec_a[l].p, b.w16.p, n.params.p + b.b_off, n.dec_b[l].p, true);
+        conv_launch_tc<bf16, bf16>(c, n, g, a.cin, a.cout, n.dec_cat[l].p, a.wflip.p, n.params.p + a.b_off, n.dec_a[l].p,
+                                   true);
+        conv_launch_tc<bf16, bf16>(c, n, g, b.cin, b.cout, n.dec_a[l].p, b.wflip.p, n.params.p + b.b_off, n.dec_b[l].p,
+                                   true);
     }
     const bf16* fin = L == 1 ? n.enc_b[0].p : n.dec_b[0].p;
     {
@@ -588,9 +836,11 @@ void forward(Context& c, Net& n) {
 // gradient of its input (post-activation of the layer below) into gin
 static void conv_backward(Context& c, Net& n, const Vol& g, const Conv& cv, const bf16* in, const float* gpre,
                           float* gin) {
-    wgrad_launch(c, g, cv.cin, cv.cout, in, gpre, n.grads.p + cv.w_off, n.part);
+    wgrad_launch_tc(c, n, g, cv.cin, cv.cout, in, gpre, n.grads.p + cv.w_off, n.part);
     bias_grad_launch(c, g.nv, cv.cout, gpre, n.grads.p + cv.b_off, n.part);
-    conv_launch<float, float>(c, g, cv.cout, cv.cin, gpre, cv.wflip.p, nullptr, gin, false);
+    // the data gradient is the convolution with W'[t][co][ci] = W[26 - t][ci][co]; its other
+    // packing, read in reverse tap order, is the plain W
+    conv_launch_tc<float, float>(c, n, g, cv.cout, cv.cin, gpre, cv.w16.p, nullptr, gin, false);
 }
 
 void backward(Context& c, Net& n) {
@@ -682,6 +932,7 @@ void set_input_host(Context& c, Net& n, const float* input) {
 }
 
 void get_output_host(Context& c, Net& n, float* output) {
+    check_errors(c, n);
     DArray<float> tmp;
     tmp.ensure((size_t)n.nn * 3);
     {
@@ -723,6 +974,7 @@ void set_grad_output_host(Context& c, Net& n, const float* grad) {
 }
 
 void get_input_grad_host(Context& c, Net& n, float* grad_input) {
+    check_errors(c, n);
     DArray<float> tmp;
     tmp.ensure((size_t)n.nn * kUsedChannels);
     {
@@ -1088,6 +1340,7 @@ void train(Context& c, Net& n, int epochs, int batch, float lr, uint64_t seed, d
     UWG_CUDA(cudaMemcpyAsync(c.host_scalars, dl.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     UWG_CUDA(cudaStreamSynchronize(c.stream));
     if (holdout_ratio) *holdout_ratio = c.host_scalars[0] / nhold;
+    check_errors(c, n);
 }
 
 }  // namespace unet

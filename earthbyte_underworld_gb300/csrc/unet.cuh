@@ -58,6 +58,7 @@ struct Net {
     DArray<float> gout, g_enc_a[kMaxLevels], g_enc_b[kMaxLevels], g_in[kMaxLevels];
     DArray<float> g_dec_a[kMaxLevels], g_dec_b[kMaxLevels], g_cat[kMaxLevels];
     DArray<float> part;                           // per-block partial gradients (ordered sums)
+    DArray<uint32_t> tc_err;                      // set by a tensor-core kernel whose MMA wait timed out
 
     int enc(int l, int k) const { return 2 * l + k; }
     int dec(int l, int k) const { return 2 * levels + 2 * l + k; }
@@ -80,6 +81,9 @@ void get_output_host(Context& c, Net& n, float* output);
 void set_grad_output_host(Context& c, Net& n, const float* grad);
 void get_input_grad_host(Context& c, Net& n, float* grad_input);
 
+// Throws (and clears the flag) when a tensor-core kernel of the network gave up waiting for its
+// MMAs; synchronises the stream.
+void check_errors(Context& c, Net& n);
 // node log10 viscosity from the assembled material points (needed before correct / training)
 void prepare_viscosity(Context& c, Net& n);
 // z += network correction for residual r, z holding the V-cycle's answer V(r) (node SoA [3][nn])

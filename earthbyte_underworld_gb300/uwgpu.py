@@ -39,6 +39,8 @@ SCHUR_PC_NONE = 2
 SCHUR_PC_SCALED_BFBT = 3
 SMOOTHER_COLOUR_GS = 0
 SMOOTHER_CHEBYSHEV = 1
+ASSEMBLY_FP64 = 0
+ASSEMBLY_TENSOR = 1
 
 KERNEL_ASSEMBLY, KERNEL_APPLY, KERNEL_SMOOTH, KERNEL_BINNING, KERNEL_SCHUR_PC, KERNEL_VECTOR, KERNEL_TRANSFER, \
     KERNEL_LEARNED = range(8)
@@ -144,6 +146,8 @@ def load(build_if_missing: bool = True):
         L.uwgpu_particles_download.argtypes = [P, P, P, P]
         L.uwgpu_learned_generate.argtypes = [P, P, C.c_int32, C.c_uint64]
         L.uwgpu_learned_train.argtypes = [P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P, P]
+        L.uwgpu_tc_check.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P, P]
+        L.uwgpu_assembly_set.argtypes = [P, C.c_int32]
         _lib = L
         return _lib
 
@@ -279,6 +283,10 @@ class Context:
         self._check(self._L.uwgpu_bin_and_map(self._h, _ptr(perm), _ptr(offsets), _ptr(xi)))
         return perm, offsets, xi
 
+    def assembly_set(self, mode):
+        """ASSEMBLY_FP64 (default) or ASSEMBLY_TENSOR (tensor-core contraction of the moments, 3D)."""
+        self._check(self._L.uwgpu_assembly_set(self._h, int(mode)))
+
     def assemble(self):
         self._check(self._L.uwgpu_assemble(self._h))
 
@@ -392,6 +400,17 @@ class Context:
         ms = C.c_double()
         self._check(self._L.uwgpu_time_chebyshev(self._h, precision, degree, iterations, C.byref(ms)))
         return ms.value
+
+    def tc_check(self, a, b, layout=0, fmt=1):
+        """Tensor-core self-check: a (128, k) and b (n, k) arrays of 16-bit patterns (uint16: bfloat16
+        bits for fmt 1, half bits for fmt 0) -> a @ b.T (128, n) FP32 from one tcgen05 MMA sequence."""
+        a = np.ascontiguousarray(a, dtype=np.uint16)
+        b = np.ascontiguousarray(b, dtype=np.uint16)
+        assert a.shape[0] == 128 and a.shape[1] == b.shape[1]
+        d = np.zeros((128, b.shape[0]), np.float32)
+        self._check(self._L.uwgpu_tc_check(self._h, int(layout), int(fmt), b.shape[0], a.shape[1], _ptr(a), _ptr(b),
+                                           _ptr(d)))
+        return d
 
     def stream(self) -> int:
         s = C.c_void_p()

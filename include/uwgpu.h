@@ -240,6 +240,16 @@ int uwgpu_integration_points(uwgpu_ctx* ctx, double* xi, double* w);
  * Results stay on the device. */
 int uwgpu_assemble(uwgpu_ctx* ctx);
 
+/* How the next assemblies contract the per-element moments into K_e (3D; 2D always uses FP64):
+ * UWGPU_ASSEMBLY_FP64 (default): FP64 arithmetic on the CUDA cores, the drop-in form.
+ * UWGPU_ASSEMBLY_TENSOR: the 63 pair tables of every element are one batched product of the
+ * moments with a small integer matrix, run on the tcgen05 tensor core in FP16 with FP64 accuracy
+ * (each moment cut into five 11-bit slices, every slice product exact in the FP32 accumulator;
+ * Ozaki, Ogita, Oishi and Rump, Numer. Algorithms 59, 2012); relative error of K_e about 2^-53.
+ * Replaces the B^T D B accumulation of ConstitutiveMatrixCartesian.c:388-407 in the same way. */
+enum { UWGPU_ASSEMBLY_FP64 = 0, UWGPU_ASSEMBLY_TENSOR = 1 };
+int uwgpu_assembly_set(uwgpu_ctx* ctx, int32_t mode);
+
 /* Per-element results of the last assembly, copied to the host: the per-element callback
  * StiffnessMatrixTerm_AssembleElementFunction (StgFEM/SLE/SystemSetup/src/StiffnessMatrixTerm.c
  * :247-266) reads element e from here.  Ke: count*(nd*nd) row-major, dof = node*dim + comp;
@@ -325,6 +335,14 @@ int uwgpu_time_smooth(uwgpu_ctx* ctx, int32_t precision, int32_t sweeps, int32_t
  * inner CG's operator kernel in that form, elapsed device milliseconds in ms. */
 int uwgpu_bfbt_operator_apply(uwgpu_ctx* ctx, int32_t form, const double* x, double* y);
 int uwgpu_time_bfbt_apply(uwgpu_ctx* ctx, int32_t form, int32_t iterations, double* ms);
+
+/* Tensor-core self-check (no reference counterpart): D = A B^T for A 128 x k and B n x k (row-major
+ * 16-bit values: bfloat16 bits for format 1, IEEE half bits for format 0), D 128 x n FP32, computed
+ * by one tcgen05 MMA sequence with the operands staged in shared memory in the layout `layout`
+ * (0: both K-major, 2: both MN-major, 4: A K-major and B MN-major; odd values exchange the
+ * descriptors' two stride fields, a diagnostic).  n and k: multiples of 16, 16..256. */
+int uwgpu_tc_check(uwgpu_ctx* ctx, int32_t layout, int32_t format, int32_t n, int32_t k, const uint16_t* a,
+                   const uint16_t* b, float* d);
 
 /* Allocation-free binning + mapping.  This entry point has no counterpart in the reference; it
  * exists for callers that cannot allocate device memory while they run (a host framework that

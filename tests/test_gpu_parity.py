@@ -65,6 +65,33 @@ def test_binning_and_assembly_parity(oracle, uw, case):
     ctx.close()
 
 
+@pytest.mark.parametrize("case", ["spheres", "grf", "layers"])
+def test_tensor_core_contraction_matches_oracle(oracle, uw, case):
+    """The tensor-core contraction of the moments (FP16 slices on tcgen05, FP64-accurate) gives the
+    oracle's element matrices to the FP64 path's 1e-12, element by element, and the FP64 path's
+    own K_e to a few ulps."""
+    from earthbyte_underworld_gb300 import workloads as W
+    O, U = oracle, uw
+    w = {"spheres": lambda: W.spheres(nel=(8, 6, 10), nspheres=12, seed=4),
+         "grf": lambda: W.grf(nel=(12, 10, 9), ppc=30, grid=32),
+         "layers": lambda: W.layers(nel=(6, 6, 8), ppc=40)}[case]()
+    with U.Context(0) as ctx:
+        W.setup_context(ctx, w)
+        ctx.bin_and_map(want=False)
+        ctx.assemble()
+        K64, f64, G64, S64 = ctx.element_matrices()
+        ctx.assembly_set(U.ASSEMBLY_TENSOR)
+        ctx.assemble()
+        Ktc, ftc, Gtc, Stc = ctx.element_matrices()
+    m, ooff, operm, oxi, oKe, ofe, oGe, oSe, oeta = _oracle(O, w)
+    E = len(oKe)
+    per_el = np.linalg.norm((Ktc - oKe).reshape(E, -1), axis=1) / np.linalg.norm(oKe.reshape(E, -1), axis=1)
+    assert per_el.max() < 1e-12
+    assert _rel(Ktc, K64) < 1e-14
+    assert _rel(Stc, oSe) < 1e-12
+    assert np.array_equal(ftc, f64) and np.array_equal(Gtc, G64)
+
+
 def test_golden_matrices_through_gpu(oracle, uw):
     """The reference golden K (2D 10x10, Gauss 2x2, Arrhenius + limiter on the sinusoid temperature)
     reproduced by the GPU path with the Gauss points as material points."""

@@ -30,9 +30,10 @@ def _mats_oracle(O, mats):
     return out
 
 
-def _assembly_parity_at_size(O, U, W, w, chunk=1 << 17):
+def _assembly_parity_at_size(O, U, W, w, chunk=1 << 17, mode=0):
     with U.Context(0) as ctx:
         W.setup_context(ctx, w)
+        ctx.assembly_set(mode)
         perm, offsets, xi = ctx.bin_and_map()
         ctx.assemble()
         dim = w["dim"]
@@ -43,7 +44,9 @@ def _assembly_parity_at_size(O, U, W, w, chunk=1 << 17):
         # integer work: bit-exact
         assert np.array_equal(offsets, ooff)
         assert np.array_equal(perm, operm)
-        assert np.max(np.abs(xi - oxi)) < 1e-13
+        # local coordinates: closed form against Newton; the rounding of (x - x0) / h grows with the
+        # number of elements per axis: 8 eps per element count
+        assert np.max(np.abs(xi - oxi)) < 8 * np.finfo(np.float64).eps * max(w["nel"])
         del xi
         f = O.make_fields(temperature=w.get("temperature"), gravity=w["gravity"], vert_axis=w["vert_axis"])
         mats = _mats_oracle(O, w["materials"])
@@ -67,9 +70,11 @@ def _assembly_parity_at_size(O, U, W, w, chunk=1 << 17):
     assert worst["fe"] < 1e-12 and worst["Ge"] < 1e-12 and worst["Se"] < 1e-12
 
 
-def test_grf128_binning_and_assembly_at_size(oracle, uw):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_grf128_binning_and_assembly_at_size(oracle, uw, mode):
+    """mode 0: FP64 contraction; mode 1: the tensor-core contraction (the mixed form's assembly)."""
     from earthbyte_underworld_gb300 import workloads as W
-    _assembly_parity_at_size(oracle, uw, W, W.grf(nel=(128, 128, 128), ppc=30, seed=11, grid=256, corr=0.1))
+    _assembly_parity_at_size(oracle, uw, W, W.grf(nel=(128, 128, 128), ppc=30, seed=11, grid=256, corr=0.1), mode=mode)
 
 
 def test_spheres64_binning_and_assembly_at_size(oracle, uw):
