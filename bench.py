@@ -56,7 +56,11 @@ def parse():
     ap.add_argument("--mode", default="step", choices=["step", "kernels", "bfbt"],
                     help="step: the full hot-path step; kernels: operator apply and smoother only")
     ap.add_argument("--iters", type=int, default=20, help="launches per kernel in --mode kernels")
-    ap.add_argument("--cpu-nel", type=int, default=16, help="mesh of the CPU baseline sample")
+    ap.add_argument("--cpu-nel", type=int, default=20, help="mesh of the CPU baseline sample")
+    ap.add_argument("--no-learned", action="store_true", help="skip the mixed+learned leg")
+    ap.add_argument("--learn-nel", type=int, default=64, help="mesh the U-Net is trained on (then transferred)")
+    ap.add_argument("--learn-rhs", type=int, default=40, help="multigrid solves that give the training pairs")
+    ap.add_argument("--learn-epochs", type=int, default=12)
     return ap.parse_args()
 
 
@@ -283,6 +287,34 @@ def run_reference(args):
 # ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
+def train_learned(U, W, args, local, skw):
+    """The U-Net of the mixed+learned form (4 levels, 16/32/64/128 channels), trained on the GPU with
+    the library's own kernels on residual/error pairs of plain multigrid solves of the same workload
+    family on a smaller mesh (args.learn_nel^3); its weights then serve the benchmark's mesh (the
+    network is convolutional, so the same parameters apply on any grid).  Outside the timed region."""
+    t0 = time.perf_counter()
+    wt = make_workload(args.workload, args.learn_nel)
+    with U.Context(local) as tctx:
+        W.setup_context(tctx, wt)
+        tctx.bin_and_map(want=False)
+        tctx.assemble()
+        kw = dict(skw)
+        kw["mg_levels"] = max(2, kw["mg_levels"] - 1)
+        opts = U.default_opts(precision=U.PREC_FP64, **kw)
+        tctx.learned_create(levels=4, base=16, seed=1)
+        t1 = time.perf_counter()
+        tctx.learned_generate(opts, nsamples=12 * args.learn_rhs, seed=7)
+        t2 = time.perf_counter()
+        loss, hold = tctx.learned_train(epochs=args.learn_epochs, batch=8, lr=1e-3, seed=2)
+        t3 = time.perf_counter()
+        params = tctx.learned_params()
+    return params, {"network": "3D U-Net, 4 levels, 16/32/64/128 channels", "parameters": int(params.size),
+                    "trained_on": f"{workload_name(args.workload, args.learn_nel)}",
+                    "pairs": 12 * args.learn_rhs, "multigrid_solves": args.learn_rhs, "epochs": args.learn_epochs,
+                    "train_loss": loss, "holdout_error_ratio": hold,
+                    "generate_s": t2 - t1, "train_s": t3 - t2, "total_s": time.perf_counter() - t0}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -302,8 +334,17 @@ def run_ours(args):
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
     flush_buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
 
-    def opts_for(prec):
-        return U.default_opts(precision=U.PREC_MIXED if prec == "mixed" else U.PREC_FP64, **skw)
+    def opts_for(prec, learned=False):
+        o = U.default_opts(precision=U.PREC_MIXED if prec != "fp64" else U.PREC_FP64, **skw)
+        if learned:
+            o.learned_pc = 1
+            o.learned_stagnation = 2
+        return o
+
+    def use_assembly(prec):
+        # the mixed forms contract the element moments on the tensor core (FP64-accurate FP16
+        # slices); the FP64 drop-in keeps the FP64 contraction
+        ctx.assembly_set(U.ASSEMBLY_TENSOR if prec != "fp64" else U.ASSEMBLY_FP64)
 
     def step(opts):
         ctx.bin_and_map(want=False)
@@ -347,19 +388,37 @@ def run_ours(args):
             for name, fam in (("assembly", U.KERNEL_ASSEMBLY), ("apply", U.KERNEL_APPLY),
                               ("smooth", U.KERNEL_SMOOTH), ("binning", U.KERNEL_BINNING),
                               ("schur_pc", U.KERNEL_SCHUR_PC), ("vector", U.KERNEL_VECTOR),
-                              ("transfer", U.KERNEL_TRANSFER)):
+                              ("transfer", U.KERNEL_TRANSFER), ("learned", U.KERNEL_LEARNED)):
                 n, t = ctx.profile_read(fam)
                 b, f = ctx.profile_work(fam)
                 prof[name] = {"launches": n, "ms": t, "bytes": b, "flops": f}
             ctx.profile_enable(False)
         return ms, wall, launches, reps, clk, prof
 
+    def leg_summary(name, ms, reps, clk, prof):
+        r = reps[-1]
+        return {"form": name, "value": dist.sum(npts) / (dist.max(ms) / 1e3 / args.steps),
+                "ms_per_step": dist.max(ms) / args.steps, "stokes_solve_s": r.t_solve_ms / 1e3,
+                "setup_ms": r.t_setup_ms, "rel_residual": r.rel_residual, "outer_its": r.outer_its,
+                "inner_its": r.inner_its_total, "vcycles": r.vcycles, "pc_inner_its": r.pc_inner_its,
+                "learned_applies": r.learned_applies, "learned_fallbacks": r.learned_fallbacks, "clocks": clk,
+                "kernels": {k: {"launches": v["launches"], "ms": v["ms"]} for k, v in prof.items()}}
+
     prec = args.precision
-    ms, wall, launches, reps, clk, _ = timed(opts_for(prec), profile=False)
+    learned = prec == "mixed" and not args.no_learned
+    learn_info = None
+    if learned:
+        params, learn_info = train_learned(U, W, args, local, skw)
+        ctx.learned_create(levels=4, base=16, seed=1)
+        ctx.learned_set_params(params)
+    head = "mixed+learned" if learned else prec
+    use_assembly(head)
+    head_opts = opts_for(head, learned=learned)
+    ms, wall, launches, reps, clk, _ = timed(head_opts, profile=False)
     # One more step of the same workload with every launch of the profiled kernel families
     # bracketed by CUDA events on the library stream: the per-family times and the roofline come
     # from it (the events add host work, so the timed steps above run without them).
-    _, _, _, _, _, prof = timed(opts_for(prec), profile=True, warmup=0, steps=1)
+    _, _, _, _, _, prof = timed(head_opts, profile=True, warmup=0, steps=1)
     ms_max = dist.max(ms)
     step_ms = ms_max / args.steps
     value = dist.sum(npts) / (ms_max / 1e3 / args.steps)
@@ -375,45 +434,56 @@ def run_ours(args):
               "achieved_GB_per_s": d["bytes"] / (d["ms"] / 1e3) / 1e9 if d["ms"] > 0 else 0.0,
               "fp_TFLOP_per_s": d["flops"] / (d["ms"] / 1e3) / 1e12 if d["ms"] > 0 else 0.0,
               "note": FAMILY_NOTES.get(dom, "")}
-    # assembly (rheology + K_e, f_e, G_e, S_e; the DVC pass too when selected): points assembled per
-    # second, and the kernel's place against HBM and against the FP64 rate, which bounds it
-    a_ = prof.get("assembly", {})
-    assembly = None
-    if a_.get("ms", 0) > 0:
-        assembly = {"points_per_s": npts / (a_["ms"] / 1e3), "ms": a_["ms"],
-                    "GB_per_s": a_["bytes"] / (a_["ms"] / 1e3) / 1e9,
-                    "frac_hbm": a_["bytes"] / (a_["ms"] / 1e3) / 1e9 / peak,
-                    "fp64_TFLOP_per_s": a_["flops"] / (a_["ms"] / 1e3) / 1e12,
-                    "frac_fp64": a_["flops"] / (a_["ms"] / 1e3) / 1e12 / FP64_TFLOPS,
-                    "note": f"FP64 work (moment accumulation per point, moment contraction per element) is bound "
-                            f"by the {FP64_TFLOPS} TFLOP/s FP64 rate measured on this part, not by HBM"}
     kernels = {k: {"launches": v["launches"], "ms": v["ms"],
                    "GB_per_s": v["bytes"] / (v["ms"] / 1e3) / 1e9 if v["ms"] > 0 else None,
                    "TFLOP_per_s": v["flops"] / (v["ms"] / 1e3) / 1e12 if v["ms"] > 0 else None}
                for k, v in prof.items()}
 
-    # the other precision form on the same inputs, and the distance between the two solutions
-    comparison = None
+    # assembly (rheology + moments + contraction into K_e, f_e, G_e, S_e) in both forms: points
+    # assembled per second and the algorithmic bytes against HBM, with the FP64 rate beside it
+    def assembly_rates(prec_form):
+        use_assembly(prec_form)
+        ctx.bin_and_map(want=False)
+        for _ in range(2):
+            ctx.assemble()
+        ctx.profile_enable(True)
+        for _ in range(3):
+            ctx.assemble()
+        n, t = ctx.profile_read(U.KERNEL_ASSEMBLY)
+        b, f = ctx.profile_work(U.KERNEL_ASSEMBLY)
+        ctx.profile_enable(False)
+        ms_a = t / 3
+        return {"contraction": "tensor core (tcgen05, FP16 slices, FP64-accurate)" if prec_form != "fp64" else
+                "FP64 CUDA cores", "ms": ms_a, "points_per_s": npts / (ms_a / 1e3),
+                "GB_per_s": b / 3 / (ms_a / 1e3) / 1e9, "frac_hbm": b / 3 / (ms_a / 1e3) / 1e9 / peak,
+                "fp64_TFLOP_per_s": f / 3 / (ms_a / 1e3) / 1e12, "launches_per_assembly": n / 3}
+    assembly = {"tensor": assembly_rates("mixed"), "fp64": assembly_rates("fp64"),
+                "note": f"algorithmic bytes: points read (xi, material, inputs), viscosity written, packed K_e, "
+                        f"f_e, G_e, S_e written (and the 27 moments written and read back in the tensor form); "
+                        f"FP64 work is bounded by the {FP64_TFLOPS} TFLOP/s FP64 rate of this part"}
+
+    # the other forms on the same inputs, and the distance between the solutions
+    comparison = {}
     if not args.no_compare:
-        other = "fp64" if prec == "mixed" else "mixed"
-        ms2, wall2, l2, reps2, clk2, _ = timed(opts_for(other), profile=False, warmup=1)
-        _, _, _, _, _, prof2 = timed(opts_for(other), profile=True, warmup=0, steps=1)
-        ms2 = dist.max(ms2)
-        ua, pa, _ = ctx.solve_bsscr(opts_for(prec), want=True)
-        ub, pb, _ = ctx.solve_bsscr(opts_for(other), want=True)
-        comparison = {"precision": other, "value": dist.sum(npts) / (ms2 / 1e3 / args.steps),
-                      "ms_per_step": ms2 / args.steps, "stokes_solve_s": reps2[-1].t_solve_ms / 1e3,
-                      "rel_residual": reps2[-1].rel_residual, "outer_its": reps2[-1].outer_its,
-                      "inner_its": reps2[-1].inner_its_total, "vcycles": reps2[-1].vcycles,
-                      "pc_inner_its": reps2[-1].pc_inner_its,
-                      f"step_speedup_of_{prec}": (ms2 / args.steps) / (ms_max / args.steps),
-                      f"solve_speedup_of_{prec}": reps2[-1].t_solve_ms / rep.t_solve_ms,
-                      f"{prec}_u_rel_diff": float(np.linalg.norm(ua - ub) / np.linalg.norm(ub)),
-                      f"{prec}_p_rel_diff": float(np.linalg.norm(pa - pb) / np.linalg.norm(pb)),
-                      "clocks": clk2,
-                      "kernels": {k: {"launches": v["launches"], "ms": v["ms"]} for k, v in prof2.items()}}
+        others = ["mixed", "fp64"] if learned else (["fp64"] if prec == "mixed" else ["mixed"])
+        sols = {}
+        for other in others:
+            use_assembly(other)
+            o_opts = opts_for(other)
+            ms2, wall2, l2, reps2, clk2, _ = timed(o_opts, profile=False, warmup=1)
+            _, _, _, _, _, prof2 = timed(o_opts, profile=True, warmup=0, steps=1)
+            comparison[other] = leg_summary(other, ms2, reps2, clk2, prof2)
+            comparison[other][f"step_speedup_of_{head}"] = (dist.max(ms2) / args.steps) / step_ms
+            comparison[other][f"solve_speedup_of_{head}"] = reps2[-1].t_solve_ms / rep.t_solve_ms
+            sols[other] = ctx.solve_bsscr(o_opts, want=True)[:2]
+        use_assembly(head)
+        ua, pa, _ = ctx.solve_bsscr(head_opts, want=True)
+        for other, (ub, pb) in sols.items():
+            comparison[other][f"{head}_u_rel_diff"] = float(np.linalg.norm(ua - ub) / np.linalg.norm(ub))
+            comparison[other][f"{head}_p_rel_diff"] = float(np.linalg.norm(pa - pb) / np.linalg.norm(pb))
 
     # end to end through the public API with host buffers (pinned)
+    use_assembly(head)
     xs = torch.from_numpy(w["x"]).pin_memory().numpy()
     ys = torch.from_numpy(w["y"]).pin_memory().numpy()
     zs = torch.from_numpy(w["z"]).pin_memory().numpy()
@@ -423,7 +493,6 @@ def run_ours(args):
     nn = ctx.nnodes
     ne = ctx.nelements
     e2e_times = []
-    opts = opts_for(prec)
     e2e_warm = 1  # the context is warm from the legs above
     for it in range(0 if args.no_e2e else e2e_warm + args.steps):
         torch.cuda.synchronize()
@@ -431,7 +500,7 @@ def run_ours(args):
         ctx.particles_upload(xs, ys, zs, ms_, pe, pr)
         ctx.bin_and_map(want=False)
         ctx.assemble()
-        u, p, _ = ctx.solve_bsscr(opts, want=True)
+        u, p, _ = ctx.solve_bsscr(head_opts, want=True)
         torch.cuda.synchronize()
         if it >= e2e_warm:
             e2e_times.append(time.perf_counter() - t0)
@@ -441,35 +510,74 @@ def run_ours(args):
            "d2h_bytes_per_step": int(nn * 3 * 8 + ne * 8)}
 
     operator_rates = kernel_rates(ctx, U, args.iters)
-    roofline = fine_roofline(dom, prec, operator_rates, nel, peak, peak_kind, family)
+    roofline = fine_roofline(dom if dom in FINE_KERNEL else "schur_pc", "mixed" if prec != "fp64" else "fp64",
+                             operator_rates, nel, peak, peak_kind, family)
 
     cpu = None
+    same_size = None
     if rank == 0 and not args.no_cpu:
         try:
             cpu = cpu_baseline(args.workload, args.cpu_nel, os.cpu_count() or 1)
+            cpu1 = cpu_baseline(args.workload, args.cpu_nel, 1)
+            cpu["single_thread"] = {"value": cpu1["value"], "cores": 1, "step_s": cpu1["step_s"]}
         except Exception as ex:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {ex}"}
+        same_size = gpu_at_cpu_size(U, W, args, local, skw)
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32/f64", "data": "synthetic",
+               "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32/f64 (bf16/fp16 tensor-core parts)",
+               "data": "synthetic",
                "config": {"workload": workload_name(args.workload, nel), "elements": ne,
-                          "points": npts, "precision": prec, "mg_levels": skw["mg_levels"],
-                          "solver": "BSSCR: Schur FGMRES(scaled BFBt) / A11 FGMRES + GMG (Chebyshev block-Jacobi, degree 2+2)",
+                          "points": npts, "precision": head, "mg_levels": skw["mg_levels"],
+                          "solver": "BSSCR: Schur FGMRES(scaled BFBt) / A11 FGMRES + GMG (Chebyshev block-Jacobi, degree 2+2)"
+                                    + (" + U-Net correction (flexible Krylov, GMG fallback)" if learned else ""),
                           "target_rel_residual": 1e-6, "rel_residual": rep.rel_residual,
                           "outer_its": rep.outer_its, "inner_its": rep.inner_its_total, "vcycles": rep.vcycles,
-                          "pc_inner_its": rep.pc_inner_its,
+                          "pc_inner_its": rep.pc_inner_its, "learned_applies": rep.learned_applies,
+                          "learned_fallbacks": rep.learned_fallbacks,
                           "stokes_solve_s": rep.t_solve_ms / 1e3, "setup_ms": rep.t_setup_ms,
                           "l2": "256 MB buffer written between timed steps", "parallelism": f"replicas x{world}"},
                "roofline": roofline, "assembly": assembly, "kernels": kernels, "operator": operator_rates,
-               "cpu_baseline": cpu, "e2e": e2e,
+               "learned": learn_info, "cpu_baseline": cpu, "gpu_at_cpu_sample_size": same_size, "e2e": e2e,
                "gpu_launches": int(launches), "clocks": clk, "comparison": comparison,
                "wall_s_timed": wall}
         print(json.dumps(out), flush=True)
     ctx.close()
     dist.close()
     return 0
+
+
+def gpu_at_cpu_size(U, W, args, local, skw):
+    """This library on the CPU baseline's sample (same workload generator and mesh, FP64 and mixed,
+    same solver options as the CPU leg): the same-configuration GPU/CPU comparison."""
+    import torch
+    w = make_workload(args.workload, args.cpu_nel)
+    npts = w["x"].shape[0]
+    out = {"workload": workload_name(args.workload, args.cpu_nel), "points": npts}
+    kw = dict(SOLVE_KW)
+    kw["mg_levels"] = 3 if args.cpu_nel % 4 == 0 else 2
+    with U.Context(local) as c:
+        W.setup_context(c, w)
+        for prec in ("fp64", "mixed"):
+            c.assembly_set(U.ASSEMBLY_TENSOR if prec == "mixed" else U.ASSEMBLY_FP64)
+            opts = U.default_opts(precision=U.PREC_MIXED if prec == "mixed" else U.PREC_FP64, **kw)
+            for _ in range(2):
+                c.bin_and_map(want=False)
+                c.assemble()
+                c.solve_bsscr(opts, want=False)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            steps = 5
+            for _ in range(steps):
+                c.bin_and_map(want=False)
+                c.assemble()
+                c.solve_bsscr(opts, want=False)
+            c.synchronize()
+            dt = (time.perf_counter() - t0) / steps
+            out[prec] = {"value": npts / dt, "unit": UNIT, "ms_per_step": 1e3 * dt}
+    return out
 
 
 # DRAM traffic (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one fine-level launch, from the

@@ -56,6 +56,9 @@ struct AssemblyArgs {
     double* eta_out;
     uint32_t* flags;  // bit0: empty element, bit1: bad material index
     double* mom;      // 3D, tensor-core contraction: moments out ([27][e]) instead of K_e and S_e
+    const uint32_t* perm;   // point of each slot
+    const double* pfw;      // strain-weakening history per point, or null
+    double* pfw_incr;       // its time derivative per point (written by yielding laws), or null
 };
 
 // G_e entry of node a, component d on a 3D element of widths h: the integral of -dN_a/dx_d
@@ -73,7 +76,8 @@ __host__ __device__ inline double ge_entry(const double h[3], int a, int d) {
 template <int DIM>
 __device__ __forceinline__ double run_rheology(const uwgpu_material& m, const double* N, const double* Tn,
                                                bool hasT, const double* xg, double ymax, double point_eta,
-                                               const double (*L)[3], double pressure, int prev) {
+                                               const double (*L)[3], double pressure, int prev, double pfw,
+                                               double* pfw_incr) {
     const double yglobal = xg[1];
     double eta = 0.0;
     for (int l = 0; l < m.n_laws; ++l) {
@@ -144,6 +148,53 @@ __device__ __forceinline__ double run_rheology(const uwgpu_material& m, const do
                 double corr = -eta * beta;
                 if ((eta + corr) < minVisc) corr = minVisc - eta;
                 eta += corr;
+            }
+            if (eta < minVisc) eta = minVisc;
+            break;
+        }
+        case UWGPU_LAW_VON_MISES:
+        case UWGPU_LAW_BYERLEE: {
+            // YieldRheology.c:198-243: indicator, criterion, strain-weakening increment (with the
+            // viscosity before the correction), the yield correction, the minimum viscosity
+            if (!prev) break;
+            const double minVisc = law.p[2], soft = law.p[3], healing = law.p[4];
+            double inv;
+            if (DIM == 3) {
+                double s0 = 2.0 * eta * L[0][0], s1 = 2.0 * eta * L[1][1], s2 = 2.0 * eta * L[2][2];
+                double s3 = eta * 2.0 * (0.5 * (L[0][1] + L[1][0]));
+                double s4 = eta * 2.0 * (0.5 * (L[0][2] + L[2][0]));
+                double s5 = eta * 2.0 * (0.5 * (L[1][2] + L[2][1]));
+                inv = 0.5 * (s0 * s0 + s1 * s1 + s2 * s2) + s3 * s3 + s4 * s4 + s5 * s5;
+            } else {
+                double s0 = 2.0 * eta * L[0][0], s1 = 2.0 * eta * L[1][1];
+                double s2 = eta * 2.0 * (0.5 * (L[0][1] + L[1][0]));
+                inv = 0.5 * (s0 * s0 + s1 * s1) + s2 * s2;
+            }
+            const double ind = sqrt(inv);
+            // StrainWeakening_CalcRatio (StrainWeakening.c:484-503)
+            const double w = pfw < 0.0 ? 0.0 : pfw;
+            double ratio = 0.0;
+            if (soft > 0.0) {
+                ratio = w / soft;
+                if (ratio > 1.0) ratio = 1.0;
+            }
+            // VonMises.c:175-198 (softened cohesion) or Byerlee.c:157-198 (cohesion + depth term,
+            // depth below the mesh's largest y)
+            const double crit = law.law == UWGPU_LAW_VON_MISES ? law.p[0] * (1.0 - ratio) + law.p[1] * ratio
+                                                               : law.p[0] + law.p[1] * (ymax - yglobal);
+            if (soft > 0.0 && pfw_incr) {   // _StrainWeakening_CalcIncrementIsotropic (:428-481)
+                const double beta = (crit == 0.0 || ind == 0.0) ? 0.0 : 1.0 - crit / ind;
+                *pfw_incr = beta <= 0.0 ? -healing * w : (crit / eta) * (beta / (1.0 - beta) - healing * w);
+            }
+            if (crit < ind) {   // _VonMises_HasYielded (VonMises.c:232-269)
+                if (law.p[5] != 0.0) {
+                    eta = 2.0 * crit * crit * eta / (crit * crit + ind * ind);
+                } else {
+                    const double beta = 1.0 - crit / ind;
+                    double corr = -eta * beta;
+                    if ((eta + corr) < minVisc) corr = minVisc - eta;
+                    eta += corr;
+                }
             }
             if (eta < minVisc) eta = minVisc;
             break;
@@ -416,7 +467,9 @@ __global__ void __launch_bounds__(128) k_assemble(AssemblyArgs A) {
 #pragma unroll
         for (int d = 0; d < DIM; ++d) xg[d] = x0[d] + 0.5 * h[d] * (xi[d] + 1.0);
         double peta = A.seta_in ? A.seta_in[s] : 0.0;
-        double eta = run_rheology<DIM>(m, N, Tn, hasT, xg, A.max[1], peta, L, pressure, A.previous_solution);
+        const uint32_t pidx = A.perm[s];
+        double eta = run_rheology<DIM>(m, N, Tn, hasT, xg, A.max[1], peta, L, pressure, A.previous_solution,
+                                       A.pfw ? A.pfw[pidx] : 0.0, A.pfw_incr ? A.pfw_incr + pidx : nullptr);
         if (A.eta_out) A.eta_out[s] = eta;
         double rho0 = A.srho_in ? A.srho_in[s] : m.density;
         double T = 0.0;
@@ -772,6 +825,24 @@ __global__ void __launch_bounds__(128, 1) k_contract_tc(ContractArgs A) {
     }
 }
 
+// One TimeIntegrand Euler step of the strain-weakening history with the derivative the last
+// assembly stored, then the clamp at zero (StrainWeakening.c:399-426).
+__global__ void k_pfw_advance(int64_t n, double dt, const double* __restrict__ incr, double* __restrict__ pfw) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = pfw[i] + dt * incr[i];
+    pfw[i] = v < 0.0 ? 0.0 : v;
+}
+
+void strain_weakening_advance(Context& c, double dt) {
+    {
+        LaunchScope ls(c, UWGPU_KERNEL_ASSEMBLY);
+        k_pfw_advance<<<blocks_for(c.np, 256), 256, 0, c.stream>>>(c.np, dt, c.pfw_incr.p, c.pfw.p);
+    }
+    check_launch("k_pfw_advance");
+    c.assembled = false;
+}
+
 void assemble(Context& c) {
     UWG_REQUIRE(c.mapped, UWGPU_ERR_STATE, "assemble called before bin_and_map");
     UWG_REQUIRE(c.nmat > 0, UWGPU_ERR_STATE, "materials not set");
@@ -819,6 +890,9 @@ void assemble(Context& c) {
     A.Se = c.Se.p;
     A.eta_out = c.seta_out.p;
     A.flags = c.err_count.p;
+    A.perm = c.perm.p;
+    A.pfw = c.has_pfw ? c.pfw.p : nullptr;
+    A.pfw_incr = c.has_pfw ? c.pfw_incr.p : nullptr;
     const bool tcpath = dim == 3 && c.assembly_mode == UWGPU_ASSEMBLY_TENSOR;
     A.mom = nullptr;
     if (tcpath) {
@@ -854,13 +928,10 @@ void assemble(Context& c) {
         C.Ke = L0.Ke.p;
         C.Se = c.Se.p;
         C.err = c.err_count.p;
-        static bool attr_set = false;
-        if (!attr_set) {
-            UWG_CUDA(cudaFuncSetAttribute(k_contract_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-            attr_set = true;
-        }
-        // 512 TMEM columns per CTA: request enough shared memory that one CTA fills an SM
-        const size_t smem = 120 * 1024;
+        // 512 TMEM columns per CTA: the shared-memory request keeps one CTA per SM
+        int per_sm = 1;
+        const size_t smem = tmem_safe_smem((const void*)k_contract_tc, c.device,
+                                           (size_t)kTabN * kMomK * 2 + (size_t)kSlices * 128 * kMomK * 2, 512, &per_sm);
         int nsm = 1;
         UWG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
         const int64_t ntiles = (ne + 127) / 128;

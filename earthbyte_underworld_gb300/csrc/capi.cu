@@ -1,5 +1,6 @@
 // extern "C" entry points of libuwgpu (declared in include/uwgpu.h).  Each converts the
 // internal uwg::Error exceptions into a status code plus a message.
+#include <cmath>
 #include <cstring>
 
 #include "internal.cuh"
@@ -221,8 +222,44 @@ int uwgpu_particles_upload(uwgpu_ctx* ctx, int64_t n, const double* x, const dou
             if (rho) upload(c.prho, rho, N, c.stream);
         }
         c.has_points = true;
+        c.has_pfw = false;   // a new point set: its strain-weakening history is set again if needed
         c.mapped = false;
         c.assembled = false;
+    });
+}
+
+int uwgpu_strain_weakening_set(uwgpu_ctx* ctx, const double* pfw) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(c.has_points && c.np > 0, UWGPU_ERR_STATE, "material points not uploaded");
+        const size_t N = (size_t)c.np;
+        if (pfw) upload(c.pfw, pfw, N, c.stream);
+        else {
+            c.pfw.ensure(N);
+            UWG_CUDA(cudaMemsetAsync(c.pfw.p, 0, N * sizeof(double), c.stream));
+        }
+        c.pfw_incr.ensure(N);
+        UWG_CUDA(cudaMemsetAsync(c.pfw_incr.p, 0, N * sizeof(double), c.stream));
+        c.has_pfw = true;
+        c.assembled = false;
+    });
+}
+
+int uwgpu_strain_weakening_advance(uwgpu_ctx* ctx, double dt) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(c.has_pfw, UWGPU_ERR_STATE, "strain-weakening history not set");
+        UWG_REQUIRE(std::isfinite(dt), UWGPU_ERR_ARGUMENT, "dt must be finite");
+        uwg::strain_weakening_advance(c, dt);
+    });
+}
+
+int uwgpu_strain_weakening_get(uwgpu_ctx* ctx, double* pfw, double* increment) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(c.has_pfw, UWGPU_ERR_STATE, "strain-weakening history not set");
+        const size_t N = (size_t)c.np;
+        if (pfw) UWG_CUDA(cudaMemcpyAsync(pfw, c.pfw.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        if (increment)
+            UWG_CUDA(cudaMemcpyAsync(increment, c.pfw_incr.p, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
     });
 }
 

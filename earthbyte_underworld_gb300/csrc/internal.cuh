@@ -25,13 +25,17 @@ struct Error : std::runtime_error {
     Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
 
+// A failed runtime call also leaves its error as the thread's last error; it is cleared here so
+// that a later launch check does not report it again.
 #define UWG_CUDA(call)                                                                     \
     do {                                                                                   \
         cudaError_t e_ = (call);                                                           \
-        if (e_ != cudaSuccess)                                                             \
+        if (e_ != cudaSuccess) {                                                           \
+            (void)cudaGetLastError();                                                      \
             throw ::uwg::Error(e_ == cudaErrorMemoryAllocation ? UWGPU_ERR_MEMORY          \
                                                                : UWGPU_ERR_CUDA,           \
                                std::string(#call) + ": " + cudaGetErrorString(e_));        \
+        }                                                                                  \
     } while (0)
 
 #define UWG_REQUIRE(cond, code, msg)                                                       \
@@ -144,6 +148,10 @@ struct Context {
     DArray<int32_t> pmat;
     DArray<double> peta, prho;
     bool has_peta = false, has_prho = false;
+    // strain-weakening history (postFailureWeakening) per point and its time derivative from the
+    // last assembly (StrainWeakening.c), when set
+    DArray<double> pfw, pfw_incr;
+    bool has_pfw = false;
     bool has_points = false;
 
     // binning / mapping
@@ -257,6 +265,31 @@ inline void check_launch(const char* what) {
     if (e != cudaSuccess) throw Error(UWGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// Dynamic shared memory for a tensor-core kernel that holds `ncols` TMEM columns per CTA: at
+// least `need` bytes, and enough that at most 512 / ncols CTAs of it fit on an SM, so the SM's 512
+// TMEM columns cover every resident CTA and no CTA waits for another one's columns.  Sets the
+// kernel's dynamic shared-memory limit; *per_sm receives the CTAs per SM the request allows.
+inline size_t tmem_safe_smem(const void* fn, int device, size_t need, uint32_t ncols, int* per_sm) {
+    int optin = 0, sm_cap = 0;
+    UWG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    UWG_CUDA(cudaDeviceGetAttribute(&sm_cap, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device));
+    cudaFuncAttributes fa;
+    UWG_CUDA(cudaFuncGetAttributes(&fa, fn));
+    const size_t stat = fa.sharedSizeBytes, reserve = 1024;
+    const size_t max_dyn = (size_t)optin - stat;
+    UWG_REQUIRE(need <= max_dyn, UWGPU_ERR_ARGUMENT, "tensor-core kernel: shared memory plan too large");
+    int max_cta = (int)(512 / ncols);
+    if (max_cta > 16) max_cta = 16;
+    size_t req = need;
+    const size_t floor_total = (size_t)sm_cap / (size_t)(max_cta + 1) + 1;   // per-CTA footprint above which max_cta + 1 do not fit
+    if (req + stat + reserve < floor_total) req = floor_total - stat - reserve;
+    if (req > max_dyn) req = max_dyn;
+    int fit = (int)((size_t)sm_cap / (req + stat + reserve));
+    *per_sm = fit < 1 ? 1 : (fit < max_cta ? fit : max_cta);
+    UWG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)req));
+    return req;
+}
+
 inline unsigned blocks_for(int64_t n, int threads) {
     int64_t b = (n + threads - 1) / threads;
     return (unsigned)(b < 1 ? 1 : b);
@@ -265,6 +298,7 @@ inline unsigned blocks_for(int64_t n, int threads) {
 // ---- functions shared between translation units ----
 void bin_and_map(Context& c);
 void assemble(Context& c);
+void strain_weakening_advance(Context& c, double dt);
 void build_operator(Context& c, int levels, bool need32);
 void apply_fine(Context& c, bool fp32, const double* x, double* y);  // device SoA vectors
 void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep);

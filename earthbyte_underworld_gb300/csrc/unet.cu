@@ -570,21 +570,6 @@ static int sm_count(Context& c) {
     return n > 0 ? n : 1;
 }
 
-constexpr size_t kSmemPerSm = 227 * 1024;   // dynamic shared memory one CTA may use
-
-// Dynamic shared memory to request so that at most 512 / ncols CTAs of a kernel share an SM: the
-// SM's 512 TMEM columns then cover every resident CTA's allocation, and no CTA waits for another
-// one's columns.  Returns the request and the number of CTAs per SM it allows.
-static size_t tmem_safe_smem(size_t need, uint32_t ncols, int* per_sm) {
-    const int max_cta = (int)(512 / ncols) < 16 ? (int)(512 / ncols) : 16;
-    size_t req = need;
-    const size_t floor_bytes = kSmemPerSm / (size_t)(max_cta + 1) + 1024;
-    if (req < floor_bytes) req = floor_bytes;
-    int fit = (int)(kSmemPerSm / req);
-    *per_sm = fit < max_cta ? (fit > 0 ? fit : 1) : max_cta;
-    return req;
-}
-
 void check_errors(Context& c, Net& n) {
     if (!n.tc_err.p) return;
     uint32_t e = 0;
@@ -602,14 +587,10 @@ template <typename TI, typename TO>
 static void conv_launch_tc(Context& c, Net& n, const Vol& g, int K, int N, const TI* in, const bf16* Wrev,
                            const float* bias, TO* out, bool relu) {
     const ConvTcPlan P = conv_tc_plan(K, N, sizeof(TI) == 4);
-    UWG_REQUIRE(P.smem <= kSmemPerSm && P.Np <= 256, UWGPU_ERR_ARGUMENT, "U-Net layer too wide for the tensor-core convolution");
-    static bool attr_set = false;   // per instantiation
-    if (!attr_set) {
-        UWG_CUDA(cudaFuncSetAttribute(k_conv3_tc<TI, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemPerSm));
-        attr_set = true;
-    }
+    UWG_REQUIRE(P.Np <= 256, UWGPU_ERR_ARGUMENT, "U-Net layer too wide for the tensor-core convolution");
     int per_sm = 1;
-    const size_t smem = tmem_safe_smem(P.smem, tc::tmem_cols(P.Np), &per_sm);
+    const size_t smem =
+        tmem_safe_smem((const void*)k_conv3_tc<TI, TO>, c.device, P.smem, tc::tmem_cols(P.Np), &per_sm);
     const int64_t ntiles = (g.nv + 127) / 128;
     const int64_t cap = (int64_t)sm_count(c) * per_sm;
     const unsigned grid = (unsigned)(ntiles < cap ? ntiles : cap);
@@ -623,13 +604,9 @@ static void wgrad_launch_tc(Context& c, Net& n, const Vol& g, int cin, int cout,
                             float* dW, DArray<float>& part) {
     const int Np = (cout + 15) / 16 * 16;
     UWG_REQUIRE(Np <= 256, UWGPU_ERR_ARGUMENT, "U-Net layer too wide for the tensor-core weight gradient");
-    static bool attr_set = false;
-    if (!attr_set) {
-        UWG_CUDA(cudaFuncSetAttribute(k_conv3_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemPerSm));
-        attr_set = true;
-    }
     int per_sm = 1;
-    const size_t smem = tmem_safe_smem(wgrad_tc_smem(Np), tc::tmem_cols(Np), &per_sm);
+    const size_t smem =
+        tmem_safe_smem((const void*)k_conv3_wgrad_tc, c.device, wgrad_tc_smem(Np), tc::tmem_cols(Np), &per_sm);
     const int rows = 27 * cin;
     const int mtiles = (rows + 127) / 128;
     int64_t slices = (2LL * sm_count(c) + mtiles - 1) / mtiles;

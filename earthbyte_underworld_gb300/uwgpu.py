@@ -28,6 +28,8 @@ LAW_PARTICLE_VISCOSITY = 6
 LAW_LINEAR_VISCOSITY = 7
 LAW_DEPTH_DEPENDENT = 8
 LAW_NON_NEWTONIAN = 9
+LAW_VON_MISES = 10
+LAW_BYERLEE = 11
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -148,6 +150,9 @@ def load(build_if_missing: bool = True):
         L.uwgpu_learned_train.argtypes = [P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P, P]
         L.uwgpu_tc_check.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P, P]
         L.uwgpu_assembly_set.argtypes = [P, C.c_int32]
+        L.uwgpu_strain_weakening_set.argtypes = [P, P]
+        L.uwgpu_strain_weakening_advance.argtypes = [P, C.c_double]
+        L.uwgpu_strain_weakening_get.argtypes = [P, P, P]
         _lib = L
         return _lib
 
@@ -282,6 +287,21 @@ class Context:
         xi = np.zeros((self.npoints, 3))
         self._check(self._L.uwgpu_bin_and_map(self._h, _ptr(perm), _ptr(offsets), _ptr(xi)))
         return perm, offsets, xi
+
+    def strain_weakening_set(self, pfw=None):
+        """Upload the per-point strain-weakening history (None: zero) and enable it."""
+        a = None if pfw is None else np.ascontiguousarray(pfw, dtype=np.float64)
+        self._check(self._L.uwgpu_strain_weakening_set(self._h, _ptr(a)))
+
+    def strain_weakening_advance(self, dt):
+        self._check(self._L.uwgpu_strain_weakening_advance(self._h, float(dt)))
+
+    def strain_weakening(self):
+        """(history, time derivative from the last assembly), per point."""
+        pfw = np.zeros(self.npoints)
+        inc = np.zeros(self.npoints)
+        self._check(self._L.uwgpu_strain_weakening_get(self._h, _ptr(pfw), _ptr(inc)))
+        return pfw, inc
 
     def assembly_set(self, mode):
         """ASSEMBLY_FP64 (default) or ASSEMBLY_TENSOR (tensor-core contraction of the moments, 3D)."""

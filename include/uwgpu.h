@@ -54,9 +54,16 @@ enum {
                                          (+ Z z + XZ x z + YZ y z + XYZ x y z in 3D); p0..p7 = C X Y Z XY XZ YZ XYZ */
     UWGPU_LAW_DEPTH_DEPENDENT = 8,    /* Underworld/Rheology/src/DepthDependentViscosity.c:165-188  eta = eta0 exp(gamma (x_axis - referencePoint));
                                          p0=eta0 p1=gamma p2=referencePoint p3=variationAxis (0, 1, 2) */
-    UWGPU_LAW_NON_NEWTONIAN = 9       /* Underworld/Rheology/src/NonNewtonian.c:139-171  eta = (2 e_II)^(1/n - 1) eta^(1/n), e_II the point's
+    UWGPU_LAW_NON_NEWTONIAN = 9,      /* Underworld/Rheology/src/NonNewtonian.c:139-171  eta = (2 e_II)^(1/n - 1) eta^(1/n), e_II the point's
                                          strain-rate invariant (defaultStrainRateInvariant before the first solve);
                                          p0=stressExponent p1=defaultStrainRateInvariant */
+    UWGPU_LAW_VON_MISES = 10,         /* Underworld/Rheology/src/VonMises.c:175-269 via YieldRheology.c:198-243, with the
+                                         StrainWeakening of its cohesion (StrainWeakening.c:428-503); p0=cohesion
+                                         p1=cohesionAfterSoftening p2=minimumViscosity p3=softeningStrain (<= 0: no weakening)
+                                         p4=healingRate p5=strainRateSoftening (0/1) */
+    UWGPU_LAW_BYERLEE = 11            /* Underworld/Rheology/src/Byerlee.c:157-198: the VonMises law with the yield stress
+                                         cohesion + depthCoefficient (max_y - y); p0=cohesion p1=depthCoefficient, p2..p5 as
+                                         for VON_MISES (p3, p4: the strain-weakening history it updates) */
 };
 
 typedef struct {
@@ -191,6 +198,19 @@ int uwgpu_solution_set(uwgpu_ctx* ctx, const double* u_nodal, const double* p);
 int uwgpu_particles_upload(uwgpu_ctx* ctx, int64_t n, const double* x, const double* y,
                            const double* z, const int32_t* material, const double* eta,
                            const double* rho);
+
+/* Strain-weakening history of the material points (the postFailureWeakening particle variable of
+ * a StrainWeakening component, StgDomain TimeIntegrand; Underworld/Rheology/src/StrainWeakening.c).
+ * _set uploads it (n values in point order; NULL: all zero) and enables the history: the next
+ * assemblies give every point of a VON_MISES / BYERLEE law with softeningStrain > 0 a softened
+ * cohesion and store the history's time derivative (_StrainWeakening_CalcIncrementIsotropic).
+ * _advance integrates one step of length dt with that derivative and clamps the history at zero
+ * (_StrainWeakening_TimeDerivative, _StrainWeakening_MakeValuesPositive, :399-426).  _get copies the
+ * history and the last derivative to the host (either may be NULL).  The initial random damage of
+ * _StrainWeakening_Initialise (libc rand()) stays on the host. */
+int uwgpu_strain_weakening_set(uwgpu_ctx* ctx, const double* pfw);
+int uwgpu_strain_weakening_advance(uwgpu_ctx* ctx, double dt);
+int uwgpu_strain_weakening_get(uwgpu_ctx* ctx, double* pfw, double* increment);
 
 /* Binning + integration-point mapping: _CoincidentMapper_Map
  * (PICellerator/MaterialPoints/src/CoincidentMapper.c:150-253) with the regular-mesh element

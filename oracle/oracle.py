@@ -24,6 +24,16 @@ LAW_FRANK_KAMENETSKII = 3
 LAW_VISCOSITY_LIMITER = 4
 LAW_DRUCKER_PRAGER = 5
 LAW_PARTICLE_VISCOSITY = 6
+LAW_VON_MISES = 10
+LAW_BYERLEE = 11
+
+
+def strain_weakening_advance(pfw, incr, dt):
+    """TimeIntegrand Euler step of postFailureWeakening with its stored time derivative, then
+    _StrainWeakening_MakeValuesPositive (StrainWeakening.c:399-426; a higher-order integrator reads
+    the same stored derivative at every stage, so the step is the same)."""
+    out = pfw + dt * incr
+    return np.where(out < 0.0, 0.0, out)
 
 
 class Mesh(C.Structure):
@@ -41,7 +51,8 @@ class Material(C.Structure):
 
 class Fields(C.Structure):
     _fields_ = [("temperature", C.c_void_p), ("velocity", C.c_void_p), ("pressure", C.c_void_p),
-                ("previous_solution", C.c_int32), ("vert_axis", C.c_int32), ("gravity", C.c_double)]
+                ("previous_solution", C.c_int32), ("vert_axis", C.c_int32), ("gravity", C.c_double),
+                ("pfw", C.c_void_p), ("pfw_incr", C.c_void_p)]
 
 
 class SolveOpts(C.Structure):
@@ -169,10 +180,16 @@ def map_points(m, xyz, use_newton=True):
 
 
 def make_fields(temperature=None, velocity=None, pressure=None, previous_solution=False,
-                vert_axis=1, gravity=0.0):
+                vert_axis=1, gravity=0.0, pfw=None, pfw_incr=None):
+    """pfw: per-point postFailureWeakening (strain-weakening history); pfw_incr: a float64 array of
+    the same length that the assembly fills with its time derivative."""
     f = Fields()
     keep = []
-    for name, arr in (("temperature", temperature), ("velocity", velocity), ("pressure", pressure)):
+    if pfw_incr is not None:
+        assert pfw_incr.dtype == np.float64 and pfw_incr.flags.c_contiguous
+        f.pfw_incr = pfw_incr.ctypes.data
+        keep.append(pfw_incr)
+    for name, arr in (("temperature", temperature), ("velocity", velocity), ("pressure", pressure), ("pfw", pfw)):
         if arr is not None:
             arr = np.ascontiguousarray(arr, dtype=np.float64)
             keep.append(arr)

@@ -493,6 +493,7 @@ typedef struct {
     const double* GNx;      /* global derivatives at xi */
     double nodes[8][3];
     double point_eta;
+    int64_t p;              /* material point index (strain-weakening history) */
 } rheo_point;
 
 static double interp_temperature(const rheo_point* rp) {
@@ -637,6 +638,47 @@ static double run_rheologies(const uwr_material* mat, const rheo_point* rp) {
             eta = law->p[0] * exp(law->p[1] * (x[axis] - law->p[2]));
             break;
         }
+        case UWR_LAW_VON_MISES:     /* YieldRheology.c:198-243 with VonMises.c:175-269 */
+        case UWR_LAW_BYERLEE: {     /* Byerlee.c:157-198: criterion cohesion + depthCoefficient (max_y - y) */
+            if (!rp->f->previous_solution) break;
+            const double minVisc = law->p[2], soft = law->p[3], healing = law->p[4];
+            double ind = stress_invariant(rp, eta);                 /* _VonMises_GetYieldIndicator */
+            /* StrainWeakening_CalcRatio (StrainWeakening.c:484-503) */
+            double pfw = (rp->f->pfw && rp->p >= 0) ? rp->f->pfw[rp->p] : 0.0;
+            if (pfw < 0.0) pfw = 0.0;
+            double ratio = 0.0;
+            if (soft > 0.0) {
+                ratio = pfw / soft;
+                if (ratio > 1.0) ratio = 1.0;
+            }
+            double crit;
+            if (law->law == UWR_LAW_VON_MISES) {
+                crit = law->p[0] * (1.0 - ratio) + law->p[1] * ratio;  /* _VonMises_GetYieldCriterion */
+            } else {
+                double x[3];
+                point_coord(rp, x);
+                crit = law->p[0] + law->p[1] * (rp->m->max[1] - x[1]);
+            }
+            /* StrainWeakening_AssignIncrement -> _StrainWeakening_CalcIncrementIsotropic (:428-481),
+             * with the viscosity before the yield correction */
+            if (soft > 0.0 && rp->f->pfw_incr && rp->p >= 0) {
+                double beta = (crit == 0.0 || ind == 0.0) ? 0.0 : 1.0 - crit / ind;
+                rp->f->pfw_incr[rp->p] = beta <= 0.0 ? -healing * pfw
+                                                     : (crit / eta) * (beta / (1.0 - beta) - healing * pfw);
+            }
+            if (crit < ind) {   /* _VonMises_HasYielded */
+                if (law->p[5] != 0.0) {
+                    eta = 2.0 * crit * crit * eta / (crit * crit + ind * ind);
+                } else {
+                    double beta = 1.0 - crit / ind;
+                    double corr = -eta * beta;
+                    if ((eta + corr) < minVisc) corr = minVisc - eta;
+                    eta += corr;
+                }
+            }
+            if (eta < minVisc) eta = minVisc;
+            break;
+        }
         case UWR_LAW_NON_NEWTONIAN: { /* NonNewtonian.c:139-171 */
             double sri = rp->f->previous_solution ? strain_rate_invariant(rp) : law->p[1];
             if (sri == 0) break;
@@ -771,6 +813,7 @@ int uwr_assemble_range(const uwr_mesh* m, int64_t first, int64_t count, int64_t 
             rp.N = N;
             rp.GNx = GNx;
             rp.point_eta = point_eta ? point_eta[p] : 0.0;
+            rp.p = p;
             int32_t mi = material ? material[p] : 0;
             if (mi < 0 || mi >= nmat) { bad |= 1; continue; }
             const uwr_material* mat = &mats[mi];
@@ -1004,6 +1047,7 @@ int uwr_assemble_gauss(const uwr_mesh* m, int32_t nmat, const uwr_material* mats
             rp.N = N;
             rp.GNx = GNx;
             rp.point_eta = 0.0;
+            rp.p = -1;
             double eta = run_rheologies(&mats[mi], &rp);
             accumulate_Ke(dim, nen, eta, detJ * 1.0, GNx, K);
         }

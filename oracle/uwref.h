@@ -37,7 +37,12 @@ enum {
     UWR_LAW_PARTICLE_VISCOSITY = 6,   /* eta = per-point viscosity input                   */
     UWR_LAW_LINEAR_VISCOSITY = 7,     /* p0..p7 = C X Y Z XY XZ YZ XYZ                      */
     UWR_LAW_DEPTH_DEPENDENT = 8,      /* p0=eta0 p1=gamma p2=referencePoint p3=axis         */
-    UWR_LAW_NON_NEWTONIAN = 9         /* p0=stressExponent p1=defaultStrainRateInvariant    */
+    UWR_LAW_NON_NEWTONIAN = 9,        /* p0=stressExponent p1=defaultStrainRateInvariant    */
+    UWR_LAW_VON_MISES = 10,           /* p0=cohesion p1=cohesionAfterSoftening p2=minimumViscosity
+                                         p3=softeningStrain (<= 0: no strain weakening) p4=healingRate
+                                         p5=strainRateSoftening (0/1)                        */
+    UWR_LAW_BYERLEE = 11              /* p0=cohesion p1=depthCoefficient p2=minimumViscosity
+                                         p3=softeningStrain p4=healingRate p5=strainRateSoftening */
 };
 
 typedef struct {
@@ -63,6 +68,8 @@ typedef struct {
     int32_t previous_solution;   /* YieldRheology yields only if a solve happened    */
     int32_t vert_axis;           /* BuoyancyForceTerm VerticalAxis                   */
     double gravity;              /* BuoyancyForceTerm gravity                        */
+    const double* pfw;           /* StrainWeakening postFailureWeakening per point (NULL: 0) */
+    double* pfw_incr;            /* out: its time derivative per point (NULL: not written)  */
 } uwr_fields;
 
 /* Mesh geometry -------------------------------------------------------------------------- */
