@@ -234,8 +234,11 @@ FAMILY_NOTES = {
               "1.2 TFLOP/s FP64 rate (fp_tflops)",
     "apply": "one operator apply (k_apply): 27 stencil blocks of 3x3 per node, x read and y written once",
     "schur_pc": "one replay of the BFBt inner-CG graph = 12 iterations of k_cg_update + the direction kernel "
-                "(k_cg_spmv_dir on the 27-point G^T W G stencil, or k_cg_mf3_dir matrix-free in FP32 on meshes "
-                "whose FP32 stencil would not fit in half of L2); the roofline line is the direction kernel",
+                "(k_cg_spmv_dir on the 27-point G^T W G stencil, or the matrix-free FP32 kernel k_cg_mf3_dir_tma, "
+                "its element and weight planes staged by TMA, on meshes whose FP32 stencil would not fit in half "
+                "of L2); the roofline line is the direction kernel",
+    "learned": "U-Net corrections: tcgen05 implicit-GEMM convolutions (BF16, FP32 accumulate) and the head",
+    "assembly": "rheology + moments per point, contraction of the moments into K_e (tensor core in the mixed forms)",
 }
 
 
@@ -661,7 +664,8 @@ def kernel_rates(ctx, U, iters):
     ne = ctx.nelements
     l2 = torch.cuda.get_device_properties(torch.cuda.current_device()).L2_cache_size
     mf = ne * 4.0 * (nb + 6) > 0.5 * l2
-    fp32_mf = ("fp32_matrix_free", 1, (dim + 3) * 4, "k_cg_mf3_dir" if dim == 3 else "k_cg_mf2_dir")
+    mf3 = "k_cg_mf3_dir_tma (planes staged by TMA)" if ctx.nel[0] % 4 == 0 else "k_cg_mf3_dir"
+    fp32_mf = ("fp32_matrix_free", 1, (dim + 3) * 4, mf3 if dim == 3 else "k_cg_mf2_dir")
     fp32_st = ("fp32_stencil", 2, (nb + 3) * 4, f"k_cg_spmv_dir<{dim},float>")
     forms = (("fp64", ("fp64_stencil", 0, (nb + 3) * 8, f"k_cg_spmv_dir<{dim},double>")),
              ("fp32", fp32_mf if mf else fp32_st), ("fp32_other", fp32_st if mf else fp32_mf))

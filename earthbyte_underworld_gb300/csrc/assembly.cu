@@ -71,20 +71,160 @@ __host__ __device__ inline double ge_entry(const double h[3], int a, int d) {
     return -sa * area * 0.25;
 }
 
+// ---- eigenvalues of a symmetric stress tensor, as the reference computes them
+// (StgDomain/Geometry/src/TensorMath.c:619-975): the real roots of the characteristic cubic, or,
+// when an eigenvector formula fails for one of them, cyclic Jacobi rotations (Numerical Recipes
+// in C, 2nd ed., section 11.1); the same decisions, with the reference's absolute 1e-8
+// comparisons, so that both sides take the same branch.  Storage: 2D [xx, yy, xy],
+// 3D [xx, yy, zz, xy, xz, yz].  Ascending order.
+__device__ __forceinline__ bool eql8(double a, double b) { return fabs(a - b) < 1.0e-8; }
+
+__device__ inline void jacobi_eig3(const double* t, double* ev) {
+    double a01 = t[3], a02 = t[4], a12 = t[5];
+    double b[3] = {t[0], t[1], t[2]}, z[3] = {0.0, 0.0, 0.0};
+    ev[0] = t[0];
+    ev[1] = t[1];
+    ev[2] = t[2];
+    for (int sweep = 1; sweep <= 50; ++sweep) {
+        const double sum = fabs(a01) + fabs(a02) + fabs(a12);
+        if (sum == 0.0) break;
+        const double tresh = sweep < 4 ? 0.2 * sum / 9.0 : 0.0;
+        for (int pr = 0; pr < 3; ++pr) {
+            const int ip = pr < 2 ? 0 : 1, iq = pr == 0 ? 1 : 2;   // (0,1), (0,2), (1,2)
+            double& apq = pr == 0 ? a01 : (pr == 1 ? a02 : a12);
+            const double g = 100.0 * fabs(apq);
+            if (sweep > 4 && (fabs(ev[ip]) + g) == fabs(ev[ip]) && (fabs(ev[iq]) + g) == fabs(ev[iq])) {
+                apq = 0.0;
+            } else if (fabs(apq) > tresh) {
+                double h = ev[iq] - ev[ip], tt;
+                if ((double)(fabs(h) + g) == (double)fabs(h)) {
+                    tt = apq / h;
+                } else {
+                    const double theta = 0.5 * h / apq;
+                    tt = 1.0 / (fabs(theta) + sqrt(1.0 + theta * theta));
+                    if (theta < 0.0) tt = -tt;
+                }
+                const double c = 1.0 / sqrt(1 + tt * tt), sn = tt * c, tau = sn / (1.0 + c);
+                h = tt * apq;
+                z[ip] -= h;
+                z[iq] += h;
+                ev[ip] -= h;
+                ev[iq] += h;
+                apq = 0.0;
+                // the rotation of the remaining off-diagonal entry (the third index r)
+                if (pr == 0) {          // (0,1): r = 2 -> a02 (row ip), a12 (row iq)
+                    const double g1 = a02, h1 = a12;
+                    a02 = g1 - sn * (h1 + g1 * tau);
+                    a12 = h1 + sn * (g1 - h1 * tau);
+                } else if (pr == 1) {   // (0,2): r = 1 lies between ip and iq -> a01 (row ip), a12 (column iq)
+                    const double g1 = a01, h1 = a12;
+                    a01 = g1 - sn * (h1 + g1 * tau);
+                    a12 = h1 + sn * (g1 - h1 * tau);
+                } else {                // (1,2): r = 0 below ip -> a01, a02
+                    const double g1 = a01, h1 = a02;
+                    a01 = g1 - sn * (h1 + g1 * tau);
+                    a02 = h1 + sn * (g1 - h1 * tau);
+                }
+            }
+        }
+        for (int i = 0; i < 3; ++i) {
+            b[i] += z[i];
+            ev[i] = b[i];
+            z[i] = 0.0;
+        }
+    }
+}
+
+__device__ inline void sym_eigenvalues(const double* t, int dim, double* ev) {
+    if (dim == 2) {
+        const double r = sqrt(0.25 * (t[0] - t[1]) * (t[0] - t[1]) + t[2] * t[2]);
+        const double avg = 0.5 * (t[0] + t[1]);
+        ev[0] = avg - r;
+        ev[1] = avg + r;
+        return;
+    }
+    const double a2 = -t[0] - t[1] - t[2];
+    const double a1 = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(t[0], t[1]), __dmul_rn(t[0], t[2])),
+                                                          __dmul_rn(t[1], t[2])),
+                                                -__dmul_rn(t[3], t[3])),
+                                      -__dmul_rn(t[4], t[4])),
+                            -__dmul_rn(t[5], t[5]));
+    const double a0 = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(-__dmul_rn(__dmul_rn(t[0], t[1]), t[2]),
+                                                          -__dmul_rn(2.0, __dmul_rn(__dmul_rn(t[3], t[4]), t[5]))),
+                                                __dmul_rn(__dmul_rn(t[0], t[5]), t[5])),
+                                      __dmul_rn(__dmul_rn(t[1], t[4]), t[4])),
+                            __dmul_rn(__dmul_rn(t[2], t[3]), t[3]));
+    // the real roots of l^3 + a2 l^2 + a1 l + a0 (Cardano, trigonometric form)
+    const double Q = __ddiv_rn(__dsub_rn(__dmul_rn(3.0, a1), __dmul_rn(a2, a2)), 9.0);
+    const double R = __ddiv_rn(__dsub_rn(__dsub_rn(__dmul_rn(__dmul_rn(9.0, a2), a1), __dmul_rn(27.0, a0)),
+                                         __dmul_rn(__dmul_rn(__dmul_rn(2.0, a2), a2), a2)),
+                               54.0);
+    const double D = __dadd_rn(__dmul_rn(__dmul_rn(Q, Q), Q), __dmul_rn(R, R));
+    if (eql8(D, 0.0)) {
+        const double halfB = R < 0.0 ? -pow(-R, 1.0 / 3.0) : pow(R, 1.0 / 3.0);
+        ev[0] = -a2 / 3.0 + 2.0 * halfB;
+        ev[1] = ev[2] = -a2 / 3.0 - halfB;
+    } else {
+        const double theta = acos(R / sqrt(-__dmul_rn(__dmul_rn(Q, Q), Q))) / 3.0;
+        const double factor = 2.0 * sqrt(-Q);
+        const double pi = 3.14159265358979323846;
+        ev[0] = factor * cos(theta) - a2 / 3.0;
+        ev[1] = factor * cos(theta + 2.0 * pi / 3.0) - a2 / 3.0;
+        ev[2] = factor * cos(theta + 4.0 * pi / 3.0) - a2 / 3.0;
+    }
+    // an eigenvector formula must apply to every root (TensorMath.c:726-758), else Jacobi
+    bool ok = true;
+    for (int i = 0; i < 3; ++i) {
+        const double A = t[0] - ev[i], B = t[1] - ev[i], d = t[3], e = t[4], f = t[5];
+        const bool good = (!eql8(B * e, f * d) && !eql8(e, 0.0)) || (!eql8(f * A, d * e) && !eql8(e, 0.0)) ||
+                          (!eql8(d * d, B * A) && !eql8(d, 0.0));
+        ok = ok && good;
+    }
+    if (!ok) jacobi_eig3(t, ev);
+    // ascending
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2 - i; ++j)
+            if (ev[j] > ev[j + 1]) {
+                const double tmp = ev[j];
+                ev[j] = ev[j + 1];
+                ev[j + 1] = tmp;
+            }
+}
+
 // Per-point rheology chain.  Every law in scope keeps D isotropic, so the constitutive matrix
 // is carried as its viscosity (D[3][3] in 3D, D[2][2] in 2D).
 template <int DIM>
 __device__ __forceinline__ double run_rheology(const uwgpu_material& m, const double* N, const double* Tn,
                                                bool hasT, const double* xg, double ymax, double point_eta,
                                                const double (*L)[3], double pressure, int prev, double pfw,
-                                               double* pfw_incr) {
+                                               double* pfw_incr, double* derivs = nullptr, bool jacobian = false) {
     const double yglobal = xg[1];
     double eta = 0.0;
+    // derivs: the viscosity derivatives of the Newton form (9 entries; zeroed with every
+    // SetIsotropicViscosity, ConstitutiveMatrix.c:362-367; VonMises-family yielding adds its terms
+    // when the Jacobian is formed, VonMises.c:259-268)
+    if (derivs)
+        for (int k = 0; k < 9; ++k) derivs[k] = 0.0;
+    auto set_visc = [&](double v) {
+        eta = v;
+        if (derivs)
+            for (int k = 0; k < 9; ++k) derivs[k] = 0.0;
+    };
+    auto yield_derivs = [&](double visc0, double crit, double ind) {
+        if (!derivs || !jacobian) return;
+        const double st0 = 2.0 * visc0 * L[0][0], st1 = 2.0 * visc0 * L[1][1];
+        const double st2 = DIM == 3 ? 2.0 * visc0 * L[2][2] : visc0 * 2.0 * (0.5 * (L[0][1] + L[1][0]));
+        const double coef = -visc0 * crit / (2.0 * ind * ind * ind);
+        derivs[0] += coef * 2.0 * visc0 * st0;
+        derivs[4] += coef * 2.0 * visc0 * st1;
+        derivs[1] += coef * 2.0 * visc0 * st2;
+        derivs[3] += coef * 2.0 * visc0 * st2;
+    };
     for (int l = 0; l < m.n_laws; ++l) {
         const uwgpu_law& law = m.laws[l];
         switch (law.law) {
         case UWGPU_LAW_MATERIAL_VISCOSITY:
-            eta = law.p[0];
+            set_visc(law.p[0]);
             break;
         case UWGPU_LAW_ARRHENIUS: {
             double T = 0.0;
@@ -94,9 +234,9 @@ __device__ __forceinline__ double run_rheology(const uwgpu_material& m, const do
             }
             if (law.p[2] > (0.0 + 1e-12)) {
                 double depth = ymax - yglobal;
-                eta = law.p[0] * exp((law.p[1] + law.p[2] * depth) / (T + law.p[3]));
+                set_visc(law.p[0] * exp((law.p[1] + law.p[2] * depth) / (T + law.p[3])));
             } else {
-                eta = law.p[0] * exp((law.p[1]) / (T + law.p[3]));
+                set_visc(law.p[0] * exp((law.p[1]) / (T + law.p[3])));
             }
             break;
         }
@@ -106,13 +246,16 @@ __device__ __forceinline__ double run_rheology(const uwgpu_material& m, const do
 #pragma unroll
                 for (int a = 0; a < (1 << DIM); ++a) T += N[a] * Tn[a];
             }
-            eta = law.p[0] * exp(-law.p[1] * T);
+            set_visc(law.p[0] * exp(-law.p[1] * T));
             break;
         }
-        case UWGPU_LAW_VISCOSITY_LIMITER:
-            if (eta > law.p[0]) eta = law.p[0];
-            if (eta < law.p[1]) eta = law.p[1];
+        case UWGPU_LAW_VISCOSITY_LIMITER: {
+            double v = eta;
+            if (v > law.p[0]) v = law.p[0];
+            if (v < law.p[1]) v = law.p[1];
+            set_visc(v);
             break;
+        }
         case UWGPU_LAW_DRUCKER_PRAGER: {
             double minVisc = law.p[3];
             if (!prev) break;
@@ -144,12 +287,14 @@ __device__ __forceinline__ double run_rheology(const uwgpu_material& m, const do
             double crit = dpFric * pressure + dpCoh;
             if (crit < law.p[2]) crit = law.p[2];
             if (crit < ind) {
+                const double visc0 = eta;
                 double beta = 1.0 - crit / ind;
                 double corr = -eta * beta;
                 if ((eta + corr) < minVisc) corr = minVisc - eta;
                 eta += corr;
+                yield_derivs(visc0, crit, ind);
             }
-            if (eta < minVisc) eta = minVisc;
+            if (eta < minVisc) set_visc(minVisc);
             break;
         }
         case UWGPU_LAW_VON_MISES:
@@ -187,30 +332,92 @@ __device__ __forceinline__ double run_rheology(const uwgpu_material& m, const do
                 *pfw_incr = beta <= 0.0 ? -healing * w : (crit / eta) * (beta / (1.0 - beta) - healing * w);
             }
             if (crit < ind) {   // _VonMises_HasYielded (VonMises.c:232-269)
+                const double visc0 = eta;
                 if (law.p[5] != 0.0) {
-                    eta = 2.0 * crit * crit * eta / (crit * crit + ind * ind);
+                    set_visc(2.0 * crit * crit * eta / (crit * crit + ind * ind));
                 } else {
                     const double beta = 1.0 - crit / ind;
                     double corr = -eta * beta;
                     if ((eta + corr) < minVisc) corr = minVisc - eta;
                     eta += corr;
                 }
+                // Newton terms with the criterion the law stored (Byerlee.c stores none: no terms)
+                yield_derivs(visc0, law.law == UWGPU_LAW_VON_MISES ? crit : 0.0, ind);
             }
-            if (eta < minVisc) eta = minVisc;
+            if (eta < minVisc) set_visc(minVisc);
+            break;
+        }
+        case UWGPU_LAW_MOHR_COULOMB: {
+            // MohrCoulomb.c:208-402 via YieldRheology.c:198-243: principal stresses of the stress
+            // of the deviatoric strain rate, a friction-modified stress difference as indicator,
+            // the pressure-dependent strength as criterion
+            if (!prev) break;
+            const double minVisc = law.p[5], soft = law.p[6], healing = law.p[7];
+            double st[6], ev[3];
+            if (DIM == 3) {
+                const double tr = L[0][0] + L[1][1] + L[2][2];
+                st[0] = 2.0 * eta * (L[0][0] - tr / 3.0);
+                st[1] = 2.0 * eta * (L[1][1] - tr / 3.0);
+                st[2] = 2.0 * eta * (L[2][2] - tr / 3.0);
+                st[3] = 2.0 * eta * (0.5 * (L[0][1] + L[1][0]));
+                st[4] = 2.0 * eta * (0.5 * (L[0][2] + L[2][0]));
+                st[5] = 2.0 * eta * (0.5 * (L[1][2] + L[2][1]));
+            } else {
+                const double tr = L[0][0] + L[1][1];
+                st[0] = 2.0 * eta * (L[0][0] - tr / 2.0);
+                st[1] = 2.0 * eta * (L[1][1] - tr / 2.0);
+                st[2] = 2.0 * eta * (0.5 * (L[0][1] + L[1][0]));
+            }
+            sym_eigenvalues(st, DIM, ev);
+            const double w = pfw < 0.0 ? 0.0 : pfw;
+            double ratio = 0.0;
+            if (soft > 0.0) {
+                ratio = w / soft;
+                if (ratio > 1.0) ratio = 1.0;
+            }
+            const double alpha = law.p[2] * (1.0 - ratio) + law.p[3] * ratio;
+            const double coh = law.p[0] * (1.0 - ratio) + law.p[1] * ratio;
+            const double smin = ev[0], smax = DIM == 2 ? ev[1] : ev[2];
+            double sigma_ns = 0.5 * (smax - smin);
+            if (DIM == 3) {
+                const double th = 0.5 * atan(1.0 / alpha);
+                const double fac = 1 / (sin(2 * th) - alpha * cos(2 * th));
+                sigma_ns -= (smax + smin) * 0.5 * alpha * fac;
+            }
+            const double ind = fabs(sigma_ns);
+            const double th = 0.5 * atan(1.0 / alpha);
+            const double fac = sin(2 * th);
+            double crit = alpha * pressure * fac + coh * fac;
+            const double minYS = law.p[4] == 0.0 ? coh : law.p[4];
+            if (crit < minYS * fac) crit = minYS * fac;
+            if (soft > 0.0 && pfw_incr) {
+                const double beta = (crit == 0.0 || ind == 0.0) ? 0.0 : 1.0 - crit / ind;
+                *pfw_incr = beta <= 0.0 ? -healing * w : (crit / eta) * (beta / (1.0 - beta) - healing * w);
+            }
+            if (crit < ind) {
+                const double beta = 1.0 - crit / ind;
+                double corr = -eta * beta;
+                if ((eta + corr) < minVisc) corr = minVisc - eta;
+                eta += corr;
+            }
+            if (eta < minVisc) set_visc(minVisc);
             break;
         }
         case UWGPU_LAW_PARTICLE_VISCOSITY:
-            eta = point_eta;
+            set_visc(point_eta);
             break;
         case UWGPU_LAW_LINEAR_VISCOSITY:
-            eta = law.p[1] * xg[0] + law.p[2] * xg[1] + law.p[4] * xg[0] * xg[1] + law.p[0];
+        {
+            double v = law.p[1] * xg[0] + law.p[2] * xg[1] + law.p[4] * xg[0] * xg[1] + law.p[0];
             if (DIM == 3)
-                eta += law.p[3] * xg[2] + law.p[5] * xg[0] * xg[2] + law.p[6] * xg[1] * xg[2] +
-                       law.p[7] * xg[0] * xg[1] * xg[2];
+                v += law.p[3] * xg[2] + law.p[5] * xg[0] * xg[2] + law.p[6] * xg[1] * xg[2] +
+                     law.p[7] * xg[0] * xg[1] * xg[2];
+            set_visc(v);
             break;
+        }
         case UWGPU_LAW_DEPTH_DEPENDENT: {
             const int axis = (int)law.p[3];
-            eta = law.p[0] * exp(law.p[1] * (xg[axis < 0 ? 0 : (axis > 2 ? 2 : axis)] - law.p[2]));
+            set_visc(law.p[0] * exp(law.p[1] * (xg[axis < 0 ? 0 : (axis > 2 ? 2 : axis)] - law.p[2])));
             break;
         }
         case UWGPU_LAW_NON_NEWTONIAN: {
@@ -228,7 +435,7 @@ __device__ __forceinline__ double run_rheology(const uwgpu_material& m, const do
             }
             const double n = law.p[0];
             if (sri == 0.0 || fabs(n - 1.0) < 1.0e-10) break;
-            eta = pow(2.0 * sri, 1.0 / n - 1.0) * pow(eta, 1.0 / n);
+            set_visc(pow(2.0 * sri, 1.0 / n - 1.0) * pow(eta, 1.0 / n));
             break;
         }
         default:
@@ -652,6 +859,101 @@ __global__ void __launch_bounds__(128) k_assemble(AssemblyArgs A) {
     }
 }
 
+// ---- the Newton (Jacobian) form of the 2D element matrices ---------------------------------
+// ConstitutiveMatrixCartesian.c:360-383: with the SLE's nlFormJacobian the 2D loop adds, per point,
+// the viscosity's derivatives with respect to the velocity gradient (set by yielding laws) to the
+// viscous term, so K_e is no longer symmetric and the moment form does not apply: each point is
+// accumulated directly into the 64 entries, element-major per entry ([i][j][e], i the matrix row
+// (test function), j the column).  S_e is formed from this K_e's diagonal.  (The reference's
+// Ni term multiplies derivs[2] and derivs[5], which no law sets; it is left out.)
+__global__ void __launch_bounds__(128) k_assemble_jacobian2d(AssemblyArgs A, double* __restrict__ Kj) {
+    constexpr int NEN = 4, ND = 8;
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= A.ne) return;
+    const int64_t ie = e % A.nel[0], je = e / A.nel[0];
+    const int64_t idx[2] = {ie, je};
+    double x0[3] = {0.0, 0.0, 0.0}, h[2];
+    for (int d = 0; d < 2; ++d) {
+        x0[d] = node_coord_1d(idx[d], A.nel[d], A.min[d], A.max[d]);
+        h[d] = node_coord_1d(idx[d] + 1, A.nel[d], A.min[d], A.max[d]) - x0[d];
+    }
+    const int64_t base = ie + A.nnx * je;
+    int64_t inc[NEN];
+    for (int a = 0; a < NEN; ++a) inc[a] = base + (a & 1) + ((a >> 1) & 1) * A.nnx;
+    double Tn[NEN];
+    const bool hasT = A.temperature != nullptr;
+    for (int a = 0; a < NEN; ++a) Tn[a] = hasT ? A.temperature[inc[a]] : 0.0;
+    double un[2][NEN];
+    for (int d = 0; d < 2; ++d)
+        for (int a = 0; a < NEN; ++a) un[d][a] = A.u ? A.u[(int64_t)d * A.nn + inc[a]] : 0.0;
+    const double pressure = A.p ? A.p[e] : 0.0;
+    const uint32_t beg = A.offsets[e], end = A.offsets[e + 1];
+    const uint32_t cnt = end - beg;
+    const double w = 4.0 / (double)(cnt ? cnt : 1);
+    const double detJ = (0.5 * h[0]) * (0.5 * h[1]);
+    double K[ND * ND];
+#pragma unroll
+    for (int k = 0; k < ND * ND; ++k) K[k] = 0.0;
+    for (uint32_t s = beg; s < end; ++s) {
+        double xi[3] = {A.sxi[s], A.sxi[A.nslots + s], 0.0};
+        int mi = A.smat[s];
+        if (mi < 0 || mi >= A.nmat) mi = 0;
+        const uwgpu_material& m = A.mats[mi];
+        double N[NEN], G[2][NEN];
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+            const double sx = (a & 1) ? 1.0 : -1.0, sy = ((a >> 1) & 1) ? 1.0 : -1.0;
+            N[a] = 0.25 * (1.0 + sx * xi[0]) * (1.0 + sy * xi[1]);
+            G[0][a] = (2.0 / h[0]) * 0.25 * sx * (1.0 + sy * xi[1]);
+            G[1][a] = (2.0 / h[1]) * 0.25 * sy * (1.0 + sx * xi[0]);
+        }
+        double L[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+        for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) L[i][j] += G[j][a] * un[i][a];
+        double xg[3] = {x0[0] + 0.5 * h[0] * (xi[0] + 1.0), x0[1] + 0.5 * h[1] * (xi[1] + 1.0), 0.0};
+        const double peta = A.seta_in ? A.seta_in[s] : 0.0;
+        const uint32_t pidx = A.perm[s];
+        double derivs[9];
+        const double eta = run_rheology<2>(m, N, Tn, hasT, xg, A.max[1], peta, L, pressure, A.previous_solution,
+                                           A.pfw ? A.pfw[pidx] : 0.0, nullptr, derivs, true);
+        const double intFac = (A.sw ? A.sw[s] : w) * detJ;
+        const double DuDx = L[0][0], DuDy = L[0][1], DvDx = L[1][0], DvDy = L[1][1];
+#pragma unroll
+        for (int r = 0; r < NEN; ++r) {
+            const double Bj_x = G[0][r], Bj_y = G[1][r];
+            const double DetaDu = derivs[0] * Bj_x + derivs[1] * Bj_y;
+            const double DetaDv = derivs[3] * Bj_x + derivs[4] * Bj_y;
+#pragma unroll
+            for (int c = 0; c < NEN; ++c) {
+                const double Bi_x = G[0][c], Bi_y = G[1][c];
+                double fac = eta * Bj_y + DuDy * DetaDu + DvDx * DetaDu;
+                K[(c * 2) * ND + r * 2] += intFac * (2.0 * Bi_x * (eta * Bj_x + DuDx * DetaDu) + Bi_y * fac);
+                K[(c * 2 + 1) * ND + r * 2] += intFac * (2.0 * Bi_y * DvDy * DetaDu + Bi_x * fac);
+                fac = eta * Bj_x + DvDx * DetaDv + DuDy * DetaDv;
+                K[(c * 2) * ND + r * 2 + 1] += intFac * (2.0 * Bi_x * DuDx * DetaDv + Bi_y * fac);
+                K[(c * 2 + 1) * ND + r * 2 + 1] += intFac * (2.0 * Bi_y * (eta * Bj_y + DvDy * DetaDv) + Bi_x * fac);
+            }
+        }
+    }
+    const int64_t ne = A.ne;
+#pragma unroll
+    for (int k = 0; k < ND * ND; ++k) Kj[(int64_t)k * ne + e] = K[k];
+    double sacc = 0.0;
+#pragma unroll
+    for (int a = 0; a < NEN; ++a)
+#pragma unroll
+        for (int d = 0; d < 2; ++d) {
+            const double sa = ((a >> d) & 1) ? 1.0 : -1.0;
+            const double Gv = -sa * h[1 - d] * 0.5;
+            sacc += Gv * (Gv / K[(a * 2 + d) * ND + a * 2 + d]);
+        }
+    A.Se[e] = sacc;
+}
+
 // ---- tensor-core contraction of the 3D moments into K_e -------------------------------------
 // The 63 pair tables are integer combinations of the 27 moments (table_coefficient), so for a
 // tile of 128 elements they form one product Tab = Mom C^T with C (63 x 27) of small integers.
@@ -945,6 +1247,17 @@ void assemble(Context& c) {
     c.assembled = true;
     c.operator_built = false;
     if (flags & 4u) throw Error(UWGPU_ERR_CUDA, "tensor-core contraction: an MMA did not complete in time");
+    c.assembled_jacobian = false;
+    if (c.jacobian && dim == 2 && !(flags & 3u)) {
+        c.Kjac.ensure((size_t)64 * ne);
+        {
+            LaunchScope ls(c, UWGPU_KERNEL_ASSEMBLY);
+            k_assemble_jacobian2d<<<blocks_for(ne, 128), 128, 0, c.stream>>>(A, c.Kjac.p);
+        }
+        check_launch("k_assemble_jacobian2d");
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+        c.assembled_jacobian = true;
+    }
     if (flags & 2u) throw Error(UWGPU_ERR_ARGUMENT, "material index out of range");
     if (flags & 1u)
         throw Error(UWGPU_ERR_ARGUMENT,

@@ -330,13 +330,16 @@ int uwgpu_get_element_matrices(uwgpu_ctx* ctx, int64_t first, int64_t count, dou
                                        count * sizeof(double), entries, cudaMemcpyDeviceToHost, c.stream));
         };
         std::vector<double> hk, hf, hg;
-        if (Ke) fetch(c.levels[0].Ke.p, np, hk);
+        const bool full = c.assembled_jacobian;   // the Newton form's non-symmetric K_e, all entries
+        if (Ke) fetch(full ? c.Kjac.p : c.levels[0].Ke.p, full ? nd * nd : np, hk);
         if (fe) fetch(c.fe.p, nd, hf);
         if (Ge) fetch(c.Ge.p, nd, hg);
         if (Se) UWG_CUDA(cudaMemcpyAsync(Se, c.Se.p + first, count * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         UWG_CUDA(cudaStreamSynchronize(c.stream));
         for (int64_t e = 0; e < count; ++e) {
-            if (Ke) {
+            if (Ke && full) {
+                for (int k = 0; k < nd * nd; ++k) Ke[e * nd * nd + k] = hk[(size_t)k * count + e];
+            } else if (Ke) {
                 double* K = Ke + e * nd * nd;
                 for (int r = 0; r < nd; ++r)
                     for (int q = r; q < nd; ++q) {
@@ -510,6 +513,15 @@ int uwgpu_bfbt_operator_apply(uwgpu_ctx* ctx, int32_t form, const double* x, dou
     return guarded(ctx, [&](Context& c) {
         UWG_REQUIRE(x && y, UWGPU_ERR_ARGUMENT, "x and y are required");
         uwg::bfbt_operator_hook(c, form, x, y, 0, nullptr);
+    });
+}
+
+int uwgpu_jacobian_set(uwgpu_ctx* ctx, int32_t on) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(!on || (c.has_mesh && c.mesh.dim == 2), UWGPU_ERR_UNSUPPORTED,
+                    "the Newton form of the element matrices is the reference's 2D branch");
+        c.jacobian = on != 0;
+        c.assembled = false;
     });
 }
 

@@ -28,7 +28,11 @@
 #include <iterator>
 #include <type_traits>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "internal.cuh"
+#include "tc.cuh"
 
 namespace uwg {
 
@@ -403,7 +407,7 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf2_dir(int ex, int ey, int6
 // overwrites a plane another thread may still read (two barriers per step).
 struct Mf3 {
     int ex, ey, ez, zc;
-    int64_t nnx, nny, nn;
+    int64_t pitch, nny, nn;   // W layout [d][node plane][y][pitch]: row pitch, rows per plane, entries per d
 };
 
 __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* __restrict__ Wc,
@@ -427,7 +431,7 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* 
     bi /= nty;
     const int zlo = bi * a.zc, zhi = min(zlo + a.zc, ez);
     const int tid = threadIdx.x, tx = tid % kMfX, ty = tid / kMfX;
-    const int64_t exy = (int64_t)ex * ey, nxy = a.nnx * a.nny;
+    const int64_t exy = (int64_t)ex * ey, nxy = a.pitch * a.nny;
     // this thread's two element-halo slots and two node slots of a plane (offsets within a plane)
     int zo[2], nbase[2];
     bool zok[2], nok[2];
@@ -440,7 +444,7 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* 
         zo[s] = zok[s] ? gx + ex * gy : 0;
         const int nx = i % NX, ny = i / NX;
         nok[s] = i < NP && x0 + nx <= ex && y0 + ny <= ey;
-        no[s] = nok[s] ? (x0 + nx) + a.nnx * (y0 + ny) : 0;
+        no[s] = nok[s] ? (x0 + nx) + a.pitch * (y0 + ny) : 0;
         nbase[s] = ny * HX + nx;   // the node's lower-left element in the halo plane
     }
     const bool eok = x0 + tx < ex && y0 + ty < ey;
@@ -543,15 +547,189 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* 
     pdl_trigger();
 }
 
-// Wc_(n,d) = a_d^2 W_(n,d) in FP32 (the weights of the matrix-free apply)
-__global__ void k_mf_weights(int64_t nn, int dim, double a0, double a1, double a2, const double* __restrict__ W,
-                             float* __restrict__ Wc) {
+// The same direction update with the element and weight planes staged by the tensor memory
+// accelerator (cp.async.bulk.tensor), for element grids whose x extent is a multiple of 4 (so
+// that every z row starts on 16 bytes).  Per z step one thread issues two copies into a ring of
+// three stages: the element plane of the column with its halo, as a 40 x 10 box from x0 - 4
+// (x aligned down to 16 bytes; coordinates outside the grid, the halo at the mesh boundary and
+// the planes below and above the mesh, read as zero), and the 36 x 9 x 3 box of the node plane's
+// three weight components.  The copies complete on the stage's mbarrier.  Ten warps: one thread
+// per node of the 33 x 9 node plane, then one per element of the 32 x 8 tile; one block barrier
+// per step.  A copy that has not arrived after a bounded wait makes the block report NaN in the
+// iteration's p.q, which ends the inner solve with UWGPU_ERR_NAN.
+constexpr int kTmThreads = 320;
+constexpr int kTzX = kMfX + 8, kTzY = kMfY + 2;     // staged element plane: 40 x 10
+constexpr int kTwX = kMfX + 4, kTwY = kMfY + 1;     // staged weight plane: 36 x 9, three components
+constexpr int kTzBytes = kTzX * kTzY * 4, kTwBytes = 3 * kTwX * kTwY * 4;
+constexpr int kTzSlot = (kTzBytes + 127) / 128 * 128, kTwSlot = (kTwBytes + 127) / 128 * 128;
+constexpr int kTmStage = kTzSlot + kTwSlot;
+constexpr int kTmNodes = (kMfX + 1) * (kMfY + 1);   // 297
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__global__ void __launch_bounds__(kTmThreads) k_cg_mf3_dir_tma(Mf3 a, const __grid_constant__ CUtensorMap tz,
+                                                              const __grid_constant__ CUtensorMap tw, float* __restrict__ p,
+                                                              float* __restrict__ q, double* __restrict__ scal, int k,
+                                                              int first) {
+    __shared__ __align__(128) unsigned char ring[3 * kTmStage];
+    __shared__ float yb[2][3][kTmNodes];
+    __shared__ __align__(8) uint64_t bar[3];
+    __shared__ double sw[32];
+    __shared__ float s_beta;
+    const int ex = a.ex, ey = a.ey, ez = a.ez;
+    const int ntx = (ex + kMfX - 1) / kMfX, nty = (ey + kMfY - 1) / kMfY;
+    int bi = blockIdx.x;
+    const int x0 = (bi % ntx) * kMfX;
+    bi /= ntx;
+    const int y0 = (bi % nty) * kMfY;
+    bi /= nty;
+    const int zlo = bi * a.zc, zhi = min(zlo + a.zc, ez);
+    const int nsteps = zhi - zlo + 2;   // stages: planes zlo - 1 .. zhi
+    const int tid = threadIdx.x, tx = tid % kMfX, ty = tid / kMfX;
+    const int64_t exy = (int64_t)ex * ey;
+    if (tid == 0) {
+        for (int i = 0; i < 3; ++i) tc::mbar_init(&bar[i], 1);
+    }
+    const uint32_t ring_s = tc::smem_u32(ring);
+    auto issue = [&](int t) {   // stage t = element plane zlo - 1 + t and node plane zlo - 1 + t
+        const int slot = t % 3, plane = zlo - 1 + t;
+        const uint32_t b = tc::smem_u32(&bar[slot]);
+        mbar_expect_tx(b, (uint32_t)(kTzBytes + kTwBytes));
+        tma_load_3d(ring_s + slot * kTmStage, &tz, x0 - 4, y0 - 1, plane, b);
+        tma_load_4d(ring_s + slot * kTmStage + kTzSlot, &tw, x0, y0, plane, 0, b);
+    };
+    pdl_wait();
+    const float beta = first ? 0.f : block_ratio<float>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
+    if (tid == 0) {
+        issue(0);
+        if (nsteps > 1) issue(1);
+    }
+    const bool eok = tid < kMfX * kMfY && x0 + tx < ex && y0 + ty < ey;
+    const int eo = eok ? (x0 + tx) + ex * (y0 + ty) : 0;
+    auto load_pq = [&](int plane, float& pv, float& qv) {
+        const bool ok = !first && eok && plane < zhi;
+        pv = ok ? p[plane * exy + eo] : 0.f;
+        qv = ok ? q[plane * exy + eo] : 0.f;
+    };
+    float pn, qn;
+    load_pq(zlo, pn, qn);
+    // this thread's node of the plane: (nx, ny) in the 33 x 9 node block
+    const bool node = tid < kTmNodes;
+    const int nx = tid % (kMfX + 1), ny = tid / (kMfX + 1);
+    const int zb_node = ny * kTzX + nx + 3;       // its lower-left element in the staged halo plane
+    const int wb_node = ny * kTwX + nx;
+    const int zb_elem = (ty + 1) * kTzX + tx + 4;  // this thread's element in the staged halo plane
+    const int ybase = ty * (kMfX + 1) + tx;
+    bool ok = true;
+    uint32_t phase_bits = 0;   // parity of the next wait, per slot
+    auto wait_slot = [&](int slot) {
+        ok = tc::mbar_wait(&bar[slot], (phase_bits >> slot) & 1u, 1u << 22) && ok;
+        phase_bits ^= 1u << slot;
+    };
+    float lo[3][4], hi[3][4];
+    float local = 0.f;
+    int issued = nsteps > 1 ? 2 : 1;
+    if (nsteps > 0) wait_slot(0);
+    for (int t = 1; t < nsteps; ++t) {
+        const int kk = zlo - 1 + t;
+        wait_slot(t % 3);
+        const float* zp = reinterpret_cast<const float*>(ring + ((t + 2) % 3) * kTmStage);   // element plane kk - 1
+        const float* zc = reinterpret_cast<const float*>(ring + (t % 3) * kTmStage);         // element plane kk
+        const float* wc = reinterpret_cast<const float*>(ring + (t % 3) * kTmStage + kTzSlot);
+        float* yc = yb[t & 1][0];
+        if (node) {
+            const int b = zb_node;
+            const float z000 = zp[b], z100 = zp[b + 1], z010 = zp[b + kTzX], z110 = zp[b + kTzX + 1];
+            const float z001 = zc[b], z101 = zc[b + 1], z011 = zc[b + kTzX], z111 = zc[b + kTzX + 1];
+            const float dx = (z100 - z000) + (z110 - z010) + (z101 - z001) + (z111 - z011);
+            const float dy = (z010 - z000) + (z110 - z100) + (z011 - z001) + (z111 - z101);
+            const float dz = (z001 - z000) + (z101 - z100) + (z011 - z010) + (z111 - z110);
+            yc[tid] = wc[wb_node] * dx;
+            yc[kTmNodes + tid] = wc[kTwX * kTwY + wb_node] * dy;
+            yc[2 * kTmNodes + tid] = wc[2 * kTwX * kTwY + wb_node] * dz;
+        }
+        const float pc = pn, qc = qn;
+        load_pq(kk, pn, qn);   // element plane kk, computed in the next step
+        ok = __syncthreads_and(ok) != 0;
+        if (!ok) break;
+        // the slot of stage t + 1 last held stage t - 2, read by every thread before the barrier
+        if (tid == 0 && issued < nsteps) issue(issued++);
+        if (tid < kMfX * kMfY) {
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4) {
+                const int ni = ybase + (c4 >> 1) * (kMfX + 1) + (c4 & 1);
+#pragma unroll
+                for (int d = 0; d < 3; ++d) hi[d][c4] = yc[d * kTmNodes + ni];
+            }
+            if (t >= 2 && eok) {
+                float out = 0.f;
+#pragma unroll
+                for (int c4 = 0; c4 < 4; ++c4) {
+                    out += (c4 & 1) ? -(lo[0][c4] + hi[0][c4]) : (lo[0][c4] + hi[0][c4]);
+                    out += (c4 >> 1) ? -(lo[1][c4] + hi[1][c4]) : (lo[1][c4] + hi[1][c4]);
+                    out += lo[2][c4] - hi[2][c4];
+                }
+                const int64_t e = (int64_t)(kk - 1) * exy + eo;
+                const float ze = zp[zb_elem];
+                const float pe = first ? ze : fmaf(beta, pc, ze);
+                const float qe = first ? out : fmaf(beta, qc, out);
+                p[e] = pe;
+                q[e] = qe;
+                local = fmaf(pe, qe, local);
+            }
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) lo[d][c4] = hi[d][c4];
+        }
+    }
+    if (!ok) {
+        // let copies still in flight land before the block's shared memory is released
+        if (tid == 0)
+            for (int t = 0; t < 3; ++t) tc::mbar_wait(&bar[t], (phase_bits >> t) & 1u, 1u << 16);
+        local = __int_as_float(0x7fc00000);   // NaN: the host ends the solve
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *rr_slot(scal, k + 1) = 0.0;
+    double tsum = block_sum<float>(local, sw);
+    if (threadIdx.x == 0) atomicAdd(pq_slot(scal, k + 1), tsum);
+    pdl_trigger();
+}
+
+// Wc_(n,d) = a_d^2 W_(n,d) in FP32 (the weights of the matrix-free apply).  2D: [d][node].  3D:
+// rows padded to `pitch` nodes (a multiple of 4, so that every row starts on 16 bytes as the
+// tensor-memory-access copies need), [d][z][y][pitch], the padding zero.
+__global__ void k_mf_weights(int64_t nn, int dim, int64_t nnx, int64_t nny, int64_t pitch, int64_t dstride, double a0,
+                             double a1, double a2, const double* __restrict__ W, float* __restrict__ Wc) {
     const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nn) return;
-    Wc[n] = (float)(a0 * a0 * W[n]);
-    Wc[nn + n] = (float)(a1 * a1 * W[nn + n]);
-    if (dim == 3) Wc[2 * nn + n] = (float)(a2 * a2 * W[2 * nn + n]);
+    if (dim == 2) {
+        Wc[n] = (float)(a0 * a0 * W[n]);
+        Wc[nn + n] = (float)(a1 * a1 * W[nn + n]);
+        return;
+    }
+    const int64_t x = n % nnx, y = (n / nnx) % nny, z = n / (nnx * nny);
+    const int64_t o = x + pitch * (y + nny * z);
+    Wc[o] = (float)(a0 * a0 * W[n]);
+    Wc[dstride + o] = (float)(a1 * a1 * W[nn + n]);
+    Wc[2 * dstride + o] = (float)(a2 * a2 * W[2 * nn + n]);
 }
+
+
 
 // the launch of the matrix-free direction kernel: in 3D the deepest column chunk (up to 16
 // element planes) that still gives four blocks per SM, at least 2 planes
@@ -562,9 +740,32 @@ struct MfLaunch {
     Mf3 a3;
     const float* Wc;
     unsigned blocks;
+    // tensor-memory-access form (3D, x extent a multiple of 4): maps of z and of Wc
+    bool tma;
+    const float* tma_z;
+    CUtensorMap tz;
+    CUtensorMap tw;
 };
 
-static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* Wc, int sms) {
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+        else
+            (void)cudaGetLastError();
+    }
+    return fn;
+}
+
+// z: the vector the direction kernel will read (the tensor map is bound to it)
+static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* Wc, const float* z, int sms) {
     MfLaunch L{};
     L.dim = m.dim;
     L.ex = (int)g.ex;
@@ -579,8 +780,30 @@ static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* Wc, int sms) 
     }
     int zc = 16;
     while (zc > 2 && txy * ((g.ez + zc - 1) / zc) < 4 * (int64_t)sms) zc /= 2;
-    L.a3 = Mf3{(int)g.ex, (int)g.ey, (int)g.ez, zc, m.nnx, m.nny, m.nn};
+    const int64_t pitch = (m.nnx + 3) / 4 * 4;
+    L.a3 = Mf3{(int)g.ex, (int)g.ey, (int)g.ez, zc, pitch, m.nny, pitch * m.nny * m.nnz};
     L.blocks = (unsigned)(txy * ((g.ez + zc - 1) / zc));
+    L.tma = false;
+    auto enc = tensor_map_encoder();
+    if (enc && z && g.ex % 4 == 0 && (reinterpret_cast<uintptr_t>(z) & 15) == 0 &&
+        (reinterpret_cast<uintptr_t>(Wc) & 15) == 0) {
+        const cuuint64_t zdim[3] = {(cuuint64_t)g.ex, (cuuint64_t)g.ey, (cuuint64_t)g.ez};
+        const cuuint64_t zstr[2] = {(cuuint64_t)g.ex * 4, (cuuint64_t)g.ex * g.ey * 4};
+        const cuuint32_t zbox[3] = {(cuuint32_t)kTzX, (cuuint32_t)kTzY, 1};
+        const cuuint64_t wdim[4] = {(cuuint64_t)pitch, (cuuint64_t)m.nny, (cuuint64_t)m.nnz, 3};
+        const cuuint64_t wstr[3] = {(cuuint64_t)pitch * 4, (cuuint64_t)pitch * m.nny * 4,
+                                    (cuuint64_t)pitch * m.nny * m.nnz * 4};
+        const cuuint32_t wbox[4] = {(cuuint32_t)kTwX, (cuuint32_t)kTwY, 1, 3};
+        const cuuint32_t one[4] = {1, 1, 1, 1};
+        CUresult r1 = enc(&L.tz, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(z), zdim, zstr, zbox, one,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        CUresult r2 = enc(&L.tw, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(Wc), wdim, wstr, wbox, one,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        L.tma = r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS;
+        L.tma_z = z;
+    }
     return L;
 }
 
@@ -588,6 +811,8 @@ static void mf_dir(const MfLaunch& L, cudaStream_t st, const float* z, float* p,
                    int first) {
     const unsigned nt = kMfX * kMfY;
     if (L.dim == 2) launch_pdl(k_cg_mf2_dir, L.blocks, nt, st, L.ex, L.ey, L.nnx, L.nn, L.Wc, z, p, q, scal, k, first);
+    else if (L.tma && z == L.tma_z)
+        launch_pdl(k_cg_mf3_dir_tma, L.blocks, (unsigned)kTmThreads, st, L.a3, L.tz, L.tw, p, q, scal, k, first);
     else launch_pdl(k_cg_mf3_dir, L.blocks, nt, st, L.a3, L.Wc, z, p, q, scal, k, first);
 }
 
@@ -863,7 +1088,7 @@ static int gwg_cg_T(Context& c, const T* A, const float* Wmf, const T* dinv, con
     if (Wmf) {
         int sms = 0;
         UWG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
-        mf = mf_launch(m, g, Wmf, sms);
+        mf = mf_launch(m, g, Wmf, reinterpret_cast<const float*>(work + ne), sms);
     }
     T* r = work;
     T* z = work + ne;
@@ -959,6 +1184,13 @@ int gwg_cg32_mf(Context& c, const float* Wc, const float* dinv, const double* b,
     return gwg_cg_T<float>(c, nullptr, Wc, dinv, b, x, rtol, maxit, work, scal);
 }
 
+// Entries of the folded-weight array of the matrix-free apply (3D rows padded, see k_mf_weights).
+int64_t mf_weights_size(const MeshDesc& m) {
+    if (m.dim == 2) return m.nn * 2;
+    const int64_t pitch = (m.nnx + 3) / 4 * 4;
+    return 3 * pitch * m.nny * m.nnz;
+}
+
 // the folded weights of the matrix-free apply, Wc_(n,d) = a_d^2 W_(n,d) (FP32), for the uniform
 // mesh's a_d = prod_{k != d} h_k / 2^(dim-1)
 void gwg_mf_weights(Context& c, const double* W, float* Wc) {
@@ -972,8 +1204,11 @@ void gwg_mf_weights(Context& c, const double* W, float* Wc) {
         for (int k = 0; k < m.dim; ++k)
             if (k != d) a[d] *= h[k];
     }
+    const int64_t pitch = (m.nnx + 3) / 4 * 4, dstride = pitch * m.nny * m.nnz;
+    if (m.dim == 3) UWG_CUDA(cudaMemsetAsync(Wc, 0, (size_t)mf_weights_size(m) * sizeof(float), c.stream));
     LaunchScope ls(c, -1);
-    k_mf_weights<<<blocks_for(m.nn, 256), 256, 0, c.stream>>>(m.nn, m.dim, a[0], a[1], a[2], W, Wc);
+    k_mf_weights<<<blocks_for(m.nn, 256), 256, 0, c.stream>>>(m.nn, m.dim, m.nnx, m.nny, pitch, dstride, a[0], a[1],
+                                                              a[2], W, Wc);
     check_launch("k_mf_weights");
 }
 
@@ -1008,11 +1243,11 @@ void bfbt_operator_hook(Context& c, int form, const double* xh, double* yh, int 
         pq32.ensure((size_t)2 * ne);
         to_float(c, x.p, x32.p, ne);
         if (form == 1) {
-            W32.ensure((size_t)nv);
+            W32.ensure((size_t)mf_weights_size(m));
             gwg_mf_weights(c, W.p, W32.p);
             int sms = 0;
             UWG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
-            mf = mf_launch(m, g, W32.p, sms);
+            mf = mf_launch(m, g, W32.p, x32.p, sms);
         } else {
             A32.ensure((size_t)nb * ne);
             to_float(c, A.p, A32.p, (int64_t)nb * ne);

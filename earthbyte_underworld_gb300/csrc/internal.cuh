@@ -174,6 +174,11 @@ struct Context {
     DArray<double> Ge;        // entry-major [k][e]
     bool assembled = false;
     int assembly_mode = UWGPU_ASSEMBLY_FP64;
+    // Newton form of the 2D element matrices (SystemLinearEquations nlFormJacobian): full
+    // non-symmetric K_e [64][e] of the last assembly
+    bool jacobian = false;
+    bool assembled_jacobian = false;
+    DArray<double> Kjac;
     DArray<double> mom;       // 3D moments [27][e] of the tensor-core contraction
 
     // per-axis element widths of the fine mesh (device), and the mesh they belong to

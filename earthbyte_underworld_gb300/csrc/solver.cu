@@ -50,6 +50,7 @@ int gwg_cg_mg32(Context& c, const float* A, const float* dinv, const double* b, 
 int gwg_cg32_mf(Context& c, const float* Wc, const float* dinv, const double* b, float* x, double rtol, int maxit,
                 float* work, double* scal);
 void gwg_mf_weights(Context& c, const double* W, float* Wc);
+int64_t mf_weights_size(const MeshDesc& m);
 void op_wg32(Context& c, const float* p, const float* W, float* s);
 void op_gt32(Context& c, const float* s, float* q);
 void to_float(Context& c, const double* a, float* b, int64_t n);
@@ -993,7 +994,7 @@ void Bsscr::run() {
             pz32.ensure(4 * npres);
             scal32.ensure(8);
             to_float(c, bw.p, bw32.p, nv);
-            bwc32.ensure(nv);
+            bwc32.ensure((size_t)mf_weights_size(c.mesh));
             gwg_mf_weights(c, bw.p, bwc32.p);   // the matrix-free inner operator's folded weights
             // Jacobi inner solves: the FP32 stencil while it and the CG vectors take at most half
             // of L2 (streamed from L2 it is the faster form), else the matrix-free apply, which
@@ -1064,6 +1065,9 @@ void Bsscr::run() {
 
 void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
     UWG_REQUIRE(c.assembled, UWGPU_ERR_STATE, "solve requested before assembly");
+    UWG_REQUIRE(!c.assembled_jacobian, UWGPU_ERR_UNSUPPORTED,
+                "the Newton form's element matrices are not symmetric; the solver here takes the Picard form "
+                "(uwgpu_jacobian_set(ctx, 0) and assemble again)");
     UWG_REQUIRE(o.precision == UWGPU_PREC_FP64 || o.precision == UWGPU_PREC_MIXED, UWGPU_ERR_ARGUMENT, "bad precision");
     UWG_REQUIRE(o.schur_type == UWGPU_SCHUR_CG || o.schur_type == UWGPU_SCHUR_FGMRES, UWGPU_ERR_ARGUMENT, "bad Schur type");
     UWG_REQUIRE(o.schur_pc >= 0 && o.schur_pc <= 3, UWGPU_ERR_ARGUMENT, "bad Schur preconditioner");

@@ -30,6 +30,7 @@ LAW_DEPTH_DEPENDENT = 8
 LAW_NON_NEWTONIAN = 9
 LAW_VON_MISES = 10
 LAW_BYERLEE = 11
+LAW_MOHR_COULOMB = 12
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -150,6 +151,7 @@ def load(build_if_missing: bool = True):
         L.uwgpu_learned_train.argtypes = [P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P, P]
         L.uwgpu_tc_check.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P, P]
         L.uwgpu_assembly_set.argtypes = [P, C.c_int32]
+        L.uwgpu_jacobian_set.argtypes = [P, C.c_int32]
         L.uwgpu_strain_weakening_set.argtypes = [P, P]
         L.uwgpu_strain_weakening_advance.argtypes = [P, C.c_double]
         L.uwgpu_strain_weakening_get.argtypes = [P, P, P]
@@ -302,6 +304,10 @@ class Context:
         inc = np.zeros(self.npoints)
         self._check(self._L.uwgpu_strain_weakening_get(self._h, _ptr(pfw), _ptr(inc)))
         return pfw, inc
+
+    def jacobian_set(self, on=True):
+        """Newton (Jacobian) form of the 2D element matrices for the next assemblies."""
+        self._check(self._L.uwgpu_jacobian_set(self._h, 1 if on else 0))
 
     def assembly_set(self, mode):
         """ASSEMBLY_FP64 (default) or ASSEMBLY_TENSOR (tensor-core contraction of the moments, 3D)."""

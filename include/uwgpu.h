@@ -61,9 +61,14 @@ enum {
                                          StrainWeakening of its cohesion (StrainWeakening.c:428-503); p0=cohesion
                                          p1=cohesionAfterSoftening p2=minimumViscosity p3=softeningStrain (<= 0: no weakening)
                                          p4=healingRate p5=strainRateSoftening (0/1) */
-    UWGPU_LAW_BYERLEE = 11            /* Underworld/Rheology/src/Byerlee.c:157-198: the VonMises law with the yield stress
+    UWGPU_LAW_BYERLEE = 11,           /* Underworld/Rheology/src/Byerlee.c:157-198: the VonMises law with the yield stress
                                          cohesion + depthCoefficient (max_y - y); p0=cohesion p1=depthCoefficient, p2..p5 as
                                          for VON_MISES (p3, p4: the strain-weakening history it updates) */
+    UWGPU_LAW_MOHR_COULOMB = 12       /* Underworld/Rheology/src/MohrCoulomb.c:208-402: indicator from the principal stresses
+                                         of the deviatoric strain rate's stress, criterion (C + mu p) sin 2 theta; p0=cohesion
+                                         p1=cohesionAfterSoftening p2=frictionCoefficient p3=frictionCoefficientAfterSoftening
+                                         p4=minimumYieldStress (0: the effective cohesion) p5=minimumViscosity
+                                         p6=softeningStrain (<= 0: no weakening) p7=healingRate */
 };
 
 typedef struct {
@@ -269,6 +274,15 @@ int uwgpu_assemble(uwgpu_ctx* ctx);
  * Replaces the B^T D B accumulation of ConstitutiveMatrixCartesian.c:388-407 in the same way. */
 enum { UWGPU_ASSEMBLY_FP64 = 0, UWGPU_ASSEMBLY_TENSOR = 1 };
 int uwgpu_assembly_set(uwgpu_ctx* ctx, int32_t mode);
+
+/* Newton form of the element matrices (the SLE's nlFormJacobian, 2D): with on != 0 the next
+ * assemblies add the viscosity's derivatives with respect to the velocity gradient that yielding
+ * laws (VON_MISES, DRUCKER_PRAGER) provide to the viscous term, as the 2D branch of
+ * ConstitutiveMatrixCartesian.c:360-383 does, around the context's current solution.  The
+ * resulting K_e is not symmetric: uwgpu_get_element_matrices returns all nd x nd entries (row =
+ * test function dof), and uwgpu_solve_bsscr refuses it with UWGPU_ERR_UNSUPPORTED (the solver
+ * here takes the Picard form).  3D: UWGPU_ERR_UNSUPPORTED (the reference has no 3D branch). */
+int uwgpu_jacobian_set(uwgpu_ctx* ctx, int32_t on);
 
 /* Per-element results of the last assembly, copied to the host: the per-element callback
  * StiffnessMatrixTerm_AssembleElementFunction (StgFEM/SLE/SystemSetup/src/StiffnessMatrixTerm.c

@@ -26,6 +26,7 @@ LAW_DRUCKER_PRAGER = 5
 LAW_PARTICLE_VISCOSITY = 6
 LAW_VON_MISES = 10
 LAW_BYERLEE = 11
+LAW_MOHR_COULOMB = 12
 
 
 def strain_weakening_advance(pfw, incr, dt):
@@ -52,7 +53,7 @@ class Material(C.Structure):
 class Fields(C.Structure):
     _fields_ = [("temperature", C.c_void_p), ("velocity", C.c_void_p), ("pressure", C.c_void_p),
                 ("previous_solution", C.c_int32), ("vert_axis", C.c_int32), ("gravity", C.c_double),
-                ("pfw", C.c_void_p), ("pfw_incr", C.c_void_p)]
+                ("pfw", C.c_void_p), ("pfw_incr", C.c_void_p), ("nl_form_jacobian", C.c_int32), ("pad", C.c_int32)]
 
 
 class SolveOpts(C.Structure):
@@ -180,7 +181,7 @@ def map_points(m, xyz, use_newton=True):
 
 
 def make_fields(temperature=None, velocity=None, pressure=None, previous_solution=False,
-                vert_axis=1, gravity=0.0, pfw=None, pfw_incr=None):
+                vert_axis=1, gravity=0.0, pfw=None, pfw_incr=None, jacobian=False):
     """pfw: per-point postFailureWeakening (strain-weakening history); pfw_incr: a float64 array of
     the same length that the assembly fills with its time derivative."""
     f = Fields()
@@ -195,6 +196,7 @@ def make_fields(temperature=None, velocity=None, pressure=None, previous_solutio
             keep.append(arr)
             setattr(f, name, arr.ctypes.data)
     f.previous_solution = 1 if previous_solution else 0
+    f.nl_form_jacobian = 1 if jacobian else 0
     f.vert_axis = vert_axis
     f.gravity = gravity
     f._keep = keep

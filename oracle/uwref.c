@@ -530,6 +530,178 @@ static double stress_invariant(const rheo_point* rp, double eta) {
     }
 }
 
+/* velocity gradient L[i][j] = du_i/dx_j at the point (FeVariable_InterpolateDerivatives_WithGNx) */
+static void velocity_gradient(const rheo_point* rp, double L[3][3]) {
+    int dim = rp->m->dim, nen = (dim == 3) ? 8 : 4;
+    memset(L, 0, 9 * sizeof(double));
+    if (!rp->f->velocity) return;
+    for (int a = 0; a < nen; ++a)
+        for (int i = 0; i < dim; ++i)
+            for (int j = 0; j < dim; ++j) L[i][j] += rp->GNx[j * nen + a] * rp->f->velocity[rp->inc[a] * dim + i];
+}
+
+/* the Newton terms of _VonMises_HasYielded (VonMises.c:259-268), with the viscosity before the
+ * correction, the stored criterion and the stress (2D [xx, yy, xy], 3D [xx, yy, zz, ...]) of the
+ * yield indicator */
+static void yield_derivs(const rheo_point* rp, double visc0, double crit, double ind, double* derivs) {
+    if (!derivs || !rp->f->nl_form_jacobian) return;
+    double L[3][3];
+    velocity_gradient(rp, L);
+    double st[3];
+    st[0] = 2.0 * visc0 * L[0][0];
+    st[1] = 2.0 * visc0 * L[1][1];
+    st[2] = rp->m->dim == 3 ? 2.0 * visc0 * L[2][2] : visc0 * 2.0 * (0.5 * (L[0][1] + L[1][0]));
+    double coef = -visc0 * crit / (2.0 * ind * ind * ind);
+    derivs[0] += coef * 2.0 * visc0 * st[0];
+    derivs[4] += coef * 2.0 * visc0 * st[1];
+    derivs[1] += coef * 2.0 * visc0 * st[2];
+    derivs[3] += coef * 2.0 * visc0 * st[2];
+}
+
+/* ---- eigenvalues of a symmetric stress tensor (StgDomain/Geometry/src/TensorMath.c) ---------
+ * Storage: 2D [xx, yy, xy], 3D [xx, yy, zz, xy, xz, yz].  EQL is the reference's absolute
+ * comparison |a - b| < 1e-8 (TensorMath.c:760). */
+#define UWR_EQL(A, B) (fabs((A) - (B)) < 1.0e-8)
+#define UWR_PI 3.14159265358979323846   /* M_PI of math.h */
+
+/* CubicSolver_OnlyRealRoots (TensorMath.c:941-975) */
+static void cubic_real_roots(double a2, double a1, double a0, double* root) {
+    double Q = (3.0 * a1 - a2 * a2) / 9.0;
+    double R = (9.0 * a2 * a1 - 27.0 * a0 - 2.0 * a2 * a2 * a2) / 54.0;
+    double D = Q * Q * Q + R * R;
+    if (UWR_EQL(D, 0.0)) {
+        double halfB = R < 0.0 ? -pow(-R, 1.0 / 3.0) : pow(R, 1.0 / 3.0);
+        root[0] = -a2 / 3.0 + 2.0 * halfB;
+        root[1] = root[2] = -a2 / 3.0 - halfB;
+        return;
+    }
+    double theta = acos(R / sqrt(-Q * Q * Q)) / 3.0;
+    double factor = 2.0 * sqrt(-Q);
+    root[0] = factor * cos(theta) - a2 / 3.0;
+    root[1] = factor * cos(theta + 2.0 * UWR_PI / 3.0) - a2 / 3.0;
+    root[2] = factor * cos(theta + 4.0 * UWR_PI / 3.0) - a2 / 3.0;
+}
+
+/* SymmetricTensor_CalcEigenvector3D's test (TensorMath.c:726-758): false when no eigenvector
+ * formula applies for this eigenvalue */
+static int eigvec3_ok(const double* t, double lam) {
+    double A = t[0] - lam, B = t[1] - lam, d = t[3], e = t[4], f = t[5];
+    if (!UWR_EQL(B * e, f * d) && !UWR_EQL(e, 0.0)) return 1;
+    if (!UWR_EQL(f * A, d * e) && !UWR_EQL(e, 0.0)) return 1;
+    if (!UWR_EQL(d * d, B * A) && !UWR_EQL(d, 0.0)) return 1;
+    return 0;
+}
+
+/* Matrix_CalcAllEigenvectorsJacobi (TensorMath.c:820-909): cyclic Jacobi rotations with the
+ * threshold sweeps of Numerical Recipes in C (2nd ed., section 11.1); eigenvalues only */
+static void jacobi_eigenvalues3(const double* t, double* ev) {
+    double a[3][3] = {{t[0], t[3], t[4]}, {t[3], t[1], t[5]}, {t[4], t[5], t[2]}};
+    double b[3], z[3];
+    for (int ip = 0; ip < 3; ++ip) {
+        b[ip] = ev[ip] = a[ip][ip];
+        z[ip] = 0.0;
+    }
+    for (int sweep = 1; sweep <= 50; ++sweep) {
+        double sum = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
+        if (sum == 0.0) break;
+        double tresh = sweep < 4 ? 0.2 * sum / 9.0 : 0.0;
+        for (int ip = 0; ip < 2; ++ip)
+            for (int iq = ip + 1; iq < 3; ++iq) {
+                double g = 100.0 * fabs(a[ip][iq]);
+                if (sweep > 4 && (fabs(ev[ip]) + g) == fabs(ev[ip]) && (fabs(ev[iq]) + g) == fabs(ev[iq])) {
+                    a[ip][iq] = 0.0;
+                } else if (fabs(a[ip][iq]) > tresh) {
+                    double h = ev[iq] - ev[ip], tt;
+                    if ((double)(fabs(h) + g) == (double)fabs(h)) {
+                        tt = a[ip][iq] / h;
+                    } else {
+                        double theta = 0.5 * h / a[ip][iq];
+                        tt = 1.0 / (fabs(theta) + sqrt(1.0 + theta * theta));
+                        if (theta < 0.0) tt = -tt;
+                    }
+                    double c = 1.0 / sqrt(1 + tt * tt), sn = tt * c, tau = sn / (1.0 + c);
+                    h = tt * a[ip][iq];
+                    z[ip] -= h;
+                    z[iq] += h;
+                    ev[ip] -= h;
+                    ev[iq] += h;
+                    a[ip][iq] = 0.0;
+                    for (int j = 0; j <= ip - 1; ++j) {
+                        double g1 = a[j][ip], h1 = a[j][iq];
+                        a[j][ip] = g1 - sn * (h1 + g1 * tau);
+                        a[j][iq] = h1 + sn * (g1 - h1 * tau);
+                    }
+                    for (int j = ip + 1; j <= iq - 1; ++j) {
+                        double g1 = a[ip][j], h1 = a[j][iq];
+                        a[ip][j] = g1 - sn * (h1 + g1 * tau);
+                        a[j][iq] = h1 + sn * (g1 - h1 * tau);
+                    }
+                    for (int j = iq + 1; j < 3; ++j) {
+                        double g1 = a[ip][j], h1 = a[iq][j];
+                        a[ip][j] = g1 - sn * (h1 + g1 * tau);
+                        a[iq][j] = h1 + sn * (g1 - h1 * tau);
+                    }
+                }
+            }
+        for (int ip = 0; ip < 3; ++ip) {
+            b[ip] += z[ip];
+            ev[ip] = b[ip];
+            z[ip] = 0.0;
+        }
+    }
+}
+
+static void sort3(double* v) {
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2 - i; ++j)
+            if (v[j] > v[j + 1]) { double t = v[j]; v[j] = v[j + 1]; v[j + 1] = t; }
+}
+
+/* SymmetricTensor_CalcAllEigenvectors (TensorMath.c:619-776): ascending eigenvalues */
+static void sym_eigenvalues(const double* t, int dim, double* ev) {
+    if (dim == 2) {   /* SymmetricTensor_CalcAllEigenvalues2D */
+        double r = sqrt(0.25 * (t[0] - t[1]) * (t[0] - t[1]) + t[2] * t[2]);
+        double avg = 0.5 * (t[0] + t[1]);
+        ev[0] = avg - r;
+        ev[1] = avg + r;
+        return;
+    }
+    double a2 = -t[0] - t[1] - t[2];
+    double a1 = (t[0] * t[1]) + (t[0] * t[2]) + (t[1] * t[2]) - (t[3] * t[3]) - (t[4] * t[4]) - (t[5] * t[5]);
+    double a0 = -(t[0] * t[1] * t[2]) - 2.0 * (t[3] * t[4] * t[5]) + (t[0] * t[5] * t[5]) + (t[1] * t[4] * t[4]) +
+                (t[2] * t[3] * t[3]);
+    cubic_real_roots(a2, a1, a0, ev);
+    for (int i = 0; i < 3; ++i)
+        if (!eigvec3_ok(t, ev[i])) {
+            jacobi_eigenvalues3(t, ev);
+            break;
+        }
+    sort3(ev);
+}
+
+/* deviatoric strain rate at the point (MohrCoulomb.c:355-402: the strain rate with its trace
+ * divided among the diagonal removed), symmetric storage */
+static void deviatoric_strain_rate(const rheo_point* rp, double* sr) {
+    int dim = rp->m->dim, nen = (dim == 3) ? 8 : 4;
+    double L[3][3] = {{0}};
+    if (rp->f->velocity) {
+        for (int a = 0; a < nen; ++a)
+            for (int i = 0; i < dim; ++i)
+                for (int j = 0; j < dim; ++j)
+                    L[i][j] += rp->GNx[j * nen + a] * rp->f->velocity[rp->inc[a] * dim + i];
+    }
+    if (dim == 3) {
+        sr[0] = L[0][0]; sr[1] = L[1][1]; sr[2] = L[2][2];
+        sr[3] = 0.5 * (L[0][1] + L[1][0]); sr[4] = 0.5 * (L[0][2] + L[2][0]); sr[5] = 0.5 * (L[1][2] + L[2][1]);
+        double tr = sr[0] + sr[1] + sr[2];
+        for (int i = 0; i < 3; ++i) sr[i] -= tr / 3.0;
+    } else {
+        sr[0] = L[0][0]; sr[1] = L[1][1]; sr[2] = 0.5 * (L[0][1] + L[1][0]);
+        double tr = sr[0] + sr[1];
+        for (int i = 0; i < 2; ++i) sr[i] -= tr / 2.0;
+    }
+}
+
 /* global coordinate of the point: FeMesh_CoordLocalToGlobal = sum_a N_a(xi) x_a */
 static void point_coord(const rheo_point* rp, double* x) {
     int nen = (rp->m->dim == 3) ? 8 : 4;
@@ -562,14 +734,23 @@ static double strain_rate_invariant(const rheo_point* rp) {
 /* The rheology list of a RheologyMaterial (Underworld/Rheology/src/Rheology_Register.c:61-77).
  * Every law in scope keeps D isotropic, so the constitutive matrix is tracked by eta:
  * SetIsotropicViscosity (ConstitutiveMatrix.c:362-367) sets it, IsotropicCorrection adds to it. */
-static double run_rheologies(const uwr_material* mat, const rheo_point* rp) {
+/* derivs (9, may be NULL): the constitutive matrix's viscosity derivatives of the Newton form
+ * (ConstitutiveMatrix.c:362-367 zeroes them with every SetIsotropicViscosity; the VonMises-family
+ * _HasYielded adds its terms when the SLE forms the Jacobian, VonMises.c:259-268). */
+#define UWR_SET_VISC(v)                                             \
+    do {                                                            \
+        eta = (v);                                                  \
+        if (derivs) memset(derivs, 0, 9 * sizeof(double));          \
+    } while (0)
+static double run_rheologies(const uwr_material* mat, const rheo_point* rp, double* derivs) {
     double eta = 0.0;
     int dim = rp->m->dim;
+    if (derivs) memset(derivs, 0, 9 * sizeof(double));
     for (int l = 0; l < mat->n_laws; ++l) {
         const uwr_law* law = &mat->laws[l];
         switch (law->law) {
         case UWR_LAW_MATERIAL_VISCOSITY: /* MaterialViscosity.c:119-139 */
-            eta = law->p[0];
+            UWR_SET_VISC(law->p[0]);
             break;
         case UWR_LAW_ARRHENIUS: { /* Arrhenius.c:156-200 */
             double T = rp->f->temperature ? interp_temperature(rp) : 0.0;
@@ -578,21 +759,24 @@ static double run_rheologies(const uwr_material* mat, const rheo_point* rp) {
                 double y = 0.0;
                 for (int a = 0; a < nen; ++a) y += rp->N[a] * rp->nodes[a][1];
                 double depth = rp->m->max[1] - y;
-                eta = law->p[0] * exp((law->p[1] + law->p[2] * depth) / (T + law->p[3]));
+                UWR_SET_VISC(law->p[0] * exp((law->p[1] + law->p[2] * depth) / (T + law->p[3])));
             } else {
-                eta = law->p[0] * exp((law->p[1]) / (T + law->p[3]));
+                UWR_SET_VISC(law->p[0] * exp((law->p[1]) / (T + law->p[3])));
             }
             break;
         }
         case UWR_LAW_FRANK_KAMENETSKII: { /* FrankKamenetskii.c:134-152 */
             double T = rp->f->temperature ? interp_temperature(rp) : 0.0;
-            eta = law->p[0] * exp(-law->p[1] * T);
+            UWR_SET_VISC(law->p[0] * exp(-law->p[1] * T));
             break;
         }
-        case UWR_LAW_VISCOSITY_LIMITER: /* ViscosityLimiter.c:106-126 */
-            if (eta > law->p[0]) eta = law->p[0];
-            if (eta < law->p[1]) eta = law->p[1];
+        case UWR_LAW_VISCOSITY_LIMITER: { /* ViscosityLimiter.c:106-126 */
+            double v = eta;
+            if (v > law->p[0]) v = law->p[0];
+            if (v < law->p[1]) v = law->p[1];
+            UWR_SET_VISC(v);
             break;
+        }
         case UWR_LAW_DRUCKER_PRAGER: { /* YieldRheology.c:198-243, VonMises.c:206-269, DruckerPrager.c:236-345 */
             double minVisc = law->p[3];
             if (!rp->f->previous_solution) break;
@@ -612,30 +796,33 @@ static double run_rheologies(const uwr_material* mat, const rheo_point* rp) {
             double crit = dpFric * pressure + dpCoh;
             if (crit < law->p[2]) crit = law->p[2];
             if (crit < ind) {
+                double visc0 = eta;
                 double beta = 1.0 - crit / ind;
                 double corr = -eta * beta;
                 if ((eta + corr) < minVisc) corr = minVisc - eta;
                 eta += corr;
+                yield_derivs(rp, visc0, crit, ind, derivs);
             }
-            if (eta < minVisc) eta = minVisc;
+            if (eta < minVisc) UWR_SET_VISC(minVisc);
             break;
         }
         case UWR_LAW_PARTICLE_VISCOSITY:
-            eta = rp->point_eta;
+            UWR_SET_VISC(rp->point_eta);
             break;
         case UWR_LAW_LINEAR_VISCOSITY: { /* LinearViscosity.c:154-190, coordinate by FeMesh_CoordLocalToGlobal */
             double x[3];
             point_coord(rp, x);
-            eta = law->p[1] * x[0] + law->p[2] * x[1] + law->p[4] * x[0] * x[1] + law->p[0];
+            double v = law->p[1] * x[0] + law->p[2] * x[1] + law->p[4] * x[0] * x[1] + law->p[0];
             if (dim == 3)
-                eta += law->p[3] * x[2] + law->p[5] * x[0] * x[2] + law->p[6] * x[1] * x[2] + law->p[7] * x[0] * x[1] * x[2];
+                v += law->p[3] * x[2] + law->p[5] * x[0] * x[2] + law->p[6] * x[1] * x[2] + law->p[7] * x[0] * x[1] * x[2];
+            UWR_SET_VISC(v);
             break;
         }
         case UWR_LAW_DEPTH_DEPENDENT: { /* DepthDependentViscosity.c:165-188 */
             double x[3];
             point_coord(rp, x);
             int axis = (int)law->p[3];
-            eta = law->p[0] * exp(law->p[1] * (x[axis] - law->p[2]));
+            UWR_SET_VISC(law->p[0] * exp(law->p[1] * (x[axis] - law->p[2])));
             break;
         }
         case UWR_LAW_VON_MISES:     /* YieldRheology.c:198-243 with VonMises.c:175-269 */
@@ -667,16 +854,67 @@ static double run_rheologies(const uwr_material* mat, const rheo_point* rp) {
                                                      : (crit / eta) * (beta / (1.0 - beta) - healing * pfw);
             }
             if (crit < ind) {   /* _VonMises_HasYielded */
+                double visc0 = eta;
                 if (law->p[5] != 0.0) {
-                    eta = 2.0 * crit * crit * eta / (crit * crit + ind * ind);
+                    UWR_SET_VISC(2.0 * crit * crit * eta / (crit * crit + ind * ind));
                 } else {
                     double beta = 1.0 - crit / ind;
                     double corr = -eta * beta;
                     if ((eta + corr) < minVisc) corr = minVisc - eta;
                     eta += corr;
                 }
+                /* the Newton terms use the criterion the law stored; Byerlee's criterion
+                 * (Byerlee.c:157-198) stores none, taken as 0 here (no terms) */
+                yield_derivs(rp, visc0, law->law == UWR_LAW_VON_MISES ? crit : 0.0, ind, derivs);
             }
-            if (eta < minVisc) eta = minVisc;
+            if (eta < minVisc) UWR_SET_VISC(minVisc);
+            break;
+        }
+        case UWR_LAW_MOHR_COULOMB: { /* MohrCoulomb.c:208-402 via YieldRheology.c:198-243 */
+            if (!rp->f->previous_solution) break;
+            const double minVisc = law->p[5], soft = law->p[6], healing = law->p[7];
+            double sr[6], st[6], ev[3];
+            deviatoric_strain_rate(rp, sr);
+            int ns = dim == 3 ? 6 : 3;
+            for (int i = 0; i < ns; ++i) st[i] = 2.0 * eta * sr[i];   /* isotropic D, isDiagonal */
+            sym_eigenvalues(st, dim, ev);
+            double pfw = (rp->f->pfw && rp->p >= 0) ? rp->f->pfw[rp->p] : 0.0;
+            if (pfw < 0.0) pfw = 0.0;
+            double ratio = 0.0;
+            if (soft > 0.0) {
+                ratio = pfw / soft;
+                if (ratio > 1.0) ratio = 1.0;
+            }
+            const double alpha = law->p[2] * (1.0 - ratio) + law->p[3] * ratio;   /* effective friction */
+            const double coh = law->p[0] * (1.0 - ratio) + law->p[1] * ratio;     /* effective cohesion */
+            /* _MohrCoulomb_GetYieldIndicator */
+            double smin = ev[0], smax = dim == 2 ? ev[1] : ev[2];
+            double sigma_ns = 0.5 * (smax - smin);
+            if (dim == 3) {
+                double theta = 0.5 * atan(1.0 / alpha);
+                double factor = 1 / (sin(2 * theta) - alpha * cos(2 * theta));
+                sigma_ns -= (smax + smin) * 0.5 * alpha * factor;
+            }
+            double ind = fabs(sigma_ns);
+            /* _MohrCoulomb_GetYieldCriterion */
+            double pressure = rp->f->pressure ? rp->f->pressure[rp->e] : 0.0;
+            double theta = 0.5 * atan(1.0 / alpha);
+            double factor = sin(2 * theta);
+            double crit = alpha * pressure * factor + coh * factor;
+            double minYS = law->p[4] == 0.0 ? coh : law->p[4];
+            if (crit < minYS * factor) crit = minYS * factor;
+            if (soft > 0.0 && rp->f->pfw_incr && rp->p >= 0) {
+                double beta = (crit == 0.0 || ind == 0.0) ? 0.0 : 1.0 - crit / ind;
+                rp->f->pfw_incr[rp->p] = beta <= 0.0 ? -healing * pfw
+                                                     : (crit / eta) * (beta / (1.0 - beta) - healing * pfw);
+            }
+            if (crit < ind) {   /* _MohrCoulomb_HasYielded */
+                double beta = 1.0 - crit / ind;
+                double corr = -eta * beta;
+                if ((eta + corr) < minVisc) corr = minVisc - eta;
+                eta += corr;
+            }
+            if (eta < minVisc) UWR_SET_VISC(minVisc);
             break;
         }
         case UWR_LAW_NON_NEWTONIAN: { /* NonNewtonian.c:139-171 */
@@ -684,7 +922,7 @@ static double run_rheologies(const uwr_material* mat, const rheo_point* rp) {
             if (sri == 0) break;
             double n = law->p[0];
             if (fabs(n - 1.0) < 1.0e-10) break;
-            eta = pow(2.0 * sri, 1.0 / n - 1.0) * pow(eta, 1.0 / n);
+            UWR_SET_VISC(pow(2.0 * sri, 1.0 / n - 1.0) * pow(eta, 1.0 / n));
             break;
         }
         default:
@@ -734,6 +972,29 @@ static void accumulate_Ke(int dim, int nen, double eta, double factor, const dou
                     K2[j] += bz * DB[2][j] + bx * DB[4][j] + by * DB[5][j];
                 }
             }
+        }
+    }
+}
+
+/* The Newton (Jacobian) branch of the 2D element loop, ConstitutiveMatrixCartesian.c:360-383:
+ * elStiffMat[col][row] with the viscosity derivatives of the point.  (The reference's Ni term is
+ * multiplied by derivs[2] and derivs[5], which no law sets: it is left out.) */
+static void accumulate_Ke_jacobian2d(double eta, const double* derivs, double L[3][3], double intFac,
+                                     const double* GNx, double* Ke) {
+    const int nen = 4, nd = 8;
+    double DuDx = L[0][0], DuDy = L[0][1], DvDx = L[1][0], DvDy = L[1][1];
+    for (int r = 0; r < nen; ++r) {
+        double Bj_x = GNx[0 * nen + r], Bj_y = GNx[1 * nen + r];
+        double DetaDu = derivs[0] * Bj_x + derivs[1] * Bj_y;
+        double DetaDv = derivs[3] * Bj_x + derivs[4] * Bj_y;
+        for (int c = 0; c < nen; ++c) {
+            double Bi_x = GNx[0 * nen + c], Bi_y = GNx[1 * nen + c];
+            double fac = eta * Bj_y + DuDy * DetaDu + DvDx * DetaDu;
+            Ke[(c * 2) * nd + r * 2] += intFac * (2.0 * Bi_x * (eta * Bj_x + DuDx * DetaDu) + Bi_y * fac);
+            Ke[(c * 2 + 1) * nd + r * 2] += intFac * (2.0 * Bi_y * DvDy * DetaDu + Bi_x * fac);
+            fac = eta * Bj_x + DvDx * DetaDv + DuDy * DetaDv;
+            Ke[(c * 2) * nd + r * 2 + 1] += intFac * (2.0 * Bi_x * DuDx * DetaDv + Bi_y * fac);
+            Ke[(c * 2 + 1) * nd + r * 2 + 1] += intFac * (2.0 * Bi_y * (eta * Bj_y + DvDy * DetaDv) + Bi_x * fac);
         }
     }
 }
@@ -817,9 +1078,16 @@ int uwr_assemble_range(const uwr_mesh* m, int64_t first, int64_t count, int64_t 
             int32_t mi = material ? material[p] : 0;
             if (mi < 0 || mi >= nmat) { bad |= 1; continue; }
             const uwr_material* mat = &mats[mi];
-            double eta = run_rheologies(mat, &rp);
+            double derivs[9];
+            double eta = run_rheologies(mat, &rp, derivs);
             if (eta_out) eta_out[s] = eta;
-            accumulate_Ke(dim, nen, eta, detJ * weight, GNx, K);
+            if (f->nl_form_jacobian && dim == 2) {
+                double L[3][3];
+                velocity_gradient(&rp, L);
+                accumulate_Ke_jacobian2d(eta, derivs, L, detJ * weight, GNx, K);
+            } else {
+                accumulate_Ke(dim, nen, eta, detJ * weight, GNx, K);
+            }
             /* PICellerator/Utils/src/BuoyancyForceTerm.c:374-450 */
             double T = f->temperature ? interp_temperature(&rp) : 0.0;
             double rho0 = point_rho ? point_rho[p] : mat->density;
@@ -1048,7 +1316,7 @@ int uwr_assemble_gauss(const uwr_mesh* m, int32_t nmat, const uwr_material* mats
             rp.GNx = GNx;
             rp.point_eta = 0.0;
             rp.p = -1;
-            double eta = run_rheologies(&mats[mi], &rp);
+            double eta = run_rheologies(&mats[mi], &rp, NULL);
             accumulate_Ke(dim, nen, eta, detJ * 1.0, GNx, K);
         }
     }

@@ -41,8 +41,11 @@ enum {
     UWR_LAW_VON_MISES = 10,           /* p0=cohesion p1=cohesionAfterSoftening p2=minimumViscosity
                                          p3=softeningStrain (<= 0: no strain weakening) p4=healingRate
                                          p5=strainRateSoftening (0/1)                        */
-    UWR_LAW_BYERLEE = 11              /* p0=cohesion p1=depthCoefficient p2=minimumViscosity
+    UWR_LAW_BYERLEE = 11,             /* p0=cohesion p1=depthCoefficient p2=minimumViscosity
                                          p3=softeningStrain p4=healingRate p5=strainRateSoftening */
+    UWR_LAW_MOHR_COULOMB = 12         /* p0=cohesion p1=cohesionAfterSoftening p2=frictionCoefficient
+                                         p3=frictionCoefficientAfterSoftening p4=minimumYieldStress
+                                         p5=minimumViscosity p6=softeningStrain p7=healingRate   */
 };
 
 typedef struct {
@@ -70,6 +73,8 @@ typedef struct {
     double gravity;              /* BuoyancyForceTerm gravity                        */
     const double* pfw;           /* StrainWeakening postFailureWeakening per point (NULL: 0) */
     double* pfw_incr;            /* out: its time derivative per point (NULL: not written)  */
+    int32_t nl_form_jacobian;    /* SystemLinearEquations nlFormJacobian: 2D Newton element matrices */
+    int32_t pad;
 } uwr_fields;
 
 /* Mesh geometry -------------------------------------------------------------------------- */

@@ -161,3 +161,20 @@ def test_oracle_bc_lift_matches_direct_solve(oracle, dim, nel, kind):
     assert np.array_equal(u.reshape(-1)[~free], bcval[~free])
     assert np.linalg.norm(u.reshape(-1) - ud) / np.linalg.norm(ud) < 1e-8
     assert np.linalg.norm(p - pd) / np.linalg.norm(pd) < 1e-8
+
+
+def test_oracle_newton_form_without_yield_equals_picard(oracle):
+    """With no yielding law the viscosity derivatives vanish and the 2D Newton element matrices
+    (ConstitutiveMatrixCartesian.c:360-383) equal the Picard ones."""
+    O = oracle
+    m = O.make_mesh(2, (6, 5, 1))
+    xyz = O.random_layout(m, 8, 5)
+    _, off, perm, xi, _ = O.map_points(m, xyz)
+    mats = [O.make_material([(O.LAW_MATERIAL_VISCOSITY, [1.3])], density=1.0)]
+    nn = O.num_nodes(m)
+    u = np.random.default_rng(2).standard_normal((nn, 2))
+    f0 = O.make_fields(velocity=u, previous_solution=True, gravity=1.0)
+    f1 = O.make_fields(velocity=u, previous_solution=True, gravity=1.0, jacobian=True)
+    K0, *_ = O.assemble(m, off, perm, xi, None, mats, f0)
+    K1, *_ = O.assemble(m, off, perm, xi, None, mats, f1)
+    assert np.abs(K1 - K0).max() < 1e-13 * np.abs(K0).max()
