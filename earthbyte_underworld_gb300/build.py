@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libuwgpu.so")
-SOURCES = ["capi.cu", "binning.cu", "assembly.cu", "operator.cu", "solver.cu", "gwg_stencil.cu", "unet.cu", "advect.cu", "noalloc.cu", "weights.cu", "tc_check.cu"]
+SOURCES = ["capi.cu", "binning.cu", "assembly.cu", "operator.cu", "solver.cu", "gwg_stencil.cu", "unet.cu", "advect.cu", "noalloc.cu", "weights.cu", "tc_check.cu", "population.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

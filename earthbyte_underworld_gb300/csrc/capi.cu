@@ -228,6 +228,28 @@ int uwgpu_particles_upload(uwgpu_ctx* ctx, int64_t n, const double* x, const dou
     });
 }
 
+int uwgpu_get_cell_tables(uwgpu_ctx* ctx, uint32_t* perm, uint32_t* offsets) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(c.mapped, UWGPU_ERR_STATE, "points not mapped");
+        if (perm && c.np > 0)
+            UWG_CUDA(cudaMemcpyAsync(perm, c.perm.p, (size_t)c.np * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream));
+        if (offsets)
+            UWG_CUDA(cudaMemcpyAsync(offsets, c.offsets.p, (size_t)(c.mesh.ne + 1) * sizeof(uint32_t),
+                                     cudaMemcpyDeviceToHost, c.stream));
+        UWG_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int uwgpu_population_control(uwgpu_ctx* ctx, const uwgpu_pcdvc_opts* opts, int64_t* count) {
+    return guarded(ctx, [&](Context& c) {
+        uwgpu_pcdvc_opts o;
+        if (opts) o = *opts;
+        else o = uwgpu_pcdvc_opts{25.0, 0.6, 2, 3, 0, 0};
+        const int64_t n = uwg::population_control(c, o);
+        if (count) *count = n;
+    });
+}
+
 int uwgpu_strain_weakening_set(uwgpu_ctx* ctx, const double* pfw) {
     return guarded(ctx, [&](Context& c) {
         UWG_REQUIRE(c.has_points && c.np > 0, UWGPU_ERR_STATE, "material points not uploaded");

@@ -304,6 +304,7 @@ inline unsigned blocks_for(int64_t n, int threads) {
 void bin_and_map(Context& c);
 void assemble(Context& c);
 void strain_weakening_advance(Context& c, double dt);
+int64_t population_control(Context& c, const uwgpu_pcdvc_opts& o);
 void build_operator(Context& c, int levels, bool need32);
 void apply_fine(Context& c, bool fp32, const double* x, double* y);  // device SoA vectors
 void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep);

@@ -77,6 +77,12 @@ class SolveOpts(C.Structure):
                 ("learned_stagnation", C.c_int32), ("mg_cycle", C.c_int32), ("bfbt_inner_pc", C.c_int32)]
 
 
+class PcdvcOpts(C.Structure):
+    _fields_ = [("upper_t", C.c_double), ("lower_t", C.c_double), ("max_deletions", C.c_int32),
+                ("max_splits", C.c_int32), ("split_in_interface_cells", C.c_int32),
+                ("delete_in_interface_cells", C.c_int32)]
+
+
 class Report(C.Structure):
     _fields_ = [("outer_its", C.c_int32), ("inner_its_total", C.c_int32), ("backsolve_its", C.c_int32),
                 ("vcycles", C.c_int32), ("converged", C.c_int32), ("status", C.c_int32),
@@ -152,6 +158,8 @@ def load(build_if_missing: bool = True):
         L.uwgpu_tc_check.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P, P]
         L.uwgpu_assembly_set.argtypes = [P, C.c_int32]
         L.uwgpu_jacobian_set.argtypes = [P, C.c_int32]
+        L.uwgpu_population_control.argtypes = [P, P, P]
+        L.uwgpu_get_cell_tables.argtypes = [P, P, P]
         L.uwgpu_strain_weakening_set.argtypes = [P, P]
         L.uwgpu_strain_weakening_advance.argtypes = [P, C.c_double]
         L.uwgpu_strain_weakening_get.argtypes = [P, P, P]
@@ -304,6 +312,23 @@ class Context:
         inc = np.zeros(self.npoints)
         self._check(self._L.uwgpu_strain_weakening_get(self._h, _ptr(pfw), _ptr(inc)))
         return pfw, inc
+
+    def population_control(self, upper_t=25.0, lower_t=0.6, max_deletions=2, max_splits=3,
+                           split_in_interface_cells=False, delete_in_interface_cells=False):
+        """PCDVC split / delete pass (DVC weights must be selected); returns the new point count."""
+        o = PcdvcOpts(upper_t, lower_t, max_deletions, max_splits, int(split_in_interface_cells),
+                      int(delete_in_interface_cells))
+        n = C.c_int64()
+        self._check(self._L.uwgpu_population_control(self._h, C.byref(o), C.byref(n)))
+        self.npoints = n.value
+        return n.value
+
+    def cell_tables(self):
+        """(perm, offsets) of the current cell tables, without re-binning."""
+        perm = np.zeros(self.npoints, np.uint32)
+        offsets = np.zeros(self.nelements + 1, np.uint32)
+        self._check(self._L.uwgpu_get_cell_tables(self._h, _ptr(perm), _ptr(offsets)))
+        return perm, offsets
 
     def jacobian_set(self, on=True):
         """Newton (Jacobian) form of the 2D element matrices for the next assemblies."""

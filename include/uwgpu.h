@@ -250,6 +250,29 @@ int uwgpu_particles_download(uwgpu_ctx* ctx, double* x, double* y, double* z);
  * discrete Voronoi region and weighs that region's volume.  res is ignored for CONSTANT. */
 enum { UWGPU_WEIGHTS_CONSTANT = 0, UWGPU_WEIGHTS_DVC = 1 };
 int uwgpu_weights_set(uwgpu_ctx* ctx, int32_t kind, const int32_t res[3]);
+/* PCDVC population control (PICellerator/Utils/src/PCDVC.c:638-1060, non-inflow branch; defaults of
+ * PCDVC.c:260-268 in brackets): with DVC weights selected and the points mapped, every element in
+ * index order splits its points whose Voronoi region exceeds upper_t percent of the element's local
+ * volume [25] (at most max_splits [3], at the region's centroid) and deletes those below lower_t
+ * percent [0.6] (at most max_deletions [2], largest swarm index first, the swarm's last point moving
+ * into the hole), with no deletions in interface cells (mixed materials) unless
+ * delete_in_interface_cells [0] and no splits there unless split_in_interface_cells [0] or the
+ * element touches the mesh boundary.  The points (coordinates, material, per-point viscosity,
+ * density and strain-weakening history) and the cell tables are replaced on the device in the
+ * reference's order; *count (optional) receives the new number of points.  The next assembly's
+ * DVC weights follow the new cell order (the reference's second DVC pass). */
+typedef struct {
+    double upper_t, lower_t;
+    int32_t max_deletions, max_splits;
+    int32_t split_in_interface_cells, delete_in_interface_cells;
+} uwgpu_pcdvc_opts;
+int uwgpu_population_control(uwgpu_ctx* ctx, const uwgpu_pcdvc_opts* opts, int64_t* count);
+
+/* The current cell tables (the integration swarm's cellParticleTbl, in slot order): perm (point
+ * of every slot) and offsets (nel + 1), without re-binning (after uwgpu_population_control they
+ * hold the reference's edited order).  Either may be NULL. */
+int uwgpu_get_cell_tables(uwgpu_ctx* ctx, uint32_t* perm, uint32_t* offsets);
+
 /* Local coordinates ([slot][3], z = 0 in 2D) and weights (slot order) of the integration points
  * the last assembly used: IntegrationPoint.xi and .weight (StgDomain/Swarm/src/
  * IntegrationPoint.h:47, StandardParticle.h:70) for CPU readers of the integration swarm.

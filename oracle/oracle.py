@@ -64,6 +64,11 @@ class SolveOpts(C.Structure):
                 ("nthreads", C.c_int32), ("bfbt_rtol", C.c_double), ("bfbt_max_it", C.c_int32), ("pad", C.c_int32)]
 
 
+class PcdvcParams(C.Structure):
+    _fields_ = [("upperT", C.c_double), ("lowerT", C.c_double), ("maxDeletions", C.c_int32), ("maxSplits", C.c_int32),
+                ("splitInInterfaceCells", C.c_int32), ("deleteInInterfaceCells", C.c_int32)]
+
+
 class Report(C.Structure):
     _fields_ = [("outer_its", C.c_int32), ("inner_its_total", C.c_int32), ("backsolve_its", C.c_int32),
                 ("converged", C.c_int32), ("rel_residual", C.c_double), ("t_setup", C.c_double),
@@ -96,6 +101,8 @@ def lib():
             L.uwr_dvc_element.argtypes = [C.c_int, P, C.c_int32, P, P, P]
             L.uwr_dvc_weights.argtypes = [P, P, P, P, P, P, C.c_int32]
             L.uwr_dvc_grid.argtypes = [C.c_int, P, P, P]
+            L.uwr_pcdvc.restype = C.c_int64
+            L.uwr_pcdvc.argtypes = [P, P, P, C.c_int64, C.c_int64, P, P, P, P, P, P, P, P, P, P]
             L.uwr_assemble_gauss.argtypes = [P, C.c_int32, P, P, P, P]
             L.uwr_eqnum.restype = C.c_int64
             L.uwr_eqnum.argtypes = [P, P, P]
@@ -285,6 +292,33 @@ def dvc_weights(m, res, offsets, xi, nthreads=0):
     lib().uwr_dvc_weights(C.byref(m), _p(r), _p(np.ascontiguousarray(offsets, dtype=np.uint32)), _p(xi), _p(cxi),
                           _p(w), nthreads)
     return cxi, w
+
+
+def pcdvc(m, res, xyz, material, offsets, perm, xi, upperT=25.0, lowerT=0.6, max_deletions=2, max_splits=3,
+          split_in_interface=False, delete_in_interface=False):
+    """One PCDVC population-control pass (non-inflow) over the cell tables of a CoincidentMapper pass
+    (offsets, perm; xi [slot][3]).  Returns (xyz (n', 3), material, src (input point of every output
+    point), offsets', perm', integration xi [slot][3], weights [slot])."""
+    n = xyz.shape[0]
+    E = num_elements(m)
+    cap = n + max_splits * E
+    X = np.zeros((cap, 3))
+    X[:n] = xyz
+    M = np.zeros(cap, np.int32)
+    M[:n] = material
+    S = np.zeros(cap, np.int64)
+    off = np.zeros(E + 1, np.uint32)
+    pr = np.zeros(cap, np.uint32)
+    xo = np.zeros((cap, 3))
+    wo = np.zeros(cap)
+    pp = PcdvcParams(upperT, lowerT, max_deletions, max_splits, int(split_in_interface), int(delete_in_interface))
+    r = np.ascontiguousarray(list(res) + [1] * (3 - len(res)), dtype=np.int32)
+    cnt = lib().uwr_pcdvc(C.byref(m), _p(r), C.byref(pp), n, cap, _p(X), _p(M), _p(S),
+                          _p(np.ascontiguousarray(offsets, dtype=np.uint32)), _p(np.ascontiguousarray(perm, dtype=np.uint32)),
+                          _p(np.ascontiguousarray(xi, dtype=np.float64)), _p(off), _p(pr), _p(xo), _p(wo))
+    if cnt < 0:
+        raise RuntimeError(f"oracle PCDVC failed ({cnt})")
+    return X[:cnt], M[:cnt], S[:cnt], off, pr[:cnt], xo[:cnt], wo[:cnt]
 
 
 def assemble_gauss(m, mats, el_material, fields):

@@ -1286,6 +1286,210 @@ void uwr_dvc_weights(const uwr_mesh* m, const int32_t res[3], const uint32_t* of
     }
 }
 
+/* ---- PCDVC population control (PICellerator/Utils/src/PCDVC.c) ----------------------------
+ * The non-inflow branch of _PCDVC_Calculate3D (:638-1060) and _PCDVC_Calculate2D (:1063-...),
+ * element after element in index order, on the swarm as the cell tables leave it after a
+ * CoincidentMapper pass (slot order = cell-table order):
+ *   DVC weights of the element's points in cell order; interface cell = its points' materials
+ *   differ; boundary cell = the element touches the mesh boundary; maxW / minW = upperT / lowerT
+ *   percent of the element's local volume 2^dim; splits: points with w > maxW in cell order,
+ *   deletions: points with w < minW sorted by swarm index, largest first (compare_indexOnCPU :621);
+ *   interface cells delete nothing unless deleteInInterfaceCells and split nothing unless
+ *   splitInInterfaceCells or a boundary cell; maxDeletions > count - 4 becomes count / 2.
+ *   A split appends a copy of the point to the swarm and to the cell, at the centroid of the
+ *   point's Voronoi region (splitIntParticleByIndexWithinCell :556-619).  A deletion removes the
+ *   point from its cell by moving the cell's last entry into its place (Swarm_RemoveParticleFromCell,
+ *   StgDomain/Swarm/src/SwarmClass.c:1055-1071) and fills its swarm slot with the swarm's last point,
+ *   whose own cell entry is renumbered (deleteIntParticleByIndexOnCPU :451-555).  After any change
+ *   the element's DVC is recomputed in its new cell order.  Every integration point ends at the
+ *   centroid of its region with the region's volume as weight (:1040-1048).
+ * The inflow branch (libc rand()) is not restated.
+ * Arrays of capacity `cap` points; returns the new point count, or -1 (cap too small / an empty
+ * element), -2 (DVC resolution out of range). */
+typedef struct {
+    uint32_t* v;
+    int64_t n, cap;
+} u32vec;
+static void u32vec_push(u32vec* a, uint32_t x) {
+    if (a->n == a->cap) {
+        a->cap = a->cap ? 2 * a->cap : 8;
+        a->v = (uint32_t*)realloc(a->v, sizeof(uint32_t) * (size_t)a->cap);
+    }
+    a->v[a->n++] = x;
+}
+static int64_t u32vec_find(const u32vec* a, uint32_t x) {
+    for (int64_t i = 0; i < a->n; ++i)
+        if (a->v[i] == x) return i;
+    return -1;
+}
+typedef struct {
+    int64_t pos;
+    uint32_t index;
+} pc_del;
+static int pc_del_cmp(const void* A, const void* B) {   /* descending swarm index */
+    const pc_del* a = (const pc_del*)A;
+    const pc_del* b = (const pc_del*)B;
+    return a->index < b->index ? 1 : (a->index > b->index ? -1 : 0);
+}
+
+int64_t uwr_pcdvc(const uwr_mesh* m, const int32_t res[3], const uwr_pcdvc_params* pp, int64_t n, int64_t cap,
+                  double* xyz, int32_t* material, int64_t* src, const uint32_t* offsets, const uint32_t* perm,
+                  const double* xi_slot, uint32_t* offsets_out, uint32_t* perm_out, double* xi_out, double* w_out) {
+    const int dim = m->dim;
+    const int64_t E = uwr_num_elements(m);
+    const double vol = dim == 3 ? 8.0 : 4.0;
+    const double maxW = pp->upperT * vol / 100.0, minW = pp->lowerT * vol / 100.0;
+    if (cap < n) return -1;
+    /* per swarm index: integration xi, owning cell */
+    double* pxi = (double*)malloc(sizeof(double) * 3 * (size_t)cap);
+    int64_t* cell = (int64_t*)malloc(sizeof(int64_t) * (size_t)cap);
+    u32vec* tab = (u32vec*)calloc((size_t)E, sizeof(u32vec));
+    for (int64_t e = 0; e < E; ++e)
+        for (uint32_t s = offsets[e]; s < offsets[e + 1]; ++s) {
+            uint32_t p = perm[s];
+            u32vec_push(&tab[e], p);
+            cell[p] = e;
+            for (int d = 0; d < 3; ++d) pxi[3 * (int64_t)p + d] = xi_slot[3 * (int64_t)s + d];
+        }
+    for (int64_t p = 0; p < n; ++p) src[p] = p;
+    int64_t count = n;
+    int rc = 0;
+    double* a = NULL;
+    double* cx = NULL;
+    double* w = NULL;
+    int64_t abuf = 0;
+    for (int64_t e = 0; e < E && rc == 0; ++e) {
+        int64_t nump = tab[e].n;
+        if (nump == 0) { rc = -1; break; }
+        if (nump + pp->maxSplits > abuf) {
+            abuf = 2 * (nump + pp->maxSplits);
+            a = (double*)realloc(a, sizeof(double) * 3 * (size_t)abuf);
+            cx = (double*)realloc(cx, sizeof(double) * 3 * (size_t)abuf);
+            w = (double*)realloc(w, sizeof(double) * (size_t)abuf);
+        }
+        for (int64_t i = 0; i < nump; ++i)
+            for (int d = 0; d < dim; ++d) a[i * dim + d] = pxi[3 * (int64_t)tab[e].v[i] + d];
+        if (uwr_dvc_element(dim, res, (int32_t)nump, a, cx, w) < 0) { rc = -2; break; }
+        /* interface and boundary cells */
+        int interface = 0;
+        for (int64_t i = 1; i < nump; ++i)
+            if (material[tab[e].v[i]] != material[tab[e].v[0]]) { interface = 1; break; }
+        int64_t ei[3] = {e % m->nel[0], (e / m->nel[0]) % m->nel[1], dim == 3 ? e / ((int64_t)m->nel[0] * m->nel[1]) : 0};
+        int boundary = 0;
+        for (int d = 0; d < dim; ++d)
+            if (ei[d] == 0 || ei[d] == m->nel[d] - 1) boundary = 1;
+        int maxDel = pp->maxDeletions, maxSpl = pp->maxSplits;
+        if (interface) {
+            if (!pp->deleteInInterfaceCells) maxDel = 0;
+            if (!pp->splitInInterfaceCells && !boundary) maxSpl = 0;
+        }
+        int64_t* splits = (int64_t*)malloc(sizeof(int64_t) * (size_t)nump);
+        pc_del* dels = (pc_del*)malloc(sizeof(pc_del) * (size_t)nump);
+        int64_t ns = 0, nd = 0;
+        for (int64_t i = 0; i < nump; ++i) {
+            if (w[i] > maxW) splits[ns++] = i;
+            if (w[i] < minW) { dels[nd].pos = i; dels[nd].index = tab[e].v[i]; nd++; }
+        }
+        qsort(dels, (size_t)nd, sizeof(pc_del), pc_del_cmp);
+        if (maxDel > nump - 4) maxDel = (int)(nump / 2);
+        int changed = 0;
+        int64_t cnt = maxSpl > ns ? ns : maxSpl;
+        for (int64_t i = 0; i < cnt; ++i) {
+            if (count >= cap) { rc = -1; break; }
+            int64_t at = splits[i];
+            uint32_t from = tab[e].v[at];
+            int64_t k = count++;
+            for (int d = 0; d < 3; ++d) xyz[3 * k + d] = xyz[3 * (int64_t)from + d];
+            material[k] = material[from];
+            src[k] = src[from];
+            double cxi[3] = {cx[at * dim + 0], cx[at * dim + 1], dim == 3 ? cx[at * dim + 2] : 0.0};
+            for (int d = 0; d < 3; ++d) pxi[3 * k + d] = cxi[d];
+            /* FeMesh_CoordLocalToGlobal of the centroid */
+            double nodes[8][3], N[8];
+            element_node_xyz(m, e, nodes);
+            uwr_shape(dim, cxi, N);
+            for (int d = 0; d < 3; ++d) {
+                double v = 0.0;
+                for (int q = 0; q < (dim == 3 ? 8 : 4); ++q) v += N[q] * nodes[q][d];
+                xyz[3 * k + d] = v;
+            }
+            cell[k] = e;
+            u32vec_push(&tab[e], (uint32_t)k);
+            changed = 1;
+        }
+        int64_t cntd = maxDel > nd ? nd : maxDel;
+        for (int64_t i = 0; i < cntd && rc == 0; ++i) {
+            uint32_t P = dels[i].index;
+            u32vec* t = &tab[cell[P]];
+            int64_t pos = u32vec_find(t, P);
+            t->v[pos] = t->v[t->n - 1];
+            t->n--;
+            int64_t L = count - 1;
+            if ((int64_t)P != L) {
+                for (int d = 0; d < 3; ++d) {
+                    xyz[3 * (int64_t)P + d] = xyz[3 * L + d];
+                    pxi[3 * (int64_t)P + d] = pxi[3 * L + d];
+                }
+                material[P] = material[L];
+                src[P] = src[L];
+                int64_t f = cell[L];
+                cell[P] = f;
+                u32vec* tf = &tab[f];
+                tf->v[u32vec_find(tf, (uint32_t)L)] = P;
+            }
+            count--;
+            changed = 1;
+        }
+        free(splits);
+        free(dels);
+        if (rc) break;
+        nump = tab[e].n;
+        if (changed) {
+            if (nump > abuf) {
+                abuf = 2 * nump;
+                a = (double*)realloc(a, sizeof(double) * 3 * (size_t)abuf);
+                cx = (double*)realloc(cx, sizeof(double) * 3 * (size_t)abuf);
+                w = (double*)realloc(w, sizeof(double) * (size_t)abuf);
+            }
+            for (int64_t i = 0; i < nump; ++i)
+                for (int d = 0; d < dim; ++d) a[i * dim + d] = pxi[3 * (int64_t)tab[e].v[i] + d];
+            if (uwr_dvc_element(dim, res, (int32_t)nump, a, cx, w) < 0) { rc = -2; break; }
+        }
+        /* the element's integration points move to their centroids */
+        for (int64_t i = 0; i < nump; ++i) {
+            int64_t p = tab[e].v[i];
+            for (int d = 0; d < dim; ++d) pxi[3 * p + d] = cx[i * dim + d];
+        }
+        /* weights per point, reordered by slot when the tables are written out */
+        for (int64_t i = 0; i < nump; ++i) w_out[tab[e].v[i]] = w[i];
+    }
+    if (rc == 0) {
+        int64_t sidx = 0;
+        for (int64_t e = 0; e < E; ++e) {
+            offsets_out[e] = (uint32_t)sidx;
+            for (int64_t i = 0; i < tab[e].n; ++i, ++sidx) perm_out[sidx] = tab[e].v[i];
+        }
+        offsets_out[E] = (uint32_t)sidx;
+        /* per slot: integration xi and weight (w_out was filled per point index; reorder) */
+        double* wtmp = (double*)malloc(sizeof(double) * (size_t)(count > 0 ? count : 1));
+        memcpy(wtmp, w_out, sizeof(double) * (size_t)count);
+        for (int64_t s = 0; s < sidx; ++s) {
+            int64_t p = perm_out[s];
+            for (int d = 0; d < 3; ++d) xi_out[3 * s + d] = d < dim ? pxi[3 * p + d] : 0.0;
+            w_out[s] = wtmp[p];
+        }
+        free(wtmp);
+    }
+    for (int64_t e = 0; e < E; ++e) free(tab[e].v);
+    free(tab);
+    free(pxi);
+    free(cell);
+    free(a);
+    free(cx);
+    free(w);
+    return rc ? rc : count;
+}
+
 int uwr_assemble_gauss(const uwr_mesh* m, int32_t nmat, const uwr_material* mats,
                        const int32_t* el_material, const uwr_fields* f, double* Ke) {
     int dim = m->dim, nen = (dim == 3) ? 8 : 4, nd = nen * dim;

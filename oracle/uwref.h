@@ -170,6 +170,21 @@ typedef struct {
     double t_setup, t_solve;
 } uwr_report;
 
+/* PCDVC population control parameters (PICellerator/Utils/src/PCDVC.c:247-284 defaults:
+ * upperT 25, lowerT 0.6, maxDeletions 2, maxSplits 3, interface switches False). */
+typedef struct {
+    double upperT, lowerT;   /* percent of the element's local volume */
+    int32_t maxDeletions, maxSplits;
+    int32_t splitInInterfaceCells, deleteInInterfaceCells;
+} uwr_pcdvc_params;
+/* One PCDVC pass (non-inflow branch) over every element; see uwref.c.  xyz (cap*3), material (cap),
+ * src (cap: the input point each output point copies) are updated in place; offsets_out (E+1),
+ * perm_out, xi_out (3 per slot), w_out (per slot; cap entries of scratch) receive the new cell
+ * tables and integration points.  Returns the new point count or a negative error. */
+int64_t uwr_pcdvc(const uwr_mesh* m, const int32_t res[3], const uwr_pcdvc_params* pp, int64_t n, int64_t cap,
+                  double* xyz, int32_t* material, int64_t* src, const uint32_t* offsets, const uint32_t* perm,
+                  const double* xi_slot, uint32_t* offsets_out, uint32_t* perm_out, double* xi_out, double* w_out);
+
 int uwr_solve_bsscr(const uwr_mesh* m, const uint8_t* fixed, const double* Ke, const double* Ge,
                     const double* fe, const double* Se, const uwr_solve_opts* o,
                     double* u_nodal /* nnode*dim */, double* p /* E */, uwr_report* rep);
