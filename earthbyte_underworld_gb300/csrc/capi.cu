@@ -150,7 +150,7 @@ int uwgpu_materials_set(uwgpu_ctx* ctx, int32_t n, const uwgpu_material* mats) {
                         "material needs 1..4 rheology laws");
             for (int l = 0; l < mats[i].n_laws; ++l) {
                 int law = mats[i].laws[l].law;
-                UWG_REQUIRE(law >= UWGPU_LAW_MATERIAL_VISCOSITY && law <= UWGPU_LAW_NON_NEWTONIAN,
+                UWG_REQUIRE(law >= UWGPU_LAW_MATERIAL_VISCOSITY && law <= UWGPU_LAW_MOHR_COULOMB,
                             UWGPU_ERR_UNSUPPORTED,
                             "rheology law " + std::to_string(law) + " is not provided by this library");
                 if (law == UWGPU_LAW_DEPTH_DEPENDENT) {

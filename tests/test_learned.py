@@ -60,7 +60,9 @@ def test_unet_forward_backward_match_reference(uw, nel, levels, base):
     (a) quantized weights and data: the FP32 sums are exact, so agreement is to ~1e-6 and every
     layer's block of the gradient is checked; (b) random FP32 data: BF16 roundings of activations
     may flip with the summation order, so the tolerance is looser, and the GPU must still sit
-    much closer to the BF16-emulating reference than the plain FP32 network does."""
+    much closer to the BF16-emulating reference than the plain FP32 network does.  The convolutions
+    run on the tensor core (tcgen05 implicit GEMM, BF16 operands, FP32 accumulation; FP32 gradients
+    enter as hi + lo BF16 parts)."""
     from oracle import unet_ref as R
     U = uw
     nodes = tuple(n + 1 for n in nel)
@@ -91,7 +93,9 @@ def test_unet_forward_backward_match_reference(uw, nel, levels, base):
     _, out, gp, gi = _gpu_pass(U, nel, levels, base, params, inp, gout)
     rout, rgp, rgi = R.value_and_grads(params, inp, gout, nodes, levels, base, emulate_bf16=True)
     fout, fgp, _ = R.value_and_grads(params, inp, gout, nodes, levels, base, emulate_bf16=False)
-    assert _rel(out, rout) < 1.5e-2 and _rel(gp, rgp) < 3e-2 and _rel(gi, rgi) < 3e-2
+    # BF16 roundings of activations flip with the tensor core's summation order; on these random
+    # inputs the gradients then differ by a few percent from the emulating reference
+    assert _rel(out, rout) < 1.5e-2 and _rel(gp, rgp) < 6e-2 and _rel(gi, rgi) < 6e-2
     assert _rel(out, rout) < 0.5 * _rel(fout, rout)
 
 
