@@ -239,6 +239,9 @@ FAMILY_NOTES = {
                 "of L2); the roofline line is the direction kernel",
     "learned": "U-Net corrections: tcgen05 implicit-GEMM convolutions (BF16, FP32 accumulate) and the head",
     "assembly": "rheology + moments per point, contraction of the moments into K_e (tensor core in the mixed forms)",
+    "setup": "every launch of the solver's setup: node stencils from K_e, the Galerkin hierarchy and coarsest "
+             "inverse, FP32 copies, Chebyshev bounds (power iterations), the right-hand side and the BFBt "
+             "operator (weights, G^T W G stencil)",
 }
 
 
@@ -391,7 +394,8 @@ def run_ours(args):
             for name, fam in (("assembly", U.KERNEL_ASSEMBLY), ("apply", U.KERNEL_APPLY),
                               ("smooth", U.KERNEL_SMOOTH), ("binning", U.KERNEL_BINNING),
                               ("schur_pc", U.KERNEL_SCHUR_PC), ("vector", U.KERNEL_VECTOR),
-                              ("transfer", U.KERNEL_TRANSFER), ("learned", U.KERNEL_LEARNED)):
+                              ("transfer", U.KERNEL_TRANSFER), ("learned", U.KERNEL_LEARNED),
+                              ("setup", U.KERNEL_SETUP)):
                 n, t = ctx.profile_read(fam)
                 b, f = ctx.profile_work(fam)
                 prof[name] = {"launches": n, "ms": t, "bytes": b, "flops": f}

@@ -605,6 +605,9 @@ __global__ void __launch_bounds__(kTmThreads) k_cg_mf3_dir_tma(Mf3 a, const __gr
     if (tid == 0) {
         for (int i = 0; i < 3; ++i) tc::mbar_init(&bar[i], 1);
     }
+    // no thread may poll a barrier before it is initialised (the shared memory may still hold an
+    // earlier block's state)
+    __syncthreads();
     const uint32_t ring_s = tc::smem_u32(ring);
     auto issue = [&](int t) {   // stage t = element plane zlo - 1 + t and node plane zlo - 1 + t
         const int slot = t % 3, plane = zlo - 1 + t;
@@ -622,7 +625,7 @@ __global__ void __launch_bounds__(kTmThreads) k_cg_mf3_dir_tma(Mf3 a, const __gr
     const bool eok = tid < kMfX * kMfY && x0 + tx < ex && y0 + ty < ey;
     const int eo = eok ? (x0 + tx) + ex * (y0 + ty) : 0;
     auto load_pq = [&](int plane, float& pv, float& qv) {
-        const bool ok = !first && eok && plane < zhi;
+        const bool ok = !first && eok && plane >= 0 && plane < zhi;
         pv = ok ? p[plane * exy + eo] : 0.f;
         qv = ok ? q[plane * exy + eo] : 0.f;
     };
@@ -635,7 +638,7 @@ __global__ void __launch_bounds__(kTmThreads) k_cg_mf3_dir_tma(Mf3 a, const __gr
     const int wb_node = ny * kTwX + nx;
     const int zb_elem = (ty + 1) * kTzX + tx + 4;  // this thread's element in the staged halo plane
     const int ybase = ty * (kMfX + 1) + tx;
-    bool ok = true;
+    bool ok = true, bad = false;
     uint32_t phase_bits = 0;   // parity of the next wait, per slot
     auto wait_slot = [&](int slot) {
         ok = tc::mbar_wait(&bar[slot], (phase_bits >> slot) & 1u, 1u << 22) && ok;
@@ -688,8 +691,12 @@ __global__ void __launch_bounds__(kTmThreads) k_cg_mf3_dir_tma(Mf3 a, const __gr
                 const float ze = zp[zb_elem];
                 const float pe = first ? ze : fmaf(beta, pc, ze);
                 const float qe = first ? out : fmaf(beta, qc, out);
-                p[e] = pe;
-                q[e] = qe;
+                if (e < exy * ez) {
+                    p[e] = pe;
+                    q[e] = qe;
+                } else {
+                    bad = true;
+                }
                 local = fmaf(pe, qe, local);
             }
 #pragma unroll
@@ -698,6 +705,7 @@ __global__ void __launch_bounds__(kTmThreads) k_cg_mf3_dir_tma(Mf3 a, const __gr
                 for (int d = 0; d < 3; ++d) lo[d][c4] = hi[d][c4];
         }
     }
+    if (bad) local = __int_as_float(0x7fc00000);
     if (!ok) {
         // let copies still in flight land before the block's shared memory is released
         if (tid == 0)

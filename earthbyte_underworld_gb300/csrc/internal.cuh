@@ -198,6 +198,8 @@ struct Context {
 
     bool profiling = false;
     ProfileFamily prof[UWGPU_KERNEL_COUNT];
+    // while >= 0, every launch is counted in this family (the solver's setup phase)
+    int family_override = -1;
 
     // multigrid hierarchy of the BFBt operator G^T W G (gwg_stencil.cu): element grids coarsened
     // 2:1 by aggregation; level 0's stencil belongs to the solve, the others live here, as do the
@@ -236,7 +238,7 @@ struct LaunchScope {
     Context& c;
     int family;
     cudaEvent_t e1 = nullptr;
-    LaunchScope(Context& ctx, int fam) : c(ctx), family(fam) {
+    LaunchScope(Context& ctx, int fam) : c(ctx), family(ctx.family_override >= 0 ? ctx.family_override : fam) {
         c.launches++;
         if (c.profiling && family >= 0) {
             ProfileFamily& f = c.prof[family];
@@ -257,8 +259,17 @@ struct LaunchScope {
     }
 };
 
+// Counts every launch of its lifetime in one family (the solver's setup phase).
+struct FamilyOverride {
+    Context& c;
+    int saved;
+    FamilyOverride(Context& ctx, int fam) : c(ctx), saved(ctx.family_override) { c.family_override = fam; }
+    ~FamilyOverride() { c.family_override = saved; }
+};
+
 // Records the algorithmic work of one launch of `family` while profiling.
 inline void note_work(Context& c, int family, double bytes, double flops) {
+    if (c.family_override >= 0) family = c.family_override;
     if (c.profiling && family >= 0) {
         c.prof[family].bytes += bytes;
         c.prof[family].flops += flops;

@@ -912,6 +912,7 @@ void Bsscr::project_nullspace(double* x) {
 
 void Bsscr::run() {
     auto t0 = std::chrono::steady_clock::now();
+    FamilyOverride setup_family(c, UWGPU_KERNEL_SETUP);
     setup_velocity();
     if (o.learned_pc) {
         UWG_REQUIRE(c.net != nullptr, UWGPU_ERR_STATE, "learned_pc requested but no network (uwgpu_learned_create)");
@@ -1013,6 +1014,7 @@ void Bsscr::run() {
     UWG_CUDA(cudaStreamSynchronize(c.stream));
     auto t1 = std::chrono::steady_clock::now();
     rep.t_setup_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    c.family_override = setup_family.saved;
 
     // h_hat = h - G^T K^{-1} f
     a11(f.p, tu2.p, o.a11_rtol);

@@ -46,7 +46,7 @@ ASSEMBLY_FP64 = 0
 ASSEMBLY_TENSOR = 1
 
 KERNEL_ASSEMBLY, KERNEL_APPLY, KERNEL_SMOOTH, KERNEL_BINNING, KERNEL_SCHUR_PC, KERNEL_VECTOR, KERNEL_TRANSFER, \
-    KERNEL_LEARNED = range(8)
+    KERNEL_LEARNED, KERNEL_SETUP = range(9)
 
 WEIGHTS_CONSTANT = 0
 WEIGHTS_DVC = 1

@@ -302,9 +302,11 @@ int uwgpu_assembly_set(uwgpu_ctx* ctx, int32_t mode);
  * assemblies add the viscosity's derivatives with respect to the velocity gradient that yielding
  * laws (VON_MISES, DRUCKER_PRAGER) provide to the viscous term, as the 2D branch of
  * ConstitutiveMatrixCartesian.c:360-383 does, around the context's current solution.  The
- * resulting K_e is not symmetric: uwgpu_get_element_matrices returns all nd x nd entries (row =
- * test function dof), and uwgpu_solve_bsscr refuses it with UWGPU_ERR_UNSUPPORTED (the solver
- * here takes the Picard form).  3D: UWGPU_ERR_UNSUPPORTED (the reference has no 3D branch). */
+ * general form is not symmetric (for these two laws the added term is a symmetric rank-one update
+ * along the stress, which can make K_e indefinite): uwgpu_get_element_matrices returns all
+ * nd x nd entries (row = test function dof), and uwgpu_solve_bsscr refuses it with
+ * UWGPU_ERR_UNSUPPORTED (the solver here takes the Picard form).  3D: UWGPU_ERR_UNSUPPORTED (the
+ * reference has no 3D branch). */
 int uwgpu_jacobian_set(uwgpu_ctx* ctx, int32_t on);
 
 /* Per-element results of the last assembly, copied to the host: the per-element callback
@@ -357,7 +359,9 @@ enum { UWGPU_KERNEL_ASSEMBLY = 0, UWGPU_KERNEL_APPLY = 1, UWGPU_KERNEL_SMOOTH = 
        UWGPU_KERNEL_BINNING = 3, UWGPU_KERNEL_SCHUR_PC = 4 /* scaled-BFBt inner solves */,
        UWGPU_KERNEL_VECTOR = 5 /* Krylov vector work, reductions, G and G^T */,
        UWGPU_KERNEL_TRANSFER = 6 /* restriction, prolongation, coarsest solve */,
-       UWGPU_KERNEL_LEARNED = 7 /* U-Net preconditioner: forward, backward, Adam */, UWGPU_KERNEL_COUNT = 8 };
+       UWGPU_KERNEL_LEARNED = 7 /* U-Net preconditioner: forward, backward, Adam */,
+       UWGPU_KERNEL_SETUP = 8 /* solver setup: stencils, multigrid hierarchy, Chebyshev bounds, BFBt operator */,
+       UWGPU_KERNEL_COUNT = 9 };
 /* (Measurement hooks, no reference counterpart.) */
 int uwgpu_profile_enable(uwgpu_ctx* ctx, int32_t on);
 int uwgpu_profile_read(uwgpu_ctx* ctx, int32_t which, int64_t* launches, double* ms);

@@ -1430,6 +1430,9 @@ int64_t uwr_pcdvc(const uwr_mesh* m, const int32_t res[3], const uwr_pcdvc_param
                     xyz[3 * (int64_t)P + d] = xyz[3 * L + d];
                     pxi[3 * (int64_t)P + d] = pxi[3 * L + d];
                 }
+                /* the moved point keeps the weight its element gave it (when that element was
+                   already processed; otherwise the element writes it later under index P) */
+                w_out[P] = w_out[L];
                 material[P] = material[L];
                 src[P] = src[L];
                 int64_t f = cell[L];

@@ -50,3 +50,46 @@ def test_dvc_partition_invariants(oracle, dim, res):
         held = w > 0
         assert np.all(np.abs(cxi[held]) <= 1.0)
         assert np.all(cxi[~held] == 0.0)
+
+
+def _clustered_swarm(dim, nel, seed):
+    """3..14 points per element, half of them crowded towards one corner; 20 % material 1."""
+    rng = np.random.default_rng(seed)
+    E = int(np.prod(nel))
+    pts, mat = [], []
+    for e in range(E):
+        idx = [e % nel[0], (e // nel[0]) % nel[1]] + ([e // (nel[0] * nel[1])] if dim == 3 else [])
+        for _ in range(int(rng.integers(3, 15))):
+            loc = rng.uniform(0, 1, dim) ** 2.5 if rng.uniform() < 0.5 else rng.uniform(0, 1, dim)
+            pts.append([(idx[d] + loc[d]) / nel[d] for d in range(dim)] + [0.0] * (3 - dim))
+            mat.append(int(rng.uniform() < 0.2))
+    order = rng.permutation(len(pts))
+    return np.array(pts)[order], np.array(mat, np.int32)[order]
+
+
+@pytest.mark.parametrize("dim,nel,res", [(2, (6, 5), (10, 10)), (3, (6, 5, 4), (10, 10, 10)),
+                                         (3, (5, 4, 4), (8, 8, 8))])
+def test_pcdvc_weights_follow_the_moved_points(oracle, dim, nel, res):
+    """After a population-control pass the weight of every slot is the discrete Voronoi weight of
+    its point within its element's final point set: a DVC pass over the final swarm (points mapped
+    back to local coordinates) gives the same weights and centroids.  Deleting a point moves the
+    swarm's last point into the hole; its weight moves with it (deleteIntParticleByIndexOnCPU,
+    PICellerator/Utils/src/PCDVC.c:451-555)."""
+    O = oracle
+    pts, mat = _clustered_swarm(dim, nel, 1)
+    m = O.make_mesh(dim, nel)
+    _, off0, perm0, xi0, _ = O.map_points(m, pts)
+    X, M, S, off2, perm2, xo, wo = O.pcdvc(m, res, pts, mat, off0, perm0, xi0, max_deletions=4, max_splits=5)
+    assert len(X) != len(pts)
+    _, off3, perm3, xi3, out = O.map_points(m, X)
+    assert out == 0
+    # the same points per element (the pass keeps its own order within an element)
+    for e in range(int(np.prod(nel))):
+        assert sorted(perm2[off2[e]:off2[e + 1]]) == sorted(perm3[off3[e]:off3[e + 1]])
+    # local coordinates of the final swarm in the pass's slot order
+    slot_of = np.empty(len(X), np.int64)
+    slot_of[perm3] = np.arange(len(X))
+    xi_final = xi3[slot_of[perm2]]
+    cx, w = O.dvc_weights(m, res, off2, xi_final)
+    assert np.allclose(w, wo, rtol=0, atol=1e-14)
+    assert np.allclose(cx[:, :dim], xo[:, :dim], rtol=0, atol=1e-14)
