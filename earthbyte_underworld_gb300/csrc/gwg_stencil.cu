@@ -547,22 +547,23 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* 
     pdl_trigger();
 }
 
-// The same direction update with the element and weight planes staged by the tensor memory
-// accelerator (cp.async.bulk.tensor), for element grids whose x extent is a multiple of 4 (so
-// that every z row starts on 16 bytes).  Per z step one thread issues two copies into a ring of
-// three stages: the element plane of the column with its halo, as a 40 x 10 box from x0 - 4
-// (x aligned down to 16 bytes; coordinates outside the grid, the halo at the mesh boundary and
-// the planes below and above the mesh, read as zero), and the 36 x 9 x 3 box of the node plane's
-// three weight components.  The copies complete on the stage's mbarrier.  Ten warps: one thread
-// per node of the 33 x 9 node plane, then one per element of the 32 x 8 tile; one block barrier
-// per step.  A copy that has not arrived after a bounded wait makes the block report NaN in the
-// iteration's p.q, which ends the inner solve with UWGPU_ERR_NAN.
+// The same direction update with every plane it reads staged by the tensor memory accelerator
+// (cp.async.bulk.tensor), for element grids whose x extent is a multiple of 4 (so that every z row
+// starts on 16 bytes).  Per z step one thread issues the copies of one stage into a ring of three:
+// the element plane of z with its halo, as a 40 x 10 box from x0 - 4 (x aligned down to 16 bytes;
+// coordinates outside the grid, the halo at the mesh boundary and the planes below and above the
+// mesh, read as zero), the 36 x 9 x 3 box of the node plane's three weight components, and (after
+// the first iteration) the tile's 32 x 8 plane of p and of q.  The copies complete on the stage's
+// mbarrier.  Ten warps: one thread per node of the 33 x 9 node plane, then one per element of the
+// 32 x 8 tile; one block barrier per step.  A copy that has not arrived after a bounded wait makes
+// the block report NaN in the iteration's p.q, which ends the inner solve with UWGPU_ERR_NAN.
 constexpr int kTmThreads = 320;
 constexpr int kTzX = kMfX + 8, kTzY = kMfY + 2;     // staged element plane: 40 x 10
 constexpr int kTwX = kMfX + 4, kTwY = kMfY + 1;     // staged weight plane: 36 x 9, three components
-constexpr int kTzBytes = kTzX * kTzY * 4, kTwBytes = 3 * kTwX * kTwY * 4;
+constexpr int kTzBytes = kTzX * kTzY * 4, kTwBytes = 3 * kTwX * kTwY * 4, kTpBytes = kMfX * kMfY * 4;
 constexpr int kTzSlot = (kTzBytes + 127) / 128 * 128, kTwSlot = (kTwBytes + 127) / 128 * 128;
-constexpr int kTmStage = kTzSlot + kTwSlot;
+constexpr int kTmStage = kTzSlot + kTwSlot + 2 * kTpBytes;   // z, W, p, q; every part 128-byte aligned
+static_assert(kTpBytes % 128 == 0, "p and q slots stay 128-byte aligned");
 constexpr int kTmNodes = (kMfX + 1) * (kMfY + 1);   // 297
 
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, uint32_t bar) {
@@ -582,10 +583,12 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 
-__global__ void __launch_bounds__(kTmThreads) k_cg_mf3_dir_tma(Mf3 a, const __grid_constant__ CUtensorMap tz,
-                                                              const __grid_constant__ CUtensorMap tw, float* __restrict__ p,
-                                                              float* __restrict__ q, double* __restrict__ scal, int k,
-                                                              int first) {
+__global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const __grid_constant__ CUtensorMap tz,
+                                                                 const __grid_constant__ CUtensorMap tw,
+                                                                 const __grid_constant__ CUtensorMap tp,
+                                                                 const __grid_constant__ CUtensorMap tq,
+                                                                 float* __restrict__ p, float* __restrict__ q,
+                                                                 double* __restrict__ scal, int k, int first) {
     __shared__ __align__(128) unsigned char ring[3 * kTmStage];
     __shared__ float yb[2][3][kTmNodes];
     __shared__ __align__(8) uint64_t bar[3];
@@ -609,12 +612,19 @@ __global__ void __launch_bounds__(kTmThreads) k_cg_mf3_dir_tma(Mf3 a, const __gr
     // earlier block's state)
     __syncthreads();
     const uint32_t ring_s = tc::smem_u32(ring);
-    auto issue = [&](int t) {   // stage t = element plane zlo - 1 + t and node plane zlo - 1 + t
+    // stage t = element plane zlo - 1 + t (z with halo; p and q of the tile when the plane is one of
+    // the block's own and p, q are read), node plane zlo - 1 + t (W)
+    auto issue = [&](int t) {
         const int slot = t % 3, plane = zlo - 1 + t;
-        const uint32_t b = tc::smem_u32(&bar[slot]);
-        mbar_expect_tx(b, (uint32_t)(kTzBytes + kTwBytes));
-        tma_load_3d(ring_s + slot * kTmStage, &tz, x0 - 4, y0 - 1, plane, b);
-        tma_load_4d(ring_s + slot * kTmStage + kTzSlot, &tw, x0, y0, plane, 0, b);
+        const bool pq = !first && plane >= zlo && plane < zhi;
+        const uint32_t b = tc::smem_u32(&bar[slot]), dst = ring_s + slot * kTmStage;
+        mbar_expect_tx(b, (uint32_t)(kTzBytes + kTwBytes + (pq ? 2 * kTpBytes : 0)));
+        tma_load_3d(dst, &tz, x0 - 4, y0 - 1, plane, b);
+        tma_load_4d(dst + kTzSlot, &tw, x0, y0, plane, 0, b);
+        if (pq) {
+            tma_load_3d(dst + kTzSlot + kTwSlot, &tp, x0, y0, plane, b);
+            tma_load_3d(dst + kTzSlot + kTwSlot + kTpBytes, &tq, x0, y0, plane, b);
+        }
     };
     pdl_wait();
     const float beta = first ? 0.f : block_ratio<float>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
@@ -624,13 +634,6 @@ __global__ void __launch_bounds__(kTmThreads) k_cg_mf3_dir_tma(Mf3 a, const __gr
     }
     const bool eok = tid < kMfX * kMfY && x0 + tx < ex && y0 + ty < ey;
     const int eo = eok ? (x0 + tx) + ex * (y0 + ty) : 0;
-    auto load_pq = [&](int plane, float& pv, float& qv) {
-        const bool ok = !first && eok && plane >= 0 && plane < zhi;
-        pv = ok ? p[plane * exy + eo] : 0.f;
-        qv = ok ? q[plane * exy + eo] : 0.f;
-    };
-    float pn, qn;
-    load_pq(zlo, pn, qn);
     // this thread's node of the plane: (nx, ny) in the 33 x 9 node block
     const bool node = tid < kTmNodes;
     const int nx = tid % (kMfX + 1), ny = tid / (kMfX + 1);
@@ -666,8 +669,6 @@ __global__ void __launch_bounds__(kTmThreads) k_cg_mf3_dir_tma(Mf3 a, const __gr
             yc[kTmNodes + tid] = wc[kTwX * kTwY + wb_node] * dy;
             yc[2 * kTmNodes + tid] = wc[2 * kTwX * kTwY + wb_node] * dz;
         }
-        const float pc = pn, qc = qn;
-        load_pq(kk, pn, qn);   // element plane kk, computed in the next step
         ok = __syncthreads_and(ok) != 0;
         if (!ok) break;
         // the slot of stage t + 1 last held stage t - 2, read by every thread before the barrier
@@ -689,8 +690,10 @@ __global__ void __launch_bounds__(kTmThreads) k_cg_mf3_dir_tma(Mf3 a, const __gr
                 }
                 const int64_t e = (int64_t)(kk - 1) * exy + eo;
                 const float ze = zp[zb_elem];
-                const float pe = first ? ze : fmaf(beta, pc, ze);
-                const float qe = first ? out : fmaf(beta, qc, out);
+                // p and q of element plane kk - 1 arrived with stage t - 1 (the slot of zp)
+                const float* pq_prev = reinterpret_cast<const float*>(ring + ((t + 2) % 3) * kTmStage + kTzSlot + kTwSlot);
+                const float pe = first ? ze : fmaf(beta, pq_prev[tid], ze);
+                const float qe = first ? out : fmaf(beta, pq_prev[kMfX * kMfY + tid], out);
                 if (e < exy * ez) {
                     p[e] = pe;
                     q[e] = qe;
@@ -748,11 +751,15 @@ struct MfLaunch {
     Mf3 a3;
     const float* Wc;
     unsigned blocks;
-    // tensor-memory-access form (3D, x extent a multiple of 4): maps of z and of Wc
+    // tensor-memory-access form (3D, x extent a multiple of 4): maps of z, Wc, p and q
     bool tma;
     const float* tma_z;
+    const float* tma_p;
+    const float* tma_q;
     CUtensorMap tz;
     CUtensorMap tw;
+    CUtensorMap tp;
+    CUtensorMap tq;
 };
 
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
@@ -772,8 +779,9 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
-// z: the vector the direction kernel will read (the tensor map is bound to it)
-static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* Wc, const float* z, int sms) {
+// z, p, q: the vectors the direction kernel will read and update (the tensor maps are bound to them)
+static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* Wc, const float* z, const float* p, const float* q,
+                          int sms) {
     MfLaunch L{};
     L.dim = m.dim;
     L.ex = (int)g.ex;
@@ -793,8 +801,8 @@ static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* Wc, const flo
     L.blocks = (unsigned)(txy * ((g.ez + zc - 1) / zc));
     L.tma = false;
     auto enc = tensor_map_encoder();
-    if (enc && z && g.ex % 4 == 0 && (reinterpret_cast<uintptr_t>(z) & 15) == 0 &&
-        (reinterpret_cast<uintptr_t>(Wc) & 15) == 0) {
+    auto al16 = [](const void* v) { return v && (reinterpret_cast<uintptr_t>(v) & 15) == 0; };
+    if (enc && g.ex % 4 == 0 && al16(z) && al16(Wc) && al16(p) && al16(q)) {
         const cuuint64_t zdim[3] = {(cuuint64_t)g.ex, (cuuint64_t)g.ey, (cuuint64_t)g.ez};
         const cuuint64_t zstr[2] = {(cuuint64_t)g.ex * 4, (cuuint64_t)g.ex * g.ey * 4};
         const cuuint32_t zbox[3] = {(cuuint32_t)kTzX, (cuuint32_t)kTzY, 1};
@@ -809,8 +817,17 @@ static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* Wc, const flo
         CUresult r2 = enc(&L.tw, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(Wc), wdim, wstr, wbox, one,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        L.tma = r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS;
+        const cuuint32_t pbox[3] = {(cuuint32_t)kMfX, (cuuint32_t)kMfY, 1};
+        CUresult r3 = enc(&L.tp, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(p), zdim, zstr, pbox, one,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        CUresult r4 = enc(&L.tq, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(q), zdim, zstr, pbox, one,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        L.tma = r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS && r3 == CUDA_SUCCESS && r4 == CUDA_SUCCESS;
         L.tma_z = z;
+        L.tma_p = p;
+        L.tma_q = q;
     }
     return L;
 }
@@ -819,8 +836,9 @@ static void mf_dir(const MfLaunch& L, cudaStream_t st, const float* z, float* p,
                    int first) {
     const unsigned nt = kMfX * kMfY;
     if (L.dim == 2) launch_pdl(k_cg_mf2_dir, L.blocks, nt, st, L.ex, L.ey, L.nnx, L.nn, L.Wc, z, p, q, scal, k, first);
-    else if (L.tma && z == L.tma_z)
-        launch_pdl(k_cg_mf3_dir_tma, L.blocks, (unsigned)kTmThreads, st, L.a3, L.tz, L.tw, p, q, scal, k, first);
+    else if (L.tma && z == L.tma_z && p == L.tma_p && q == L.tma_q)
+        launch_pdl(k_cg_mf3_dir_tma, L.blocks, (unsigned)kTmThreads, st, L.a3, L.tz, L.tw, L.tp, L.tq, p, q, scal, k,
+                   first);
     else launch_pdl(k_cg_mf3_dir, L.blocks, nt, st, L.a3, L.Wc, z, p, q, scal, k, first);
 }
 
@@ -1096,7 +1114,8 @@ static int gwg_cg_T(Context& c, const T* A, const float* Wmf, const T* dinv, con
     if (Wmf) {
         int sms = 0;
         UWG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
-        mf = mf_launch(m, g, Wmf, reinterpret_cast<const float*>(work + ne), sms);
+        const float* w32 = reinterpret_cast<const float*>(work);
+        mf = mf_launch(m, g, Wmf, w32 + ne, w32 + 2 * ne, w32 + 3 * ne, sms);
     }
     T* r = work;
     T* z = work + ne;
@@ -1255,7 +1274,7 @@ void bfbt_operator_hook(Context& c, int form, const double* xh, double* yh, int 
             gwg_mf_weights(c, W.p, W32.p);
             int sms = 0;
             UWG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device));
-            mf = mf_launch(m, g, W32.p, x32.p, sms);
+            mf = mf_launch(m, g, W32.p, x32.p, pq32.p, pq32.p + ne, sms);
         } else {
             A32.ensure((size_t)nb * ne);
             to_float(c, A.p, A32.p, (int64_t)nb * ne);
