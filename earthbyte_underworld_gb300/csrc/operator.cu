@@ -513,26 +513,34 @@ __global__ void k_dense_from_stencil(Grid g, const double* __restrict__ A, doubl
     }
 }
 
-__global__ void k_gj_save(int64_t n, int64_t k, const double* __restrict__ M, double* __restrict__ row,
-                          double* __restrict__ col) {
-    // row <- pivot row scaled by 1/pivot (row[k] <- 1/pivot), col <- pivot column
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Gauss-Jordan inverse, one launch per pivot k.  rr / cc hold the pivot row and column of step k
+// as they are before the step (unscaled); the step writes the row and column of pivot k + 1, as
+// they are after it, into the other pair of buffers.  Block (x, y) covers columns
+// 256 x .. 256 x + 255 of row y, so no thread divides.  In place, no pivoting: the coarse operator
+// is SPD.
+__global__ void k_gj_first(int64_t n, const double* __restrict__ M, double* __restrict__ rr, double* __restrict__ cc) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) {
-        double ip = 1.0 / M[k * n + k];
-        row[t] = t == k ? ip : M[k * n + t] * ip;
-        col[t] = M[t * n + k];
+        rr[t] = M[t];
+        cc[t] = M[t * n];
     }
 }
 
-// In-place Gauss-Jordan step k (no pivoting: the coarse operator is SPD).
-__global__ void k_gj_update(int64_t n, int64_t k, double* __restrict__ M, const double* __restrict__ row,
-                            const double* __restrict__ col) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n * n) return;
-    int64_t i = t / n, j = t % n;
-    if (i == k) M[t] = row[j];
-    else if (j == k) M[t] = -col[i] * row[k];
-    else M[t] = fma(-col[i], row[j], M[t]);
+__global__ void k_gj_step(int64_t n, int64_t k, double* __restrict__ M, const double* __restrict__ rr,
+                          const double* __restrict__ cc, double* __restrict__ rr_next, double* __restrict__ cc_next) {
+    __shared__ double s_ip;
+    if (threadIdx.x == 0) s_ip = 1.0 / rr[k];
+    __syncthreads();
+    const double ip = s_ip;
+    const int64_t i = blockIdx.y, j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    double v;
+    if (i == k) v = j == k ? ip : rr[j] * ip;
+    else if (j == k) v = -cc[i] * ip;
+    else v = fma(-cc[i], rr[j] * ip, M[i * n + j]);
+    M[i * n + j] = v;
+    if (i == k + 1) rr_next[j] = v;
+    if (j == k + 1) cc_next[i] = v;
 }
 
 // x = M b (one warp per row)
@@ -576,21 +584,22 @@ static void to_fp32(Context& c, const DArray<double>& a, DArray<float>& b) {
 
 // In-place Gauss-Jordan inverse of an SPD dense n x n matrix (no pivoting), on the stream.
 void dense_inverse(Context& c, double* M, int64_t n) {
-    DArray<double> row, col;
-    row.ensure((size_t)n);
-    col.ensure((size_t)n);
-    for (int64_t k = 0; k < n; ++k) {
-        {
-            LaunchScope ls(c, -1);
-            k_gj_save<<<blocks_for(n, 256), 256, 0, c.stream>>>(n, k, M, row.p, col.p);
-        }
-        {
-            LaunchScope ls(c, -1);
-            k_gj_update<<<blocks_for(n * n, 256), 256, 0, c.stream>>>(n, k, M, row.p, col.p);
-        }
+    UWG_REQUIRE(n < 65536, UWGPU_ERR_TOO_LARGE, "dense inverse: matrix too large");
+    DArray<double> buf;
+    buf.ensure((size_t)(4 * n));
+    double* rr[2] = {buf.p, buf.p + n};
+    double* cc[2] = {buf.p + 2 * n, buf.p + 3 * n};
+    {
+        LaunchScope ls(c, -1);
+        k_gj_first<<<blocks_for(n, 256), 256, 0, c.stream>>>(n, M, rr[0], cc[0]);
     }
-    check_launch("k_gj_update");
-    UWG_CUDA(cudaStreamSynchronize(c.stream));   // row and col are released on return
+    const dim3 grid((unsigned)((n + 255) / 256), (unsigned)n);
+    for (int64_t k = 0; k < n; ++k) {
+        LaunchScope ls(c, -1);
+        k_gj_step<<<grid, 256, 0, c.stream>>>(n, k, M, rr[k & 1], cc[k & 1], rr[(k + 1) & 1], cc[(k + 1) & 1]);
+    }
+    check_launch("k_gj_step");
+    UWG_CUDA(cudaStreamSynchronize(c.stream));   // the row and column buffers are released on return
 }
 
 // x = M b with a dense FP64 n x n matrix (one warp per row), vectors of type T
