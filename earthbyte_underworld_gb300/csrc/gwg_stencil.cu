@@ -564,6 +564,9 @@ constexpr int kTzBytes = kTzX * kTzY * 4, kTwBytes = 3 * kTwX * kTwY * 4, kTpByt
 constexpr int kTzSlot = (kTzBytes + 127) / 128 * 128, kTwSlot = (kTwBytes + 127) / 128 * 128;
 constexpr int kTmStage = kTzSlot + kTwSlot + 2 * kTpBytes;   // z, W, p, q; every part 128-byte aligned
 static_assert(kTpBytes % 128 == 0, "p and q slots stay 128-byte aligned");
+// Ring of stages: step t reads stages t - 1 and t, so a slot is free again two steps after its
+// stage was read; with kTmRing slots the copies run kTmRing - 2 stages ahead of the computation.
+constexpr int kTmRing = 5;
 constexpr int kTmNodes = (kMfX + 1) * (kMfY + 1);   // 297
 
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, uint32_t bar) {
@@ -589,9 +592,9 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
                                                                  const __grid_constant__ CUtensorMap tq,
                                                                  float* __restrict__ p, float* __restrict__ q,
                                                                  double* __restrict__ scal, int k, int first) {
-    __shared__ __align__(128) unsigned char ring[3 * kTmStage];
+    __shared__ __align__(128) unsigned char ring[kTmRing * kTmStage];
     __shared__ float yb[2][3][kTmNodes];
-    __shared__ __align__(8) uint64_t bar[3];
+    __shared__ __align__(8) uint64_t bar[kTmRing];
     __shared__ double sw[32];
     __shared__ float s_beta;
     const int ex = a.ex, ey = a.ey, ez = a.ez;
@@ -606,7 +609,7 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
     const int tid = threadIdx.x, tx = tid % kMfX, ty = tid / kMfX;
     const int64_t exy = (int64_t)ex * ey;
     if (tid == 0) {
-        for (int i = 0; i < 3; ++i) tc::mbar_init(&bar[i], 1);
+        for (int i = 0; i < kTmRing; ++i) tc::mbar_init(&bar[i], 1);
     }
     // no thread may poll a barrier before it is initialised (the shared memory may still hold an
     // earlier block's state)
@@ -615,7 +618,7 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
     // stage t = element plane zlo - 1 + t (z with halo; p and q of the tile when the plane is one of
     // the block's own and p, q are read), node plane zlo - 1 + t (W)
     auto issue = [&](int t) {
-        const int slot = t % 3, plane = zlo - 1 + t;
+        const int slot = t % kTmRing, plane = zlo - 1 + t;
         const bool pq = !first && plane >= zlo && plane < zhi;
         const uint32_t b = tc::smem_u32(&bar[slot]), dst = ring_s + slot * kTmStage;
         mbar_expect_tx(b, (uint32_t)(kTzBytes + kTwBytes + (pq ? 2 * kTpBytes : 0)));
@@ -628,10 +631,9 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
     };
     pdl_wait();
     const float beta = first ? 0.f : block_ratio<float>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
-    if (tid == 0) {
-        issue(0);
-        if (nsteps > 1) issue(1);
-    }
+    int issued = 0;   // stages issued so far (thread 0)
+    if (tid == 0)
+        while (issued < nsteps && issued < kTmRing - 1) issue(issued++);
     const bool eok = tid < kMfX * kMfY && x0 + tx < ex && y0 + ty < ey;
     const int eo = eok ? (x0 + tx) + ex * (y0 + ty) : 0;
     // this thread's node of the plane: (nx, ny) in the 33 x 9 node block
@@ -649,14 +651,13 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
     };
     float lo[3][4], hi[3][4];
     float local = 0.f;
-    int issued = nsteps > 1 ? 2 : 1;
     if (nsteps > 0) wait_slot(0);
     for (int t = 1; t < nsteps; ++t) {
         const int kk = zlo - 1 + t;
-        wait_slot(t % 3);
-        const float* zp = reinterpret_cast<const float*>(ring + ((t + 2) % 3) * kTmStage);   // element plane kk - 1
-        const float* zc = reinterpret_cast<const float*>(ring + (t % 3) * kTmStage);         // element plane kk
-        const float* wc = reinterpret_cast<const float*>(ring + (t % 3) * kTmStage + kTzSlot);
+        wait_slot(t % kTmRing);
+        const float* zp = reinterpret_cast<const float*>(ring + ((t - 1) % kTmRing) * kTmStage);   // element plane kk - 1
+        const float* zc = reinterpret_cast<const float*>(ring + (t % kTmRing) * kTmStage);         // element plane kk
+        const float* wc = reinterpret_cast<const float*>(ring + (t % kTmRing) * kTmStage + kTzSlot);
         float* yc = yb[t & 1][0];
         if (node) {
             const int b = zb_node;
@@ -671,7 +672,8 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
         }
         ok = __syncthreads_and(ok) != 0;
         if (!ok) break;
-        // the slot of stage t + 1 last held stage t - 2, read by every thread before the barrier
+        // the next stage, t + kTmRing - 2, goes to the slot of stage t - 2, which every thread
+        // finished reading before this barrier
         if (tid == 0 && issued < nsteps) issue(issued++);
         if (tid < kMfX * kMfY) {
 #pragma unroll
@@ -691,7 +693,7 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
                 const int64_t e = (int64_t)(kk - 1) * exy + eo;
                 const float ze = zp[zb_elem];
                 // p and q of element plane kk - 1 arrived with stage t - 1 (the slot of zp)
-                const float* pq_prev = reinterpret_cast<const float*>(ring + ((t + 2) % 3) * kTmStage + kTzSlot + kTwSlot);
+                const float* pq_prev = reinterpret_cast<const float*>(ring + ((t - 1) % kTmRing) * kTmStage + kTzSlot + kTwSlot);
                 const float pe = first ? ze : fmaf(beta, pq_prev[tid], ze);
                 const float qe = first ? out : fmaf(beta, pq_prev[kMfX * kMfY + tid], out);
                 if (e < exy * ez) {
@@ -712,7 +714,7 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
     if (!ok) {
         // let copies still in flight land before the block's shared memory is released
         if (tid == 0)
-            for (int t = 0; t < 3; ++t) tc::mbar_wait(&bar[t], (phase_bits >> t) & 1u, 1u << 16);
+            for (int t = 0; t < kTmRing; ++t) tc::mbar_wait(&bar[t], (phase_bits >> t) & 1u, 1u << 16);
         local = __int_as_float(0x7fc00000);   // NaN: the host ends the solve
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) *rr_slot(scal, k + 1) = 0.0;
@@ -825,6 +827,10 @@ static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* Wc, const flo
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         L.tma = r1 == CUDA_SUCCESS && r2 == CUDA_SUCCESS && r3 == CUDA_SUCCESS && r4 == CUDA_SUCCESS;
+        // four blocks of about 46 KB each per SM: ask for the largest shared-memory carveout
+        if (L.tma && cudaFuncSetAttribute(k_cg_mf3_dir_tma, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                          (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+            (void)cudaGetLastError();
         L.tma_z = z;
         L.tma_p = p;
         L.tma_q = q;
