@@ -1059,6 +1059,227 @@ EGrid egrid_of(const MeshDesc& m) {
     return g;
 }
 
+
+// ------------------------------------------------------------------------------------------
+// Coarse correction of the Jacobi inner solves on plane checkerboards (3D, option 4).
+// Q1-P0's spurious pressure modes make G^T W G nearly singular on element checkerboards: the
+// checkerboard (-1)^(i+j) of one z plane, multiplied by anything along z, is mapped to zero by G
+// away from the walls, and likewise for the other two axis pairs.  Jacobi removes them slowly, and
+// more slowly the finer the mesh.  The coarse space holds, per family F, one vector per plane:
+//   xy: v_k0(e) = (-1)^(i+j) [k = k0]   xz: v_j0(e) = (-1)^(i+k) [j = j0]   yz: v_i0(e) = (-1)^(j+k) [i = i0]
+// and the preconditioner is additive and block-diagonal over the families,
+//   M^-1 r = D^-1 r + sum_F Z_F E_F^-1 Z_F^T r,   E_F = Z_F^T A Z_F (tridiagonal, A couples
+// neighbouring planes only), still symmetric positive definite, so CG keeps its form.  Per
+// iteration: Z^T r (k_cc_sums), y = E^-1 Z^T r and the extra r.z term s.y (k_cc_small), z += Z y
+// (k_cc_zcorr).  Layout of s and y: the xy family (ez entries), then xz (ey), then yz (ex).
+// ------------------------------------------------------------------------------------------
+struct CcArgs {
+    int ex, ey, ez;
+    const double* einv;   // E_F^-1, row-major blocks ez^2 | ey^2 | ex^2
+    double* s;            // [2][ez + ey + ex]
+    double* y;            // [ez + ey + ex]
+};
+constexpr int kCcMaxX = 512;   // largest x extent (the column sums live in registers, 32 per lane)
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// s = Z^T r into buffer (k + 1) & 1: one warp per x row (j, k), lanes along x.  The row's
+// alternating sum alt = sum_i (-1)^i r gives both of its plane sums ((-1)^j alt to xy bin k,
+// (-1)^k alt to xz bin j); the yz bins (per i) are summed per lane over the warp's rows, then per
+// block in shared memory.
+template <typename T, int M>
+__global__ void __launch_bounds__(256) k_cc_sums(CcArgs a, const T* __restrict__ r, int k) {
+    __shared__ double col[kCcMaxX];
+    pdl_wait();
+    for (int i = threadIdx.x; i < a.ex; i += blockDim.x) col[i] = 0.0;
+    __syncthreads();
+    double* sb = a.s + (size_t)((k + 1) & 1) * (size_t)(a.ex + a.ey + a.ez);
+    double* sxy = sb;
+    double* sxz = sb + a.ez;
+    double* syz = sb + a.ez + a.ey;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rows = a.ey * a.ez;
+    double cacc[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) cacc[m] = 0.0;
+    for (int row = blockIdx.x * 8 + warp; row < rows; row += gridDim.x * 8) {
+        const int j = row % a.ey, kz = row / a.ey;
+        const T* rr = r + (int64_t)row * a.ex;
+        const bool neg = ((j + kz) & 1) != 0;
+        double alt = 0.0;
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            const int i = lane + 32 * m;
+            if (i < a.ex) {
+                const double v = (double)rr[i];
+                alt += (i & 1) ? -v : v;
+                cacc[m] += neg ? -v : v;
+            }
+        }
+        alt = warp_sum_d(alt);
+        if (lane == 0) {
+            atomicAdd(sxy + kz, (j & 1) ? -alt : alt);
+            atomicAdd(sxz + j, (kz & 1) ? -alt : alt);
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        const int i = lane + 32 * m;
+        if (i < a.ex) atomicAdd(&col[i], cacc[m]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < a.ex; i += blockDim.x) atomicAdd(syz + i, col[i]);
+    pdl_trigger();
+}
+
+// y = E^-1 s (one warp per coarse unknown), rz_{k+1} += s . y, and the other s buffer cleared for
+// the next iteration
+__global__ void __launch_bounds__(256) k_cc_small(CcArgs a, double* __restrict__ scal, int k) {
+    __shared__ double sw[8];
+    pdl_wait();
+    const int n = a.ex + a.ey + a.ez;
+    const double* sb = a.s + (size_t)((k + 1) & 1) * (size_t)n;
+    double* so = a.s + (size_t)(k & 1) * (size_t)n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int b = blockIdx.x * 8 + warp;
+    double part = 0.0;
+    if (b < n) {
+        int off, len;
+        const double* E;
+        if (b < a.ez) {
+            off = 0;
+            len = a.ez;
+            E = a.einv + (size_t)b * a.ez;
+        } else if (b < a.ez + a.ey) {
+            off = a.ez;
+            len = a.ey;
+            E = a.einv + (size_t)a.ez * a.ez + (size_t)(b - off) * a.ey;
+        } else {
+            off = a.ez + a.ey;
+            len = a.ex;
+            E = a.einv + (size_t)a.ez * a.ez + (size_t)a.ey * a.ey + (size_t)(b - off) * a.ex;
+        }
+        double acc = 0.0;
+        for (int cc = lane; cc < len; cc += 32) acc = fma(E[cc], sb[off + cc], acc);
+        acc = warp_sum_d(acc);
+        if (lane == 0) {
+            a.y[b] = acc;
+            part = acc * sb[b];
+        }
+    }
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) so[t] = 0.0;
+    if (lane == 0) sw[warp] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t += sw[w];
+        if (t != 0.0) atomicAdd(rz_slot(scal, k + 1), t);
+    }
+    pdl_trigger();
+}
+
+// z += Z y: grid (x-y plane chunks, z planes)
+template <typename T>
+__global__ void __launch_bounds__(256) k_cc_zcorr(CcArgs a, T* __restrict__ z) {
+    pdl_wait();
+    const int pxy = blockIdx.x * blockDim.x + threadIdx.x, kz = blockIdx.y;
+    if (pxy < a.ex * a.ey) {
+        const int i = pxy % a.ex, j = pxy / a.ex;
+        const double yxy = a.y[kz], yxz = a.y[a.ez + j], yyz = a.y[a.ez + a.ey + i];
+        const double v = (((i + j) & 1) ? -yxy : yxy) + (((i + kz) & 1) ? -yxz : yxz) + (((j + kz) & 1) ? -yyz : yyz);
+        const int64_t e = (int64_t)kz * a.ex * a.ey + pxy;
+        z[e] = (T)((double)z[e] + v);
+    }
+    pdl_trigger();
+}
+
+// The three diagonals of every E_F from the element stencil A[q][e] (q = (dx+1) + 3 (dy+1) +
+// 9 (dz+1), zero towards neighbours outside the mesh): E_xy[k][k+dz] = sum over the elements e of
+// plane k and their neighbours f at dz of A_ef (-1)^(dx+dy) (the product of the two checkerboard
+// signs), and the same for xz (offset dy, sign (-1)^(dx+dz)) and yz (offset dx, sign
+// (-1)^(dy+dz)).  ed: [xy: ez][3] | [xz: ey][3] | [yz: ex][3].  One warp per x row.
+template <int M>
+__global__ void __launch_bounds__(256) k_cc_build(EGrid g, const double* __restrict__ A, double* __restrict__ ed) {
+    __shared__ double col[kCcMaxX * 3];
+    const int ex = (int)g.ex, ey = (int)g.ey, ez = (int)g.ez;
+    for (int i = threadIdx.x; i < 3 * ex; i += blockDim.x) col[i] = 0.0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rows = ey * ez;
+    double cacc[M][3];
+#pragma unroll
+    for (int m = 0; m < M; ++m) cacc[m][0] = cacc[m][1] = cacc[m][2] = 0.0;
+    for (int row = blockIdx.x * 8 + warp; row < rows; row += gridDim.x * 8) {
+        const int j = row % ey, kz = row / ey;
+        double vxy[3] = {0.0, 0.0, 0.0}, vxz[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            const int i = lane + 32 * m;
+            if (i < ex) {
+                const int64_t e = (int64_t)row * ex + i;
+                for (int q = 0; q < 27; ++q) {
+                    const int dx = q % 3 - 1, dy = (q / 3) % 3 - 1, dz = q / 9 - 1;
+                    const double v = A[(int64_t)q * g.ne + e];
+                    vxy[dz + 1] += ((dx + dy) & 1) ? -v : v;
+                    vxz[dy + 1] += ((dx + dz) & 1) ? -v : v;
+                    cacc[m][dx + 1] += ((dy + dz) & 1) ? -v : v;
+                }
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double sxy = warp_sum_d(vxy[d]), sxz = warp_sum_d(vxz[d]);
+            if (lane == 0) {
+                atomicAdd(ed + kz * 3 + d, sxy);
+                atomicAdd(ed + 3 * ez + j * 3 + d, sxz);
+            }
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        const int i = lane + 32 * m;
+        if (i < ex)
+            for (int d = 0; d < 3; ++d) atomicAdd(&col[i * 3 + d], cacc[m][d]);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < 3 * ex; t += blockDim.x) atomicAdd(ed + 3 * (ez + ey) + t, col[t]);
+}
+
+CcArgs cc_args(Context& c) {
+    return CcArgs{c.cc.ex, c.cc.ey, c.cc.ez, c.cc.einv.p, c.cc.s.p, c.cc.y.p};
+}
+
+template <typename T>
+void cc_sums_launch(Context& c, const T* r, int k) {
+    const CcArgs a = cc_args(c);
+    const unsigned blocks = (unsigned)std::min<int64_t>(((int64_t)a.ey * a.ez + 7) / 8, 256);
+    if (a.ex <= 128) launch_pdl(k_cc_sums<T, 4>, blocks, 256u, c.stream, a, r, k);
+    else if (a.ex <= 256) launch_pdl(k_cc_sums<T, 8>, blocks, 256u, c.stream, a, r, k);
+    else launch_pdl(k_cc_sums<T, 16>, blocks, 256u, c.stream, a, r, k);
+}
+
+// the correction of iteration k: s = Z^T r, y = E^-1 s (and rz_{k+1} += s.y), z += Z y
+template <typename T>
+void cc_apply(Context& c, const T* r, T* z, double* scal, int k) {
+    const CcArgs a = cc_args(c);
+    cc_sums_launch<T>(c, r, k);
+    launch_pdl(k_cc_small, (unsigned)((a.ex + a.ey + a.ez + 7) / 8), 256u, c.stream, a, scal, k);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)((a.ex * a.ey + 255) / 256), (unsigned)a.ez);
+    cfg.blockDim = dim3(256);
+    cfg.stream = c.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    UWG_CUDA(cudaLaunchKernelEx(&cfg, k_cc_zcorr<T>, a, z));
+}
+
 }  // namespace
 
 // Builds the FP64 stencil A (stencil_points * ne values, entry-major) and dinv = 1/diag for the
@@ -1105,6 +1326,77 @@ void gwg_stencil_apply(Context& c, const double* A, const double* x, double* y, 
     check_launch("k_gwg_spmv");
 }
 
+// Builds the plane-checkerboard coarse correction for the FP64 element stencil A of G^T W G (3D):
+// the tridiagonal E_F from the stencil on the device, their inverses on the host (column by column
+// with the tridiagonal LDL^T factors; n^2 per family), and the device buffers.  Returns false (the
+// inner solves keep plain Jacobi) in 2D, on meshes wider than 512 elements along x, or when an
+// E_F is not positive definite.
+bool gwg_cc_build(Context& c, const double* A) {
+    const MeshDesc& m = c.levels[0].mesh;
+    c.cc.on = false;
+    if (m.dim != 3) return false;
+    const EGrid g = egrid_of(m);
+    if (g.ex > kCcMaxX || g.ey > 4096 || g.ez > 4096) return false;
+    const int ex = (int)g.ex, ey = (int)g.ey, ez = (int)g.ez, n = ex + ey + ez;
+    c.cc.ed.ensure((size_t)3 * n);
+    UWG_CUDA(cudaMemsetAsync(c.cc.ed.p, 0, sizeof(double) * 3 * n, c.stream));
+    {
+        LaunchScope ls(c, -1);
+        const unsigned blocks = (unsigned)std::min<int64_t>(((int64_t)ey * ez + 7) / 8, 1024);
+        if (ex <= 128) k_cc_build<4><<<blocks, 256, 0, c.stream>>>(g, A, c.cc.ed.p);
+        else if (ex <= 256) k_cc_build<8><<<blocks, 256, 0, c.stream>>>(g, A, c.cc.ed.p);
+        else k_cc_build<16><<<blocks, 256, 0, c.stream>>>(g, A, c.cc.ed.p);
+    }
+    check_launch("k_cc_build");
+    std::vector<double> ed((size_t)3 * n);
+    UWG_CUDA(cudaMemcpyAsync(ed.data(), c.cc.ed.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c.stream));
+    UWG_CUDA(cudaStreamSynchronize(c.stream));
+    std::vector<double> einv((size_t)ez * ez + (size_t)ey * ey + (size_t)ex * ex);
+    const int lens[3] = {ez, ey, ex};
+    size_t eoff = 0;
+    int doff = 0;
+    for (int f = 0; f < 3; ++f) {
+        const int len = lens[f];
+        const double* d3 = ed.data() + 3 * doff;
+        // symmetric tridiagonal: diagonal d3[b][1], off-diagonal between b and b + 1 the mean of
+        // d3[b][2] and d3[b + 1][0] (equal up to rounding, A being symmetric)
+        std::vector<double> dg(len), od(len > 1 ? len - 1 : 1, 0.0);
+        for (int b = 0; b < len; ++b) dg[b] = d3[3 * b + 1];
+        for (int b = 0; b + 1 < len; ++b) od[b] = 0.5 * (d3[3 * b + 2] + d3[3 * (b + 1)]);
+        // LDL^T: l[b] below the diagonal, D[b]
+        std::vector<double> D(len), l(len, 0.0);
+        double dmax = 0.0;
+        for (int b = 0; b < len; ++b) dmax = std::max(dmax, std::fabs(dg[b]));
+        for (int b = 0; b < len; ++b) {
+            D[b] = dg[b] - (b > 0 ? l[b - 1] * od[b - 1] : 0.0);
+            if (!(D[b] > 1e-12 * dmax)) return false;
+            if (b + 1 < len) l[b] = od[b] / D[b];
+        }
+        // columns of the inverse: L D L^T x = e_col
+        double* Ei = einv.data() + eoff;
+        std::vector<double> x(len);
+        for (int col = 0; col < len; ++col) {
+            for (int b = 0; b < len; ++b) x[b] = b == col ? 1.0 : 0.0;
+            for (int b = 1; b < len; ++b) x[b] -= l[b - 1] * x[b - 1];
+            for (int b = 0; b < len; ++b) x[b] /= D[b];
+            for (int b = len - 2; b >= 0; --b) x[b] -= l[b] * x[b + 1];
+            for (int b = 0; b < len; ++b) Ei[(size_t)b * len + col] = x[b];
+        }
+        eoff += (size_t)len * len;
+        doff += len;
+    }
+    c.cc.einv.ensure(einv.size());
+    c.cc.s.ensure((size_t)2 * n);
+    c.cc.y.ensure((size_t)n);
+    UWG_CUDA(cudaMemcpyAsync(c.cc.einv.p, einv.data(), sizeof(double) * einv.size(), cudaMemcpyHostToDevice, c.stream));
+    UWG_CUDA(cudaStreamSynchronize(c.stream));   // the host copy is released on return
+    c.cc.ex = ex;
+    c.cc.ey = ey;
+    c.cc.ez = ez;
+    c.cc.on = true;
+    return true;
+}
+
 // Solves A x = b (b projected off the constant by the caller when A has it) to
 // ||r|| <= rtol ||b|| by Jacobi-preconditioned CG.  work holds 4*ne values of T, scal 8 doubles.
 // With Wmf (FP32 only) A is applied matrix-free from the nodal weights instead of the stencil.
@@ -1139,10 +1431,14 @@ static int gwg_cg_T(Context& c, const T* A, const float* Wmf, const T* dinv, con
         if (m.dim == 3) launch_pdl(k_cg_spmv_dir<3, T>, eb, 256, c.stream, g, A, z, p, q, scal, k, first);
         else launch_pdl(k_cg_spmv_dir<2, T>, eb, 256, c.stream, g, A, z, p, q, scal, k, first);
     };
+    // the plane-checkerboard coarse correction, when the solver built it for this operator
+    const bool cc = c.cc.on && m.dim == 3 && c.cc.ex == g.ex && c.cc.ey == g.ey && c.cc.ez == g.ez;
     UWG_CUDA(cudaMemsetAsync(scal, 0, 8 * sizeof(double), c.stream));
+    if (cc) UWG_CUDA(cudaMemsetAsync(c.cc.s.p, 0, c.cc.s.n * sizeof(double), c.stream));
     {
         LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
         k_gwg_init<T><<<eb, 256, 0, c.stream>>>(ne, b, dinv, x, r, z, scal);
+        if (cc) cc_apply<T>(c, r, z, scal, -1);
     }
     {
         LaunchScope ls(c, UWGPU_KERNEL_VECTOR);
@@ -1158,10 +1454,12 @@ static int gwg_cg_T(Context& c, const T* A, const float* Wmf, const T* dinv, con
     const int block = 12;
     auto issue = [&](int k) {
         launch_pdl(k_cg_update<T>, ebv, 256, c.stream, ne, p, q, dinv, x, r, z, scal, k, (int)(k == block - 1));
+        if (cc) cc_apply<T>(c, r, z, scal, k);
         dir(k, 0);
     };
-    const void* key[8] = {Wmf ? (const void*)Wmf : (const void*)A, dinv, x, work, scal, (const void*)(intptr_t)ne,
-                          (const void*)(intptr_t)sizeof(T), (const void*)(intptr_t)(m.dim + (Wmf ? 48 : 16))};
+    const void* key[9] = {Wmf ? (const void*)Wmf : (const void*)A, dinv, x, work, scal, (const void*)(intptr_t)ne,
+                          (const void*)(intptr_t)sizeof(T), (const void*)(intptr_t)(m.dim + (Wmf ? 48 : 16)),
+                          cc ? (const void*)c.cc.einv.p : nullptr};
     Context::PcgGraph* pg = nullptr;
     for (auto& cand : c.pcg_graphs)
         if (std::equal(std::begin(key), std::end(key), std::begin(cand.key))) pg = &cand;
@@ -1179,7 +1477,7 @@ static int gwg_cg_T(Context& c, const T* A, const float* Wmf, const T* dinv, con
     // algorithmic traffic of one iteration: update (p, q, dinv, x, r read; x, r, z written) and
     // spmv+direction (the stencil, z, p, q read; p, q written; matrix-free: the dim nodal
     // weights of about one node per element in place of the stencil)
-    const double it_bytes = (double)ne * sizeof(T) * (8 + (Wmf ? m.dim : nb) + 5);
+    const double it_bytes = (double)ne * sizeof(T) * (8 + (Wmf ? m.dim : nb) + 5 + (cc ? 3 : 0));
     const double it_flops = Wmf ? (double)ne * (m.dim == 3 ? 110.0 : 46.0) : (double)ne * (2.0 * nb + 14.0);
     int it = 0;
     while (it < maxit) {
@@ -1188,7 +1486,7 @@ static int gwg_cg_T(Context& c, const T* A, const float* Wmf, const T* dinv, con
             UWG_CUDA(cudaGraphLaunch(pg->exec, c.stream));
         }
         note_work(c, UWGPU_KERNEL_SCHUR_PC, block * it_bytes, block * it_flops);
-        c.launches += 2 * block - 1;
+        c.launches += (cc ? 5 : 2) * block - 1;
         it += block;
         UWG_CUDA(cudaMemcpyAsync(hs, scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         UWG_CUDA(cudaStreamSynchronize(c.stream));
@@ -1555,8 +1853,8 @@ static int gwg_cg_mg_T(Context& c, const T* A, const T* dinv, const double* b, T
         if (m.dim == 3) k_cg_spmv_dir<3, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, 0);
         else k_cg_spmv_dir<2, T><<<eb, 256, 0, c.stream>>>(g, A, z, p, q, scal, k, 0);
     };
-    const void* key[8] = {A, dinv, x, work, scal, (const void*)(intptr_t)ne, (const void*)(intptr_t)sizeof(T),
-                          (const void*)(intptr_t)(m.dim + 32)};
+    const void* key[9] = {A, dinv, x, work, scal, (const void*)(intptr_t)ne, (const void*)(intptr_t)sizeof(T),
+                          (const void*)(intptr_t)(m.dim + 32), nullptr};
     Context::PcgGraph* pg = nullptr;
     for (auto& cand : c.pcg_graphs)
         if (std::equal(std::begin(key), std::end(key), std::begin(cand.key))) pg = &cand;

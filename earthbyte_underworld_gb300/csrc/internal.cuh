@@ -217,9 +217,18 @@ struct Context {
 
     // CUDA graphs of the BFBt inner-CG iteration block, one per buffer set
     struct PcgGraph {
-        const void* key[8];
+        const void* key[9];
         cudaGraphExec_t exec = nullptr;
     };
+    // Coarse correction of the BFBt inner solves on the element checkerboards of single planes
+    // (gwg_stencil.cu), built per solve when requested: E_F^-1 per family (row-major blocks of
+    // ez^2, ey^2, ex^2), the coarse residuals s (two buffers of ez + ey + ex) and the coarse
+    // solution y
+    struct CoarseCheckerboards {
+        bool on = false;
+        int ex = 0, ey = 0, ez = 0;
+        DArray<double> einv, s, y, ed;
+    } cc;
     std::vector<PcgGraph> pcg_graphs;
 
     // learned velocity preconditioner (csrc/unet.cu), created on request

@@ -43,6 +43,7 @@ int gwg_cg32(Context& c, const float* A, const float* dinv, const double* b, flo
              float* work, double* scal);
 double g_inf_norm(Context& c);
 bool gwg_mg_build(Context& c, const double* A0, const double* dinv0, bool need32, bool const_null);
+bool gwg_cc_build(Context& c, const double* A);
 int gwg_cg_mg(Context& c, const double* A, const double* dinv, const double* b, double* x, double rtol, int maxit,
               double* work, double* scal);
 int gwg_cg_mg32(Context& c, const float* A, const float* dinv, const double* b, float* x, double rtol, int maxit,
@@ -471,6 +472,7 @@ struct Bsscr {
 
     Bsscr(Context& ctx, const uwgpu_solve_opts& opts, uwgpu_report& r)
         : c(ctx), o(opts), rep(r), red(ctx), gm64(ctx, red), gm32(ctx, red), gms(ctx, red) {}
+    ~Bsscr() { c.cc.on = false; }   // the coarse correction belongs to this solve's operator
 
     // velocity hierarchy: operator, levels, Chebyshev bounds
     void setup_velocity() {
@@ -1004,12 +1006,16 @@ void Bsscr::run() {
             int l2 = 0;
             UWG_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c.device));
             const double st_bytes = (double)npres * 4.0 * ((dim == 3 ? 27 : 9) + 6);
-            stencil32 = o.bfbt_inner_pc == 2 || (o.bfbt_inner_pc == 0 && st_bytes <= 0.5 * l2);
+            stencil32 = o.bfbt_inner_pc == 2 ||
+                        ((o.bfbt_inner_pc == 0 || o.bfbt_inner_pc == 4) && st_bytes <= 0.5 * l2);
             const bool want_stencil32 = stencil32 || o.bfbt_inner_pc == 1;
             if (want_stencil32) bA32.ensure((size_t)(dim == 3 ? 27 : 9) * npres);
             gwg_stencil_fp32(c, bA.p, bd.p, want_stencil32 ? bA32.p : nullptr, bd32.p);
         }
         if (o.bfbt_inner_pc == 1) bfbt_mg = gwg_mg_build(c, bA.p, bd.p, mixed, bbt_const);
+        // option 4: Jacobi plus the plane-checkerboard coarse correction (3D; plain Jacobi in 2D)
+        c.cc.on = false;
+        if (o.bfbt_inner_pc == 4) gwg_cc_build(c, bA.p);
     }
     UWG_CUDA(cudaStreamSynchronize(c.stream));
     auto t1 = std::chrono::steady_clock::now();
@@ -1077,7 +1083,7 @@ void solve_bsscr(Context& c, const uwgpu_solve_opts& o, uwgpu_report& rep) {
     UWG_REQUIRE(o.remove_const_p >= 0 && o.remove_const_p <= 2, UWGPU_ERR_ARGUMENT, "bad pressure null-space mode");
     UWG_REQUIRE(o.learned_pc == 0 || o.learned_pc == 1, UWGPU_ERR_ARGUMENT, "bad learned_pc");
     UWG_REQUIRE(o.mg_cycle == 1 || o.mg_cycle == 2, UWGPU_ERR_ARGUMENT, "mg_cycle must be 1 (V) or 2 (W)");
-    UWG_REQUIRE(o.bfbt_inner_pc >= 0 && o.bfbt_inner_pc <= 3, UWGPU_ERR_ARGUMENT, "bfbt_inner_pc must be 0..3");
+    UWG_REQUIRE(o.bfbt_inner_pc >= 0 && o.bfbt_inner_pc <= 4, UWGPU_ERR_ARGUMENT, "bfbt_inner_pc must be 0..4");
     Bsscr s(c, o, rep);
     s.run();
 }

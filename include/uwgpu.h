@@ -139,7 +139,11 @@ typedef struct {
                                  as the reference's KSP; the mixed form reads the FP32 stencil
                                  while it fits in half of L2, else applies G^T W G matrix-free),
                                  1 aggregation multigrid V-cycle, 2 Jacobi on the FP32 stencil,
-                                 3 Jacobi with the matrix-free FP32 apply (2, 3: mixed form)     */
+                                 3 Jacobi with the matrix-free FP32 apply (2, 3: mixed form),
+                                 4 Jacobi plus an additive coarse correction on the element
+                                 checkerboards of single planes, Q1-P0's near-null pressure
+                                 modes (3D; the operator form chosen as for 0; 2D: as 0).  No
+                                 reference counterpart: the reference's inner KSP is Jacobi. */
 } uwgpu_solve_opts;
 
 typedef struct {
