@@ -377,6 +377,8 @@ def solve_bsscr(m, fixed, Ke, Ge, fe, Se, mg_levels=3, smooth=2, schur_type=1, s
     rc = lib().uwr_solve_bsscr_bc(C.byref(m), _p(fx), _p(bv), _p(np.ascontiguousarray(Ke)),
                                   _p(np.ascontiguousarray(Ge)), _p(np.ascontiguousarray(fe)),
                                   _p(np.ascontiguousarray(Se)), C.byref(o), _p(u), _p(p), C.byref(rep))
+    if rc == -3:
+        raise ValueError(f"oracle BSSCR: {m.dim}D mesh {tuple(m.nel[:m.dim])} does not coarsen {mg_levels - 1} times")
     if rc != 0:
         raise RuntimeError("oracle BSSCR setup failed (coarse factorisation)")
     return u, p, rep

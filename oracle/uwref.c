@@ -1904,6 +1904,15 @@ typedef struct {
  * Richardson/SOR smoothers (PETScMGSolver.c:641-716). */
 static int mg_setup(mg_t* mg, const uwr_mesh* m, const int64_t* eq, const csr* K, int levels, int down, int up) {
     memset(mg, 0, sizeof(*mg));
+    /* every coarsening halves each axis: the element counts must stay even down to level 1 */
+    {
+        uwr_mesh t = *m;
+        for (int l = levels - 1; l >= 1; --l)
+            for (int d = 0; d < t.dim; ++d) {
+                if (t.nel[d] < 2 || (t.nel[d] & 1)) return -3;
+                t.nel[d] /= 2;
+            }
+    }
     mg->nlev = levels;
     mg->down = down;
     mg->up = up;

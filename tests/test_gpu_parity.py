@@ -251,11 +251,11 @@ def test_bfbt_preconditioner_matches_oracle(oracle, uw, case, inner_pc):
     # with inner_pc = 1: 32x32 coarsens once (V-cycle to a dense 16x16), 8^3 is solved densely,
     # 16^3 coarsens once in 3D; inner_pc = 3: the mixed form's matrix-free inner operator;
     # inner_pc = 4: the plane-checkerboard coarse correction (2D: plain Jacobi), also on a mesh
-    # of unequal, odd extents
+    # of unequal extents that are not multiples of a tile
     w = {"rt2d": lambda: W.rt2d(nel=(32, 32), ppc=20),
          "spheres": lambda: W.spheres(nel=(8, 8, 8), nspheres=10, seed=9),
          "spheres16": lambda: W.spheres(nel=(16, 16, 16), nspheres=20, seed=5),
-         "spheres_ragged": lambda: W.spheres(nel=(12, 9, 7), nspheres=8, seed=4)}[case]()
+         "spheres_ragged": lambda: W.spheres(nel=(12, 8, 20), nspheres=8, seed=4)}[case]()
     ctx, perm, offsets, xi, Ke, fe, Ge, Se, eta = _run_gpu(U, W, w)
     m = O.make_mesh(w["dim"], w["nel"])
     ou, op, orep = O.solve_bsscr(m, w["fixed"], Ke, Ge, fe, Se, mg_levels=3, schur_type=1, schur_pc=3,

@@ -178,3 +178,15 @@ def test_oracle_newton_form_without_yield_equals_picard(oracle):
     K0, *_ = O.assemble(m, off, perm, xi, None, mats, f0)
     K1, *_ = O.assemble(m, off, perm, xi, None, mats, f1)
     assert np.abs(K1 - K0).max() < 1e-13 * np.abs(K0).max()
+
+
+def test_oracle_refuses_meshes_that_do_not_coarsen(oracle):
+    """The oracle's multigrid halves every axis per level: an odd element count on a level that
+    is still coarsened is refused with an error instead of a broken hierarchy."""
+    O = oracle
+    m = O.make_mesh(2, (6, 5))
+    nn, E = 7 * 6, 30
+    fixed = np.zeros(nn * 2, np.uint8)
+    Ke = np.tile(np.eye(8), (E, 1, 1))
+    with pytest.raises(ValueError):
+        O.solve_bsscr(m, fixed, Ke, np.zeros((E, 8)), np.zeros((E, 8)), np.ones(E), mg_levels=2)
