@@ -554,6 +554,13 @@ int uwgpu_assembly_set(uwgpu_ctx* ctx, int32_t mode) {
     });
 }
 
+int uwgpu_smoother_storage_set(uwgpu_ctx* ctx, int32_t bits) {
+    return guarded(ctx, [&](Context& c) {
+        UWG_REQUIRE(bits == 16 || bits == 32, UWGPU_ERR_ARGUMENT, "smoother stencil storage must be 16 or 32 bits");
+        c.smooth16 = bits == 16;
+    });
+}
+
 int uwgpu_tc_check(uwgpu_ctx* ctx, int32_t layout, int32_t format, int32_t n, int32_t k, const uint16_t* a,
                    const uint16_t* b, float* d) {
     return guarded(ctx, [&](Context& c) {

@@ -272,17 +272,29 @@ __global__ void k_cg_update(int64_t ne, const T* __restrict__ p, const T* __rest
     __shared__ double sw[32];
     __shared__ T s_alpha;
     pdl_wait();
-    const T alpha = block_ratio<T>(rz_slot(scal, k), pq_slot(scal, k), &s_alpha);
+    // the vectors first: their loads are in flight while thread 0 fetches the scalars for alpha
     const int64_t base = (int64_t)blockIdx.x * blockDim.x * kEpt + threadIdx.x;
+    T pv[kEpt], qv[kEpt], xv[kEpt], rv[kEpt], dv[kEpt];
+#pragma unroll
+    for (int m = 0; m < kEpt; ++m) {
+        const int64_t e = base + (int64_t)m * blockDim.x;
+        const bool in = e < ne;
+        pv[m] = in ? p[e] : (T)0;
+        qv[m] = in ? q[e] : (T)0;
+        xv[m] = in ? x[e] : (T)0;
+        rv[m] = in ? r[e] : (T)0;
+        dv[m] = in ? dinv[e] : (T)0;
+    }
+    const T alpha = block_ratio<T>(rz_slot(scal, k), pq_slot(scal, k), &s_alpha);
     T rz = (T)0, rr = (T)0;
 #pragma unroll
     for (int m = 0; m < kEpt; ++m) {
         const int64_t e = base + (int64_t)m * blockDim.x;
         if (e < ne) {
-            x[e] = fma(alpha, p[e], x[e]);
-            T re = fma(-alpha, q[e], r[e]);
+            x[e] = fma(alpha, pv[m], xv[m]);
+            T re = fma(-alpha, qv[m], rv[m]);
             r[e] = re;
-            T ze = re * dinv[e];
+            T ze = re * dv[m];
             z[e] = ze;
             rz = fma(re, ze, rz);
             rr = fma(re, re, rr);
@@ -630,10 +642,11 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
         }
     };
     pdl_wait();
-    const float beta = first ? 0.f : block_ratio<float>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
+    // the first copies go out before the block waits for the scalars of beta
     int issued = 0;   // stages issued so far (thread 0)
     if (tid == 0)
         while (issued < nsteps && issued < kTmRing - 1) issue(issued++);
+    const float beta = first ? 0.f : block_ratio<float>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
     const bool eok = tid < kMfX * kMfY && x0 + tx < ex && y0 + ty < ey;
     const int eo = eok ? (x0 + tx) + ex * (y0 + ty) : 0;
     // this thread's node of the plane: (nx, ny) in the 33 x 9 node block

@@ -95,6 +95,11 @@ struct Level {
     DArray<float> A32;
     DArray<double> Dinv64;   // inverse of the node's diagonal block [r][c][node]
     DArray<float> Dinv32;
+    // FP16 copy of the stencil for the mixed form's smoothing and V-cycle residuals: each row
+    // (r, node) divided by its largest magnitude S16[r][node] (IEEE half bits, same layout as A32)
+    DArray<uint16_t> A16;
+    DArray<float> S16;
+    bool has16 = false;
     DArray<uint8_t> fixed;   // per dof (node*dim+d), Dirichlet mask
     // work vectors (SoA by component: [d][node])
     DArray<double> r64, x64, b64, t64;
@@ -200,6 +205,8 @@ struct Context {
     ProfileFamily prof[UWGPU_KERNEL_COUNT];
     // while >= 0, every launch is counted in this family (the solver's setup phase)
     int family_override = -1;
+    // the mixed form smooths (and forms V-cycle residuals) with the FP16 row-scaled stencils
+    bool smooth16 = true;
 
     // multigrid hierarchy of the BFBt operator G^T W G (gwg_stencil.cu): element grids coarsened
     // 2:1 by aggregation; level 0's stencil belongs to the solve, the others live here, as do the

@@ -19,10 +19,12 @@
 // Coarse element matrices are formed element by element (P_c^T K_c P_c over the 2^dim children),
 // which equals the Galerkin product for this interpolation.
 #include <cooperative_groups.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cstring>
 #include <iterator>
+#include <type_traits>
 
 #include "internal.cuh"
 
@@ -237,6 +239,71 @@ __device__ __forceinline__ T stencil_row_r(const Grid& g, int64_t n, int64_t i, 
     return out;
 }
 
+// The same row product from the FP16 row-scaled stencil (A16 = A / S16 per row), unscaled: the
+// caller multiplies by S16[r][n].  Loads in batches of 9 neighbours, as the FP32 form.
+template <int DIM>
+__device__ __forceinline__ float stencil_row_h(const Grid& g, int64_t n, int64_t i, int64_t j, int64_t k, int r,
+                                               const uint16_t* __restrict__ A, const float* __restrict__ x) {
+    constexpr int NB = nblocks<DIM>();
+    constexpr int QB = 9;
+    const NbrOffsets o = nbr_offsets<DIM>(g, i, j, k);
+    float out = 0.f;
+#pragma unroll
+    for (int q0 = 0; q0 < NB; q0 += QB) {
+        unsigned short a[QB * DIM];
+        float xv[QB * DIM];
+#pragma unroll
+        for (int qq = 0; qq < QB; ++qq) {
+            const int q = q0 + qq;
+            const int64_t m = n + o.dx[q % 3] + o.dy[(q / 3) % 3] + o.dz[DIM == 3 ? q / 9 : 1];
+#pragma unroll
+            for (int cc = 0; cc < DIM; ++cc) {
+                a[qq * DIM + cc] = __ldg(A + ((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n);
+                xv[qq * DIM + cc] = x[(int64_t)cc * g.nn + m];
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < QB * DIM; ++t) out = fmaf(__half2float(__ushort_as_half(a[t])), xv[t], out);
+    }
+    return out;
+}
+
+// r = b - A x with the FP16 stencil (V-cycle residuals of the mixed form)
+template <int DIM>
+__global__ void __launch_bounds__(kRowThreads) k_residual_h(Grid g, const uint16_t* __restrict__ A,
+                                                            const float* __restrict__ S, const float* __restrict__ x,
+                                                            const float* __restrict__ b, float* __restrict__ y) {
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int r = warp % DIM, grp = warp / DIM;
+    int64_t n = (int64_t)blockIdx.x * (kRowThreads / DIM) + grp * 32 + lane;
+    if (n >= g.nn) return;
+    int64_t i, j, k;
+    node_ijk<DIM>(g, n, i, j, k);
+    const int64_t idx = (int64_t)r * g.nn + n;
+    y[idx] = b[idx] - S[idx] * stencil_row_h<DIM>(g, n, i, j, k, r, A, x);
+}
+
+// FP32 -> FP16 row-scaled stencil: S16[r][n] = max over the row's entries of |A|, A16 = A / S16
+template <int DIM>
+__global__ void k_to_fp16_rows(Grid g, const float* __restrict__ A, uint16_t* __restrict__ A16,
+                               float* __restrict__ S16) {
+    constexpr int NB = nblocks<DIM>();
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)DIM * g.nn) return;
+    const int r = (int)(t / g.nn);
+    const int64_t n = t % g.nn;
+    float mx = 0.f;
+    for (int q = 0; q < NB; ++q)
+        for (int cc = 0; cc < DIM; ++cc) mx = fmaxf(mx, fabsf(A[((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n]));
+    const float sc = mx > 0.f ? mx : 1.f, inv = 1.f / sc;
+    S16[t] = sc;
+    for (int q = 0; q < NB; ++q)
+        for (int cc = 0; cc < DIM; ++cc) {
+            const int64_t o = ((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n;
+            A16[o] = __half_as_ushort(__float2half_rn(A[o] * inv));
+        }
+}
+
 // y = A x (or r = b - A x when b is given), row-split
 template <int DIM, typename T>
 __global__ void __launch_bounds__(kRowThreads) k_apply(Grid g, const T* __restrict__ A, const T* __restrict__ x,
@@ -337,6 +404,38 @@ __global__ void __launch_bounds__(kRowThreads) k_cheb_step(Grid g, const T* __re
     T dn = first ? c2 * z : fma(c1, d[idx], c2 * z);
     d[idx] = dn;
     xout[idx] = (xin ? xin[idx] : (T)0) + dn;
+}
+
+// The Chebyshev step with the FP16 row-scaled stencil (mixed form)
+template <int DIM>
+__global__ void __launch_bounds__(kRowThreads) k_cheb_step_h(Grid g, const uint16_t* __restrict__ A,
+                                                             const float* __restrict__ S, const float* __restrict__ Dinv,
+                                                             const float* __restrict__ b, const float* __restrict__ xin,
+                                                             float* __restrict__ xout, float* __restrict__ d, float c1,
+                                                             float c2, int first) {
+    __shared__ float sres[kRowThreads];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int r = warp % DIM, grp = warp / DIM;
+    int64_t n = (int64_t)blockIdx.x * (kRowThreads / DIM) + grp * 32 + lane;
+    bool act = n < g.nn;
+    float res = 0.f;
+    if (act) {
+        int64_t i, j, k;
+        node_ijk<DIM>(g, n, i, j, k);
+        const int64_t idx = (int64_t)r * g.nn + n;
+        res = b[idx];
+        if (xin) res -= S[idx] * stencil_row_h<DIM>(g, n, i, j, k, r, A, xin);
+    }
+    sres[threadIdx.x] = res;
+    __syncthreads();
+    if (!act) return;
+    float z = 0.f;
+#pragma unroll
+    for (int cc = 0; cc < DIM; ++cc) z = fmaf(Dinv[(int64_t)(r * DIM + cc) * g.nn + n], sres[(grp * DIM + cc) * 32 + lane], z);
+    int64_t idx = (int64_t)r * g.nn + n;
+    float dn = first ? c2 * z : fmaf(c1, d[idx], c2 * z);
+    d[idx] = dn;
+    xout[idx] = (xin ? xin[idx] : 0.f) + dn;
 }
 
 // z = Dinv y (block diagonal)
@@ -806,9 +905,23 @@ void build_operator(Context& c, int levels, bool need32) {
         L.b64.ensure(nv);
         L.t64.ensure(nv);
         L.has32 = false;
+        L.has16 = false;
         if (need32) {
             to_fp32(c, L.A64, L.A32);
             to_fp32(c, L.Dinv64, L.Dinv32);
+            {
+                const Grid g = grid_of(L.mesh);
+                const int nb = dim == 3 ? 27 : 9;
+                L.A16.ensure((size_t)nb * dim * dim * g.nn);
+                L.S16.ensure((size_t)dim * g.nn);
+                LaunchScope ls(c, -1);
+                if (dim == 3)
+                    k_to_fp16_rows<3><<<blocks_for(3 * g.nn, 256), 256, 0, c.stream>>>(g, L.A32.p, L.A16.p, L.S16.p);
+                else
+                    k_to_fp16_rows<2><<<blocks_for(2 * g.nn, 256), 256, 0, c.stream>>>(g, L.A32.p, L.A16.p, L.S16.p);
+                check_launch("k_to_fp16_rows");
+                L.has16 = true;
+            }
             L.r32.ensure(nv);
             L.x32.ensure(nv);
             L.b32.ensure(nv);
@@ -855,6 +968,17 @@ template <typename T>
 void level_residual(Context& c, const Level& L, const T* x, const T* b, T* r) {
     Grid g = grid_of(L.mesh);
     int D = g.dim, NB = D == 3 ? 27 : 9;
+    if constexpr (std::is_same<T, float>::value) {
+        if (L.has16 && c.smooth16) {
+            note_work(c, UWGPU_KERNEL_APPLY, (double)g.nn * (NB * D * D * 2 + 4 * D * 4), 2.0 * g.nn * NB * D * D);
+            LaunchScope ls(c, UWGPU_KERNEL_APPLY);
+            if (g.dim == 3)
+                k_residual_h<3><<<blocks_for(g.nn, kRowThreads / 3), kRowThreads, 0, c.stream>>>(g, L.A16.p, L.S16.p, x, b, r);
+            else
+                k_residual_h<2><<<blocks_for(g.nn, kRowThreads / 2), kRowThreads, 0, c.stream>>>(g, L.A16.p, L.S16.p, x, b, r);
+            return;
+        }
+    }
     note_work(c, UWGPU_KERNEL_APPLY, (double)g.nn * (NB * D * D + 3 * D) * sizeof(T), 2.0 * g.nn * NB * D * D);
     LaunchScope ls(c, UWGPU_KERNEL_APPLY);
     if (g.dim == 3)
@@ -955,8 +1079,14 @@ void level_cheb(Context& c, Level& L, const T* b, T* x, int degree, bool zero_in
     double sigma = theta / delta, rho = 1.0 / sigma;
     T* alt = tmp_of<T>(L);
     T* d = dvec_of<T>(L);
-    note_work(c, UWGPU_KERNEL_SMOOTH, (double)degree * g.nn * (NB * D * D + D * D + 5 * D) * sizeof(T),
-              (double)degree * 2.0 * g.nn * (NB * D * D + D * D));
+    bool half = false;
+    if constexpr (std::is_same<T, float>::value) half = L.has16 && c.smooth16;
+    if (half)
+        note_work(c, UWGPU_KERNEL_SMOOTH, (double)degree * g.nn * (NB * D * D * 2 + (D * D + 6 * D) * 4),
+                  (double)degree * 2.0 * g.nn * (NB * D * D + D * D));
+    else
+        note_work(c, UWGPU_KERNEL_SMOOTH, (double)degree * g.nn * (NB * D * D + D * D + 5 * D) * sizeof(T),
+                  (double)degree * 2.0 * g.nn * (NB * D * D + D * D));
     const T* cur = zero_init ? nullptr : x;
     for (int k = 0; k < degree; ++k) {
         T* dst = (k % 2 == 0) ? alt : x;
@@ -970,6 +1100,18 @@ void level_cheb(Context& c, Level& L, const T* b, T* x, int degree, bool zero_in
             rho = rho_new;
         }
         LaunchScope ls(c, UWGPU_KERNEL_SMOOTH);
+        if constexpr (std::is_same<T, float>::value) {
+            if (half) {
+                if (D == 3)
+                    k_cheb_step_h<3><<<blocks_for(g.nn, kRowThreads / 3), kRowThreads, 0, c.stream>>>(
+                        g, L.A16.p, L.S16.p, L.Dinv32.p, b, cur, dst, d, (float)c1, (float)c2, k == 0);
+                else
+                    k_cheb_step_h<2><<<blocks_for(g.nn, kRowThreads / 2), kRowThreads, 0, c.stream>>>(
+                        g, L.A16.p, L.S16.p, L.Dinv32.p, b, cur, dst, d, (float)c1, (float)c2, k == 0);
+                cur = dst;
+                continue;
+            }
+        }
         if (D == 3)
             k_cheb_step<3, T><<<blocks_for(g.nn, kRowThreads / 3), kRowThreads, 0, c.stream>>>(
                 g, stencil_of<T>(L), dinv_of<T>(L), b, cur, dst, d, (T)c1, (T)c2, k == 0);

@@ -157,6 +157,7 @@ def load(build_if_missing: bool = True):
         L.uwgpu_learned_train.argtypes = [P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, P, P]
         L.uwgpu_tc_check.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P, P]
         L.uwgpu_assembly_set.argtypes = [P, C.c_int32]
+        L.uwgpu_smoother_storage_set.argtypes = [P, C.c_int32]
         L.uwgpu_jacobian_set.argtypes = [P, C.c_int32]
         L.uwgpu_population_control.argtypes = [P, P, P]
         L.uwgpu_get_cell_tables.argtypes = [P, P, P]
@@ -333,6 +334,10 @@ class Context:
     def jacobian_set(self, on=True):
         """Newton (Jacobian) form of the 2D element matrices for the next assemblies."""
         self._check(self._L.uwgpu_jacobian_set(self._h, 1 if on else 0))
+
+    def smoother_storage_set(self, bits):
+        """16 (default): the mixed form smooths with FP16 row-scaled stencils; 32: FP32."""
+        self._check(self._L.uwgpu_smoother_storage_set(self._h, int(bits)))
 
     def assembly_set(self, mode):
         """ASSEMBLY_FP64 (default) or ASSEMBLY_TENSOR (tensor-core contraction of the moments, 3D)."""

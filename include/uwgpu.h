@@ -302,6 +302,14 @@ int uwgpu_assemble(uwgpu_ctx* ctx);
 enum { UWGPU_ASSEMBLY_FP64 = 0, UWGPU_ASSEMBLY_TENSOR = 1 };
 int uwgpu_assembly_set(uwgpu_ctx* ctx, int32_t mode);
 
+/* Storage of the stencils the mixed form's V-cycle smooths with (no reference counterpart: the
+ * reference's PCMG smooths in FP64): 16 (default) keeps an FP16 copy of every level's stencil with
+ * each row divided by its largest magnitude (relative error 2^-11 of the row's largest entry),
+ * read by the Chebyshev smoother and the V-cycle residuals, which halves their stencil bytes; the
+ * Krylov products and the FP64 refinement residuals keep the FP32 / FP64 stencils, so the
+ * converged answer is unchanged.  32: the FP32 stencil everywhere. */
+int uwgpu_smoother_storage_set(uwgpu_ctx* ctx, int32_t bits);
+
 /* Newton form of the element matrices (the SLE's nlFormJacobian, 2D): with on != 0 the next
  * assemblies add the viscosity's derivatives with respect to the velocity gradient that yielding
  * laws (VON_MISES, DRUCKER_PRAGER) provide to the viscous term, as the 2D branch of

@@ -354,3 +354,31 @@ def test_bfbt_checkerboard_coarse_correction_cuts_inner_iterations(uw):
     for prec in (U.PREC_FP64, U.PREC_MIXED):
         assert out[(prec, 4)][0] < 0.75 * out[(prec, 0)][0]
         assert out[(prec, 4)][2] < 2 * out[(prec, 0)][2] + 1e-6
+
+
+def test_fp16_smoother_stencils_keep_the_mixed_solution(uw):
+    """The mixed form's V-cycle smooths (and forms its residuals) with FP16 row-scaled stencils by
+    default.  Against the FP32 stencils, on the benchmark's GRF field at 32^3: the same converged
+    solution (both to a full residual of 1e-6, checked against a tight FP64 solve) and about the
+    same number of V-cycles."""
+    from earthbyte_underworld_gb300 import workloads as W
+    U = uw
+    w = W.grf(nel=(32, 32, 32), ppc=8, grid=64, corr=0.1)
+    kw = dict(mg_levels=3, schur_type=1, schur_pc=3, scr_rtol=1e-6, a11_rtol=5e-7, back_rtol=5e-7, max_outer=400,
+              max_inner=2000, bfbt_rtol=1e-2, bfbt_max_it=5000, smoother=1, smooth_down=2, smooth_up=2)
+    ctx = U.Context(0)
+    W.setup_context(ctx, w)
+    ctx.bin_and_map(want=False)
+    ctx.assemble()
+    ref_u, ref_p, _ = ctx.solve_bsscr(U.default_opts(**dict(kw, scr_rtol=1e-9, a11_rtol=1e-10, back_rtol=1e-10)))
+    out = {}
+    for bits in (32, 16):
+        ctx.smoother_storage_set(bits)
+        u, p, r = ctx.solve_bsscr(U.default_opts(precision=U.PREC_MIXED, **kw))
+        assert r.rel_residual < 1e-6
+        out[bits] = (r.vcycles, _rel(u, ref_u), _rel(p, ref_p))
+    ctx.close()
+    print(f"\nFP32 stencils: {out[32][0]} V-cycles, u err {out[32][1]:.2e}; "
+          f"FP16 stencils: {out[16][0]} V-cycles, u err {out[16][1]:.2e}")
+    assert out[16][0] <= 1.1 * out[32][0] + 5
+    assert out[16][1] < 2 * out[32][1] + 1e-6 and out[16][2] < 2 * out[32][2] + 1e-5
