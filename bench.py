@@ -642,6 +642,7 @@ def kernel_rates(ctx, U, iters):
     nb = 27 if dim == 3 else 9
     peak, kind = measured_peaks()
     out = {}
+    ctx.smoother_storage_set(32)
     for name, prec, size in (("fp64", U.PREC_FP64, 8), ("fp32", U.PREC_MIXED, 4)):
         ctx.time_apply(prec, 3)
         ms = ctx.time_apply(prec, iters) / iters
@@ -666,6 +667,16 @@ def kernel_rates(ctx, U, iters):
                      "smooth2_ms": sms, "smooth2_GB_per_s": smooth_bytes / sms / 1e6,
                      "smooth2_frac_hbm": smooth_bytes / sms / 1e6 / peak,
                      "smooth2_fp_TFLOP_per_s": 2 * 2 * 2.0 * nn * (nb + 1) * dim * dim / sms / 1e9})
+    # the mixed form's default smoother storage: FP16 row-scaled stencils, neighbour pairs packed in
+    # 32-bit words (14 pair words per 3x3 block position in 3D), plus one FP32 row scale per row
+    ctx.smoother_storage_set(16)
+    ctx.time_chebyshev(U.PREC_MIXED, 2, 2)
+    nsteps = 2 * max(iters // 2, 2)
+    cms = ctx.time_chebyshev(U.PREC_MIXED, 2, nsteps // 2) / nsteps
+    cheb_bytes = nn * (((nb + 1) // 2) * dim * dim * 4 + dim * dim * 4 + 7 * dim * 4)
+    out["fp16_stencil"] = {"cheb_step_ms": cms, "cheb_step_GB_per_s": cheb_bytes / cms / 1e6,
+                           "cheb_step_frac_hbm": cheb_bytes / cms / 1e6 / peak, "cheb_step_bytes": cheb_bytes,
+                           "cheb_step_fp_TFLOP_per_s": 2.0 * nn * (nb + 1) * dim * dim / cms / 1e9}
     # the scaled BFBt inner operator (one value per element): the CG's direction kernel with p = z,
     # q = A z; algorithmic bytes: z read and p, q written, plus the 3^d stencil coefficients
     # (stencil forms) or the nodal W of about one node per element (matrix-free FP32 form).  The

@@ -96,8 +96,9 @@ struct Level {
     DArray<double> Dinv64;   // inverse of the node's diagonal block [r][c][node]
     DArray<float> Dinv32;
     // FP16 copy of the stencil for the mixed form's smoothing and V-cycle residuals: each row
-    // (r, node) divided by its largest magnitude S16[r][node] (IEEE half bits, same layout as A32)
-    DArray<uint16_t> A16;
+    // (r, node) divided by its largest magnitude S16[r][node]; IEEE half bits, the entries of
+    // neighbours 2p and 2p + 1 in one word [p][r][c][node]
+    DArray<uint32_t> A16;
     DArray<float> S16;
     bool has16 = false;
     DArray<uint8_t> fixed;   // per dof (node*dim+d), Dirichlet mask

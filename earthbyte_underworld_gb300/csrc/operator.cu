@@ -239,38 +239,54 @@ __device__ __forceinline__ T stencil_row_r(const Grid& g, int64_t n, int64_t i, 
     return out;
 }
 
-// The same row product from the FP16 row-scaled stencil (A16 = A / S16 per row), unscaled: the
-// caller multiplies by S16[r][n].  Loads in batches of 9 neighbours, as the FP32 form.
+// The same row product from the FP16 row-scaled stencil (A / S16 per row), unscaled: the caller
+// multiplies by S16[r][n].  The FP16 entries of neighbours q = 2p and 2p + 1 share one 32-bit word,
+// [p][r][c][node], so a load brings two entries and one conversion widens both.  Loads go out in
+// batches of five pairs.
 template <int DIM>
 __device__ __forceinline__ float stencil_row_h(const Grid& g, int64_t n, int64_t i, int64_t j, int64_t k, int r,
-                                               const uint16_t* __restrict__ A, const float* __restrict__ x) {
-    constexpr int NB = nblocks<DIM>();
-    constexpr int QB = 9;
+                                               const uint32_t* __restrict__ A, const float* __restrict__ x) {
+    constexpr int NB = nblocks<DIM>(), NP = (NB + 1) / 2, PB = 5;
     const NbrOffsets o = nbr_offsets<DIM>(g, i, j, k);
     float out = 0.f;
 #pragma unroll
-    for (int q0 = 0; q0 < NB; q0 += QB) {
-        unsigned short a[QB * DIM];
-        float xv[QB * DIM];
+    for (int p0 = 0; p0 < NP; p0 += PB) {
+        uint32_t w[PB * DIM];
+        float xv[2 * PB * DIM];
 #pragma unroll
-        for (int qq = 0; qq < QB; ++qq) {
-            const int q = q0 + qq;
-            const int64_t m = n + o.dx[q % 3] + o.dy[(q / 3) % 3] + o.dz[DIM == 3 ? q / 9 : 1];
+        for (int pp = 0; pp < PB; ++pp) {
+            const int pr = p0 + pp;
+            if (pr < NP) {
+                const int q0 = 2 * pr, q1 = 2 * pr + 1;
+                const int64_t m0 = n + o.dx[q0 % 3] + o.dy[(q0 / 3) % 3] + o.dz[DIM == 3 ? q0 / 9 : 1];
+                const int64_t m1 = q1 < NB ? n + o.dx[q1 % 3] + o.dy[(q1 / 3) % 3] + o.dz[DIM == 3 ? q1 / 9 : 1] : n;
 #pragma unroll
-            for (int cc = 0; cc < DIM; ++cc) {
-                a[qq * DIM + cc] = __ldg(A + ((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n);
-                xv[qq * DIM + cc] = x[(int64_t)cc * g.nn + m];
+                for (int cc = 0; cc < DIM; ++cc) {
+                    w[pp * DIM + cc] = __ldg(A + ((int64_t)(pr * DIM + r) * DIM + cc) * g.nn + n);
+                    xv[(2 * pp) * DIM + cc] = x[(int64_t)cc * g.nn + m0];
+                    xv[(2 * pp + 1) * DIM + cc] = q1 < NB ? x[(int64_t)cc * g.nn + m1] : 0.f;
+                }
             }
         }
 #pragma unroll
-        for (int t = 0; t < QB * DIM; ++t) out = fmaf(__half2float(__ushort_as_half(a[t])), xv[t], out);
+        for (int pp = 0; pp < PB; ++pp) {
+            if (p0 + pp < NP) {
+#pragma unroll
+                for (int cc = 0; cc < DIM; ++cc) {
+                    const uint32_t wv = w[pp * DIM + cc];
+                    const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&wv));
+                    out = fmaf(f.x, xv[(2 * pp) * DIM + cc], out);
+                    out = fmaf(f.y, xv[(2 * pp + 1) * DIM + cc], out);
+                }
+            }
+        }
     }
     return out;
 }
 
 // r = b - A x with the FP16 stencil (V-cycle residuals of the mixed form)
 template <int DIM>
-__global__ void __launch_bounds__(kRowThreads) k_residual_h(Grid g, const uint16_t* __restrict__ A,
+__global__ void __launch_bounds__(kRowThreads) k_residual_h(Grid g, const uint32_t* __restrict__ A,
                                                             const float* __restrict__ S, const float* __restrict__ x,
                                                             const float* __restrict__ b, float* __restrict__ y) {
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -283,11 +299,13 @@ __global__ void __launch_bounds__(kRowThreads) k_residual_h(Grid g, const uint16
     y[idx] = b[idx] - S[idx] * stencil_row_h<DIM>(g, n, i, j, k, r, A, x);
 }
 
-// FP32 -> FP16 row-scaled stencil: S16[r][n] = max over the row's entries of |A|, A16 = A / S16
+// FP32 -> FP16 row-scaled stencil: S16[r][n] = max over the row's entries of |A|; the entries of
+// A / S16 in FP16, neighbours 2p and 2p + 1 packed in word [p][r][c][n] (the last pair's upper half
+// zero when the neighbour count is odd)
 template <int DIM>
-__global__ void k_to_fp16_rows(Grid g, const float* __restrict__ A, uint16_t* __restrict__ A16,
+__global__ void k_to_fp16_rows(Grid g, const float* __restrict__ A, uint32_t* __restrict__ A16,
                                float* __restrict__ S16) {
-    constexpr int NB = nblocks<DIM>();
+    constexpr int NB = nblocks<DIM>(), NP = (NB + 1) / 2;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)DIM * g.nn) return;
     const int r = (int)(t / g.nn);
@@ -297,10 +315,13 @@ __global__ void k_to_fp16_rows(Grid g, const float* __restrict__ A, uint16_t* __
         for (int cc = 0; cc < DIM; ++cc) mx = fmaxf(mx, fabsf(A[((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n]));
     const float sc = mx > 0.f ? mx : 1.f, inv = 1.f / sc;
     S16[t] = sc;
-    for (int q = 0; q < NB; ++q)
+    for (int pr = 0; pr < NP; ++pr)
         for (int cc = 0; cc < DIM; ++cc) {
-            const int64_t o = ((int64_t)(q * DIM + r) * DIM + cc) * g.nn + n;
-            A16[o] = __half_as_ushort(__float2half_rn(A[o] * inv));
+            const int q0 = 2 * pr, q1 = 2 * pr + 1;
+            const float a0 = A[((int64_t)(q0 * DIM + r) * DIM + cc) * g.nn + n] * inv;
+            const float a1 = q1 < NB ? A[((int64_t)(q1 * DIM + r) * DIM + cc) * g.nn + n] * inv : 0.f;
+            const uint32_t lo = __half_as_ushort(__float2half_rn(a0)), hi = __half_as_ushort(__float2half_rn(a1));
+            A16[((int64_t)(pr * DIM + r) * DIM + cc) * g.nn + n] = lo | (hi << 16);
         }
 }
 
@@ -408,7 +429,7 @@ __global__ void __launch_bounds__(kRowThreads) k_cheb_step(Grid g, const T* __re
 
 // The Chebyshev step with the FP16 row-scaled stencil (mixed form)
 template <int DIM>
-__global__ void __launch_bounds__(kRowThreads) k_cheb_step_h(Grid g, const uint16_t* __restrict__ A,
+__global__ void __launch_bounds__(kRowThreads) k_cheb_step_h(Grid g, const uint32_t* __restrict__ A,
                                                              const float* __restrict__ S, const float* __restrict__ Dinv,
                                                              const float* __restrict__ b, const float* __restrict__ xin,
                                                              float* __restrict__ xout, float* __restrict__ d, float c1,
@@ -911,8 +932,8 @@ void build_operator(Context& c, int levels, bool need32) {
             to_fp32(c, L.Dinv64, L.Dinv32);
             {
                 const Grid g = grid_of(L.mesh);
-                const int nb = dim == 3 ? 27 : 9;
-                L.A16.ensure((size_t)nb * dim * dim * g.nn);
+                const int np = dim == 3 ? 14 : 5;   // neighbour pairs
+                L.A16.ensure((size_t)np * dim * dim * g.nn);
                 L.S16.ensure((size_t)dim * g.nn);
                 LaunchScope ls(c, -1);
                 if (dim == 3)
@@ -970,7 +991,7 @@ void level_residual(Context& c, const Level& L, const T* x, const T* b, T* r) {
     int D = g.dim, NB = D == 3 ? 27 : 9;
     if constexpr (std::is_same<T, float>::value) {
         if (L.has16 && c.smooth16) {
-            note_work(c, UWGPU_KERNEL_APPLY, (double)g.nn * (NB * D * D * 2 + 4 * D * 4), 2.0 * g.nn * NB * D * D);
+            note_work(c, UWGPU_KERNEL_APPLY, (double)g.nn * ((NB + 1) / 2 * D * D * 4 + 4 * D * 4), 2.0 * g.nn * NB * D * D);
             LaunchScope ls(c, UWGPU_KERNEL_APPLY);
             if (g.dim == 3)
                 k_residual_h<3><<<blocks_for(g.nn, kRowThreads / 3), kRowThreads, 0, c.stream>>>(g, L.A16.p, L.S16.p, x, b, r);
@@ -1082,7 +1103,7 @@ void level_cheb(Context& c, Level& L, const T* b, T* x, int degree, bool zero_in
     bool half = false;
     if constexpr (std::is_same<T, float>::value) half = L.has16 && c.smooth16;
     if (half)
-        note_work(c, UWGPU_KERNEL_SMOOTH, (double)degree * g.nn * (NB * D * D * 2 + (D * D + 6 * D) * 4),
+        note_work(c, UWGPU_KERNEL_SMOOTH, (double)degree * g.nn * ((NB + 1) / 2 * D * D * 4 + (D * D + 6 * D) * 4),
                   (double)degree * 2.0 * g.nn * (NB * D * D + D * D));
     else
         note_work(c, UWGPU_KERNEL_SMOOTH, (double)degree * g.nn * (NB * D * D + D * D + 5 * D) * sizeof(T),
