@@ -602,10 +602,10 @@ __global__ void k_galerkin(Grid gf, Grid gc, int64_t nef, int64_t nec, const dou
 }
 
 // 3D form of the same product through the 27-node patch of the eight children: the patch matrix
-// A (81 x 81, each entry gathered from the children that hold both of its nodes), then
+// A (81 x 81), the children's element matrices added into it child after child (the 576 entries
+// of one child land on distinct patch entries, so no two threads add to the same place), then
 // B = A P and K_E = P^T B with the trilinear prolongation P (81 x 24), whose weights are products
-// of 1 (fine node on the coarse node), 1/2 (fine node halfway) and 0 per axis.  About 20k FP64
-// operations per coarse element instead of about 100k for the per-child form above.
+// of 1 (fine node on the coarse node), 1/2 (fine node halfway) and 0 per axis.
 __device__ __forceinline__ double half_weight(int fine_pos, int coarse_bit) {
     const int d = fine_pos - 2 * coarse_bit;
     return d == 0 ? 1.0 : (d == 1 || d == -1) ? 0.5 : 0.0;
@@ -616,46 +616,32 @@ __global__ void __launch_bounds__(256) k_galerkin3(Grid gf, Grid gc, int64_t nef
                                                   double* __restrict__ Kc) {
     constexpr int ND = 24, NP = ND * (ND + 1) / 2, PN = 81;
     extern __shared__ double sm3[];
-    double* sK = sm3;                 // 8 children x 24 x 24 (reused for B: 81 x 24)
-    double* sA = sm3 + 8 * ND * ND;   // 81 x 81
+    double* sA = sm3;             // 81 x 81
+    double* sB = sm3 + PN * PN;   // 81 x 24
     const int64_t E = blockIdx.x;
     if (E >= nec) return;
     const int64_t EI = E % gc.ex, EJ = (E / gc.ex) % gc.ey, EK = E / ((int64_t)gc.ex * gc.ey);
-    for (int t = threadIdx.x; t < 8 * ND * ND; t += blockDim.x) {
-        const int ch = t / (ND * ND), rc = t % (ND * ND), R = rc / ND, C = rc % ND;
+    for (int t = threadIdx.x; t < PN * PN; t += blockDim.x) sA[t] = 0.0;
+    __syncthreads();
+    for (int ch = 0; ch < 8; ++ch) {
         const int cx = ch & 1, cy = (ch >> 1) & 1, cz = (ch >> 2) & 1;
         const int64_t fe = (2 * EI + cx) + (int64_t)gf.ex * ((2 * EJ + cy) + (int64_t)gf.ey * (2 * EK + cz));
-        const int la = R / 3, lb = C / 3;
         const int64_t fo = (2 * EI + cx) + gf.nx * ((2 * EJ + cy) + gf.ny * (2 * EK + cz));
-        const int64_t na = fo + (la & 1) + ((la >> 1) & 1) * gf.nx + ((la >> 2) & 1) * gf.nx * gf.ny;
-        const int64_t nb = fo + (lb & 1) + ((lb >> 1) & 1) * gf.nx + ((lb >> 2) & 1) * gf.nx * gf.ny;
-        const bool fx = fixf && (fixf[na * 3 + R % 3] || fixf[nb * 3 + C % 3]);
-        const int pi = R <= C ? packed_index(ND, R, C) : packed_index(ND, C, R);
-        sK[t] = fx ? 0.0 : Kf[(int64_t)pi * nef + fe];
-    }
-    __syncthreads();
-    // patch matrix: A[(n1, d1)][(n2, d2)] = sum over the children c holding n1 and n2
-    for (int t = threadIdx.x; t < PN * PN; t += blockDim.x) {
-        const int P = t / PN, Q = t % PN;
-        const int n1 = P / 3, d1 = P % 3, n2 = Q / 3, d2 = Q % 3;
-        const int x1 = n1 % 3, y1 = (n1 / 3) % 3, z1 = n1 / 9;
-        const int x2 = n2 % 3, y2 = (n2 / 3) % 3, z2 = n2 / 9;
-        double acc = 0.0;
-#pragma unroll
-        for (int ch = 0; ch < 8; ++ch) {
-            const int cx = ch & 1, cy = (ch >> 1) & 1, cz = (ch >> 2) & 1;
-            const int ax = x1 - cx, ay = y1 - cy, az = z1 - cz, bx = x2 - cx, by = y2 - cy, bz = z2 - cz;
-            if ((unsigned)ax <= 1u && (unsigned)ay <= 1u && (unsigned)az <= 1u && (unsigned)bx <= 1u &&
-                (unsigned)by <= 1u && (unsigned)bz <= 1u) {
-                const int la = ax + 2 * ay + 4 * az, lb = bx + 2 * by + 4 * bz;
-                acc += sK[ch * ND * ND + (la * 3 + d1) * ND + lb * 3 + d2];
-            }
+        for (int t = threadIdx.x; t < ND * ND; t += blockDim.x) {
+            const int R = t / ND, C = t % ND, la = R / 3, lb = C / 3;
+            const int64_t na = fo + (la & 1) + ((la >> 1) & 1) * gf.nx + ((la >> 2) & 1) * gf.nx * gf.ny;
+            const int64_t nb = fo + (lb & 1) + ((lb >> 1) & 1) * gf.nx + ((lb >> 2) & 1) * gf.nx * gf.ny;
+            const bool fx = fixf && (fixf[na * 3 + R % 3] || fixf[nb * 3 + C % 3]);
+            if (fx) continue;
+            const int pi = R <= C ? packed_index(ND, R, C) : packed_index(ND, C, R);
+            // patch nodes of the child's local nodes la, lb
+            const int pa = (cx + (la & 1)) + 3 * (cy + ((la >> 1) & 1)) + 9 * (cz + ((la >> 2) & 1));
+            const int pb = (cx + (lb & 1)) + 3 * (cy + ((lb >> 1) & 1)) + 9 * (cz + ((lb >> 2) & 1));
+            sA[(pa * 3 + R % 3) * PN + pb * 3 + C % 3] += Kf[(int64_t)pi * nef + fe];
         }
-        sA[t] = acc;
+        __syncthreads();
     }
-    __syncthreads();
-    // B = A P (81 x 24), into the children's buffer
-    double* sB = sK;
+    // B = A P (81 x 24)
     for (int t = threadIdx.x; t < PN * ND; t += blockDim.x) {
         const int P = t / ND, c = t % ND, C = c / 3, d = c % 3;
         const int X = C & 1, Y = (C >> 1) & 1, Z = (C >> 2) & 1;
@@ -898,7 +884,7 @@ void build_operator(Context& c, int levels, bool need32) {
             LaunchScope ls(c, -1);
             size_t smem = (size_t)(1 << dim) * nd * nd * sizeof(double);
             if (dim == 3) {
-                const size_t smem3 = (size_t)(8 * 24 * 24 + 81 * 81) * sizeof(double);
+                const size_t smem3 = (size_t)(81 * 81 + 81 * 24) * sizeof(double);
                 UWG_CUDA(cudaFuncSetAttribute(k_galerkin3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3));
                 k_galerkin3<<<(unsigned)C.mesh.ne, 256, smem3, c.stream>>>(gf, gc, F.mesh.ne, C.mesh.ne, F.Ke.p, F.fixed.p,
                                                                           C.Ke.p);
