@@ -710,10 +710,11 @@ __global__ void k_dense_from_stencil(Grid g, const double* __restrict__ A, doubl
 
 // Gauss-Jordan inverse, one launch per pivot k.  rr / cc hold the pivot row and column of step k
 // as they are before the step (unscaled); the step writes the row and column of pivot k + 1, as
-// they are after it, into the other pair of buffers.  A block covers kGjRows whole rows (the
-// reciprocal of the pivot is formed once per block), its threads striding along the columns, so
-// no thread divides.  In place, no pivoting: the coarse operator is SPD.
-constexpr int kGjRows = 4;
+// they are after it, into the other pair of buffers.  A block covers a tile of kGjRows rows x 256
+// columns: each thread owns one column of the tile and walks its rows (independent loads, coalesced
+// across the block), the tile's pivot-column entries and the reciprocal of the pivot sit in shared
+// memory, and no thread divides an index.  In place, no pivoting: the coarse operator is SPD.
+constexpr int kGjRows = 32;
 
 __global__ void k_gj_first(int64_t n, const double* __restrict__ M, double* __restrict__ rr, double* __restrict__ cc) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -727,24 +728,27 @@ __global__ void __launch_bounds__(256) k_gj_step(int64_t n, int64_t k, double* _
                                                  const double* __restrict__ rr, const double* __restrict__ cc,
                                                  double* __restrict__ rr_next, double* __restrict__ cc_next) {
     __shared__ double s_ip;
+    __shared__ double s_c[kGjRows];
+    const int64_t i0 = (int64_t)blockIdx.y * kGjRows;
     if (threadIdx.x == 0) s_ip = 1.0 / rr[k];
+    if (threadIdx.x < kGjRows) s_c[threadIdx.x] = i0 + threadIdx.x < n ? cc[i0 + threadIdx.x] : 0.0;
     __syncthreads();
     const double ip = s_ip;
-    const int64_t i0 = (int64_t)blockIdx.x * kGjRows;
-    for (int ri = 0; ri < kGjRows; ++ri) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double rj = j == k ? 1.0 : rr[j] * ip;   // the scaled pivot row (its pivot entry unused below)
+    const int rows = (int)(n - i0 < kGjRows ? n - i0 : kGjRows);
+#pragma unroll 8
+    for (int ri = 0; ri < rows; ++ri) {
         const int64_t i = i0 + ri;
-        if (i >= n) break;
-        const double ci = cc[i];
-        double* Mi = M + i * n;
-        for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
-            double v;
-            if (i == k) v = j == k ? ip : rr[j] * ip;
-            else if (j == k) v = -ci * ip;
-            else v = fma(-ci, rr[j] * ip, Mi[j]);
-            Mi[j] = v;
-            if (i == k + 1) rr_next[j] = v;
-            if (j == k + 1) cc_next[i] = v;
-        }
+        double* mij = M + i * n + j;
+        double v;
+        if (i == k) v = j == k ? ip : rj;
+        else if (j == k) v = -s_c[ri] * ip;
+        else v = fma(-s_c[ri], rj, *mij);
+        *mij = v;
+        if (i == k + 1) rr_next[j] = v;
+        if (j == k + 1) cc_next[i] = v;
     }
 }
 
@@ -797,7 +801,7 @@ void dense_inverse(Context& c, double* M, int64_t n) {
         LaunchScope ls(c, -1);
         k_gj_first<<<blocks_for(n, 256), 256, 0, c.stream>>>(n, M, rr[0], cc[0]);
     }
-    const unsigned grid = (unsigned)((n + kGjRows - 1) / kGjRows);
+    const dim3 grid((unsigned)((n + 255) / 256), (unsigned)((n + kGjRows - 1) / kGjRows));
     for (int64_t k = 0; k < n; ++k) {
         LaunchScope ls(c, -1);
         k_gj_step<<<grid, 256, 0, c.stream>>>(n, k, M, rr[k & 1], cc[k & 1], rr[(k + 1) & 1], cc[(k + 1) & 1]);
