@@ -622,22 +622,43 @@ __global__ void __launch_bounds__(256) k_galerkin3(Grid gf, Grid gc, int64_t nef
     if (E >= nec) return;
     const int64_t EI = E % gc.ex, EJ = (E / gc.ex) % gc.ey, EK = E / ((int64_t)gc.ex * gc.ey);
     for (int t = threadIdx.x; t < PN * PN; t += blockDim.x) sA[t] = 0.0;
-    __syncthreads();
+    // every entry this thread adds, of all eight children, loaded first (the loads of one block
+    // are then in flight together), then added child after child
+    constexpr int KT = (ND * ND + 255) / 256;   // entries per thread and child (256 threads)
+    double kv[8][KT];
+#pragma unroll
     for (int ch = 0; ch < 8; ++ch) {
         const int cx = ch & 1, cy = (ch >> 1) & 1, cz = (ch >> 2) & 1;
         const int64_t fe = (2 * EI + cx) + (int64_t)gf.ex * ((2 * EJ + cy) + (int64_t)gf.ey * (2 * EK + cz));
         const int64_t fo = (2 * EI + cx) + gf.nx * ((2 * EJ + cy) + gf.ny * (2 * EK + cz));
-        for (int t = threadIdx.x; t < ND * ND; t += blockDim.x) {
-            const int R = t / ND, C = t % ND, la = R / 3, lb = C / 3;
-            const int64_t na = fo + (la & 1) + ((la >> 1) & 1) * gf.nx + ((la >> 2) & 1) * gf.nx * gf.ny;
-            const int64_t nb = fo + (lb & 1) + ((lb >> 1) & 1) * gf.nx + ((lb >> 2) & 1) * gf.nx * gf.ny;
-            const bool fx = fixf && (fixf[na * 3 + R % 3] || fixf[nb * 3 + C % 3]);
-            if (fx) continue;
-            const int pi = R <= C ? packed_index(ND, R, C) : packed_index(ND, C, R);
-            // patch nodes of the child's local nodes la, lb
-            const int pa = (cx + (la & 1)) + 3 * (cy + ((la >> 1) & 1)) + 9 * (cz + ((la >> 2) & 1));
-            const int pb = (cx + (lb & 1)) + 3 * (cy + ((lb >> 1) & 1)) + 9 * (cz + ((lb >> 2) & 1));
-            sA[(pa * 3 + R % 3) * PN + pb * 3 + C % 3] += Kf[(int64_t)pi * nef + fe];
+#pragma unroll
+        for (int u = 0; u < KT; ++u) {
+            const int t = threadIdx.x + u * 256;
+            kv[ch][u] = 0.0;
+            if (t < ND * ND) {
+                const int R = t / ND, C = t % ND, la = R / 3, lb = C / 3;
+                const int64_t na = fo + (la & 1) + ((la >> 1) & 1) * gf.nx + ((la >> 2) & 1) * gf.nx * gf.ny;
+                const int64_t nb = fo + (lb & 1) + ((lb >> 1) & 1) * gf.nx + ((lb >> 2) & 1) * gf.nx * gf.ny;
+                const bool fx = fixf && (fixf[na * 3 + R % 3] || fixf[nb * 3 + C % 3]);
+                const int pi = R <= C ? packed_index(ND, R, C) : packed_index(ND, C, R);
+                if (!fx) kv[ch][u] = Kf[(int64_t)pi * nef + fe];
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ch = 0; ch < 8; ++ch) {
+        const int cx = ch & 1, cy = (ch >> 1) & 1, cz = (ch >> 2) & 1;
+#pragma unroll
+        for (int u = 0; u < KT; ++u) {
+            const int t = threadIdx.x + u * 256;
+            if (t < ND * ND) {
+                const int R = t / ND, C = t % ND, la = R / 3, lb = C / 3;
+                // patch nodes of the child's local nodes la, lb
+                const int pa = (cx + (la & 1)) + 3 * (cy + ((la >> 1) & 1)) + 9 * (cz + ((la >> 2) & 1));
+                const int pb = (cx + (lb & 1)) + 3 * (cy + ((lb >> 1) & 1)) + 9 * (cz + ((lb >> 2) & 1));
+                sA[(pa * 3 + R % 3) * PN + pb * 3 + C % 3] += kv[ch][u];
+            }
         }
         __syncthreads();
     }
