@@ -262,13 +262,13 @@ __global__ void __launch_bounds__(256) k_cg_spmv_dir(EGrid g, const T* __restric
 // so every access stays coalesced.
 constexpr int kEpt = 2;
 
-// iteration k, first kernel: alpha = rz_k / pq_k; x += alpha p; r -= alpha q; z = dinv r;
-// rz_{k+1} += r.z; and, when want_rr (the host's convergence check follows), rr_k += r.r.
-// Clears the slots of rz_{k+2} and pq_{k+1}.
+// iteration k, first kernel: alpha = rz_k / pq_k; x += alpha p (unless with_x is 0: the direction
+// kernel then updates x); r -= alpha q; z = dinv r; rz_{k+1} += r.z; and, when want_rr (the host's
+// convergence check follows), rr_k += r.r.  Clears the slots of rz_{k+2} and pq_{k+1}.
 template <typename T>
 __global__ void k_cg_update(int64_t ne, const T* __restrict__ p, const T* __restrict__ q,
                             const T* __restrict__ dinv, T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
-                            double* __restrict__ scal, int k, int want_rr) {
+                            double* __restrict__ scal, int k, int want_rr, int with_x) {
     __shared__ double sw[32];
     __shared__ T s_alpha;
     pdl_wait();
@@ -279,9 +279,9 @@ __global__ void k_cg_update(int64_t ne, const T* __restrict__ p, const T* __rest
     for (int m = 0; m < kEpt; ++m) {
         const int64_t e = base + (int64_t)m * blockDim.x;
         const bool in = e < ne;
-        pv[m] = in ? p[e] : (T)0;
+        pv[m] = in && with_x ? p[e] : (T)0;
         qv[m] = in ? q[e] : (T)0;
-        xv[m] = in ? x[e] : (T)0;
+        xv[m] = in && with_x ? x[e] : (T)0;
         rv[m] = in ? r[e] : (T)0;
         dv[m] = in ? dinv[e] : (T)0;
     }
@@ -291,7 +291,7 @@ __global__ void k_cg_update(int64_t ne, const T* __restrict__ p, const T* __rest
     for (int m = 0; m < kEpt; ++m) {
         const int64_t e = base + (int64_t)m * blockDim.x;
         if (e < ne) {
-            x[e] = fma(alpha, pv[m], xv[m]);
+            if (with_x) x[e] = fma(alpha, pv[m], xv[m]);
             T re = fma(-alpha, qv[m], rv[m]);
             r[e] = re;
             T ze = re * dv[m];
@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* 
     __shared__ float zb[3][HP];
     __shared__ float yb[2][3][NP];
     __shared__ double sw[32];
-    __shared__ float s_beta;
+    __shared__ float s_beta, s_alpha;
     const int ex = a.ex, ey = a.ey, ez = a.ez;
     const int ntx = (ex + kMfX - 1) / kMfX, nty = (ey + kMfY - 1) / kMfY;
     int bi = blockIdx.x;
@@ -603,12 +603,13 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
                                                                  const __grid_constant__ CUtensorMap tp,
                                                                  const __grid_constant__ CUtensorMap tq,
                                                                  float* __restrict__ p, float* __restrict__ q,
-                                                                 double* __restrict__ scal, int k, int first) {
+                                                                 float* __restrict__ x, double* __restrict__ scal, int k,
+                                                                 int first) {
     __shared__ __align__(128) unsigned char ring[kTmRing * kTmStage];
     __shared__ float yb[2][3][kTmNodes];
     __shared__ __align__(8) uint64_t bar[kTmRing];
     __shared__ double sw[32];
-    __shared__ float s_beta;
+    __shared__ float s_beta, s_alpha;
     const int ex = a.ex, ey = a.ey, ez = a.ez;
     const int ntx = (ex + kMfX - 1) / kMfX, nty = (ey + kMfY - 1) / kMfY;
     int bi = blockIdx.x;
@@ -646,7 +647,15 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
     int issued = 0;   // stages issued so far (thread 0)
     if (tid == 0)
         while (issued < nsteps && issued < kTmRing - 1) issue(issued++);
-    const float beta = first ? 0.f : block_ratio<float>(rz_slot(scal, k + 1), rz_slot(scal, k), &s_beta);
+    // x += alpha_k p_k here when x is given (the update kernel then leaves x alone): p_k is the p
+    // plane this kernel reads before it forms p_{k+1}
+    const bool xupd = x != nullptr && !first;
+    if (tid == 0) {
+        s_beta = first ? 0.f : (float)(*rz_slot(scal, k + 1) / *rz_slot(scal, k));
+        s_alpha = xupd ? (float)(*rz_slot(scal, k) / *pq_slot(scal, k)) : 0.f;
+    }
+    __syncthreads();
+    const float beta = s_beta, alpha = s_alpha;
     const bool eok = tid < kMfX * kMfY && x0 + tx < ex && y0 + ty < ey;
     const int eo = eok ? (x0 + tx) + ex * (y0 + ty) : 0;
     // this thread's node of the plane: (nx, ny) in the 33 x 9 node block
@@ -664,6 +673,7 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
     };
     float lo[3][4], hi[3][4];
     float local = 0.f;
+    float xn = 0.f;   // x of the element plane computed in the next step
     if (nsteps > 0) wait_slot(0);
     for (int t = 1; t < nsteps; ++t) {
         const int kk = zlo - 1 + t;
@@ -683,6 +693,8 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
             yc[kTmNodes + tid] = wc[kTwX * kTwY + wb_node] * dy;
             yc[2 * kTmNodes + tid] = wc[2 * kTwX * kTwY + wb_node] * dz;
         }
+        const float xc = xn;
+        xn = xupd && eok && kk < zhi ? x[(int64_t)kk * exy + eo] : 0.f;
         ok = __syncthreads_and(ok) != 0;
         if (!ok) break;
         // the next stage, t + kTmRing - 2, goes to the slot of stage t - 2, which every thread
@@ -712,6 +724,7 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
                 if (e < exy * ez) {
                     p[e] = pe;
                     q[e] = qe;
+                    if (xupd) x[e] = fmaf(alpha, pq_prev[tid], xc);
                 } else {
                     bad = true;
                 }
@@ -851,12 +864,17 @@ static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* Wc, const flo
     return L;
 }
 
+// whether mf_dir runs the TMA kernel for these vectors (it then also updates x when given one)
+static bool mf_tma(const MfLaunch& L, const float* z, const float* p, const float* q) {
+    return L.dim == 3 && L.tma && z == L.tma_z && p == L.tma_p && q == L.tma_q;
+}
+
 static void mf_dir(const MfLaunch& L, cudaStream_t st, const float* z, float* p, float* q, double* scal, int k,
-                   int first) {
+                   int first, float* x = nullptr) {
     const unsigned nt = kMfX * kMfY;
     if (L.dim == 2) launch_pdl(k_cg_mf2_dir, L.blocks, nt, st, L.ex, L.ey, L.nnx, L.nn, L.Wc, z, p, q, scal, k, first);
-    else if (L.tma && z == L.tma_z && p == L.tma_p && q == L.tma_q)
-        launch_pdl(k_cg_mf3_dir_tma, L.blocks, (unsigned)kTmThreads, st, L.a3, L.tz, L.tw, L.tp, L.tq, p, q, scal, k,
+    else if (mf_tma(L, z, p, q))
+        launch_pdl(k_cg_mf3_dir_tma, L.blocks, (unsigned)kTmThreads, st, L.a3, L.tz, L.tw, L.tp, L.tq, p, q, x, scal, k,
                    first);
     else launch_pdl(k_cg_mf3_dir, L.blocks, nt, st, L.a3, L.Wc, z, p, q, scal, k, first);
 }
@@ -1434,10 +1452,14 @@ static int gwg_cg_T(Context& c, const T* A, const float* Wmf, const T* dinv, con
     T* q = work + 3 * ne;
     const unsigned eb = blocks_for(ne, 256), ebv = blocks_for(ne, 256 * kEpt);
     // direction kernel of iteration k: p = z + beta p, q = A z + beta q, pq_{k+1}
+    // the TMA direction kernel also updates x (x += alpha p with the p it reads), so the update
+    // kernel then leaves x and p alone
+    bool fused_x = false;
+    if constexpr (std::is_same<T, float>::value) fused_x = Wmf && mf_tma(mf, z, p, q);
     auto dir = [&](int k, int first) {
         if constexpr (std::is_same<T, float>::value) {
             if (Wmf) {
-                mf_dir(mf, c.stream, z, p, q, scal, k, first);
+                mf_dir(mf, c.stream, z, p, q, scal, k, first, fused_x ? x : nullptr);
                 return;
             }
         }
@@ -1466,7 +1488,8 @@ static int gwg_cg_T(Context& c, const T* A, const float* Wmf, const T* dinv, con
     // graph per buffer set, replayed until converged; the host checks the residual once per replay.
     const int block = 12;
     auto issue = [&](int k) {
-        launch_pdl(k_cg_update<T>, ebv, 256, c.stream, ne, p, q, dinv, x, r, z, scal, k, (int)(k == block - 1));
+        launch_pdl(k_cg_update<T>, ebv, 256, c.stream, ne, p, q, dinv, x, r, z, scal, k, (int)(k == block - 1),
+                   (int)!fused_x);
         if (cc) cc_apply<T>(c, r, z, scal, k);
         dir(k, 0);
     };
