@@ -265,18 +265,22 @@ constexpr int kEpt = 2;
 // iteration k, first kernel: alpha = rz_k / pq_k; x += alpha p (unless with_x is 0: the direction
 // kernel then updates x); r -= alpha q; z = dinv r; rz_{k+1} += r.z; and, when want_rr (the host's
 // convergence check follows), rr_k += r.r.  Clears the slots of rz_{k+2} and pq_{k+1}.
+// k_cg_update: 512 threads x 4 elements per block, so that few blocks (1,024 at 128^3) add their
+// partial sums to the same two scalars (same-address atomics serialise in L2)
+constexpr int kUpdThreads = 512, kUpdEpt = 4;
+
 template <typename T>
-__global__ void k_cg_update(int64_t ne, const T* __restrict__ p, const T* __restrict__ q,
+__global__ void __launch_bounds__(kUpdThreads) k_cg_update(int64_t ne, const T* __restrict__ p, const T* __restrict__ q,
                             const T* __restrict__ dinv, T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
                             double* __restrict__ scal, int k, int want_rr, int with_x) {
     __shared__ double sw[32];
     __shared__ T s_alpha;
     pdl_wait();
     // the vectors first: their loads are in flight while thread 0 fetches the scalars for alpha
-    const int64_t base = (int64_t)blockIdx.x * blockDim.x * kEpt + threadIdx.x;
-    T pv[kEpt], qv[kEpt], xv[kEpt], rv[kEpt], dv[kEpt];
+    const int64_t base = (int64_t)blockIdx.x * blockDim.x * kUpdEpt + threadIdx.x;
+    T pv[kUpdEpt], qv[kUpdEpt], xv[kUpdEpt], rv[kUpdEpt], dv[kUpdEpt];
 #pragma unroll
-    for (int m = 0; m < kEpt; ++m) {
+    for (int m = 0; m < kUpdEpt; ++m) {
         const int64_t e = base + (int64_t)m * blockDim.x;
         const bool in = e < ne;
         pv[m] = in && with_x ? p[e] : (T)0;
@@ -288,7 +292,7 @@ __global__ void k_cg_update(int64_t ne, const T* __restrict__ p, const T* __rest
     const T alpha = block_ratio<T>(rz_slot(scal, k), pq_slot(scal, k), &s_alpha);
     T rz = (T)0, rr = (T)0;
 #pragma unroll
-    for (int m = 0; m < kEpt; ++m) {
+    for (int m = 0; m < kUpdEpt; ++m) {
         const int64_t e = base + (int64_t)m * blockDim.x;
         if (e < ne) {
             if (with_x) x[e] = fma(alpha, pv[m], xv[m]);
@@ -1488,8 +1492,8 @@ static int gwg_cg_T(Context& c, const T* A, const float* Wmf, const T* dinv, con
     // graph per buffer set, replayed until converged; the host checks the residual once per replay.
     const int block = 12;
     auto issue = [&](int k) {
-        launch_pdl(k_cg_update<T>, ebv, 256, c.stream, ne, p, q, dinv, x, r, z, scal, k, (int)(k == block - 1),
-                   (int)!fused_x);
+        launch_pdl(k_cg_update<T>, blocks_for(ne, kUpdThreads * kUpdEpt), (unsigned)kUpdThreads, c.stream, ne, p, q, dinv,
+                   x, r, z, scal, k, (int)(k == block - 1), (int)!fused_x);
         if (cc) cc_apply<T>(c, r, z, scal, k);
         dir(k, 0);
     };
