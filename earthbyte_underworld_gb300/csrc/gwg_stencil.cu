@@ -662,9 +662,12 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
     const float beta = s_beta, alpha = s_alpha;
     const bool eok = tid < kMfX * kMfY && x0 + tx < ex && y0 + ty < ey;
     const int eo = eok ? (x0 + tx) + ex * (y0 + ty) : 0;
-    // this thread's node of the plane: (nx, ny) in the 33 x 9 node block
+    // this thread's node of the plane, (nx, ny) in the 33 x 9 node block: warp w < 9 takes nodes
+    // 0..31 of row w (32 consecutive words of the staged planes, no bank conflict), and nine
+    // threads of the tenth warp take node 32 of every row
     const bool node = tid < kTmNodes;
-    const int nx = tid % (kMfX + 1), ny = tid / (kMfX + 1);
+    const int nx = tid < 9 * kMfX ? tid % kMfX : kMfX, ny = tid < 9 * kMfX ? tid / kMfX : tid - 9 * kMfX;
+    const int node_i = ny * (kMfX + 1) + nx;      // its index in the node-plane buffers
     const int zb_node = ny * kTzX + nx + 3;       // its lower-left element in the staged halo plane
     const int wb_node = ny * kTwX + nx;
     const int zb_elem = (ty + 1) * kTzX + tx + 4;  // this thread's element in the staged halo plane
@@ -679,12 +682,20 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
     float local = 0.f;
     float xn = 0.f;   // x of the element plane computed in the next step
     if (nsteps > 0) wait_slot(0);
-    for (int t = 1; t < nsteps; ++t) {
+    // element offsets fit 32 bits (mf_launch takes this kernel only below 2^32 elements)
+    const uint32_t exy32 = (uint32_t)exy, emax = (uint32_t)(exy * ez);
+    uint32_t e_prev = (uint32_t)(zlo - 1) * exy32 + (uint32_t)eo;   // this thread's element in plane kk - 1
+    int s_cur = 0, s_prev = 0;                        // ring slots of stages t and t - 1
+    for (int t = 1; t < nsteps; ++t, e_prev += exy32) {
         const int kk = zlo - 1 + t;
-        wait_slot(t % kTmRing);
-        const float* zp = reinterpret_cast<const float*>(ring + ((t - 1) % kTmRing) * kTmStage);   // element plane kk - 1
-        const float* zc = reinterpret_cast<const float*>(ring + (t % kTmRing) * kTmStage);         // element plane kk
-        const float* wc = reinterpret_cast<const float*>(ring + (t % kTmRing) * kTmStage + kTzSlot);
+        s_prev = s_cur;
+        s_cur = s_cur + 1 == kTmRing ? 0 : s_cur + 1;
+        wait_slot(s_cur);
+        const unsigned char* st_prev = ring + s_prev * kTmStage;
+        const unsigned char* st_cur = ring + s_cur * kTmStage;
+        const float* zp = reinterpret_cast<const float*>(st_prev);            // element plane kk - 1
+        const float* zc = reinterpret_cast<const float*>(st_cur);             // element plane kk
+        const float* wc = reinterpret_cast<const float*>(st_cur + kTzSlot);
         float* yc = yb[t & 1][0];
         if (node) {
             const int b = zb_node;
@@ -693,12 +704,12 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
             const float dx = (z100 - z000) + (z110 - z010) + (z101 - z001) + (z111 - z011);
             const float dy = (z010 - z000) + (z110 - z100) + (z011 - z001) + (z111 - z101);
             const float dz = (z001 - z000) + (z101 - z100) + (z011 - z010) + (z111 - z110);
-            yc[tid] = wc[wb_node] * dx;
-            yc[kTmNodes + tid] = wc[kTwX * kTwY + wb_node] * dy;
-            yc[2 * kTmNodes + tid] = wc[2 * kTwX * kTwY + wb_node] * dz;
+            yc[node_i] = wc[wb_node] * dx;
+            yc[kTmNodes + node_i] = wc[kTwX * kTwY + wb_node] * dy;
+            yc[2 * kTmNodes + node_i] = wc[2 * kTwX * kTwY + wb_node] * dz;
         }
         const float xc = xn;
-        xn = xupd && eok && kk < zhi ? x[(int64_t)kk * exy + eo] : 0.f;
+        xn = xupd && eok && kk < zhi ? x[e_prev + exy32] : 0.f;
         ok = __syncthreads_and(ok) != 0;
         if (!ok) break;
         // the next stage, t + kTmRing - 2, goes to the slot of stage t - 2, which every thread
@@ -719,13 +730,13 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
                     out += (c4 >> 1) ? -(lo[1][c4] + hi[1][c4]) : (lo[1][c4] + hi[1][c4]);
                     out += lo[2][c4] - hi[2][c4];
                 }
-                const int64_t e = (int64_t)(kk - 1) * exy + eo;
+                const uint32_t e = e_prev;
                 const float ze = zp[zb_elem];
                 // p and q of element plane kk - 1 arrived with stage t - 1 (the slot of zp)
-                const float* pq_prev = reinterpret_cast<const float*>(ring + ((t - 1) % kTmRing) * kTmStage + kTzSlot + kTwSlot);
+                const float* pq_prev = reinterpret_cast<const float*>(st_prev + kTzSlot + kTwSlot);
                 const float pe = first ? ze : fmaf(beta, pq_prev[tid], ze);
                 const float qe = first ? out : fmaf(beta, pq_prev[kMfX * kMfY + tid], out);
-                if (e < exy * ez) {
+                if (e < emax) {
                     p[e] = pe;
                     q[e] = qe;
                     if (xupd) x[e] = fmaf(alpha, pq_prev[tid], xc);
@@ -834,7 +845,7 @@ static MfLaunch mf_launch(const MeshDesc& m, EGrid g, const float* Wc, const flo
     L.tma = false;
     auto enc = tensor_map_encoder();
     auto al16 = [](const void* v) { return v && (reinterpret_cast<uintptr_t>(v) & 15) == 0; };
-    if (enc && g.ex % 4 == 0 && al16(z) && al16(Wc) && al16(p) && al16(q)) {
+    if (enc && g.ex % 4 == 0 && g.ne < ((int64_t)1 << 32) && al16(z) && al16(Wc) && al16(p) && al16(q)) {
         const cuuint64_t zdim[3] = {(cuuint64_t)g.ex, (cuuint64_t)g.ey, (cuuint64_t)g.ez};
         const cuuint64_t zstr[2] = {(cuuint64_t)g.ex * 4, (cuuint64_t)g.ex * g.ey * 4};
         const cuuint32_t zbox[3] = {(cuuint32_t)kTzX, (cuuint32_t)kTzY, 1};
