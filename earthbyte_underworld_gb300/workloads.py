@@ -11,6 +11,7 @@ Workloads:
   spheres  3D 64^3, 27 points/element on a jittered 3x3x3 grid, 50 seeded spheres
   grf      3D 128^3, 30 uniform points/element, log10(viscosity) a Gaussian random field
   layers   3D 96^3, 40 points/element, Arrhenius + Drucker-Prager + limiter (nonlinear)
+  solcx    2D analytic-solution case of the reference's performance tests (viscosity jump)
 """
 from __future__ import annotations
 
@@ -79,6 +80,31 @@ def rt2d(nel=(64, 64), ppc=20, seed=13):
     return dict(name="rt2d", dim=2, nel=tuple(nel), x=x, y=y, z=None, material=mat, eta=None, rho=None,
                 materials=mats, fixed=U.free_slip_mask(2, nel), gravity=1.0, vert_axis=1, seed=seed,
                 mg_levels=4)
+
+
+def solcx(n=64, ppc=20, seed=13, eta_a=100.0, eta_b=1.0, xc=0.5, ky=2.0):
+    """2D solCx (Underworld/SysTest/PerformanceTests/testVelicSolCx.xml): viscosity eta_a left of
+    x = xc and eta_b right of it, a nodal temperature T = sin(ky pi y) cos(pi x) (VelicTemperatureIC,
+    StgFEM/plugins/StandardConditionFunctions/StandardConditionFunctions.c:1298-1338) driving the
+    buoyancy as rho = -T (density 1e-12 with expansivity 1e12 about T = 0, so rho = 1e-12 - T), g = 1;
+    free-slip walls; ppc points per element on the Park-Miller layout of the reference's test."""
+    E = n * n
+    r = park_miller_stream(seed, E * ppc * 3).reshape(E, ppc, 3)
+    ex = np.arange(E) % n
+    ey = np.arange(E) // n
+    x0, x1 = _node_coord(ex, n), _node_coord(ex + 1, n)
+    y0, y1 = _node_coord(ey, n), _node_coord(ey + 1, n)
+    x = ((x1 - x0)[:, None] * r[:, :, 0] / float(PM_M) + x0[:, None]).reshape(-1)
+    y = ((y1 - y0)[:, None] * r[:, :, 1] / float(PM_M) + y0[:, None]).reshape(-1)
+    mat = np.where(x < xc, 0, 1).astype(np.int32)
+    mats = [U.make_material([(U.LAW_MATERIAL_VISCOSITY, [eta_a])], density=1e-12, alpha=1e12, ref_temp=0.0),
+            U.make_material([(U.LAW_MATERIAL_VISCOSITY, [eta_b])], density=1e-12, alpha=1e12, ref_temp=0.0)]
+    k = np.arange((n + 1) ** 2)
+    xn, yn = _node_coord(k % (n + 1), n), _node_coord(k // (n + 1), n)
+    temp = np.sin(ky * np.pi * yn) * np.cos(np.pi * xn)
+    return dict(name="solcx", dim=2, nel=(n, n), x=x, y=y, z=None, material=mat, eta=None, rho=None,
+                materials=mats, fixed=U.free_slip_mask(2, (n, n)), gravity=1.0, vert_axis=1, seed=seed,
+                temperature=temp, mg_levels=3)
 
 
 def spheres(nel=(64, 64, 64), nspheres=50, seed=2024, jitter=0.15, shuffle=True):

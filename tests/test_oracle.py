@@ -190,3 +190,37 @@ def test_oracle_refuses_meshes_that_do_not_coarsen(oracle):
     Ke = np.tile(np.eye(8), (E, 1, 1))
     with pytest.raises(ValueError):
         O.solve_bsscr(m, fixed, Ke, np.zeros((E, 8)), np.zeros((E, 8)), np.ones(E), mg_levels=2)
+
+
+def test_oracle_solcx_convergence_rates_match_reference(oracle):
+    """The oracle's particle-in-cell Stokes solve of the solCx problem (viscosity jump 100 : 1 at
+    x = 0.5, the reference's Underworld/SysTest/PerformanceTests/testVelicSolCx.xml: 20 points per
+    element on the Park-Miller layout, PCDVC population control and DVC weights at resolution 10)
+    at 16^2, 32^2, 64^2: the L2 errors against the analytic solution (the reference's own analytic
+    plugin, fixture tests/golden/solcx_golden.npz) converge at the rates the reference's expected
+    results state (velocity 1.99 / 1.99, pressure 1.00, PerformanceTests/expected/
+    Underworld_Velic_solCx-analysis.cvg-convergence-rates.dat)."""
+    from earthbyte_underworld_gb300 import workloads as W
+    import solcx_norms as SN
+    O = oracle
+    g = SN.golden()
+    ns = (16, 32, 64)
+    errs = []
+    for n in ns:
+        w = W.solcx(n)
+        m = O.make_mesh(2, w["nel"])
+        pts = np.stack([w["x"], w["y"], np.zeros_like(w["x"])], axis=1)
+        _, off, perm, xi, _ = O.map_points(m, pts)
+        X, M, S, off2, perm2, xo, wo = O.pcdvc(m, (10, 10), pts, w["material"], off, perm, xi, max_deletions=3,
+                                             max_splits=3)
+        mats = [O.make_material([(mm.laws[i].law, list(mm.laws[i].p)) for i in range(mm.n_laws)],
+                                density=mm.density, alpha=mm.alpha, ref_temp=mm.ref_temp) for mm in w["materials"]]
+        f = O.make_fields(temperature=w["temperature"], gravity=1.0, vert_axis=1)
+        Ke, fe, Ge, Se, _ = O.assemble(m, off2, perm2, xo, M, mats, f, weights=wo)
+        u, p, rep = O.solve_bsscr(m, w["fixed"], Ke, Ge, fe, Se, mg_levels=3, schur_type=1, schur_pc=3,
+                                  scr_rtol=1e-10, a11_rtol=1e-12, back_rtol=1e-12, bfbt_rtol=1e-8, bfbt_max_it=5000)
+        errs.append(SN.errors(n, u, p, g))
+    errs = np.array(errs)
+    r = SN.rates(errs, ns)
+    print("\nsolCx L2 errors", errs.tolist(), "rates", r.tolist())
+    assert np.all(np.abs(r - g["expected_rates"]) < 0.1), r
