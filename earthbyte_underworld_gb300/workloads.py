@@ -12,6 +12,7 @@ Workloads:
   grf      3D 128^3, 30 uniform points/element, log10(viscosity) a Gaussian random field
   layers   3D 96^3, 40 points/element, Arrhenius + Drucker-Prager + limiter (nonlinear)
   solcx    2D analytic-solution case of the reference's performance tests (viscosity jump)
+  solkz    2D analytic-solution case of the reference's performance tests (exponential viscosity)
 """
 from __future__ import annotations
 
@@ -105,6 +106,19 @@ def solcx(n=64, ppc=20, seed=13, eta_a=100.0, eta_b=1.0, xc=0.5, ky=2.0):
     return dict(name="solcx", dim=2, nel=(n, n), x=x, y=y, z=None, material=mat, eta=None, rho=None,
                 materials=mats, fixed=U.free_slip_mask(2, (n, n)), gravity=1.0, vert_axis=1, seed=seed,
                 temperature=temp, mg_levels=3)
+
+
+def solkz(n=64, ppc=20, seed=13, twice_b=2.0, km_waves=1.0):
+    """2D solKz (Underworld/SysTest/PerformanceTests/testVelicSolKz.xml): viscosity exp(twice_b y)
+    (DepthDependentViscosity along y, eta0 1, reference point 0), temperature
+    T = sin(km_waves pi y) cos(pi x) driving the buoyancy as rho = -T, g = 1; free-slip walls; ppc
+    points per element on the Park-Miller layout."""
+    w = solcx(n, ppc, seed, ky=km_waves)
+    law = [(U.LAW_DEPTH_DEPENDENT, [1.0, twice_b, 0.0, 1.0])]
+    w["materials"] = [U.make_material(law, density=1e-12, alpha=1e12, ref_temp=0.0)]
+    w["material"] = np.zeros_like(w["material"])
+    w["name"] = "solkz"
+    return w
 
 
 def spheres(nel=(64, 64, 64), nspheres=50, seed=2024, jitter=0.15, shuffle=True):

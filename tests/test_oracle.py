@@ -192,22 +192,24 @@ def test_oracle_refuses_meshes_that_do_not_coarsen(oracle):
         O.solve_bsscr(m, fixed, Ke, np.zeros((E, 8)), np.zeros((E, 8)), np.ones(E), mg_levels=2)
 
 
-def test_oracle_solcx_convergence_rates_match_reference(oracle):
-    """The oracle's particle-in-cell Stokes solve of the solCx problem (viscosity jump 100 : 1 at
-    x = 0.5, the reference's Underworld/SysTest/PerformanceTests/testVelicSolCx.xml: 20 points per
-    element on the Park-Miller layout, PCDVC population control and DVC weights at resolution 10)
-    at 16^2, 32^2, 64^2: the L2 errors against the analytic solution (the reference's own analytic
-    plugin, fixture tests/golden/solcx_golden.npz) converge at the rates the reference's expected
-    results state (velocity 1.99 / 1.99, pressure 1.00, PerformanceTests/expected/
-    Underworld_Velic_solCx-analysis.cvg-convergence-rates.dat)."""
+@pytest.mark.parametrize("case", ["cx", "kz"])
+def test_oracle_velic_convergence_rates_match_reference(oracle, case):
+    """The oracle's particle-in-cell Stokes solve of the reference's analytic-solution tests
+    (Underworld/SysTest/PerformanceTests/testVelicSolCx.xml: viscosity jump 100 : 1 at x = 0.5;
+    testVelicSolKz.xml: viscosity exp(2 y)), with 20 points per element on the Park-Miller layout,
+    PCDVC population control and DVC weights at resolution 10, at 16^2, 32^2, 64^2: the L2 errors
+    against the analytic solutions (the reference's own analytic plugins, fixture
+    tests/golden/velic_golden.npz) converge at the rates the reference's expected results state
+    (PerformanceTests/expected/Underworld_Velic_sol{Cx,Kz}-analysis.cvg-convergence-rates.dat:
+    velocity 1.99 / 1.99 and 2.00 / 2.00, pressure 1.00)."""
     from earthbyte_underworld_gb300 import workloads as W
-    import solcx_norms as SN
+    import velic_norms as VN
     O = oracle
-    g = SN.golden()
+    g = VN.golden()
     ns = (16, 32, 64)
     errs = []
     for n in ns:
-        w = W.solcx(n)
+        w = W.solcx(n) if case == "cx" else W.solkz(n)
         m = O.make_mesh(2, w["nel"])
         pts = np.stack([w["x"], w["y"], np.zeros_like(w["x"])], axis=1)
         _, off, perm, xi, _ = O.map_points(m, pts)
@@ -219,8 +221,8 @@ def test_oracle_solcx_convergence_rates_match_reference(oracle):
         Ke, fe, Ge, Se, _ = O.assemble(m, off2, perm2, xo, M, mats, f, weights=wo)
         u, p, rep = O.solve_bsscr(m, w["fixed"], Ke, Ge, fe, Se, mg_levels=3, schur_type=1, schur_pc=3,
                                   scr_rtol=1e-10, a11_rtol=1e-12, back_rtol=1e-12, bfbt_rtol=1e-8, bfbt_max_it=5000)
-        errs.append(SN.errors(n, u, p, g))
+        errs.append(VN.errors(case, n, u, p, g))
     errs = np.array(errs)
-    r = SN.rates(errs, ns)
-    print("\nsolCx L2 errors", errs.tolist(), "rates", r.tolist())
-    assert np.all(np.abs(r - g["expected_rates"]) < 0.1), r
+    r = VN.rates(errs, ns)
+    print(f"\nsol{case}: L2 errors", errs.tolist(), "rates", r.tolist())
+    assert np.all(np.abs(r - g[f"{case}_expected_rates"]) < 0.1), r

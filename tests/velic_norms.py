@@ -1,11 +1,11 @@
-"""L2 error norms of a Q1-P0 solution against the solCx analytic solution (the norms the reference's
-FieldTest integrates with its 2 x 2 Gauss swarm: Underworld/SysTest/PerformanceTests/testVelicSolCx.xml),
-from the fixture tests/golden/solcx_golden.npz, and the convergence rates of the three norms."""
+"""L2 error norms of a Q1-P0 solution against the analytic solutions of the reference's performance
+tests (solCx, solKz: the norms its FieldTest integrates with a 2 x 2 Gauss swarm), from the fixture
+tests/golden/velic_golden.npz, and the convergence rates of the three norms."""
 import os
 
 import numpy as np
 
-GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "solcx_golden.npz")
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "velic_golden.npz")
 G = (1.0 - 1.0 / np.sqrt(3.0)) / 2.0
 LOC = [(G, G), (1 - G, G), (G, 1 - G), (1 - G, 1 - G)]
 
@@ -14,11 +14,11 @@ def golden():
     return np.load(GOLDEN)
 
 
-def errors(n, u, p, g):
+def errors(case, n, u, p, g):
     """u: nodal velocity (nn, 2) (node = i + (n + 1) j), p: element pressures (n^2); -> L2 errors of
     vx, vy and p (pressure compared after removing each field's integrated mean)."""
-    ug = g[f"ug_{n}"].astype(np.float64).reshape(n * n, 4, 2)
-    pg = g[f"pg_{n}"].astype(np.float64).reshape(n * n, 4)
+    ug = g[f"{case}_ug_{n}"].astype(np.float64).reshape(n * n, 4, 2)
+    pg = g[f"{case}_pg_{n}"].astype(np.float64).reshape(n * n, 4)
     e = np.arange(n * n)
     i, j = e % n, e // n
     n00, n10 = i + (n + 1) * j, i + 1 + (n + 1) * j
