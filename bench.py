@@ -53,7 +53,7 @@ def parse():
                     help="skip the other precision form")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
-    ap.add_argument("--mode", default="step", choices=["step", "kernels", "bfbt"],
+    ap.add_argument("--mode", default="step", choices=["step", "kernels", "bfbt", "accuracy"],
                     help="step: the full hot-path step; kernels: operator apply and smoother only")
     ap.add_argument("--iters", type=int, default=20, help="launches per kernel in --mode kernels")
     ap.add_argument("--cpu-nel", type=int, default=20, help="mesh of the CPU baseline sample")
@@ -754,6 +754,57 @@ def run_bfbt(args):
     return 0
 
 
+def run_accuracy(args):
+    """Accuracy at equal cost: a converged FP64 solve of the workload (Schur 1e-10, velocity 1e-11)
+    is the reference; the mixed and FP64 forms are then solved on a ladder of tolerances (Schur,
+    velocity), each timed once after a warm-up, with the relative L2 distance of u and p from the
+    reference.  For each form the first rung whose velocity is within 1e-6 of the reference gives
+    its time at that accuracy; the line states both and their ratio."""
+    import numpy as np
+    import torch
+
+    from earthbyte_underworld_gb300 import uwgpu as U
+    from earthbyte_underworld_gb300 import workloads as W
+    nel = args.nel or default_nel(args.workload)
+    w = make_workload(args.workload, nel)
+    kw = solve_kw(w)
+    ctx = U.Context(0)
+    W.setup_context(ctx, w)
+    ctx.bin_and_map(want=False)
+    ctx.assemble()
+    t0 = time.perf_counter()
+    ref_opts = U.default_opts(precision=U.PREC_FP64, **dict(kw, scr_rtol=1e-10, a11_rtol=1e-11, back_rtol=1e-11,
+                                                           max_outer=2000, max_inner=20000))
+    ur, pr, rr = ctx.solve_bsscr(ref_opts)
+    t_ref = time.perf_counter() - t0
+    ladder = [(1e-6, 5e-7), (1e-7, 5e-8), (3e-8, 1.5e-8), (1e-8, 5e-9)]
+    out = {"mode": "accuracy", "workload": workload_name(args.workload, nel), "target_u_rel": 1e-6,
+           "reference": {"rel_residual": rr.rel_residual, "outer_its": rr.outer_its, "s": t_ref}, "forms": {}}
+    ctx.solve_bsscr(U.default_opts(precision=U.PREC_MIXED, **kw))   # warm-up
+    for name, prec in (("mixed", U.PREC_MIXED), ("fp64", U.PREC_FP64)):
+        rows = []
+        for scr, a11 in ladder:
+            o = U.default_opts(precision=prec, **dict(kw, scr_rtol=scr, a11_rtol=a11, back_rtol=a11 / 5,
+                                                      max_outer=2000, max_inner=20000))
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            u, p, r = ctx.solve_bsscr(o)
+            dt = time.perf_counter() - t1
+            rows.append({"scr_rtol": scr, "a11_rtol": a11, "s": dt, "rel_residual": r.rel_residual,
+                         "outer_its": r.outer_its,
+                         "u_rel": float(np.linalg.norm(u - ur) / np.linalg.norm(ur)),
+                         "p_rel": float(np.linalg.norm(p - pr) / np.linalg.norm(pr))})
+            if rows[-1]["u_rel"] <= 1e-6:
+                break
+        hit = [r for r in rows if r["u_rel"] <= 1e-6]
+        out["forms"][name] = {"ladder": rows, "s_at_target": hit[0]["s"] if hit else None}
+    m, f = out["forms"]["mixed"]["s_at_target"], out["forms"]["fp64"]["s_at_target"]
+    out["speedup_at_equal_accuracy"] = f / m if m and f else None
+    print(json.dumps(out), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -762,6 +813,8 @@ def main():
         return run_bfbt(args)
     if args.mode == "kernels":
         return run_kernels(args)
+    if args.mode == "accuracy":
+        return run_accuracy(args)
     return run_ours(args)
 
 
