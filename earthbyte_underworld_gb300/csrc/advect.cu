@@ -171,13 +171,10 @@ void advect_particles(Context& c, double dt, int order, bool fallback, uint32_t&
     if (counters[0] > 0)
         throw Error(UWGPU_ERR_DOMAIN, std::to_string(counters[0]) +
                                           " material points have no velocity (outside the mesh); the swarm is unchanged");
-    std::swap(c.px.p, c.qx.p);
-    std::swap(c.px.n, c.qx.n);
-    std::swap(c.py.p, c.qy.p);
-    std::swap(c.py.n, c.qy.n);
+    c.px.swap(c.qx);
+    c.py.swap(c.qy);
     if (md.dim == 3) {
-        std::swap(c.pz.p, c.qz.p);
-        std::swap(c.pz.n, c.qz.n);
+        c.pz.swap(c.qz);
     }
     c.mapped = false;   // ownership changes: the next bin_and_map rebuilds the cell tables
     fell_back = counters[1];

@@ -18,6 +18,12 @@ namespace {
 template <typename F>
 int guarded(uwgpu_ctx* ctx, F&& fn) {
     if (!ctx) return UWGPU_ERR_ARGUMENT;
+    // device arrays of this call come from the pool on the context's stream
+    struct AllocStream {
+        cudaStream_t saved;
+        explicit AllocStream(cudaStream_t s) : saved(uwg::alloc_stream()) { uwg::alloc_stream() = s; }
+        ~AllocStream() { uwg::alloc_stream() = saved; }
+    } as(ctx->c.stream);
     try {
         cudaSetDevice(ctx->c.device);
         fn(ctx->c);
@@ -52,6 +58,17 @@ int uwgpu_create(int32_t device, uwgpu_ctx** out) {
     if (device < 0 || device >= ndev) return UWGPU_ERR_ARGUMENT;
     uwgpu_ctx* ctx = new uwgpu_ctx();
     ctx->c.device = device;
+    // freed device arrays stay in this process's pool of the device (reused by the next solve)
+    {
+        cudaMemPool_t pool;
+        if (cudaSetDevice(device) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess)
+                (void)cudaGetLastError();
+        } else {
+            (void)cudaGetLastError();
+        }
+    }
     if (cudaSetDevice(device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMallocHost(&ctx->c.host_scalars, 1024 * sizeof(double)) != cudaSuccess) {

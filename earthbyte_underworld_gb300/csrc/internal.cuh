@@ -44,25 +44,60 @@ struct Error : std::runtime_error {
     } while (0)
 
 // Owning device array (cudaMalloc / cudaFree), grown on demand, never shrunk.
+// The stream of the API call in progress on this thread (the C entry points set it): device arrays
+// are taken from and returned to the device's stream-ordered memory pool on it, whose release
+// threshold keeps freed memory in the pool, so the work buffers of a solve cost no cudaMalloc or
+// cudaFree after the first solve.  Outside an API call arrays use plain cudaMalloc.
+inline cudaStream_t& alloc_stream() {
+    static thread_local cudaStream_t s = nullptr;
+    return s;
+}
+
 template <typename T>
 struct DArray {
     T* p = nullptr;
     size_t n = 0;
+    cudaStream_t s = nullptr;   // stream it was allocated on (pooled arrays)
+    bool pooled = false;
     DArray() = default;
     DArray(const DArray&) = delete;
     DArray& operator=(const DArray&) = delete;
     ~DArray() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            // a pooled array goes back to the pool in stream order; if its stream is gone the
+            // synchronous free is the fallback
+            if (!pooled || cudaFreeAsync(p, s) != cudaSuccess) {
+                (void)cudaGetLastError();
+                cudaFree(p);
+            }
+        }
         p = nullptr;
         n = 0;
+        pooled = false;
     }
     void ensure(size_t count) {
         if (count <= n && p) return;
         release();
         if (count == 0) count = 1;
-        UWG_CUDA(cudaMalloc(&p, count * sizeof(T)));
+        cudaStream_t st = alloc_stream();
+        if (st) {
+            UWG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p), count * sizeof(T), st));
+            // the allocation completes before any stream (and synchronous copies) may use it
+            UWG_CUDA(cudaStreamSynchronize(st));
+            s = st;
+            pooled = true;
+        } else {
+            UWG_CUDA(cudaMalloc(&p, count * sizeof(T)));
+        }
         n = count;
+    }
+    // exchanges the storage of two arrays (every field)
+    void swap(DArray& o) {
+        std::swap(p, o.p);
+        std::swap(n, o.n);
+        std::swap(s, o.s);
+        std::swap(pooled, o.pooled);
     }
     T* get() const { return p; }
 };

@@ -393,27 +393,20 @@ int64_t population_control(Context& c, const uwgpu_pcdvc_opts& o) {
     }
     check_launch("k_pc_gather");
     UWG_CUDA(cudaStreamSynchronize(c.stream));
-    std::swap(c.px.p, nx.p);
-    std::swap(c.px.n, nx.n);
-    std::swap(c.py.p, ny.p);
-    std::swap(c.py.n, ny.n);
+    c.px.swap(nx);
+    c.py.swap(ny);
     if (dim == 3) {
-        std::swap(c.pz.p, nz.p);
-        std::swap(c.pz.n, nz.n);
+        c.pz.swap(nz);
     }
-    std::swap(c.pmat.p, nmat.p);
-    std::swap(c.pmat.n, nmat.n);
+    c.pmat.swap(nmat);
     if (c.has_peta) {
-        std::swap(c.peta.p, neta.p);
-        std::swap(c.peta.n, neta.n);
+        c.peta.swap(neta);
     }
     if (c.has_prho) {
-        std::swap(c.prho.p, nrho.p);
-        std::swap(c.prho.n, nrho.n);
+        c.prho.swap(nrho);
     }
     if (c.has_pfw) {
-        std::swap(c.pfw.p, npfw.p);
-        std::swap(c.pfw.n, npfw.n);
+        c.pfw.swap(npfw);
         c.pfw_incr.ensure(N);
         UWG_CUDA(cudaMemsetAsync(c.pfw_incr.p, 0, N * sizeof(double), c.stream));
     }
