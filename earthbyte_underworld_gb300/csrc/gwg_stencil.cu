@@ -678,7 +678,7 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
         ok = tc::mbar_wait(&bar[slot], (phase_bits >> slot) & 1u, 1u << 22) && ok;
         phase_bits ^= 1u << slot;
     };
-    float lo[3][4], hi[3][4];
+    float la[3][4], lb[3][4];   // the node values of two node planes, used in turn as lower and upper
     float local = 0.f;
     float xn = 0.f;   // x of the element plane computed in the next step
     if (nsteps > 0) wait_slot(0);
@@ -686,7 +686,9 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
     const uint32_t exy32 = (uint32_t)exy, emax = (uint32_t)(exy * ez);
     uint32_t e_prev = (uint32_t)(zlo - 1) * exy32 + (uint32_t)eo;   // this thread's element in plane kk - 1
     int s_cur = 0, s_prev = 0;                        // ring slots of stages t and t - 1
-    for (int t = 1; t < nsteps; ++t, e_prev += exy32) {
+    // one z step; lo holds node plane kk - 1 on entry, hi receives node plane kk (the two register
+    // sets swap roles from step to step, so no values are copied)
+    auto step = [&](int t, float (&lo)[3][4], float (&hi)[3][4]) -> bool {
         const int kk = zlo - 1 + t;
         s_prev = s_cur;
         s_cur = s_cur + 1 == kTmRing ? 0 : s_cur + 1;
@@ -711,7 +713,7 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
         const float xc = xn;
         xn = xupd && eok && kk < zhi ? x[e_prev + exy32] : 0.f;
         ok = __syncthreads_and(ok) != 0;
-        if (!ok) break;
+        if (!ok) return false;
         // the next stage, t + kTmRing - 2, goes to the slot of stage t - 2, which every thread
         // finished reading before this barrier
         if (tid == 0 && issued < nsteps) issue(issued++);
@@ -745,11 +747,13 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
                 }
                 local = fmaf(pe, qe, local);
             }
-#pragma unroll
-            for (int c4 = 0; c4 < 4; ++c4)
-#pragma unroll
-                for (int d = 0; d < 3; ++d) lo[d][c4] = hi[d][c4];
         }
+        e_prev += exy32;
+        return true;
+    };
+    for (int t = 1; t < nsteps; t += 2) {
+        if (!step(t, la, lb)) break;
+        if (t + 1 < nsteps && !step(t + 1, lb, la)) break;
     }
     if (bad) local = __int_as_float(0x7fc00000);
     if (!ok) {
