@@ -565,15 +565,16 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* 
 
 // The same direction update with every plane it reads staged by the tensor memory accelerator
 // (cp.async.bulk.tensor), for element grids whose x extent is a multiple of 4 (so that every z row
-// starts on 16 bytes).  Per z step one thread issues the copies of one stage into a ring of three:
+// starts on 16 bytes).  Per z step one thread issues the copies of one stage into a ring of five:
 // the element plane of z with its halo, as a 40 x 10 box from x0 - 4 (x aligned down to 16 bytes;
 // coordinates outside the grid, the halo at the mesh boundary and the planes below and above the
 // mesh, read as zero), the 36 x 9 x 3 box of the node plane's three weight components, and (after
 // the first iteration) the tile's 32 x 8 plane of p and of q.  The copies complete on the stage's
-// mbarrier.  Ten warps: one thread per node of the 33 x 9 node plane, then one per element of the
-// 32 x 8 tile; one block barrier per step.  A copy that has not arrived after a bounded wait makes
+// mbarrier.  Six warps: a thread forms two nodes of the 33 x 9 node plane (rows 2i and 2i + 1, one
+// column; the element rows they share are summed once), then two elements of the 32 x 8 tile (rows
+// 2j and 2j + 1; the node rows they share are combined once); one block barrier per step.  A copy that has not arrived after a bounded wait makes
 // the block report NaN in the iteration's p.q, which ends the inner solve with UWGPU_ERR_NAN.
-constexpr int kTmThreads = 320;
+constexpr int kTmThreads = 192;
 constexpr int kTzX = kMfX + 8, kTzY = kMfY + 2;     // staged element plane: 40 x 10
 constexpr int kTwX = kMfX + 4, kTwY = kMfY + 1;     // staged weight plane: 36 x 9, three components
 constexpr int kTzBytes = kTzX * kTzY * 4, kTwBytes = 3 * kTwX * kTwY * 4, kTpBytes = kMfX * kMfY * 4;
@@ -623,7 +624,7 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
     bi /= nty;
     const int zlo = bi * a.zc, zhi = min(zlo + a.zc, ez);
     const int nsteps = zhi - zlo + 2;   // stages: planes zlo - 1 .. zhi
-    const int tid = threadIdx.x, tx = tid % kMfX, ty = tid / kMfX;
+    const int tid = threadIdx.x;
     const int64_t exy = (int64_t)ex * ey;
     if (tid == 0) {
         for (int i = 0; i < kTmRing; ++i) tc::mbar_init(&bar[i], 1);
@@ -660,35 +661,40 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
     }
     __syncthreads();
     const float beta = s_beta, alpha = s_alpha;
-    const bool eok = tid < kMfX * kMfY && x0 + tx < ex && y0 + ty < ey;
-    const int eo = eok ? (x0 + tx) + ex * (y0 + ty) : 0;
-    // this thread's node of the plane, (nx, ny) in the 33 x 9 node block: warp w < 9 takes nodes
-    // 0..31 of row w (32 consecutive words of the staged planes, no bank conflict), and nine
-    // threads of the tenth warp take node 32 of every row
-    const bool node = tid < kTmNodes;
-    const int nx = tid < 9 * kMfX ? tid % kMfX : kMfX, ny = tid < 9 * kMfX ? tid / kMfX : tid - 9 * kMfX;
-    const int node_i = ny * (kMfX + 1) + nx;      // its index in the node-plane buffers
-    const int zb_node = ny * kTzX + nx + 3;       // its lower-left element in the staged halo plane
-    const int wb_node = ny * kTwX + nx;
-    const int zb_elem = (ty + 1) * kTzX + tx + 4;  // this thread's element in the staged halo plane
-    const int ybase = ty * (kMfX + 1) + tx;
+    // element role (threads 0..127): elements (tx, ty0) and (tx, ty0 + 1) of the 32 x 8 tile
+    const bool elem = tid < kMfX * kMfY / 2;
+    const int tx = tid % kMfX, ty0 = 2 * (tid / kMfX);
+    const bool eok0 = elem && x0 + tx < ex && y0 + ty0 < ey;
+    const bool eok1 = elem && x0 + tx < ex && y0 + ty0 + 1 < ey;
+    const int eo = eok0 ? (x0 + tx) + ex * (y0 + ty0) : 0;   // element (tx, ty0); (tx, ty0 + 1) is ex further
+    const int ybase = ty0 * (kMfX + 1) + tx;   // node (tx, ty0) in the node-plane buffers
+    // node role (threads 0..164): nodes (nx, ny0) and (nx, ny0 + 1) of the 33 x 9 node block; warp
+    // w < 5 takes columns 0..31 of row pair w, threads 160..164 column 32 of each pair; the last
+    // pair (rows 8, 9) has only row 8
+    const bool node = tid < 5 * kMfX + 5;
+    const int nx = tid < 5 * kMfX ? tid % kMfX : kMfX;
+    const int ny0 = 2 * (tid < 5 * kMfX ? tid / kMfX : tid - 5 * kMfX);
+    const bool pair = ny0 + 1 <= kMfY;
+    const int node_i = ny0 * (kMfX + 1) + nx;    // index of (nx, ny0) in the node-plane buffers
+    const int zb_node = ny0 * kTzX + nx + 3;     // its lower-left element in the staged halo plane
+    const int wb_node = ny0 * kTwX + nx;
     bool ok = true, bad = false;
     uint32_t phase_bits = 0;   // parity of the next wait, per slot
     auto wait_slot = [&](int slot) {
         ok = tc::mbar_wait(&bar[slot], (phase_bits >> slot) & 1u, 1u << 22) && ok;
         phase_bits ^= 1u << slot;
     };
-    float la[3][4], lb[3][4];   // the node values of two node planes, used in turn as lower and upper
+    // node values of two node planes ([d][row 0..2][column 0..1] around the thread's elements),
+    // used in turn as lower and upper
+    float la[3][3][2], lb[3][3][2];
     float local = 0.f;
-    float xn = 0.f;   // x of the element plane computed in the next step
+    float xn0 = 0.f, xn1 = 0.f;   // x of the two elements of the plane computed in the next step
     if (nsteps > 0) wait_slot(0);
     // element offsets fit 32 bits (mf_launch takes this kernel only below 2^32 elements)
-    const uint32_t exy32 = (uint32_t)exy, emax = (uint32_t)(exy * ez);
-    uint32_t e_prev = (uint32_t)(zlo - 1) * exy32 + (uint32_t)eo;   // this thread's element in plane kk - 1
+    const uint32_t exy32 = (uint32_t)exy, emax = (uint32_t)(exy * ez), ex32 = (uint32_t)ex;
+    uint32_t e_prev = (uint32_t)(zlo - 1) * exy32 + (uint32_t)eo;   // element (tx, ty0) in plane kk - 1
     int s_cur = 0, s_prev = 0;                        // ring slots of stages t and t - 1
-    // one z step; lo holds node plane kk - 1 on entry, hi receives node plane kk (the two register
-    // sets swap roles from step to step, so no values are copied)
-    auto step = [&](int t, float (&lo)[3][4], float (&hi)[3][4]) -> bool {
+    auto step = [&](int t, float (&lo)[3][3][2], float (&hi)[3][3][2]) -> bool {
         const int kk = zlo - 1 + t;
         s_prev = s_cur;
         s_cur = s_cur + 1 == kTmRing ? 0 : s_cur + 1;
@@ -700,52 +706,79 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
         const float* wc = reinterpret_cast<const float*>(st_cur + kTzSlot);
         float* yc = yb[t & 1][0];
         if (node) {
-            const int b = zb_node;
-            const float z000 = zp[b], z100 = zp[b + 1], z010 = zp[b + kTzX], z110 = zp[b + kTzX + 1];
-            const float z001 = zc[b], z101 = zc[b + 1], z011 = zc[b + kTzX], z111 = zc[b + kTzX + 1];
-            const float dx = (z100 - z000) + (z110 - z010) + (z101 - z001) + (z111 - z011);
-            const float dy = (z010 - z000) + (z110 - z100) + (z011 - z001) + (z111 - z101);
-            const float dz = (z001 - z000) + (z101 - z100) + (z011 - z010) + (z111 - z110);
-            yc[node_i] = wc[wb_node] * dx;
-            yc[kTmNodes + node_i] = wc[kTwX * kTwY + wb_node] * dy;
-            yc[2 * kTmNodes + node_i] = wc[2 * kTwX * kTwY + wb_node] * dz;
+            // per staged element row r around the nodes: with A = plane kk - 1, B = plane kk, and
+            // columns nx - 1 (0) and nx (1): sx = (A1 - A0) + (B1 - B0), sz = (B0 - A0) + (B1 - A1),
+            // ss = A0 + A1 + B0 + B1.  A node between rows r and r + 1 has
+            // D_x = sx(r) + sx(r+1), D_y = ss(r+1) - ss(r), D_z = sz(r) + sz(r+1).
+            float sx[3], sz[3], ss[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                if (r < 2 || pair) {
+                    const int b = zb_node + r * kTzX;
+                    const float a0 = zp[b], a1 = zp[b + 1], b0 = zc[b], b1 = zc[b + 1];
+                    sx[r] = (a1 - a0) + (b1 - b0);
+                    sz[r] = (b0 - a0) + (b1 - a1);
+                    ss[r] = (a0 + a1) + (b0 + b1);
+                } else {
+                    sx[r] = sz[r] = ss[r] = 0.f;
+                }
+            }
+            yc[node_i] = wc[wb_node] * (sx[0] + sx[1]);
+            yc[kTmNodes + node_i] = wc[kTwX * kTwY + wb_node] * (ss[1] - ss[0]);
+            yc[2 * kTmNodes + node_i] = wc[2 * kTwX * kTwY + wb_node] * (sz[0] + sz[1]);
+            if (pair) {
+                yc[node_i + kMfX + 1] = wc[wb_node + kTwX] * (sx[1] + sx[2]);
+                yc[kTmNodes + node_i + kMfX + 1] = wc[kTwX * kTwY + wb_node + kTwX] * (ss[2] - ss[1]);
+                yc[2 * kTmNodes + node_i + kMfX + 1] = wc[2 * kTwX * kTwY + wb_node + kTwX] * (sz[1] + sz[2]);
+            }
         }
-        const float xc = xn;
-        xn = xupd && eok && kk < zhi ? x[e_prev + exy32] : 0.f;
+        const float xc0 = xn0, xc1 = xn1;
+        xn0 = xupd && eok0 && kk < zhi ? x[e_prev + exy32] : 0.f;
+        xn1 = xupd && eok1 && kk < zhi ? x[e_prev + exy32 + ex32] : 0.f;
         ok = __syncthreads_and(ok) != 0;
         if (!ok) return false;
         // the next stage, t + kTmRing - 2, goes to the slot of stage t - 2, which every thread
         // finished reading before this barrier
         if (tid == 0 && issued < nsteps) issue(issued++);
-        if (tid < kMfX * kMfY) {
+        if (elem) {
 #pragma unroll
-            for (int c4 = 0; c4 < 4; ++c4) {
-                const int ni = ybase + (c4 >> 1) * (kMfX + 1) + (c4 & 1);
+            for (int r = 0; r < 3; ++r)
 #pragma unroll
-                for (int d = 0; d < 3; ++d) hi[d][c4] = yc[d * kTmNodes + ni];
-            }
-            if (t >= 2 && eok) {
-                float out = 0.f;
+                for (int c = 0; c < 2; ++c)
 #pragma unroll
-                for (int c4 = 0; c4 < 4; ++c4) {
-                    out += (c4 & 1) ? -(lo[0][c4] + hi[0][c4]) : (lo[0][c4] + hi[0][c4]);
-                    out += (c4 >> 1) ? -(lo[1][c4] + hi[1][c4]) : (lo[1][c4] + hi[1][c4]);
-                    out += lo[2][c4] - hi[2][c4];
+                    for (int d = 0; d < 3; ++d) hi[d][r][c] = yc[d * kTmNodes + ybase + r * (kMfX + 1) + c];
+            if (t >= 2 && eok0) {
+                // per node row r: X = u0(r, 0) - u0(r, 1), S1 = u1(r, 0) + u1(r, 1),
+                // S2 = u2(r, 0) + u2(r, 1) with u0 = lo0 + hi0, u1 = lo1 + hi1, u2 = lo2 - hi2; the
+                // element between rows r and r + 1 gets X(r) + X(r+1) + S1(r) - S1(r+1) + S2(r) + S2(r+1)
+                float X[3], S1[3], S2[3];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    X[r] = (lo[0][r][0] + hi[0][r][0]) - (lo[0][r][1] + hi[0][r][1]);
+                    S1[r] = (lo[1][r][0] + hi[1][r][0]) + (lo[1][r][1] + hi[1][r][1]);
+                    S2[r] = (lo[2][r][0] - hi[2][r][0]) + (lo[2][r][1] - hi[2][r][1]);
                 }
-                const uint32_t e = e_prev;
-                const float ze = zp[zb_elem];
-                // p and q of element plane kk - 1 arrived with stage t - 1 (the slot of zp)
                 const float* pq_prev = reinterpret_cast<const float*>(st_prev + kTzSlot + kTwSlot);
-                const float pe = first ? ze : fmaf(beta, pq_prev[tid], ze);
-                const float qe = first ? out : fmaf(beta, pq_prev[kMfX * kMfY + tid], out);
-                if (e < emax) {
-                    p[e] = pe;
-                    q[e] = qe;
-                    if (xupd) x[e] = fmaf(alpha, pq_prev[tid], xc);
-                } else {
-                    bad = true;
+                const int lt = ty0 * kMfX + tx;   // element (tx, ty0) in the tile's p, q planes
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (h == 1 && !eok1) break;
+                    const float out = (X[h] + X[h + 1]) + (S1[h] - S1[h + 1]) + (S2[h] + S2[h + 1]);
+                    const uint32_t e = e_prev + (h ? ex32 : 0u);
+                    const float ze = zp[(ty0 + h + 1) * kTzX + tx + 4];
+                    // p and q of element plane kk - 1 arrived with stage t - 1 (the slot of zp)
+                    const float pv = pq_prev[lt + h * kMfX], qv = pq_prev[kMfX * kMfY + lt + h * kMfX];
+                    const float pe = first ? ze : fmaf(beta, pv, ze);
+                    const float qe = first ? out : fmaf(beta, qv, out);
+                    if (e < emax) {
+                        p[e] = pe;
+                        q[e] = qe;
+                        if (xupd) x[e] = fmaf(alpha, pv, h ? xc1 : xc0);
+                    } else {
+                        bad = true;
+                    }
+                    local = fmaf(pe, qe, local);
                 }
-                local = fmaf(pe, qe, local);
             }
         }
         e_prev += exy32;
