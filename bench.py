@@ -601,7 +601,7 @@ MEASURED_TRAFFIC = {
     ("cheb_step", "fp64"): (588.15e6, 65 ** 3),
     ("apply", "fp64"): (539.1e6, 65 ** 3),
     ("apply", "fp32"): (275.66e6, 65 ** 3),
-    ("bfbt_dir", "fp32_matrix_free"): (34.87e6, 128 ** 3),   # k_cg_mf3_dir_tma, profiles/bfbt_mf_tma_fp32_grf128.md
+    ("bfbt_dir", "fp32_matrix_free"): (34.80e6, 128 ** 3),   # k_cg_mf3_dir_tma, profiles/bfbt_mf_tma_fp32_grf128.md
 }
 FINE_KERNEL = {"smooth": ("cheb_step", "k_cheb_step<3,{t}> (one Chebyshev step, fine level)"),
                "apply": ("apply", "k_apply<3,{t}> (fine level)"),
@@ -627,7 +627,8 @@ def fine_roofline(dom, prec, rates, nel, peak, peak_kind, family):
             "fp_tflops": r[key + "_fp_TFLOP_per_s"],
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
             "traffic_source": "ncu capture (profiles/), scaled by nodes / elements" if traffic is not None else None,
-            "note": ("the matrix-free kernel is bound by instruction issue (ncu: 75% issue active, DRAM 17%); it "
+            "note": ("the matrix-free kernel is bound by instruction issue and latency (ncu: 59% issue active at 24 warps "
+                     "per SM, DRAM 18%); it "
                      "replaces an HBM-bound stencil kernel that moves five times the bytes"
                      if r.get("bfbt_form") == "fp32_matrix_free" and key == "bfbt_dir" else
                      "FP64 kernels on this part are also bounded by its 1.2 TFLOP/s FP64 rate (fp_tflops)"),
