@@ -572,7 +572,10 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* 
 // the first iteration) the tile's 32 x 8 plane of p and of q.  The copies complete on the stage's
 // mbarrier.  Six warps: a thread forms two nodes of the 33 x 9 node plane (rows 2i and 2i + 1, one
 // column; the element rows they share are summed once), then two elements of the 32 x 8 tile (rows
-// 2j and 2j + 1; the node rows they share are combined once); one block barrier per step.  A copy that has not arrived after a bounded wait makes
+// 2j and 2j + 1; the node rows they share are combined once); one block barrier per step.  The
+// arithmetic runs on FP32 pairs where the values come in twos (the two planes of a staged element
+// row, the two columns of a node row, the two nodes or two elements of a thread): one packed add,
+// multiply or fma (__fadd2_rn, __fmul2_rn, __ffma2_rn) does the work of two scalar ones.  A copy that has not arrived after a bounded wait makes
 // the block report NaN in the iteration's p.q, which ends the inner solve with UWGPU_ERR_NAN.
 constexpr int kTmThreads = 192;
 constexpr int kTzX = kMfX + 8, kTzY = kMfY + 2;     // staged element plane: 40 x 10
@@ -684,17 +687,18 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
         ok = tc::mbar_wait(&bar[slot], (phase_bits >> slot) & 1u, 1u << 22) && ok;
         phase_bits ^= 1u << slot;
     };
-    // node values of two node planes ([d][row 0..2][column 0..1] around the thread's elements),
-    // used in turn as lower and upper
-    float la[3][3][2], lb[3][3][2];
-    float local = 0.f;
-    float xn0 = 0.f, xn1 = 0.f;   // x of the two elements of the plane computed in the next step
+    // node values of two node planes ([d][row 0..2] around the thread's elements, the two columns
+    // as one pair), used in turn as lower and upper
+    float2 la[3][3], lb[3][3];
+    float2 local2 = make_float2(0.f, 0.f);
+    float2 xn = make_float2(0.f, 0.f);   // x of the two elements of the plane computed in the next step
+    const float2 beta2 = make_float2(beta, beta), alpha2 = make_float2(alpha, alpha);
     if (nsteps > 0) wait_slot(0);
     // element offsets fit 32 bits (mf_launch takes this kernel only below 2^32 elements)
     const uint32_t exy32 = (uint32_t)exy, emax = (uint32_t)(exy * ez), ex32 = (uint32_t)ex;
     uint32_t e_prev = (uint32_t)(zlo - 1) * exy32 + (uint32_t)eo;   // element (tx, ty0) in plane kk - 1
     int s_cur = 0, s_prev = 0;                        // ring slots of stages t and t - 1
-    auto step = [&](int t, float (&lo)[3][3][2], float (&hi)[3][3][2]) -> bool {
+    auto step = [&](int t, float2 (&lo)[3][3], float2 (&hi)[3][3]) -> bool {
         const int kk = zlo - 1 + t;
         s_prev = s_cur;
         s_cur = s_cur + 1 == kTmRing ? 0 : s_cur + 1;
@@ -706,35 +710,48 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
         const float* wc = reinterpret_cast<const float*>(st_cur + kTzSlot);
         float* yc = yb[t & 1][0];
         if (node) {
-            // per staged element row r around the nodes: with A = plane kk - 1, B = plane kk, and
-            // columns nx - 1 (0) and nx (1): sx = (A1 - A0) + (B1 - B0), sz = (B0 - A0) + (B1 - A1),
-            // ss = A0 + A1 + B0 + B1.  A node between rows r and r + 1 has
+            // per staged element row r around the nodes, with A = plane kk - 1, B = plane kk and
+            // columns nx - 1 (0) and nx (1), the pairs (A0, B0) and (A1, B1) give
+            // d = (A1 - A0, B1 - B0) and s = (A0 + A1, B0 + B1), and from them sx = dA + dB,
+            // ss = sA + sB, sz = sB - sA.  A node between rows r and r + 1 has
             // D_x = sx(r) + sx(r+1), D_y = ss(r+1) - ss(r), D_z = sz(r) + sz(r+1).
             float sx[3], sz[3], ss[3];
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
                 if (r < 2 || pair) {
                     const int b = zb_node + r * kTzX;
-                    const float a0 = zp[b], a1 = zp[b + 1], b0 = zc[b], b1 = zc[b + 1];
-                    sx[r] = (a1 - a0) + (b1 - b0);
-                    sz[r] = (b0 - a0) + (b1 - a1);
-                    ss[r] = (a0 + a1) + (b0 + b1);
+                    const float2 c0 = make_float2(zp[b], zc[b]), c1 = make_float2(zp[b + 1], zc[b + 1]);
+                    const float2 d = __ffma2_rn(c0, make_float2(-1.f, -1.f), c1);
+                    const float2 sm = __fadd2_rn(c0, c1);
+                    sx[r] = d.x + d.y;
+                    sz[r] = sm.y - sm.x;
+                    ss[r] = sm.x + sm.y;
                 } else {
                     sx[r] = sz[r] = ss[r] = 0.f;
                 }
             }
-            yc[node_i] = wc[wb_node] * (sx[0] + sx[1]);
-            yc[kTmNodes + node_i] = wc[kTwX * kTwY + wb_node] * (ss[1] - ss[0]);
-            yc[2 * kTmNodes + node_i] = wc[2 * kTwX * kTwY + wb_node] * (sz[0] + sz[1]);
+            // the two nodes as one pair: (ny0, ny0 + 1)
+            const int w1 = pair ? kTwX : 0;
+            const float2 yx = __fmul2_rn(make_float2(wc[wb_node], wc[wb_node + w1]),
+                                         make_float2(sx[0] + sx[1], sx[1] + sx[2]));
+            const float2 yy = __fmul2_rn(make_float2(wc[kTwX * kTwY + wb_node], wc[kTwX * kTwY + wb_node + w1]),
+                                         make_float2(ss[1] - ss[0], ss[2] - ss[1]));
+            const float2 yz = __fmul2_rn(make_float2(wc[2 * kTwX * kTwY + wb_node], wc[2 * kTwX * kTwY + wb_node + w1]),
+                                         make_float2(sz[0] + sz[1], sz[1] + sz[2]));
+            yc[node_i] = yx.x;
+            yc[kTmNodes + node_i] = yy.x;
+            yc[2 * kTmNodes + node_i] = yz.x;
             if (pair) {
-                yc[node_i + kMfX + 1] = wc[wb_node + kTwX] * (sx[1] + sx[2]);
-                yc[kTmNodes + node_i + kMfX + 1] = wc[kTwX * kTwY + wb_node + kTwX] * (ss[2] - ss[1]);
-                yc[2 * kTmNodes + node_i + kMfX + 1] = wc[2 * kTwX * kTwY + wb_node + kTwX] * (sz[1] + sz[2]);
+                yc[node_i + kMfX + 1] = yx.y;
+                yc[kTmNodes + node_i + kMfX + 1] = yy.y;
+                yc[2 * kTmNodes + node_i + kMfX + 1] = yz.y;
             }
         }
-        const float xc0 = xn0, xc1 = xn1;
-        xn0 = xupd && eok0 && kk < zhi ? x[e_prev + exy32] : 0.f;
-        xn1 = xupd && eok1 && kk < zhi ? x[e_prev + exy32 + ex32] : 0.f;
+        const float2 xc = xn;
+        if (xupd && eok0 && kk < zhi) {
+            xn.x = x[e_prev + exy32];
+            xn.y = eok1 ? x[e_prev + exy32 + ex32] : 0.f;
+        }
         ok = __syncthreads_and(ok) != 0;
         if (!ok) return false;
         // the next stage, t + kTmRing - 2, goes to the slot of stage t - 2, which every thread
@@ -744,41 +761,52 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
 #pragma unroll
             for (int r = 0; r < 3; ++r)
 #pragma unroll
-                for (int c = 0; c < 2; ++c)
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) hi[d][r][c] = yc[d * kTmNodes + ybase + r * (kMfX + 1) + c];
+                for (int d = 0; d < 3; ++d) {
+                    const float* yr = yc + d * kTmNodes + ybase + r * (kMfX + 1);
+                    hi[d][r] = make_float2(yr[0], yr[1]);
+                }
             if (t >= 2 && eok0) {
-                // per node row r: X = u0(r, 0) - u0(r, 1), S1 = u1(r, 0) + u1(r, 1),
-                // S2 = u2(r, 0) + u2(r, 1) with u0 = lo0 + hi0, u1 = lo1 + hi1, u2 = lo2 - hi2; the
+                // per node row r, over its two columns: u0 = lo0 + hi0, u1 = lo1 + hi1,
+                // u2 = lo2 - hi2, X = u0(0) - u0(1), S1 = u1(0) + u1(1), S2 = u2(0) + u2(1); the
                 // element between rows r and r + 1 gets X(r) + X(r+1) + S1(r) - S1(r+1) + S2(r) + S2(r+1)
                 float X[3], S1[3], S2[3];
 #pragma unroll
                 for (int r = 0; r < 3; ++r) {
-                    X[r] = (lo[0][r][0] + hi[0][r][0]) - (lo[0][r][1] + hi[0][r][1]);
-                    S1[r] = (lo[1][r][0] + hi[1][r][0]) + (lo[1][r][1] + hi[1][r][1]);
-                    S2[r] = (lo[2][r][0] - hi[2][r][0]) + (lo[2][r][1] - hi[2][r][1]);
+                    const float2 u0 = __fadd2_rn(lo[0][r], hi[0][r]);
+                    const float2 u1 = __fadd2_rn(lo[1][r], hi[1][r]);
+                    const float2 u2 = __ffma2_rn(hi[2][r], make_float2(-1.f, -1.f), lo[2][r]);
+                    X[r] = u0.x - u0.y;
+                    S1[r] = u1.x + u1.y;
+                    S2[r] = u2.x + u2.y;
                 }
+                const float2 out = make_float2((X[0] + X[1]) + (S1[0] - S1[1]) + (S2[0] + S2[1]),
+                                               (X[1] + X[2]) + (S1[1] - S1[2]) + (S2[1] + S2[2]));
                 const float* pq_prev = reinterpret_cast<const float*>(st_prev + kTzSlot + kTwSlot);
                 const int lt = ty0 * kMfX + tx;   // element (tx, ty0) in the tile's p, q planes
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    if (h == 1 && !eok1) break;
-                    const float out = (X[h] + X[h + 1]) + (S1[h] - S1[h + 1]) + (S2[h] + S2[h + 1]);
-                    const uint32_t e = e_prev + (h ? ex32 : 0u);
-                    const float ze = zp[(ty0 + h + 1) * kTzX + tx + 4];
-                    // p and q of element plane kk - 1 arrived with stage t - 1 (the slot of zp)
-                    const float pv = pq_prev[lt + h * kMfX], qv = pq_prev[kMfX * kMfY + lt + h * kMfX];
-                    const float pe = first ? ze : fmaf(beta, pv, ze);
-                    const float qe = first ? out : fmaf(beta, qv, out);
-                    if (e < emax) {
-                        p[e] = pe;
-                        q[e] = qe;
-                        if (xupd) x[e] = fmaf(alpha, pv, h ? xc1 : xc0);
-                    } else {
-                        bad = true;
+                const int zi = (ty0 + 1) * kTzX + tx + 4;
+                // the second element's row lies outside the mesh when !eok1: its staged z, p and q
+                // read as zero there, so it adds nothing to p.q and is not stored
+                const float2 ze = make_float2(zp[zi], zp[zi + kTzX]);
+                // p and q of element plane kk - 1 arrived with stage t - 1 (the slot of zp)
+                const float2 pv = make_float2(pq_prev[lt], pq_prev[lt + kMfX]);
+                const float2 qv = make_float2(pq_prev[kMfX * kMfY + lt], pq_prev[kMfX * kMfY + lt + kMfX]);
+                const float2 pe = first ? ze : __ffma2_rn(beta2, pv, ze);
+                const float2 qe = first ? out : __ffma2_rn(beta2, qv, out);
+                const float2 xv = __ffma2_rn(alpha2, pv, xc);
+                const uint32_t e1 = e_prev + ex32;
+                if (e_prev < emax && (!eok1 || e1 < emax)) {
+                    p[e_prev] = pe.x;
+                    q[e_prev] = qe.x;
+                    if (xupd) x[e_prev] = xv.x;
+                    if (eok1) {
+                        p[e1] = pe.y;
+                        q[e1] = qe.y;
+                        if (xupd) x[e1] = xv.y;
                     }
-                    local = fmaf(pe, qe, local);
+                } else {
+                    bad = true;
                 }
+                local2 = __ffma2_rn(pe, qe, local2);
             }
         }
         e_prev += exy32;
@@ -788,6 +816,7 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
         if (!step(t, la, lb)) break;
         if (t + 1 < nsteps && !step(t + 1, lb, la)) break;
     }
+    float local = local2.x + local2.y;
     if (bad) local = __int_as_float(0x7fc00000);
     if (!ok) {
         // let copies still in flight land before the block's shared memory is released
