@@ -627,8 +627,8 @@ def fine_roofline(dom, prec, rates, nel, peak, peak_kind, family):
             "fp_tflops": r[key + "_fp_TFLOP_per_s"],
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
             "traffic_source": "ncu capture (profiles/), scaled by nodes / elements" if traffic is not None else None,
-            "note": ("the matrix-free kernel is bound by instruction issue and latency (ncu: 59% issue active at 24 warps "
-                     "per SM, DRAM 18%); it "
+            "note": ("the matrix-free kernel is bound by instruction issue and latency (ncu: 58% issue active at 24 warps "
+                     "per SM, DRAM 20%); it "
                      "replaces an HBM-bound stencil kernel that moves five times the bytes"
                      if r.get("bfbt_form") == "fp32_matrix_free" and key == "bfbt_dir" else
                      "FP64 kernels on this part are also bounded by its 1.2 TFLOP/s FP64 rate (fp_tflops)"),
