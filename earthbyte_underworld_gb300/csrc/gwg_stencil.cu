@@ -830,6 +830,43 @@ __global__ void __launch_bounds__(kTmThreads, 4) k_cg_mf3_dir_tma(Mf3 a, const _
     pdl_trigger();
 }
 
+// Build-time check of k_cg_mf3_dir_tma's thread roles, restating the kernel's mapping: every
+// index a thread forms into the staged z plane, the staged weight plane, the node-plane buffers
+// and the tile's p and q planes lies inside that buffer, every node of the 33 x 9 block is formed
+// by exactly one thread, and every element of the 32 x 8 tile by exactly one.
+constexpr bool mf_tma_roles_ok() {
+    int nodes[kTmNodes] = {};
+    int elems[kMfX * kMfY] = {};
+    for (int tid = 0; tid < kTmThreads; ++tid) {
+        if (tid < 5 * kMfX + 5) {
+            const int nx = tid < 5 * kMfX ? tid % kMfX : kMfX;
+            const int ny0 = 2 * (tid < 5 * kMfX ? tid / kMfX : tid - 5 * kMfX);
+            const bool pair = ny0 + 1 <= kMfY;
+            const int node_i = ny0 * (kMfX + 1) + nx, zb = ny0 * kTzX + nx + 3, wb = ny0 * kTwX + nx;
+            for (int r = 0; r < 3; ++r)
+                if ((r < 2 || pair) && zb + r * kTzX + 1 >= kTzX * kTzY) return false;
+            if (2 * kTwX * kTwY + wb + (pair ? kTwX : 0) >= 3 * kTwX * kTwY) return false;
+            if (node_i + (pair ? kMfX + 1 : 0) >= kTmNodes) return false;
+            ++nodes[node_i];
+            if (pair) ++nodes[node_i + kMfX + 1];
+        }
+        if (tid < kMfX * kMfY / 2) {
+            const int tx = tid % kMfX, ty0 = 2 * (tid / kMfX);
+            if (ty0 * (kMfX + 1) + tx + 2 * (kMfX + 1) + 1 >= kTmNodes) return false;
+            if ((ty0 + 1) * kTzX + tx + 4 + kTzX >= kTzX * kTzY) return false;
+            if (ty0 * kMfX + tx + kMfX >= kMfX * kMfY) return false;
+            ++elems[ty0 * kMfX + tx];
+            ++elems[(ty0 + 1) * kMfX + tx];
+        }
+    }
+    for (int i = 0; i < kTmNodes; ++i)
+        if (nodes[i] != 1) return false;
+    for (int i = 0; i < kMfX * kMfY; ++i)
+        if (elems[i] != 1) return false;
+    return true;
+}
+static_assert(mf_tma_roles_ok(), "k_cg_mf3_dir_tma: a thread role leaves its buffer or misses a node or element");
+
 // Wc_(n,d) = a_d^2 W_(n,d) in FP32 (the weights of the matrix-free apply).  2D: [d][node].  3D:
 // rows padded to `pitch` nodes (a multiple of 4, so that every row starts on 16 bytes as the
 // tensor-memory-access copies need), [d][z][y][pitch], the padding zero.
