@@ -575,8 +575,9 @@ __global__ void __launch_bounds__(kMfX * kMfY) k_cg_mf3_dir(Mf3 a, const float* 
 // 2j and 2j + 1; the node rows they share are combined once); one block barrier per step.  The
 // arithmetic runs on FP32 pairs where the values come in twos (the two planes of a staged element
 // row, the two columns of a node row, the two nodes or two elements of a thread): one packed add,
-// multiply or fma (__fadd2_rn, __fmul2_rn, __ffma2_rn) does the work of two scalar ones.  A copy that has not arrived after a bounded wait makes
-// the block report NaN in the iteration's p.q, which ends the inner solve with UWGPU_ERR_NAN.
+// multiply or fma (__fadd2_rn, __fmul2_rn, __ffma2_rn) does the work of two scalar ones.  A copy
+// that has not arrived after a bounded wait makes the block report NaN in the iteration's p.q,
+// which ends the inner solve with UWGPU_ERR_NAN.
 constexpr int kTmThreads = 192;
 constexpr int kTzX = kMfX + 8, kTzY = kMfY + 2;     // staged element plane: 40 x 10
 constexpr int kTwX = kMfX + 4, kTwY = kMfY + 1;     // staged weight plane: 36 x 9, three components
