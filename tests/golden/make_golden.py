@@ -1,8 +1,10 @@
 """Convert the reference's golden stiffness matrices into small numpy fixtures.
 
 Reads the PETSc-binary AIJ files that Underworld/Rheology/tests/ViscousSuite.c compares against
-(Underworld/Rheology/tests/expected/test*2D.matrix, testArrheniusWithLimiter.matrix) from the
-read-only reference tree and writes them as CSR arrays to tests/golden/viscous_golden.npz.
+(Underworld/Rheology/tests/expected/test*2D.matrix, testArrheniusWithLimiter.matrix) and the one
+StgFEM's isoviscous assembly test compares against (StgFEM/Assembly/tests/expected/
+testIsoviscousSiffness.matrix, the file's own spelling) from the read-only reference tree, and
+writes them as CSR arrays to tests/golden/viscous_golden.npz.
 Run once with the reference tree's path as the only argument; the fixtures are committed.
 
 PETSc binary layout (big-endian): int32 MAT_FILE_CLASSID (1211216), int32 rows, int32 cols,
@@ -18,6 +20,8 @@ if len(sys.argv) != 2:
 REF = sys.argv[1]
 SRC = os.path.join(REF, "Underworld/Rheology/tests/expected")
 NAMES = ["testMaterialViscosity2D", "testArrhenius2D", "testArrheniusWithLimiter", "testFrankKamenetskii2D"]
+SOURCES = {name: os.path.join(SRC, name + ".matrix") for name in NAMES}
+SOURCES["testIsoviscousSiffness"] = os.path.join(REF, "StgFEM/Assembly/tests/expected/testIsoviscousSiffness.matrix")
 
 
 def read_petsc_aij(path):
@@ -37,8 +41,8 @@ def read_petsc_aij(path):
 
 def main():
     out = {}
-    for name in NAMES:
-        m, n, rp, ci, v = read_petsc_aij(os.path.join(SRC, name + ".matrix"))
+    for name, path in SOURCES.items():
+        m, n, rp, ci, v = read_petsc_aij(path)
         out[name + "_shape"] = np.array([m, n])
         out[name + "_rowptr"] = rp
         out[name + "_cols"] = ci

@@ -56,6 +56,27 @@ def test_oracle_reproduces_golden(oracle, name):
     assert err < 1e-11, err
 
 
+def test_oracle_reproduces_isoviscous_golden(oracle):
+    """StgFEM's own assembly test (StgFEM/Assembly/tests/input/IsoviscousStiffnessMatrix.xml): a 2D
+    3x3 Q1 mesh on the unit square, the 2x2 Gauss swarm, IsoviscousStressTensorTerm with viscosity
+    1 (StgFEM/Assembly/src/IsoviscousStressTensorTerm.c:166-252, the same operator as B^T D B with
+    D = diag(2, 2, 1)) and no velocity BCs, compared against testIsoviscousSiffness.matrix at
+    1e-4 (StiffnessMatrixCompareTolerance)."""
+    O = oracle
+    g = np.load(GOLDEN)
+    m = O.make_mesh(2, (3, 3, 1))
+    mats = [O.make_material([(O.LAW_MATERIAL_VISCOSITY, [1.0])])]
+    Ke = O.assemble_gauss(m, mats, None, O.make_fields())
+    rp, ci, v, eq, nf = O.global_csr(m, Ke, None)
+    K = sp.csr_matrix((v, ci, rp), shape=(nf, nf))
+    G = golden_matrix(g, "testIsoviscousSiffness")
+    assert K.shape == G.shape == (32, 32)
+    assert K.nnz == G.nnz == 400
+    err = sp.linalg.norm(G - K) / sp.linalg.norm(G)
+    assert err < 1e-4
+    assert err < 1e-12, err
+
+
 def test_oracle_pic_quadrature_matches_gauss_when_points_are_gauss_points(oracle):
     """Points placed at the 2x2 Gauss points of every element, mapped by the coincident mapper
     (Newton xi, constant weights 4/4 = 1), give the Gauss-swarm matrix."""
