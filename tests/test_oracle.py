@@ -43,6 +43,55 @@ def test_map_is_stable_by_point_index(oracle):
     assert np.array_equal(np.diff(offsets.astype(np.int64)), np.bincount(owning, minlength=12))
 
 
+def _drand48(n, seed=0):
+    """POSIX srand48(seed) / drand48(): the 48-bit linear congruence X' = (0x5DEECE66D X + 0xB)
+    mod 2^48 from X = (seed << 16) + 0x330E, returning X' / 2^48."""
+    x = ((seed & 0xFFFFFFFF) << 16) | 0x330E
+    out = []
+    for _ in range(n):
+        x = (0x5DEECE66D * x + 0xB) % (1 << 48)
+        out.append(x / float(1 << 48))
+    return out
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_element_type_suite_points_map_back(oracle, dim):
+    """StgFEM/Discretisation/tests/ElementTypeSuite.c (TestLinear2D / TestLinear3D): 40 points
+    drawn by srand48(0) / drand48() in a 6 x 6 (x 1) Q1 mesh over [0, 1.2]^dim are searched,
+    converted to local coordinates and mapped back through the shape functions; the suite requires
+    the round trip within 1e-8.  Here the oracle's element search and local coordinates (its
+    Newton iteration and the closed form) must reproduce the points to that tolerance."""
+    import ctypes
+    try:
+        libc = ctypes.CDLL("libc.so.6")
+        libc.drand48.restype = ctypes.c_double
+        libc.srand48(0)
+        assert [libc.drand48() for _ in range(8)] == _drand48(8)   # the restated stream is libc's
+    except OSError:
+        pass
+    O = oracle
+    nel = (6, 6, 1)
+    h = [1.2 / n for n in nel]
+    m = O.make_mesh(dim, nel, mn=(0.0, 0.0, 0.0), mx=(1.2, 1.2, 1.2))
+    r = _drand48(40 * dim)
+    pts = np.zeros((40, 3))
+    pts[:, :dim] = np.array(r).reshape(40, dim)
+    for newton in (True, False):
+        owning, offsets, perm, xi, outside = O.map_points(m, pts, use_newton=newton)
+        assert outside == 0
+        xi_pt = np.zeros_like(xi)
+        xi_pt[perm] = xi                     # xi is in slot order
+        e = owning.astype(np.int64)
+        idx = [e % nel[0], (e // nel[0]) % nel[1], e // (nel[0] * nel[1])]
+        back = np.zeros((40, dim))
+        for d in range(dim):
+            # Q1 shape functions on the rectangular element: sum_a N_a(xi) x_a
+            lo = idx[d] * h[d]
+            back[:, d] = lo * (1.0 - xi_pt[:, d]) / 2.0 + (lo + h[d]) * (1.0 + xi_pt[:, d]) / 2.0
+        assert np.all(np.abs(xi_pt[:, :dim]) <= 1.0 + 1e-12)
+        assert np.linalg.norm(back - pts[:, :dim], axis=1).max() < 1e-8
+
+
 def test_newton_xi_equals_affine_closed_form(oracle):
     O = oracle
     m = O.make_mesh(3, (5, 3, 7))
