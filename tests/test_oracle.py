@@ -275,3 +275,36 @@ def test_oracle_velic_convergence_rates_match_reference(oracle, case):
     r = VN.rates(errs, ns)
     print(f"\nsol{case}: L2 errors", errs.tolist(), "rates", r.tolist())
     assert np.all(np.abs(r - g[f"{case}_expected_rates"]) < 0.1), r
+
+
+@pytest.mark.parametrize("order,radius_tol,theta_tol", [(1, 0.005, 1.0e-5), (2, 1.0e-7, 1.0e-5)])
+def test_advection_suite_solid_body_rotation(oracle, order, radius_tol, theta_tol):
+    """PICellerator/MaterialPoints/tests/AdvectionSuite.c (TestEuler / TestRK2 with
+    input/testAdvection.xml, testEuler.xml, testRK2.xml): points inside the unit circle on a 20 x 20
+    Q1 mesh over [-1.1, 1.1]^2, nodal velocity Velocity_SolidBodyRotation (StgFEM/plugins/
+    StandardConditionFunctions/StandardConditionFunctions.c:665-693: (-y, x), omega 1), dt 0.01,
+    ten steps; at every step the radius, the angle to the analytic rotation and the out-of-plane
+    drift stay below the suite's tolerances (radius 0.005 / 1e-7, angle 1e-5, depth 1e-10)."""
+    O = oracle
+    m = O.make_mesh(2, (20, 20, 1), mn=(-1.1, -1.1, 0.0), mx=(1.1, 1.1, 0.0))
+    xn = O.node_coords(m)
+    u = np.stack([-xn[:, 1], xn[:, 0]], axis=1)
+    rng = np.random.default_rng(0)
+    r = np.sqrt(rng.random(4000))
+    th = 2.0 * np.pi * rng.random(4000)
+    x0 = np.stack([r * np.cos(th), r * np.sin(th), np.zeros_like(r)], axis=1)
+    xyz = x0.copy()
+    r0 = np.linalg.norm(x0[:, :2], axis=1)
+    th0 = np.arctan2(x0[:, 1], x0[:, 0])
+    dt, t = 0.01, 0.0
+    for step in range(10):
+        xyz, failed, _ = O.advect(m, u, xyz, dt, order=order)
+        assert failed == 0
+        t += dt
+        ra = np.linalg.norm(xyz[:, :2], axis=1)
+        ana = np.stack([r0 * np.cos(t + th0), r0 * np.sin(t + th0)], axis=1)
+        cosang = np.sum(ana * xyz[:, :2], axis=1) / (np.linalg.norm(ana, axis=1) * ra)
+        theta = np.arccos(np.clip(cosang, -1.0, 1.0))
+        assert np.abs(ra - r0).max() < radius_tol
+        assert theta.max() < theta_tol
+        assert np.abs(xyz[:, 2] - x0[:, 2]).max() < 1e-10
