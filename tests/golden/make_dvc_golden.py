@@ -5,8 +5,11 @@ _DVCWeightsSuite_InitialiseParticleCoords / ...2D assign, on a 10 x 10 (x 10) gr
 [-1, 1]^dim), the expected centroids and weights the suite compares against
 (PICellerator/Weights/tests/expected/DVCWeightsSuite_testGetCentroids.txt, ...2D.txt, printed
 with six decimals) and the expected cell grids (links and centres,
-DVCWeightsSuite_testConstructGrid.txt, ...2D.txt), from the read-only reference tree, and writes
-tests/golden/dvc_golden.json.
+DVCWeightsSuite_testConstructGrid.txt, ...2D.txt), and the PCDVC integration suite's setup and
+expected error statistics (PICellerator/Utils/tests/input/testPCDVC.xml, testElementIntegral.xml,
+expected/testPCDVC_{CircleInterface,PolynomialFunction,ExponentialInterface}.expected: a tolerance
+and a value for the mean relative error, then for its standard deviation), from the read-only
+reference tree, and writes tests/golden/dvc_golden.json.
 Run once with the reference tree's path as the only argument; the fixture is committed.
 """
 import json
@@ -52,6 +55,32 @@ def grid(path, dim):
     return links, cen
 
 
+def _params(path):
+    txt = re.sub(r"<!--.*?-->", "", open(path).read(), flags=re.S)
+    return {k: v.strip() for k, v in re.findall(r'<param name="([^"]+)"[^>]*>([^<]*)</param>', txt)}
+
+
+def pcdvc_suite():
+    tests = os.path.join(REF, "PICellerator/Utils/tests")
+    base = _params(os.path.join(tests, "input/testElementIntegral.xml"))
+    pc = _params(os.path.join(tests, "input/testPCDVC.xml"))
+    cases = {}
+    for name in ("CircleInterface", "PolynomialFunction", "ExponentialInterface"):
+        vals = [float(v) for v in open(os.path.join(tests, "expected", f"testPCDVC_{name}.expected")).read().split()[:4]]
+        cases[name] = {"mean_tol": vals[0], "mean": vals[1], "sd_tol": vals[2], "sd": vals[3]}
+    return {
+        "source": "PICellerator/Utils/tests/PCDVCSuite.c with input/testPCDVC.xml",
+        "elementRes": [int(base["elementResI"]), int(base["elementResJ"])],
+        "min": [float(base["minX"]), float(base["minY"])],
+        "max": [float(base["maxX"]), float(base["maxY"])],
+        "particleCount": int(base["particleCount"]),
+        "sampleSize": int(base["SampleSize"]),
+        "res": [int(pc["resolutionX"]), int(pc["resolutionY"])],
+        "maxDeletions": int(pc["maxDeletions"]), "maxSplits": int(pc["maxSplits"]),
+        "cases": cases,
+    }
+
+
 def main():
     src = open(SUITE).read()
     c3 = coords(src, "void _DVCWeightsSuite_InitialiseParticleCoords(", "pList")
@@ -72,6 +101,7 @@ def main():
     assert len(l3) == 1000 and len(l2) == 100
     assert len(out["3d"]["xi"]) == len(cen3) == len(w3) == 10
     assert len(out["2d"]["xi"]) == len(cen2) == len(w2) == 10
+    out["pcdvc_suite"] = pcdvc_suite()
     with open(OUT, "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", OUT)

@@ -1,6 +1,7 @@
 """The oracle's discrete Voronoi cell weights (DVCWeights.c restated) against the reference's known
 answers (PICellerator/Weights/tests/DVCWeightsSuite.c and its expected files, converted by
-tests/golden/make_dvc_golden.py), and the invariants of the construction."""
+tests/golden/make_dvc_golden.py), the invariants of the construction, and the integration error
+statistics of PICellerator/Utils/tests/PCDVCSuite.c."""
 import json
 import os
 
@@ -93,3 +94,42 @@ def test_pcdvc_weights_follow_the_moved_points(oracle, dim, nel, res):
     cx, w = O.dvc_weights(m, res, off2, xi_final)
     assert np.allclose(w, wo, rtol=0, atol=1e-14)
     assert np.allclose(cx[:, :dim], xo[:, :dim], rtol=0, atol=1e-14)
+
+
+# PICellerator/Utils/tests/PCDVCSuite.c: the integrands (functions of the local coordinates) and
+# their exact integrals over the reference element [-1, 1]^2
+PCDVC_CASES = {
+    "CircleInterface": (lambda x, y: (x * x + y * y <= 1.0).astype(float), np.pi),
+    "PolynomialFunction": (lambda x, y: 11 + 2 * x * x + 3 * x ** 3 * y + y + x ** 3 + 2 * y * y, 148.0 / 3.0),
+    "ExponentialInterface": (lambda x, y: (y <= 0.1 * np.exp(2 * x)).astype(float),
+                             0.05 * (np.exp(2.0) - np.exp(-2.0)) + 2.0),
+}
+
+
+def test_pcdvc_suite_integration_error_statistics(oracle):
+    """PCDVCSuite.c: for seeds 0 .. SampleSize - 1, Swarm_Random_Seed(seed) and a RandomParticleLayout
+    of 20 points per cell on a 2 x 2 mesh over [0, 4]^2; the integration points of element 0 get
+    PCDVC weights (resolution 10, no splits or deletions, so the discrete Voronoi centroids and
+    volumes); each integrand is integrated over the element at those points and weights.  The mean
+    and the standard deviation of the relative error must lie within the suite's tolerances of its
+    expected values (expected/testPCDVC_*.expected).  The oracle's layout restates the reference's
+    Park-Miller stream, so the samples are the reference's own."""
+    O = oracle
+    g = json.load(open(GOLDEN))["pcdvc_suite"]
+    assert g["maxDeletions"] == 0 and g["maxSplits"] == 0
+    m = O.make_mesh(2, g["elementRes"] + [1], mn=g["min"] + [0.0], mx=g["max"] + [1.0])
+    errs = {k: [] for k in PCDVC_CASES}
+    for seed in range(g["sampleSize"]):
+        xyz = O.random_layout(m, g["particleCount"], seed)
+        _, off, perm, xi, outside = O.map_points(m, xyz)
+        assert outside == 0 and off[1] - off[0] == g["particleCount"]
+        cxi, w, _ = O.dvc_element(2, g["res"], xi[off[0]:off[1], :2])
+        assert abs(w.sum() - 4.0) < 1e-12   # the element's local area; detJ = 1 for its 2 x 2 size
+        for name, (f, exact) in PCDVC_CASES.items():
+            errs[name].append(abs(np.sum(w * f(cxi[:, 0], cxi[:, 1])) - exact) / abs(exact))
+    for name, c in g["cases"].items():
+        e = np.array(errs[name])
+        mean = e.mean()
+        sd = np.sqrt((e * e).mean() - mean * mean)
+        assert abs(c["mean"] - mean) < c["mean_tol"], (name, mean)
+        assert abs(c["sd"] - sd) < c["sd_tol"], (name, sd)
