@@ -8,7 +8,9 @@ with six decimals) and the expected cell grids (links and centres,
 DVCWeightsSuite_testConstructGrid.txt, ...2D.txt), and the PCDVC integration suite's setup and
 expected error statistics (PICellerator/Utils/tests/input/testPCDVC.xml, testElementIntegral.xml,
 expected/testPCDVC_{CircleInterface,PolynomialFunction,ExponentialInterface}.expected: a tolerance
-and a value for the mean relative error, then for its standard deviation), from the read-only
+and a value for the mean relative error, then for its standard deviation), and the same statistics
+that PICellerator/Weights/tests/ConstantWeightsSuite.c states for ConstantWeights (its
+WeightsSuite_TestElementIntegral calls, on input/testConstantWeights.xml), from the read-only
 reference tree, and writes tests/golden/dvc_golden.json.
 Run once with the reference tree's path as the only argument; the fixture is committed.
 """
@@ -81,6 +83,27 @@ def pcdvc_suite():
     }
 
 
+def constant_weights_suite():
+    tests = os.path.join(REF, "PICellerator/Weights/tests")
+    base = _params(os.path.join(tests, "input/testElementIntegral.xml"))
+    src = re.sub(r"/\*.*?\*/", "", open(os.path.join(tests, "ConstantWeightsSuite.c")).read(), flags=re.S)
+    cases = {}
+    for args in re.findall(r"WeightsSuite_TestElementIntegral\(\s*data->context,([^;]*)\);", src):
+        a = [v.strip() for v in args.split(",")]
+        name = a[0].strip('"')
+        cases[name] = {"count": int(a[1]), "mean_tol": float(a[2]), "sd_tol": float(a[3]),
+                       "mean": float(a[4]), "sd": float(a[5])}
+    assert len(cases) == 6, cases
+    return {
+        "source": "PICellerator/Weights/tests/ConstantWeightsSuite.c with input/testConstantWeights.xml",
+        "elementRes": [int(base["elementResI"]), int(base["elementResJ"])],
+        "min": [float(base["minX"]), float(base["minY"])],
+        "max": [float(base["maxX"]), float(base["maxY"])],
+        "particleCount": int(base["particleCount"]),
+        "cases": cases,
+    }
+
+
 def main():
     src = open(SUITE).read()
     c3 = coords(src, "void _DVCWeightsSuite_InitialiseParticleCoords(", "pList")
@@ -102,6 +125,7 @@ def main():
     assert len(out["3d"]["xi"]) == len(cen3) == len(w3) == 10
     assert len(out["2d"]["xi"]) == len(cen2) == len(w2) == 10
     out["pcdvc_suite"] = pcdvc_suite()
+    out["constant_weights_suite"] = constant_weights_suite()
     with open(OUT, "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", OUT)

@@ -1,7 +1,8 @@
 """The oracle's discrete Voronoi cell weights (DVCWeights.c restated) against the reference's known
 answers (PICellerator/Weights/tests/DVCWeightsSuite.c and its expected files, converted by
 tests/golden/make_dvc_golden.py), the invariants of the construction, and the integration error
-statistics of PICellerator/Utils/tests/PCDVCSuite.c."""
+statistics of PICellerator/Utils/tests/PCDVCSuite.c and PICellerator/Weights/tests/
+ConstantWeightsSuite.c."""
 import json
 import os
 
@@ -133,3 +134,46 @@ def test_pcdvc_suite_integration_error_statistics(oracle):
         sd = np.sqrt((e * e).mean() - mean * mean)
         assert abs(c["mean"] - mean) < c["mean_tol"], (name, mean)
         assert abs(c["sd"] - sd) < c["sd_tol"], (name, sd)
+
+
+# PICellerator/Weights/tests/ConstantWeightsSuite.c: integrands and exact integrals over [-1, 1]^2
+CONSTANT_WEIGHTS_CASES = {
+    "ConstantFunction": (lambda x, y: -3.0, -12.0),
+    "LinearFunction": (lambda x, y: 2.0 + 2.2 * x - y, 8.0),
+    "QuadraticFunction": (lambda x, y: 1 + x + x * x, 16.0 / 3.0),
+    "PolynomialFunction": (lambda x, y: 11 + 2 * x * x + 3 * x * x * x * y + y + x * x * x + 2 * y * y, 148.0 / 3.0),
+    "CircleInterface": (lambda x, y: float(x * x + y * y <= 1.0), np.pi),
+    "ExponentialInterface": (lambda x, y: float(y <= 0.1 * np.exp(2 * x)), 0.05 * (np.exp(2.0) - np.exp(-2.0)) + 2.0),
+}
+
+
+def test_constant_weights_suite_integration_error_statistics(oracle):
+    """ConstantWeightsSuite.c (WeightsSuite_TestElementIntegral): the same seeded layouts as the
+    PCDVC suite, integrated over element 0 at the points' own local coordinates with the constant
+    weights 4 / count (ConstantWeights.c:180-189); the reference states the mean and standard
+    deviation of the relative error to six digits with a tolerance of 1e-6 (1e-10 for the constant
+    integrand).  The oracle meets every one: its layout, element search, local coordinates and
+    weights reproduce the reference's samples."""
+    O = oracle
+    g = json.load(open(GOLDEN))["constant_weights_suite"]
+    m = O.make_mesh(2, g["elementRes"] + [1], mn=g["min"] + [0.0], mx=g["max"] + [1.0])
+    count = {c["count"] for c in g["cases"].values()}
+    assert len(count) == 1
+    errs = {k: [] for k in CONSTANT_WEIGHTS_CASES}
+    for seed in range(count.pop()):
+        xyz = O.random_layout(m, g["particleCount"], seed)
+        _, off, perm, xi, outside = O.map_points(m, xyz)
+        assert outside == 0
+        pts = xi[off[0]:off[1]]
+        w = 4.0 / len(pts)
+        for name, (f, exact) in CONSTANT_WEIGHTS_CASES.items():
+            integral = 0.0
+            for x, y in pts[:, :2]:          # in the swarm's order, as FeVariable_IntegrateElement sums
+                integral += 1.0 * w * f(x, y)
+            errs[name].append(abs(integral - exact) / abs(exact))
+    for name, c in g["cases"].items():
+        e = np.array(errs[name])
+        mean = e.mean()
+        sd = np.sqrt((e * e).mean() - mean * mean)
+        assert abs(mean - c["mean"]) <= c["mean_tol"], (name, mean)
+        assert abs(sd - c["sd"]) <= c["sd_tol"], (name, sd)
