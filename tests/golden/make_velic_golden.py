@@ -10,6 +10,12 @@ gcc into oracle/_ref/), and the convergence rates the reference's expected resul
 - solKz (PerformanceTests/testVelicSolKz.xml): sigma = 1, km = pi, n = 1, B = 1 (viscosity
   exp(2 y)); expected rates (Underworld_Velic_solKz-analysis.cvg-convergence-rates.dat): velocity
   2.00 / 2.00, pressure 1.00.
+- solA (testVelicSolA.xml): isoviscous (Z = 1), buoyancy Ra T with T = sin(3.5 pi y) cos(pi x)
+  (VelicTemperatureIC), solA's sigma = 1, n = 1, km = 3.5 pi; solB (testVelicSolB.xml): isoviscous,
+  T = sinh(2 y) cos(pi x) (VelicTemperatureIC_SolB), sigma = 1, n = 1, km = 2; solS
+  (testVelicSolS.xml): isoviscous, no buoyancy, top lid v_x = sin(pi x) (Velocity_SinusoidalLid),
+  bottom no-slip, side walls v_x = 0, n = 1, eta = 1.  Their expected rates are read from
+  Underworld_Velic_sol{A,B,S}-analysis.cvg-convergence-rates.dat (velocity x, y, pressure).
 
 Usage: python tests/golden/make_velic_golden.py <path of the Underworld 1.x source tree>
 """
@@ -42,6 +48,20 @@ cx = build("solCx")
 cx._Velic_solCx.argtypes = [D, C.c_double, C.c_double, C.c_double, C.c_int, D, D, D, D]
 kz = build("solKz")
 kz._Velic_solKz.argtypes = [D, C.c_double, C.c_double, C.c_int, C.c_double, D, D, D, D]
+sa = build("solA")
+sa._Velic_solA.argtypes = [D, C.c_double, C.c_double, C.c_int, C.c_double, D, D, D, D]
+sb = build("solB")
+sb._Velic_solB.argtypes = [D, C.c_double, C.c_double, C.c_int, C.c_double, D, D, D, D]
+ss = build("solS")
+ss._Velic_solS.argtypes = [D, C.c_int, C.c_double, D, D, D, D]
+
+
+def expected_rates(name):
+    """velocity x, velocity y and pressure rates of the reference's convergence-rate file"""
+    path = os.path.join(REF, "Underworld", "SysTest", "PerformanceTests", "expected",
+                        f"Underworld_Velic_{name}-analysis.cvg-convergence-rates.dat")
+    line = [l for l in open(path) if l.startswith("cvg. rate")][0]
+    return [float(v) for v in line.split()[2:5]]
 
 
 def call(f, x, y, *params):
@@ -57,6 +77,9 @@ def call(f, x, y, *params):
 CASES = {
     "cx": (lambda x, y: call(cx._Velic_solCx, x, y, 100.0, 1.0, 0.5, 2), [1.99, 1.99, 1.00]),
     "kz": (lambda x, y: call(kz._Velic_solKz, x, y, 1.0, math.pi, 1, 1.0), [2.00, 2.00, 1.00]),
+    "a": (lambda x, y: call(sa._Velic_solA, x, y, 1.0, 1.0, 1, 3.5 * math.pi), expected_rates("solA")),
+    "b": (lambda x, y: call(sb._Velic_solB, x, y, 1.0, 1.0, 1, 2.0), expected_rates("solB")),
+    "s": (lambda x, y: call(ss._Velic_solS, x, y, 1, 1.0), expected_rates("solS")),
 }
 g = (1.0 - 1.0 / np.sqrt(3.0)) / 2.0
 LOC = [(g, g), (1 - g, g), (g, 1 - g), (1 - g, 1 - g)]

@@ -277,6 +277,71 @@ def test_oracle_velic_convergence_rates_match_reference(oracle, case):
     assert np.all(np.abs(r - g[f"{case}_expected_rates"]) < 0.1), r
 
 
+def _velic_fem_case(O, case, n):
+    """solA / solB / solS of the reference's performance tests (testVelicSol{A,B,S}.xml): the FEM
+    base application (ThermalConvectionBase.xml: 2 x 2 Gauss swarm, ThermalBuoyancyForceTerm with
+    Ra = 1, StgFEM/Assembly/src/ThermalBuoyancyForceTerm.c:179-240, f_y = Ra T), isoviscous.
+    The Gauss points are placed as points with constant weights (the same integral); the
+    buoyancy Ra T is written as rho = -T (density 1e-12, expansivity 1e12 about T = 0)."""
+    m = O.make_mesh(2, (n, n, 1))
+    a = 1.0 / np.sqrt(3.0)
+    e = np.arange(n * n)
+    ex, ey = e % n, e // n
+    pts = []
+    for gy in (-a, a):
+        for gx in (-a, a):
+            pts.append(np.stack([(ex + 0.5 + 0.5 * gx) / n, (ey + 0.5 + 0.5 * gy) / n, np.zeros(n * n)], axis=1))
+    pts = np.concatenate(pts)
+    xn = O.node_coords(m)
+    bc = None
+    if case == "s":
+        # velocityBC.topLidSinusoidal_NoSlipBottom.xml: top v_x = sin(pi x) (Velocity_SinusoidalLid,
+        # StandardConditionFunctions.c:1076-1095), v_y = 0; bottom no-slip; sides v_x = 0
+        mats = [O.make_material([(O.LAW_MATERIAL_VISCOSITY, [1.0])], density=0.0)]
+        T = None
+        top, bot = np.isclose(xn[:, 1], 1.0), np.isclose(xn[:, 1], 0.0)
+        side = np.isclose(xn[:, 0], 0.0) | np.isclose(xn[:, 0], 1.0)
+        fixed = np.zeros((xn.shape[0], 2), np.uint8)
+        fixed[top | bot, :] = 1
+        fixed[side, 0] = 1
+        bc = np.zeros((xn.shape[0], 2))
+        bc[top, 0] = np.sin(np.pi * xn[top, 0])
+        bc[side, 0] = 0.0
+        fixed = fixed.reshape(-1)
+    else:
+        mats = [O.make_material([(O.LAW_MATERIAL_VISCOSITY, [1.0])], density=1e-12, alpha=1e12, ref_temp=0.0)]
+        if case == "a":   # VelicTemperatureIC (StandardConditionFunctions.c:1298-1338), wavenumberY 3.5
+            T = np.sin(3.5 * np.pi * xn[:, 1]) * np.cos(np.pi * xn[:, 0])
+        else:             # VelicTemperatureIC_SolB (StandardConditionFunctions.c:1341-1375), km = 2
+            T = np.sinh(2.0 * xn[:, 1]) * np.cos(np.pi * xn[:, 0])
+        fixed = O.free_slip_mask(m)
+    _, off, perm, xi, outside = O.map_points(m, pts)
+    assert outside == 0
+    f = O.make_fields(temperature=T, gravity=1.0, vert_axis=1)
+    Ke, fe, Ge, Se, _ = O.assemble(m, off, perm, xi, np.zeros(pts.shape[0], np.int32), mats, f)
+    u, p, rep = O.solve_bsscr(m, fixed, Ke, Ge, fe, Se, mg_levels=3, schur_type=1, schur_pc=3, scr_rtol=1e-10,
+                              a11_rtol=1e-12, back_rtol=1e-12, bfbt_rtol=1e-8, bfbt_max_it=5000, bcval=bc)
+    return u, p
+
+
+@pytest.mark.parametrize("case", ["a", "b", "s"])
+def test_oracle_velic_fem_convergence_rates_match_reference(oracle, case):
+    """solA (buoyancy from a non-integer vertical wavenumber), solB (a sinh temperature) and solS
+    (a driven sinusoidal lid: non-zero Dirichlet values lifted into the right-hand side), on the
+    reference's Gauss-swarm FEM setup at 16^2, 32^2, 64^2: the L2 errors against the reference's
+    analytic plugins (Underworld/SysTest/AnalyticPlugins/Velic_sol{A,B,S}/sol{A,B,S}.c, fixture
+    tests/golden/velic_golden.npz) converge at the rates the reference's expected results state
+    (PerformanceTests/expected/Underworld_Velic_sol{A,B,S}-analysis.cvg-convergence-rates.dat)."""
+    import velic_norms as VN
+    O = oracle
+    g = VN.golden()
+    ns = (16, 32, 64)
+    errs = np.array([VN.errors(case, n, *_velic_fem_case(O, case, n), g) for n in ns])
+    r = VN.rates(errs, ns)
+    print(f"\nsol{case}: L2 errors", errs.tolist(), "rates", r.tolist())
+    assert np.all(np.abs(r - g[f"{case}_expected_rates"]) < 0.1), r
+
+
 @pytest.mark.parametrize("order,radius_tol,theta_tol", [(1, 0.005, 1.0e-5), (2, 1.0e-7, 1.0e-5)])
 def test_advection_suite_solid_body_rotation(oracle, order, radius_tol, theta_tol):
     """PICellerator/MaterialPoints/tests/AdvectionSuite.c (TestEuler / TestRK2 with
